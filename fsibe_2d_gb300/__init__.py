@@ -1,0 +1,61 @@
+"""fsibe_2d_gb300 -- GB300-native (sm_103a) FSIBE_2D fluid step + flexible-beam coupling.
+
+The compute path is the in-tree CUDA library fsibe_2d_gb300/_lib/libfsibe_gb300.so behind the
+C ABI of include/fsibe.h.  This module only binds that ABI (ctypes); there is no CPU
+fallback: if the library is missing, `Run(...)` raises.
+"""
+import ctypes as C
+import os
+
+from ._abi import (FsibeParams, FsibeScalars, make_params, BEAM_DATA_COLUMNS, STATUS_NAMES,  # noqa: F401
+                   FSIBE_FP64, FSIBE_FP32C, FSIBE_BDF2, FSIBE_CRANK_NICHOLSON, FSIBE_EULER_IMPLICIT)
+from ._binding import FsibeError, declare, Run as _Run  # noqa: F401
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_lib", "libfsibe_gb300.so")
+
+_lib = None
+
+
+def library():
+    """Load libfsibe_gb300.so (raises if it was not built: there is no fallback)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"CUDA library not built: {LIB_PATH} is missing "
+                               "(run __graft_entry__.build() or python -m fsibe_2d_gb300.build)")
+        L = C.CDLL(LIB_PATH)
+        declare(L, "fsibe_")
+        L.fsibe_set_stream.argtypes = [C.c_void_p, C.c_void_p]
+        L.fsibe_strerror.argtypes = [C.c_int]
+        L.fsibe_strerror.restype = C.c_char_p
+        L.fsibe_time_steps.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_float)]
+        L.fsibe_launches_per_step.argtypes = [C.c_void_p, C.POINTER(C.c_int)]
+        L.fsibe_use_graph.argtypes = [C.c_void_p, C.c_int]
+        _lib = L
+    return _lib
+
+
+class Run(_Run):
+    """One GPU simulation context: device-resident fields, reference-named entry points."""
+
+    def __init__(self, params: FsibeParams):
+        super().__init__(library(), "fsibe_", params)
+
+    def set_stream(self, stream_handle):
+        """Run this context's kernels on a cudaStream_t (an int handle, e.g. torch's)."""
+        self._call("set_stream", C.c_void_p(stream_handle))
+
+    def time_steps(self, nsteps):
+        """Device milliseconds (CUDA events on the context's stream) for nsteps steps."""
+        ms = C.c_float()
+        self._call("time_steps", C.c_int(nsteps), C.byref(ms), soft=(10,))
+        return ms.value
+
+    def launches_per_step(self):
+        n = C.c_int()
+        self._call("launches_per_step", C.byref(n))
+        return n.value
+
+    def use_graph(self, enable=True):
+        self._call("use_graph", C.c_int(1 if enable else 0))

@@ -1,0 +1,1197 @@
+// api.cu -- the C ABI of include/fsibe.h: run context, step orchestration, state transfer.
+//
+// One fsibe_ctx holds every field of one run in HBM and a CUDA stream.  A step is a fixed
+// sequence of kernel launches whose time-dependent inputs (time, dt, AB2 weights, drag
+// window, status) live in a device struct, so a step needs no host round trip and can be
+// captured once in a CUDA graph and replayed.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "fluid.cuh"
+#include "solid.cuh"
+
+namespace fsibe {
+void fill_sizes_32(SizeKernels<double>&, SizeKernels<float>&);
+void fill_sizes_64(SizeKernels<double>&, SizeKernels<float>&);
+void fill_sizes_128(SizeKernels<double>&, SizeKernels<float>&);
+void fill_sizes_256(SizeKernels<double>&, SizeKernels<float>&);
+void fill_sizes_512(SizeKernels<double>&, SizeKernels<float>&);
+void fill_sizes_1024(SizeKernels<double>&, SizeKernels<float>&);
+void fill_sizes_2048(SizeKernels<double>&, SizeKernels<float>&);
+void fill_sizes_4096(SizeKernels<double>&, SizeKernels<float>&);
+size_t beam_ws_doubles(int ns);
+void launch_mask(const MaskArgs& a, double gerf, bool fp32, cudaStream_t st);
+void launch_forces(const ForceArgs& a, double dxi, double dyi, cudaStream_t st);
+void launch_beam(const BeamArgs& b, cudaStream_t st);
+void launch_init_beam(const BeamArgs& b, cudaStream_t st);
+
+static bool get_sizes(int N, SizeKernels<double>& d, SizeKernels<float>& f) {
+    switch (N) {
+        case 32: fill_sizes_32(d, f); return true;
+        case 64: fill_sizes_64(d, f); return true;
+        case 128: fill_sizes_128(d, f); return true;
+        case 256: fill_sizes_256(d, f); return true;
+        case 512: fill_sizes_512(d, f); return true;
+        case 1024: fill_sizes_1024(d, f); return true;
+        case 2048: fill_sizes_2048(d, f); return true;
+        case 4096: fill_sizes_4096(d, f); return true;
+        default: return false;
+    }
+}
+
+// ---------------------------------------------------------------------------------
+// Scalar kernels of the step
+// ---------------------------------------------------------------------------------
+struct StepArgs {
+    DevScalars* S;
+    const double* red;
+    int nblk, explicit_step, iBeam, iMeanVelocity, ns, nx, ny;
+    double cfl, dx, dy, eps, dt_fixed, time_end, theta_inf, T_fullspeed, U_mean_true, pi, nu;
+    double x0, y0, t_beam, NN;
+    const double *bx, *by;
+};
+
+__device__ double mean_ux(int mode, double time, double theta_inf, double Tf, double pi) {  // mean_velocity.f90:4-42
+    double tf;
+    switch (mode) {
+        case 1:
+            tf = (time < Tf) ? (time * time * time) / (-0.5 * Tf * Tf * Tf) + 3.0 * (time * time) / (Tf * Tf) : 1.0;
+            return cos(theta_inf) * tf;
+        case 2:
+            tf = (time < Tf) ? 0.5 * (1.0 - cos(0.5 * pi * time / Tf)) : 1.0;
+            return cos(theta_inf) * tf;
+        case 3: return cos(theta_inf);
+        case 6: return time;
+        case 22: return 0.1;
+        default: return 0.0;
+    }
+}
+__device__ double mean_uy(int mode, double time, double theta_inf, double Tf, double pi) {  // mean_velocity.f90:46-84
+    double tf;
+    switch (mode) {
+        case 1:
+            tf = (time < Tf) ? (time * time * time) / (-0.5 * Tf * Tf * Tf) + 3.0 * (time * time) / (Tf * Tf) : 1.0;
+            return sin(theta_inf) * tf;
+        case 2:
+            tf = (time < Tf) ? 0.5 * (1.0 - cos(0.5 * pi * time / Tf)) : 1.0;
+            return sin(theta_inf) * tf;
+        case 3: return sin(theta_inf);
+        default: return 0.0;
+    }
+}
+
+// Start of a fluid step: the CFL/penalization/fixed dt of cal_nlk (NavierStokes.f90:59-78)
+// from the velocity statistics of the previous step, the AB2 weights (:488-489), the mean
+// flow at time+dt1 and the drag window of cal_drag (:539-564).
+__global__ void __launch_bounds__(256) k_step_begin(StepArgs a) {
+    __shared__ double smax[256], su[256], sv[256];
+    __shared__ double bmin[2][256], bmax[2][256];
+    double m = 0.0, s0 = 0.0, s1 = 0.0;
+    for (int b = threadIdx.x; b < a.nblk; b += blockDim.x) {
+        const double* r = a.red + (size_t)b * RED_NSLOTS;
+        m = fmax(m, r[RED_UMAX2]);
+        s0 += r[RED_SUM_U];
+        s1 += r[RED_SUM_V];
+    }
+    double xmn = 1e300, xmx = -1e300, ymn = 1e300, ymx = -1e300;
+    for (int i = threadIdx.x; i < a.ns; i += blockDim.x) {
+        xmn = fmin(xmn, a.bx[i]); xmx = fmax(xmx, a.bx[i]);
+        ymn = fmin(ymn, a.by[i]); ymx = fmax(ymx, a.by[i]);
+    }
+    smax[threadIdx.x] = m; su[threadIdx.x] = s0; sv[threadIdx.x] = s1;
+    bmin[0][threadIdx.x] = xmn; bmax[0][threadIdx.x] = xmx; bmin[1][threadIdx.x] = ymn; bmax[1][threadIdx.x] = ymx;
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1) {
+        if (threadIdx.x < o) {
+            const int j = threadIdx.x + o;
+            smax[threadIdx.x] = fmax(smax[threadIdx.x], smax[j]);
+            su[threadIdx.x] += su[j];
+            sv[threadIdx.x] += sv[j];
+            bmin[0][threadIdx.x] = fmin(bmin[0][threadIdx.x], bmin[0][j]);
+            bmax[0][threadIdx.x] = fmax(bmax[0][threadIdx.x], bmax[0][j]);
+            bmin[1][threadIdx.x] = fmin(bmin[1][threadIdx.x], bmin[1][j]);
+            bmax[1][threadIdx.x] = fmax(bmax[1][threadIdx.x], bmax[1][j]);
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x != 0) return;
+    DevScalars* S = a.S;
+    if (!a.explicit_step) S->dt0 = S->dt1;
+    const double time = S->time;
+    const double u_max = sqrt(smax[0]);
+    double dt1 = a.cfl * fmin(a.dx, a.dy) / u_max;
+    if (u_max < 1.e-10) dt1 = 1.e-2;
+    if (a.iBeam > 0) dt1 = fmin(0.9 * a.eps, dt1);
+    if (a.dt_fixed > 0.0) dt1 = fmin(a.dt_fixed, dt1);
+    if ((a.time_end - time) < dt1) dt1 = a.time_end - time;
+    S->dt1 = dt1;
+    S->u_max = u_max;
+    S->umax2 = smax[0];
+    S->mean_ux = su[0] / a.NN;
+    S->mean_uy = sv[0] / a.NN;
+    S->explicit_step = a.explicit_step;
+    if (!a.explicit_step) {
+        const double dt0 = S->dt0;
+        S->b10 = dt1 / dt0 * (0.5 * dt1 + dt0);
+        S->b11 = -0.5 * (dt1 * dt1) / dt0;
+    } else {
+        S->b10 = dt1;
+        S->b11 = 0.0;
+    }
+    S->mean_u_next = a.U_mean_true * mean_ux(a.iMeanVelocity, time + dt1, a.theta_inf, a.T_fullspeed, a.pi);
+    S->mean_v_next = a.U_mean_true * mean_uy(a.iMeanVelocity, time + dt1, a.theta_inf, a.T_fullspeed, a.pi);
+    if (a.iBeam > 0) {
+        const double r_cyl = 0.0, tb = a.t_beam;
+        int iymax = (int)((fmax(bmax[1][0] + 1.5 * tb, a.y0 + 2.0 * r_cyl)) / a.dy);
+        int iymin = (int)((fmin(bmin[1][0] - 1.5 * tb, a.y0 - 2.0 * r_cyl)) / a.dy);
+        int ixmin = (int)(fmin((a.x0 - fmax(2.5 * r_cyl, 1.5 * tb)), (bmin[0][0] - 1.5 * tb)) / a.dx);
+        int ixmax = (int)((bmax[0][0] + 1.5 * tb) / a.dx);
+        if (ixmin < 0) ixmin = 0;
+        if (ixmax > a.nx - 1) ixmax = a.nx - 1;
+        if (iymin < 0) iymin = 0;
+        if (iymax > a.ny - 1) iymax = a.ny - 1;
+        S->win[0] = ixmin; S->win[1] = ixmax; S->win[2] = iymin; S->win[3] = iymax;
+    } else {
+        S->win[0] = 0; S->win[1] = a.nx - 1; S->win[2] = 0; S->win[3] = a.ny - 1;
+    }
+}
+
+// End of the fluid part: cal_energy (NavierStokes.f90:222-263) and cal_drag (:566-589)
+// from the per-block partial sums, summed in a fixed order.
+__global__ void __launch_bounds__(256) k_fluid_finish(StepArgs a) {
+    __shared__ double sm[RED_NSLOTS][256];
+    double acc[RED_NSLOTS];
+    for (int s = 0; s < RED_NSLOTS; ++s) acc[s] = 0.0;
+    for (int b = threadIdx.x; b < a.nblk; b += blockDim.x) {
+        const double* r = a.red + (size_t)b * RED_NSLOTS;
+        for (int s = 0; s < RED_NSLOTS; ++s) acc[s] = (s == RED_UMAX2) ? fmax(acc[s], r[s]) : acc[s] + r[s];
+    }
+    for (int s = 0; s < RED_NSLOTS; ++s) sm[s][threadIdx.x] = acc[s];
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1) {
+        if (threadIdx.x < o)
+            for (int s = 0; s < RED_NSLOTS; ++s)
+                sm[s][threadIdx.x] = (s == RED_UMAX2) ? fmax(sm[s][threadIdx.x], sm[s][threadIdx.x + o]) : sm[s][threadIdx.x] + sm[s][threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x != 0) return;
+    DevScalars* S = a.S;
+    const double dx = a.dx, dy = a.dy, norm = dx * dy;
+    S->vor_rms = dx * dy * sqrt(sm[RED_OMEGA2][0]);
+    S->kinetic = 0.5 * dx * dy * sm[RED_KIN][0];
+    S->dissipation = a.nu * dx * dy * sm[RED_OMEGA2][0];
+    S->porous_diss = dx * dy * sm[RED_POROUS][0];
+    S->inflow_solid = dx * dy * sm[RED_INFLOW_SOLID][0];
+    S->inflow_mean = dx * dy * a.U_mean_true * sm[RED_INFLOW_MEAN][0];
+    if (a.iBeam > 0) {
+        S->force[0] = sm[RED_DRAG_X][0] * norm;
+        S->force[1] = sm[RED_DRAG_Y][0] * norm;
+        const double dn = sm[RED_UNST_X][0] * norm * a.eps, ln = sm[RED_UNST_Y][0] * norm * a.eps;
+        if (S->unst_ready) {
+            S->force_unst[0] = (dn - S->drag_unst_old) / S->dt1;
+            S->force_unst[1] = (ln - S->lift_unst_old) / S->dt1;
+        } else {
+            S->force_unst[0] = 0.0;
+            S->force_unst[1] = 0.0;
+        }
+        S->drag_unst_old = dn;
+        S->lift_unst_old = ln;
+        S->unst_ready = 1;
+    }
+}
+
+struct AdvArgs {
+    DevScalars* S;
+    int ns;
+    double *x, *y, *vx, *vy, *th, *thd, *p_old, *p_new, *tau_old, *tau_new;
+    double* rows;
+};
+
+// time_step.f90:152-161 / :222-236: swap, time += dt1, old <- new beam loads, beam_data row.
+__global__ void __launch_bounds__(256) k_advance(AdvArgs a) {
+    for (int i = threadIdx.x; i < a.ns; i += blockDim.x) {
+        a.p_old[i] = a.p_new[i];
+        a.tau_old[i] = a.tau_new[i];
+    }
+    if (threadIdx.x == 0) {
+        DevScalars* S = a.S;
+        const int ns = a.ns;
+        S->time = S->time + S->dt1;
+        S->step += 1;
+        const double row[21] = {S->time, a.p_new[ns - 1], a.p_new[3 * ns / 4], a.p_new[ns / 2], a.x[ns - 1], a.y[ns - 1],
+                                a.vx[ns - 1], a.vy[ns - 1], a.th[ns - 1], a.thd[ns - 1], S->force[0], S->force[1],
+                                S->force_unst[0], S->force_unst[1], S->force_press[0], S->force_press[1],
+                                S->inertial_force[0], S->inertial_force[1], S->e_kinetic, S->e_elastic, S->e_pot};
+        for (int c = 0; c < 21; ++c) S->row[c] = row[c];
+        if (a.rows && S->run_row < S->run_cap) {
+            for (int c = 0; c < 21; ++c) a.rows[(size_t)S->run_row * 21 + c] = row[c];
+            S->run_row += 1;
+        }
+    }
+}
+
+// ---- the packed Temperton layout (ABI boundary only) ---------------------------------
+// unpack: fk (Fortran (0:nx-1,0:ny-1)) -> S[kx][ky]   (cof_fftw33.f90:214-233)
+template <typename R>
+__global__ void k_unpack(const double* fk, C2<R>* H, int nx, int ny) {
+    const int hx = nx / 2;
+    const int kx = blockIdx.x;
+    for (int l = threadIdx.x; l <= ny / 2; l += blockDim.x) {
+        C2<R>* row = H + (size_t)kx * ny;
+        if (l == 0) {
+            row[0] = mk<R>((R)fk[2 * kx], (R)fk[2 * kx + 1]);
+        } else if (l == ny / 2) {
+            row[ny / 2] = mk<R>(0, 0);
+        } else {
+            const double a = fk[(size_t)(2 * l) * nx + 2 * kx], b = fk[(size_t)(2 * l + 1) * nx + 2 * kx];
+            const double c = fk[(size_t)(2 * l) * nx + 2 * kx + 1], d = fk[(size_t)(2 * l + 1) * nx + 2 * kx + 1];
+            row[l] = mk<R>((R)(a - d), (R)(b + c));
+            row[ny - l] = mk<R>((R)(a + d), (R)(-b + c));
+        }
+    }
+    (void)hx;
+}
+// pack: S[kx][ky] -> fk   (cof_fftw33.f90:168-190)
+template <typename R>
+__global__ void k_pack(const C2<R>* H, double* fk, int nx, int ny) {
+    const int kx = blockIdx.x;
+    const C2<R>* row = H + (size_t)kx * ny;
+    for (int l = threadIdx.x; l < ny / 2; l += blockDim.x) {
+        if (l == 0) {
+            fk[2 * kx] = (double)row[0].x;
+            fk[2 * kx + 1] = (double)row[0].y;
+            fk[(size_t)nx + 2 * kx] = 0.0;
+            fk[(size_t)nx + 2 * kx + 1] = 0.0;
+        } else {
+            const C2<R> p = row[l], m = row[ny - l];
+            fk[(size_t)(2 * l) * nx + 2 * kx] = 0.5 * ((double)p.x + (double)m.x);
+            fk[(size_t)(2 * l + 1) * nx + 2 * kx] = 0.5 * ((double)p.y - (double)m.y);
+            fk[(size_t)(2 * l) * nx + 2 * kx + 1] = 0.5 * ((double)p.y + (double)m.y);
+            fk[(size_t)(2 * l + 1) * nx + 2 * kx + 1] = 0.5 * (-(double)p.x + (double)m.x);
+        }
+    }
+}
+
+// Pointwise spectral operators directly on packed arrays (cofdx.f90, cofdy.f90, cofdxdx.f90,
+// cofdydy.f90, cofdxdy.f90, poisson.f90, cal_vis.f90, dealiase_mask.f90).
+enum PackedOp { PK_DX = 0, PK_DY, PK_DXDX, PK_DYDY, PK_DXDY, PK_POISSON, PK_VIS, PK_DEALIAS };
+__global__ void k_packed_op(const double* in, double* out, int op, int nx, int ny, double xl, double yl, double pi,
+                            double scalex, double scaley, double nu, double dt, int idealis) {
+    const size_t N = (size_t)nx * ny;
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < N; e += (size_t)gridDim.x * blockDim.x) {
+        const int kx = (int)(e % nx), ky = (int)(e / nx);
+        auto IN = [&](int x, int y) { return in[(size_t)y * nx + x]; };
+        double r = 0.0;
+        switch (op) {
+            case PK_DX: {
+                const double s1 = 2.0 * pi / xl;
+                r = ((kx & 1) == 0) ? -IN(kx + 1, ky) * (double)(kx / 2) * s1 : IN(kx - 1, ky) * (double)((kx - 1) / 2) * s1;
+                break;
+            }
+            case PK_DY: {
+                const double s1 = 2.0 * pi / yl;
+                r = ((ky & 1) == 0) ? -IN(kx, ky + 1) * (double)(ky / 2) * s1 : IN(kx, ky - 1) * (double)((ky - 1) / 2) * s1;
+                break;
+            }
+            case PK_DXDX: {
+                const double t = 2.0 * pi / xl, k = (double)(kx / 2);
+                r = -IN(kx, ky) * (k * k) * (t * t);
+                break;
+            }
+            case PK_DYDY: {
+                const double t = 2.0 * pi / yl, k = (double)(ky / 2);
+                r = -IN(kx, ky) * (k * k) * (t * t);
+                break;
+            }
+            case PK_DXDY: {
+                const int a = kx / 2, b = ky / 2, ia = kx & 1, ib = ky & 1;
+                const double fac = -(double)a * (double)b * ((2.0 * pi / xl) * (2.0 * pi / yl));
+                if (!ia && !ib) r = fac * IN(2 * a + 1, 2 * b + 1);
+                else if (ia && !ib) r = -fac * IN(2 * a, 2 * b + 1);
+                else if (!ia && ib) r = -fac * IN(2 * a + 1, 2 * b);
+                else r = fac * IN(2 * a, 2 * b);
+                break;
+            }
+            case PK_POISSON: {
+                const int a = kx / 2, b = ky / 2;
+                if (a == 0 && b == 0) r = 0.0;
+                else r = IN(kx, ky) / ((double)(a * a) * scalex + (double)(b * b) * scaley);
+                break;
+            }
+            case PK_VIS: {
+                const int a = kx / 2, b = ky / 2;
+                const double coefx = -dt * nu * scalex, coefy = -dt * nu * scaley;
+                r = exp(coefx * (double)(a * a) + coefy * (double)(b * b));
+                break;
+            }
+            default: {
+                const int a = kx / 2, b = ky / 2;
+                const double kxt = 2.0 / 3.0 * (double)(nx / 2 - 1), kyt = 2.0 / 3.0 * (double)(ny / 2 - 1);
+                r = 1.0;
+                if (idealis == 1 && (double)a * (double)a / (kxt * kxt) + (double)b * (double)b / (kyt * kyt) >= 1.0) r = 0.0;
+                break;
+            }
+        }
+        out[e] = r;
+    }
+}
+
+template <typename R>
+__global__ void k_convert(const R* in, double* out, size_t n) {
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) out[e] = (double)in[e];
+}
+template <typename R>
+__global__ void k_convert_in(const double* in, R* out, size_t n) {
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) out[e] = (R)in[e];
+}
+
+}  // namespace fsibe
+
+using namespace fsibe;
+
+enum PhysIdx { PH_U = 0, PH_V, PH_MASK, PH_MVX, PH_MVY, PH_VORMEAN, PH_PRESS, PH_SA, PH_SB, PH_0, PH_N };
+enum SpecIdx { SP_W = 0, SP_M, SP_WLO, SP_A, SP_B, SP_TU, SP_TV, SP_TW, SP_TSA, SP_TSB, SP_TDX, SP_TDY, SP_P1, SP_P2, SP_TQ, SP_0, SP_1, SP_N };
+enum BeamIdx { B_X = 0, B_Y, B_VX, B_VY, B_TH, B_THD, B_AX, B_AY, B_PO, B_PN, B_TO, B_TN, B_N };
+
+struct fsibe_ctx {
+    fsibe_params P;
+    Geometry g;
+    bool fp32 = false;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    SizeKernels<double> kxd{}, kyd{};
+    SizeKernels<float> kxf{}, kyf{};
+    void* phys[PH_N] = {};
+    void* spec[SP_N] = {};
+    void *twX = nullptr, *twR = nullptr, *twY = nullptr;
+    DevScalars* S = nullptr;
+    double* red = nullptr;
+    double* beam[B_N] = {};
+    double* oo = nullptr;
+    double *ws = nullptr, *band = nullptr, *urow = nullptr;
+    Prim* prims = nullptr;
+    int *nprims = nullptr, *rect = nullptr;
+    unsigned* counter = nullptr;
+    double* rows = nullptr;
+    int rows_cap = 0;
+    double* dscratch = nullptr;   // 2*nx*ny doubles (ABI transfers, packed arrays)
+    double* dscratch2 = nullptr;  // nx*ny doubles
+    double gerf = 0.0;
+    double U_mean_true = 1.0;
+    bool initialized = false, startup_done = false;
+    bool use_graph = false, graph_ready = false;
+    cudaGraphExec_t gexec = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    std::string err;
+    int launches = 0;
+};
+
+static std::string g_err;
+
+#define CK(ctx, call)                                                                   \
+    do {                                                                                \
+        cudaError_t e_ = (call);                                                        \
+        if (e_ != cudaSuccess) {                                                        \
+            (ctx)->err = std::string(#call) + ": " + cudaGetErrorString(e_);            \
+            return FSIBE_ERR_CUDA;                                                      \
+        }                                                                               \
+    } while (0)
+
+#define CKL(ctx)                                                                        \
+    do {                                                                                \
+        cudaError_t e_ = cudaGetLastError();                                            \
+        if (e_ != cudaSuccess) {                                                        \
+            (ctx)->err = std::string("kernel launch: ") + cudaGetErrorString(e_);       \
+            return FSIBE_ERR_CUDA;                                                      \
+        }                                                                               \
+    } while (0)
+
+static bool pow2_ok(int n) { return n >= 32 && n <= 4096 && (n & (n - 1)) == 0; }
+
+template <typename T>
+static void make_table(std::vector<T>& out, long n, long count) {
+    const long double pi_l = 3.141592653589793238462643383279502884L;
+    out.resize(count);
+    for (long m = 0; m < count; ++m) {
+        const long double a = 2.0L * pi_l * (long double)m / (long double)n;
+        out[m].x = (decltype(out[m].x))cosl(a);
+        out[m].y = (decltype(out[m].y))(-sinl(a));
+    }
+}
+
+template <typename R>
+static KArgs<R> kargs(fsibe_ctx* c) {
+    KArgs<R> a;
+    std::memset(&a, 0, sizeof(a));
+    a.g = c->g;
+    a.nu = c->P.nu;
+    a.eps = c->P.eps;
+    R** ph[] = {&a.u, &a.v, &a.mask, &a.mvx, &a.mvy, &a.vor_mean, &a.press, &a.sa, &a.sb, &a.phys0};
+    for (int i = 0; i < PH_N; ++i) *ph[i] = reinterpret_cast<R*>(c->phys[i]);
+    C2<R>** sp[] = {&a.W, &a.M, &a.Wlo, &a.A, &a.B, &a.Tu, &a.Tv, &a.Tw, &a.Tsa, &a.Tsb, &a.Tdx, &a.Tdy, &a.P1, &a.P2, &a.Tq, &a.spec0, &a.spec1};
+    for (int i = 0; i < SP_N; ++i) *sp[i] = reinterpret_cast<C2<R>*>(c->spec[i]);
+    a.twX = reinterpret_cast<const C2<R>*>(c->twX);
+    a.twR = reinterpret_cast<const C2<R>*>(c->twR);
+    a.twY = reinterpret_cast<const C2<R>*>(c->twY);
+    a.S = c->S;
+    a.red = c->red;
+    a.viscous = c->P.iViscous == 1;
+    a.pressure_on = (c->P.iFLUSI == 1 || c->P.iSaveBeam > 0);
+    a.penalize = c->P.iBeam > 0;
+    a.op = OP_ID;
+    return a;
+}
+
+template <typename R> static SizeKernels<R>& kx_of(fsibe_ctx* c);
+template <> SizeKernels<double>& kx_of<double>(fsibe_ctx* c) { return c->kxd; }
+template <> SizeKernels<float>& kx_of<float>(fsibe_ctx* c) { return c->kxf; }
+template <typename R> static SizeKernels<R>& ky_of(fsibe_ctx* c);
+template <> SizeKernels<double>& ky_of<double>(fsibe_ctx* c) { return c->kyd; }
+template <> SizeKernels<float>& ky_of<float>(fsibe_ctx* c) { return c->kyf; }
+
+// launch helpers (count launches for the bench's gpu_launches)
+template <typename R>
+static void launch_x(fsibe_ctx* c, void (*k)(KArgs<R>), int smem, const KArgs<R>& a) {
+    const SizeKernels<R>& K = kx_of<R>(c);
+    k<<<c->g.ny / K.x_rows, K.x_threads, smem, c->stream>>>(a);
+    c->launches++;
+}
+template <typename R>
+static void launch_y(fsibe_ctx* c, void (*k)(KArgs<R>), int smem, const KArgs<R>& a) {
+    const SizeKernels<R>& K = ky_of<R>(c);
+    k<<<c->g.hx, K.y_threads, smem, c->stream>>>(a);
+    c->launches++;
+}
+
+static StepArgs step_args(fsibe_ctx* c, int explicit_step, int nblk) {
+    StepArgs a;
+    std::memset(&a, 0, sizeof(a));
+    a.S = c->S;
+    a.red = c->red;
+    a.nblk = nblk;
+    a.explicit_step = explicit_step;
+    a.iBeam = c->P.iBeam;
+    a.iMeanVelocity = c->P.iMeanVelocity;
+    a.ns = c->P.ns;
+    a.nx = c->P.nx;
+    a.ny = c->P.ny;
+    a.cfl = c->P.cfl;
+    a.dx = c->g.dx;
+    a.dy = c->g.dy;
+    a.eps = c->P.eps;
+    a.dt_fixed = c->P.dt_fixed;
+    a.time_end = c->P.time_end;
+    a.theta_inf = c->P.theta_inf;
+    a.T_fullspeed = c->P.T_fullspeed;
+    a.U_mean_true = c->U_mean_true;
+    a.pi = c->g.pi;
+    a.nu = c->P.nu;
+    a.x0 = c->P.x0;
+    a.y0 = c->P.y0;
+    a.t_beam = c->P.t_beam;
+    a.NN = (double)c->P.nx * (double)c->P.ny;
+    a.bx = c->beam[B_X];
+    a.by = c->beam[B_Y];
+    return a;
+}
+
+template <typename R>
+static int x_blocks(fsibe_ctx* c) { return c->g.ny / kx_of<R>(c).x_rows; }
+
+// EvolveFluidExplicit / EvolveFluidAB2 + pressure (NavierStokes.f90:422-508, 273-403)
+template <typename R>
+static int fluid_step_t(fsibe_ctx* c, int explicit_step) {
+    KArgs<R> a = kargs<R>(c);
+    SizeKernels<R>& KX = kx_of<R>(c);
+    SizeKernels<R>& KY = ky_of<R>(c);
+    const int nblk = x_blocks<R>(c);
+    StepArgs sa = step_args(c, explicit_step, nblk);
+    k_step_begin<<<1, 256, 0, c->stream>>>(sa);
+    c->launches++;
+    launch_x<R>(c, KX.nl_x, KX.x_smem2, a);
+    launch_y<R>(c, KY.nl_y, KY.y_smem2, a);
+    launch_x<R>(c, KX.press_x, KX.x_smem2, a);
+    k_fluid_finish<<<1, 256, 0, c->stream>>>(sa);
+    c->launches++;
+    if (a.pressure_on) {
+        launch_y<R>(c, KY.press_y, KY.y_smem2, a);
+        launch_x<R>(c, KX.press_fin, KX.x_smem1, a);
+    } else {
+        CK(c, cudaMemsetAsync(c->phys[PH_PRESS], 0, sizeof(R) * (size_t)c->g.nx * c->g.ny, c->stream));
+    }
+    CKL(c);
+    return FSIBE_OK;
+}
+
+static int fluid_step(fsibe_ctx* c, int explicit_step) {
+    return c->fp32 ? fluid_step_t<float>(c, explicit_step) : fluid_step_t<double>(c, explicit_step);
+}
+
+static MaskArgs mask_args(fsibe_ctx* c) {
+    MaskArgs m;
+    std::memset(&m, 0, sizeof(m));
+    m.S = c->S;
+    m.nx = c->P.nx; m.ny = c->P.ny; m.ns = c->P.ns;
+    m.sharp_trailing = c->P.iSharpTrailing;
+    m.sharp = std::fabs(c->P.N_smooth) < 1e-4;
+    m.dx = c->g.dx; m.dy = c->g.dy; m.ds = c->g.ds;
+    m.t_beam = c->P.t_beam; m.N_smooth = c->P.N_smooth; m.eps = c->P.eps; m.pi = c->g.pi;
+    m.angle_deg = c->P.angle_beam;
+    m.x = c->beam[B_X]; m.y = c->beam[B_Y]; m.vx = c->beam[B_VX]; m.vy = c->beam[B_VY]; m.th = c->beam[B_TH];
+    m.prims = c->prims; m.nprims = c->nprims; m.rect = c->rect;
+    m.mask = c->phys[PH_MASK]; m.mvx = c->phys[PH_MVX]; m.mvy = c->phys[PH_MVY];
+    return m;
+}
+
+static int create_mask(fsibe_ctx* c) {
+    if (c->P.iBeam <= 0) {
+        const size_t bytes = (c->fp32 ? 4 : 8) * (size_t)c->g.nx * c->g.ny;
+        for (int q : {PH_MASK, PH_MVX, PH_MVY}) CK(c, cudaMemsetAsync(c->phys[q], 0, bytes, c->stream));
+        return FSIBE_OK;
+    }
+    launch_mask(mask_args(c), c->gerf, c->fp32, c->stream);
+    c->launches += 2;
+    CKL(c);
+    return FSIBE_OK;
+}
+
+static int get_forces(fsibe_ctx* c) {
+    ForceArgs f;
+    std::memset(&f, 0, sizeof(f));
+    f.S = c->S;
+    f.nx = c->P.nx; f.ny = c->P.ny; f.ns = c->P.ns; f.viscous = c->P.iViscous == 1;
+    f.xl = c->P.xl; f.yl = c->P.yl; f.dx = c->g.dx; f.dy = c->g.dy; f.ds = c->g.ds;
+    f.t_beam = c->P.t_beam; f.N_smooth = c->P.N_smooth; f.pi = c->g.pi; f.angle_deg = c->P.angle_beam;
+    f.t_release = c->P.t_release; f.tau = c->P.tau;
+    f.x = c->beam[B_X]; f.y = c->beam[B_Y]; f.th = c->beam[B_TH];
+    f.press = c->phys[PH_PRESS]; f.sa = c->phys[PH_SA]; f.sb = c->phys[PH_SB];
+    f.p_new = c->beam[B_PN]; f.tau_new = c->beam[B_TN];
+    f.counter = c->counter;
+    f.fp32 = c->fp32 ? 1 : 0;
+    const double dxi = (c->P.xl - c->g.dx) / (double)(c->P.nx - 1);
+    const double dyi = (c->P.yl - c->g.dy) / (double)(c->P.ny - 1);
+    launch_forces(f, dxi, dyi, c->stream);
+    c->launches++;
+    CKL(c);
+    return FSIBE_OK;
+}
+
+static BeamArgs beam_args(fsibe_ctx* c) {
+    BeamArgs b;
+    std::memset(&b, 0, sizeof(b));
+    b.S = c->S;
+    b.ns = c->P.ns; b.iImpulse = c->P.iImpulse; b.maxit = c->P.newton_maxit; b.iFLUSI = c->P.iFLUSI;
+    b.ds = c->g.ds; b.eta = c->P.eta; b.mue = c->P.mue; b.sigma = c->P.sigma;
+    b.t_release = c->P.t_release; b.tau = c->P.tau; b.tol = c->P.newton_tol; b.pi = c->g.pi;
+    b.x0 = c->P.x0; b.y0 = c->P.y0; b.angle_deg = c->P.angle_beam;
+    b.x = c->beam[B_X]; b.y = c->beam[B_Y]; b.vx = c->beam[B_VX]; b.vy = c->beam[B_VY];
+    b.th = c->beam[B_TH]; b.thd = c->beam[B_THD]; b.ax = c->beam[B_AX]; b.ay = c->beam[B_AY];
+    b.p_old = c->beam[B_PO]; b.p_new = c->beam[B_PN]; b.tau_old = c->beam[B_TO]; b.tau_new = c->beam[B_TN];
+    b.oo = c->oo;
+    b.ws = c->ws; b.band = c->band; b.urow = c->urow;
+    return b;
+}
+
+static int solid_step(fsibe_ctx* c) {
+    launch_beam(beam_args(c), c->stream);
+    c->launches++;
+    CKL(c);
+    return FSIBE_OK;
+}
+
+static int advance(fsibe_ctx* c) {
+    AdvArgs a;
+    a.S = c->S;
+    a.ns = c->P.ns;
+    a.x = c->beam[B_X]; a.y = c->beam[B_Y]; a.vx = c->beam[B_VX]; a.vy = c->beam[B_VY];
+    a.th = c->beam[B_TH]; a.thd = c->beam[B_THD];
+    a.p_old = c->beam[B_PO]; a.p_new = c->beam[B_PN]; a.tau_old = c->beam[B_TO]; a.tau_new = c->beam[B_TN];
+    a.rows = c->rows;
+    k_advance<<<1, 256, 0, c->stream>>>(a);
+    c->launches++;
+    CKL(c);
+    return FSIBE_OK;
+}
+
+// time_step.f90:178-228 (or :120-162 for the start-up step)
+static int step_body(fsibe_ctx* c, int explicit_step) {
+    const fsibe_params& P = c->P;
+    int st;
+    if (P.iFLUSI == 1 || P.iMotion > 0) { st = create_mask(c); if (st) return st; }
+    st = fluid_step(c, explicit_step);
+    if (st) return st;
+    if (P.iFLUSI == 1 || P.iSaveBeam > 0) { st = get_forces(c); if (st) return st; }
+    if (P.iFLUSI == 1) { st = solid_step(c); if (st) return st; }
+    return advance(c);
+}
+
+static int do_step(fsibe_ctx* c) {
+    if (!c->initialized) { c->err = "step before init_fields"; return FSIBE_ERR_STATE; }
+    if (!c->startup_done) {
+        int st = step_body(c, 1);
+        if (st) return st;
+        c->startup_done = true;
+        return FSIBE_OK;
+    }
+    if (c->use_graph) {
+        if (!c->graph_ready) {
+            CK(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+            const int before = c->launches;
+            int st = step_body(c, 0);
+            cudaGraph_t g = nullptr;
+            cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+            if (st) return st;
+            if (e != cudaSuccess) { c->err = std::string("capture: ") + cudaGetErrorString(e); return FSIBE_ERR_CUDA; }
+            c->graph = g;
+            CK(c, cudaGraphInstantiate(&c->gexec, g, 0));
+            c->graph_ready = true;
+            c->launches = before;
+        }
+        CK(c, cudaGraphLaunch(c->gexec, c->stream));
+        c->launches += 0;
+        return FSIBE_OK;
+    }
+    return step_body(c, 0);
+}
+
+static void free_graph(fsibe_ctx* c) {
+    if (c->gexec) cudaGraphExecDestroy(c->gexec);
+    if (c->graph) cudaGraphDestroy(c->graph);
+    c->gexec = nullptr;
+    c->graph = nullptr;
+    c->graph_ready = false;
+}
+
+// ---- transfers ----------------------------------------------------------------------
+static int to_host(fsibe_ctx* c, const void* dev, size_t n, double* host) {
+    if (c->fp32) {
+        k_convert<float><<<256, 256, 0, c->stream>>>(reinterpret_cast<const float*>(dev), c->dscratch, n);
+        CKL(c);
+        CK(c, cudaMemcpyAsync(host, c->dscratch, n * 8, cudaMemcpyDeviceToHost, c->stream));
+    } else {
+        CK(c, cudaMemcpyAsync(host, dev, n * 8, cudaMemcpyDeviceToHost, c->stream));
+    }
+    CK(c, cudaStreamSynchronize(c->stream));
+    return FSIBE_OK;
+}
+
+static int from_host(fsibe_ctx* c, const double* host, size_t n, void* dev) {
+    if (c->fp32) {
+        CK(c, cudaMemcpyAsync(c->dscratch, host, n * 8, cudaMemcpyHostToDevice, c->stream));
+        k_convert_in<float><<<256, 256, 0, c->stream>>>(c->dscratch, reinterpret_cast<float*>(dev), n);
+        CKL(c);
+    } else {
+        CK(c, cudaMemcpyAsync(dev, host, n * 8, cudaMemcpyHostToDevice, c->stream));
+    }
+    CK(c, cudaStreamSynchronize(c->stream));
+    return FSIBE_OK;
+}
+
+static int spec_to_packed(fsibe_ctx* c, const void* H, double* host_fk) {
+    if (c->fp32) k_pack<float><<<c->g.hx, 256, 0, c->stream>>>(reinterpret_cast<const float2*>(H), c->dscratch, c->g.nx, c->g.ny);
+    else k_pack<double><<<c->g.hx, 256, 0, c->stream>>>(reinterpret_cast<const double2*>(H), c->dscratch, c->g.nx, c->g.ny);
+    CKL(c);
+    CK(c, cudaMemcpyAsync(host_fk, c->dscratch, 8 * (size_t)c->g.nx * c->g.ny, cudaMemcpyDeviceToHost, c->stream));
+    CK(c, cudaStreamSynchronize(c->stream));
+    return FSIBE_OK;
+}
+
+static int packed_to_spec(fsibe_ctx* c, const double* host_fk, void* H) {
+    CK(c, cudaMemcpyAsync(c->dscratch, host_fk, 8 * (size_t)c->g.nx * c->g.ny, cudaMemcpyHostToDevice, c->stream));
+    if (c->fp32) k_unpack<float><<<c->g.hx, 256, 0, c->stream>>>(c->dscratch, reinterpret_cast<float2*>(H), c->g.nx, c->g.ny);
+    else k_unpack<double><<<c->g.hx, 256, 0, c->stream>>>(c->dscratch, reinterpret_cast<double2*>(H), c->g.nx, c->g.ny);
+    CKL(c);
+    CK(c, cudaStreamSynchronize(c->stream));
+    return FSIBE_OK;
+}
+
+template <typename R>
+static int fwd2d(fsibe_ctx* c, void* spec_out) {
+    KArgs<R> a = kargs<R>(c);
+    a.spec1 = reinterpret_cast<C2<R>*>(spec_out);
+    launch_x<R>(c, kx_of<R>(c).xfwd, kx_of<R>(c).x_smem1, a);
+    launch_y<R>(c, ky_of<R>(c).yfwd, ky_of<R>(c).y_smem1, a);
+    CKL(c);
+    return FSIBE_OK;
+}
+
+template <typename R>
+static int inv_y(fsibe_ctx* c, const void* spec_in, void* t_out, int op) {
+    KArgs<R> a = kargs<R>(c);
+    a.spec1 = reinterpret_cast<C2<R>*>(const_cast<void*>(spec_in));
+    a.spec0 = reinterpret_cast<C2<R>*>(t_out);
+    a.op = op;
+    launch_y<R>(c, ky_of<R>(c).yinv, ky_of<R>(c).y_smem1, a);
+    CKL(c);
+    return FSIBE_OK;
+}
+
+template <typename R>
+static int inv_x(fsibe_ctx* c) {
+    KArgs<R> a = kargs<R>(c);
+    launch_x<R>(c, kx_of<R>(c).xinv, kx_of<R>(c).x_smem1, a);
+    CKL(c);
+    return FSIBE_OK;
+}
+
+// cal_velocity at time (init) : u, v and the velocity statistics for the first cal_nlk
+template <typename R>
+static int init_velocity(fsibe_ctx* c) {
+    int st;
+    if ((st = inv_y<R>(c, c->spec[SP_W], c->spec[SP_TU], OP_U))) return st;
+    if ((st = inv_y<R>(c, c->spec[SP_W], c->spec[SP_TV], OP_V))) return st;
+    if ((st = inv_y<R>(c, c->spec[SP_W], c->spec[SP_TDX], OP_DX))) return st;
+    if ((st = inv_y<R>(c, c->spec[SP_W], c->spec[SP_TDY], OP_DY))) return st;
+    KArgs<R> a = kargs<R>(c);
+    launch_x<R>(c, kx_of<R>(c).vel_x, kx_of<R>(c).x_smem2, a);
+    CKL(c);
+    return FSIBE_OK;
+}
+
+static double host_mean(const fsibe_params& P, double t, bool x) {
+    const double pi = 4.0 * std::atan(1.0);
+    double tf = 1.0;
+    switch (P.iMeanVelocity) {
+        case 1: tf = (t < P.T_fullspeed) ? (t * t * t) / (-0.5 * P.T_fullspeed * P.T_fullspeed * P.T_fullspeed) + 3.0 * (t * t) / (P.T_fullspeed * P.T_fullspeed) : 1.0; break;
+        case 2: tf = (t < P.T_fullspeed) ? 0.5 * (1.0 - std::cos(0.5 * pi * t / P.T_fullspeed)) : 1.0; break;
+        case 3: break;
+        case 6: return x ? t : 0.0;
+        case 22: return x ? 0.1 : 0.0;
+        default: return 0.0;
+    }
+    return (x ? std::cos(P.theta_inf) : std::sin(P.theta_inf)) * tf;
+}
+
+// =====================================================================================
+// C ABI
+// =====================================================================================
+extern "C" {
+
+const char* fsibe_strerror(int s) {
+    switch (s) {
+        case FSIBE_OK: return "ok";
+        case FSIBE_ERR_PARAM: return "bad parameters";
+        case FSIBE_ERR_CUDA: return "CUDA error";
+        case FSIBE_ERR_NAN: return "NaN in the beam system";
+        case FSIBE_ERR_NEWTON_MAXIT: return "Newton iteration limit";
+        case FSIBE_ERR_SINGULAR: return "singular matrix";
+        case FSIBE_ERR_INTERP_OOB: return "interpolation target outside the grid";
+        case FSIBE_ERR_TIMEOUT: return "device wait timed out";
+        case FSIBE_ERR_UNSUPPORTED: return "unsupported size or option";
+        case FSIBE_ERR_MASK_OOB: return "beam point outside the domain";
+        case FSIBE_ERR_BRAKE: return "emergency brake (continue_timestep = .false.)";
+        case FSIBE_ERR_STATE: return "call out of order";
+        default: return "unknown status";
+    }
+}
+
+const char* fsibe_last_error(const fsibe_ctx* ctx) { return ctx ? ctx->err.c_str() : g_err.c_str(); }
+
+int fsibe_destroy(fsibe_ctx* c) {
+    if (!c) return FSIBE_OK;
+    free_graph(c);
+    for (void* p : c->phys) if (p) cudaFree(p);
+    for (void* p : c->spec) if (p) cudaFree(p);
+    for (double* p : c->beam) if (p) cudaFree(p);
+    void* others[] = {c->twX, c->twR, c->twY, c->S, c->red, c->oo, c->ws, c->band, c->urow, c->prims, c->nprims,
+                      c->rect, c->counter, c->rows, c->dscratch, c->dscratch2};
+    for (void* p : others) if (p) cudaFree(p);
+    if (c->ev0) cudaEventDestroy(c->ev0);
+    if (c->ev1) cudaEventDestroy(c->ev1);
+    if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+    return FSIBE_OK;
+}
+
+int fsibe_create(const fsibe_params* p, fsibe_ctx** out) {
+    if (!p || !out) { g_err = "null argument"; return FSIBE_ERR_PARAM; }
+    *out = nullptr;
+    if (!pow2_ok(p->nx) || !pow2_ok(p->ny)) { g_err = "nx, ny must be powers of two in [32, 4096]"; return FSIBE_ERR_UNSUPPORTED; }
+    if (p->iBeam > 0 && p->ns < 8) { g_err = "ns must be >= 8"; return FSIBE_ERR_PARAM; }
+    if (p->iBeam > 1) { g_err = "one beam per run"; return FSIBE_ERR_UNSUPPORTED; }
+    if (p->iMotion != 0) { g_err = "only the clamped leading edge (iMotion = 0) is implemented"; return FSIBE_ERR_UNSUPPORTED; }
+    if (p->precision != FSIBE_FP64 && p->precision != FSIBE_FP32C) { g_err = "precision"; return FSIBE_ERR_PARAM; }
+    if (p->iMeanVelocity == 11) { g_err = "iMeanVelocity = 11 is not implemented"; return FSIBE_ERR_UNSUPPORTED; }
+    if (p->time_method_solid != FSIBE_BDF2 && p->time_method_solid != FSIBE_CRANK_NICHOLSON &&
+        p->time_method_solid != FSIBE_EULER_IMPLICIT) { g_err = "time_method_solid"; return FSIBE_ERR_PARAM; }
+    fsibe_ctx* c = new fsibe_ctx();
+    c->P = *p;
+    if (c->P.newton_tol <= 0.0) c->P.newton_tol = 1.0e-7;
+    if (c->P.newton_maxit <= 0) c->P.newton_maxit = 50;
+    c->fp32 = p->precision == FSIBE_FP32C;
+    Geometry& g = c->g;
+    g.nx = p->nx; g.ny = p->ny; g.hx = p->nx / 2; g.ns = p->ns;
+    g.xl = p->xl; g.yl = p->yl;
+    g.dx = p->xl / (double)p->nx;
+    g.dy = p->yl / (double)p->ny;
+    g.ds = p->length / (double)(p->ns - 1);
+    g.pi = 4.0 * std::atan(1.0);
+    g.kxs = 2.0 * g.pi / p->xl;
+    g.kys = 2.0 * g.pi / p->yl;
+    g.scalex = g.kxs * g.kxs;
+    g.scaley = g.kys * g.kys;
+    const double kxt = 2.0 / 3.0 * (double)(p->nx / 2 - 1), kyt = 2.0 / 3.0 * (double)(p->ny / 2 - 1);
+    g.kx_trunc2 = kxt * kxt;
+    g.ky_trunc2 = kyt * kyt;
+    g.idealis = p->idealis;
+    c->gerf = std::fabs((std::exp(-(2.0 * 1.0) * (2.0 * 1.0)) - 1.0) / std::sqrt(g.pi));
+    SizeKernels<double> dx_, dy_;
+    SizeKernels<float> fx_, fy_;
+    if (!get_sizes(p->nx, dx_, fx_) || !get_sizes(p->ny, dy_, fy_)) { g_err = "size"; delete c; return FSIBE_ERR_UNSUPPORTED; }
+    c->kxd = dx_; c->kxf = fx_; c->kyd = dy_; c->kyf = fy_;
+    const size_t NN = (size_t)p->nx * p->ny;
+    const size_t rs = c->fp32 ? 4 : 8;
+#define ALLOC(ptr, bytes)                                                                       \
+    do {                                                                                        \
+        cudaError_t e_ = cudaMalloc((void**)&(ptr), (bytes));                                   \
+        if (e_ != cudaSuccess) { g_err = std::string("cudaMalloc: ") + cudaGetErrorString(e_); \
+                                 fsibe_destroy(c); return FSIBE_ERR_CUDA; }                     \
+        cudaMemset((ptr), 0, (bytes));                                                          \
+    } while (0)
+    for (int i = 0; i < PH_N; ++i) ALLOC(c->phys[i], rs * NN);
+    for (int i = 0; i < SP_N; ++i) ALLOC(c->spec[i], rs * NN);
+    const int ns = p->ns > 8 ? p->ns : 8, n = 2 * ns + 4;
+    for (int i = 0; i < B_N; ++i) ALLOC(c->beam[i], 8 * (size_t)ns);
+    ALLOC(c->oo, 8 * (size_t)ns * 6);
+    ALLOC(c->ws, 8 * beam_ws_doubles(ns));
+    ALLOC(c->band, 8 * (size_t)(n + 16) * 15);
+    ALLOC(c->urow, 8 * (size_t)(n + 16) * 16);
+    ALLOC(c->prims, sizeof(Prim) * (size_t)(2 * ns + 8));
+    ALLOC(c->nprims, 16);
+    ALLOC(c->rect, 16);
+    ALLOC(c->counter, 16);
+    ALLOC(c->S, sizeof(DevScalars));
+    ALLOC(c->red, 8 * (size_t)p->ny * RED_NSLOTS);
+    ALLOC(c->dscratch, 8 * 2 * NN);
+    ALLOC(c->dscratch2, 8 * NN);
+    if (c->fp32) {
+        std::vector<float2> tX, tR, tY;
+        make_table(tX, p->nx / 2, p->nx / 2);
+        make_table(tR, p->nx, p->nx / 2 + 1);
+        make_table(tY, p->ny, p->ny);
+        ALLOC(c->twX, 8 * tX.size()); ALLOC(c->twR, 8 * tR.size()); ALLOC(c->twY, 8 * tY.size());
+        cudaMemcpy(c->twX, tX.data(), 8 * tX.size(), cudaMemcpyHostToDevice);
+        cudaMemcpy(c->twR, tR.data(), 8 * tR.size(), cudaMemcpyHostToDevice);
+        cudaMemcpy(c->twY, tY.data(), 8 * tY.size(), cudaMemcpyHostToDevice);
+    } else {
+        std::vector<double2> tX, tR, tY;
+        make_table(tX, p->nx / 2, p->nx / 2);
+        make_table(tR, p->nx, p->nx / 2 + 1);
+        make_table(tY, p->ny, p->ny);
+        ALLOC(c->twX, 16 * tX.size()); ALLOC(c->twR, 16 * tR.size()); ALLOC(c->twY, 16 * tY.size());
+        cudaMemcpy(c->twX, tX.data(), 16 * tX.size(), cudaMemcpyHostToDevice);
+        cudaMemcpy(c->twR, tR.data(), 16 * tR.size(), cudaMemcpyHostToDevice);
+        cudaMemcpy(c->twY, tY.data(), 16 * tY.size(), cudaMemcpyHostToDevice);
+    }
+#undef ALLOC
+    cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) { g_err = cudaGetErrorString(e); fsibe_destroy(c); return FSIBE_ERR_CUDA; }
+    c->own_stream = true;
+    cudaEventCreate(&c->ev0);
+    cudaEventCreate(&c->ev1);
+    e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) { g_err = std::string("create: ") + cudaGetErrorString(e); fsibe_destroy(c); return FSIBE_ERR_CUDA; }
+    *out = c;
+    return FSIBE_OK;
+}
+
+int fsibe_set_stream(fsibe_ctx* c, void* stream) {
+    if (!c) return FSIBE_ERR_PARAM;
+    CK(c, cudaStreamSynchronize(c->stream));
+    free_graph(c);
+    if (c->own_stream) { cudaStreamDestroy(c->stream); c->own_stream = false; }
+    c->stream = reinterpret_cast<cudaStream_t>(stream);
+    return FSIBE_OK;
+}
+
+int fsibe_use_graph(fsibe_ctx* c, int enable) {
+    if (!c) return FSIBE_ERR_PARAM;
+    if (!enable) free_graph(c);
+    c->use_graph = enable != 0;
+    return FSIBE_OK;
+}
+
+// ---- spectral operators on packed arrays --------------------------------------------
+int fsibe_fft_forward(fsibe_ctx* c, const double* f, double* fk) {
+    if (!c || !f || !fk) return FSIBE_ERR_PARAM;
+    int st = from_host(c, f, (size_t)c->g.nx * c->g.ny, c->phys[PH_0]);
+    if (st) return st;
+    st = c->fp32 ? fwd2d<float>(c, c->spec[SP_1]) : fwd2d<double>(c, c->spec[SP_1]);
+    if (st) return st;
+    return spec_to_packed(c, c->spec[SP_1], fk);
+}
+
+int fsibe_fft_inverse(fsibe_ctx* c, const double* fk, double* f) {
+    if (!c || !f || !fk) return FSIBE_ERR_PARAM;
+    int st = packed_to_spec(c, fk, c->spec[SP_1]);
+    if (st) return st;
+    if (c->fp32) {
+        if ((st = inv_y<float>(c, c->spec[SP_1], c->spec[SP_0], OP_ID))) return st;
+        if ((st = inv_x<float>(c))) return st;
+    } else {
+        if ((st = inv_y<double>(c, c->spec[SP_1], c->spec[SP_0], OP_ID))) return st;
+        if ((st = inv_x<double>(c))) return st;
+    }
+    return to_host(c, c->phys[PH_0], (size_t)c->g.nx * c->g.ny, f);
+}
+
+static int packed_op(fsibe_ctx* c, const double* in, double* out, int op, double dt) {
+    if (!c || !out) return FSIBE_ERR_PARAM;
+    const size_t NN = (size_t)c->g.nx * c->g.ny;
+    if (in) CK(c, cudaMemcpyAsync(c->dscratch, in, 8 * NN, cudaMemcpyHostToDevice, c->stream));
+    k_packed_op<<<512, 256, 0, c->stream>>>(c->dscratch, c->dscratch2, op, c->g.nx, c->g.ny, c->P.xl, c->P.yl, c->g.pi,
+                                            c->g.scalex, c->g.scaley, c->P.nu, dt, c->P.idealis);
+    CKL(c);
+    CK(c, cudaMemcpyAsync(out, c->dscratch2, 8 * NN, cudaMemcpyDeviceToHost, c->stream));
+    CK(c, cudaStreamSynchronize(c->stream));
+    return FSIBE_OK;
+}
+
+int fsibe_cofdx(fsibe_ctx* c, const double* a, double* b) { return packed_op(c, a, b, PK_DX, 0.0); }
+int fsibe_cofdy(fsibe_ctx* c, const double* a, double* b) { return packed_op(c, a, b, PK_DY, 0.0); }
+int fsibe_cofdxdx(fsibe_ctx* c, const double* a, double* b) { return packed_op(c, a, b, PK_DXDX, 0.0); }
+int fsibe_cofdydy(fsibe_ctx* c, const double* a, double* b) { return packed_op(c, a, b, PK_DYDY, 0.0); }
+int fsibe_cofdxdy(fsibe_ctx* c, const double* a, double* b) { return packed_op(c, a, b, PK_DXDY, 0.0); }
+int fsibe_poisson(fsibe_ctx* c, const double* a, double* b) { return packed_op(c, a, b, PK_POISSON, 0.0); }
+int fsibe_vis(fsibe_ctx* c, double dt, double* w) { return packed_op(c, nullptr, w, PK_VIS, dt); }
+int fsibe_dealiase_mask(fsibe_ctx* c, double* d) { return packed_op(c, nullptr, d, PK_DEALIAS, 0.0); }
+
+// ---- the time step ------------------------------------------------------------------
+int fsibe_init_fields(fsibe_ctx* c, const double* vort) {
+    if (!c || !vort) return FSIBE_ERR_PARAM;
+    const size_t NN = (size_t)c->g.nx * c->g.ny;
+    const size_t rs = c->fp32 ? 4 : 8;
+    free_graph(c);
+    int st = from_host(c, vort, NN, c->phys[PH_0]);
+    if (st) return st;
+    for (int q : {SP_W, SP_M, SP_WLO}) CK(c, cudaMemsetAsync(c->spec[q], 0, rs * NN, c->stream));
+    for (int q : {PH_VORMEAN, PH_PRESS, PH_SA, PH_SB}) CK(c, cudaMemsetAsync(c->phys[q], 0, rs * NN, c->stream));
+    st = c->fp32 ? fwd2d<float>(c, c->spec[SP_W]) : fwd2d<double>(c, c->spec[SP_W]);
+    if (st) return st;
+    DevScalars h;
+    std::memset(&h, 0, sizeof(h));
+    h.startup_step = 1;
+    h.method = c->P.time_method_solid;
+    h.grav = c->P.grav;
+    c->U_mean_true = 1.0;
+    h.mean_u_next = c->U_mean_true * host_mean(c->P, 0.0, true);
+    h.mean_v_next = c->U_mean_true * host_mean(c->P, 0.0, false);
+    CK(c, cudaMemcpyAsync(c->S, &h, sizeof(h), cudaMemcpyHostToDevice, c->stream));
+    launch_init_beam(beam_args(c), c->stream);
+    CKL(c);
+    st = c->fp32 ? init_velocity<float>(c) : init_velocity<double>(c);
+    if (st) return st;
+    st = create_mask(c);
+    if (st) return st;
+    CK(c, cudaStreamSynchronize(c->stream));
+    c->initialized = true;
+    c->startup_done = false;
+    return FSIBE_OK;
+}
+
+int fsibe_create_mask(fsibe_ctx* c, double time) {
+    if (!c) return FSIBE_ERR_PARAM;
+    (void)time;  // mouvement case 0 does not depend on time
+    int st = create_mask(c);
+    if (st) return st;
+    CK(c, cudaStreamSynchronize(c->stream));
+    return FSIBE_OK;
+}
+
+static int read_status(fsibe_ctx* c) {
+    int32_t s = 0;
+    CK(c, cudaMemcpyAsync(&s, &c->S->status, 4, cudaMemcpyDeviceToHost, c->stream));
+    CK(c, cudaStreamSynchronize(c->stream));
+    if (s) c->err = fsibe_strerror(s);
+    return s;
+}
+
+int fsibe_fluid_step(fsibe_ctx* c, int explicit_step) {
+    if (!c) return FSIBE_ERR_PARAM;
+    if (!c->initialized) return FSIBE_ERR_STATE;
+    int st = fluid_step(c, explicit_step ? 1 : 0);
+    if (st) return st;
+    return read_status(c);
+}
+
+static int set_time(fsibe_ctx* c, double time) {
+    CK(c, cudaMemcpyAsync(&c->S->time, &time, 8, cudaMemcpyHostToDevice, c->stream));
+    return FSIBE_OK;
+}
+
+int fsibe_get_forces(fsibe_ctx* c, double time) {
+    if (!c) return FSIBE_ERR_PARAM;
+    int st = set_time(c, time);
+    if (st) return st;
+    st = get_forces(c);
+    if (st) return st;
+    return read_status(c);
+}
+
+int fsibe_solid_step(fsibe_ctx* c, double time) {
+    if (!c) return FSIBE_ERR_PARAM;
+    int st = set_time(c, time);
+    if (st) return st;
+    st = solid_step(c);
+    if (st) return st;
+    return read_status(c);
+}
+
+int fsibe_advance(fsibe_ctx* c) {
+    if (!c) return FSIBE_ERR_PARAM;
+    int st = advance(c);
+    if (st) return st;
+    if (!c->startup_done) c->startup_done = true;
+    return read_status(c);
+}
+
+int fsibe_step(fsibe_ctx* c) {
+    if (!c) return FSIBE_ERR_PARAM;
+    return do_step(c);
+}
+
+int fsibe_run(fsibe_ctx* c, int nsteps, double* rows) {
+    if (!c || nsteps < 0) return FSIBE_ERR_PARAM;
+    if (rows) {
+        if (c->rows_cap < nsteps) {
+            if (c->rows) cudaFree(c->rows);
+            c->rows = nullptr;
+            CK(c, cudaMalloc((void**)&c->rows, 8 * 21 * (size_t)(nsteps > 0 ? nsteps : 1)));
+            c->rows_cap = nsteps;
+            free_graph(c);  // the graph captured the old ring pointer
+        }
+        int32_t z[2] = {0, nsteps};
+        CK(c, cudaMemcpyAsync(&c->S->run_row, z, 8, cudaMemcpyHostToDevice, c->stream));
+    } else {
+        int32_t z[2] = {0, 0};
+        CK(c, cudaMemcpyAsync(&c->S->run_row, z, 8, cudaMemcpyHostToDevice, c->stream));
+    }
+    for (int s = 0; s < nsteps; ++s) {
+        int st = do_step(c);
+        if (st) return st;
+    }
+    if (rows && nsteps > 0) CK(c, cudaMemcpyAsync(rows, c->rows, 8 * 21 * (size_t)nsteps, cudaMemcpyDeviceToHost, c->stream));
+    return read_status(c);
+}
+
+// ---- state transfer -------------------------------------------------------------------
+int fsibe_upload_vortk(fsibe_ctx* c, const double* v) { return c ? packed_to_spec(c, v, c->spec[SP_W]) : FSIBE_ERR_PARAM; }
+int fsibe_download_vortk(fsibe_ctx* c, double* v) { return c ? spec_to_packed(c, c->spec[SP_W], v) : FSIBE_ERR_PARAM; }
+int fsibe_download_vort(fsibe_ctx* c, double* v) {
+    if (!c) return FSIBE_ERR_PARAM;
+    int st;
+    if (c->fp32) {
+        if ((st = inv_y<float>(c, c->spec[SP_W], c->spec[SP_0], OP_ID))) return st;
+        if ((st = inv_x<float>(c))) return st;
+    } else {
+        if ((st = inv_y<double>(c, c->spec[SP_W], c->spec[SP_0], OP_ID))) return st;
+        if ((st = inv_x<double>(c))) return st;
+    }
+    return to_host(c, c->phys[PH_0], (size_t)c->g.nx * c->g.ny, v);
+}
+int fsibe_upload_u(fsibe_ctx* c, const double* u) {
+    if (!c) return FSIBE_ERR_PARAM;
+    const size_t NN = (size_t)c->g.nx * c->g.ny;
+    int st = from_host(c, u, NN, c->phys[PH_U]);
+    return st ? st : from_host(c, u + NN, NN, c->phys[PH_V]);
+}
+int fsibe_download_u(fsibe_ctx* c, double* u) {
+    if (!c) return FSIBE_ERR_PARAM;
+    const size_t NN = (size_t)c->g.nx * c->g.ny;
+    int st = to_host(c, c->phys[PH_U], NN, u);
+    return st ? st : to_host(c, c->phys[PH_V], NN, u + NN);
+}
+int fsibe_download_press(fsibe_ctx* c, double* p) { return c ? to_host(c, c->phys[PH_PRESS], (size_t)c->g.nx * c->g.ny, p) : FSIBE_ERR_PARAM; }
+int fsibe_upload_press(fsibe_ctx* c, const double* p) { return c ? from_host(c, p, (size_t)c->g.nx * c->g.ny, c->phys[PH_PRESS]) : FSIBE_ERR_PARAM; }
+int fsibe_download_vor_mean(fsibe_ctx* c, double* p) { return c ? to_host(c, c->phys[PH_VORMEAN], (size_t)c->g.nx * c->g.ny, p) : FSIBE_ERR_PARAM; }
+int fsibe_upload_mask(fsibe_ctx* c, const double* m, const double* vx, const double* vy) {
+    if (!c) return FSIBE_ERR_PARAM;
+    const size_t NN = (size_t)c->g.nx * c->g.ny;
+    int st = from_host(c, m, NN, c->phys[PH_MASK]);
+    if (!st) st = from_host(c, vx, NN, c->phys[PH_MVX]);
+    if (!st) st = from_host(c, vy, NN, c->phys[PH_MVY]);
+    return st;
+}
+int fsibe_download_mask(fsibe_ctx* c, double* m, double* vx, double* vy) {
+    if (!c) return FSIBE_ERR_PARAM;
+    const size_t NN = (size_t)c->g.nx * c->g.ny;
+    int st = to_host(c, c->phys[PH_MASK], NN, m);
+    if (!st) st = to_host(c, c->phys[PH_MVX], NN, vx);
+    if (!st) st = to_host(c, c->phys[PH_MVY], NN, vy);
+    return st;
+}
+int fsibe_upload_beam(fsibe_ctx* c, const double* beam, const double* po, const double* pn, const double* to,
+                      const double* tn) {
+    if (!c) return FSIBE_ERR_PARAM;
+    const size_t ns = (size_t)c->P.ns;
+    if (beam) for (int q = 0; q < 6; ++q) CK(c, cudaMemcpyAsync(c->beam[q == 4 ? B_TH : (q == 5 ? B_THD : q)], beam + q * ns, 8 * ns, cudaMemcpyHostToDevice, c->stream));
+    if (po) CK(c, cudaMemcpyAsync(c->beam[B_PO], po, 8 * ns, cudaMemcpyHostToDevice, c->stream));
+    if (pn) CK(c, cudaMemcpyAsync(c->beam[B_PN], pn, 8 * ns, cudaMemcpyHostToDevice, c->stream));
+    if (to) CK(c, cudaMemcpyAsync(c->beam[B_TO], to, 8 * ns, cudaMemcpyHostToDevice, c->stream));
+    if (tn) CK(c, cudaMemcpyAsync(c->beam[B_TN], tn, 8 * ns, cudaMemcpyHostToDevice, c->stream));
+    CK(c, cudaStreamSynchronize(c->stream));
+    return FSIBE_OK;
+}
+int fsibe_download_beam(fsibe_ctx* c, double* beam, double* po, double* pn, double* to, double* tn) {
+    if (!c) return FSIBE_ERR_PARAM;
+    const size_t ns = (size_t)c->P.ns;
+    if (beam) for (int q = 0; q < 6; ++q) CK(c, cudaMemcpyAsync(beam + q * ns, c->beam[q == 4 ? B_TH : (q == 5 ? B_THD : q)], 8 * ns, cudaMemcpyDeviceToHost, c->stream));
+    if (po) CK(c, cudaMemcpyAsync(po, c->beam[B_PO], 8 * ns, cudaMemcpyDeviceToHost, c->stream));
+    if (pn) CK(c, cudaMemcpyAsync(pn, c->beam[B_PN], 8 * ns, cudaMemcpyDeviceToHost, c->stream));
+    if (to) CK(c, cudaMemcpyAsync(to, c->beam[B_TO], 8 * ns, cudaMemcpyDeviceToHost, c->stream));
+    if (tn) CK(c, cudaMemcpyAsync(tn, c->beam[B_TN], 8 * ns, cudaMemcpyDeviceToHost, c->stream));
+    CK(c, cudaStreamSynchronize(c->stream));
+    return FSIBE_OK;
+}
+
+int fsibe_get_scalars(fsibe_ctx* c, fsibe_scalars* o) {
+    if (!c || !o) return FSIBE_ERR_PARAM;
+    DevScalars h;
+    CK(c, cudaMemcpyAsync(&h, c->S, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+    CK(c, cudaStreamSynchronize(c->stream));
+    std::memset(o, 0, sizeof(*o));
+    o->time = h.time; o->dt0 = h.dt0; o->dt1 = h.dt1;
+    o->u_max = h.u_max; o->mean_ux = h.mean_ux; o->mean_uy = h.mean_uy;
+    o->vor_rms = h.vor_rms; o->kinetic = h.kinetic; o->dissipation = h.dissipation;
+    o->porous_diss = h.porous_diss; o->inflow_solid = h.inflow_solid; o->inflow_mean = h.inflow_mean;
+    for (int q = 0; q < 2; ++q) {
+        o->force[q] = h.force[q]; o->force_unst[q] = h.force_unst[q];
+        o->force_press[q] = h.force_press[q]; o->inertial_force[q] = h.inertial_force[q];
+    }
+    o->e_kinetic = h.e_kinetic; o->e_elastic = h.e_elastic; o->e_pot = h.e_pot;
+    for (int q = 0; q < 21; ++q) o->beam_data[q] = h.row[q];
+    o->newton_iters = h.newton_iters;
+    o->status = h.status;
+    o->step = h.step;
+    return FSIBE_OK;
+}
+
+int fsibe_time_steps(fsibe_ctx* c, int nsteps, float* ms) {
+    if (!c || !ms) return FSIBE_ERR_PARAM;
+    CK(c, cudaEventRecord(c->ev0, c->stream));
+    for (int s = 0; s < nsteps; ++s) {
+        int st = do_step(c);
+        if (st) return st;
+    }
+    CK(c, cudaEventRecord(c->ev1, c->stream));
+    CK(c, cudaEventSynchronize(c->ev1));
+    CK(c, cudaEventElapsedTime(ms, c->ev0, c->ev1));
+    return read_status(c);
+}
+
+int fsibe_launches_per_step(fsibe_ctx* c, int* n) {
+    if (!c || !n) return FSIBE_ERR_PARAM;
+    const fsibe_params& P = c->P;
+    int k = 6;  // step_begin, nl_x, nl_y, press_x, fluid_finish, advance
+    if (P.iFLUSI == 1 || P.iSaveBeam > 0) k += 2 + 1;  // press_y, press_fin, forces
+    if ((P.iFLUSI == 1 || P.iMotion > 0) && P.iBeam > 0) k += 2;  // mask prep + raster
+    if (P.iFLUSI == 1) k += 1;  // beam
+    *n = k;
+    return FSIBE_OK;
+}
+
+}  // extern "C"

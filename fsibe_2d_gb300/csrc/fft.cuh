@@ -1,0 +1,178 @@
+// fft.cuh -- block-level Stockham FFT engine for power-of-two lengths.
+//
+// A length-N complex sequence lives in shared memory (padded with pad8) and is transformed
+// in place by a group of G = N/8 threads.  Each stage is a radix-8 Stockham pass (radix 4
+// or 2 for the last stage when log2 N is not a multiple of 3): every thread loads its
+// butterfly inputs into registers, the block synchronises, and the outputs are written to
+// their autosorted positions.  Twiddles come from a table W_N^m = exp(-2 pi i m/N) computed
+// on the host in long double and rounded once to the storage type.
+//
+// Forward = exp(-i..), inverse = exp(+i..), both unnormalised (like FFTW).
+#pragma once
+#include "common.cuh"
+
+namespace fsibe {
+
+template <typename R, bool INV>
+__device__ __forceinline__ void dft2(C2<R>* v) {
+    C2<R> a = v[0];
+    v[0] = cadd<R>(a, v[1]);
+    v[1] = csub<R>(a, v[1]);
+}
+
+template <typename R, bool INV>
+__device__ __forceinline__ void dft4(C2<R>* v) {
+    C2<R> a = cadd<R>(v[0], v[2]), b = csub<R>(v[0], v[2]);
+    C2<R> c = cadd<R>(v[1], v[3]), d = csub<R>(v[1], v[3]);
+    C2<R> sd = INV ? mk<R>(-d.y, d.x) : mk<R>(d.y, -d.x);  // (+-i) * d
+    v[0] = cadd<R>(a, c);
+    v[2] = csub<R>(a, c);
+    v[1] = cadd<R>(b, sd);
+    v[3] = csub<R>(b, sd);
+}
+
+template <typename R, bool INV>
+__device__ __forceinline__ void dft8(C2<R>* v) {
+    const R h = (R)0.70710678118654752440084436210485;
+    C2<R> e[4], o[4];
+    e[0] = cadd<R>(v[0], v[4]); o[0] = csub<R>(v[0], v[4]);
+    e[1] = cadd<R>(v[1], v[5]); C2<R> t1 = csub<R>(v[1], v[5]);
+    e[2] = cadd<R>(v[2], v[6]); C2<R> t2 = csub<R>(v[2], v[6]);
+    e[3] = cadd<R>(v[3], v[7]); C2<R> t3 = csub<R>(v[3], v[7]);
+    if (!INV) {
+        o[1] = mk<R>((t1.x + t1.y) * h, (t1.y - t1.x) * h);    // * (1-i)/sqrt2
+        o[2] = mk<R>(t2.y, -t2.x);                              // * -i
+        o[3] = mk<R>((t3.y - t3.x) * h, -(t3.x + t3.y) * h);   // * (-1-i)/sqrt2
+    } else {
+        o[1] = mk<R>((t1.x - t1.y) * h, (t1.x + t1.y) * h);    // * (1+i)/sqrt2
+        o[2] = mk<R>(-t2.y, t2.x);                              // * +i
+        o[3] = mk<R>(-(t3.x + t3.y) * h, (t3.x - t3.y) * h);   // * (-1+i)/sqrt2
+    }
+    dft4<R, INV>(e);
+    dft4<R, INV>(o);
+    v[0] = e[0]; v[2] = e[1]; v[4] = e[2]; v[6] = e[3];
+    v[1] = o[0]; v[3] = o[1]; v[5] = o[2]; v[7] = o[3];
+}
+
+template <typename R, int P, bool INV>
+__device__ __forceinline__ void dftp(C2<R>* v) {
+    if constexpr (P == 8) dft8<R, INV>(v);
+    else if constexpr (P == 4) dft4<R, INV>(v);
+    else dft2<R, INV>(v);
+}
+
+// One Stockham stage of radix P; NS = product of the radices already applied.
+template <typename R, int N, int P, int NS, bool INV>
+__device__ __forceinline__ void fft_stage(C2<R>* buf, const C2<R>* __restrict__ tw, int t) {
+    constexpr int G = N / 8, B = N / P, PER = 8 / P;
+    C2<R> v[8];
+#pragma unroll
+    for (int q = 0; q < PER; ++q) {
+        const int j = t + q * G;
+#pragma unroll
+        for (int r = 0; r < P; ++r) v[q * P + r] = buf[pad8(j + r * B)];
+    }
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < PER; ++q) {
+        const int j = t + q * G;
+        const int k = j & (NS - 1);
+        if constexpr (NS > 1) {
+#pragma unroll
+            for (int r = 1; r < P; ++r) {
+                C2<R> w = __ldg(&tw[r * k * (N / (NS * P))]);
+                if (INV) w.y = -w.y;
+                v[q * P + r] = cmul<R>(v[q * P + r], w);
+            }
+        }
+        dftp<R, P, INV>(v + q * P);
+        const int base = (j - k) * P + k;
+#pragma unroll
+        for (int r = 0; r < P; ++r) buf[pad8(base + r * NS)] = v[q * P + r];
+    }
+    __syncthreads();
+}
+
+template <typename R, int N, bool INV, int NS = 1>
+__device__ __forceinline__ void fft_run(C2<R>* buf, const C2<R>* __restrict__ tw, int t) {
+    if constexpr (NS * 8 <= N) {
+        fft_stage<R, N, 8, NS, INV>(buf, tw, t);
+        fft_run<R, N, INV, NS * 8>(buf, tw, t);
+    } else if constexpr (NS * 4 == N) {
+        fft_stage<R, N, 4, NS, INV>(buf, tw, t);
+    } else if constexpr (NS * 2 == N) {
+        fft_stage<R, N, 2, NS, INV>(buf, tw, t);
+    }
+}
+
+// In-place transform of buf (padded, natural order). All threads of the block must call it;
+// the caller synchronises before (data written by other threads) -- the routine ends synced.
+template <typename R, int N, bool INV>
+__device__ __forceinline__ void block_fft(C2<R>* buf, const C2<R>* __restrict__ tw, int t) {
+    static_assert(N >= 16 && (N & (N - 1)) == 0, "power-of-two length >= 16");
+    fft_run<R, N, INV>(buf, tw, t);
+}
+
+// ---- real <-> half-length complex split steps (x direction) -------------------------------
+// A real row x[0..2H) is handled as z[m] = x[2m] + i x[2m+1], m < H, transformed with a
+// length-H complex FFT.  twr[k] = exp(-2 pi i k / 2H), k <= H.
+
+// After the forward length-H FFT of z (in buf): X[k], k in [0,H), in place.  The Nyquist bin
+// X[H] is dropped (the reference's filtering).  Pairs (k, H-k) handled by the same thread.
+template <typename R, int H>
+__device__ __forceinline__ void r2c_split(C2<R>* buf, const C2<R>* __restrict__ twr, int t) {
+    constexpr int G = H / 8;
+    // pairs k = 1 .. H/2-1, plus k = 0 and k = H/2 handled by thread 0
+    for (int k = 1 + t; k < H / 2; k += G) {
+        const C2<R> zk = buf[pad8(k)], zm = buf[pad8(H - k)];
+        const C2<R> wk = __ldg(&twr[k]), wm = __ldg(&twr[H - k]);
+        // X[k] = 1/2 (zk + conj zm) + w^k (zk - conj zm)/(2i)
+        C2<R> e = mk<R>((R)0.5 * (zk.x + zm.x), (R)0.5 * (zk.y - zm.y));
+        C2<R> d = mk<R>(zk.x - zm.x, zk.y + zm.y);           // zk - conj zm
+        C2<R> o = mk<R>((R)0.5 * d.y, (R)-0.5 * d.x);         // d / (2i)
+        C2<R> Xk = cadd<R>(e, cmul<R>(wk, o));
+        // X[H-k] = 1/2 (zm + conj zk) + w^(H-k) (zm - conj zk)/(2i)
+        C2<R> e2 = mk<R>((R)0.5 * (zm.x + zk.x), (R)0.5 * (zm.y - zk.y));
+        C2<R> d2 = mk<R>(zm.x - zk.x, zm.y + zk.y);
+        C2<R> o2 = mk<R>((R)0.5 * d2.y, (R)-0.5 * d2.x);
+        C2<R> Xm = cadd<R>(e2, cmul<R>(wm, o2));
+        buf[pad8(k)] = Xk;
+        buf[pad8(H - k)] = Xm;
+    }
+    if (t == 0) {
+        C2<R> z0 = buf[pad8(0)];
+        buf[pad8(0)] = mk<R>(z0.x + z0.y, (R)0);
+        C2<R> zh = buf[pad8(H / 2)];
+        buf[pad8(H / 2)] = mk<R>(zh.x, -zh.y);
+    }
+    __syncthreads();
+}
+
+// Before the inverse length-H FFT: X[k], k in [0,H) (X[H] = 0, Im X[0] ignored) -> Z'[k] so
+// that z = IFFT_H(Z') gives x[2m] = Re z[m], x[2m+1] = Im z[m] (unnormalised c2r).
+template <typename R, int H>
+__device__ __forceinline__ void c2r_merge(C2<R>* buf, const C2<R>* __restrict__ twr, int t) {
+    constexpr int G = H / 8;
+    for (int k = 1 + t; k < H / 2; k += G) {
+        const C2<R> xk = buf[pad8(k)], xm = buf[pad8(H - k)];
+        const C2<R> wk = __ldg(&twr[k]), wm = __ldg(&twr[H - k]);
+        // Z'[k] = (xk + conj xm) + i (xk - conj xm) conj(w^k)
+        C2<R> e = mk<R>(xk.x + xm.x, xk.y - xm.y);
+        C2<R> o = cmul<R>(mk<R>(xk.x - xm.x, xk.y + xm.y), mk<R>(wk.x, -wk.y));
+        C2<R> Zk = mk<R>(e.x - o.y, e.y + o.x);
+        C2<R> e2 = mk<R>(xm.x + xk.x, xm.y - xk.y);
+        C2<R> o2 = cmul<R>(mk<R>(xm.x - xk.x, xm.y + xk.y), mk<R>(wm.x, -wm.y));
+        C2<R> Zm = mk<R>(e2.x - o2.y, e2.y + o2.x);
+        buf[pad8(k)] = Zk;
+        buf[pad8(H - k)] = Zm;
+    }
+    if (t == 0) {
+        C2<R> x0 = buf[pad8(0)];
+        buf[pad8(0)] = mk<R>(x0.x, x0.x);
+        C2<R> xh = buf[pad8(H / 2)];
+        buf[pad8(H / 2)] = mk<R>((R)2 * xh.x, (R)-2 * xh.y);
+    }
+    __syncthreads();
+}
+
+}  // namespace fsibe

@@ -1,0 +1,662 @@
+// fluid.cuh -- fused pseudo-spectral kernels of the vorticity step (templates).
+//
+// x pass ("X" kernels): a block owns TR physical rows; each row is a length-H=nx/2 complex
+//   FFT (real-to-complex split) done by G = H/8 threads.  Spectral intermediates are read /
+//   written transposed, T[kx][iy], through shared memory, so both sides stay coalesced.
+// y pass ("Y" kernels): a block owns one kx row of ny complex values (contiguous), does the
+//   y FFTs and all pointwise spectral work for that row.
+//
+// Kernel map onto the reference (NavierStokes.f90):
+//   k_nl_x     cal_nlk :40-52 and :88-132  inverse-x of dw/dx, dw/dy; -u.grad(w); the
+//              penalization -chi(u-us); forward-x of all three; A = X(w) + i kx X(pen_y),
+//              B = X(pen_x)
+//   k_nl_y     cal_nlk's forward-y + curl (:169-173), EvolveFluidAB2/Explicit (:478-498, :446-450)
+//              with vis (cal_vis.f90) and dealiasing, then the inverse-y transforms
+//              that cal_velocity (:194-202), pressure (:331), GetForces' stresses
+//              (BeamForces.f90:105-124) and the next cal_nlk (:40-44) need.
+//   k_press_x  pressure :305-338 and :354-370: velocity at n+1 (+ mean flow), penalty term,
+//              drag window sums, energies, time_avg_vort, the Poisson right-hand side and its
+//              forward-x transform; viscous stresses to physical space.
+//   k_press_y  pressure :366-383: forward-y, divergence, poisson, inverse-y
+//   k_press_fin pressure :383-392: inverse-x, p = q - |u|^2/2
+#pragma once
+#include "fft.cuh"
+
+namespace fsibe {
+
+template <typename R>
+struct KArgs {
+    Geometry g;
+    double nu, eps;
+    // physical fields R[ny][nx]
+    R *u, *v, *mask, *mvx, *mvy, *vor_mean, *press, *sa, *sb, *phys0;
+    // half spectra C2<R>[hx][ny]
+    C2<R> *W, *M, *Wlo, *A, *B, *Tu, *Tv, *Tw, *Tsa, *Tsb, *Tdx, *Tdy, *P1, *P2, *Tq, *spec0, *spec1;
+    const C2<R> *twX, *twR, *twY;
+    DevScalars* S;
+    double* red;
+    int viscous, pressure_on, penalize, op;
+};
+
+// Operators the generic inverse-y kernel applies before the transform.
+enum SpecOp { OP_ID = 0, OP_DX = 1, OP_DY = 2, OP_U = 3, OP_V = 4 };
+
+__device__ __forceinline__ int signed_k(int k, int n) { return (k <= n / 2) ? k : k - n; }
+
+template <typename R, int H>
+struct XRows {
+    static constexpr int G = H / 8;
+    // rows per block: keep the transposed chunks >= 32 bytes while bounding shared memory
+    static constexpr int TR0 = (sizeof(R) == 8) ? (H <= 512 ? 4 : 2) : (H <= 256 ? 8 : (H <= 1024 ? 4 : 2));
+    // at least one full warp per block (the block reductions use full-warp shuffles)
+    static constexpr int TR = (G * TR0 >= 32) ? TR0 : 32 / G;
+    static constexpr int PL = padded_len(H) + 1;  // row stride (complex) in shared memory
+    static constexpr int THREADS = G * TR;
+};
+
+// ---- x-pass helpers -------------------------------------------------------------------
+template <typename R, int H, int TR, int PL>
+__device__ __forceinline__ void load_tileT(C2<R>* buf, const C2<R>* __restrict__ T, int ny, int iy0) {
+    for (int i = threadIdx.x; i < H * TR; i += blockDim.x) {
+        const int r = i % TR, kx = i / TR;
+        buf[r * PL + pad8(kx)] = T[(size_t)kx * ny + iy0 + r];
+    }
+}
+
+// inverse x transform of one row buffer (after load + __syncthreads)
+template <typename R, int H>
+__device__ __forceinline__ void row_c2r(C2<R>* rb, const C2<R>* __restrict__ twR, const C2<R>* __restrict__ twX, int t) {
+    c2r_merge<R, H>(rb, twR, t);
+    block_fft<R, H, true>(rb, twX, t);
+}
+
+template <typename R, int H>
+__device__ __forceinline__ void row_r2c(C2<R>* rb, const C2<R>* __restrict__ twR, const C2<R>* __restrict__ twX, int t) {
+    block_fft<R, H, false>(rb, twX, t);
+    r2c_split<R, H>(rb, twR, t);
+}
+
+template <typename R>
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+__device__ __forceinline__ double warp_max(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
+// ======================================================================================
+// Generic transforms (used by the ABI's coftxy/cofitxy and by the start-up path)
+// ======================================================================================
+
+// real field (phys0) -> T (spec0): forward x
+template <typename R, int H>
+__global__ void __launch_bounds__(XRows<R, H>::THREADS) k_xfwd(KArgs<R> a) {
+    using X = XRows<R, H>;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    C2<R>* buf = reinterpret_cast<C2<R>*>(smem_raw);
+    const int r = threadIdx.x / X::G, t = threadIdx.x % X::G;
+    const int iy0 = blockIdx.x * X::TR, ny = a.g.ny;
+    C2<R>* rb = buf + r * X::PL;
+    const C2<R>* f2 = reinterpret_cast<const C2<R>*>(a.phys0) + (size_t)(iy0 + r) * H;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) rb[pad8(t + q * X::G)] = f2[t + q * X::G];
+    __syncthreads();
+    row_r2c<R, H>(rb, a.twR, a.twX, t);
+    for (int i = threadIdx.x; i < H * X::TR; i += blockDim.x) {
+        const int rr = i % X::TR, kx = i / X::TR;
+        a.spec0[(size_t)kx * ny + iy0 + rr] = buf[rr * X::PL + pad8(kx)];
+    }
+}
+
+// T (spec0) -> real field (phys0): inverse x (unnormalised)
+template <typename R, int H>
+__global__ void __launch_bounds__(XRows<R, H>::THREADS) k_xinv(KArgs<R> a) {
+    using X = XRows<R, H>;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    C2<R>* buf = reinterpret_cast<C2<R>*>(smem_raw);
+    const int r = threadIdx.x / X::G, t = threadIdx.x % X::G;
+    const int iy0 = blockIdx.x * X::TR, ny = a.g.ny;
+    C2<R>* rb = buf + r * X::PL;
+    load_tileT<R, H, X::TR, X::PL>(buf, a.spec0, ny, iy0);
+    __syncthreads();
+    row_c2r<R, H>(rb, a.twR, a.twX, t);
+    C2<R>* f2 = reinterpret_cast<C2<R>*>(a.phys0) + (size_t)(iy0 + r) * H;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) f2[t + q * X::G] = rb[pad8(t + q * X::G)];
+}
+
+// forward y of spec0 (T) -> spec1 (S), scaled by 1/(nx ny), ky = ny/2 zeroed
+template <typename R, int NY>
+__global__ void __launch_bounds__(NY / 8) k_yfwd(KArgs<R> a) {
+    constexpr int G = NY / 8;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    C2<R>* buf = reinterpret_cast<C2<R>*>(smem_raw);
+    const int kx = blockIdx.x, t = threadIdx.x;
+    const C2<R>* in = a.spec0 + (size_t)kx * NY;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) buf[pad8(t + q * G)] = in[t + q * G];
+    __syncthreads();
+    block_fft<R, NY, false>(buf, a.twY, t);
+    const R norm = (R)(1.0 / ((double)a.g.nx * (double)a.g.ny));
+    C2<R>* out = a.spec1 + (size_t)kx * NY;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+        const int ky = t + q * G;
+        C2<R> z = buf[pad8(ky)];
+        out[ky] = (ky == NY / 2) ? mk<R>(0, 0) : cscale<R>(z, norm);
+    }
+}
+
+// inverse y of op(spec1) -> spec0 (T)
+template <typename R, int NY>
+__global__ void __launch_bounds__(NY / 8) k_yinv(KArgs<R> a) {
+    constexpr int G = NY / 8;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    C2<R>* buf = reinterpret_cast<C2<R>*>(smem_raw);
+    const int kx = blockIdx.x, t = threadIdx.x;
+    const C2<R>* in = a.spec1 + (size_t)kx * NY;
+    const Geometry& g = a.g;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+        const int ky = t + q * G;
+        const int ks = signed_k(ky, NY);
+        C2<R> s = in[ky];
+        C2<R> o = s;
+        if (a.op != OP_ID) {
+            const double k2 = (double)(kx * kx) * g.scalex + (double)(ks * ks) * g.scaley;
+            const R kxs = (R)((double)kx * g.kxs), kys = (R)((double)ks * g.kys);
+            if (a.op == OP_DX) o = cimul<R>(s, kxs);
+            else if (a.op == OP_DY) o = cimul<R>(s, kys);
+            else {
+                C2<R> psi = (kx == 0 && ky == 0) ? mk<R>(0, 0) : cscale<R>(s, (R)(1.0 / k2));
+                o = (a.op == OP_U) ? cimul<R>(psi, kys) : cimul<R>(psi, kxs);
+            }
+        }
+        if (ky == NY / 2) o = mk<R>(0, 0);
+        buf[pad8(ky)] = o;
+    }
+    __syncthreads();
+    block_fft<R, NY, true>(buf, a.twY, t);
+    C2<R>* out = a.spec0 + (size_t)kx * NY;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) out[t + q * G] = buf[pad8(t + q * G)];
+}
+
+// ======================================================================================
+// Start-up velocity: from Tu, Tv (inverse-y done) to u, v at `time` (cal_velocity) plus the
+// statistics cal_nlk needs (max |u|^2, mean u, mean v).
+// ======================================================================================
+template <typename R, int H>
+__global__ void __launch_bounds__(XRows<R, H>::THREADS) k_vel_x(KArgs<R> a) {
+    using X = XRows<R, H>;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    C2<R>* bufA = reinterpret_cast<C2<R>*>(smem_raw);
+    C2<R>* bufB = bufA + X::TR * X::PL;
+    __shared__ double red_s[3][X::THREADS / 32];
+    const int r = threadIdx.x / X::G, t = threadIdx.x % X::G;
+    const int iy0 = blockIdx.x * X::TR, ny = a.g.ny;
+    load_tileT<R, H, X::TR, X::PL>(bufA, a.Tu, ny, iy0);
+    load_tileT<R, H, X::TR, X::PL>(bufB, a.Tv, ny, iy0);
+    __syncthreads();
+    row_c2r<R, H>(bufA + r * X::PL, a.twR, a.twX, t);
+    row_c2r<R, H>(bufB + r * X::PL, a.twR, a.twX, t);
+    const R U = (R)a.S->mean_u_next, V = (R)a.S->mean_v_next;
+    const int iy = iy0 + r;
+    C2<R>* u2 = reinterpret_cast<C2<R>*>(a.u) + (size_t)iy * H;
+    C2<R>* v2 = reinterpret_cast<C2<R>*>(a.v) + (size_t)iy * H;
+    double mx = 0.0, su = 0.0, sv = 0.0;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+        const int m = t + q * X::G;
+        C2<R> ur = bufA[r * X::PL + pad8(m)], vr = bufB[r * X::PL + pad8(m)];
+        C2<R> uu = mk<R>(ur.x + U, ur.y + U);
+        C2<R> vv = mk<R>(-vr.x + V, -vr.y + V);
+        u2[m] = uu;
+        v2[m] = vv;
+        mx = fmax(mx, fmax((double)(uu.x * uu.x + vv.x * vv.x), (double)(uu.y * uu.y + vv.y * vv.y)));
+        su += (double)uu.x + (double)uu.y;
+        sv += (double)vv.x + (double)vv.y;
+    }
+    mx = warp_max(mx);
+    su = warp_sum<R>(su);
+    sv = warp_sum<R>(sv);
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    if (l == 0) { red_s[0][w] = mx; red_s[1][w] = su; red_s[2][w] = sv; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double m0 = 0.0, s0 = 0.0, s1 = 0.0;
+        for (int i = 0; i < X::THREADS / 32; ++i) { m0 = fmax(m0, red_s[0][i]); s0 += red_s[1][i]; s1 += red_s[2][i]; }
+        double* out = a.red + (size_t)blockIdx.x * RED_NSLOTS;
+        for (int s = 0; s < RED_NSLOTS; ++s) out[s] = 0.0;
+        out[RED_UMAX2] = m0;
+        out[RED_SUM_U] = s0;
+        out[RED_SUM_V] = s1;
+    }
+}
+
+// ======================================================================================
+// K2: nonlinear term and penalization in physical space (cal_nlk)
+// ======================================================================================
+template <typename R, int H>
+__global__ void __launch_bounds__(XRows<R, H>::THREADS) k_nl_x(KArgs<R> a) {
+    using X = XRows<R, H>;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    C2<R>* bufA = reinterpret_cast<C2<R>*>(smem_raw);
+    C2<R>* bufB = bufA + X::TR * X::PL;
+    const int r = threadIdx.x / X::G, t = threadIdx.x % X::G;
+    const int iy0 = blockIdx.x * X::TR, ny = a.g.ny;
+    C2<R>* ra = bufA + r * X::PL;
+    C2<R>* rb = bufB + r * X::PL;
+    load_tileT<R, H, X::TR, X::PL>(bufA, a.Tdx, ny, iy0);
+    load_tileT<R, H, X::TR, X::PL>(bufB, a.Tdy, ny, iy0);
+    __syncthreads();
+    row_c2r<R, H>(ra, a.twR, a.twX, t);
+    row_c2r<R, H>(rb, a.twR, a.twX, t);
+    const int iy = iy0 + r;
+    const size_t roff = (size_t)iy * H;
+    const C2<R>* u2 = reinterpret_cast<const C2<R>*>(a.u) + roff;
+    const C2<R>* v2 = reinterpret_cast<const C2<R>*>(a.v) + roff;
+    const C2<R>* k2 = reinterpret_cast<const C2<R>*>(a.mask) + roff;
+    const C2<R>* x2 = reinterpret_cast<const C2<R>*>(a.mvx) + roff;
+    const C2<R>* y2 = reinterpret_cast<const C2<R>*>(a.mvy) + roff;
+    C2<R> wv[8], pyv[8], pxv[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+        const int m = t + q * X::G;
+        const C2<R> dx = ra[pad8(m)], dy = rb[pad8(m)];
+        const C2<R> uu = u2[m], vv = v2[m];
+        wv[q] = mk<R>(-uu.x * dx.x - vv.x * dy.x, -uu.y * dx.y - vv.y * dy.y);
+        if (a.penalize) {
+            const C2<R> kk = k2[m], mx = x2[m], my = y2[m];
+            pxv[q] = mk<R>(-kk.x * (uu.x - mx.x), -kk.y * (uu.y - mx.y));
+            pyv[q] = mk<R>(-kk.x * (vv.x - my.x), -kk.y * (vv.y - my.y));
+        } else {
+            pxv[q] = mk<R>(0, 0);
+            pyv[q] = mk<R>(0, 0);
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+        const int m = t + q * X::G;
+        ra[pad8(m)] = wv[q];
+        rb[pad8(m)] = pyv[q];
+    }
+    __syncthreads();
+    row_r2c<R, H>(ra, a.twR, a.twX, t);
+    row_r2c<R, H>(rb, a.twR, a.twX, t);
+    for (int i = threadIdx.x; i < H * X::TR; i += blockDim.x) {
+        const int rr = i % X::TR, kx = i / X::TR;
+        const C2<R> xa = bufA[rr * X::PL + pad8(kx)], xb = bufB[rr * X::PL + pad8(kx)];
+        const R kxs = (R)((double)kx * a.g.kxs);
+        a.A[(size_t)kx * ny + iy0 + rr] = cadd<R>(xa, cimul<R>(xb, kxs));
+    }
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < 8; ++q) ra[pad8(t + q * X::G)] = pxv[q];
+    __syncthreads();
+    row_r2c<R, H>(ra, a.twR, a.twX, t);
+    for (int i = threadIdx.x; i < H * X::TR; i += blockDim.x) {
+        const int rr = i % X::TR, kx = i / X::TR;
+        a.B[(size_t)kx * ny + iy0 + rr] = bufA[rr * X::PL + pad8(kx)];
+    }
+}
+
+// ======================================================================================
+// K3: forward-y of the right-hand side, AB2 / Euler integrating-factor update, and the
+// inverse-y transforms of everything the velocity/pressure/force kernels need.
+// ======================================================================================
+template <typename R, int NY>
+__global__ void __launch_bounds__(NY / 8) k_nl_y(KArgs<R> a) {
+    constexpr int G = NY / 8;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    C2<R>* bufA = reinterpret_cast<C2<R>*>(smem_raw);
+    C2<R>* bufB = bufA + padded_len(NY);
+    const int kx = blockIdx.x, t = threadIdx.x;
+    const Geometry& g = a.g;
+    const size_t row = (size_t)kx * NY;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+        bufA[pad8(t + q * G)] = a.A[row + t + q * G];
+        bufB[pad8(t + q * G)] = a.B[row + t + q * G];
+    }
+    __syncthreads();
+    block_fft<R, NY, false>(bufA, a.twY, t);
+    block_fft<R, NY, false>(bufB, a.twY, t);
+    const DevScalars* S = a.S;
+    const double dt1 = S->dt1, b10 = S->b10, b11 = S->b11;
+    const bool expl = S->explicit_step != 0;
+    const double norm = 1.0 / ((double)g.nx * (double)g.ny);
+    const double coefx = -dt1 * a.nu * g.scalex, coefy = -dt1 * a.nu * g.scaley;
+    C2<R> wn[8], ps[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+        const int ky = t + q * G;
+        const int ks = signed_k(ky, NY);
+        const bool nyq = (ky == NY / 2);
+        const R kys = (R)((double)ks * g.kys);
+        const C2<R> fa = bufA[pad8(ky)], fb = bufB[pad8(ky)];
+        C2<R> N = csub<R>(fa, cimul<R>(fb, kys));
+        N = cscale<R>(N, (R)norm);
+        if (nyq) N = mk<R>(0, 0);
+        const double kx2 = (double)(kx * kx), ky2 = (double)(ks * ks);
+        const R E1 = (R)exp(coefx * kx2 + coefy * ky2);
+        const bool keep = !(g.idealis == 1 && (kx2 / g.kx_trunc2 + ky2 / g.ky_trunc2 >= 1.0));
+        const R D = keep ? (R)1 : (R)0;
+        const C2<R> Wo = a.W[row + ky];
+        C2<R> Wn;
+        if (expl) {
+            Wn = mk<R>((Wo.x + (R)dt1 * N.x) * E1 * D, (Wo.y + (R)dt1 * N.y) * E1 * D);
+        } else {
+            const C2<R> Mo = a.M[row + ky];
+            Wn = mk<R>(((Wo.x + (R)b10 * N.x) + (R)b11 * Mo.x) * E1 * D, ((Wo.y + (R)b10 * N.y) + (R)b11 * Mo.y) * E1 * D);
+        }
+        if (nyq) Wn = mk<R>(0, 0);
+        a.W[row + ky] = Wn;
+        a.M[row + ky] = cscale<R>(N, E1);
+        wn[q] = Wn;
+        const double k2 = kx2 * g.scalex + ky2 * g.scaley;
+        ps[q] = (kx == 0 && ky == 0) ? mk<R>(0, 0) : cscale<R>(Wn, (R)(1.0 / k2));
+    }
+    // inverse-y outputs
+    const R kxs = (R)((double)kx * g.kxs);
+    const int nout = a.viscous ? 7 : 5;
+    for (int o = 0; o < nout; ++o) {
+        C2<R>* dst;
+        switch (o) {
+            case 0: dst = a.Tu; break;
+            case 1: dst = a.Tv; break;
+            case 2: dst = a.Tw; break;
+            case 3: dst = a.Tdx; break;
+            case 4: dst = a.Tdy; break;
+            case 5: dst = a.Tsa; break;
+            default: dst = a.Tsb; break;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            const int ky = t + q * G;
+            const int ks = signed_k(ky, NY);
+            const R kys = (R)((double)ks * g.kys);
+            C2<R> val;
+            switch (o) {
+                case 0: val = cimul<R>(ps[q], kys); break;                 // cofdy(psi)   -> u
+                case 1: val = cimul<R>(ps[q], kxs); break;                 // cofdx(psi)   -> -v
+                case 2: val = wn[q]; break;                                // omega
+                case 3: val = cimul<R>(wn[q], kxs); break;                 // cofdx(omega)
+                case 4: val = cimul<R>(wn[q], kys); break;                 // cofdy(omega)
+                case 5: val = cscale<R>(ps[q], -(kxs * kys)); break;       // d2psi/dxdy = du/dx
+                default: val = cscale<R>(ps[q], kxs * kxs - kys * kys); break;  // du/dy + dv/dx
+            }
+            if (ky == NY / 2) val = mk<R>(0, 0);
+            bufA[pad8(ky)] = val;
+        }
+        __syncthreads();
+        block_fft<R, NY, true>(bufA, a.twY, t);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) dst[row + t + q * G] = bufA[pad8(t + q * G)];
+    }
+}
+
+// ======================================================================================
+// K4: velocity at n+1, penalty, drag/energy reductions, vor_mean, Poisson RHS (forward-x),
+// stresses to physical space.
+// ======================================================================================
+template <typename R, int H>
+__global__ void __launch_bounds__(XRows<R, H>::THREADS) k_press_x(KArgs<R> a) {
+    using X = XRows<R, H>;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    C2<R>* bufA = reinterpret_cast<C2<R>*>(smem_raw);
+    C2<R>* bufB = bufA + X::TR * X::PL;
+    __shared__ double red_s[RED_NSLOTS][X::THREADS / 32];
+    const int r = threadIdx.x / X::G, t = threadIdx.x % X::G;
+    const int iy0 = blockIdx.x * X::TR, ny = a.g.ny;
+    C2<R>* ra = bufA + r * X::PL;
+    C2<R>* rb = bufB + r * X::PL;
+    const DevScalars* S = a.S;
+    const double time = S->time, dt1 = S->dt1;
+    const R U = (R)S->mean_u_next, V = (R)S->mean_v_next;
+    const int ixmin = S->win[0], ixmax = S->win[1], iymin = S->win[2], iymax = S->win[3];
+
+    load_tileT<R, H, X::TR, X::PL>(bufA, a.Tu, ny, iy0);
+    load_tileT<R, H, X::TR, X::PL>(bufB, a.Tv, ny, iy0);
+    __syncthreads();
+    row_c2r<R, H>(ra, a.twR, a.twX, t);
+    row_c2r<R, H>(rb, a.twR, a.twX, t);
+    C2<R> uv[8], vv[8], wv[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+        const int m = t + q * X::G;
+        const C2<R> ur = ra[pad8(m)], vr = rb[pad8(m)];
+        uv[q] = mk<R>(ur.x + U, ur.y + U);
+        vv[q] = mk<R>(-vr.x + V, -vr.y + V);
+    }
+    __syncthreads();
+    load_tileT<R, H, X::TR, X::PL>(bufA, a.Tw, ny, iy0);
+    __syncthreads();
+    row_c2r<R, H>(ra, a.twR, a.twX, t);
+#pragma unroll
+    for (int q = 0; q < 8; ++q) wv[q] = ra[pad8(t + q * X::G)];
+    __syncthreads();
+
+    const int iy = iy0 + r;
+    const size_t roff = (size_t)iy * H;
+    C2<R>* u2 = reinterpret_cast<C2<R>*>(a.u) + roff;
+    C2<R>* v2 = reinterpret_cast<C2<R>*>(a.v) + roff;
+    C2<R>* vm2 = reinterpret_cast<C2<R>*>(a.vor_mean) + roff;
+    const C2<R>* k2 = reinterpret_cast<const C2<R>*>(a.mask) + roff;
+    const C2<R>* x2 = reinterpret_cast<const C2<R>*>(a.mvx) + roff;
+    const C2<R>* y2 = reinterpret_cast<const C2<R>*>(a.mvy) + roff;
+    const bool in_rows = (iy >= iymin && iy <= iymax);
+    double acc[RED_NSLOTS];
+#pragma unroll
+    for (int s = 0; s < RED_NSLOTS; ++s) acc[s] = 0.0;
+    const double Ud = S->mean_u_next, Vd = S->mean_v_next;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+        const int m = t + q * X::G;
+        const C2<R> uu = uv[q], vq = vv[q], w = wv[q];
+        u2[m] = uu;
+        v2[m] = vq;
+        const C2<R> kk = k2[m], mx = x2[m], my = y2[m];
+        const C2<R> vmo = vm2[m];
+        R px[2], py[2];
+        const R uc[2] = {uu.x, uu.y}, vc[2] = {vq.x, vq.y}, wc[2] = {w.x, w.y};
+        const R kc[2] = {kk.x, kk.y}, xc[2] = {mx.x, mx.y}, yc[2] = {my.x, my.y}, vmc[2] = {vmo.x, vmo.y};
+        R vmn[2];
+#pragma unroll
+        for (int e = 0; e < 2; ++e) {
+            const int ix = 2 * m + e;
+            const R rx = uc[e] - xc[e], ry = vc[e] - yc[e];
+            const R penx = kc[e] * rx, peny = kc[e] * ry;
+            acc[RED_OMEGA2] += (double)(wc[e] * wc[e]);
+            const double du = (double)uc[e] - Ud, dv = (double)vc[e] - Vd;
+            acc[RED_KIN] += du * du + dv * dv;
+            acc[RED_POROUS] += (double)(kc[e] * (rx * rx + ry * ry));
+            acc[RED_INFLOW_SOLID] += (double)(kc[e] * (xc[e] * rx + yc[e] * ry));
+            acc[RED_INFLOW_MEAN] += Ud * (double)penx + Vd * (double)peny;
+            acc[RED_SUM_U] += (double)uc[e];
+            acc[RED_SUM_V] += (double)vc[e];
+            acc[RED_UMAX2] = fmax(acc[RED_UMAX2], (double)(uc[e] * uc[e] + vc[e] * vc[e]));
+            if (in_rows && ix >= ixmin && ix <= ixmax) {
+                acc[RED_DRAG_X] += (double)penx;
+                acc[RED_DRAG_Y] += (double)peny;
+                acc[RED_UNST_X] += (double)(xc[e] * kc[e]);
+                acc[RED_UNST_Y] += (double)(yc[e] * kc[e]);
+            }
+            vmn[e] = (R)(((double)vmc[e] * time + dt1 * (double)wc[e]) / (time + dt1));
+            px[e] = penx - wc[e] * vc[e];
+            py[e] = peny + wc[e] * uc[e];
+        }
+        vm2[m] = mk<R>(vmn[0], vmn[1]);
+        ra[pad8(m)] = mk<R>(px[0], px[1]);
+        rb[pad8(m)] = mk<R>(py[0], py[1]);
+    }
+    // block reduction (fixed order -> deterministic)
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+#pragma unroll
+    for (int s = 0; s < RED_NSLOTS; ++s) {
+        double v = (s == RED_UMAX2) ? warp_max(acc[s]) : warp_sum<R>(acc[s]);
+        if (l == 0) red_s[s][w] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < RED_NSLOTS) {
+        const int s = threadIdx.x;
+        double v = 0.0;
+        for (int i = 0; i < X::THREADS / 32; ++i) v = (s == RED_UMAX2) ? fmax(v, red_s[s][i]) : v + red_s[s][i];
+        a.red[(size_t)blockIdx.x * RED_NSLOTS + s] = v;
+    }
+    if (a.pressure_on) {
+        row_r2c<R, H>(ra, a.twR, a.twX, t);
+        row_r2c<R, H>(rb, a.twR, a.twX, t);
+        for (int i = threadIdx.x; i < H * X::TR; i += blockDim.x) {
+            const int rr = i % X::TR, kx = i / X::TR;
+            const R kxs = (R)((double)kx * a.g.kxs);
+            const size_t o = (size_t)kx * ny + iy0 + rr;
+            a.P1[o] = cimul<R>(bufA[rr * X::PL + pad8(kx)], kxs);
+            a.P2[o] = bufB[rr * X::PL + pad8(kx)];
+        }
+    }
+    if (a.viscous) {
+        __syncthreads();
+        load_tileT<R, H, X::TR, X::PL>(bufA, a.Tsa, ny, iy0);
+        load_tileT<R, H, X::TR, X::PL>(bufB, a.Tsb, ny, iy0);
+        __syncthreads();
+        row_c2r<R, H>(ra, a.twR, a.twX, t);
+        row_c2r<R, H>(rb, a.twR, a.twX, t);
+        C2<R>* sa2 = reinterpret_cast<C2<R>*>(a.sa) + roff;
+        C2<R>* sb2 = reinterpret_cast<C2<R>*>(a.sb) + roff;
+        const R c2 = (R)(2.0 * a.nu), c1 = (R)a.nu;
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            const int m = t + q * X::G;
+            const C2<R> x = ra[pad8(m)], y = rb[pad8(m)];
+            sa2[m] = mk<R>(c2 * x.x, c2 * x.y);
+            sb2[m] = mk<R>(c1 * y.x, c1 * y.y);
+        }
+    }
+}
+
+// K5: forward-y of the Poisson right-hand side, divergence, poisson, inverse-y -> Tq
+template <typename R, int NY>
+__global__ void __launch_bounds__(NY / 8) k_press_y(KArgs<R> a) {
+    constexpr int G = NY / 8;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    C2<R>* bufA = reinterpret_cast<C2<R>*>(smem_raw);
+    C2<R>* bufB = bufA + padded_len(NY);
+    const int kx = blockIdx.x, t = threadIdx.x;
+    const Geometry& g = a.g;
+    const size_t row = (size_t)kx * NY;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+        bufA[pad8(t + q * G)] = a.P1[row + t + q * G];
+        bufB[pad8(t + q * G)] = a.P2[row + t + q * G];
+    }
+    __syncthreads();
+    block_fft<R, NY, false>(bufA, a.twY, t);
+    block_fft<R, NY, false>(bufB, a.twY, t);
+    const R norm = (R)(1.0 / ((double)g.nx * (double)g.ny));
+    C2<R> qv[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+        const int ky = t + q * G;
+        const int ks = signed_k(ky, NY);
+        const R kys = (R)((double)ks * g.kys);
+        C2<R> Q = cadd<R>(cscale<R>(bufA[pad8(ky)], norm), cimul<R>(cscale<R>(bufB[pad8(ky)], norm), kys));
+        const double k2 = (double)(kx * kx) * g.scalex + (double)(ks * ks) * g.scaley;
+        C2<R> qh = (kx == 0 && ky == 0) ? mk<R>(0, 0) : cscale<R>(Q, (R)(1.0 / k2));
+        if (ky == NY / 2) qh = mk<R>(0, 0);
+        qv[q] = qh;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < 8; ++q) bufA[pad8(t + q * G)] = qv[q];
+    __syncthreads();
+    block_fft<R, NY, true>(bufA, a.twY, t);
+#pragma unroll
+    for (int q = 0; q < 8; ++q) a.Tq[row + t + q * G] = bufA[pad8(t + q * G)];
+}
+
+// K6: inverse-x of q, p = q - |u|^2/2
+template <typename R, int H>
+__global__ void __launch_bounds__(XRows<R, H>::THREADS) k_press_fin(KArgs<R> a) {
+    using X = XRows<R, H>;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    C2<R>* buf = reinterpret_cast<C2<R>*>(smem_raw);
+    const int r = threadIdx.x / X::G, t = threadIdx.x % X::G;
+    const int iy0 = blockIdx.x * X::TR, ny = a.g.ny;
+    C2<R>* rb = buf + r * X::PL;
+    load_tileT<R, H, X::TR, X::PL>(buf, a.Tq, ny, iy0);
+    __syncthreads();
+    row_c2r<R, H>(rb, a.twR, a.twX, t);
+    const size_t roff = (size_t)(iy0 + r) * H;
+    const C2<R>* u2 = reinterpret_cast<const C2<R>*>(a.u) + roff;
+    const C2<R>* v2 = reinterpret_cast<const C2<R>*>(a.v) + roff;
+    C2<R>* p2 = reinterpret_cast<C2<R>*>(a.press) + roff;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+        const int m = t + q * X::G;
+        const C2<R> qq = rb[pad8(m)], uu = u2[m], vq = v2[m];
+        p2[m] = mk<R>(qq.x - (R)0.5 * (uu.x * uu.x + vq.x * vq.x), qq.y - (R)0.5 * (uu.y * uu.y + vq.y * vq.y));
+    }
+}
+
+// ======================================================================================
+// Dispatch table: one entry per supported length, filled by the inst_*.cu units.
+// ======================================================================================
+template <typename R>
+struct SizeKernels {
+    // x-pass kernels for H = nx/2
+    void (*xfwd)(KArgs<R>);
+    void (*xinv)(KArgs<R>);
+    void (*vel_x)(KArgs<R>);
+    void (*nl_x)(KArgs<R>);
+    void (*press_x)(KArgs<R>);
+    void (*press_fin)(KArgs<R>);
+    int x_threads, x_rows, x_smem1, x_smem2;
+    // y-pass kernels for NY
+    void (*yfwd)(KArgs<R>);
+    void (*yinv)(KArgs<R>);
+    void (*nl_y)(KArgs<R>);
+    void (*press_y)(KArgs<R>);
+    int y_threads, y_smem1, y_smem2;
+};
+
+template <typename R, int N>
+inline void fill_size_kernels(SizeKernels<R>& k) {
+    constexpr int H = N / 2;
+    using X = XRows<R, H>;
+    k.xfwd = k_xfwd<R, H>;
+    k.xinv = k_xinv<R, H>;
+    k.vel_x = k_vel_x<R, H>;
+    k.nl_x = k_nl_x<R, H>;
+    k.press_x = k_press_x<R, H>;
+    k.press_fin = k_press_fin<R, H>;
+    k.x_threads = X::THREADS;
+    k.x_rows = X::TR;
+    k.x_smem1 = (int)(X::TR * X::PL * sizeof(C2<R>));
+    k.x_smem2 = 2 * k.x_smem1;
+    cudaFuncSetAttribute(k_xfwd<R, H>, cudaFuncAttributeMaxDynamicSharedMemorySize, k.x_smem1);
+    cudaFuncSetAttribute(k_xinv<R, H>, cudaFuncAttributeMaxDynamicSharedMemorySize, k.x_smem1);
+    cudaFuncSetAttribute(k_press_fin<R, H>, cudaFuncAttributeMaxDynamicSharedMemorySize, k.x_smem1);
+    cudaFuncSetAttribute(k_vel_x<R, H>, cudaFuncAttributeMaxDynamicSharedMemorySize, k.x_smem2);
+    cudaFuncSetAttribute(k_nl_x<R, H>, cudaFuncAttributeMaxDynamicSharedMemorySize, k.x_smem2);
+    cudaFuncSetAttribute(k_press_x<R, H>, cudaFuncAttributeMaxDynamicSharedMemorySize, k.x_smem2);
+    k.yfwd = k_yfwd<R, N>;
+    k.yinv = k_yinv<R, N>;
+    k.nl_y = k_nl_y<R, N>;
+    k.press_y = k_press_y<R, N>;
+    k.y_threads = N / 8;
+    k.y_smem1 = (int)(padded_len(N) * sizeof(C2<R>));
+    k.y_smem2 = 2 * k.y_smem1;
+    cudaFuncSetAttribute(k_yfwd<R, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, k.y_smem1);
+    cudaFuncSetAttribute(k_yinv<R, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, k.y_smem1);
+    cudaFuncSetAttribute(k_nl_y<R, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, k.y_smem2);
+    cudaFuncSetAttribute(k_press_y<R, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, k.y_smem2);
+}
+
+}  // namespace fsibe

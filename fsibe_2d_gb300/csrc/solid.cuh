@@ -1,0 +1,49 @@
+// solid.cuh -- mask rasterisation, beam-force interpolation and the IBES beam solver (FP64).
+#pragma once
+#include "common.cuh"
+
+namespace fsibe {
+
+// One drawing primitive of create_mask (create_mask.f90:91-117), in drawing order.
+enum PrimType { PRIM_SEGMENT = 0, PRIM_SHARP = 1, PRIM_HINGE = 2, PRIM_DOT = 3 };
+struct Prim {
+    int type;
+    int box[4];   // ixmin, ixmax, iymin, iymax (inclusive, clipped to the grid)
+    double p[12];
+};
+
+struct MaskArgs {
+    DevScalars* S;
+    int nx, ny, ns, sharp_trailing, sharp;
+    double dx, dy, ds, t_beam, N_smooth, eps, pi, angle_deg;
+    const double *x, *y, *vx, *vy, *th;
+    Prim* prims;
+    int* nprims;
+    int* rect;    // union of all primitive boxes
+    void *mask, *mvx, *mvy;  // R*[ny][nx]
+};
+
+struct ForceArgs {
+    DevScalars* S;
+    int nx, ny, ns, viscous;
+    double xl, yl, dx, dy, ds, t_beam, N_smooth, pi, angle_deg, t_release, tau;
+    const double *x, *y, *th;
+    const void *press, *sa, *sb;   // R*[ny][nx]
+    double *p_new, *tau_new;
+    unsigned int* counter;  // blocks done (last block computes the force integral)
+    int fp32;
+};
+
+struct BeamArgs {
+    DevScalars* S;
+    int ns, iImpulse, maxit, iFLUSI;
+    double ds, eta, mue, sigma, t_release, tau, tol, pi, x0, y0, angle_deg;
+    double *x, *y, *vx, *vy, *th, *thd, *ax, *ay, *p_old, *p_new, *tau_old, *tau_new, *oo;
+    double* ws;      // work vectors
+    double* band;    // (2ns+4) x 15 original band of the Newton matrix
+    double* urow;    // (2ns+4) x 16: U rows (15) and the forward-solved right-hand side
+    double* rows;    // beam_data ring (21 per step) or nullptr
+    int row_cap;
+};
+
+}  // namespace fsibe

@@ -1,0 +1,190 @@
+/*
+ * fsibe.h -- C ABI of the GB300 (sm_103a) implementation of the FSIBE_2D hot path:
+ * the pseudo-spectral vorticity step with volume penalization, coupled to the
+ * inextensible flexible-beam (IBES) solver.
+ *
+ * Every entry point replaces one Fortran routine of the reference (cited per
+ * function as file:line of tommy-engels/FSIBE_2D).  All entry points return an
+ * int status (FSIBE_OK == 0).  The reference has no status returns: it calls
+ * `stop`, or sets `continue_timestep=.false.`; the Fortran shim in
+ * fortran/fsibe_iso_c.f90 maps non-zero codes back onto that behaviour.
+ *
+ * Conventions shared with the reference:
+ *   - physical fields are (0:nx-1, 0:ny-1) column-major, x fastest, FP64 on the
+ *     host side of the ABI: element (ix,iy) sits at f[iy*nx + ix];
+ *   - spectral fields at the ABI are in the reference's packed "Temperton"
+ *     bicomplex real layout produced by coftxy (cof_fftw33.f90:142-193), scaled
+ *     by 1/(nx*ny), Nyquist row and column dropped;
+ *   - u is (0:nx-1, 0:ny-1, 1:2): u[c*nx*ny + iy*nx + ix], c = 0 (x), 1 (y);
+ *   - a beam is (0:ns-1, 1:6): beam[c*ns + n], columns x, y, vx, vy, theta,
+ *     theta_dot (create_mask.f90:12).
+ * Device state lives inside the opaque context in HBM; the host sees it only
+ * through the fsibe_upload_* / fsibe_download_* calls.
+ */
+#ifndef FSIBE_H
+#define FSIBE_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define FSIBE_OK                 0
+#define FSIBE_ERR_PARAM          1  /* bad parameters (params.f90:152-233 checks) */
+#define FSIBE_ERR_CUDA           2  /* a CUDA runtime call failed                   */
+#define FSIBE_ERR_NAN            3  /* NaN in the beam system (SolidSolver.f90:539-546,854-857) */
+#define FSIBE_ERR_NEWTON_MAXIT   4  /* Newton did not converge (SolidSolver.f90:298-301) */
+#define FSIBE_ERR_SINGULAR       5  /* zero pivot in an LU (SolidSolver.f90:515-525,1074-1077) */
+#define FSIBE_ERR_INTERP_OOB     6  /* delta-interpolation target or stencil off the grid (Interpolation.f90:19-24) */
+#define FSIBE_ERR_TIMEOUT        7  /* a bounded device-side wait gave up              */
+#define FSIBE_ERR_UNSUPPORTED    8  /* size or option this build does not implement     */
+#define FSIBE_ERR_MASK_OOB       9  /* beam point below the domain (create_mask.f90:685-688) */
+#define FSIBE_ERR_BRAKE         10  /* emergency brake |d theta_dot| > 100 (SolidSolver.f90:370-380);
+                                       soft: the reference sets continue_timestep=.false. */
+#define FSIBE_ERR_STATE         11  /* call out of order (e.g. step before init_fields) */
+
+/* ---- precision forms ------------------------------------------------- */
+#define FSIBE_FP64    0  /* plain form: FP64 everywhere (the reference's arithmetic)          */
+#define FSIBE_FP32C   1  /* FP32 transforms / derivatives / products; FP64 k=0 mode, vorticity
+                            state (compensated hi+lo), reductions, forces and beam Newton   */
+
+/* ---- solid time methods (share_vars.f90:43) ----------------------------- */
+#define FSIBE_EULER_IMPLICIT   1
+#define FSIBE_CRANK_NICHOLSON  2
+#define FSIBE_BDF2             5
+
+/*
+ * Run parameters.  Mirrors the module globals of share_vars.f90:8-37 that the
+ * hot path reads, in the units the reference uses after params.f90 ran
+ * (nu = 1/Re already inverted; theta_inf in radians).
+ */
+typedef struct fsibe_params {
+    int32_t nx, ny, ns;          /* grid and beam nodes (share_vars.f90:8)                   */
+    int32_t precision;           /* FSIBE_FP64 or FSIBE_FP32C                                 */
+    double  xl, yl;              /* box size                                                  */
+    double  nu;                  /* kinematic viscosity = 1/Re                                */
+    double  eps;                 /* penalization parameter (BASELINE's eta)                   */
+    double  cfl, dt_fixed, time_end;
+    double  eta;                 /* beam stiffness (BASELINE's EI)                            */
+    double  mue;                 /* beam inertia (BASELINE's density ratio)                   */
+    double  t_release, tau;      /* release time, soft-startup duration                       */
+    double  angle_beam;          /* static beam angle, degrees (mouvement.f90:26)             */
+    double  grav, sigma;         /* gravity, beam damping                                     */
+    int32_t iImpulse;            /* GravityImpulse mode (SolidSolver.f90:874-911)             */
+    int32_t time_method_solid;   /* FSIBE_BDF2 / FSIBE_CRANK_NICHOLSON / FSIBE_EULER_IMPLICIT */
+    int32_t iFLUSI, iMotion, iViscous, iSaveBeam;
+    int32_t iBeam, iSharpTrailing, iMeanVelocity, idealis;
+    double  T_fullspeed, theta_inf;
+    double  x0, y0, length;      /* leading edge and beam length                              */
+    double  t_beam;              /* HALF thickness                                            */
+    double  N_smooth;            /* half smoothing-layer width in grid points                 */
+    double  newton_tol;          /* reference hard-codes 1e-7 (SolidSolver.f90:126)           */
+    int32_t newton_maxit;        /* reference stops after iteration 49 (SolidSolver.f90:298)  */
+    int32_t reserved;
+} fsibe_params;
+
+/* Per-step scalar outputs: the columns of beam_data (BeamIO.f90:193-216),
+ * u_max (NavierStokes.f90:80-82), energies (NavierStokes.f90:259-261) and
+ * IBES_iter (SolidSolver.f90:392-394). */
+typedef struct fsibe_scalars {
+    double time, dt0, dt1;
+    double u_max, mean_ux, mean_uy;                    /* u_max file, columns 3..5 */
+    double vor_rms, kinetic, dissipation, porous_diss, inflow_solid, inflow_mean;
+    double force[2], force_unst[2], force_press[2], inertial_force[2];
+    double e_kinetic, e_elastic, e_pot;
+    double beam_data[21];                              /* one beam_data row        */
+    int32_t newton_iters;
+    int32_t status;
+    int32_t step;
+    int32_t reserved;
+} fsibe_scalars;
+
+typedef struct fsibe_ctx fsibe_ctx;
+
+/* ---- lifecycle (replaces dns.f90:170-207 StartSimulation set-up) ------------ */
+/* Allocates every device field of one run, builds the dealiasing predicate
+ * (dealiase_mask.f90:1-33) and the transform tables (fft_initialize,
+ * cof_fftw33.f90:18-66).  Device-resident from here on. */
+int fsibe_create(const fsibe_params* p, fsibe_ctx** out);
+/* fft_free (cof_fftw33.f90:119-137) plus release of every field. */
+int fsibe_destroy(fsibe_ctx* ctx);
+/* Run all kernels of ctx on this cudaStream_t (NULL = the legacy stream). */
+int fsibe_set_stream(fsibe_ctx* ctx, void* cuda_stream);
+const char* fsibe_strerror(int status);
+/* Last error message recorded by ctx (or the library when ctx is NULL). */
+const char* fsibe_last_error(const fsibe_ctx* ctx);
+
+/* ---- spectral operators on packed arrays (host in, host out) ------------------ */
+int fsibe_fft_forward(fsibe_ctx* ctx, const double* f, double* fk);      /* coftxy  cof_fftw33.f90:142-193 */
+int fsibe_fft_inverse(fsibe_ctx* ctx, const double* fk, double* f);      /* cofitxy cof_fftw33.f90:197-243 */
+int fsibe_cofdx(fsibe_ctx* ctx, const double* fk, double* out);          /* cofdx.f90:1-29   */
+int fsibe_cofdy(fsibe_ctx* ctx, const double* fk, double* out);          /* cofdy.f90:1-30   */
+int fsibe_cofdxdx(fsibe_ctx* ctx, const double* fk, double* out);        /* cofdxdx.f90:1-27 */
+int fsibe_cofdydy(fsibe_ctx* ctx, const double* fk, double* out);        /* cofdydy.f90:1-27 */
+int fsibe_cofdxdy(fsibe_ctx* ctx, const double* fk, double* out);        /* cofdxdy.f90:1-32 */
+int fsibe_poisson(fsibe_ctx* ctx, const double* f, double* ans);         /* poisson.f90:1-30 */
+int fsibe_vis(fsibe_ctx* ctx, double dt, double* work);                  /* cal_vis.f90:1-36 */
+int fsibe_dealiase_mask(fsibe_ctx* ctx, double* dealiase);               /* dealiase_mask.f90:1-33 */
+
+/* ---- the time step ------------------------------------------------------ */
+/* init_fields with inicond=111 (init_fields.f90:110-130) followed by the rest of
+ * time_step's set-up (time_step.f90:60-100): init_beams, InitializeSolidSolver,
+ * the zero state, then cal_velocity at t=0. vort is the physical vorticity. */
+int fsibe_init_fields(fsibe_ctx* ctx, const double* vort);
+/* create_mask(time, beams) (create_mask.f90:2-218): beam segments, sharp end,
+ * hinges, leading/trailing dots, then mask /= eps. */
+int fsibe_create_mask(fsibe_ctx* ctx, double time);
+/* EvolveFluidExplicit (NavierStokes.f90:422-459) when explicit_step != 0, else
+ * EvolveFluidAB2 (NavierStokes.f90:463-508); both end with pressure()
+ * (NavierStokes.f90:273-403): velocity at n+1, drag/lift, energies, vor_mean,
+ * pressure. */
+int fsibe_fluid_step(fsibe_ctx* ctx, int explicit_step);
+/* GetForces(time, beams, press, u, "new") (BeamForces.f90:6-51) with SPL=3. */
+int fsibe_get_forces(fsibe_ctx* ctx, double time);
+/* GravityImpulse(time) + SolidSolverWrapper(time, dt1, beams)
+ * (SolidSolver.f90:874-911, 13-44). */
+int fsibe_solid_step(fsibe_ctx* ctx, double time);
+/* Time-level swap, time += dt1, pressure_old = pressure_new, tau_old = tau_new
+ * (time_step.f90:152-159, 222-228). */
+int fsibe_advance(fsibe_ctx* ctx);
+/* One whole step in the reference order (time_step.f90:120-162 when the
+ * startup step is due, else :178-228). */
+int fsibe_step(fsibe_ctx* ctx);
+/* nsteps calls of fsibe_step; when rows != NULL writes one 21-column beam_data
+ * row per step (rows[s*21 + c]). Stops early on a non-zero status. */
+int fsibe_run(fsibe_ctx* ctx, int nsteps, double* rows);
+
+/* ---- state transfer (host <-> HBM) --------------------------------------- */
+int fsibe_upload_vortk(fsibe_ctx* ctx, const double* vortk_packed);
+int fsibe_download_vortk(fsibe_ctx* ctx, double* vortk_packed);
+int fsibe_download_vort(fsibe_ctx* ctx, double* vort);   /* cofitxy of vortk(n0) */
+int fsibe_upload_u(fsibe_ctx* ctx, const double* u);
+int fsibe_download_u(fsibe_ctx* ctx, double* u);
+int fsibe_download_press(fsibe_ctx* ctx, double* press);
+int fsibe_download_vor_mean(fsibe_ctx* ctx, double* vor_mean);
+int fsibe_upload_mask(fsibe_ctx* ctx, const double* mask, const double* maskvx, const double* maskvy);
+int fsibe_download_mask(fsibe_ctx* ctx, double* mask, double* maskvx, double* maskvy);
+int fsibe_upload_press(fsibe_ctx* ctx, const double* press);
+/* beam (ns,6) plus pressure_old/new, tau_old/new (ns each) */
+int fsibe_upload_beam(fsibe_ctx* ctx, const double* beam, const double* p_old, const double* p_new,
+                      const double* tau_old, const double* tau_new);
+int fsibe_download_beam(fsibe_ctx* ctx, double* beam, double* p_old, double* p_new,
+                        double* tau_old, double* tau_new);
+int fsibe_get_scalars(fsibe_ctx* ctx, fsibe_scalars* out);
+
+/* ---- measurement helpers ---------------------------------------------------- */
+/* Device time (ms, CUDA events on ctx's stream) of nsteps whole steps. */
+int fsibe_time_steps(fsibe_ctx* ctx, int nsteps, float* ms);
+/* Number of kernel launches one fsibe_step issues (for the bench's gpu_launches). */
+int fsibe_launches_per_step(fsibe_ctx* ctx, int* launches);
+/* Capture one fsibe_step in a CUDA graph and replay it for later steps (1) or
+ * launch kernels directly (0, default). */
+int fsibe_use_graph(fsibe_ctx* ctx, int enable);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FSIBE_H */
