@@ -1,0 +1,336 @@
+"""Benchmark of the FSIBE_2D fluid step + flexible-beam coupling on GB300.
+
+Workload (the precision configuration): periodic box 4 x 4, nx = ny = 1024, ns = 256 beam
+nodes, Re = 500, dt = 5e-5, clamped flexible beam (length 1, thickness 4 dx, leading edge
+(1, 2), EI = 0.1, density ratio 1), penalization 1e-3 over a 2-cell smoothed mask, initial
+vorticity = seeded N(0, 1e-3) noise low-passed to |k| <= 8.  Inputs are seeded synthetic
+fields of exactly that shape (there is no dataset).
+
+One step = one full time step of the reference's loop (mask -> vorticity AB2 step with the
+pressure solve -> beam forces -> beam Newton solve).  `value` is the FP32-compensated form's
+throughput in Mcell-steps/s with the state resident in HBM; the FP64 plain form is measured
+on the same workload and reported beside it, with the FP32 form's relative L2 vorticity error
+against the FP64 form after a fixed number of steps.  `e2e` runs through the C ABI with
+host buffers (initial field upload, a per-step beam_data read-back, the final field read).
+
+--impl reference times the CPU restatement of the reference (oracle/, FP64, OpenMP on every
+host core): the reference's own Fortran/FFTW/MKL build cannot be built on this machine
+(no Fortran compiler, FFTW, MKL or LAPACK).
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+NX = NY = 1024
+NS = 256
+RE = 500.0
+DT = 5.0e-5
+L2_BYTES = 129 * 1024 * 1024
+METRIC = "Mcell-steps/s at 1024^2 (FP32-compensated form; FP64 plain form beside it)"
+
+
+def seeded_vorticity(n, K=8, sigma=1e-3, seed=0):
+    rng = np.random.default_rng(seed)
+    w = rng.normal(0.0, sigma, (n, n))
+    wk = np.fft.rfft2(w)
+    kx = np.fft.rfftfreq(n, 1.0 / n)
+    ky = np.fft.fftfreq(n, 1.0 / n)
+    wk[(kx[None, :] ** 2 + ky[:, None] ** 2) > K * K] = 0.0
+    return np.fft.irfft2(wk, s=(n, n))
+
+
+def params(precision):
+    from fsibe_2d_gb300 import make_params
+    return make_params(nx=NX, ny=NY, ns=NS, Re=RE, dt=DT, precision=precision)
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """Samples SM clocks and throttle reasons with nvidia-smi during the timed region."""
+
+    def __init__(self, index):
+        self.index = index
+        self.samples = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def start(self):
+        def run():
+            q = ("clocks.sm,clocks.max.sm,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+                 "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_power_cap")
+            while not self._stop.is_set():
+                try:
+                    out = subprocess.run(["nvidia-smi", "-i", str(self.index), f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits"], capture_output=True, text=True,
+                                         timeout=5).stdout.strip()
+                    if out:
+                        self.samples.append([v.strip() for v in out.split(",")])
+                except Exception:
+                    pass
+                self._stop.wait(0.2)
+        self._t = threading.Thread(target=run, daemon=True)
+        self._t.start()
+
+    def stop(self):
+        self._stop.set()
+        if self._t:
+            self._t.join(timeout=10)
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4) if len(s) > 3 + i and "Active" in s[3 + i]})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def algorithmic_bytes(kernel, nx, ny, rbytes):
+    """Bytes one launch must move (fields read + written once), per the kernel map in the design doc."""
+    field = nx * ny * rbytes  # one real field == one half spectrum of complex values
+    passes = {"nl_y": 4 + 9, "nl_x": 7 + 2, "press_x": 9 + 9, "press_y": 3, "press_fin": 4, "mask": 3}
+    return passes.get(kernel, 0) * field
+
+
+def measured_peaks():
+    p = os.path.join(HERE, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        return json.load(open(p)), "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+def ncu_traffic(kernel, precision):
+    p = os.path.join(HERE, "profiles", "roofline_traffic.json")
+    if not os.path.exists(p):
+        return None
+    d = json.load(open(p))
+    return d.get(f"{kernel}:{precision}")
+
+
+def gpu_arm(args):
+    import torch
+    import fsibe_2d_gb300 as F
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+        torch.cuda.set_device(local)
+    dev = torch.device("cuda", local if world > 1 else 0)
+    torch.cuda.set_device(dev)
+    stream = torch.cuda.current_stream(dev)
+    w0 = seeded_vorticity(NX)
+    flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=dev)
+
+    def timed_steps(run, K):
+        """K steps, each bracketed by CUDA events on the run's stream, L2 flushed between."""
+        ms = 0.0
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
+        for k in range(K):
+            flush.add_(1.0)
+            ev[k][0].record(stream)
+            st = run._lib.fsibe_step(run._ctx)
+            ev[k][1].record(stream)
+            if st:
+                raise RuntimeError(f"fsibe_step status {st}")
+        torch.cuda.synchronize(dev)
+        for a, b in ev:
+            ms += a.elapsed_time(b)
+        return ms
+
+    results = {}
+    for prec, tag in ((F.FSIBE_FP32C, "fp32c"), (F.FSIBE_FP64, "fp64")):
+        run = F.Run(params(prec))
+        run.set_stream(stream.cuda_stream)
+        run.use_graph(True)
+        run.init_fields(w0)
+        for _ in range(args.warmup):
+            run.step()
+        torch.cuda.synchronize(dev)
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize(dev)
+        sampler = ClockSampler(local) if tag == "fp32c" else None
+        if sampler:
+            sampler.start()
+        ms = timed_steps(run, args.steps)
+        clocks = sampler.stop() if sampler else None
+        if world > 1:
+            t = torch.tensor([ms], device=dev)
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            ms = float(t.item())
+        s = run.scalars()
+        if s.status:
+            raise RuntimeError(f"device status {s.status}")
+        kt = kernel_times(run, 3)
+        results[tag] = {"ms": ms, "clocks": clocks, "kernels": kt, "launches": run.launches_per_step(),
+                        "newton_iters": s.newton_iters}
+        run.close()
+
+    # FP32-compensated vs FP64 on the GPU from the same seed (relative L2 of vorticity)
+    err_steps = args.err_steps
+    r64, r32 = F.Run(params(F.FSIBE_FP64)), F.Run(params(F.FSIBE_FP32C))
+    r64.init_fields(w0)
+    r32.init_fields(w0)
+    d64, d32 = r64.time_step(err_steps), r32.time_step(err_steps)
+    v64, v32 = r64.vort(), r32.vort()
+    rel_err = float(np.linalg.norm(v32 - v64) / np.linalg.norm(v64))
+    drag_err = float(np.abs(d32[:, 10] - d64[:, 10]).max() / np.abs(d64[:, 10]).max())
+    r64.close()
+    r32.close()
+
+    # end to end through the C ABI with host buffers
+    e2e_steps = args.steps
+    r = F.Run(params(F.FSIBE_FP32C))
+    r.use_graph(True)
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    r.init_fields(w0)
+    for _ in range(e2e_steps):
+        r.step()
+        r.scalars()  # per-step device->host read of the beam_data row
+    vfin = r.vort()
+    t1 = time.perf_counter()
+    r.close()
+    e2e_val = NX * NY * e2e_steps / (t1 - t0) / 1e6
+    del vfin
+
+    cells = NX * NY * world
+    val32 = cells * args.steps / (results["fp32c"]["ms"] * 1e-3) / 1e6
+    val64 = cells * args.steps / (results["fp64"]["ms"] * 1e-3) / 1e6
+    peaks, which = measured_peaks()
+    kt = results["fp32c"]["kernels"]
+    top = max((k for k in kt if k in ("nl_y", "nl_x", "press_x", "press_y", "press_fin")), key=lambda k: kt[k])
+    top_ms = kt[top]
+    ab = algorithmic_bytes(top, NX, NY, 4)
+    achieved = ab / (top_ms * 1e-3) / 1e9
+    traffic = ncu_traffic(top, "fp32c")
+    roof = {"bound": "hbm", "kernel": top, "achieved": round(achieved, 1), "peak": peaks["hbm_gbs"], "unit": "GB/s",
+            "frac": round(achieved / peaks["hbm_gbs"], 3), "traffic": traffic, "peak_source": which,
+            "algorithmic_bytes_per_launch": ab, "avg_launch_ms": round(top_ms, 5)}
+    cpu = cpu_baseline_sample() if rank == 0 else None
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": round(val32, 2), "unit": "Mcell-steps/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(results["fp32c"]["ms"] / args.steps, 5),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32",
+            "data": "synthetic (seeded N(0,1e-3) vorticity, |k|<=8)",
+            "config": {"workload": "precision form: 1024^2 box 4x4, ns=256, Re=500, dt=5e-5, clamped flexible beam EI=0.1, mu=1, eta=1e-3",
+                       "nx": NX, "ny": NY, "ns": NS, "parallelism": f"replicas x{world}" if world > 1 else "single run",
+                       "l2": "flushed between timed steps (256 MB write outside the event pair)",
+                       "cuda_graph": True},
+            "fp64_value": round(val64, 2), "fp64_ms_per_step": round(results["fp64"]["ms"] / args.steps, 5),
+            "fp32_over_fp64": round(val32 / val64, 3),
+            "fp32_rel_l2_vorticity_vs_fp64": rel_err, "fp32_drag_rel_err_vs_fp64": drag_err, "error_steps": err_steps,
+            "newton_iters_last_step": results["fp32c"]["newton_iters"],
+            "kernel_ms_per_step_fp32c": {k: round(v, 5) for k, v in kt.items()},
+            "kernel_ms_per_step_fp64": {k: round(v, 5) for k, v in results["fp64"]["kernels"].items()},
+            "adjoint_over_forward": None,
+            "roofline": roof,
+            "cpu_baseline": cpu,
+            "e2e": {"value": round(e2e_val, 2), "unit": "Mcell-steps/s", "h2d_bytes_per_step": int(8 * NX * NY / e2e_steps),
+                    "d2h_bytes_per_step": int(8 * 21 + 8 * NX * NY / e2e_steps)},
+            "gpu_launches": results["fp32c"]["launches"] * args.steps,
+            "clocks": results["fp32c"]["clocks"],
+        }
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def kernel_times(run, nsteps):
+    import ctypes as C
+    from fsibe_2d_gb300 import library
+    lib = library()
+
+    class KT(C.Structure):
+        _fields_ = [("name", C.c_char * 32), ("ms_total", C.c_float), ("launches", C.c_int32)]
+    lib.fsibe_kernel_times.argtypes = [C.c_void_p, C.c_int, C.POINTER(KT), C.c_int, C.POINTER(C.c_int)]
+    out = (KT * 32)()
+    n = C.c_int()
+    st = lib.fsibe_kernel_times(run._ctx, nsteps, out, 32, C.byref(n))
+    if st:
+        raise RuntimeError(f"fsibe_kernel_times status {st}")
+    return {out[i].name.decode(): out[i].ms_total / nsteps for i in range(n.value)}
+
+
+def oracle_steps(nsteps, threads):
+    sys.path.insert(0, os.path.join(HERE, "oracle"))
+    import pyoracle
+    from fsibe_2d_gb300 import FSIBE_FP64
+    used = pyoracle.set_threads(threads)
+    r = pyoracle.OracleRun(params(FSIBE_FP64))
+    r.init_fields(seeded_vorticity(NX))
+    r.time_step(1)  # start-up step outside the timing
+    t0 = time.perf_counter()
+    r.time_step(nsteps)
+    dt = time.perf_counter() - t0
+    r.close()
+    return dt, used
+
+
+def cpu_baseline_sample():
+    threads = os.cpu_count() or 1
+    n = int(os.environ.get("FSIBE_CPU_SAMPLE_STEPS", "8"))
+    dt, used = oracle_steps(n, threads)
+    return {"value": round(NX * NY * n / dt / 1e6, 3), "unit": "Mcell-steps/s", "cores": used, "kind": "port",
+            "sample": f"{n} FP64 AB2 steps of the same 1024^2 workload (after the start-up step), oracle/ C++ OpenMP"}
+
+
+def reference_arm(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    total_dt = 0.0
+    for _ in range(args.warmup):
+        oracle_steps(1, threads)
+    dt, used = oracle_steps(args.steps, threads)
+    total_dt += dt
+    val = NX * NY * args.steps / total_dt / 1e6
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(val, 3), "unit": "Mcell-steps/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * total_dt / args.steps, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp64",
+        "data": "synthetic (seeded N(0,1e-3) vorticity, |k|<=8)",
+        "config": {"workload": "precision form: 1024^2 box 4x4, ns=256, Re=500, dt=5e-5, clamped flexible beam EI=0.1, mu=1, eta=1e-3",
+                   "nx": NX, "ny": NY, "ns": NS},
+        "cpu_baseline": {"value": round(val, 3), "unit": "Mcell-steps/s", "cores": used, "kind": "port",
+                         "sample": f"{args.steps} FP64 AB2 steps at 1024^2 (CPU restatement; the Fortran/FFTW/MKL build is unavailable here)"},
+        "e2e": {"value": round(val, 3), "unit": "Mcell-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--err-steps", type=int, default=200)
+    args = ap.parse_args()
+    if args.impl == "reference":
+        reference_arm(args)
+    else:
+        gpu_arm(args)
+
+
+if __name__ == "__main__":
+    main()

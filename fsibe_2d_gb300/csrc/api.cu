@@ -388,7 +388,28 @@ struct fsibe_ctx {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     std::string err;
     int launches = 0;
+    // per-kernel event timing (fsibe_kernel_times)
+    bool profiling = false;
+    std::vector<cudaEvent_t> pool;
+    size_t pool_used = 0;
+    std::vector<std::pair<const char*, size_t>> prof;  // name, index of the start event
 };
+
+static void prof_begin(fsibe_ctx* c, const char* name) {
+    if (!c->profiling) return;
+    while (c->pool.size() < c->pool_used + 2) {
+        cudaEvent_t e;
+        cudaEventCreate(&e);
+        c->pool.push_back(e);
+    }
+    cudaEventRecord(c->pool[c->pool_used], c->stream);
+    c->prof.push_back({name, c->pool_used});
+    c->pool_used += 2;
+}
+static void prof_end(fsibe_ctx* c) {
+    if (!c->profiling) return;
+    cudaEventRecord(c->pool[c->prof.back().second + 1], c->stream);
+}
 
 static std::string g_err;
 
@@ -455,15 +476,19 @@ template <> SizeKernels<float>& ky_of<float>(fsibe_ctx* c) { return c->kyf; }
 
 // launch helpers (count launches for the bench's gpu_launches)
 template <typename R>
-static void launch_x(fsibe_ctx* c, void (*k)(KArgs<R>), int smem, const KArgs<R>& a) {
+static void launch_x(fsibe_ctx* c, void (*k)(KArgs<R>), int smem, const KArgs<R>& a, const char* name = "x_pass") {
     const SizeKernels<R>& K = kx_of<R>(c);
+    prof_begin(c, name);
     k<<<c->g.ny / K.x_rows, K.x_threads, smem, c->stream>>>(a);
+    prof_end(c);
     c->launches++;
 }
 template <typename R>
-static void launch_y(fsibe_ctx* c, void (*k)(KArgs<R>), int smem, const KArgs<R>& a) {
+static void launch_y(fsibe_ctx* c, void (*k)(KArgs<R>), int smem, const KArgs<R>& a, const char* name = "y_pass") {
     const SizeKernels<R>& K = ky_of<R>(c);
+    prof_begin(c, name);
     k<<<c->g.hx, K.y_threads, smem, c->stream>>>(a);
+    prof_end(c);
     c->launches++;
 }
 
@@ -510,16 +535,20 @@ static int fluid_step_t(fsibe_ctx* c, int explicit_step) {
     SizeKernels<R>& KY = ky_of<R>(c);
     const int nblk = x_blocks<R>(c);
     StepArgs sa = step_args(c, explicit_step, nblk);
+    prof_begin(c, "step_begin");
     k_step_begin<<<1, 256, 0, c->stream>>>(sa);
+    prof_end(c);
     c->launches++;
-    launch_x<R>(c, KX.nl_x, KX.x_smem2, a);
-    launch_y<R>(c, KY.nl_y, KY.y_smem2, a);
-    launch_x<R>(c, KX.press_x, KX.x_smem2, a);
+    launch_x<R>(c, KX.nl_x, KX.x_smem2, a, "nl_x");
+    launch_y<R>(c, KY.nl_y, KY.y_smem2, a, "nl_y");
+    launch_x<R>(c, KX.press_x, KX.x_smem2, a, "press_x");
+    prof_begin(c, "fluid_finish");
     k_fluid_finish<<<1, 256, 0, c->stream>>>(sa);
+    prof_end(c);
     c->launches++;
     if (a.pressure_on) {
-        launch_y<R>(c, KY.press_y, KY.y_smem2, a);
-        launch_x<R>(c, KX.press_fin, KX.x_smem1, a);
+        launch_y<R>(c, KY.press_y, KY.y_smem2, a, "press_y");
+        launch_x<R>(c, KX.press_fin, KX.x_smem1, a, "press_fin");
     } else {
         CK(c, cudaMemsetAsync(c->phys[PH_PRESS], 0, sizeof(R) * (size_t)c->g.nx * c->g.ny, c->stream));
     }
@@ -553,7 +582,9 @@ static int create_mask(fsibe_ctx* c) {
         for (int q : {PH_MASK, PH_MVX, PH_MVY}) CK(c, cudaMemsetAsync(c->phys[q], 0, bytes, c->stream));
         return FSIBE_OK;
     }
+    prof_begin(c, "mask");
     launch_mask(mask_args(c), c->gerf, c->fp32, c->stream);
+    prof_end(c);
     c->launches += 2;
     CKL(c);
     return FSIBE_OK;
@@ -574,7 +605,9 @@ static int get_forces(fsibe_ctx* c) {
     f.fp32 = c->fp32 ? 1 : 0;
     const double dxi = (c->P.xl - c->g.dx) / (double)(c->P.nx - 1);
     const double dyi = (c->P.yl - c->g.dy) / (double)(c->P.ny - 1);
+    prof_begin(c, "forces");
     launch_forces(f, dxi, dyi, c->stream);
+    prof_end(c);
     c->launches++;
     CKL(c);
     return FSIBE_OK;
@@ -597,7 +630,9 @@ static BeamArgs beam_args(fsibe_ctx* c) {
 }
 
 static int solid_step(fsibe_ctx* c) {
+    prof_begin(c, "beam");
     launch_beam(beam_args(c), c->stream);
+    prof_end(c);
     c->launches++;
     CKL(c);
     return FSIBE_OK;
@@ -611,7 +646,9 @@ static int advance(fsibe_ctx* c) {
     a.th = c->beam[B_TH]; a.thd = c->beam[B_THD];
     a.p_old = c->beam[B_PO]; a.p_new = c->beam[B_PN]; a.tau_old = c->beam[B_TO]; a.tau_new = c->beam[B_TN];
     a.rows = c->rows;
+    prof_begin(c, "advance");
     k_advance<<<1, 256, 0, c->stream>>>(a);
+    prof_end(c);
     c->launches++;
     CKL(c);
     return FSIBE_OK;
@@ -800,6 +837,7 @@ int fsibe_destroy(fsibe_ctx* c) {
     void* others[] = {c->twX, c->twR, c->twY, c->S, c->red, c->oo, c->ws, c->band, c->urow, c->prims, c->nprims,
                       c->rect, c->counter, c->rows, c->dscratch, c->dscratch2};
     for (void* p : others) if (p) cudaFree(p);
+    for (cudaEvent_t e : c->pool) cudaEventDestroy(e);
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
@@ -1180,6 +1218,40 @@ int fsibe_time_steps(fsibe_ctx* c, int nsteps, float* ms) {
     CK(c, cudaEventRecord(c->ev1, c->stream));
     CK(c, cudaEventSynchronize(c->ev1));
     CK(c, cudaEventElapsedTime(ms, c->ev0, c->ev1));
+    return read_status(c);
+}
+
+int fsibe_kernel_times(fsibe_ctx* c, int nsteps, fsibe_kernel_time* out, int cap, int* count) {
+    if (!c || !out || !count || cap <= 0) return FSIBE_ERR_PARAM;
+    CK(c, cudaStreamSynchronize(c->stream));
+    const bool graph = c->use_graph;
+    c->use_graph = false;
+    c->profiling = true;
+    c->prof.clear();
+    c->pool_used = 0;
+    int st = FSIBE_OK;
+    for (int s = 0; s < nsteps && !st; ++s) st = do_step(c);
+    c->profiling = false;
+    c->use_graph = graph;
+    if (st) return st;
+    CK(c, cudaStreamSynchronize(c->stream));
+    int n = 0;
+    for (auto& r : c->prof) {
+        float ms = 0.f;
+        CK(c, cudaEventElapsedTime(&ms, c->pool[r.second], c->pool[r.second + 1]));
+        int k = 0;
+        while (k < n && std::strncmp(out[k].name, r.first, sizeof(out[k].name)) != 0) ++k;
+        if (k == n) {
+            if (n == cap) continue;
+            std::memset(&out[n], 0, sizeof(out[n]));
+            std::strncpy(out[n].name, r.first, sizeof(out[n].name) - 1);
+            ++n;
+        }
+        out[k].ms_total += ms;
+        out[k].launches += 1;
+    }
+    *count = n;
+    c->prof.clear();
     return read_status(c);
 }
 

@@ -178,6 +178,14 @@ int fsibe_get_scalars(fsibe_ctx* ctx, fsibe_scalars* out);
 /* ---- measurement helpers ---------------------------------------------------- */
 /* Device time (ms, CUDA events on ctx's stream) of nsteps whole steps. */
 int fsibe_time_steps(fsibe_ctx* ctx, int nsteps, float* ms);
+/* Device time of each kernel of the step: runs nsteps whole steps (no graph) with CUDA events
+ * around every launch on ctx's stream; out[k] = {name, summed ms, launches}. */
+typedef struct fsibe_kernel_time {
+    char name[32];
+    float ms_total;
+    int32_t launches;
+} fsibe_kernel_time;
+int fsibe_kernel_times(fsibe_ctx* ctx, int nsteps, fsibe_kernel_time* out, int cap, int* count);
 /* Number of kernel launches one fsibe_step issues (for the bench's gpu_launches). */
 int fsibe_launches_per_step(fsibe_ctx* ctx, int* launches);
 /* Capture one fsibe_step in a CUDA graph and replay it for later steps (1) or
