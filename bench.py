@@ -134,7 +134,8 @@ def gpu_arm(args):
         torch.cuda.set_device(local)
     dev = torch.device("cuda", local if world > 1 else 0)
     torch.cuda.set_device(dev)
-    stream = torch.cuda.current_stream(dev)
+    stream = torch.cuda.Stream(dev)  # a capturable (non-legacy) stream for the library and the events
+    torch.cuda.set_stream(stream)
     w0 = seeded_vorticity(NX)
     flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=dev)
 
@@ -224,6 +225,7 @@ def gpu_arm(args):
     roof = {"bound": "hbm", "kernel": top, "achieved": round(achieved, 1), "peak": peaks["hbm_gbs"], "unit": "GB/s",
             "frac": round(achieved / peaks["hbm_gbs"], 3), "traffic": traffic, "peak_source": which,
             "algorithmic_bytes_per_launch": ab, "avg_launch_ms": round(top_ms, 5)}
+    flops = measure_gemm_peaks(dev)
     cpu = cpu_baseline_sample() if rank == 0 else None
     if rank == 0:
         line = {
@@ -242,6 +244,7 @@ def gpu_arm(args):
             "kernel_ms_per_step_fp32c": {k: round(v, 5) for k, v in kt.items()},
             "kernel_ms_per_step_fp64": {k: round(v, 5) for k, v in results["fp64"]["kernels"].items()},
             "adjoint_over_forward": None,
+            "measured_gemm_tflops": flops,
             "roofline": roof,
             "cpu_baseline": cpu,
             "e2e": {"value": round(e2e_val, 2), "unit": "Mcell-steps/s", "h2d_bytes_per_step": int(8 * NX * NY / e2e_steps),
@@ -252,6 +255,31 @@ def gpu_arm(args):
         print(json.dumps(line))
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def measure_gemm_peaks(dev):
+    """FP64 (DGEMM 4096^3) and FP32 (SGEMM 8192^3, TF32 off) throughput through cuBLAS, the
+    denominators for the FP64 form's compute roofline."""
+    import torch
+    out = {}
+    torch.backends.cuda.matmul.allow_tf32 = False
+    for dt, n, tag in ((torch.float64, 4096, "fp64"), (torch.float32, 8192, "fp32")):
+        a = torch.randn(n, n, dtype=dt, device=dev)
+        b = torch.randn(n, n, dtype=dt, device=dev)
+        for _ in range(2):
+            torch.matmul(a, b)
+        torch.cuda.synchronize(dev)
+        best = 1e30
+        for _ in range(5):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            torch.matmul(a, b)
+            e1.record()
+            torch.cuda.synchronize(dev)
+            best = min(best, e0.elapsed_time(e1))
+        out[tag] = round(2.0 * n ** 3 / (best * 1e-3) / 1e12, 2)
+        del a, b
+    return out
 
 
 def kernel_times(run, nsteps):

@@ -27,6 +27,7 @@ void launch_mask(const MaskArgs& a, double gerf, bool fp32, cudaStream_t st);
 void launch_forces(const ForceArgs& a, double dxi, double dyi, cudaStream_t st);
 void launch_beam(const BeamArgs& b, cudaStream_t st);
 void launch_init_beam(const BeamArgs& b, cudaStream_t st);
+bool beam_smem_setup(int ns);
 
 static bool get_sizes(int N, SizeKernels<double>& d, SizeKernels<float>& f) {
     switch (N) {
@@ -50,8 +51,11 @@ struct StepArgs {
     const double* red;
     int nblk, explicit_step, iBeam, iMeanVelocity, ns, nx, ny;
     double cfl, dx, dy, eps, dt_fixed, time_end, theta_inf, T_fullspeed, U_mean_true, pi, nu;
-    double x0, y0, t_beam, NN;
+    double x0, y0, t_beam, NN, scalex, scaley;
     const double *bx, *by;
+    double* etab;
+    float2* etabf;
+    int hx;
 };
 
 __device__ double mean_ux(int mode, double time, double theta_inf, double Tf, double pi) {  // mean_velocity.f90:4-42
@@ -117,8 +121,8 @@ __global__ void __launch_bounds__(256) k_step_begin(StepArgs a) {
         }
         __syncthreads();
     }
-    if (threadIdx.x != 0) return;
     DevScalars* S = a.S;
+    if (threadIdx.x == 0) {
     if (!a.explicit_step) S->dt0 = S->dt1;
     const double time = S->time;
     const double u_max = sqrt(smax[0]);
@@ -157,6 +161,19 @@ __global__ void __launch_bounds__(256) k_step_begin(StepArgs a) {
     } else {
         S->win[0] = 0; S->win[1] = a.nx - 1; S->win[2] = 0; S->win[3] = a.ny - 1;
     }
+    }
+    __syncthreads();
+    // integrating factor exp(-nu dt |k|^2) = exp(coefx kx^2) exp(coefy ky^2) (cal_vis.f90:183-189),
+    // one table per direction, FP64 and split FP32 hi + lo
+    const double dt1 = ((volatile DevScalars*)S)->dt1;
+    const double coefx = -dt1 * a.nu * a.scalex, coefy = -dt1 * a.nu * a.scaley;
+    const int ntab = a.hx + a.ny / 2 + 1;
+    for (int i = threadIdx.x; i < ntab; i += blockDim.x) {
+        const double e = (i < a.hx) ? exp(coefx * (double)(i * i)) : exp(coefy * (double)((i - a.hx) * (i - a.hx)));
+        a.etab[i] = e;
+        const float h = (float)e;
+        a.etabf[i] = make_float2(h, (float)(e - (double)h));
+    }
 }
 
 // End of the fluid part: cal_energy (NavierStokes.f90:222-263) and cal_drag (:566-589)
@@ -179,6 +196,8 @@ __global__ void __launch_bounds__(256) k_fluid_finish(StepArgs a) {
     }
     if (threadIdx.x != 0) return;
     DevScalars* S = a.S;
+    S->mean_u_cur = S->mean_u_next;
+    S->mean_v_cur = S->mean_v_next;
     const double dx = a.dx, dy = a.dy, norm = dx * dy;
     S->vor_rms = dx * dy * sqrt(sm[RED_OMEGA2][0]);
     S->kinetic = 0.5 * dx * dy * sm[RED_KIN][0];
@@ -236,41 +255,53 @@ __global__ void __launch_bounds__(256) k_advance(AdvArgs a) {
 // ---- the packed Temperton layout (ABI boundary only) ---------------------------------
 // unpack: fk (Fortran (0:nx-1,0:ny-1)) -> S[kx][ky]   (cof_fftw33.f90:214-233)
 template <typename R>
-__global__ void k_unpack(const double* fk, C2<R>* H, int nx, int ny) {
-    const int hx = nx / 2;
+__device__ __forceinline__ void put_split(C2<R>* hi, C2<R>* lo, size_t i, double re, double im) {
+    const R h0 = (R)re, h1 = (R)im;
+    hi[i] = mk<R>(h0, h1);
+    if (lo) lo[i] = mk<R>((R)(re - (double)h0), (R)(im - (double)h1));
+}
+template <typename R>
+__global__ void k_unpack(const double* fk, C2<R>* H, C2<R>* Hlo, int nx, int ny) {
     const int kx = blockIdx.x;
+    const size_t r0 = (size_t)kx * ny;
     for (int l = threadIdx.x; l <= ny / 2; l += blockDim.x) {
-        C2<R>* row = H + (size_t)kx * ny;
         if (l == 0) {
-            row[0] = mk<R>((R)fk[2 * kx], (R)fk[2 * kx + 1]);
+            put_split<R>(H, Hlo, r0, fk[2 * kx], fk[2 * kx + 1]);
         } else if (l == ny / 2) {
-            row[ny / 2] = mk<R>(0, 0);
+            put_split<R>(H, Hlo, r0 + ny / 2, 0.0, 0.0);
         } else {
             const double a = fk[(size_t)(2 * l) * nx + 2 * kx], b = fk[(size_t)(2 * l + 1) * nx + 2 * kx];
             const double c = fk[(size_t)(2 * l) * nx + 2 * kx + 1], d = fk[(size_t)(2 * l + 1) * nx + 2 * kx + 1];
-            row[l] = mk<R>((R)(a - d), (R)(b + c));
-            row[ny - l] = mk<R>((R)(a + d), (R)(-b + c));
+            put_split<R>(H, Hlo, r0 + l, a - d, b + c);
+            put_split<R>(H, Hlo, r0 + ny - l, a + d, -b + c);
         }
     }
-    (void)hx;
 }
 // pack: S[kx][ky] -> fk   (cof_fftw33.f90:168-190)
 template <typename R>
-__global__ void k_pack(const C2<R>* H, double* fk, int nx, int ny) {
+__device__ __forceinline__ double2 get_sum(const C2<R>* hi, const C2<R>* lo, size_t i) {
+    const C2<R> h = hi[i];
+    double2 r = make_double2((double)h.x, (double)h.y);
+    if (lo) { const C2<R> l = lo[i]; r.x += (double)l.x; r.y += (double)l.y; }
+    return r;
+}
+template <typename R>
+__global__ void k_pack(const C2<R>* H, const C2<R>* Hlo, double* fk, int nx, int ny) {
     const int kx = blockIdx.x;
-    const C2<R>* row = H + (size_t)kx * ny;
+    const size_t r0 = (size_t)kx * ny;
     for (int l = threadIdx.x; l < ny / 2; l += blockDim.x) {
         if (l == 0) {
-            fk[2 * kx] = (double)row[0].x;
-            fk[2 * kx + 1] = (double)row[0].y;
+            const double2 z = get_sum<R>(H, Hlo, r0);
+            fk[2 * kx] = z.x;
+            fk[2 * kx + 1] = z.y;
             fk[(size_t)nx + 2 * kx] = 0.0;
             fk[(size_t)nx + 2 * kx + 1] = 0.0;
         } else {
-            const C2<R> p = row[l], m = row[ny - l];
-            fk[(size_t)(2 * l) * nx + 2 * kx] = 0.5 * ((double)p.x + (double)m.x);
-            fk[(size_t)(2 * l + 1) * nx + 2 * kx] = 0.5 * ((double)p.y - (double)m.y);
-            fk[(size_t)(2 * l) * nx + 2 * kx + 1] = 0.5 * ((double)p.y + (double)m.y);
-            fk[(size_t)(2 * l + 1) * nx + 2 * kx + 1] = 0.5 * (-(double)p.x + (double)m.x);
+            const double2 p = get_sum<R>(H, Hlo, r0 + l), m = get_sum<R>(H, Hlo, r0 + ny - l);
+            fk[(size_t)(2 * l) * nx + 2 * kx] = 0.5 * (p.x + m.x);
+            fk[(size_t)(2 * l + 1) * nx + 2 * kx] = 0.5 * (p.y - m.y);
+            fk[(size_t)(2 * l) * nx + 2 * kx + 1] = 0.5 * (p.y + m.y);
+            fk[(size_t)(2 * l + 1) * nx + 2 * kx + 1] = 0.5 * (-p.x + m.x);
         }
     }
 }
@@ -340,12 +371,14 @@ __global__ void k_packed_op(const double* in, double* out, int op, int nx, int n
 }
 
 template <typename R>
-__global__ void k_convert(const R* in, double* out, size_t n) {
-    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) out[e] = (double)in[e];
+__global__ void k_convert(const R* in, double* out, size_t n, const double* offset) {
+    const double o = offset ? *offset : 0.0;
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) out[e] = (double)in[e] + o;
 }
 template <typename R>
-__global__ void k_convert_in(const double* in, R* out, size_t n) {
-    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) out[e] = (R)in[e];
+__global__ void k_convert_in(const double* in, R* out, size_t n, const double* offset) {
+    const double o = offset ? *offset : 0.0;
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) out[e] = (R)(in[e] - o);
 }
 
 }  // namespace fsibe
@@ -371,16 +404,20 @@ struct fsibe_ctx {
     double* red = nullptr;
     double* beam[B_N] = {};
     double* oo = nullptr;
-    double *ws = nullptr, *band = nullptr, *urow = nullptr;
+    double* ws = nullptr;
     Prim* prims = nullptr;
     int *nprims = nullptr, *rect = nullptr;
     unsigned* counter = nullptr;
     double* rows = nullptr;
     int rows_cap = 0;
+    double* etab = nullptr;       // integrating-factor tables (hx + ny/2 + 1)
+    float2* etabf = nullptr;
+    int* dcut = nullptr;          // dealiasing cut per kx
     double* dscratch = nullptr;   // 2*nx*ny doubles (ABI transfers, packed arrays)
     double* dscratch2 = nullptr;  // nx*ny doubles
     double gerf = 0.0;
     double U_mean_true = 1.0;
+    bool beam_smem = false;
     bool initialized = false, startup_done = false;
     bool use_graph = false, graph_ready = false;
     cudaGraphExec_t gexec = nullptr;
@@ -460,6 +497,9 @@ static KArgs<R> kargs(fsibe_ctx* c) {
     a.twY = reinterpret_cast<const C2<R>*>(c->twY);
     a.S = c->S;
     a.red = c->red;
+    a.etab = c->etab;
+    a.etabf = c->etabf;
+    a.dcut = c->dcut;
     a.viscous = c->P.iViscous == 1;
     a.pressure_on = (c->P.iFLUSI == 1 || c->P.iSaveBeam > 0);
     a.penalize = c->P.iBeam > 0;
@@ -521,6 +561,11 @@ static StepArgs step_args(fsibe_ctx* c, int explicit_step, int nblk) {
     a.NN = (double)c->P.nx * (double)c->P.ny;
     a.bx = c->beam[B_X];
     a.by = c->beam[B_Y];
+    a.scalex = c->g.scalex;
+    a.scaley = c->g.scaley;
+    a.etab = c->etab;
+    a.etabf = c->etabf;
+    a.hx = c->g.hx;
     return a;
 }
 
@@ -625,7 +670,8 @@ static BeamArgs beam_args(fsibe_ctx* c) {
     b.th = c->beam[B_TH]; b.thd = c->beam[B_THD]; b.ax = c->beam[B_AX]; b.ay = c->beam[B_AY];
     b.p_old = c->beam[B_PO]; b.p_new = c->beam[B_PN]; b.tau_old = c->beam[B_TO]; b.tau_new = c->beam[B_TN];
     b.oo = c->oo;
-    b.ws = c->ws; b.band = c->band; b.urow = c->urow;
+    b.ws = c->ws;
+    b.use_smem = c->beam_smem ? 1 : 0;
     return b;
 }
 
@@ -704,9 +750,9 @@ static void free_graph(fsibe_ctx* c) {
 }
 
 // ---- transfers ----------------------------------------------------------------------
-static int to_host(fsibe_ctx* c, const void* dev, size_t n, double* host) {
+static int to_host(fsibe_ctx* c, const void* dev, size_t n, double* host, const double* offset = nullptr) {
     if (c->fp32) {
-        k_convert<float><<<256, 256, 0, c->stream>>>(reinterpret_cast<const float*>(dev), c->dscratch, n);
+        k_convert<float><<<256, 256, 0, c->stream>>>(reinterpret_cast<const float*>(dev), c->dscratch, n, offset);
         CKL(c);
         CK(c, cudaMemcpyAsync(host, c->dscratch, n * 8, cudaMemcpyDeviceToHost, c->stream));
     } else {
@@ -716,10 +762,10 @@ static int to_host(fsibe_ctx* c, const void* dev, size_t n, double* host) {
     return FSIBE_OK;
 }
 
-static int from_host(fsibe_ctx* c, const double* host, size_t n, void* dev) {
+static int from_host(fsibe_ctx* c, const double* host, size_t n, void* dev, const double* offset = nullptr) {
     if (c->fp32) {
         CK(c, cudaMemcpyAsync(c->dscratch, host, n * 8, cudaMemcpyHostToDevice, c->stream));
-        k_convert_in<float><<<256, 256, 0, c->stream>>>(c->dscratch, reinterpret_cast<float*>(dev), n);
+        k_convert_in<float><<<256, 256, 0, c->stream>>>(c->dscratch, reinterpret_cast<float*>(dev), n, offset);
         CKL(c);
     } else {
         CK(c, cudaMemcpyAsync(dev, host, n * 8, cudaMemcpyHostToDevice, c->stream));
@@ -728,19 +774,19 @@ static int from_host(fsibe_ctx* c, const double* host, size_t n, void* dev) {
     return FSIBE_OK;
 }
 
-static int spec_to_packed(fsibe_ctx* c, const void* H, double* host_fk) {
-    if (c->fp32) k_pack<float><<<c->g.hx, 256, 0, c->stream>>>(reinterpret_cast<const float2*>(H), c->dscratch, c->g.nx, c->g.ny);
-    else k_pack<double><<<c->g.hx, 256, 0, c->stream>>>(reinterpret_cast<const double2*>(H), c->dscratch, c->g.nx, c->g.ny);
+static int spec_to_packed(fsibe_ctx* c, const void* H, double* host_fk, const void* Hlo = nullptr) {
+    if (c->fp32) k_pack<float><<<c->g.hx, 256, 0, c->stream>>>(reinterpret_cast<const float2*>(H), reinterpret_cast<const float2*>(Hlo), c->dscratch, c->g.nx, c->g.ny);
+    else k_pack<double><<<c->g.hx, 256, 0, c->stream>>>(reinterpret_cast<const double2*>(H), nullptr, c->dscratch, c->g.nx, c->g.ny);
     CKL(c);
     CK(c, cudaMemcpyAsync(host_fk, c->dscratch, 8 * (size_t)c->g.nx * c->g.ny, cudaMemcpyDeviceToHost, c->stream));
     CK(c, cudaStreamSynchronize(c->stream));
     return FSIBE_OK;
 }
 
-static int packed_to_spec(fsibe_ctx* c, const double* host_fk, void* H) {
+static int packed_to_spec(fsibe_ctx* c, const double* host_fk, void* H, void* Hlo = nullptr) {
     CK(c, cudaMemcpyAsync(c->dscratch, host_fk, 8 * (size_t)c->g.nx * c->g.ny, cudaMemcpyHostToDevice, c->stream));
-    if (c->fp32) k_unpack<float><<<c->g.hx, 256, 0, c->stream>>>(c->dscratch, reinterpret_cast<float2*>(H), c->g.nx, c->g.ny);
-    else k_unpack<double><<<c->g.hx, 256, 0, c->stream>>>(c->dscratch, reinterpret_cast<double2*>(H), c->g.nx, c->g.ny);
+    if (c->fp32) k_unpack<float><<<c->g.hx, 256, 0, c->stream>>>(c->dscratch, reinterpret_cast<float2*>(H), reinterpret_cast<float2*>(Hlo), c->g.nx, c->g.ny);
+    else k_unpack<double><<<c->g.hx, 256, 0, c->stream>>>(c->dscratch, reinterpret_cast<double2*>(H), nullptr, c->g.nx, c->g.ny);
     CKL(c);
     CK(c, cudaStreamSynchronize(c->stream));
     return FSIBE_OK;
@@ -834,8 +880,8 @@ int fsibe_destroy(fsibe_ctx* c) {
     for (void* p : c->phys) if (p) cudaFree(p);
     for (void* p : c->spec) if (p) cudaFree(p);
     for (double* p : c->beam) if (p) cudaFree(p);
-    void* others[] = {c->twX, c->twR, c->twY, c->S, c->red, c->oo, c->ws, c->band, c->urow, c->prims, c->nprims,
-                      c->rect, c->counter, c->rows, c->dscratch, c->dscratch2};
+    void* others[] = {c->twX, c->twR, c->twY, c->S, c->red, c->oo, c->ws, c->prims, c->nprims,
+                      c->rect, c->counter, c->rows, c->dscratch, c->dscratch2, c->etab, c->etabf, c->dcut};
     for (void* p : others) if (p) cudaFree(p);
     for (cudaEvent_t e : c->pool) cudaEventDestroy(e);
     if (c->ev0) cudaEventDestroy(c->ev0);
@@ -896,14 +942,27 @@ int fsibe_create(const fsibe_params* p, fsibe_ctx** out) {
     for (int i = 0; i < B_N; ++i) ALLOC(c->beam[i], 8 * (size_t)ns);
     ALLOC(c->oo, 8 * (size_t)ns * 6);
     ALLOC(c->ws, 8 * beam_ws_doubles(ns));
-    ALLOC(c->band, 8 * (size_t)(n + 16) * 15);
-    ALLOC(c->urow, 8 * (size_t)(n + 16) * 16);
+    c->beam_smem = beam_smem_setup(ns);
     ALLOC(c->prims, sizeof(Prim) * (size_t)(2 * ns + 8));
     ALLOC(c->nprims, 16);
     ALLOC(c->rect, 16);
     ALLOC(c->counter, 16);
     ALLOC(c->S, sizeof(DevScalars));
     ALLOC(c->red, 8 * (size_t)p->ny * RED_NSLOTS);
+    ALLOC(c->etab, 8 * (size_t)(p->nx / 2 + p->ny / 2 + 8));
+    ALLOC(c->etabf, 8 * (size_t)(p->nx / 2 + p->ny / 2 + 8));
+    ALLOC(c->dcut, 4 * (size_t)(p->nx / 2 + 8));
+    {
+        // 2/3 rule (dealiase_mask.f90:9-26), evaluated with the reference's FP64 expression:
+        // dcut[kx] = smallest |ky| that is removed
+        std::vector<int> cut(p->nx / 2);
+        for (int kx = 0; kx < p->nx / 2; ++kx) {
+            int k = 0;
+            while (k < p->ny / 2 && !((double)kx * (double)kx / (kxt * kxt) + (double)k * (double)k / (kyt * kyt) >= 1.0)) ++k;
+            cut[kx] = k;
+        }
+        cudaMemcpy(c->dcut, cut.data(), 4 * cut.size(), cudaMemcpyHostToDevice);
+    }
     ALLOC(c->dscratch, 8 * 2 * NN);
     ALLOC(c->dscratch2, 8 * NN);
     if (c->fp32) {
@@ -1018,6 +1077,8 @@ int fsibe_init_fields(fsibe_ctx* c, const double* vort) {
     c->U_mean_true = 1.0;
     h.mean_u_next = c->U_mean_true * host_mean(c->P, 0.0, true);
     h.mean_v_next = c->U_mean_true * host_mean(c->P, 0.0, false);
+    h.mean_u_cur = h.mean_u_next;
+    h.mean_v_cur = h.mean_v_next;
     CK(c, cudaMemcpyAsync(c->S, &h, sizeof(h), cudaMemcpyHostToDevice, c->stream));
     launch_init_beam(beam_args(c), c->stream);
     CKL(c);
@@ -1117,8 +1178,12 @@ int fsibe_run(fsibe_ctx* c, int nsteps, double* rows) {
 }
 
 // ---- state transfer -------------------------------------------------------------------
-int fsibe_upload_vortk(fsibe_ctx* c, const double* v) { return c ? packed_to_spec(c, v, c->spec[SP_W]) : FSIBE_ERR_PARAM; }
-int fsibe_download_vortk(fsibe_ctx* c, double* v) { return c ? spec_to_packed(c, c->spec[SP_W], v) : FSIBE_ERR_PARAM; }
+int fsibe_upload_vortk(fsibe_ctx* c, const double* v) {
+    return c ? packed_to_spec(c, v, c->spec[SP_W], c->fp32 ? c->spec[SP_WLO] : nullptr) : FSIBE_ERR_PARAM;
+}
+int fsibe_download_vortk(fsibe_ctx* c, double* v) {
+    return c ? spec_to_packed(c, c->spec[SP_W], v, c->fp32 ? c->spec[SP_WLO] : nullptr) : FSIBE_ERR_PARAM;
+}
 int fsibe_download_vort(fsibe_ctx* c, double* v) {
     if (!c) return FSIBE_ERR_PARAM;
     int st;
@@ -1131,17 +1196,22 @@ int fsibe_download_vort(fsibe_ctx* c, double* v) {
     }
     return to_host(c, c->phys[PH_0], (size_t)c->g.nx * c->g.ny, v);
 }
+// The FP32 form stores u - U (U = mean flow of that velocity, kept as FP64 scalars).
 int fsibe_upload_u(fsibe_ctx* c, const double* u) {
     if (!c) return FSIBE_ERR_PARAM;
     const size_t NN = (size_t)c->g.nx * c->g.ny;
-    int st = from_host(c, u, NN, c->phys[PH_U]);
-    return st ? st : from_host(c, u + NN, NN, c->phys[PH_V]);
+    const double* ou = c->fp32 ? &c->S->mean_u_cur : nullptr;
+    const double* ov = c->fp32 ? &c->S->mean_v_cur : nullptr;
+    int st = from_host(c, u, NN, c->phys[PH_U], ou);
+    return st ? st : from_host(c, u + NN, NN, c->phys[PH_V], ov);
 }
 int fsibe_download_u(fsibe_ctx* c, double* u) {
     if (!c) return FSIBE_ERR_PARAM;
     const size_t NN = (size_t)c->g.nx * c->g.ny;
-    int st = to_host(c, c->phys[PH_U], NN, u);
-    return st ? st : to_host(c, c->phys[PH_V], NN, u + NN);
+    const double* ou = c->fp32 ? &c->S->mean_u_cur : nullptr;
+    const double* ov = c->fp32 ? &c->S->mean_v_cur : nullptr;
+    int st = to_host(c, c->phys[PH_U], NN, u, ou);
+    return st ? st : to_host(c, c->phys[PH_V], NN, u + NN, ov);
 }
 int fsibe_download_press(fsibe_ctx* c, double* p) { return c ? to_host(c, c->phys[PH_PRESS], (size_t)c->g.nx * c->g.ny, p) : FSIBE_ERR_PARAM; }
 int fsibe_upload_press(fsibe_ctx* c, const double* p) { return c ? from_host(c, p, (size_t)c->g.nx * c->g.ny, c->phys[PH_PRESS]) : FSIBE_ERR_PARAM; }

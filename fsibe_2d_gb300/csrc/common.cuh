@@ -51,6 +51,7 @@ struct DevScalars {
     double e_kinetic, e_elastic, e_pot;
     double grav;                     // GravityImpulse state
     double mean_u_next, mean_v_next; // Mean_Ux/Uy(time+dt1) used by the velocity kernel
+    double mean_u_cur, mean_v_cur;   // mean flow of the stored velocity (FP32 form stores u - U)
     int32_t unst_ready;
     int32_t startup_step;            // beam StartupStep
     int32_t method;                  // current TimeMethodSolid

@@ -35,8 +35,34 @@ struct KArgs {
     const C2<R> *twX, *twR, *twY;
     DevScalars* S;
     double* red;
+    const double* etab;   // integrating factor per direction: exp(coefx kx^2) [hx], exp(coefy ky^2) [ny/2+1]
+    const float2* etabf;  // the same split hi + lo (FP32-compensated form)
+    const int* dcut;      // 2/3-rule: modes with |ky| >= dcut[kx] are removed (dealiase_mask.f90:9-26)
     int viscous, pressure_on, penalize, op;
 };
+
+template <typename R> constexpr bool kIsF32 = std::is_same<R, float>::value;
+
+// Error-free transformations for the compensated (hi + lo) vorticity state of the FP32 form.
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+    s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+__device__ __forceinline__ void fast_two_sum(float a, float b, float& s, float& e) {
+    s = __fadd_rn(a, b);
+    e = __fsub_rn(b, __fsub_rn(s, a));
+}
+// (h + l) = ((wh + wl) + d) * (Eh + El), all floats, ~1e-14 relative
+__device__ __forceinline__ void ff_update(float wh, float wl, float d, float Eh, float El, float& oh, float& ol) {
+    float s, e, sh, sl;
+    two_sum(wh, d, s, e);
+    fast_two_sum(s, __fadd_rn(e, wl), sh, sl);
+    const float ph = __fmul_rn(sh, Eh);
+    const float pe = __fmaf_rn(sh, Eh, -ph);
+    const float pl = __fadd_rn(pe, __fmaf_rn(sh, El, __fmul_rn(sl, Eh)));
+    fast_two_sum(ph, pl, oh, ol);
+}
 
 // Operators the generic inverse-y kernel applies before the transform.
 enum SpecOp { OP_ID = 0, OP_DX = 1, OP_DY = 2, OP_U = 3, OP_V = 4 };
@@ -215,8 +241,13 @@ __global__ void __launch_bounds__(XRows<R, H>::THREADS) k_vel_x(KArgs<R> a) {
         C2<R> ur = bufA[r * X::PL + pad8(m)], vr = bufB[r * X::PL + pad8(m)];
         C2<R> uu = mk<R>(ur.x + U, ur.y + U);
         C2<R> vv = mk<R>(-vr.x + V, -vr.y + V);
-        u2[m] = uu;
-        v2[m] = vv;
+        if constexpr (kIsF32<R>) {  // FP32 form keeps the k=0 mean flow out of the stored field
+            u2[m] = ur;
+            v2[m] = mk<R>(-vr.x, -vr.y);
+        } else {
+            u2[m] = uu;
+            v2[m] = vv;
+        }
         mx = fmax(mx, fmax((double)(uu.x * uu.x + vv.x * vv.x), (double)(uu.y * uu.y + vv.y * vv.y)));
         su += (double)uu.x + (double)uu.y;
         sv += (double)vv.x + (double)vv.y;
@@ -268,7 +299,12 @@ __global__ void __launch_bounds__(XRows<R, H>::THREADS) k_nl_x(KArgs<R> a) {
     for (int q = 0; q < 8; ++q) {
         const int m = t + q * X::G;
         const C2<R> dx = ra[pad8(m)], dy = rb[pad8(m)];
-        const C2<R> uu = u2[m], vv = v2[m];
+        C2<R> uu = u2[m], vv = v2[m];
+        if constexpr (kIsF32<R>) {
+            const R Uc = (R)a.S->mean_u_cur, Vc = (R)a.S->mean_v_cur;
+            uu = mk<R>(uu.x + Uc, uu.y + Uc);
+            vv = mk<R>(vv.x + Vc, vv.y + Vc);
+        }
         wv[q] = mk<R>(-uu.x * dx.x - vv.x * dy.x, -uu.y * dx.y - vv.y * dy.y);
         if (a.penalize) {
             const C2<R> kk = k2[m], mx = x2[m], my = y2[m];
@@ -331,39 +367,65 @@ __global__ void __launch_bounds__(NY / 8) k_nl_y(KArgs<R> a) {
     const double dt1 = S->dt1, b10 = S->b10, b11 = S->b11;
     const bool expl = S->explicit_step != 0;
     const double norm = 1.0 / ((double)g.nx * (double)g.ny);
-    const double coefx = -dt1 * a.nu * g.scalex, coefy = -dt1 * a.nu * g.scaley;
+    const int cut = a.dcut[kx];
     C2<R> wn[8], ps[8];
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
         const int ky = t + q * G;
         const int ks = signed_k(ky, NY);
+        const int ka = ks < 0 ? -ks : ks;
         const bool nyq = (ky == NY / 2);
-        const R kys = (R)((double)ks * g.kys);
+        const R kys = (R)ks * (R)g.kys;
         const C2<R> fa = bufA[pad8(ky)], fb = bufB[pad8(ky)];
         C2<R> N = csub<R>(fa, cimul<R>(fb, kys));
         N = cscale<R>(N, (R)norm);
         if (nyq) N = mk<R>(0, 0);
-        const double kx2 = (double)(kx * kx), ky2 = (double)(ks * ks);
-        const R E1 = (R)exp(coefx * kx2 + coefy * ky2);
-        const bool keep = !(g.idealis == 1 && (kx2 / g.kx_trunc2 + ky2 / g.ky_trunc2 >= 1.0));
-        const R D = keep ? (R)1 : (R)0;
-        const C2<R> Wo = a.W[row + ky];
-        C2<R> Wn;
-        if (expl) {
-            Wn = mk<R>((Wo.x + (R)dt1 * N.x) * E1 * D, (Wo.y + (R)dt1 * N.y) * E1 * D);
+        const bool keep = (g.idealis != 1) || (ka < cut);
+        C2<R> Wn, Mn;
+        if constexpr (kIsF32<R>) {
+            const float2 ex = a.etabf[kx], ey = a.etabf[g.hx + ka];
+            const float Eh = __fmul_rn(ex.x, ey.x);
+            const float El = __fadd_rn(__fmaf_rn(ex.x, ey.x, -Eh), __fmaf_rn(ex.x, ey.y, __fmul_rn(ex.y, ey.x)));
+            const C2<R> Wo = a.W[row + ky], Wl = a.Wlo[row + ky];
+            float dx_, dy_;
+            if (expl) {
+                dx_ = (float)dt1 * N.x;
+                dy_ = (float)dt1 * N.y;
+            } else {
+                const C2<R> Mo = a.M[row + ky];
+                dx_ = fmaf((float)b10, N.x, (float)b11 * Mo.x);
+                dy_ = fmaf((float)b10, N.y, (float)b11 * Mo.y);
+            }
+            float h0, l0, h1, l1;
+            ff_update(Wo.x, Wl.x, dx_, Eh, El, h0, l0);
+            ff_update(Wo.y, Wl.y, dy_, Eh, El, h1, l1);
+            if (!keep || nyq) { h0 = l0 = h1 = l1 = 0.f; }
+            Wn = mk<R>(h0, h1);
+            a.Wlo[row + ky] = mk<R>(l0, l1);
+            Mn = cscale<R>(N, Eh);
         } else {
-            const C2<R> Mo = a.M[row + ky];
-            Wn = mk<R>(((Wo.x + (R)b10 * N.x) + (R)b11 * Mo.x) * E1 * D, ((Wo.y + (R)b10 * N.y) + (R)b11 * Mo.y) * E1 * D);
+            const R E1 = a.etab[kx] * a.etab[g.hx + ka];
+            const R D = keep ? (R)1 : (R)0;
+            const C2<R> Wo = a.W[row + ky];
+            if (expl) {
+                Wn = mk<R>((Wo.x + (R)dt1 * N.x) * E1 * D, (Wo.y + (R)dt1 * N.y) * E1 * D);
+            } else {
+                const C2<R> Mo = a.M[row + ky];
+                Wn = mk<R>(((Wo.x + (R)b10 * N.x) + (R)b11 * Mo.x) * E1 * D, ((Wo.y + (R)b10 * N.y) + (R)b11 * Mo.y) * E1 * D);
+            }
+            if (nyq) Wn = mk<R>(0, 0);
+            Mn = cscale<R>(N, E1);
         }
-        if (nyq) Wn = mk<R>(0, 0);
         a.W[row + ky] = Wn;
-        a.M[row + ky] = cscale<R>(N, E1);
+        a.M[row + ky] = Mn;
         wn[q] = Wn;
-        const double k2 = kx2 * g.scalex + ky2 * g.scaley;
-        ps[q] = (kx == 0 && ky == 0) ? mk<R>(0, 0) : cscale<R>(Wn, (R)(1.0 / k2));
+        const R k2 = (R)(kx * kx) * (R)g.scalex + (R)(ks * ks) * (R)g.scaley;
+        if (kx == 0 && ky == 0) ps[q] = mk<R>(0, 0);
+        else if constexpr (kIsF32<R>) ps[q] = cscale<R>(Wn, (R)1 / k2);
+        else ps[q] = mk<R>(Wn.x / k2, Wn.y / k2);   // poisson.f90:159-162 divides
     }
     // inverse-y outputs
-    const R kxs = (R)((double)kx * g.kxs);
+    const R kxs = (R)kx * (R)g.kxs;
     const int nout = a.viscous ? 7 : 5;
     for (int o = 0; o < nout; ++o) {
         C2<R>* dst;
@@ -381,7 +443,7 @@ __global__ void __launch_bounds__(NY / 8) k_nl_y(KArgs<R> a) {
         for (int q = 0; q < 8; ++q) {
             const int ky = t + q * G;
             const int ks = signed_k(ky, NY);
-            const R kys = (R)((double)ks * g.kys);
+            const R kys = (R)ks * (R)g.kys;
             C2<R> val;
             switch (o) {
                 case 0: val = cimul<R>(ps[q], kys); break;                 // cofdy(psi)   -> u
@@ -432,8 +494,13 @@ __global__ void __launch_bounds__(XRows<R, H>::THREADS) k_press_x(KArgs<R> a) {
     for (int q = 0; q < 8; ++q) {
         const int m = t + q * X::G;
         const C2<R> ur = ra[pad8(m)], vr = rb[pad8(m)];
-        uv[q] = mk<R>(ur.x + U, ur.y + U);
-        vv[q] = mk<R>(-vr.x + V, -vr.y + V);
+        if constexpr (kIsF32<R>) {   // keep the raw perturbation; the mean is added in the FP32 path
+            uv[q] = ur;
+            vv[q] = mk<R>(-vr.x, -vr.y);
+        } else {
+            uv[q] = mk<R>(ur.x + U, ur.y + U);
+            vv[q] = mk<R>(-vr.x + V, -vr.y + V);
+        }
     }
     __syncthreads();
     load_tileT<R, H, X::TR, X::PL>(bufA, a.Tw, ny, iy0);
@@ -456,6 +523,58 @@ __global__ void __launch_bounds__(XRows<R, H>::THREADS) k_press_x(KArgs<R> a) {
 #pragma unroll
     for (int s = 0; s < RED_NSLOTS; ++s) acc[s] = 0.0;
     const double Ud = S->mean_u_next, Vd = S->mean_v_next;
+    if constexpr (kIsF32<R>) {
+        // FP32 form: stored velocity is the perturbation u' (mean flow U,V kept in FP64 scalars);
+        // per-thread partial sums in FP32 over 16 cells, FP64 across threads and blocks.
+        float f[RED_NSLOTS];
+#pragma unroll
+        for (int s = 0; s < RED_NSLOTS; ++s) f[s] = 0.f;
+        float spx = 0.f, spy = 0.f;
+        const float Uf = (float)Ud, Vf = (float)Vd;
+        const float ca = (float)(time / (time + dt1)), cb = (float)(dt1 / (time + dt1));
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            const int m = t + q * X::G;
+            const C2<R> up = uv[q], vp = vv[q];
+            u2[m] = up;
+            v2[m] = vp;
+            const C2<R> kk = k2[m], mx = x2[m], my = y2[m], w = wv[q], vmo = vm2[m];
+            const float upc[2] = {up.x, up.y}, vpc[2] = {vp.x, vp.y}, wc[2] = {w.x, w.y};
+            const float kc[2] = {kk.x, kk.y}, xc[2] = {mx.x, mx.y}, yc[2] = {my.x, my.y}, vmc[2] = {vmo.x, vmo.y};
+            float px[2], py[2], vmn[2];
+#pragma unroll
+            for (int e = 0; e < 2; ++e) {
+                const int ix = 2 * m + e;
+                const float uc = upc[e] + Uf, vc = vpc[e] + Vf;
+                const float rx = uc - xc[e], ry = vc - yc[e];
+                const float penx = kc[e] * rx, peny = kc[e] * ry;
+                f[RED_OMEGA2] += wc[e] * wc[e];
+                f[RED_KIN] += upc[e] * upc[e] + vpc[e] * vpc[e];
+                f[RED_POROUS] += kc[e] * (rx * rx + ry * ry);
+                f[RED_INFLOW_SOLID] += kc[e] * (xc[e] * rx + yc[e] * ry);
+                spx += penx;
+                spy += peny;
+                f[RED_SUM_U] += uc;
+                f[RED_SUM_V] += vc;
+                f[RED_UMAX2] = fmaxf(f[RED_UMAX2], uc * uc + vc * vc);
+                if (in_rows && ix >= ixmin && ix <= ixmax) {
+                    f[RED_DRAG_X] += penx;
+                    f[RED_DRAG_Y] += peny;
+                    f[RED_UNST_X] += xc[e] * kc[e];
+                    f[RED_UNST_Y] += yc[e] * kc[e];
+                }
+                vmn[e] = vmc[e] * ca + wc[e] * cb;
+                px[e] = penx - wc[e] * vc;
+                py[e] = peny + wc[e] * uc;
+            }
+            vm2[m] = mk<R>(vmn[0], vmn[1]);
+            ra[pad8(m)] = mk<R>(px[0], px[1]);
+            rb[pad8(m)] = mk<R>(py[0], py[1]);
+        }
+#pragma unroll
+        for (int s = 0; s < RED_NSLOTS; ++s) acc[s] = (double)f[s];
+        acc[RED_INFLOW_MEAN] = Ud * (double)spx + Vd * (double)spy;
+    } else {
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
         const int m = t + q * X::G;
@@ -495,6 +614,7 @@ __global__ void __launch_bounds__(XRows<R, H>::THREADS) k_press_x(KArgs<R> a) {
         vm2[m] = mk<R>(vmn[0], vmn[1]);
         ra[pad8(m)] = mk<R>(px[0], px[1]);
         rb[pad8(m)] = mk<R>(py[0], py[1]);
+    }
     }
     // block reduction (fixed order -> deterministic)
     const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
@@ -565,10 +685,13 @@ __global__ void __launch_bounds__(NY / 8) k_press_y(KArgs<R> a) {
     for (int q = 0; q < 8; ++q) {
         const int ky = t + q * G;
         const int ks = signed_k(ky, NY);
-        const R kys = (R)((double)ks * g.kys);
+        const R kys = (R)ks * (R)g.kys;
         C2<R> Q = cadd<R>(cscale<R>(bufA[pad8(ky)], norm), cimul<R>(cscale<R>(bufB[pad8(ky)], norm), kys));
-        const double k2 = (double)(kx * kx) * g.scalex + (double)(ks * ks) * g.scaley;
-        C2<R> qh = (kx == 0 && ky == 0) ? mk<R>(0, 0) : cscale<R>(Q, (R)(1.0 / k2));
+        const R k2 = (R)(kx * kx) * (R)g.scalex + (R)(ks * ks) * (R)g.scaley;
+        C2<R> qh;
+        if (kx == 0 && ky == 0) qh = mk<R>(0, 0);
+        else if constexpr (kIsF32<R>) qh = cscale<R>(Q, (R)1 / k2);
+        else qh = mk<R>(Q.x / k2, Q.y / k2);
         if (ky == NY / 2) qh = mk<R>(0, 0);
         qv[q] = qh;
     }
@@ -600,7 +723,13 @@ __global__ void __launch_bounds__(XRows<R, H>::THREADS) k_press_fin(KArgs<R> a) 
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
         const int m = t + q * X::G;
-        const C2<R> qq = rb[pad8(m)], uu = u2[m], vq = v2[m];
+        const C2<R> qq = rb[pad8(m)];
+        C2<R> uu = u2[m], vq = v2[m];
+        if constexpr (kIsF32<R>) {
+            const R Uc = (R)a.S->mean_u_cur, Vc = (R)a.S->mean_v_cur;
+            uu = mk<R>(uu.x + Uc, uu.y + Uc);
+            vq = mk<R>(vq.x + Vc, vq.y + Vc);
+        }
         p2[m] = mk<R>(qq.x - (R)0.5 * (uu.x * uu.x + vq.x * vq.x), qq.y - (R)0.5 * (uu.y * uu.y + vq.y * vq.y));
     }
 }

@@ -347,44 +347,46 @@ __global__ void __launch_bounds__(128) k_forces(ForceArgs a, double dxi, double 
 // ===================================================================================
 // Beam solver
 // ===================================================================================
+// Differentiate1D (SolidSolver.f90:1085-1233): the rows of create_diff_matrices as stencils.
+// Coefficients live in constant memory; each row is divided by 2dx / dx^2 / 2dx^3 / dx^4 first
+// and summed over increasing column index, like the reference's matmul.
+__constant__ double cD1[3][3] = {{-3., 4., -1.}, {1., -4., 3.}, {-1., 0., 1.}};
+__constant__ double cD2[3][4] = {{2., -5., 4., -1.}, {-1., 4., -5., 2.}, {1., -2., 1., 0.}};
+__constant__ double cD3[3][6] = {{-17.0 / 2., 71.0 / 2., -59., 49., -41.0 / 2., 7.0 / 2.},
+                                 {-7.0 / 2., 41.0 / 2., -49., 59., -71.0 / 2., 17.0 / 2.},
+                                 {-1., 2., 0., -2., 1., 0.}};
+__constant__ double cD4[3][7] = {{35.0 / 6., -31., 137.0 / 2., -242.0 / 3., 107.0 / 2., -19.0, 17.0 / 6.},
+                                 {17.0 / 6.0, -19.0, 107.0 / 2.0, -242.0 / 3.0, 137.0 / 2.0, -31.0, 35.0 / 6.0},
+                                 {1., -4., 6., -4., 1., 0., 0.}};
+
 namespace {
-// Differentiate1D (SolidSolver.f90:1085-1233) element i of the derivative of f (length N).
 __device__ double d1d(const double* f, int N, double dx, int order, int i) {
     const int L = N - 1;
     const double* cf;
     int j0, len;
     double den;
-    // stencils as in create_diff_matrices
-    const double r1_0[3] = {-3., 4., -1.}, r1_N[3] = {1., -4., 3.}, r1_i[3] = {-1., 0., 1.};
-    const double r2_0[4] = {2., -5., 4., -1.}, r2_N[4] = {-1., 4., -5., 2.}, r2_i[3] = {1., -2., 1.};
-    const double r3_0[6] = {-17.0 / 2., 71.0 / 2., -59., 49., -41.0 / 2., 7.0 / 2.};
-    const double r3_N[6] = {-7.0 / 2., 41.0 / 2., -49., 59., -71.0 / 2., 17.0 / 2.};
-    const double r3_i[5] = {-1., 2., 0., -2., 1.};
-    const double r4_0[7] = {35.0 / 6., -31., 137.0 / 2., -242.0 / 3., 107.0 / 2., -19.0, 17.0 / 6.};
-    const double r4_N[7] = {17.0 / 6.0, -19.0, 107.0 / 2.0, -242.0 / 3.0, 137.0 / 2.0, -31.0, 35.0 / 6.0};
-    const double r4_i[5] = {1., -4., 6., -4., 1.};
     if (order == 1) {
         den = 2.0 * dx;
-        if (i == 0) { cf = r1_0; j0 = 0; len = 3; }
-        else if (i == L) { cf = r1_N; j0 = L - 2; len = 3; }
-        else { cf = r1_i; j0 = i - 1; len = 3; }
+        if (i == 0) { cf = cD1[0]; j0 = 0; len = 3; }
+        else if (i == L) { cf = cD1[1]; j0 = L - 2; len = 3; }
+        else { cf = cD1[2]; j0 = i - 1; len = 3; }
     } else if (order == 2) {
         den = dx * dx;
-        if (i == 0) { cf = r2_0; j0 = 0; len = 4; }
-        else if (i == L) { cf = r2_N; j0 = L - 3; len = 4; }
-        else { cf = r2_i; j0 = i - 1; len = 3; }
+        if (i == 0) { cf = cD2[0]; j0 = 0; len = 4; }
+        else if (i == L) { cf = cD2[1]; j0 = L - 3; len = 4; }
+        else { cf = cD2[2]; j0 = i - 1; len = 3; }
     } else if (order == 3) {
         den = 2.0 * (dx * dx * dx);
-        if (i == 0 || i == 1) { cf = r3_0; j0 = i; len = 6; }
-        else if (i == L - 1) { cf = r3_N; j0 = L - 6; len = 6; }
-        else if (i == L) { cf = r3_N; j0 = L - 5; len = 6; }
-        else { cf = r3_i; j0 = i - 2; len = 5; }
+        if (i == 0 || i == 1) { cf = cD3[0]; j0 = i; len = 6; }
+        else if (i == L - 1) { cf = cD3[1]; j0 = L - 6; len = 6; }
+        else if (i == L) { cf = cD3[1]; j0 = L - 5; len = 6; }
+        else { cf = cD3[2]; j0 = i - 2; len = 5; }
     } else {
         den = (dx * dx) * (dx * dx);
-        if (i == 0 || i == 1) { cf = r4_0; j0 = i; len = 7; }
-        else if (i == L - 1) { cf = r4_N; j0 = L - 7; len = 7; }
-        else if (i == L) { cf = r4_N; j0 = L - 6; len = 7; }
-        else { cf = r4_i; j0 = i - 2; len = 5; }
+        if (i == 0 || i == 1) { cf = cD4[0]; j0 = i; len = 7; }
+        else if (i == L - 1) { cf = cD4[1]; j0 = L - 7; len = 7; }
+        else if (i == L) { cf = cD4[1]; j0 = L - 6; len = 7; }
+        else { cf = cD4[2]; j0 = i - 2; len = 5; }
     }
     double s = 0.0;
     for (int q = 0; q < len; ++q) s += (cf[q] / den) * f[j0 + q];
@@ -392,17 +394,17 @@ __device__ double d1d(const double* f, int N, double dx, int order, int i) {
 }
 
 struct BeamWS {
-    // vectors of length ns (+3 where noted) carved from BeamArgs::ws
+    // vectors of length ns (+3 where noted) carved from one workspace (shared memory when it fits)
     double *T, *T_s, *th_s, *th_ss, *th_sss, *tau_s, *dmain, *dup, *ddown, *rhs, *du2;
     double *te, *te_s, *te_ss, *te_ssss;  // ns+3
     double *p_s, *th1, *td1, *td_in, *old_rhs, *tdn, *taun_s, *bo3, *bo4, *bo5, *bo6, *oo5, *oo6;
-    double *g5, *x, *F, *xd, *xdi, *bvec, *cs, *sn, *pre;  // x/F/xd/xdi/bvec length n; cs/sn/pre length 4*ns
+    double *g5, *x, *F, *xd, *xdi, *bvec, *cs, *pre;  // x/F/xd/xdi/bvec length n; cs/pre length 4*(ns+8)
+    double* band;   // n x 16: original band rows (15 used), overwritten in place by the U rows
     int* ipiv;
 };
 
-__device__ BeamWS carve(const BeamArgs& b) {
-    const int ns = b.ns, n = 2 * ns + 4, L = ns + 8;
-    double* p = b.ws;
+__device__ BeamWS carve(double* p, int ns) {
+    const int n = 2 * ns + 4, L = ns + 8;
     BeamWS w;
     double** one[] = {&w.T, &w.T_s, &w.th_s, &w.th_ss, &w.th_sss, &w.tau_s, &w.dmain, &w.dup, &w.ddown, &w.rhs, &w.du2,
                       &w.te, &w.te_s, &w.te_ss, &w.te_ssss, &w.p_s, &w.th1, &w.td1, &w.td_in, &w.old_rhs, &w.tdn,
@@ -411,17 +413,17 @@ __device__ BeamWS carve(const BeamArgs& b) {
     double** nn[] = {&w.x, &w.F, &w.xd, &w.xdi, &w.bvec};
     for (unsigned k = 0; k < sizeof(nn) / sizeof(nn[0]); ++k) { *nn[k] = p; p += n + 8; }
     w.cs = p; p += 4 * L;
-    w.sn = p; p += 4 * L;
     w.pre = p; p += 4 * L;
+    w.band = p; p += (size_t)(n + 16) * 16;
     w.ipiv = reinterpret_cast<int*>(p);
     return w;
 }
 }  // namespace
 
-// Scratch length (doubles) the beam kernel needs for ns nodes.
+// Workspace length (doubles) the beam kernel needs for ns nodes.
 __host__ size_t beam_ws_doubles(int ns) {
     const int n = 2 * ns + 4, L = ns + 8;
-    return (size_t)29 * L + 5 * (size_t)(n + 8) + 12 * (size_t)L + (size_t)L + 64;
+    return (size_t)29 * L + 5 * (size_t)(n + 8) + 8 * (size_t)L + (size_t)(n + 16) * 16 + (size_t)L + 64;
 }
 
 namespace {
@@ -687,8 +689,8 @@ __device__ int jac_row(const BeamArgs& b, const BeamWS& w, const NewtonCtx& c, i
     auto TT = [&](int j) { return x[ns + 4 + j]; };
     const double ds2 = ds * ds, ds3 = ds * ds * ds, ds4 = (ds * ds) * (ds * ds);
     const int row = row_of(ns, k);
-    double* Ab = b.band + (size_t)row * BW;
-    for (int q = 0; q < BW; ++q) Ab[q] = 0.0;
+    double* Ab = w.band + (size_t)row * 16;
+    for (int q = 0; q < 16; ++q) Ab[q] = 0.0;
     int bad = 0;
     auto put = [&](int l, double v) {
         const int cidx = col_of(ns, l) - row + KL;
@@ -792,35 +794,35 @@ __device__ int jac_row(const BeamArgs& b, const BeamWS& w, const NewtonCtx& c, i
     return bad;
 }
 
-// Banded LU with partial pivoting and the forward substitution fused (one warp), then the back
-// substitution.  Matrix: b.band rows (interleaved order), RHS w.bvec.  Solution -> w.xdi.
-// Lanes 0..14 own the columns k..k+14 of the 8-row active window, lane 15 the right-hand side.
+// Banded LU with partial pivoting (dgbtrf semantics, kl = ku = 7) with the forward
+// substitution fused, then the back substitution; one warp.  Matrix: w.band rows in the
+// interleaved order (stride 16, band index col - row + 7), RHS w.bvec, solution -> w.xdi.
+// Lane c < 16 owns the window column j with j = c (mod 16), so the window never shifts
+// across lanes; lane 16 owns the right-hand side.  Registers v[r] hold window rows k..k+7.
+// U row k overwrites band row k (consumed 8 steps earlier): [1/u_kk, u_k,k+1 .. u_k,k+14, y_k].
 // Returns non-zero on an exactly zero pivot (dgbtrf's INFO > 0).
-__device__ int band_solve(const BeamArgs& b, BeamWS& w, int n) {
+__device__ int band_solve(BeamWS& w, int n) {
     const int lane = threadIdx.x & 31;
+    const bool mat = lane < 16, rhs = lane == 16;
+    double* U = w.band;
     double v[KL + 1];
-    auto orig = [&](int row, int ln) -> double {
-        if (row >= n) return 0.0;
-        if (ln == 15) return w.bvec[row];
-        if (ln > 14) return 0.0;
-        return b.band[(size_t)row * BW + ln];
-    };
-    // initial window, step k = 0: row r holds columns 0..14 -> band index c - r + KL
 #pragma unroll
     for (int r = 0; r <= KL; ++r) {
         double val = 0.0;
-        if (lane == 15) val = (r < n) ? w.bvec[r] : 0.0;
-        else if (lane < 15) {
-            const int ci = lane - r + KL;
-            if (r < n && ci >= 0 && ci < BW) val = b.band[(size_t)r * BW + ci];
+        if (r < n) {
+            if (rhs) val = w.bvec[r];
+            else if (mat) {
+                const int ci = lane - r + KL;  // window [0, 15], column j = lane
+                if (ci >= 0 && ci < BW) val = U[(size_t)r * 16 + ci];
+            }
         }
         v[r] = val;
     }
     int info = 0;
     for (int k = 0; k < n; ++k) {
-        // pivot search on column k (lane 0)
+        const int pl = k & 15;
         int p = 0;
-        if (lane == 0) {
+        if (lane == pl) {
             double best = fabs(v[0]);
 #pragma unroll
             for (int r = 1; r <= KL; ++r) {
@@ -828,54 +830,60 @@ __device__ int band_solve(const BeamArgs& b, BeamWS& w, int n) {
                 if (k + r < n && a > best) { best = a; p = r; }
             }
         }
-        p = __shfl_sync(0xffffffffu, p, 0);
-        // swap rows 0 and p
+        p = __shfl_sync(0xffffffffu, p, pl);
         double t0 = v[0];
 #pragma unroll
-        for (int r = 1; r <= KL; ++r) {
+        for (int r = 1; r <= KL; ++r)
             if (r == p) { const double tmp = v[r]; v[r] = t0; t0 = tmp; }
-        }
         v[0] = t0;
-        const double piv = __shfl_sync(0xffffffffu, v[0], 0);
+        const double piv = __shfl_sync(0xffffffffu, v[0], pl);
         if (piv == 0.0) { info = k + 1; break; }
         const double rinv = 1.0 / piv;
         double l[KL + 1];
 #pragma unroll
-        for (int r = 1; r <= KL; ++r) l[r] = __shfl_sync(0xffffffffu, v[r], 0) * rinv;
-        if (lane >= 1 && lane <= 15) {
+        for (int r = 1; r <= KL; ++r) l[r] = __shfl_sync(0xffffffffu, v[r], pl) * rinv;
+        const int c = (lane - k) & 15;  // offset of this lane's column from k
+        if ((mat && c >= 1 && c <= 14) || rhs) {
 #pragma unroll
             for (int r = 1; r <= KL; ++r) v[r] = v[r] - l[r] * v[0];
         }
-        // emit U row k and the forward-solved RHS
-        if (lane < 16) b.urow[(size_t)k * 16 + lane] = (lane == 0) ? rinv : v[0];
-        // shift the window: rows up, matrix columns left
+        if (mat && c <= 14) U[(size_t)k * 16 + c] = (c == 0) ? rinv : v[0];
+        if (rhs) U[(size_t)k * 16 + 15] = v[0];
 #pragma unroll
         for (int r = 0; r < KL; ++r) v[r] = v[r + 1];
-        const int src = (lane < 14) ? lane + 1 : lane;
-#pragma unroll
-        for (int r = 0; r < KL; ++r) {
-            const double s = __shfl_sync(0xffffffffu, v[r], src);
-            if (lane < 14) v[r] = s;
-            else if (lane == 14) v[r] = 0.0;
+        // next window [k+1, k+16]: the pivot lane now holds column k+16 (zero for every row),
+        // the new row k+8 enters with its original band values
+        const int r8 = k + 1 + KL;
+        double nv = 0.0;
+        if (r8 < n) {
+            if (rhs) nv = w.bvec[r8];
+            else if (mat) {
+                const int cn = (lane - (k + 1)) & 15;
+                if (cn < BW) nv = U[(size_t)r8 * 16 + cn];
+            }
         }
-        v[KL] = orig(k + 1 + KL, lane);
+        if (lane == pl) {
+#pragma unroll
+            for (int r = 0; r < KL; ++r) v[r] = 0.0;
+        }
+        v[KL] = nv;
     }
     info = __shfl_sync(0xffffffffu, info, 0);
     if (info) return info;
-    // back substitution with a sliding set of partial sums: lane c accumulates row (k - c)
+    // back substitution: lane l accumulates its pending row r = l (mod 16), r < k
     double acc = 0.0;
     for (int k = n - 1; k >= 0; --k) {
+        const int ol = k & 15;
         double xk = 0.0;
-        if (lane == 0) {
-            const double* U = b.urow + (size_t)k * 16;
-            xk = (U[15] - acc) * U[0];
+        if (lane == ol) {
+            const double* Uk = U + (size_t)k * 16;
+            xk = (Uk[15] - acc) * Uk[0];
             w.xdi[k] = xk;
+            acc = 0.0;
         }
-        xk = __shfl_sync(0xffffffffu, xk, 0);
-        // lane c (1..14): row k - c gets U[k-c][c] * x[k]
-        if (lane >= 1 && lane <= 14 && k - lane >= 0) acc += b.urow[(size_t)(k - lane) * 16 + lane] * xk;
-        const double s = __shfl_sync(0xffffffffu, acc, (lane < 14) ? lane + 1 : lane);
-        acc = (lane < 14) ? s : 0.0;
+        xk = __shfl_sync(0xffffffffu, xk, ol);
+        const int c = (k - lane) & 15;
+        if (mat && lane != ol && c <= 14 && k - c >= 0) acc += U[(size_t)(k - c) * 16 + c] * xk;
     }
     return 0;
 }
@@ -884,10 +892,11 @@ __device__ int band_solve(const BeamArgs& b, BeamWS& w, int n) {
 
 // IBES_solver / SolidSolverWrapper / SolidEnergies / the force integral, one CTA.
 __global__ void __launch_bounds__(256) k_beam(BeamArgs b) {
+    extern __shared__ __align__(16) double smem_ws[];
     DevScalars* S = b.S;
     if (S->status != 0) return;
     const int ns = b.ns, n = 2 * ns + 4;
-    BeamWS w = carve(b);
+    BeamWS w = carve(b.use_smem ? smem_ws : b.ws, ns);
     const double time = S->time, dt = S->dt1;
     const double ds = b.ds, mue = b.mue, eta = b.eta;
     const double alpha = b.angle_deg * b.pi / 180.0;
@@ -994,7 +1003,7 @@ __global__ void __launch_bounds__(256) k_beam(BeamArgs b) {
             __syncthreads();
             if (flag) { if (threadIdx.x == 0) set_status(S, flag); return; }
             if (threadIdx.x < 32) {
-                const int info = band_solve(b, w, n);
+                const int info = band_solve(w, n);
                 if (threadIdx.x == 0 && info) flag = FSIBE_ERR_SINGULAR;
             }
             __syncthreads();
@@ -1155,7 +1164,16 @@ void launch_forces(const ForceArgs& a, double dxi, double dyi, cudaStream_t st) 
     k_forces<<<a.ns, 128, 0, st>>>(a, dxi, dyi);
 }
 
-void launch_beam(const BeamArgs& b, cudaStream_t st) { k_beam<<<1, 256, 0, st>>>(b); }
+void launch_beam(const BeamArgs& b, cudaStream_t st) {
+    const size_t bytes = b.use_smem ? 8 * beam_ws_doubles(b.ns) : 0;
+    k_beam<<<1, 256, bytes, st>>>(b);
+}
+// Opt the beam kernel into a shared-memory workspace when it fits (<= 200 KB).
+bool beam_smem_setup(int ns) {
+    const size_t bytes = 8 * beam_ws_doubles(ns);
+    if (bytes > 200 * 1024) return false;
+    return cudaFuncSetAttribute(k_beam, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) == cudaSuccess;
+}
 void launch_init_beam(const BeamArgs& b, cudaStream_t st) { k_init_beam<<<1, 256, 0, st>>>(b); }
 
 }  // namespace fsibe

@@ -39,9 +39,8 @@ struct BeamArgs {
     int ns, iImpulse, maxit, iFLUSI;
     double ds, eta, mue, sigma, t_release, tau, tol, pi, x0, y0, angle_deg;
     double *x, *y, *vx, *vy, *th, *thd, *ax, *ay, *p_old, *p_new, *tau_old, *tau_new, *oo;
-    double* ws;      // work vectors
-    double* band;    // (2ns+4) x 15 original band of the Newton matrix
-    double* urow;    // (2ns+4) x 16: U rows (15) and the forward-solved right-hand side
+    double* ws;      // global workspace (used when the shared-memory workspace does not fit)
+    int use_smem;    // 1: workspace in dynamic shared memory
     double* rows;    // beam_data ring (21 per step) or nullptr
     int row_cap;
 };
