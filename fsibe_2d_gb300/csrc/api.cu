@@ -413,6 +413,7 @@ struct fsibe_ctx {
     double* etab = nullptr;       // integrating-factor tables (hx + ny/2 + 1)
     float2* etabf = nullptr;
     int* dcut = nullptr;          // dealiasing cut per kx
+    int kcut = 0;                 // first kx whose row is entirely removed by the 2/3 rule
     double* dscratch = nullptr;   // 2*nx*ny doubles (ABI transfers, packed arrays)
     double* dscratch2 = nullptr;  // nx*ny doubles
     double gerf = 0.0;
@@ -500,6 +501,7 @@ static KArgs<R> kargs(fsibe_ctx* c) {
     a.etab = c->etab;
     a.etabf = c->etabf;
     a.dcut = c->dcut;
+    a.kcut = c->kcut;
     a.viscous = c->P.iViscous == 1;
     a.pressure_on = (c->P.iFLUSI == 1 || c->P.iSaveBeam > 0);
     a.penalize = c->P.iBeam > 0;
@@ -962,6 +964,10 @@ int fsibe_create(const fsibe_params* p, fsibe_ctx** out) {
             cut[kx] = k;
         }
         cudaMemcpy(c->dcut, cut.data(), 4 * cut.size(), cudaMemcpyHostToDevice);
+        c->kcut = p->nx / 2;
+        if (p->idealis == 1)
+            for (int kx = 0; kx < p->nx / 2; ++kx)
+                if (cut[kx] == 0) { c->kcut = kx; break; }
     }
     ALLOC(c->dscratch, 8 * 2 * NN);
     ALLOC(c->dscratch2, 8 * NN);

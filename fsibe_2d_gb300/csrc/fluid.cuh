@@ -38,6 +38,7 @@ struct KArgs {
     const double* etab;   // integrating factor per direction: exp(coefx kx^2) [hx], exp(coefy ky^2) [ny/2+1]
     const float2* etabf;  // the same split hi + lo (FP32-compensated form)
     const int* dcut;      // 2/3-rule: modes with |ky| >= dcut[kx] are removed (dealiase_mask.f90:9-26)
+    int kcut;             // rows kx >= kcut hold no dealiased mode (dcut = 0): exact zeros after the update
     int viscous, pressure_on, penalize, op;
 };
 
@@ -81,11 +82,12 @@ struct XRows {
 };
 
 // ---- x-pass helpers -------------------------------------------------------------------
+// Rows kx >= kmax are known to be zero and are not read.
 template <typename R, int H, int TR, int PL>
-__device__ __forceinline__ void load_tileT(C2<R>* buf, const C2<R>* __restrict__ T, int ny, int iy0) {
+__device__ __forceinline__ void load_tileT(C2<R>* buf, const C2<R>* __restrict__ T, int ny, int iy0, int kmax = H) {
     for (int i = threadIdx.x; i < H * TR; i += blockDim.x) {
         const int r = i % TR, kx = i / TR;
-        buf[r * PL + pad8(kx)] = T[(size_t)kx * ny + iy0 + r];
+        buf[r * PL + pad8(kx)] = (kx < kmax) ? T[(size_t)kx * ny + iy0 + r] : mk<R>(0, 0);
     }
 }
 
@@ -282,8 +284,10 @@ __global__ void __launch_bounds__(XRows<R, H>::THREADS) k_nl_x(KArgs<R> a) {
     const int iy0 = blockIdx.x * X::TR, ny = a.g.ny;
     C2<R>* ra = bufA + r * X::PL;
     C2<R>* rb = bufB + r * X::PL;
-    load_tileT<R, H, X::TR, X::PL>(bufA, a.Tdx, ny, iy0);
-    load_tileT<R, H, X::TR, X::PL>(bufB, a.Tdy, ny, iy0);
+    // after the first AB2/Euler update the vorticity is dealiased: rows kx >= kcut are zero
+    const int kin = a.S->explicit_step ? H : a.kcut;
+    load_tileT<R, H, X::TR, X::PL>(bufA, a.Tdx, ny, iy0, kin);
+    load_tileT<R, H, X::TR, X::PL>(bufB, a.Tdy, ny, iy0, kin);
     __syncthreads();
     row_c2r<R, H>(ra, a.twR, a.twX, t);
     row_c2r<R, H>(rb, a.twR, a.twX, t);
@@ -325,7 +329,8 @@ __global__ void __launch_bounds__(XRows<R, H>::THREADS) k_nl_x(KArgs<R> a) {
     __syncthreads();
     row_r2c<R, H>(ra, a.twR, a.twX, t);
     row_r2c<R, H>(rb, a.twR, a.twX, t);
-    for (int i = threadIdx.x; i < H * X::TR; i += blockDim.x) {
+    // the right-hand side only matters where the update keeps modes (kx < kcut)
+    for (int i = threadIdx.x; i < a.kcut * X::TR; i += blockDim.x) {
         const int rr = i % X::TR, kx = i / X::TR;
         const C2<R> xa = bufA[rr * X::PL + pad8(kx)], xb = bufB[rr * X::PL + pad8(kx)];
         const R kxs = (R)((double)kx * a.g.kxs);
@@ -336,7 +341,7 @@ __global__ void __launch_bounds__(XRows<R, H>::THREADS) k_nl_x(KArgs<R> a) {
     for (int q = 0; q < 8; ++q) ra[pad8(t + q * X::G)] = pxv[q];
     __syncthreads();
     row_r2c<R, H>(ra, a.twR, a.twX, t);
-    for (int i = threadIdx.x; i < H * X::TR; i += blockDim.x) {
+    for (int i = threadIdx.x; i < a.kcut * X::TR; i += blockDim.x) {
         const int rr = i % X::TR, kx = i / X::TR;
         a.B[(size_t)kx * ny + iy0 + rr] = bufA[rr * X::PL + pad8(kx)];
     }
@@ -355,6 +360,17 @@ __global__ void __launch_bounds__(NY / 8) k_nl_y(KArgs<R> a) {
     const int kx = blockIdx.x, t = threadIdx.x;
     const Geometry& g = a.g;
     const size_t row = (size_t)kx * NY;
+    if (kx >= a.kcut) {
+        // every mode of this row is removed by the 2/3 rule: the new state is exactly zero and
+        // none of the inverse transforms is read (the x pass treats rows >= kcut as zero)
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            a.W[row + t + q * G] = mk<R>(0, 0);
+            a.M[row + t + q * G] = mk<R>(0, 0);
+            if constexpr (kIsF32<R>) a.Wlo[row + t + q * G] = mk<R>(0, 0);
+        }
+        return;
+    }
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
         bufA[pad8(t + q * G)] = a.A[row + t + q * G];
@@ -484,8 +500,8 @@ __global__ void __launch_bounds__(XRows<R, H>::THREADS) k_press_x(KArgs<R> a) {
     const R U = (R)S->mean_u_next, V = (R)S->mean_v_next;
     const int ixmin = S->win[0], ixmax = S->win[1], iymin = S->win[2], iymax = S->win[3];
 
-    load_tileT<R, H, X::TR, X::PL>(bufA, a.Tu, ny, iy0);
-    load_tileT<R, H, X::TR, X::PL>(bufB, a.Tv, ny, iy0);
+    load_tileT<R, H, X::TR, X::PL>(bufA, a.Tu, ny, iy0, a.kcut);
+    load_tileT<R, H, X::TR, X::PL>(bufB, a.Tv, ny, iy0, a.kcut);
     __syncthreads();
     row_c2r<R, H>(ra, a.twR, a.twX, t);
     row_c2r<R, H>(rb, a.twR, a.twX, t);
@@ -503,7 +519,7 @@ __global__ void __launch_bounds__(XRows<R, H>::THREADS) k_press_x(KArgs<R> a) {
         }
     }
     __syncthreads();
-    load_tileT<R, H, X::TR, X::PL>(bufA, a.Tw, ny, iy0);
+    load_tileT<R, H, X::TR, X::PL>(bufA, a.Tw, ny, iy0, a.kcut);
     __syncthreads();
     row_c2r<R, H>(ra, a.twR, a.twX, t);
 #pragma unroll
@@ -643,8 +659,8 @@ __global__ void __launch_bounds__(XRows<R, H>::THREADS) k_press_x(KArgs<R> a) {
     }
     if (a.viscous) {
         __syncthreads();
-        load_tileT<R, H, X::TR, X::PL>(bufA, a.Tsa, ny, iy0);
-        load_tileT<R, H, X::TR, X::PL>(bufB, a.Tsb, ny, iy0);
+        load_tileT<R, H, X::TR, X::PL>(bufA, a.Tsa, ny, iy0, a.kcut);
+        load_tileT<R, H, X::TR, X::PL>(bufB, a.Tsb, ny, iy0, a.kcut);
         __syncthreads();
         row_c2r<R, H>(ra, a.twR, a.twX, t);
         row_c2r<R, H>(rb, a.twR, a.twX, t);
