@@ -408,6 +408,7 @@ struct fsibe_ctx {
     Prim* prims = nullptr;
     int *nprims = nullptr, *rect = nullptr;
     unsigned* counter = nullptr;
+    double* fterm = nullptr;
     double* rows = nullptr;
     int rows_cap = 0;
     double* etab = nullptr;       // integrating-factor tables (hx + ny/2 + 1)
@@ -649,6 +650,7 @@ static int get_forces(fsibe_ctx* c) {
     f.press = c->phys[PH_PRESS]; f.sa = c->phys[PH_SA]; f.sb = c->phys[PH_SB];
     f.p_new = c->beam[B_PN]; f.tau_new = c->beam[B_TN];
     f.counter = c->counter;
+    f.fterm = c->fterm;
     f.fp32 = c->fp32 ? 1 : 0;
     const double dxi = (c->P.xl - c->g.dx) / (double)(c->P.nx - 1);
     const double dyi = (c->P.yl - c->g.dy) / (double)(c->P.ny - 1);
@@ -883,7 +885,7 @@ int fsibe_destroy(fsibe_ctx* c) {
     for (void* p : c->spec) if (p) cudaFree(p);
     for (double* p : c->beam) if (p) cudaFree(p);
     void* others[] = {c->twX, c->twR, c->twY, c->S, c->red, c->oo, c->ws, c->prims, c->nprims,
-                      c->rect, c->counter, c->rows, c->dscratch, c->dscratch2, c->etab, c->etabf, c->dcut};
+                      c->rect, c->counter, c->fterm, c->rows, c->dscratch, c->dscratch2, c->etab, c->etabf, c->dcut};
     for (void* p : others) if (p) cudaFree(p);
     for (cudaEvent_t e : c->pool) cudaEventDestroy(e);
     if (c->ev0) cudaEventDestroy(c->ev0);
@@ -949,6 +951,7 @@ int fsibe_create(const fsibe_params* p, fsibe_ctx** out) {
     ALLOC(c->nprims, 16);
     ALLOC(c->rect, 16);
     ALLOC(c->counter, 16);
+    ALLOC(c->fterm, 16 * (size_t)ns);
     ALLOC(c->S, sizeof(DevScalars));
     ALLOC(c->red, 8 * (size_t)p->ny * RED_NSLOTS);
     ALLOC(c->etab, 8 * (size_t)(p->nx / 2 + p->ny / 2 + 8));
@@ -1343,3 +1346,4 @@ int fsibe_launches_per_step(fsibe_ctx* c, int* n) {
 }
 
 }  // extern "C"
+

@@ -127,6 +127,13 @@ __global__ void k_mask_prep(MaskArgs a, double gerf) {
 #define MASK_TX 32
 #define MASK_TY 8
 
+// FP32 pre-test data of one primitive: a cell that fails the pre-test is outside the primitive
+// by more than the margin, so the exact FP64 test (the reference's arithmetic) is skipped.
+struct PrimF {
+    float4 a;  // segment/sharp: (cos, sin, x*_lo, x*_hi)   hinge/dot: (px, py, R^2 limit, 0)
+    float2 b;  // segment/sharp: (y*_hi, y*_lo)
+};
+
 template <typename R>
 __global__ void __launch_bounds__(256) k_mask_raster(MaskArgs a, double gerf) {
     const int tx = threadIdx.x % MASK_TX, ty = threadIdx.x / MASK_TX;
@@ -142,28 +149,47 @@ __global__ void __launch_bounds__(256) k_mask_raster(MaskArgs a, double gerf) {
         mk_[cell] = (R)0; vx_[cell] = (R)0; vy_[cell] = (R)0;
         return;
     }
-    __shared__ int list[256];
+    __shared__ Prim sp[256];
+    __shared__ PrimF sf[256];
     __shared__ int wcount[8];
     __shared__ int nlist;
     const double dx = a.dx, dy = a.dy, mxd = fmax(dx, dy), t = a.t_beam, N = a.N_smooth;
     const double t_star = t + 2.0 * N * mxd, h = N * mxd;
+    const double rcut = t + 10.0 * h * gerf;
+    const float mg = 1.0e-5f * (float)fmax((double)a.nx * dx, (double)a.ny * dy);
     const double xi = (double)i * dx, yj = (double)j * dy;
+    const float xf = (float)xi, yf = (float)yj;
     double m = 0.0, vx = 0.0, vy = 0.0;
     const int total = *a.nprims;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (int base = 0; base < total; base += 256) {
         const int q = base + threadIdx.x;
         bool hit = false;
+        Prim P;
         if (q < total) {
-            const int* b = a.prims[q].box;
-            hit = !(b[1] < ix0 || b[0] > ix1 || b[3] < iy0 || b[2] > iy1) && b[0] <= b[1] && b[2] <= b[3];
+            P = a.prims[q];
+            const int* bx = P.box;
+            hit = !(bx[1] < ix0 || bx[0] > ix1 || bx[3] < iy0 || bx[2] > iy1) && bx[0] <= bx[1] && bx[2] <= bx[3];
         }
         const unsigned bal = __ballot_sync(0xffffffffu, hit);
         if (lane == 0) wcount[warp] = __popc(bal);
         __syncthreads();
         int off = 0;
         for (int w = 0; w < warp; ++w) off += wcount[w];
-        if (hit) list[off + __popc(bal & ((1u << lane) - 1u))] = q;
+        if (hit) {
+            const int e = off + __popc(bal & ((1u << lane) - 1u));
+            sp[e] = P;
+            PrimF F;
+            if (P.type == PRIM_SEGMENT || P.type == PRIM_SHARP) {
+                F.a = make_float4((float)P.p[0], (float)P.p[1], (float)P.p[2] - mg, (float)P.p[4] + mg);
+                F.b = make_float2((float)(P.p[3] + t_star) + mg, (float)(P.p[5] - t_star) - mg);
+            } else {
+                const float lim = (float)((P.type == PRIM_HINGE) ? t_star : rcut) + mg;
+                F.a = make_float4((float)P.p[0], (float)P.p[1], lim * lim, 0.f);
+                F.b = make_float2(0.f, 0.f);
+            }
+            sf[e] = F;
+        }
         if (threadIdx.x == 0) {
             int s = 0;
             for (int w = 0; w < 8; ++w) s += wcount[w];
@@ -172,59 +198,66 @@ __global__ void __launch_bounds__(256) k_mask_raster(MaskArgs a, double gerf) {
         __syncthreads();
         const int nl = nlist;
         for (int e = 0; e < nl; ++e) {
-            const Prim& P = a.prims[list[e]];
-            if (i < P.box[0] || i > P.box[1] || j < P.box[2] || j > P.box[3]) continue;
-            if (P.type == PRIM_SEGMENT) {
-                const double ca = P.p[0], sa = P.p[1];
+            const Prim& Q = sp[e];
+            if (i < Q.box[0] || i > Q.box[1] || j < Q.box[2] || j > Q.box[3]) continue;
+            const PrimF F = sf[e];
+            if (Q.type == PRIM_SEGMENT) {
+                const float xs_f = xf * F.a.x - yf * F.a.y, ys_f = xf * F.a.y + yf * F.a.x;
+                if (xs_f < F.a.z || xs_f > F.a.w || ys_f > F.b.x || ys_f < F.b.y) continue;
+                const double ca = Q.p[0], sa = Q.p[1];
                 const double xs = xi * ca - yj * sa, ys = xi * sa + yj * ca;
-                if (xs >= P.p[2] && xs <= P.p[4] && ys <= (P.p[3] + t_star) && ys >= (P.p[5] - t_star)) {
-                    const double temp = smooth_step(fabs(ys - P.p[3]), t, h, a.sharp, gerf);
+                if (xs >= Q.p[2] && xs <= Q.p[4] && ys <= (Q.p[3] + t_star) && ys >= (Q.p[5] - t_star)) {
+                    const double temp = smooth_step(fabs(ys - Q.p[3]), t, h, a.sharp, gerf);
                     if (temp > m) {
                         m = temp;
-                        vx = (P.p[6] + (xs - P.p[2]) * (P.p[8] - P.p[6]) / a.ds);
-                        vy = (P.p[7] + (xs - P.p[2]) * (P.p[9] - P.p[7]) / a.ds);
+                        vx = (Q.p[6] + (xs - Q.p[2]) * (Q.p[8] - Q.p[6]) / a.ds);
+                        vy = (Q.p[7] + (xs - Q.p[2]) * (Q.p[9] - Q.p[7]) / a.ds);
                     }
                 }
-            } else if (P.type == PRIM_SHARP) {
-                const double ca = P.p[0], sa = P.p[1];
+            } else if (Q.type == PRIM_SHARP) {
+                const float xs_f = xf * F.a.x + yf * F.a.y, ys_f = -xf * F.a.y + yf * F.a.x;
+                if (xs_f < F.a.z || xs_f > F.a.w || ys_f > F.b.x || ys_f < F.b.y) continue;
+                const double ca = Q.p[0], sa = Q.p[1];
                 const double xs = xi * ca + yj * sa, ys = -xi * sa + yj * ca;
-                if (xs >= P.p[2] && xs <= P.p[4] && ys <= (P.p[3] + t_star) && ys >= (P.p[5] - t_star)) {
-                    const double tmp2 = smooth_step(xs - P.p[2], 2.0 * mxd, h, a.sharp, gerf);
-                    const double temp = smooth_step(fabs(ys - P.p[3]), t, h, a.sharp, gerf);
+                if (xs >= Q.p[2] && xs <= Q.p[4] && ys <= (Q.p[3] + t_star) && ys >= (Q.p[5] - t_star)) {
+                    const double tmp2 = smooth_step(xs - Q.p[2], 2.0 * mxd, h, a.sharp, gerf);
+                    const double temp = smooth_step(fabs(ys - Q.p[3]), t, h, a.sharp, gerf);
                     m = temp * tmp2;
-                    if (xs - P.p[2] >= 2.0 * mxd) { vx = P.p[6]; vy = P.p[7]; }
-                }
-            } else if (P.type == PRIM_HINGE) {
-                const double ddx = xi - P.p[0], ddy = yj - P.p[1];
-                const double Rr = sqrt(ddx * ddx + ddy * ddy);
-                if (Rr <= t_star) {
-                    const double gamma = convert_angle(atan2(ddy, ddx), a.pi) * 180.0 / a.pi;
-                    const double beta1 = P.p[2], beta2 = P.p[3];
-                    bool in1 = false, in2 = false;
-                    if (beta1 < 90.0) {
-                        if ((gamma >= 0.0 && gamma <= 90.0 + beta1) || (gamma >= 270.0 + beta1 && gamma <= 360.0)) in1 = true;
-                    } else if (beta1 >= 90.0 && beta1 < 270.0) {
-                        if (gamma >= 270.0 + beta1 - 360.0 && gamma <= 90.0 + beta1) in1 = true;
-                    } else if (beta1 >= 270.0) {
-                        if ((gamma >= 0.0 && gamma <= 90.0 + beta1 - 360.0) || (gamma >= 270.0 + beta1 - 360.0 && gamma <= 360.0)) in1 = true;
-                    }
-                    if (beta2 <= 90.0) {
-                        if (gamma >= 90.0 + beta2 && gamma < 270.0 + beta2) in2 = true;
-                    } else if (beta2 >= 90.0 && beta2 < 270.0) {
-                        if ((gamma >= 0.0 && gamma <= 270.0 + beta2 - 360.0) || (gamma >= 90.0 + beta2 && gamma <= 360.0)) in2 = true;
-                    } else if (beta2 >= 270.0) {
-                        if (gamma >= 90.0 + beta2 - 360.0 && gamma < 270.0 + beta2 - 360.0) in2 = true;
-                    }
-                    if (in1 && in2) {
-                        const double temp = smooth_step(Rr, t, h, a.sharp, gerf);
-                        if (temp > m) { m = temp; vx = P.p[4]; vy = P.p[5]; }
-                    }
+                    if (xs - Q.p[2] >= 2.0 * mxd) { vx = Q.p[6]; vy = Q.p[7]; }
                 }
             } else {
-                const double ddx = xi - P.p[0], ddy = yj - P.p[1];
+                const float ex = xf - F.a.x, ey = yf - F.a.y;
+                if (ex * ex + ey * ey > F.a.z) continue;
+                const double ddx = xi - Q.p[0], ddy = yj - Q.p[1];
                 const double Rr = sqrt(ddx * ddx + ddy * ddy);
-                const double temp = smooth_step(Rr, t, h, a.sharp, gerf);
-                if (temp > m) { m = temp; vx = P.p[2]; vy = P.p[3]; }
+                if (Q.type == PRIM_HINGE) {
+                    if (Rr <= t_star) {
+                        const double gamma = convert_angle(atan2(ddy, ddx), a.pi) * 180.0 / a.pi;
+                        const double beta1 = Q.p[2], beta2 = Q.p[3];
+                        bool in1 = false, in2 = false;
+                        if (beta1 < 90.0) {
+                            if ((gamma >= 0.0 && gamma <= 90.0 + beta1) || (gamma >= 270.0 + beta1 && gamma <= 360.0)) in1 = true;
+                        } else if (beta1 >= 90.0 && beta1 < 270.0) {
+                            if (gamma >= 270.0 + beta1 - 360.0 && gamma <= 90.0 + beta1) in1 = true;
+                        } else if (beta1 >= 270.0) {
+                            if ((gamma >= 0.0 && gamma <= 90.0 + beta1 - 360.0) || (gamma >= 270.0 + beta1 - 360.0 && gamma <= 360.0)) in1 = true;
+                        }
+                        if (beta2 <= 90.0) {
+                            if (gamma >= 90.0 + beta2 && gamma < 270.0 + beta2) in2 = true;
+                        } else if (beta2 >= 90.0 && beta2 < 270.0) {
+                            if ((gamma >= 0.0 && gamma <= 270.0 + beta2 - 360.0) || (gamma >= 90.0 + beta2 && gamma <= 360.0)) in2 = true;
+                        } else if (beta2 >= 270.0) {
+                            if (gamma >= 90.0 + beta2 - 360.0 && gamma < 270.0 + beta2 - 360.0) in2 = true;
+                        }
+                        if (in1 && in2) {
+                            const double temp = smooth_step(Rr, t, h, a.sharp, gerf);
+                            if (temp > m) { m = temp; vx = Q.p[4]; vy = Q.p[5]; }
+                        }
+                    }
+                } else {
+                    const double temp = smooth_step(Rr, t, h, a.sharp, gerf);
+                    if (temp > m) { m = temp; vx = Q.p[2]; vy = Q.p[3]; }
+                }
             }
         }
         __syncthreads();
@@ -325,17 +358,20 @@ __global__ void __launch_bounds__(128) k_forces(ForceArgs a, double dxi, double 
         } else soft = 1.0;
         a.p_new[n] = pb * soft;
         a.tau_new[n] = tb * soft;
+        // this node's term of the force integral (BeamForces.f90:264-267), summed below in order
+        const double pn = pb * soft, tn = tb * soft;
+        a.fterm[2 * n] = (sin(thn) * pn + cos(thn) * tn) * a.ds;
+        a.fterm[2 * n + 1] = (cos(thn) * pn + sin(thn) * tn) * a.ds;
         __threadfence();
         const unsigned done = atomicAdd(a.counter, 1u);
         if (done == (unsigned)a.ns - 1) {
-            // last block: Force_press (BeamForces.f90:261-270), sequential like the reference
+            // last block: Force_press = the sequential sum of the node terms, like the reference
             __threadfence();
+            const volatile double* ft = a.fterm;
             double fx = 0.0, fy = 0.0;
             for (int i = 0; i < a.ns; ++i) {
-                const double th = a.th[i] + alpha;
-                const double pi_ = ((volatile double*)a.p_new)[i], ti = ((volatile double*)a.tau_new)[i];
-                fx = fx - (sin(th) * pi_ + cos(th) * ti) * a.ds;
-                fy = fy + (cos(th) * pi_ + sin(th) * ti) * a.ds;
+                fx = fx - ft[2 * i];
+                fy = fy + ft[2 * i + 1];
             }
             a.S->force_press[0] = fx;
             a.S->force_press[1] = fy;
@@ -360,36 +396,46 @@ __constant__ double cD4[3][7] = {{35.0 / 6., -31., 137.0 / 2., -242.0 / 3., 107.
                                  {1., -4., 6., -4., 1., 0., 0.}};
 
 namespace {
-__device__ double d1d(const double* f, int N, double dx, int order, int i) {
-    const int L = N - 1;
-    const double* cf;
-    int j0, len;
-    double den;
-    if (order == 1) {
-        den = 2.0 * dx;
-        if (i == 0) { cf = cD1[0]; j0 = 0; len = 3; }
-        else if (i == L) { cf = cD1[1]; j0 = L - 2; len = 3; }
-        else { cf = cD1[2]; j0 = i - 1; len = 3; }
-    } else if (order == 2) {
-        den = dx * dx;
-        if (i == 0) { cf = cD2[0]; j0 = 0; len = 4; }
-        else if (i == L) { cf = cD2[1]; j0 = L - 3; len = 4; }
-        else { cf = cD2[2]; j0 = i - 1; len = 3; }
-    } else if (order == 3) {
-        den = 2.0 * (dx * dx * dx);
-        if (i == 0 || i == 1) { cf = cD3[0]; j0 = i; len = 6; }
-        else if (i == L - 1) { cf = cD3[1]; j0 = L - 6; len = 6; }
-        else if (i == L) { cf = cD3[1]; j0 = L - 5; len = 6; }
-        else { cf = cD3[2]; j0 = i - 2; len = 5; }
-    } else {
-        den = (dx * dx) * (dx * dx);
-        if (i == 0 || i == 1) { cf = cD4[0]; j0 = i; len = 7; }
-        else if (i == L - 1) { cf = cD4[1]; j0 = L - 7; len = 7; }
-        else if (i == L) { cf = cD4[1]; j0 = L - 6; len = 7; }
-        else { cf = cD4[2]; j0 = i - 2; len = 5; }
+// The coefficient tables divided once by 2dx / dx^2 / 2dx^3 / dx^4: tab[order-1][row type][q]
+struct D1DTab {
+    double c[4][3][8];
+};
+
+__device__ void d1d_tables(D1DTab* t, double dx) {
+    const double den[4] = {2.0 * dx, dx * dx, 2.0 * (dx * dx * dx), (dx * dx) * (dx * dx)};
+    for (int e = threadIdx.x; e < 4 * 3 * 8; e += blockDim.x) {
+        const int o = e / 24, r = (e / 8) % 3, q = e % 8;
+        double v = 0.0;
+        if (o == 0 && q < 3) v = cD1[r][q];
+        else if (o == 1 && q < 4) v = cD2[r][q];
+        else if (o == 2 && q < 6) v = cD3[r][q];
+        else if (o == 3 && q < 7) v = cD4[r][q];
+        t->c[o][r][q] = v / den[o];
     }
+}
+
+__device__ double d1d(const D1DTab* tab, const double* f, int N, int order, int i) {
+    const int L = N - 1;
+    int rt, j0, len;
+    if (order == 1) {
+        len = 3;
+        if (i == 0) { rt = 0; j0 = 0; } else if (i == L) { rt = 1; j0 = L - 2; } else { rt = 2; j0 = i - 1; }
+    } else if (order == 2) {
+        if (i == 0) { rt = 0; j0 = 0; len = 4; } else if (i == L) { rt = 1; j0 = L - 3; len = 4; } else { rt = 2; j0 = i - 1; len = 3; }
+    } else if (order == 3) {
+        if (i == 0 || i == 1) { rt = 0; j0 = i; len = 6; }
+        else if (i == L - 1) { rt = 1; j0 = L - 6; len = 6; }
+        else if (i == L) { rt = 1; j0 = L - 5; len = 6; }
+        else { rt = 2; j0 = i - 2; len = 5; }
+    } else {
+        if (i == 0 || i == 1) { rt = 0; j0 = i; len = 7; }
+        else if (i == L - 1) { rt = 1; j0 = L - 7; len = 7; }
+        else if (i == L) { rt = 1; j0 = L - 6; len = 7; }
+        else { rt = 2; j0 = i - 2; len = 5; }
+    }
+    const double* cf = tab->c[order - 1][rt];
     double s = 0.0;
-    for (int q = 0; q < len; ++q) s += (cf[q] / den) * f[j0 + q];
+    for (int q = 0; q < len; ++q) s += cf[q] * f[j0 + q];
     return s;
 }
 
@@ -401,6 +447,7 @@ struct BeamWS {
     double *g5, *x, *F, *xd, *xdi, *bvec, *cs, *pre;  // x/F/xd/xdi/bvec length n; cs/pre length 4*(ns+8)
     double* band;   // n x 16: original band rows (15 used), overwritten in place by the U rows
     int* ipiv;
+    const D1DTab* dtab;
 };
 
 __device__ BeamWS carve(double* p, int ns) {
@@ -440,44 +487,30 @@ __device__ void solid_coeffs(int method, double dt, double dt_old, double& C1, d
     }
 }
 
-// LAPACK dgttrf + dgtts2 (one thread). Returns non-zero on a zero pivot.
+// LAPACK dgttrf + dgtts2 (one thread), with each division replaced by a correctly rounded
+// reciprocal and a multiplication (the serial chain is FP64-latency bound on this chip).
+// Returns non-zero on a zero pivot.
 __device__ int gttrf_solve(int n, double* dl, double* d, double* du, double* du2, int* ipiv, double* b) {
     for (int i = 0; i < n; ++i) ipiv[i] = i;
     for (int i = 0; i < n - 2; ++i) du2[i] = 0.0;
-    for (int i = 0; i < n - 2; ++i) {
+    for (int i = 0; i < n - 1; ++i) {
         if (fabs(d[i]) >= fabs(dl[i])) {
             if (d[i] != 0.0) {
-                const double fact = dl[i] / d[i];
+                const double fact = dl[i] * __drcp_rn(d[i]);
                 dl[i] = fact;
                 d[i + 1] = d[i + 1] - fact * du[i];
             }
         } else {
-            const double fact = d[i] / dl[i];
+            const double fact = d[i] * __drcp_rn(dl[i]);
             d[i] = dl[i];
             dl[i] = fact;
             const double temp = du[i];
             du[i] = d[i + 1];
             d[i + 1] = temp - fact * d[i + 1];
-            du2[i] = du[i + 1];
-            du[i + 1] = -fact * du[i + 1];
-            ipiv[i] = i + 1;
-        }
-    }
-    if (n > 1) {
-        const int i = n - 2;
-        if (fabs(d[i]) >= fabs(dl[i])) {
-            if (d[i] != 0.0) {
-                const double fact = dl[i] / d[i];
-                dl[i] = fact;
-                d[i + 1] = d[i + 1] - fact * du[i];
+            if (i < n - 2) {
+                du2[i] = du[i + 1];
+                du[i + 1] = -fact * du[i + 1];
             }
-        } else {
-            const double fact = d[i] / dl[i];
-            d[i] = dl[i];
-            dl[i] = fact;
-            const double temp = du[i];
-            du[i] = d[i + 1];
-            d[i + 1] = temp - fact * d[i + 1];
             ipiv[i] = i + 1;
         }
     }
@@ -487,9 +520,9 @@ __device__ int gttrf_solve(int n, double* dl, double* d, double* du, double* du2
         if (ipiv[i] == i) b[i + 1] = b[i + 1] - dl[i] * b[i];
         else { const double temp = b[i]; b[i] = b[i + 1]; b[i + 1] = temp - dl[i] * b[i]; }
     }
-    b[n - 1] = b[n - 1] / d[n - 1];
-    if (n > 1) b[n - 2] = (b[n - 2] - du[n - 2] * b[n - 1]) / d[n - 2];
-    for (int i = n - 3; i >= 0; --i) b[i] = (b[i] - du[i] * b[i + 1] - du2[i] * b[i + 2]) / d[i];
+    b[n - 1] = b[n - 1] * __drcp_rn(d[n - 1]);
+    if (n > 1) b[n - 2] = (b[n - 2] - du[n - 2] * b[n - 1]) * __drcp_rn(d[n - 2]);
+    for (int i = n - 3; i >= 0; --i) b[i] = (b[i] - du[i] * b[i + 1] - du2[i] * b[i + 2]) * __drcp_rn(d[i]);
     return 0;
 }
 
@@ -501,10 +534,10 @@ __device__ int tension(const BeamArgs& b, BeamWS& w, double* T, double* T_s, con
     const double alpha = b.angle_deg * b.pi / 180.0, alpha_t = 0.0;
     const double LE4 = 0.0, LE5 = 0.0;  // leading-edge accelerations, mouvement case 0
     for (int i = threadIdx.x; i < ns; i += blockDim.x) {
-        w.th_s[i] = d1d(th, ns, ds, 1, i);
-        w.th_ss[i] = d1d(th, ns, ds, 2, i);
-        w.th_sss[i] = d1d(th, ns, ds, 3, i);
-        w.tau_s[i] = d1d(tau, ns, ds, 1, i);
+        w.th_s[i] = d1d(w.dtab, th, ns, 1, i);
+        w.th_ss[i] = d1d(w.dtab, th, ns, 2, i);
+        w.th_sss[i] = d1d(w.dtab, th, ns, 3, i);
+        w.tau_s[i] = d1d(w.dtab, tau, ns, 1, i);
     }
     __syncthreads();
     const double K1 = mue * (LE4 * cos(alpha) + LE5 * sin(alpha) + grav * sin(alpha)) - tau[0];
@@ -532,7 +565,7 @@ __device__ int tension(const BeamArgs& b, BeamWS& w, double* T, double* T_s, con
     __syncthreads();
     for (int i = threadIdx.x; i < ns; i += blockDim.x) T[i] = w.rhs[i];
     __syncthreads();
-    for (int i = threadIdx.x; i < ns; i += blockDim.x) T_s[i] = (i == 0) ? T_s0 : d1d(T, ns, ds, 1, i);
+    for (int i = threadIdx.x; i < ns; i += blockDim.x) T_s[i] = (i == 0) ? T_s0 : d1d(w.dtab, T, ns, 1, i);
     __syncthreads();
     return info;
 }
@@ -561,10 +594,10 @@ __device__ int rhs_beameqn(const BeamArgs& b, BeamWS& w, double* th, double* thd
     for (int i = threadIdx.x; i < ns; i += blockDim.x) w.te[i + 1] = th[i];
     __syncthreads();
     for (int i = threadIdx.x; i < ns; i += blockDim.x) {
-        w.te_s[i + 1] = d1d(w.te, ns + 3, ds, 1, i + 1);
-        w.te_ss[i + 1] = d1d(w.te, ns + 3, ds, 2, i + 1);
-        w.te_ssss[i + 1] = d1d(w.te, ns + 3, ds, 4, i + 1);
-        w.p_s[i] = d1d(p, ns, ds, 1, i);
+        w.te_s[i + 1] = d1d(w.dtab, w.te, ns + 3, 1, i + 1);
+        w.te_ss[i + 1] = d1d(w.dtab, w.te, ns + 3, 2, i + 1);
+        w.te_ssss[i + 1] = d1d(w.dtab, w.te, ns + 3, 4, i + 1);
+        w.p_s[i] = d1d(w.dtab, p, ns, 1, i);
     }
     __syncthreads();
     for (int i = threadIdx.x; i < ns; i += blockDim.x) {
@@ -617,63 +650,78 @@ __device__ __forceinline__ int row_of(int ns, int k) {
 
 struct NewtonCtx {
     double time, dt, dt_old, C1, C2, C3, C4, D, K1, K2, alpha_t, alpha_tt, grav;
+    // reciprocal constants: the device evaluates F and J with multiplications only
+    double i2ds, ids, ids2, i2ds2, ids4, e2ds3, eds4, e2ds4, g, gds2, gds4e, mue2;
 };
+
+__device__ void newton_consts(NewtonCtx& c, double ds, double eta, double mue) {
+    const double ds2 = ds * ds, ds3 = ds * ds * ds, ds4 = (ds * ds) * (ds * ds);
+    c.ids = 1.0 / ds;
+    c.i2ds = 1.0 / (2.0 * ds);
+    c.ids2 = 1.0 / ds2;
+    c.i2ds2 = 1.0 / (2.0 * ds2);
+    c.ids4 = 1.0 / ds4;
+    c.e2ds3 = eta / (2.0 * ds3);
+    c.eds4 = eta / ds4;
+    c.e2ds4 = eta / (2.0 * ds4);
+    c.g = c.dt / (c.C1 * mue);
+    c.gds2 = c.dt / (c.C1 * mue * ds2);
+    c.gds4e = c.dt * eta / (c.C1 * mue * ds4);
+    c.mue2 = mue * mue;
+}
 
 // F_nonlinear (SolidSolver.f90:552-667) equation k (1-based) at x (Fortran order).
 __device__ double f_eq(const BeamArgs& b, const BeamWS& w, const NewtonCtx& c, int k) {
     const int ns = b.ns;
-    const double ds = b.ds, eta = b.eta, mue = b.mue, sigma = b.sigma;
+    const double eta = b.eta, mue = b.mue, sigma = b.sigma;
     const double* x = w.x;
     const double* p = b.p_new;
     const double* tau = b.tau_new;
     auto TH = [&](int j) { return x[j + 1]; };
     auto TT = [&](int j) { return x[ns + 4 + j]; };
-    const double ds2 = ds * ds, ds3 = ds * ds * ds, ds4 = (ds * ds) * (ds * ds);
     switch (k) {
         case 1: return TH(0);
-        case 2: return (TT(1) - TT(-1)) / (2.0 * ds) + (eta / (2.0 * ds3)) * (TH(-1) - 2.0 * TH(0) + TH(1)) * (TH(1) - TH(-1)) - c.K1;
-        case 3: return TT(0) * (TH(1) - TH(-1)) / (2.0 * ds) - (eta / (2.0 * ds3)) * (-3.0 * TH(-1) + 10.0 * TH(0) - 12.0 * TH(1) + 6.0 * TH(2) - TH(3)) - c.K2;
-        case 4: return ((1.0 / 12.0) * TH(ns - 3) - (2.0 / 3.0) * TH(ns - 2) + (2.0 / 3.0) * TH(ns) - (1.0 / 12.0) * TH(ns + 1)) / ds;
-        case 5: return ((-1.0 / 12.0) * TH(ns - 3) + (4.0 / 3.0) * TH(ns - 2) - 2.5 * TH(ns - 1) + (4.0 / 3.0) * TH(ns) + (-1.0 / 12.0) * TH(ns + 1)) / ds2;
+        case 2: return (TT(1) - TT(-1)) * c.i2ds + c.e2ds3 * (TH(-1) - 2.0 * TH(0) + TH(1)) * (TH(1) - TH(-1)) - c.K1;
+        case 3: return TT(0) * (TH(1) - TH(-1)) * c.i2ds - c.e2ds3 * (-3.0 * TH(-1) + 10.0 * TH(0) - 12.0 * TH(1) + 6.0 * TH(2) - TH(3)) - c.K2;
+        case 4: return ((1.0 / 12.0) * TH(ns - 3) - (2.0 / 3.0) * TH(ns - 2) + (2.0 / 3.0) * TH(ns) - (1.0 / 12.0) * TH(ns + 1)) * c.ids;
+        case 5: return ((-1.0 / 12.0) * TH(ns - 3) + (4.0 / 3.0) * TH(ns - 2) - 2.5 * TH(ns - 1) + (4.0 / 3.0) * TH(ns) + (-1.0 / 12.0) * TH(ns + 1)) * c.ids2;
         case 6: return TT(ns - 1);
         case 7: {
-            const double d1 = (TH(1) - TH(-1)) / (2.0 * ds);
-            const double lap = (TH(1) - 2.0 * TH(0) + TH(-1)) / ds2;
+            const double d1 = (TH(1) - TH(-1)) * c.i2ds;
+            const double lap = (TH(1) - 2.0 * TH(0) + TH(-1)) * c.ids2;
             const double wv = w.tdn[0] + c.alpha_t;
-            return (TT(-1) - 2.0 * TT(0) + TT(1)) / ds2 - TT(0) * (d1 * d1) + p[0] * d1 +
-                   (eta / ds4) * (TH(1) - TH(-1)) * (-2.5 * TH(0) + 9.0 * TH(1) - 12.0 * TH(2) + 7.0 * TH(3) - 1.5 * TH(4)) +
+            return (TT(-1) - 2.0 * TT(0) + TT(1)) * c.ids2 - TT(0) * (d1 * d1) + p[0] * d1 +
+                   c.eds4 * (TH(1) - TH(-1)) * (-2.5 * TH(0) + 9.0 * TH(1) - 12.0 * TH(2) + 7.0 * TH(3) - 1.5 * TH(4)) +
                    eta * (lap * lap) + mue * (wv * wv) - w.taun_s[0];
         }
         case 8: {
             const int m = ns - 1;
-            const double d1 = (TH(ns) - TH(ns - 2)) / (2. * ds);
+            const double d1 = (TH(ns) - TH(ns - 2)) * c.i2ds;
             return c.C3 * w.bo6[m] + c.C4 * w.oo6[m] - w.tdn[m] +
-                   (c.dt / (c.C1 * mue)) *
-                       (-(3. * p[m] - 4. * p[m - 1] + p[m - 2]) / (2. * ds) -
-                        eta * (TH(ns + 1) - 4. * TH(ns) + 6. * TH(ns - 1) - 4. * TH(ns - 2) + TH(ns - 3)) / ds4 +
-                        (TT(m) + eta * (d1 * d1)) * (TH(ns) - 2. * TH(ns - 1) + TH(ns - 2)) / ds2 +
-                        (3. * TT(m) - 4. * TT(m - 1) + TT(m - 2)) * (TH(ns) - TH(ns - 2)) / (2. * ds2) - c.alpha_tt * (mue * mue) -
-                        sigma * w.tdn[m] + tau[m] * (TH(ns) - TH(ns - 2)) / (2.0 * ds) + c.C2 * mue * w.old_rhs[m]);
+                   c.g * (-(3. * p[m] - 4. * p[m - 1] + p[m - 2]) * c.i2ds -
+                          c.eds4 * (TH(ns + 1) - 4. * TH(ns) + 6. * TH(ns - 1) - 4. * TH(ns - 2) + TH(ns - 3)) +
+                          (TT(m) + eta * (d1 * d1)) * (TH(ns) - 2. * TH(ns - 1) + TH(ns - 2)) * c.ids2 +
+                          (3. * TT(m) - 4. * TT(m - 1) + TT(m - 2)) * (TH(ns) - TH(ns - 2)) * c.i2ds2 - c.alpha_tt * c.mue2 -
+                          sigma * w.tdn[m] + tau[m] * (TH(ns) - TH(ns - 2)) * c.i2ds + c.C2 * mue * w.old_rhs[m]);
         }
         default: break;
     }
     if (k <= 8 + ns - 2) {
         const int i = k - 8;
-        const double d1 = (TH(i + 1) - TH(i - 1)) / (2. * ds);
+        const double d1 = (TH(i + 1) - TH(i - 1)) * c.i2ds;
         return c.C3 * w.bo6[i] + c.C4 * w.oo6[i] - w.tdn[i] +
-               (c.dt / (c.C1 * mue)) *
-                   (-1.0 * (p[i + 1] - p[i - 1]) / (2. * ds) -
-                    eta * (TH(i + 2) - 4. * TH(i + 1) + 6. * TH(i) - 4. * TH(i - 1) + TH(i - 2)) / ds4 +
-                    (TT(i) + eta * (d1 * d1)) * (TH(i + 1) - 2. * TH(i) + TH(i - 1)) / ds2 +
-                    (TT(i + 1) - TT(i - 1)) * (TH(i + 1) - TH(i - 1)) / (2.0 * ds2) - c.alpha_tt * (mue * mue) - sigma * w.tdn[i] +
-                    tau[i] * (TH(i + 1) - TH(i - 1)) / (2.0 * ds) + c.C2 * mue * w.old_rhs[i]);
+               c.g * (-1.0 * (p[i + 1] - p[i - 1]) * c.i2ds -
+                      c.eds4 * (TH(i + 2) - 4. * TH(i + 1) + 6. * TH(i) - 4. * TH(i - 1) + TH(i - 2)) +
+                      (TT(i) + eta * (d1 * d1)) * (TH(i + 1) - 2. * TH(i) + TH(i - 1)) * c.ids2 +
+                      (TT(i + 1) - TT(i - 1)) * (TH(i + 1) - TH(i - 1)) * c.i2ds2 - c.alpha_tt * c.mue2 - sigma * w.tdn[i] +
+                      tau[i] * (TH(i + 1) - TH(i - 1)) * c.i2ds + c.C2 * mue * w.old_rhs[i]);
     }
     const int i = k - 8 - (ns - 2);
-    const double d1b = (TH(i + 1) - TH(i - 1)) / (2.0 * ds);
-    const double lap = (TH(i + 1) - 2.0 * TH(i) + TH(i - 1)) / ds2;
+    const double d1b = (TH(i + 1) - TH(i - 1)) * c.i2ds;
+    const double lap = (TH(i + 1) - 2.0 * TH(i) + TH(i - 1)) * c.ids2;
     const double wv = w.tdn[i] + c.alpha_t;
-    return (TT(i - 1) - 2.0 * TT(i) + TT(i + 1)) / ds2 - TT(i) * (d1b * d1b) + p[i] * d1b +
-           eta * (TH(i + 1) - TH(i - 1)) * (TH(i + 2) - 2.0 * TH(i + 1) + 2.0 * TH(i - 1) - TH(i - 2)) / (2.0 * ds4) +
+    return (TT(i - 1) - 2.0 * TT(i) + TT(i + 1)) * c.ids2 - TT(i) * (d1b * d1b) + p[i] * d1b +
+           c.e2ds4 * (TH(i + 1) - TH(i - 1)) * (TH(i + 2) - 2.0 * TH(i + 1) + 2.0 * TH(i - 1) - TH(i - 2)) +
            eta * (lap * lap) + mue * (wv * wv) - w.taun_s[i];
 }
 
@@ -681,13 +729,12 @@ __device__ double f_eq(const BeamArgs& b, const BeamWS& w, const NewtonCtx& c, i
 // the band row of its interleaved position.  Returns non-zero when a NaN is produced.
 __device__ int jac_row(const BeamArgs& b, const BeamWS& w, const NewtonCtx& c, int k) {
     const int ns = b.ns;
-    const double ds = b.ds, eta = b.eta, mue = b.mue, sigma = b.sigma;
+    const double eta = b.eta, mue = b.mue, sigma = b.sigma;
     const double* x = w.x;
     const double* p = b.p_new;
     const double* tau = b.tau_new;
     auto TH = [&](int j) { return x[j + 1]; };
     auto TT = [&](int j) { return x[ns + 4 + j]; };
-    const double ds2 = ds * ds, ds3 = ds * ds * ds, ds4 = (ds * ds) * (ds * ds);
     const int row = row_of(ns, k);
     double* Ab = w.band + (size_t)row * 16;
     for (int q = 0; q < 16; ++q) Ab[q] = 0.0;
@@ -699,66 +746,69 @@ __device__ int jac_row(const BeamArgs& b, const BeamWS& w, const NewtonCtx& c, i
     };
     const int T0 = ns + 4;
     const double D = c.D;
-    const double g = c.dt / (c.C1 * mue);
+    const double g = c.g;
+    const double e2ds3 = c.e2ds3, eds4 = c.eds4;
     switch (k) {
         case 1: put(2, 1.0); return bad;
         case 2:
-            put(1, (eta / (2.0 * ds3)) * (-2.0 * TH(-1) + 2.0 * TH(0)));
-            put(2, -(eta / (ds3)) * (TH(1) - TH(-1)));
-            put(3, (eta / (2.0 * ds3)) * (-2.0 * TH(0) + 2.0 * TH(1)));
-            put(T0, -0.5 / ds);
-            put(T0 + 2, 0.5 / ds);
+            put(1, e2ds3 * (-2.0 * TH(-1) + 2.0 * TH(0)));
+            put(2, -(2.0 * e2ds3) * (TH(1) - TH(-1)));
+            put(3, e2ds3 * (-2.0 * TH(0) + 2.0 * TH(1)));
+            put(T0, -0.5 * c.ids);
+            put(T0 + 2, 0.5 * c.ids);
             return bad;
         case 3:
-            put(1, (-0.5 * eta / (ds3)) * (-3.0) - TT(0) / (2.0 * ds));
-            put(2, (-0.5 * eta / (ds3)) * (10.0));
-            put(3, (-0.5 * eta / (ds3)) * (-12.0) + TT(0) / (2.0 * ds));
-            put(4, (-0.5 * eta / (ds3)) * (6.0));
-            put(5, (-0.5 * eta / (ds3)) * (-1.0));
-            put(T0 + 1, (TH(1) - TH(-1)) / (2.0 * ds));
+            put(1, -e2ds3 * (-3.0) - TT(0) * c.i2ds);
+            put(2, -e2ds3 * (10.0));
+            put(3, -e2ds3 * (-12.0) + TT(0) * c.i2ds);
+            put(4, -e2ds3 * (6.0));
+            put(5, -e2ds3 * (-1.0));
+            put(T0 + 1, (TH(1) - TH(-1)) * c.i2ds);
             return bad;
         case 4:
-            put(ns + 3, (-1.0 / 12.0) / ds);
-            put(ns + 2, (2.0 / 3.0) / ds);
-            put(ns, (-2.0 / 3.0) / ds);
-            put(ns - 1, (1.0 / 12.0) / ds);
+            put(ns + 3, (-1.0 / 12.0) * c.ids);
+            put(ns + 2, (2.0 / 3.0) * c.ids);
+            put(ns, (-2.0 / 3.0) * c.ids);
+            put(ns - 1, (1.0 / 12.0) * c.ids);
             return bad;
         case 5:
-            put(ns + 3, (-1.0 / 12.0) / ds2);
-            put(ns + 2, (4.0 / 3.0) / ds2);
-            put(ns + 1, (-5.0 / 2.0) / ds2);
-            put(ns, (4.0 / 3.0) / ds2);
-            put(ns - 1, (-1.0 / 12.0) / ds2);
+            put(ns + 3, (-1.0 / 12.0) * c.ids2);
+            put(ns + 2, (4.0 / 3.0) * c.ids2);
+            put(ns + 1, (-5.0 / 2.0) * c.ids2);
+            put(ns, (4.0 / 3.0) * c.ids2);
+            put(ns - 1, (-1.0 / 12.0) * c.ids2);
             return bad;
         case 6: put(2 * ns + 4, 1.0); return bad;
         case 7: {
             const double t1m = TH(1) - TH(-1);
             const double lap = TH(1) - 2.0 * TH(0) + TH(-1);
             const double q = -2.5 * TH(0) + 9.0 * TH(1) - 12.0 * TH(2) + 7.0 * TH(3) - 1.5 * TH(4);
-            put(1, TT(0) * t1m / (2.0 * ds2) - p[0] / (2.0 * ds) - (eta / ds4) * q + 2.0 * eta * lap / ds4);
-            put(2, -2.5 * eta * t1m / ds4 - 4.0 * eta * lap / ds4 + 2.0 * mue * (w.tdn[0] + c.alpha_t) * D);
-            put(3, -TT(0) * t1m / (2.0 * ds2) + p[0] / (2.0 * ds) + (eta / ds4) * q + 9.0 * eta * t1m / ds4 + 2.0 * eta * lap / ds4);
-            put(4, -12.0 * eta * t1m / ds4);
-            put(5, 7.0 * eta * t1m / ds4);
-            put(6, -1.5 * eta * t1m / ds4);
-            put(ns + 4, 1.0 / ds2);
-            put(ns + 5, (-2.0 - (t1m * t1m) / 4.0) / ds2);
-            put(ns + 6, 1.0 / ds2);
+            put(1, TT(0) * t1m * c.i2ds2 - p[0] * c.i2ds - eds4 * q + 2.0 * eds4 * lap);
+            put(2, -2.5 * eds4 * t1m - 4.0 * eds4 * lap + 2.0 * mue * (w.tdn[0] + c.alpha_t) * D);
+            put(3, -TT(0) * t1m * c.i2ds2 + p[0] * c.i2ds + eds4 * q + 9.0 * eds4 * t1m + 2.0 * eds4 * lap);
+            put(4, -12.0 * eds4 * t1m);
+            put(5, 7.0 * eds4 * t1m);
+            put(6, -1.5 * eds4 * t1m);
+            put(ns + 4, c.ids2);
+            put(ns + 5, (-2.0 - (t1m * t1m) * 0.25) * c.ids2);
+            put(ns + 6, c.ids2);
             return bad;
         }
         case 8: {
             const double d0 = TH(ns) - TH(ns - 2);
             const double lap = TH(ns) - 2.0 * TH(ns - 1) + TH(ns - 2);
-            const double Tp = TT(ns - 1) + eta * ((d0 / (2.0 * ds)) * (d0 / (2.0 * ds)));
+            const double h = d0 * c.i2ds;
+            const double Tp = TT(ns - 1) + eta * (h * h);
             const double Tb = 3.0 * TT(ns - 1) - 4.0 * TT(ns - 2) + TT(ns - 3);
-            put(2 * ns + 4, (c.dt / (c.C1 * mue * ds2)) * (lap + (3.0 / 2.0) * d0));
-            put(2 * ns + 3, -4.0 * g * d0 / (2.0 * ds2));
-            put(2 * ns + 2, 1.0 * g * d0 / (2.0 * ds2));
-            put(ns + 3, -c.dt * eta / ((c.C1 * mue) * ds4));
-            put(ns + 2, (c.dt / (c.C1 * mue * ds2)) * (4.0 * eta / ds2 + Tp + tau[ns - 1] * ds / (2.0) + eta * lap * d0 / (2.0 * ds2) + Tb / 2.0));
-            put(ns, (c.dt / (c.C1 * mue * ds2)) * (4.0 * eta / ds2 + Tp - tau[ns - 1] * ds / (2.0) - eta * lap * d0 / (2.0 * ds2) - Tb / 2.0));
-            put(ns + 1, -D + g * (-6.0 * eta / ds4 - 2.0 * Tp / ds2 - D * sigma));
-            put(ns - 1, -c.dt * eta / (c.C1 * mue * ds4));
+            const double ds = b.ds;
+            put(2 * ns + 4, c.gds2 * (lap + 1.5 * d0));
+            put(2 * ns + 3, -4.0 * g * d0 * c.i2ds2);
+            put(2 * ns + 2, g * d0 * c.i2ds2);
+            put(ns + 3, -c.gds4e);
+            put(ns + 2, c.gds2 * (4.0 * eta * c.ids2 + Tp + tau[ns - 1] * ds * 0.5 + eta * lap * d0 * c.i2ds2 + Tb * 0.5));
+            put(ns, c.gds2 * (4.0 * eta * c.ids2 + Tp - tau[ns - 1] * ds * 0.5 - eta * lap * d0 * c.i2ds2 - Tb * 0.5));
+            put(ns + 1, -D + g * (-6.0 * eds4 - 2.0 * Tp * c.ids2 - D * sigma));
+            put(ns - 1, -c.gds4e);
             return bad;
         }
         default: break;
@@ -767,30 +817,32 @@ __device__ int jac_row(const BeamArgs& b, const BeamWS& w, const NewtonCtx& c, i
         const int i = k - 8, l = i + 2, m = i + ns + 5;
         const double d1 = TH(i + 1) - TH(i - 1);
         const double lap = TH(i + 1) - 2.0 * TH(i) + TH(i - 1);
-        const double Tp = TT(i) + eta * ((d1 / (2.0 * ds)) * (d1 / (2.0 * ds)));
+        const double h = d1 * c.i2ds;
+        const double Tp = TT(i) + eta * (h * h);
         const double dT = TT(i + 1) - TT(i - 1);
-        put(l, -D + g * (-6.0 * eta / ds4 - (2.0 / ds2) * Tp - D * sigma));
-        put(l - 1, g * (4.0 * eta / ds4 + Tp / ds2 - tau[i] / (2.0 * ds) - eta * lap * d1 / (2.0 * ds4) - dT / (2.0 * ds2)));
-        put(l + 1, g * (4.0 * eta / ds4 + Tp / ds2 + tau[i] / (2.0 * ds) + eta * lap * d1 / (2.0 * ds4) + dT / (2.0 * ds2)));
-        put(l - 2, -eta * c.dt / (c.C1 * mue * ds4));
-        put(l + 2, -eta * c.dt / (c.C1 * mue * ds4));
-        put(m, g * lap / ds2);
-        put(m - 1, -g * d1 / (2.0 * ds2));
-        put(m + 1, g * d1 / (2.0 * ds2));
+        put(l, -D + g * (-6.0 * eds4 - (2.0 * c.ids2) * Tp - D * sigma));
+        put(l - 1, g * (4.0 * eds4 + Tp * c.ids2 - tau[i] * c.i2ds - c.e2ds4 * lap * d1 - dT * c.i2ds2));
+        put(l + 1, g * (4.0 * eds4 + Tp * c.ids2 + tau[i] * c.i2ds + c.e2ds4 * lap * d1 + dT * c.i2ds2));
+        put(l - 2, -c.gds4e);
+        put(l + 2, -c.gds4e);
+        put(m, g * lap * c.ids2);
+        put(m - 1, -g * d1 * c.i2ds2);
+        put(m + 1, g * d1 * c.i2ds2);
         return bad;
     }
     const int i = k - 8 - (ns - 2), l = i + 2, m = i + ns + 5;
     const double d1 = TH(i + 1) - TH(i - 1);
     const double lap = TH(i + 1) - 2.0 * TH(i) + TH(i - 1);
     const double q = TH(i + 2) - 2.0 * TH(i + 1) + 2.0 * TH(i - 1) - TH(i - 2);
-    put(l, -4.0 * eta * lap / ds4 + 2.0 * mue * (w.tdn[i] + c.alpha_t) * D);
-    put(l - 1, TT(i) * d1 / (2.0 * ds2) - p[i] / (2.0 * ds) + eta * d1 / ds4 - eta * q / (2.0 * ds4) + 2.0 * eta * lap / ds4);
-    put(l + 1, -TT(i) * d1 / (2.0 * ds2) + p[i] / (2.0 * ds) - eta * d1 / ds4 + eta * q / (2.0 * ds4) + 2.0 * eta * lap / ds4);
-    put(l - 2, -eta * d1 / (2.0 * ds4));
-    put(l + 2, eta * d1 / (2.0 * ds4));
-    put(m, -2.0 / ds2 - ((d1 / (2.0 * ds)) * (d1 / (2.0 * ds))));
-    put(m - 1, 1.0 / ds2);
-    put(m + 1, 1.0 / ds2);
+    const double h = d1 * c.i2ds;
+    put(l, -4.0 * eds4 * lap + 2.0 * mue * (w.tdn[i] + c.alpha_t) * D);
+    put(l - 1, TT(i) * d1 * c.i2ds2 - p[i] * c.i2ds + eds4 * d1 - c.e2ds4 * q + 2.0 * eds4 * lap);
+    put(l + 1, -TT(i) * d1 * c.i2ds2 + p[i] * c.i2ds - eds4 * d1 + c.e2ds4 * q + 2.0 * eds4 * lap);
+    put(l - 2, -c.e2ds4 * d1);
+    put(l + 2, c.e2ds4 * d1);
+    put(m, -2.0 * c.ids2 - (h * h));
+    put(m - 1, c.ids2);
+    put(m + 1, c.ids2);
     return bad;
 }
 
@@ -821,27 +873,31 @@ __device__ int band_solve(BeamWS& w, int n) {
     int info = 0;
     for (int k = 0; k < n; ++k) {
         const int pl = k & 15;
-        int p = 0;
-        if (lane == pl) {
-            double best = fabs(v[0]);
+        // the pivot column (rows k..k+7) to every lane; |v| compared as integer keys
+        double col[KL + 1];
 #pragma unroll
-            for (int r = 1; r <= KL; ++r) {
-                const double a = fabs(v[r]);
-                if (k + r < n && a > best) { best = a; p = r; }
-            }
+        for (int r = 0; r <= KL; ++r) col[r] = __shfl_sync(0xffffffffu, v[r], pl);
+        int p = 0;
+        unsigned long long best = (unsigned long long)__double_as_longlong(col[0]) & 0x7fffffffffffffffull;
+#pragma unroll
+        for (int r = 1; r <= KL; ++r) {
+            const unsigned long long a = (unsigned long long)__double_as_longlong(col[r]) & 0x7fffffffffffffffull;
+            if (k + r < n && a > best) { best = a; p = r; }
         }
-        p = __shfl_sync(0xffffffffu, p, pl);
-        double t0 = v[0];
+        double t0 = v[0], c0 = col[0];
 #pragma unroll
         for (int r = 1; r <= KL; ++r)
-            if (r == p) { const double tmp = v[r]; v[r] = t0; t0 = tmp; }
+            if (r == p) {
+                const double tmp = v[r]; v[r] = t0; t0 = tmp;
+                const double cm = col[r]; col[r] = c0; c0 = cm;
+            }
         v[0] = t0;
-        const double piv = __shfl_sync(0xffffffffu, v[0], pl);
+        const double piv = c0;
         if (piv == 0.0) { info = k + 1; break; }
-        const double rinv = 1.0 / piv;
+        const double rinv = __drcp_rn(piv);
         double l[KL + 1];
 #pragma unroll
-        for (int r = 1; r <= KL; ++r) l[r] = __shfl_sync(0xffffffffu, v[r], pl) * rinv;
+        for (int r = 1; r <= KL; ++r) l[r] = col[r] * rinv;
         const int c = (lane - k) & 15;  // offset of this lane's column from k
         if ((mat && c >= 1 && c <= 14) || rhs) {
 #pragma unroll
@@ -902,6 +958,10 @@ __global__ void __launch_bounds__(256) k_beam(BeamArgs b) {
     const double alpha = b.angle_deg * b.pi / 180.0;
     __shared__ double red[4][8];
     __shared__ int flag;
+    __shared__ D1DTab dtab;
+    d1d_tables(&dtab, b.ds);
+    w.dtab = &dtab;
+    __syncthreads();
 
     if (threadIdx.x == 0) {
         // GravityImpulse (SolidSolver.f90:874-911)
@@ -972,7 +1032,7 @@ __global__ void __launch_bounds__(256) k_beam(BeamArgs b) {
             w.x[xi_th(i)] = w.g5[i];
             w.x[xi_T(ns, i)] = w.T[i];
             w.old_rhs[i] = 0.0;
-            w.taun_s[i] = d1d(b.tau_new, ns, ds, 1, i);
+            w.taun_s[i] = d1d(w.dtab, b.tau_new, ns, 1, i);
         }
         __syncthreads();
         if (method == FSIBE_CRANK_NICHOLSON) {
@@ -985,6 +1045,7 @@ __global__ void __launch_bounds__(256) k_beam(BeamArgs b) {
         c.time = time; c.dt = dt; c.dt_old = dt_old; c.alpha_t = 0.0; c.alpha_tt = 0.0; c.grav = grav;
         solid_coeffs(method, dt, dt_old, c.C1, c.C2, c.C3, c.C4);
         c.D = c.C1 / dt;
+        newton_consts(c, ds, eta, mue);
         c.K1 = mue * (0.0 * cos(alpha) + 0.0 * sin(alpha) + grav * sin(alpha)) - b.tau_new[0];
         c.K2 = b.p_new[0] + mue * (0.0 * cos(alpha) - 0.0 * sin(alpha) + grav * cos(alpha));
         int iter = 0;
@@ -1105,7 +1166,7 @@ __global__ void __launch_bounds__(256) k_beam(BeamArgs b) {
         }
     }
     // SolidEnergies (SolidSolver.f90:76-92)
-    for (int i = threadIdx.x; i < ns; i += blockDim.x) w.T_s[i] = d1d(b.th, ns, ds, 1, i);
+    for (int i = threadIdx.x; i < ns; i += blockDim.x) w.T_s[i] = d1d(w.dtab, b.th, ns, 1, i);
     __syncthreads();
     if (threadIdx.x == 0) {
         double sk = 0, sp = 0, se = 0, sax = 0, say = 0;

@@ -31,6 +31,7 @@ struct ForceArgs {
     const void *press, *sa, *sb;   // R*[ny][nx]
     double *p_new, *tau_new;
     unsigned int* counter;  // blocks done (last block computes the force integral)
+    double* fterm;          // 2*ns per-node terms of the force integral
     int fp32;
 };
 
