@@ -7,6 +7,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -1347,3 +1348,89 @@ int fsibe_launches_per_step(fsibe_ctx* c, int* n) {
 
 }  // extern "C"
 
+// =====================================================================================
+// coftxy on caller-owned device buffers with file-scope scratch (allocates nothing)
+// =====================================================================================
+// Scratch for one forward transform: the x-transformed half spectrum T and the result S
+// (nx*ny doubles each) and the twiddle tables (ny + nx/2 + nx/2+1 complex values).
+#define FSIBE_STATIC_MAX_CELLS 65536
+#define FSIBE_STATIC_MAX_DIM 2048
+#define FSIBE_STATIC_TABLES (2 * (FSIBE_STATIC_MAX_DIM + FSIBE_STATIC_MAX_DIM / 2 + FSIBE_STATIC_MAX_DIM / 2 + 1))
+static __device__ __align__(256) double g_static_scratch[2 * FSIBE_STATIC_MAX_CELLS + FSIBE_STATIC_TABLES];
+
+namespace {
+// Device address of g_static_scratch, looked up once per device (host code may not use the
+// symbol itself: on the host it names a stand-in, not device memory).
+double* g_static_dev[128] = {};
+std::mutex g_static_mu;
+
+__global__ void k_static_twiddles(double2* twY, int ny, double2* twX, int hx, double2* twR, int nx) {
+    const int total = ny + hx + hx + 1;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+        double s, c;
+        if (i < ny) {
+            sincospi(2.0 * (double)i / (double)ny, &s, &c);
+            twY[i] = make_double2(c, -s);
+        } else if (i < ny + hx) {
+            const int m = i - ny;
+            sincospi(2.0 * (double)m / (double)hx, &s, &c);
+            twX[m] = make_double2(c, -s);
+        } else {
+            const int m = i - ny - hx;
+            sincospi(2.0 * (double)m / (double)nx, &s, &c);
+            twR[m] = make_double2(c, -s);
+        }
+    }
+}
+}  // namespace
+
+extern "C" int fsibe_coftxy_static(const double* f_dev, double* fk_dev, int32_t nx, int32_t ny, void* stream) {
+    if (!f_dev || !fk_dev) { g_err = "fsibe_coftxy_static: null buffer"; return FSIBE_ERR_PARAM; }
+    if (!pow2_ok(nx) || !pow2_ok(ny) || nx > FSIBE_STATIC_MAX_DIM || ny > FSIBE_STATIC_MAX_DIM ||
+        (long)nx * (long)ny > FSIBE_STATIC_MAX_CELLS) {
+        g_err = "fsibe_coftxy_static: nx, ny must be powers of two in [32, 2048] with nx*ny <= 65536 "
+                "(the size of its static scratch)";
+        return FSIBE_ERR_UNSUPPORTED;
+    }
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess || dev < 0 || dev >= 128) { g_err = "fsibe_coftxy_static: cudaGetDevice failed"; return FSIBE_ERR_CUDA; }
+    double* base;
+    {
+        std::lock_guard<std::mutex> lk(g_static_mu);
+        if (!g_static_dev[dev]) {
+            void* p = nullptr;
+            e = cudaGetSymbolAddress(&p, g_static_scratch);
+            if (e != cudaSuccess || !p) {
+                g_err = std::string("fsibe_coftxy_static: cudaGetSymbolAddress: ") + cudaGetErrorString(e);
+                return FSIBE_ERR_CUDA;
+            }
+            g_static_dev[dev] = static_cast<double*>(p);
+        }
+        base = g_static_dev[dev];
+    }
+    SizeKernels<double> kx, ky;
+    SizeKernels<float> fx, fy;
+    if (!get_sizes(nx, kx, fx) || !get_sizes(ny, ky, fy)) { g_err = "fsibe_coftxy_static: size"; return FSIBE_ERR_UNSUPPORTED; }
+    const int hx = nx / 2;
+    double2* T = reinterpret_cast<double2*>(base);
+    double2* Sx = reinterpret_cast<double2*>(base + FSIBE_STATIC_MAX_CELLS);
+    double2* twY = reinterpret_cast<double2*>(base + 2 * FSIBE_STATIC_MAX_CELLS);
+    double2* twX = twY + ny;
+    double2* twR = twX + hx;
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    k_static_twiddles<<<16, 256, 0, st>>>(twY, ny, twX, hx, twR, nx);
+    KArgs<double> a;
+    std::memset(&a, 0, sizeof(a));
+    a.g.nx = nx; a.g.ny = ny; a.g.hx = hx;
+    a.phys0 = const_cast<double*>(f_dev);
+    a.spec0 = T;
+    a.spec1 = Sx;
+    a.twX = twX; a.twR = twR; a.twY = twY;
+    kx.xfwd<<<ny / kx.x_rows, kx.x_threads, kx.x_smem1, st>>>(a);
+    ky.yfwd<<<hx, ky.y_threads, ky.y_smem1, st>>>(a);
+    k_pack<double><<<hx, 256, 0, st>>>(Sx, nullptr, fk_dev, nx, ny);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) { g_err = std::string("fsibe_coftxy_static: ") + cudaGetErrorString(e); return FSIBE_ERR_CUDA; }
+    return FSIBE_OK;
+}

@@ -192,6 +192,28 @@ int fsibe_launches_per_step(fsibe_ctx* ctx, int* launches);
  * launch kernels directly (0, default). */
 int fsibe_use_graph(fsibe_ctx* ctx, int enable);
 
+/* ---- forward transform without any device allocation ------------------------------
+ * No counterpart in the reference.  coftxy (the packed forward transform, same result as
+ * fsibe_fft_forward) of a device field f_dev (nx*ny FP64, (0:nx-1,0:ny-1) column-major,
+ * 16-byte aligned) into the device array fk_dev (nx*ny FP64, packed layout), on
+ * cuda_stream (NULL = the legacy stream).  It needs no context and calls no cudaMalloc,
+ * cudaFree or allocating library routine: its scratch is one file-scope device array of
+ * about 1.1 MB that every GPU loading this library holds until the process exits.
+ *
+ * Why: some callers must not allocate device memory.  A host code whose device memory is
+ * owned by a pool (a framework's caching allocator, a Fortran code that sizes every array
+ * at start-up) cannot take extra cudaMalloc'd buffers outside that budget; and a per-step
+ * loop cannot afford cudaFree, which synchronises the whole device.
+ *
+ * Limits: nx and ny powers of two in [32, 2048] with nx*ny <= 65536; larger sizes return
+ * FSIBE_ERR_UNSUPPORTED (message in fsibe_last_error(NULL)) without launching anything.
+ * The first call on a device looks up the scratch's device address
+ * (cudaGetSymbolAddress) with that device current; make that first call before any stream
+ * capture.  All calls share the one scratch array, so calls that overlap on the GPU
+ * (different streams, or different host threads) race; every call rewrites all the
+ * scratch it reads, so nothing carries over from the previous call. */
+int fsibe_coftxy_static(const double* f_dev, double* fk_dev, int32_t nx, int32_t ny, void* cuda_stream);
+
 #ifdef __cplusplus
 }
 #endif
