@@ -28,7 +28,7 @@ void launch_mask(const MaskArgs& a, double gerf, bool fp32, cudaStream_t st);
 void launch_forces(const ForceArgs& a, double dxi, double dyi, cudaStream_t st);
 void launch_beam(const BeamArgs& b, cudaStream_t st);
 void launch_init_beam(const BeamArgs& b, cudaStream_t st);
-bool beam_smem_setup(int ns);
+int beam_smem_setup(int ns);
 
 static bool get_sizes(int N, SizeKernels<double>& d, SizeKernels<float>& f) {
     switch (N) {
@@ -420,7 +420,7 @@ struct fsibe_ctx {
     double* dscratch2 = nullptr;  // nx*ny doubles
     double gerf = 0.0;
     double U_mean_true = 1.0;
-    bool beam_smem = false;
+    int beam_smem = 0;  // beam workspace placement (0 global, 1 FP32 factor in shared memory, 2 all)
     bool initialized = false, startup_done = false;
     bool use_graph = false, graph_ready = false;
     cudaGraphExec_t gexec = nullptr;
@@ -676,7 +676,7 @@ static BeamArgs beam_args(fsibe_ctx* c) {
     b.p_old = c->beam[B_PO]; b.p_new = c->beam[B_PN]; b.tau_old = c->beam[B_TO]; b.tau_new = c->beam[B_TN];
     b.oo = c->oo;
     b.ws = c->ws;
-    b.use_smem = c->beam_smem ? 1 : 0;
+    b.use_smem = c->beam_smem;
     return b;
 }
 
@@ -1251,6 +1251,7 @@ int fsibe_upload_beam(fsibe_ctx* c, const double* beam, const double* po, const 
     if (pn) CK(c, cudaMemcpyAsync(c->beam[B_PN], pn, 8 * ns, cudaMemcpyHostToDevice, c->stream));
     if (to) CK(c, cudaMemcpyAsync(c->beam[B_TO], to, 8 * ns, cudaMemcpyHostToDevice, c->stream));
     if (tn) CK(c, cudaMemcpyAsync(c->beam[B_TN], tn, 8 * ns, cudaMemcpyHostToDevice, c->stream));
+    CK(c, cudaMemsetAsync(&c->S->beam_fact, 0, sizeof(int32_t), c->stream));  // a new state: refactor
     CK(c, cudaStreamSynchronize(c->stream));
     return FSIBE_OK;
 }
@@ -1333,6 +1334,14 @@ int fsibe_kernel_times(fsibe_ctx* c, int nsteps, fsibe_kernel_time* out, int cap
     *count = n;
     c->prof.clear();
     return read_status(c);
+}
+
+int fsibe_beam_phase_cycles(fsibe_ctx* c, long long* out16, int reset) {
+    if (!c || !out16) return FSIBE_ERR_PARAM;
+    CK(c, cudaMemcpyAsync(out16, c->S->phase, 16 * sizeof(long long), cudaMemcpyDeviceToHost, c->stream));
+    if (reset) CK(c, cudaMemsetAsync(c->S->phase, 0, 16 * sizeof(long long), c->stream));
+    CK(c, cudaStreamSynchronize(c->stream));
+    return FSIBE_OK;
 }
 
 int fsibe_launches_per_step(fsibe_ctx* c, int* n) {

@@ -124,8 +124,34 @@ __global__ void k_mask_prep(MaskArgs a, double gerf) {
     }
 }
 
-#define MASK_TX 32
+#define MASK_TX 16
 #define MASK_TY 8
+#define MASK_NT (MASK_TX * MASK_TY)
+
+// DrawHinge's angular test (create_mask.f90:623-641): both half-circle sectors contain gamma.
+// near (optional) is set when gamma lies within `margin` degrees of an interval end.
+template <typename T>
+__device__ __forceinline__ bool hinge_inside(T gamma, T beta1, T beta2, T margin, bool* near) {
+    bool in1 = false, in2 = false;
+    auto ge = [&](T a, T b) { if (near && fabs(a - b) < margin) *near = true; return a >= b; };
+    auto le = [&](T a, T b) { if (near && fabs(a - b) < margin) *near = true; return a <= b; };
+    auto lt = [&](T a, T b) { if (near && fabs(a - b) < margin) *near = true; return a < b; };
+    if (beta1 < (T)90) {
+        if ((ge(gamma, (T)0) && le(gamma, (T)90 + beta1)) || (ge(gamma, (T)270 + beta1) && le(gamma, (T)360))) in1 = true;
+    } else if (beta1 >= (T)90 && beta1 < (T)270) {
+        if (ge(gamma, (T)270 + beta1 - (T)360) && le(gamma, (T)90 + beta1)) in1 = true;
+    } else if (beta1 >= (T)270) {
+        if ((ge(gamma, (T)0) && le(gamma, (T)90 + beta1 - (T)360)) || (ge(gamma, (T)270 + beta1 - (T)360) && le(gamma, (T)360))) in1 = true;
+    }
+    if (beta2 <= (T)90) {
+        if (ge(gamma, (T)90 + beta2) && lt(gamma, (T)270 + beta2)) in2 = true;
+    } else if (beta2 >= (T)90 && beta2 < (T)270) {
+        if ((ge(gamma, (T)0) && le(gamma, (T)270 + beta2 - (T)360)) || (ge(gamma, (T)90 + beta2) && le(gamma, (T)360))) in2 = true;
+    } else if (beta2 >= (T)270) {
+        if (ge(gamma, (T)90 + beta2 - (T)360) && lt(gamma, (T)270 + beta2 - (T)360)) in2 = true;
+    }
+    return in1 && in2;
+}
 
 // FP32 pre-test data of one primitive: a cell that fails the pre-test is outside the primitive
 // by more than the margin, so the exact FP64 test (the reference's arithmetic) is skipped.
@@ -135,7 +161,7 @@ struct PrimF {
 };
 
 template <typename R>
-__global__ void __launch_bounds__(256) k_mask_raster(MaskArgs a, double gerf) {
+__global__ void __launch_bounds__(MASK_NT) k_mask_raster(MaskArgs a, double gerf) {
     const int tx = threadIdx.x % MASK_TX, ty = threadIdx.x / MASK_TX;
     const int ix0 = blockIdx.x * MASK_TX, iy0 = blockIdx.y * MASK_TY;
     const int i = ix0 + tx, j = iy0 + ty;
@@ -149,9 +175,9 @@ __global__ void __launch_bounds__(256) k_mask_raster(MaskArgs a, double gerf) {
         mk_[cell] = (R)0; vx_[cell] = (R)0; vy_[cell] = (R)0;
         return;
     }
-    __shared__ Prim sp[256];
-    __shared__ PrimF sf[256];
-    __shared__ int wcount[8];
+    __shared__ Prim sp[MASK_NT];
+    __shared__ PrimF sf[MASK_NT];
+    __shared__ int wcount[MASK_NT / 32];
     __shared__ int nlist;
     const double dx = a.dx, dy = a.dy, mxd = fmax(dx, dy), t = a.t_beam, N = a.N_smooth;
     const double t_star = t + 2.0 * N * mxd, h = N * mxd;
@@ -162,7 +188,7 @@ __global__ void __launch_bounds__(256) k_mask_raster(MaskArgs a, double gerf) {
     double m = 0.0, vx = 0.0, vy = 0.0;
     const int total = *a.nprims;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    for (int base = 0; base < total; base += 256) {
+    for (int base = 0; base < total; base += MASK_NT) {
         const int q = base + threadIdx.x;
         bool hit = false;
         Prim P;
@@ -192,7 +218,7 @@ __global__ void __launch_bounds__(256) k_mask_raster(MaskArgs a, double gerf) {
         }
         if (threadIdx.x == 0) {
             int s = 0;
-            for (int w = 0; w < 8; ++w) s += wcount[w];
+            for (int w = 0; w < MASK_NT / 32; ++w) s += wcount[w];
             nlist = s;
         }
         __syncthreads();
@@ -229,32 +255,26 @@ __global__ void __launch_bounds__(256) k_mask_raster(MaskArgs a, double gerf) {
                 const float ex = xf - F.a.x, ey = yf - F.a.y;
                 if (ex * ex + ey * ey > F.a.z) continue;
                 const double ddx = xi - Q.p[0], ddy = yj - Q.p[1];
-                const double Rr = sqrt(ddx * ddx + ddy * ddy);
                 if (Q.type == PRIM_HINGE) {
-                    if (Rr <= t_star) {
+                    // angular wedge first: FP32 atan2 of the FP64 offsets, exact FP64 only near an end
+                    const float beta1f = (float)Q.p[2], beta2f = (float)Q.p[3];
+                    float gf = atan2f((float)ddy, (float)ddx);
+                    if (gf < 0.f) gf = 6.28318530717958647692f + gf;
+                    gf = gf * 57.2957795130823208768f;
+                    bool near = (fabsf(gf) < 1e-3f) || (fabsf(gf - 360.f) < 1e-3f) || (ddx == 0.0 && ddy == 0.0);
+                    bool inw = hinge_inside<float>(gf, beta1f, beta2f, 1e-3f, &near);
+                    if (near) {
                         const double gamma = convert_angle(atan2(ddy, ddx), a.pi) * 180.0 / a.pi;
-                        const double beta1 = Q.p[2], beta2 = Q.p[3];
-                        bool in1 = false, in2 = false;
-                        if (beta1 < 90.0) {
-                            if ((gamma >= 0.0 && gamma <= 90.0 + beta1) || (gamma >= 270.0 + beta1 && gamma <= 360.0)) in1 = true;
-                        } else if (beta1 >= 90.0 && beta1 < 270.0) {
-                            if (gamma >= 270.0 + beta1 - 360.0 && gamma <= 90.0 + beta1) in1 = true;
-                        } else if (beta1 >= 270.0) {
-                            if ((gamma >= 0.0 && gamma <= 90.0 + beta1 - 360.0) || (gamma >= 270.0 + beta1 - 360.0 && gamma <= 360.0)) in1 = true;
-                        }
-                        if (beta2 <= 90.0) {
-                            if (gamma >= 90.0 + beta2 && gamma < 270.0 + beta2) in2 = true;
-                        } else if (beta2 >= 90.0 && beta2 < 270.0) {
-                            if ((gamma >= 0.0 && gamma <= 270.0 + beta2 - 360.0) || (gamma >= 90.0 + beta2 && gamma <= 360.0)) in2 = true;
-                        } else if (beta2 >= 270.0) {
-                            if (gamma >= 90.0 + beta2 - 360.0 && gamma < 270.0 + beta2 - 360.0) in2 = true;
-                        }
-                        if (in1 && in2) {
-                            const double temp = smooth_step(Rr, t, h, a.sharp, gerf);
-                            if (temp > m) { m = temp; vx = Q.p[4]; vy = Q.p[5]; }
-                        }
+                        inw = hinge_inside<double>(gamma, Q.p[2], Q.p[3], 0.0, nullptr);
+                    }
+                    if (!inw) continue;
+                    const double Rr = sqrt(ddx * ddx + ddy * ddy);
+                    if (Rr <= t_star) {
+                        const double temp = smooth_step(Rr, t, h, a.sharp, gerf);
+                        if (temp > m) { m = temp; vx = Q.p[4]; vy = Q.p[5]; }
                     }
                 } else {
+                    const double Rr = sqrt(ddx * ddx + ddy * ddy);
                     const double temp = smooth_step(Rr, t, h, a.sharp, gerf);
                     if (temp > m) { m = temp; vx = Q.p[2]; vy = Q.p[3]; }
                 }
@@ -445,12 +465,32 @@ struct BeamWS {
     double *te, *te_s, *te_ss, *te_ssss;  // ns+3
     double *p_s, *th1, *td1, *td_in, *old_rhs, *tdn, *taun_s, *bo3, *bo4, *bo5, *bo6, *oo5, *oo6;
     double *g5, *x, *F, *xd, *xdi, *bvec, *cs, *pre;  // x/F/xd/xdi/bvec length n; cs/pre length 4*(ns+8)
-    double* band;   // n x 16: original band rows (15 used), overwritten in place by the U rows
+    float* tf;      // 6 (ns+8) floats: FP32 scratch of the tridiagonal solve
+    double* band;   // n x 16: Jacobian band rows (15 used), FP64, kept for the residuals
     int* ipiv;
+    // FP32 factor (shared memory when it fits): U rows [1/u_kk, u_k,k+1 .. u_k,k+14, -],
+    // L rows [pivot offset (int bits), l_1 .. l_7], the biased exponents e of the row maxima
+    // (row scale 2^(1023-e)), and the solve vector
+    float *Uf, *Lf, *yf;
+    int* rse;
     const D1DTab* dtab;
 };
 
-__device__ BeamWS carve(double* p, int ns) {
+// The workspace has three parts: the FP64 vectors, the FP64 Jacobian band, the FP32 factor.
+__host__ __device__ inline size_t beam_vec_doubles(int ns) {
+    const int n = 2 * ns + 4, L = ns + 8;
+    const size_t d = (size_t)29 * L + 5 * (size_t)(n + 8) + 11 * (size_t)L + (size_t)L + 64;
+    return (d + 1) & ~(size_t)1;
+}
+__host__ __device__ inline size_t beam_band_doubles(int ns) { return (size_t)(2 * ns + 4 + 16) * 16; }
+__host__ __device__ inline size_t beam_f32_floats_(int ns) {
+    const int n = 2 * ns + 4;
+    return ((size_t)(n + 16) * 16 + (size_t)(n + 16) * 8 + 2 * (size_t)(n + 16) + 3) & ~(size_t)3;
+}
+// Floats of the FP32 factor that persist between steps (U, L, row exponents).
+__host__ __device__ inline size_t beam_fact_floats(int ns) { return ((size_t)(2 * ns + 4 + 16) * 25 + 3) & ~(size_t)3; }
+
+__device__ BeamWS carve(double* p, double* band, float* f, int ns) {
     const int n = 2 * ns + 4, L = ns + 8;
     BeamWS w;
     double** one[] = {&w.T, &w.T_s, &w.th_s, &w.th_ss, &w.th_sss, &w.tau_s, &w.dmain, &w.dup, &w.ddown, &w.rhs, &w.du2,
@@ -461,16 +501,20 @@ __device__ BeamWS carve(double* p, int ns) {
     for (unsigned k = 0; k < sizeof(nn) / sizeof(nn[0]); ++k) { *nn[k] = p; p += n + 8; }
     w.cs = p; p += 4 * L;
     w.pre = p; p += 4 * L;
-    w.band = p; p += (size_t)(n + 16) * 16;
+    w.tf = reinterpret_cast<float*>(p); p += 3 * L;
     w.ipiv = reinterpret_cast<int*>(p);
+    w.band = band;
+    w.Uf = f; f += (size_t)(n + 16) * 16;
+    w.Lf = f; f += (size_t)(n + 16) * 8;
+    w.rse = reinterpret_cast<int*>(f); f += n + 16;
+    w.yf = f;
     return w;
 }
 }  // namespace
 
-// Workspace length (doubles) the beam kernel needs for ns nodes.
+// Workspace length (doubles) of the global copy of the beam workspace for ns nodes.
 __host__ size_t beam_ws_doubles(int ns) {
-    const int n = 2 * ns + 4, L = ns + 8;
-    return (size_t)29 * L + 5 * (size_t)(n + 8) + 8 * (size_t)L + (size_t)(n + 16) * 16 + (size_t)L + 64;
+    return beam_vec_doubles(ns) + beam_band_doubles(ns) + (beam_f32_floats_(ns) + 1) / 2;
 }
 
 namespace {
@@ -487,42 +531,137 @@ __device__ void solid_coeffs(int method, double dt, double dt_old, double& C1, d
     }
 }
 
-// LAPACK dgttrf + dgtts2 (one thread), with each division replaced by a correctly rounded
-// reciprocal and a multiplication (the serial chain is FP64-latency bound on this chip).
-// Returns non-zero on a zero pivot.
-__device__ int gttrf_solve(int n, double* dl, double* d, double* du, double* du2, int* ipiv, double* b) {
-    for (int i = 0; i < n; ++i) ipiv[i] = i;
-    for (int i = 0; i < n - 2; ++i) du2[i] = 0.0;
-    for (int i = 0; i < n - 1; ++i) {
-        if (fabs(d[i]) >= fabs(dl[i])) {
-            if (d[i] != 0.0) {
-                const double fact = dl[i] * __drcp_rn(d[i]);
-                dl[i] = fact;
-                d[i + 1] = d[i + 1] - fact * du[i];
+// One pass of an FP64 iterative refinement driven by an FP32 solve (block-cooperative):
+// x += c for the FP32 correction c in cf, then the block maxima of |c| and |x| decide.
+// Returns 1 when converged (the correction, or the next one predicted from the contraction
+// c_k / c_(k-1), is below 2^-44 of the solution, or the corrections stopped shrinking at the
+// FP64 residual's rounding floor below 2^-30), -1 on a failure (10 passes, or a stall above
+// that floor), 0 to go on.  rbuf: 16 doubles of shared memory.
+__device__ int refine_step(double* x, const float* cf, int n, int pass, float& cprev, double* rbuf) {
+    unsigned cm = 0;
+    unsigned long long xm = 0;
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+        const float ck = cf[k];
+        const double xn = (pass == 0) ? (double)ck : x[k] + (double)ck;
+        x[k] = xn;
+        const unsigned a = __float_as_uint(ck) & 0x7fffffffu;
+        const unsigned long long ax = (unsigned long long)__double_as_longlong(xn) & 0x7fffffffffffffffull;
+        cm = (a > cm) ? a : cm;
+        xm = (ax > xm) ? ax : xm;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned c2 = __shfl_xor_sync(0xffffffffu, cm, o);
+        const unsigned long long x2 = __shfl_xor_sync(0xffffffffu, xm, o);
+        cm = (c2 > cm) ? c2 : cm;
+        xm = (x2 > xm) ? x2 : xm;
+    }
+    if ((threadIdx.x & 31) == 0) {
+        rbuf[threadIdx.x >> 5] = __longlong_as_double((long long)cm);
+        rbuf[8 + (threadIdx.x >> 5)] = __longlong_as_double((long long)xm);
+    }
+    __syncthreads();
+    for (int q = 0; q < (int)(blockDim.x >> 5); ++q) {
+        const unsigned c2 = (unsigned)__double_as_longlong(rbuf[q]);
+        const unsigned long long x2 = (unsigned long long)__double_as_longlong(rbuf[8 + q]);
+        cm = (c2 > cm) ? c2 : cm;
+        xm = (x2 > xm) ? x2 : xm;
+    }
+    const double cmd = (double)__uint_as_float(cm), cpd = (double)cprev;
+    const double xmd = __longlong_as_double((long long)xm);
+    const double tol = 0x1p-44 * xmd;
+    const bool conv = !(cmd > tol) || (pass >= 1 && cmd * cmd <= tol * cpd);
+    const bool stall = pass >= 2 && cmd > 0.5 * cpd;
+    cprev = __uint_as_float(cm);
+    __syncthreads();
+    if (conv || (stall && cmd <= 0x1p-30 * xmd)) return 1;
+    if (stall || pass >= 9) return -1;
+    return 0;
+}
+
+// Tridiagonal system (dl, d, du) x = b (dl, du: n-1 entries) solved to the accuracy of
+// LAPACK dgttrf + dgttrs: dgttrf's elimination with partial pivoting, in FP32 on one thread,
+// preconditions an FP64 iterative refinement with block-cooperative residuals.  fs: 5n
+// floats of scratch, ip: n ints.  Returns non-zero on an exactly zero pivot.
+__device__ int tri_solve(int n, const double* dl, const double* d, const double* du, const double* b, double* x,
+                         float* fs, int* ip) {
+    float* __restrict__ fl = fs;
+    float* __restrict__ fd = fs + n;
+    float* __restrict__ fu = fs + 2 * n;
+    float* __restrict__ fu2 = fs + 3 * n;
+    float* __restrict__ fy = fs + 4 * n;
+    __shared__ int info_s;
+    __shared__ double rbuf[16];
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        fd[i] = __double2float_rn(d[i]);
+        if (i < n - 1) { fl[i] = __double2float_rn(dl[i]); fu[i] = __double2float_rn(du[i]); }
+        fu2[i] = 0.f;
+        fy[i] = __double2float_rn(b[i]);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int info = 0;
+        for (int i = 0; i < n - 1; ++i) {
+            const float di = fd[i], li = fl[i];
+            if (fabsf(di) >= fabsf(li)) {
+                ip[i] = 0;
+                if (di != 0.f) {
+                    const float f = __fmul_rn(li, __frcp_rn(di));
+                    fl[i] = f;
+                    fd[i + 1] = __fmaf_rn(-f, fu[i], fd[i + 1]);
+                }
+            } else {
+                const float f = __fmul_rn(di, __frcp_rn(li));
+                fd[i] = li;
+                fl[i] = f;
+                const float t = fu[i];
+                fu[i] = fd[i + 1];
+                fd[i + 1] = __fmaf_rn(-f, fd[i + 1], t);
+                if (i < n - 2) { fu2[i] = fu[i + 1]; fu[i + 1] = -f * fu[i + 1]; }
+                ip[i] = 1;
             }
-        } else {
-            const double fact = d[i] * __drcp_rn(dl[i]);
-            d[i] = dl[i];
-            dl[i] = fact;
-            const double temp = du[i];
-            du[i] = d[i + 1];
-            d[i + 1] = temp - fact * d[i + 1];
-            if (i < n - 2) {
-                du2[i] = du[i + 1];
-                du[i + 1] = -fact * du[i + 1];
-            }
-            ipiv[i] = i + 1;
         }
+        for (int i = 0; i < n; ++i) {
+            if (fd[i] == 0.f) { info = i + 1; break; }
+            fd[i] = __frcp_rn(fd[i]);
+        }
+        info_s = info;
     }
-    for (int i = 0; i < n; ++i)
-        if (d[i] == 0.0) return i + 1;
-    for (int i = 0; i < n - 1; ++i) {
-        if (ipiv[i] == i) b[i + 1] = b[i + 1] - dl[i] * b[i];
-        else { const double temp = b[i]; b[i] = b[i + 1]; b[i + 1] = temp - dl[i] * b[i]; }
+    __syncthreads();
+    if (info_s) return info_s;
+    float cprev = 0.f;
+    for (int pass = 0;; ++pass) {
+        if (pass > 0) {
+            for (int i = threadIdx.x; i < n; i += blockDim.x) {
+                double r = fma(-d[i], x[i], b[i]);
+                if (i > 0) r = fma(-dl[i - 1], x[i - 1], r);
+                if (i < n - 1) r = fma(-du[i], x[i + 1], r);
+                fy[i] = __double2float_rn(r);
+            }
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) {
+            float bi = fy[0];
+            for (int i = 0; i < n - 1; ++i) {
+                const float bn = fy[i + 1];
+                if (ip[i] == 0) { fy[i] = bi; bi = __fmaf_rn(-fl[i], bi, bn); }
+                else { fy[i] = bn; bi = __fmaf_rn(-fl[i], bn, bi); }
+            }
+            float x1 = __fmul_rn(bi, fd[n - 1]);
+            fy[n - 1] = x1;
+            if (n > 1) {
+                float x0 = __fmul_rn(__fmaf_rn(-fu[n - 2], x1, fy[n - 2]), fd[n - 2]);
+                fy[n - 2] = x0;
+                for (int i = n - 3; i >= 0; --i) {
+                    const float xi = __fmul_rn(__fmaf_rn(-fu2[i], x1, __fmaf_rn(-fu[i], x0, fy[i])), fd[i]);
+                    fy[i] = xi;
+                    x1 = x0;
+                    x0 = xi;
+                }
+            }
+        }
+        __syncthreads();
+        if (refine_step(x, fy, n, pass, cprev, rbuf) != 0) break;
     }
-    b[n - 1] = b[n - 1] * __drcp_rn(d[n - 1]);
-    if (n > 1) b[n - 2] = (b[n - 2] - du[n - 2] * b[n - 1]) * __drcp_rn(d[n - 2]);
-    for (int i = n - 3; i >= 0; --i) b[i] = (b[i] - du[i] * b[i + 1] - du2[i] * b[i + 2]) * __drcp_rn(d[i]);
     return 0;
 }
 
@@ -560,10 +699,7 @@ __device__ int tension(const BeamArgs& b, BeamWS& w, double* T, double* T_s, con
         w.dmain[i] = 1.0;
     }
     __syncthreads();
-    __shared__ int info;
-    if (threadIdx.x == 0) info = gttrf_solve(ns, w.ddown, w.dmain, w.dup, w.du2, w.ipiv, w.rhs);
-    __syncthreads();
-    for (int i = threadIdx.x; i < ns; i += blockDim.x) T[i] = w.rhs[i];
+    const int info = tri_solve(ns, w.ddown, w.dmain, w.dup, w.rhs, T, w.tf, w.ipiv);
     __syncthreads();
     for (int i = threadIdx.x; i < ns; i += blockDim.x) T_s[i] = (i == 0) ? T_s0 : d1d(w.dtab, T, ns, 1, i);
     __syncthreads();
@@ -846,105 +982,185 @@ __device__ int jac_row(const BeamArgs& b, const BeamWS& w, const NewtonCtx& c, i
     return bad;
 }
 
-// Banded LU with partial pivoting (dgbtrf semantics, kl = ku = 7) with the forward
-// substitution fused, then the back substitution; one warp.  Matrix: w.band rows in the
-// interleaved order (stride 16, band index col - row + 7), RHS w.bvec, solution -> w.xdi.
-// Lane c < 16 owns the window column j with j = c (mod 16), so the window never shifts
-// across lanes; lane 16 owns the right-hand side.  Registers v[r] hold window rows k..k+7.
-// U row k overwrites band row k (consumed 8 steps earlier): [1/u_kk, u_k,k+1 .. u_k,k+14, y_k].
-// Returns non-zero on an exactly zero pivot (dgbtrf's INFO > 0).
-__device__ int band_solve(BeamWS& w, int n) {
+// Row scale 2^(1023-e) of a row whose largest entry has biased exponent e (1 for e = 0).
+__device__ __forceinline__ double row_scale(int e) {
+    return (e == 0) ? 1.0 : __longlong_as_double((long long)(2046 - e) << 52);
+}
+
+// Row scaling of band row `row` by the power of two that brings its largest entry into
+// [1, 2) (exact in FP64), and its FP32 copy for the factorisation.  The maximum is taken on
+// the IEEE bit patterns (integer compares only).
+__device__ __forceinline__ void scale_row(const BeamWS& w, int row) {
+    const double* Ab = w.band + (size_t)row * 16;
+    unsigned long long m = 0;
+#pragma unroll
+    for (int q = 0; q < BW; ++q) {
+        const unsigned long long a = (unsigned long long)__double_as_longlong(Ab[q]) & 0x7fffffffffffffffull;
+        m = (a > m) ? a : m;
+    }
+    const int e = (int)(m >> 52);
+    const double sc = row_scale(e);
+    w.rse[row] = e;
+    float4* U4 = reinterpret_cast<float4*>(w.Uf + (size_t)row * 16);
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+        U4[q] = make_float4(__double2float_rn(Ab[4 * q] * sc), __double2float_rn(Ab[4 * q + 1] * sc),
+                            __double2float_rn(Ab[4 * q + 2] * sc), __double2float_rn(Ab[4 * q + 3] * sc));
+}
+
+// FP32 banded LU with partial pivoting (dgbtrf semantics, kl = ku = 7) of the row-scaled
+// Jacobian, in place in w.Uf; one warp.  Lane c < 16 owns the window column j with
+// j = c (mod 16), so the window never shifts across lanes; registers v[r] hold window rows
+// k..k+7.  U row k overwrites band row k (consumed 8 steps earlier): [1/u_kk, u_k,k+1 ..
+// u_k,k+14]; L row k = [pivot offset, l_1 .. l_7] with the multipliers in window order after
+// the interchange.  Returns non-zero on an exactly zero pivot (dgbtrf's INFO > 0).
+__device__ int band_factor_f32(const BeamWS& w, int n) {
     const int lane = threadIdx.x & 31;
-    const bool mat = lane < 16, rhs = lane == 16;
-    double* U = w.band;
-    double v[KL + 1];
+    const bool mat = lane < 16;
+    float* U = w.Uf;
+    float v[KL + 1];
 #pragma unroll
     for (int r = 0; r <= KL; ++r) {
-        double val = 0.0;
-        if (r < n) {
-            if (rhs) val = w.bvec[r];
-            else if (mat) {
-                const int ci = lane - r + KL;  // window [0, 15], column j = lane
-                if (ci >= 0 && ci < BW) val = U[(size_t)r * 16 + ci];
-            }
-        }
-        v[r] = val;
+        const int ci = lane - r + KL;  // window [0, 15], column j = lane
+        v[r] = (r < n && mat && ci >= 0 && ci < BW) ? U[r * 16 + ci] : 0.f;
     }
     int info = 0;
     for (int k = 0; k < n; ++k) {
         const int pl = k & 15;
-        // the pivot column (rows k..k+7) to every lane; |v| compared as integer keys
-        double col[KL + 1];
+        float col[KL + 1];
 #pragma unroll
         for (int r = 0; r <= KL; ++r) col[r] = __shfl_sync(0xffffffffu, v[r], pl);
         int p = 0;
-        unsigned long long best = (unsigned long long)__double_as_longlong(col[0]) & 0x7fffffffffffffffull;
+        unsigned best = __float_as_uint(col[0]) & 0x7fffffffu;
 #pragma unroll
         for (int r = 1; r <= KL; ++r) {
-            const unsigned long long a = (unsigned long long)__double_as_longlong(col[r]) & 0x7fffffffffffffffull;
+            const unsigned a = __float_as_uint(col[r]) & 0x7fffffffu;
             if (k + r < n && a > best) { best = a; p = r; }
         }
-        double t0 = v[0], c0 = col[0];
+        float t0 = v[0], c0 = col[0];
 #pragma unroll
         for (int r = 1; r <= KL; ++r)
             if (r == p) {
-                const double tmp = v[r]; v[r] = t0; t0 = tmp;
-                const double cm = col[r]; col[r] = c0; c0 = cm;
+                const float tmp = v[r]; v[r] = t0; t0 = tmp;
+                const float cm = col[r]; col[r] = c0; c0 = cm;
             }
         v[0] = t0;
-        const double piv = c0;
-        if (piv == 0.0) { info = k + 1; break; }
-        const double rinv = __drcp_rn(piv);
-        double l[KL + 1];
+        if (c0 == 0.f) { info = k + 1; break; }  // c0 is the same in every lane
+        const float rinv = __frcp_rn(c0);
+        float l[KL + 1];
 #pragma unroll
-        for (int r = 1; r <= KL; ++r) l[r] = col[r] * rinv;
+        for (int r = 1; r <= KL; ++r) l[r] = __fmul_rn(col[r], rinv);
         const int c = (lane - k) & 15;  // offset of this lane's column from k
-        if ((mat && c >= 1 && c <= 14) || rhs) {
+        if (mat && c >= 1 && c <= 14) {
 #pragma unroll
-            for (int r = 1; r <= KL; ++r) v[r] = v[r] - l[r] * v[0];
+            for (int r = 1; r <= KL; ++r) v[r] = __fmaf_rn(-l[r], v[0], v[r]);
         }
         if (mat && c <= 14) U[(size_t)k * 16 + c] = (c == 0) ? rinv : v[0];
-        if (rhs) U[(size_t)k * 16 + 15] = v[0];
+        if (lane == 16) {
+            float4* L4 = reinterpret_cast<float4*>(w.Lf + (size_t)k * 8);
+            L4[0] = make_float4(__int_as_float(p), l[1], l[2], l[3]);
+            L4[1] = make_float4(l[4], l[5], l[6], l[7]);
+        }
 #pragma unroll
         for (int r = 0; r < KL; ++r) v[r] = v[r + 1];
         // next window [k+1, k+16]: the pivot lane now holds column k+16 (zero for every row),
-        // the new row k+8 enters with its original band values
+        // the new row k+8 enters with its scaled band values
         const int r8 = k + 1 + KL;
-        double nv = 0.0;
-        if (r8 < n) {
-            if (rhs) nv = w.bvec[r8];
-            else if (mat) {
-                const int cn = (lane - (k + 1)) & 15;
-                if (cn < BW) nv = U[(size_t)r8 * 16 + cn];
-            }
+        float nv = 0.f;
+        if (r8 < n && mat) {
+            const int cn = (lane - (k + 1)) & 15;
+            if (cn < BW) nv = U[(size_t)r8 * 16 + cn];
         }
         if (lane == pl) {
 #pragma unroll
-            for (int r = 0; r < KL; ++r) v[r] = 0.0;
+            for (int r = 0; r < KL; ++r) v[r] = 0.f;
         }
         v[KL] = nv;
     }
-    info = __shfl_sync(0xffffffffu, info, 0);
-    if (info) return info;
-    // back substitution: lane l accumulates its pending row r = l (mod 16), r < k
-    double acc = 0.0;
-    for (int k = n - 1; k >= 0; --k) {
-        const int ol = k & 15;
-        double xk = 0.0;
-        if (lane == ol) {
-            const double* Uk = U + (size_t)k * 16;
-            xk = (Uk[15] - acc) * Uk[0];
-            w.xdi[k] = xk;
-            acc = 0.0;
+    return __shfl_sync(0xffffffffu, info, 0);
+}
+
+// Solve with the FP32 factor in place on w.yf (one thread): the interchanges and L
+// eliminations in the order dgbtrf made them (dgbtrs), then U x = y with the row written as
+// a dot product, far terms first, so only x_{k+1} and x_{k+2} are on the recurrence.
+__device__ void band_solve_f32(const BeamWS& w, int n) {
+    float* __restrict__ y = w.yf;
+    const float* __restrict__ L = w.Lf;
+    const float* __restrict__ U = w.Uf;
+    float q[KL + 1];
+#pragma unroll
+    for (int r = 0; r <= KL; ++r) q[r] = (r < n) ? y[r] : 0.f;
+#pragma unroll 4
+    for (int k = 0; k < n; ++k) {
+        const float4 la = *reinterpret_cast<const float4*>(L + (size_t)k * 8);
+        const float4 lb = *reinterpret_cast<const float4*>(L + (size_t)k * 8 + 4);
+        const int p = __float_as_int(la.x);
+        float t = q[0];
+        if (p != 0) {
+            const float q0 = q[0];
+#pragma unroll
+            for (int r = 1; r <= KL; ++r)
+                if (r == p) { t = q[r]; q[r] = q0; }
         }
-        xk = __shfl_sync(0xffffffffu, xk, ol);
-        const int c = (k - lane) & 15;
-        if (mat && lane != ol && c <= 14 && k - c >= 0) acc += U[(size_t)(k - c) * 16 + c] * xk;
+        q[1] = __fmaf_rn(-la.y, t, q[1]);
+        q[2] = __fmaf_rn(-la.z, t, q[2]);
+        q[3] = __fmaf_rn(-la.w, t, q[3]);
+        q[4] = __fmaf_rn(-lb.x, t, q[4]);
+        q[5] = __fmaf_rn(-lb.y, t, q[5]);
+        q[6] = __fmaf_rn(-lb.z, t, q[6]);
+        q[7] = __fmaf_rn(-lb.w, t, q[7]);
+        y[k] = t;
+#pragma unroll
+        for (int r = 0; r < KL; ++r) q[r] = q[r + 1];
+        q[KL] = (k + 1 + KL < n) ? y[k + 1 + KL] : 0.f;
     }
-    return 0;
+    float xw[15];  // xw[c] = x_{k+c}
+#pragma unroll
+    for (int c = 0; c < 15; ++c) xw[c] = 0.f;
+#pragma unroll 4
+    for (int k = n - 1; k >= 0; --k) {
+        const float4* Uk = reinterpret_cast<const float4*>(U + (size_t)k * 16);
+        const float4 u0 = Uk[0], u1 = Uk[1], u2 = Uk[2], u3 = Uk[3];
+        float sa = __fmul_rn(u3.z, xw[14]);
+        sa = __fmaf_rn(u3.y, xw[13], sa);
+        sa = __fmaf_rn(u3.x, xw[12], sa);
+        sa = __fmaf_rn(u2.w, xw[11], sa);
+        sa = __fmaf_rn(u2.z, xw[10], sa);
+        sa = __fmaf_rn(u2.y, xw[9], sa);
+        sa = __fmaf_rn(u2.x, xw[8], sa);
+        float sb = __fmul_rn(u1.w, xw[7]);
+        sb = __fmaf_rn(u1.z, xw[6], sb);
+        sb = __fmaf_rn(u1.y, xw[5], sb);
+        sb = __fmaf_rn(u1.x, xw[4], sb);
+        sb = __fmaf_rn(u0.w, xw[3], sb);
+        float t = __fsub_rn(y[k], __fadd_rn(sa, sb));
+        t = __fmaf_rn(-u0.z, xw[2], t);
+        t = __fmaf_rn(-u0.y, xw[1], t);
+        const float xk = __fmul_rn(t, u0.x);
+        y[k] = xk;
+#pragma unroll
+        for (int c = 14; c >= 2; --c) xw[c] = xw[c - 1];
+        xw[1] = xk;
+    }
+}
+
+// FP64 residual of band row k at the current solution, row-scaled into the FP32 solve vector.
+__device__ __forceinline__ void residual_row(const BeamWS& w, int n, int k) {
+    const double* Bk = w.band + (size_t)k * 16;
+    double acc = w.bvec[k];
+#pragma unroll
+    for (int ci = 0; ci < BW; ++ci) {
+        const int j = k - KL + ci;
+        if (j >= 0 && j < n) acc = fma(-Bk[ci], w.xdi[j], acc);
+    }
+    w.yf[k] = __double2float_rn(acc * row_scale(w.rse[k]));
 }
 
 }  // namespace
+
+// Cycle counters of the beam kernel's phases (thread 0, registers; added to the scalars at the
+// end of the kernel), read by fsibe_beam_phase_cycles.
+#define PH(k) do { const long long t_ = clock64(); ph[k] += t_ - ph_t; ph_t = t_; } while (0)
 
 // IBES_solver / SolidSolverWrapper / SolidEnergies / the force integral, one CTA.
 __global__ void __launch_bounds__(256) k_beam(BeamArgs b) {
@@ -952,13 +1168,21 @@ __global__ void __launch_bounds__(256) k_beam(BeamArgs b) {
     DevScalars* S = b.S;
     if (S->status != 0) return;
     const int ns = b.ns, n = 2 * ns + 4;
-    BeamWS w = carve(b.use_smem ? smem_ws : b.ws, ns);
+    // use_smem: which workspace parts live in shared memory (0 none, 1 the FP32 factor,
+    // 2 also the FP64 vectors, 3 also the FP64 band); the others in the global copy
+    const int mode = b.use_smem;
+    const size_t nv = beam_vec_doubles(ns), nb = beam_band_doubles(ns);
+    double* vec = (mode >= 2) ? smem_ws : b.ws;
+    double* band = (mode >= 3) ? smem_ws + nv : b.ws + nv;
+    float* f32 = reinterpret_cast<float*>(mode == 3 ? smem_ws + nv + nb : (mode == 2 ? smem_ws + nv : (mode == 1 ? smem_ws : b.ws + nv + nb)));
+    BeamWS w = carve(vec, band, f32, ns);
     const double time = S->time, dt = S->dt1;
     const double ds = b.ds, mue = b.mue, eta = b.eta;
     const double alpha = b.angle_deg * b.pi / 180.0;
     __shared__ double red[4][8];
     __shared__ int flag;
     __shared__ D1DTab dtab;
+    long long ph_t = clock64(), ph[14] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
     d1d_tables(&dtab, b.ds);
     w.dtab = &dtab;
     __syncthreads();
@@ -1006,7 +1230,9 @@ __global__ void __launch_bounds__(256) k_beam(BeamArgs b) {
         // EE1 predictor: th1 = theta, td1 = theta_dot -> RHS
         for (int i = threadIdx.x; i < ns; i += blockDim.x) { w.th1[i] = b.th[i]; w.td1[i] = b.thd[i]; }
         __syncthreads();
+        PH(0);
         int st = rhs_beameqn(b, w, w.th1, w.td1, b.p_old, w.T, b.tau_old, grav);
+        PH(1);
         if (st) { if (threadIdx.x == 0) set_status(S, FSIBE_ERR_SINGULAR); return; }
         for (int i = threadIdx.x; i < ns; i += blockDim.x) w.g5[i] = b.th[i] + dt * w.th1[i];
         __syncthreads();
@@ -1035,6 +1261,7 @@ __global__ void __launch_bounds__(256) k_beam(BeamArgs b) {
             w.taun_s[i] = d1d(w.dtab, b.tau_new, ns, 1, i);
         }
         __syncthreads();
+        PH(2);
         if (method == FSIBE_CRANK_NICHOLSON) {
             for (int i = threadIdx.x; i < ns; i += blockDim.x) { w.th1[i] = w.bo5[i]; w.old_rhs[i] = w.bo6[i]; }
             __syncthreads();
@@ -1048,8 +1275,17 @@ __global__ void __launch_bounds__(256) k_beam(BeamArgs b) {
         newton_consts(c, ds, eta, mue);
         c.K1 = mue * (0.0 * cos(alpha) + 0.0 * sin(alpha) + grav * sin(alpha)) - b.tau_new[0];
         c.K2 = b.p_new[0] + mue * (0.0 * cos(alpha) - 0.0 * sin(alpha) + grav * cos(alpha));
+        // the FP32 factor of an earlier step, when one is stored
+        bool need_factor = (S->beam_fact == 0), factored = false;
+        if (!need_factor && mode >= 1) {
+            const float4* g = reinterpret_cast<const float4*>(b.ws + beam_vec_doubles(ns) + beam_band_doubles(ns));
+            float4* d = reinterpret_cast<float4*>(w.Uf);
+            for (size_t q = threadIdx.x; q < beam_fact_floats(ns) / 4; q += blockDim.x) d[q] = g[q];
+            __syncthreads();
+        }
         int iter = 0;
         bool iterate = true;
+        PH(3);
         while (iterate) {
             if (threadIdx.x == 0) flag = 0;
             for (int i = threadIdx.x; i < ns; i += blockDim.x)
@@ -1063,12 +1299,52 @@ __global__ void __launch_bounds__(256) k_beam(BeamArgs b) {
             }
             __syncthreads();
             if (flag) { if (threadIdx.x == 0) set_status(S, flag); return; }
-            if (threadIdx.x < 32) {
-                const int info = band_solve(w, n);
-                if (threadIdx.x == 0 && info) flag = FSIBE_ERR_SINGULAR;
+            PH(4);
+            // J dx = -F: FP32 LU of the row-scaled band as the preconditioner of an FP64
+            // iterative refinement, run to the accuracy of an FP64 factorisation.  The factor is
+            // kept across Newton iterations and steps while it still contracts fast (<= 5
+            // solves); a stale factor that stops converging is replaced and the solve redone.
+            int solves = 0;
+            for (int attempt = 0; attempt < 2; ++attempt) {
+                const bool fresh = need_factor;
+                if (need_factor) {
+                    for (int k = threadIdx.x; k < n; k += blockDim.x) scale_row(w, k);
+                    __syncthreads();
+                    if (threadIdx.x < 32) {
+                        const int info = band_factor_f32(w, n);
+                        if (threadIdx.x == 0 && info) flag = FSIBE_ERR_SINGULAR;
+                    }
+                    __syncthreads();
+                    if (flag) { if (threadIdx.x == 0) set_status(S, flag); return; }
+                    need_factor = false;
+                    factored = true;
+                }
+                PH(5);
+                for (int k = threadIdx.x; k < n; k += blockDim.x)
+                    w.yf[k] = __double2float_rn(w.bvec[k] * row_scale(w.rse[k]));
+                __syncthreads();
+                float cprev = 0.f;
+                bool ok = false;
+                for (int pass = 0;; ++pass) {
+                    if (pass > 0) {
+                        for (int k = threadIdx.x; k < n; k += blockDim.x) residual_row(w, n, k);
+                        __syncthreads();
+                    }
+                    PH(11);
+                    if (threadIdx.x == 0) band_solve_f32(w, n);
+                    __syncthreads();
+                    PH(12);
+                    ++solves;
+                    const int rs = refine_step(w.xdi, w.yf, n, pass, cprev, &red[2][0]);
+                    PH(13);
+                    if (rs != 0) { ok = rs > 0; break; }
+                }
+                if (ok || fresh) break;
+                need_factor = true;
             }
-            __syncthreads();
-            if (flag) { if (threadIdx.x == 0) set_status(S, flag); return; }
+            if (solves > 5) need_factor = true;
+            if (threadIdx.x == 0) ph[10] += solves;
+            PH(6);
             double sd = 0.0, sx = 0.0;
             for (int l = threadIdx.x; l < n; l += blockDim.x) {
                 const double d = w.xdi[col_of(ns, l + 1)];
@@ -1104,6 +1380,14 @@ __global__ void __launch_bounds__(256) k_beam(BeamArgs b) {
             b.th[i] = th;
             b.thd[i] = (C1 / dt) * (th - C3 * w.bo5[i] - C4 * w.oo5[i]) - C2 * w.bo6[i];
         }
+        if (factored) {
+            if (mode >= 1) {
+                float4* g = reinterpret_cast<float4*>(b.ws + beam_vec_doubles(ns) + beam_band_doubles(ns));
+                const float4* d = reinterpret_cast<const float4*>(w.Uf);
+                for (size_t q = threadIdx.x; q < beam_fact_floats(ns) / 4; q += blockDim.x) g[q] = d[q];
+            }
+            if (threadIdx.x == 0) S->beam_fact = 1;
+        }
         if (threadIdx.x == 0) {
             S->newton_iters = iter;
             if (S->actually_bdf2) { S->method = FSIBE_BDF2; S->actually_bdf2 = 0; }
@@ -1116,6 +1400,7 @@ __global__ void __launch_bounds__(256) k_beam(BeamArgs b) {
         }
         __syncthreads();
     }
+    PH(7);
     // integrate_position(time + dt) (integrate_position.f90:14-44): running sums in order
     for (int i = threadIdx.x; i < ns; i += blockDim.x) {
         const double th = b.th[i], td = b.thd[i];
@@ -1165,6 +1450,7 @@ __global__ void __launch_bounds__(256) k_beam(BeamArgs b) {
             if (m > 100.0) set_status(S, FSIBE_ERR_BRAKE);
         }
     }
+    PH(8);
     // SolidEnergies (SolidSolver.f90:76-92)
     for (int i = threadIdx.x; i < ns; i += blockDim.x) w.T_s[i] = d1d(w.dtab, b.th, ns, 1, i);
     __syncthreads();
@@ -1183,11 +1469,15 @@ __global__ void __launch_bounds__(256) k_beam(BeamArgs b) {
         S->inertial_force[0] = mue * ds * sax;
         S->inertial_force[1] = mue * ds * say;
     }
+    PH(9);
+    if (threadIdx.x == 0)
+        for (int k = 0; k < 14; ++k) S->phase[k] += ph[k];
 }
 
 // Beam start state (init_beam.f90:83-120): straight beam at the leading edge, at rest.
 __global__ void k_init_beam(BeamArgs b) {
     const int ns = b.ns;
+    if (threadIdx.x == 0) b.S->beam_fact = 0;
     const double alpha = b.angle_deg * b.pi / 180.0, ca = cos(alpha), sa = sin(alpha);
     for (int i = threadIdx.x; i < ns; i += blockDim.x) {
         b.th[i] = 0.0; b.thd[i] = 0.0; b.ax[i] = 0.0; b.ay[i] = 0.0;
@@ -1217,23 +1507,33 @@ __global__ void k_init_beam(BeamArgs b) {
 void launch_mask(const MaskArgs& a, double gerf, bool fp32, cudaStream_t st) {
     k_mask_prep<<<1, 256, 0, st>>>(a, gerf);
     dim3 grid(a.nx / MASK_TX, a.ny / MASK_TY);
-    if (fp32) k_mask_raster<float><<<grid, 256, 0, st>>>(a, gerf);
-    else k_mask_raster<double><<<grid, 256, 0, st>>>(a, gerf);
+    if (fp32) k_mask_raster<float><<<grid, MASK_NT, 0, st>>>(a, gerf);
+    else k_mask_raster<double><<<grid, MASK_NT, 0, st>>>(a, gerf);
 }
 
 void launch_forces(const ForceArgs& a, double dxi, double dyi, cudaStream_t st) {
     k_forces<<<a.ns, 128, 0, st>>>(a, dxi, dyi);
 }
 
-void launch_beam(const BeamArgs& b, cudaStream_t st) {
-    const size_t bytes = b.use_smem ? 8 * beam_ws_doubles(b.ns) : 0;
-    k_beam<<<1, 256, bytes, st>>>(b);
+static size_t beam_smem_bytes(int ns, int mode) {
+    const size_t f = 4 * beam_f32_floats_(ns), v = 8 * beam_vec_doubles(ns), bd = 8 * beam_band_doubles(ns);
+    if (mode == 3) return v + bd + f;
+    if (mode == 2) return v + f;
+    if (mode == 1) return f;
+    return 0;
 }
-// Opt the beam kernel into a shared-memory workspace when it fits (<= 200 KB).
-bool beam_smem_setup(int ns) {
-    const size_t bytes = 8 * beam_ws_doubles(ns);
-    if (bytes > 200 * 1024) return false;
-    return cudaFuncSetAttribute(k_beam, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) == cudaSuccess;
+void launch_beam(const BeamArgs& b, cudaStream_t st) {
+    k_beam<<<1, 256, beam_smem_bytes(b.ns, b.use_smem), st>>>(b);
+}
+// Shared-memory placement of the beam workspace: the largest set of parts that fits in
+// 216 KB, in the order FP32 factor, FP64 vectors, FP64 band.
+int beam_smem_setup(int ns) {
+    for (int mode = 3; mode >= 1; --mode) {
+        const size_t bytes = beam_smem_bytes(ns, mode);
+        if (bytes > 216 * 1024) continue;
+        if (cudaFuncSetAttribute(k_beam, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) == cudaSuccess) return mode;
+    }
+    return 0;
 }
 void launch_init_beam(const BeamArgs& b, cudaStream_t st) { k_init_beam<<<1, 256, 0, st>>>(b); }
 

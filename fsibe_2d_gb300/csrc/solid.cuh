@@ -41,7 +41,7 @@ struct BeamArgs {
     double ds, eta, mue, sigma, t_release, tau, tol, pi, x0, y0, angle_deg;
     double *x, *y, *vx, *vy, *th, *thd, *ax, *ay, *p_old, *p_new, *tau_old, *tau_new, *oo;
     double* ws;      // global workspace (used when the shared-memory workspace does not fit)
-    int use_smem;    // 1: workspace in dynamic shared memory
+    int use_smem;    // workspace parts in shared memory: 0 none, 1 FP32 factor, 2 + FP64 vectors, 3 + band
     double* rows;    // beam_data ring (21 per step) or nullptr
     int row_cap;
 };
