@@ -24,9 +24,13 @@ void fill_sizes_1024(SizeKernels<double>&, SizeKernels<float>&);
 void fill_sizes_2048(SizeKernels<double>&, SizeKernels<float>&);
 void fill_sizes_4096(SizeKernels<double>&, SizeKernels<float>&);
 size_t beam_ws_doubles(int ns);
+void launch_mask_prep(const MaskArgs& a, double gerf, cudaStream_t st);
 void launch_mask(const MaskArgs& a, double gerf, bool fp32, cudaStream_t st);
 void launch_forces(const ForceArgs& a, double dxi, double dyi, cudaStream_t st);
 void launch_beam(const BeamArgs& b, cudaStream_t st);
+void launch_beam_pre(const BeamArgs& b, cudaStream_t st);
+int beam_pre_smem_setup(int ns);
+size_t beam_pred_doubles(int ns);
 void launch_init_beam(const BeamArgs& b, cudaStream_t st);
 int beam_smem_setup(int ns);
 
@@ -420,7 +424,12 @@ struct fsibe_ctx {
     double* dscratch2 = nullptr;  // nx*ny doubles
     double gerf = 0.0;
     double U_mean_true = 1.0;
-    int beam_smem = 0;  // beam workspace placement (0 global, 1 FP32 factor in shared memory, 2 all)
+    int beam_smem = 0;      // beam workspace parts in shared memory (bit mask, see k_beam)
+    int beam_pre_smem = 0;  // the same for the predictor kernel
+    double* pred = nullptr; // predictor output
+    cudaStream_t side = nullptr;  // the beam predictor runs here beside the fluid step
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    bool pre_launched = false;    // the predictor of the current step is in flight
     bool initialized = false, startup_done = false;
     bool use_graph = false, graph_ready = false;
     cudaGraphExec_t gexec = nullptr;
@@ -428,6 +437,7 @@ struct fsibe_ctx {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     std::string err;
     int launches = 0;
+    int nsm = 152;                // SMs of the device
     // per-kernel event timing (fsibe_kernel_times)
     bool profiling = false;
     std::vector<cudaEvent_t> pool;
@@ -435,20 +445,20 @@ struct fsibe_ctx {
     std::vector<std::pair<const char*, size_t>> prof;  // name, index of the start event
 };
 
-static void prof_begin(fsibe_ctx* c, const char* name) {
+static void prof_begin(fsibe_ctx* c, const char* name, cudaStream_t st = nullptr) {
     if (!c->profiling) return;
     while (c->pool.size() < c->pool_used + 2) {
         cudaEvent_t e;
         cudaEventCreate(&e);
         c->pool.push_back(e);
     }
-    cudaEventRecord(c->pool[c->pool_used], c->stream);
+    cudaEventRecord(c->pool[c->pool_used], st ? st : c->stream);
     c->prof.push_back({name, c->pool_used});
     c->pool_used += 2;
 }
-static void prof_end(fsibe_ctx* c) {
+static void prof_end(fsibe_ctx* c, cudaStream_t st = nullptr) {
     if (!c->profiling) return;
-    cudaEventRecord(c->pool[c->prof.back().second + 1], c->stream);
+    cudaEventRecord(c->pool[c->prof.back().second + 1], st ? st : c->stream);
 }
 
 static std::string g_err;
@@ -573,6 +583,48 @@ static StepArgs step_args(fsibe_ctx* c, int explicit_step, int nblk) {
     return a;
 }
 
+static BeamArgs beam_args(fsibe_ctx* c) {
+    BeamArgs b;
+    std::memset(&b, 0, sizeof(b));
+    b.S = c->S;
+    b.ns = c->P.ns; b.iImpulse = c->P.iImpulse; b.maxit = c->P.newton_maxit; b.iFLUSI = c->P.iFLUSI;
+    b.ds = c->g.ds; b.eta = c->P.eta; b.mue = c->P.mue; b.sigma = c->P.sigma;
+    b.t_release = c->P.t_release; b.tau = c->P.tau; b.tol = c->P.newton_tol; b.pi = c->g.pi;
+    b.x0 = c->P.x0; b.y0 = c->P.y0; b.angle_deg = c->P.angle_beam;
+    {
+        const double alpha = c->P.angle_beam * c->g.pi / 180.0;
+        b.cos_a = std::cos(alpha);
+        b.sin_a = std::sin(alpha);
+    }
+    b.x = c->beam[B_X]; b.y = c->beam[B_Y]; b.vx = c->beam[B_VX]; b.vy = c->beam[B_VY];
+    b.th = c->beam[B_TH]; b.thd = c->beam[B_THD]; b.ax = c->beam[B_AX]; b.ay = c->beam[B_AY];
+    b.p_old = c->beam[B_PO]; b.p_new = c->beam[B_PN]; b.tau_old = c->beam[B_TO]; b.tau_new = c->beam[B_TN];
+    b.oo = c->oo;
+    b.ws = c->ws;
+    b.use_smem = c->beam_smem;
+    b.pred = c->pred;
+    return b;
+}
+
+// The beam predictor of the current step (k_beam_pre) on the side stream, forked from the
+// main stream after the step's time step is known; solid_step joins it.
+static int beam_predict(fsibe_ctx* c) {
+    BeamArgs b = beam_args(c);
+    b.use_smem = c->beam_pre_smem;
+    CK(c, cudaEventRecord(c->ev_fork, c->stream));
+    CK(c, cudaStreamWaitEvent(c->side, c->ev_fork, 0));
+    prof_begin(c, "beam_pre", c->side);
+    launch_beam_pre(b, c->side);
+    prof_end(c, c->side);
+    CKL(c);
+    CK(c, cudaEventRecord(c->ev_join, c->side));
+    c->launches++;
+    c->pre_launched = true;
+    return FSIBE_OK;
+}
+
+
+
 template <typename R>
 static int x_blocks(fsibe_ctx* c) { return c->g.ny / kx_of<R>(c).x_rows; }
 
@@ -588,6 +640,7 @@ static int fluid_step_t(fsibe_ctx* c, int explicit_step) {
     k_step_begin<<<1, 256, 0, c->stream>>>(sa);
     prof_end(c);
     c->launches++;
+    if (c->P.iFLUSI == 1) { const int st = beam_predict(c); if (st) return st; }
     launch_x<R>(c, KX.nl_x, KX.x_smem2, a, "nl_x");
     launch_y<R>(c, KY.nl_y, KY.y_smem2, a, "nl_y");
     launch_x<R>(c, KX.press_x, KX.x_smem2, a, "press_x");
@@ -620,7 +673,7 @@ static MaskArgs mask_args(fsibe_ctx* c) {
     m.t_beam = c->P.t_beam; m.N_smooth = c->P.N_smooth; m.eps = c->P.eps; m.pi = c->g.pi;
     m.angle_deg = c->P.angle_beam;
     m.x = c->beam[B_X]; m.y = c->beam[B_Y]; m.vx = c->beam[B_VX]; m.vy = c->beam[B_VY]; m.th = c->beam[B_TH];
-    m.prims = c->prims; m.nprims = c->nprims; m.rect = c->rect;
+    m.prims = c->prims; m.nprims = c->nprims; m.rect = c->rect; m.nsm = c->nsm;
     m.mask = c->phys[PH_MASK]; m.mvx = c->phys[PH_MVX]; m.mvy = c->phys[PH_MVY];
     return m;
 }
@@ -631,8 +684,12 @@ static int create_mask(fsibe_ctx* c) {
         for (int q : {PH_MASK, PH_MVX, PH_MVY}) CK(c, cudaMemsetAsync(c->phys[q], 0, bytes, c->stream));
         return FSIBE_OK;
     }
+    const MaskArgs m = mask_args(c);
+    prof_begin(c, "mask_prep");
+    launch_mask_prep(m, c->gerf, c->stream);
+    prof_end(c);
     prof_begin(c, "mask");
-    launch_mask(mask_args(c), c->gerf, c->fp32, c->stream);
+    launch_mask(m, c->gerf, c->fp32, c->stream);
     prof_end(c);
     c->launches += 2;
     CKL(c);
@@ -663,24 +720,10 @@ static int get_forces(fsibe_ctx* c) {
     return FSIBE_OK;
 }
 
-static BeamArgs beam_args(fsibe_ctx* c) {
-    BeamArgs b;
-    std::memset(&b, 0, sizeof(b));
-    b.S = c->S;
-    b.ns = c->P.ns; b.iImpulse = c->P.iImpulse; b.maxit = c->P.newton_maxit; b.iFLUSI = c->P.iFLUSI;
-    b.ds = c->g.ds; b.eta = c->P.eta; b.mue = c->P.mue; b.sigma = c->P.sigma;
-    b.t_release = c->P.t_release; b.tau = c->P.tau; b.tol = c->P.newton_tol; b.pi = c->g.pi;
-    b.x0 = c->P.x0; b.y0 = c->P.y0; b.angle_deg = c->P.angle_beam;
-    b.x = c->beam[B_X]; b.y = c->beam[B_Y]; b.vx = c->beam[B_VX]; b.vy = c->beam[B_VY];
-    b.th = c->beam[B_TH]; b.thd = c->beam[B_THD]; b.ax = c->beam[B_AX]; b.ay = c->beam[B_AY];
-    b.p_old = c->beam[B_PO]; b.p_new = c->beam[B_PN]; b.tau_old = c->beam[B_TO]; b.tau_new = c->beam[B_TN];
-    b.oo = c->oo;
-    b.ws = c->ws;
-    b.use_smem = c->beam_smem;
-    return b;
-}
-
 static int solid_step(fsibe_ctx* c) {
+    if (!c->pre_launched) { const int st = beam_predict(c); if (st) return st; }
+    CK(c, cudaStreamWaitEvent(c->stream, c->ev_join, 0));
+    c->pre_launched = false;
     prof_begin(c, "beam");
     launch_beam(beam_args(c), c->stream);
     prof_end(c);
@@ -885,12 +928,15 @@ int fsibe_destroy(fsibe_ctx* c) {
     for (void* p : c->phys) if (p) cudaFree(p);
     for (void* p : c->spec) if (p) cudaFree(p);
     for (double* p : c->beam) if (p) cudaFree(p);
-    void* others[] = {c->twX, c->twR, c->twY, c->S, c->red, c->oo, c->ws, c->prims, c->nprims,
+    void* others[] = {c->twX, c->twR, c->twY, c->S, c->red, c->oo, c->ws, c->pred, c->prims, c->nprims,
                       c->rect, c->counter, c->fterm, c->rows, c->dscratch, c->dscratch2, c->etab, c->etabf, c->dcut};
     for (void* p : others) if (p) cudaFree(p);
     for (cudaEvent_t e : c->pool) cudaEventDestroy(e);
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
+    if (c->ev_fork) cudaEventDestroy(c->ev_fork);
+    if (c->ev_join) cudaEventDestroy(c->ev_join);
+    if (c->side) { cudaStreamSynchronize(c->side); cudaStreamDestroy(c->side); }
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return FSIBE_OK;
@@ -947,10 +993,12 @@ int fsibe_create(const fsibe_params* p, fsibe_ctx** out) {
     for (int i = 0; i < B_N; ++i) ALLOC(c->beam[i], 8 * (size_t)ns);
     ALLOC(c->oo, 8 * (size_t)ns * 6);
     ALLOC(c->ws, 8 * beam_ws_doubles(ns));
+    ALLOC(c->pred, 8 * beam_pred_doubles(ns));
     c->beam_smem = beam_smem_setup(ns);
+    c->beam_pre_smem = beam_pre_smem_setup(ns);
     ALLOC(c->prims, sizeof(Prim) * (size_t)(2 * ns + 8));
     ALLOC(c->nprims, 16);
-    ALLOC(c->rect, 16);
+    ALLOC(c->rect, 32);
     ALLOC(c->counter, 16);
     ALLOC(c->fterm, 16 * (size_t)ns);
     ALLOC(c->S, sizeof(DevScalars));
@@ -995,11 +1043,21 @@ int fsibe_create(const fsibe_params* p, fsibe_ctx** out) {
         cudaMemcpy(c->twY, tY.data(), 16 * tY.size(), cudaMemcpyHostToDevice);
     }
 #undef ALLOC
+    {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, dev);
+        if (c->nsm <= 0) c->nsm = 152;
+    }
     cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) { g_err = cudaGetErrorString(e); fsibe_destroy(c); return FSIBE_ERR_CUDA; }
     c->own_stream = true;
     cudaEventCreate(&c->ev0);
     cudaEventCreate(&c->ev1);
+    e = cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking);
+    if (e != cudaSuccess) { g_err = cudaGetErrorString(e); fsibe_destroy(c); return FSIBE_ERR_CUDA; }
+    cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming);
+    cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming);
     e = cudaDeviceSynchronize();
     if (e != cudaSuccess) { g_err = std::string("create: ") + cudaGetErrorString(e); fsibe_destroy(c); return FSIBE_ERR_CUDA; }
     *out = c;
@@ -1090,6 +1148,7 @@ int fsibe_init_fields(fsibe_ctx* c, const double* vort) {
     h.mean_u_cur = h.mean_u_next;
     h.mean_v_cur = h.mean_v_next;
     CK(c, cudaMemcpyAsync(c->S, &h, sizeof(h), cudaMemcpyHostToDevice, c->stream));
+    c->pre_launched = false;
     launch_init_beam(beam_args(c), c->stream);
     CKL(c);
     st = c->fp32 ? init_velocity<float>(c) : init_velocity<double>(c);
@@ -1232,7 +1291,12 @@ int fsibe_upload_mask(fsibe_ctx* c, const double* m, const double* vx, const dou
     int st = from_host(c, m, NN, c->phys[PH_MASK]);
     if (!st) st = from_host(c, vx, NN, c->phys[PH_MVX]);
     if (!st) st = from_host(c, vy, NN, c->phys[PH_MVY]);
-    return st;
+    if (st) return st;
+    // any cell may be non-zero now: the next raster pass clears the whole grid
+    const int full[4] = {0, c->g.nx - 1, 0, c->g.ny - 1};
+    CK(c, cudaMemcpyAsync(c->rect, full, sizeof(full), cudaMemcpyHostToDevice, c->stream));
+    CK(c, cudaStreamSynchronize(c->stream));
+    return FSIBE_OK;
 }
 int fsibe_download_mask(fsibe_ctx* c, double* m, double* vx, double* vy) {
     if (!c) return FSIBE_ERR_PARAM;
@@ -1252,6 +1316,7 @@ int fsibe_upload_beam(fsibe_ctx* c, const double* beam, const double* po, const 
     if (to) CK(c, cudaMemcpyAsync(c->beam[B_TO], to, 8 * ns, cudaMemcpyHostToDevice, c->stream));
     if (tn) CK(c, cudaMemcpyAsync(c->beam[B_TN], tn, 8 * ns, cudaMemcpyHostToDevice, c->stream));
     CK(c, cudaMemsetAsync(&c->S->beam_fact, 0, sizeof(int32_t), c->stream));  // a new state: refactor
+    c->pre_launched = false;
     CK(c, cudaStreamSynchronize(c->stream));
     return FSIBE_OK;
 }
@@ -1336,10 +1401,10 @@ int fsibe_kernel_times(fsibe_ctx* c, int nsteps, fsibe_kernel_time* out, int cap
     return read_status(c);
 }
 
-int fsibe_beam_phase_cycles(fsibe_ctx* c, long long* out16, int reset) {
-    if (!c || !out16) return FSIBE_ERR_PARAM;
-    CK(c, cudaMemcpyAsync(out16, c->S->phase, 16 * sizeof(long long), cudaMemcpyDeviceToHost, c->stream));
-    if (reset) CK(c, cudaMemsetAsync(c->S->phase, 0, 16 * sizeof(long long), c->stream));
+int fsibe_beam_phase_cycles(fsibe_ctx* c, long long* out32, int reset) {
+    if (!c || !out32) return FSIBE_ERR_PARAM;
+    CK(c, cudaMemcpyAsync(out32, c->S->phase, 32 * sizeof(long long), cudaMemcpyDeviceToHost, c->stream));
+    if (reset) CK(c, cudaMemsetAsync(c->S->phase, 0, 32 * sizeof(long long), c->stream));
     CK(c, cudaStreamSynchronize(c->stream));
     return FSIBE_OK;
 }
@@ -1350,7 +1415,7 @@ int fsibe_launches_per_step(fsibe_ctx* c, int* n) {
     int k = 6;  // step_begin, nl_x, nl_y, press_x, fluid_finish, advance
     if (P.iFLUSI == 1 || P.iSaveBeam > 0) k += 2 + 1;  // press_y, press_fin, forces
     if ((P.iFLUSI == 1 || P.iMotion > 0) && P.iBeam > 0) k += 2;  // mask prep + raster
-    if (P.iFLUSI == 1) k += 1;  // beam
+    if (P.iFLUSI == 1) k += 2;  // beam predictor + beam
     *n = k;
     return FSIBE_OK;
 }

@@ -64,7 +64,7 @@ struct DevScalars {
     double dt_old;                   // beam dt_old
     double row[21];                  // last beam_data row (BeamIO.f90:193-216)
     int32_t run_row, run_cap;        // beam_data ring position / capacity of fsibe_run
-    long long phase[16];             // beam kernel phase cycle counters (measurement)
+    long long phase[32];             // beam kernel phase cycle counters (measurement)
     int32_t beam_fact;               // 1: the global copy of the beam's FP32 band factor is usable
 };
 

@@ -19,7 +19,9 @@ struct MaskArgs {
     const double *x, *y, *vx, *vy, *th;
     Prim* prims;
     int* nprims;
-    int* rect;    // union of all primitive boxes
+    int* rect;    // [0..3] union of this step's primitive boxes (x0, x1, y0, y1), [4..7] its union
+                  // with the previous step's box; every cell outside [0..3] is zero
+    int nsm;      // SMs of the device (raster grid size)
     void *mask, *mvx, *mvy;  // R*[ny][nx]
 };
 
@@ -39,9 +41,11 @@ struct BeamArgs {
     DevScalars* S;
     int ns, iImpulse, maxit, iFLUSI;
     double ds, eta, mue, sigma, t_release, tau, tol, pi, x0, y0, angle_deg;
+    double cos_a, sin_a;  // cos and sin of the beam angle (angle_deg * pi / 180), from the host
     double *x, *y, *vx, *vy, *th, *thd, *ax, *ay, *p_old, *p_new, *tau_old, *tau_new, *oo;
     double* ws;      // global workspace (used when the shared-memory workspace does not fit)
     int use_smem;    // workspace parts in shared memory: 0 none, 1 FP32 factor, 2 + FP64 vectors, 3 + band
+    double* pred;    // predictor output (beam_pred_doubles)
     double* rows;    // beam_data ring (21 per step) or nullptr
     int row_cap;
 };

@@ -186,14 +186,18 @@ typedef struct fsibe_kernel_time {
     int32_t launches;
 } fsibe_kernel_time;
 int fsibe_kernel_times(fsibe_ctx* ctx, int nsteps, fsibe_kernel_time* out, int cap, int* count);
-/* Accumulated SM cycles of the beam kernel's phases since the last reset: [0] set-up,
- * [1] EE1 predictor (tension solve), [2] initial guess, [3] Crank-Nicolson right-hand side,
- * [4] Newton F + Jacobian (with the previous iteration's update and norms), [5] FP32 band
- * factorisation, [6] refinement solves (the rest of them), [7] last Newton update and bookkeeping,
- * [8] positions, [9] energies; [10] is the number of refinement solves (a count, not cycles);
- * [11] FP64 residuals, [12] FP32 triangular solves, [13] correction updates (parts of [6]).
+/* Accumulated SM cycles of the beam kernels' phases since the last reset.  Predictor kernel
+ * (runs beside the fluid step): [0] set-up, [1] EE1 predictor (tension solve), [2] initial
+ * guess, [3] Crank-Nicolson right-hand side.  Newton kernel: [4] Newton F + Jacobian (with
+ * the previous iteration's update and norms), [5] FP32 band factorisation, [6] the rest of
+ * the refinement, [7] set-up, last Newton update and bookkeeping, [8] positions,
+ * [9] energies, [11] FP64 residuals, [12] FP32 chunked solves, [13] correction updates;
+ * [10] is the number of refinement solves (a count, not cycles).  Parts of [12]: [16] local
+ * forward eliminations, [17] window carry, [18] forward correction, [19] local back
+ * substitutions, [20] state carry, [21] back correction.  Parts of [7]: [22] set-up before
+ * the Newton loop.  Parts of [4]: [23] Newton update and norms.  out32 receives 32 values;
  * reset != 0 zeroes them after reading. */
-int fsibe_beam_phase_cycles(fsibe_ctx* ctx, long long* out16, int reset);
+int fsibe_beam_phase_cycles(fsibe_ctx* ctx, long long* out32, int reset);
 /* Number of kernel launches one fsibe_step issues (for the bench's gpu_launches). */
 int fsibe_launches_per_step(fsibe_ctx* ctx, int* launches);
 /* Capture one fsibe_step in a CUDA graph and replay it for later steps (1) or
