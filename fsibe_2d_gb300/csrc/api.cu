@@ -57,37 +57,38 @@ struct StepArgs {
     int nblk, explicit_step, iBeam, iMeanVelocity, ns, nx, ny;
     double cfl, dx, dy, eps, dt_fixed, time_end, theta_inf, T_fullspeed, U_mean_true, pi, nu;
     double x0, y0, t_beam, NN, scalex, scaley;
+    double cos_ti, sin_ti;  // cos and sin of theta_inf, from the host
     const double *bx, *by;
     double* etab;
     float2* etabf;
     int hx;
 };
 
-__device__ double mean_ux(int mode, double time, double theta_inf, double Tf, double pi) {  // mean_velocity.f90:4-42
+__device__ double mean_ux(int mode, double time, double cos_ti, double Tf, double pi) {  // mean_velocity.f90:4-42
     double tf;
     switch (mode) {
         case 1:
             tf = (time < Tf) ? (time * time * time) / (-0.5 * Tf * Tf * Tf) + 3.0 * (time * time) / (Tf * Tf) : 1.0;
-            return cos(theta_inf) * tf;
+            return cos_ti * tf;
         case 2:
             tf = (time < Tf) ? 0.5 * (1.0 - cos(0.5 * pi * time / Tf)) : 1.0;
-            return cos(theta_inf) * tf;
-        case 3: return cos(theta_inf);
+            return cos_ti * tf;
+        case 3: return cos_ti;
         case 6: return time;
         case 22: return 0.1;
         default: return 0.0;
     }
 }
-__device__ double mean_uy(int mode, double time, double theta_inf, double Tf, double pi) {  // mean_velocity.f90:46-84
+__device__ double mean_uy(int mode, double time, double sin_ti, double Tf, double pi) {  // mean_velocity.f90:46-84
     double tf;
     switch (mode) {
         case 1:
             tf = (time < Tf) ? (time * time * time) / (-0.5 * Tf * Tf * Tf) + 3.0 * (time * time) / (Tf * Tf) : 1.0;
-            return sin(theta_inf) * tf;
+            return sin_ti * tf;
         case 2:
             tf = (time < Tf) ? 0.5 * (1.0 - cos(0.5 * pi * time / Tf)) : 1.0;
-            return sin(theta_inf) * tf;
-        case 3: return sin(theta_inf);
+            return sin_ti * tf;
+        case 3: return sin_ti;
         default: return 0.0;
     }
 }
@@ -96,36 +97,37 @@ __device__ double mean_uy(int mode, double time, double theta_inf, double Tf, do
 // from the velocity statistics of the previous step, the AB2 weights (:488-489), the mean
 // flow at time+dt1 and the drag window of cal_drag (:539-564).
 __global__ void __launch_bounds__(256) k_step_begin(StepArgs a) {
-    __shared__ double smax[256], su[256], sv[256];
-    __shared__ double bmin[2][256], bmax[2][256];
-    double m = 0.0, s0 = 0.0, s1 = 0.0;
-    for (int b = threadIdx.x; b < a.nblk; b += blockDim.x) {
-        const double* r = a.red + (size_t)b * RED_NSLOTS;
-        m = fmax(m, r[RED_UMAX2]);
-        s0 += r[RED_SUM_U];
-        s1 += r[RED_SUM_V];
-    }
-    double xmn = 1e300, xmx = -1e300, ymn = 1e300, ymx = -1e300;
-    for (int i = threadIdx.x; i < a.ns; i += blockDim.x) {
-        xmn = fmin(xmn, a.bx[i]); xmx = fmax(xmx, a.bx[i]);
-        ymn = fmin(ymn, a.by[i]); ymx = fmax(ymx, a.by[i]);
-    }
-    smax[threadIdx.x] = m; su[threadIdx.x] = s0; sv[threadIdx.x] = s1;
-    bmin[0][threadIdx.x] = xmn; bmax[0][threadIdx.x] = xmx; bmin[1][threadIdx.x] = ymn; bmax[1][threadIdx.x] = ymx;
-    __syncthreads();
-    for (int o = 128; o > 0; o >>= 1) {
-        if (threadIdx.x < o) {
-            const int j = threadIdx.x + o;
-            smax[threadIdx.x] = fmax(smax[threadIdx.x], smax[j]);
-            su[threadIdx.x] += su[j];
-            sv[threadIdx.x] += sv[j];
-            bmin[0][threadIdx.x] = fmin(bmin[0][threadIdx.x], bmin[0][j]);
-            bmax[0][threadIdx.x] = fmax(bmax[0][threadIdx.x], bmax[0][j]);
-            bmin[1][threadIdx.x] = fmin(bmin[1][threadIdx.x], bmin[1][j]);
-            bmax[1][threadIdx.x] = fmax(bmax[1][threadIdx.x], bmax[1][j]);
+    // one warp per statistic (FP64 adds and compares are slow here: each warp reduces its own
+    // quantity with shuffles): 0 max |u|^2, 1 sum u, 2 sum v, 3 min x, 4 max x, 5 min y, 6 max y
+    __shared__ double q[8];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (warp < 3) {
+        const int slot = (warp == 0) ? RED_UMAX2 : (warp == 1 ? RED_SUM_U : RED_SUM_V);
+        double v = 0.0;
+        for (int b = lane; b < a.nblk; b += 32) {
+            const double r = a.red[(size_t)b * RED_NSLOTS + slot];
+            v = (warp == 0) ? fmax(v, r) : v + r;
         }
-        __syncthreads();
+        for (int o = 16; o > 0; o >>= 1) {
+            const double t = __shfl_xor_sync(0xffffffffu, v, o);
+            v = (warp == 0) ? fmax(v, t) : v + t;
+        }
+        if (lane == 0) q[warp] = v;
+    } else if (warp < 7) {
+        const int w = warp - 3;
+        const double* src = (w < 2) ? a.bx : a.by;
+        const bool mx = (w & 1) != 0;
+        double v = mx ? -1e300 : 1e300;
+        for (int i = lane; i < a.ns; i += 32) v = mx ? fmax(v, src[i]) : fmin(v, src[i]);
+        for (int o = 16; o > 0; o >>= 1) {
+            const double t = __shfl_xor_sync(0xffffffffu, v, o);
+            v = mx ? fmax(v, t) : fmin(v, t);
+        }
+        if (lane == 0) q[warp] = v;
     }
+    __syncthreads();
+    double smax[1] = {q[0]}, su[1] = {q[1]}, sv[1] = {q[2]};
+    double bmin[2][1] = {{q[3]}, {q[5]}}, bmax[2][1] = {{q[4]}, {q[6]}};
     DevScalars* S = a.S;
     if (threadIdx.x == 0) {
     if (!a.explicit_step) S->dt0 = S->dt1;
@@ -150,8 +152,8 @@ __global__ void __launch_bounds__(256) k_step_begin(StepArgs a) {
         S->b10 = dt1;
         S->b11 = 0.0;
     }
-    S->mean_u_next = a.U_mean_true * mean_ux(a.iMeanVelocity, time + dt1, a.theta_inf, a.T_fullspeed, a.pi);
-    S->mean_v_next = a.U_mean_true * mean_uy(a.iMeanVelocity, time + dt1, a.theta_inf, a.T_fullspeed, a.pi);
+    S->mean_u_next = a.U_mean_true * mean_ux(a.iMeanVelocity, time + dt1, a.cos_ti, a.T_fullspeed, a.pi);
+    S->mean_v_next = a.U_mean_true * mean_uy(a.iMeanVelocity, time + dt1, a.sin_ti, a.T_fullspeed, a.pi);
     if (a.iBeam > 0) {
         const double r_cyl = 0.0, tb = a.t_beam;
         int iymax = (int)((fmax(bmax[1][0] + 1.5 * tb, a.y0 + 2.0 * r_cyl)) / a.dy);
@@ -170,8 +172,11 @@ __global__ void __launch_bounds__(256) k_step_begin(StepArgs a) {
     __syncthreads();
     // integrating factor exp(-nu dt |k|^2) = exp(coefx kx^2) exp(coefy ky^2) (cal_vis.f90:183-189),
     // one table per direction, FP64 and split FP32 hi + lo
+    // (rebuilt only when dt changed: the tables of the same coefficients are already in place)
     const double dt1 = ((volatile DevScalars*)S)->dt1;
     const double coefx = -dt1 * a.nu * a.scalex, coefy = -dt1 * a.nu * a.scaley;
+    const volatile DevScalars* VS = S;
+    if (VS->etab_valid && VS->etab_cx == coefx && VS->etab_cy == coefy) return;
     const int ntab = a.hx + a.ny / 2 + 1;
     for (int i = threadIdx.x; i < ntab; i += blockDim.x) {
         const double e = (i < a.hx) ? exp(coefx * (double)(i * i)) : exp(coefy * (double)((i - a.hx) * (i - a.hx)));
@@ -179,26 +184,29 @@ __global__ void __launch_bounds__(256) k_step_begin(StepArgs a) {
         const float h = (float)e;
         a.etabf[i] = make_float2(h, (float)(e - (double)h));
     }
+    __syncthreads();
+    if (threadIdx.x == 0) { S->etab_cx = coefx; S->etab_cy = coefy; S->etab_valid = 1; }
 }
 
 // End of the fluid part: cal_energy (NavierStokes.f90:222-263) and cal_drag (:566-589)
 // from the per-block partial sums, summed in a fixed order.
 __global__ void __launch_bounds__(256) k_fluid_finish(StepArgs a) {
-    __shared__ double sm[RED_NSLOTS][256];
-    double acc[RED_NSLOTS];
-    for (int s = 0; s < RED_NSLOTS; ++s) acc[s] = 0.0;
-    for (int b = threadIdx.x; b < a.nblk; b += blockDim.x) {
-        const double* r = a.red + (size_t)b * RED_NSLOTS;
-        for (int s = 0; s < RED_NSLOTS; ++s) acc[s] = (s == RED_UMAX2) ? fmax(acc[s], r[s]) : acc[s] + r[s];
+    // one warp per slot group: warp w reduces slots w and w + 8 with shuffles
+    __shared__ double sm[RED_NSLOTS][1];
+    const int lane = threadIdx.x & 31;
+    for (int s = threadIdx.x >> 5; s < RED_NSLOTS; s += blockDim.x >> 5) {
+        double v = 0.0;
+        for (int b = lane; b < a.nblk; b += 32) {
+            const double r = a.red[(size_t)b * RED_NSLOTS + s];
+            v = (s == RED_UMAX2) ? fmax(v, r) : v + r;
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            const double t = __shfl_xor_sync(0xffffffffu, v, o);
+            v = (s == RED_UMAX2) ? fmax(v, t) : v + t;
+        }
+        if (lane == 0) sm[s][0] = v;
     }
-    for (int s = 0; s < RED_NSLOTS; ++s) sm[s][threadIdx.x] = acc[s];
     __syncthreads();
-    for (int o = 128; o > 0; o >>= 1) {
-        if (threadIdx.x < o)
-            for (int s = 0; s < RED_NSLOTS; ++s)
-                sm[s][threadIdx.x] = (s == RED_UMAX2) ? fmax(sm[s][threadIdx.x], sm[s][threadIdx.x + o]) : sm[s][threadIdx.x] + sm[s][threadIdx.x + o];
-        __syncthreads();
-    }
     if (threadIdx.x != 0) return;
     DevScalars* S = a.S;
     S->mean_u_cur = S->mean_u_next;
@@ -577,6 +585,8 @@ static StepArgs step_args(fsibe_ctx* c, int explicit_step, int nblk) {
     a.by = c->beam[B_Y];
     a.scalex = c->g.scalex;
     a.scaley = c->g.scaley;
+    a.cos_ti = std::cos(c->P.theta_inf);
+    a.sin_ti = std::sin(c->P.theta_inf);
     a.etab = c->etab;
     a.etabf = c->etabf;
     a.hx = c->g.hx;
@@ -595,6 +605,15 @@ static BeamArgs beam_args(fsibe_ctx* c) {
         const double alpha = c->P.angle_beam * c->g.pi / 180.0;
         b.cos_a = std::cos(alpha);
         b.sin_a = std::sin(alpha);
+        const double ds = b.ds, eta = b.eta, ds2 = ds * ds, ds3 = ds * ds * ds, ds4 = (ds * ds) * (ds * ds);
+        b.k.ids = 1.0 / ds;
+        b.k.i2ds = 1.0 / (2.0 * ds);
+        b.k.ids2 = 1.0 / ds2;
+        b.k.i2ds2 = 1.0 / (2.0 * ds2);
+        b.k.ids4 = 1.0 / ds4;
+        b.k.e2ds3 = eta / (2.0 * ds3);
+        b.k.eds4 = eta / ds4;
+        b.k.e2ds4 = eta / (2.0 * ds4);
     }
     b.x = c->beam[B_X]; b.y = c->beam[B_Y]; b.vx = c->beam[B_VX]; b.vy = c->beam[B_VY];
     b.th = c->beam[B_TH]; b.thd = c->beam[B_THD]; b.ax = c->beam[B_AX]; b.ay = c->beam[B_AY];
@@ -674,6 +693,7 @@ static MaskArgs mask_args(fsibe_ctx* c) {
     m.angle_deg = c->P.angle_beam;
     m.x = c->beam[B_X]; m.y = c->beam[B_Y]; m.vx = c->beam[B_VX]; m.vy = c->beam[B_VY]; m.th = c->beam[B_TH];
     m.prims = c->prims; m.nprims = c->nprims; m.rect = c->rect; m.nsm = c->nsm;
+    m.rdx = 1.0 / m.dx; m.rdy = 1.0 / m.dy; m.rpi = 1.0 / m.pi; m.angle_rad = m.angle_deg * m.pi / 180.0;
     m.mask = c->phys[PH_MASK]; m.mvx = c->phys[PH_MVX]; m.mvy = c->phys[PH_MVY];
     return m;
 }
@@ -998,7 +1018,12 @@ int fsibe_create(const fsibe_params* p, fsibe_ctx** out) {
     c->beam_pre_smem = beam_pre_smem_setup(ns);
     ALLOC(c->prims, sizeof(Prim) * (size_t)(2 * ns + 8));
     ALLOC(c->nprims, 16);
-    ALLOC(c->rect, 32);
+    ALLOC(c->rect, 64);
+    {
+        // previous box: none drawn yet (all cells zero); box accumulator: empty
+        const int r0[16] = {0, 0, 0, 0, 0, 0, 0, 0, p->nx, -1, p->ny, -1, 0, 0, 0, 0};
+        cudaMemcpy(c->rect, r0, sizeof(r0), cudaMemcpyHostToDevice);
+    }
     ALLOC(c->counter, 16);
     ALLOC(c->fterm, 16 * (size_t)ns);
     ALLOC(c->S, sizeof(DevScalars));

@@ -480,16 +480,18 @@ struct NewtonCtx {
     double i2ds, ids, ids2, i2ds2, ids4, e2ds3, eds4, e2ds4, g, gds2, gds4e, mue2;
 };
 
-__device__ void newton_consts(NewtonCtx& c, double ds, double eta, double mue) {
-    const double ds2 = ds * ds, ds3 = ds * ds * ds, ds4 = (ds * ds) * (ds * ds);
-    c.ids = 1.0 / ds;
-    c.i2ds = 1.0 / (2.0 * ds);
-    c.ids2 = 1.0 / ds2;
-    c.i2ds2 = 1.0 / (2.0 * ds2);
-    c.ids4 = 1.0 / ds4;
-    c.e2ds3 = eta / (2.0 * ds3);
-    c.eds4 = eta / ds4;
-    c.e2ds4 = eta / (2.0 * ds4);
+// The reciprocal constants: those of ds alone come from the host (BeamArgs::k), those of the
+// step's dt are formed here.
+__device__ void newton_consts(NewtonCtx& c, const BeamArgs& b) {
+    const double eta = b.eta, mue = b.mue, ds2 = b.ds * b.ds, ds4 = ds2 * ds2;
+    c.ids = b.k.ids;
+    c.i2ds = b.k.i2ds;
+    c.ids2 = b.k.ids2;
+    c.i2ds2 = b.k.i2ds2;
+    c.ids4 = b.k.ids4;
+    c.e2ds3 = b.k.e2ds3;
+    c.eds4 = b.k.eds4;
+    c.e2ds4 = b.k.e2ds4;
     c.g = c.dt / (c.C1 * mue);
     c.gds2 = c.dt / (c.C1 * mue * ds2);
     c.gds4e = c.dt * eta / (c.C1 * mue * ds4);
@@ -1000,6 +1002,19 @@ __device__ __forceinline__ void residual_row(const BeamWS& w, int n, int k) {
 // end of the kernel), read by fsibe_beam_phase_cycles.
 #define PH(k) do { const long long t_ = clock64(); ph[k] += t_ - ph_t; ph_t = t_; } while (0)
 
+// Block copy of m float4 with eight loads in flight per thread (the source may be in L2).
+__device__ __forceinline__ void copy_f4(float4* __restrict__ d, const float4* __restrict__ g, size_t m) {
+    size_t q = threadIdx.x;
+    for (; q + 7 * blockDim.x < m; q += 8 * blockDim.x) {
+        float4 v[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) v[u] = g[q + u * blockDim.x];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) d[q + u * blockDim.x] = v[u];
+    }
+    for (; q < m; q += blockDim.x) d[q] = g[q];
+}
+
 // Doubles of the predictor's output: the initial guess x (n), the Crank-Nicolson right-hand
 // side old_rhs, the EE1 angles g5 and the EE1 tension T (ns each).
 __host__ size_t beam_pred_doubles(int ns) { return (size_t)(2 * ns + 4) + 3 * (size_t)ns + 8; }
@@ -1138,8 +1153,8 @@ __global__ void __launch_bounds__(256) k_beam(BeamArgs b) {
             const double C2v = 2.0 * ds * K2 - T[0] * g5[1] + (eta / ds2) * (10.0 * g5[0] - 12.0 * g5[1] + 6.0 * g5[2] - g5[3]);
             w.x[xi_th(-1)] = C2v / ((3.0 * eta / ds2) - T[0]);
             const double K1 = mue * (0.0 * b.cos_a + 0.0 * b.sin_a + grav * b.sin_a) - b.tau_new[0];
-            const double th_ss0 = (2.0 * g5[0] - 5.0 * g5[1] + 4.0 * g5[2] - 1.0 * g5[3]) / ds2;
-            const double th_s0 = (-1.5 * g5[0] + 2.0 * g5[1] - 0.5 * g5[2]) / ds;
+            const double th_ss0 = (2.0 * g5[0] - 5.0 * g5[1] + 4.0 * g5[2] - 1.0 * g5[3]) * b.k.ids2;
+            const double th_s0 = (-1.5 * g5[0] + 2.0 * g5[1] - 0.5 * g5[2]) * b.k.ids;
             const double T_s0 = -eta * th_ss0 * th_s0 + K1;
             w.x[xi_T(ns, -1)] = T[1] - 2.0 * ds * T_s0;
         }
@@ -1150,7 +1165,7 @@ __global__ void __launch_bounds__(256) k_beam(BeamArgs b) {
             cs.time = time; cs.dt = dt; cs.dt_old = dt_old; cs.alpha_t = 0.0; cs.alpha_tt = 0.0; cs.grav = grav;
             solid_coeffs(method, dt, dt_old, cs.C1, cs.C2, cs.C3, cs.C4);
             cs.D = cs.C1 / dt;
-            newton_consts(cs, ds, eta, mue);
+            newton_consts(cs, b);
             cs.K1 = mue * (0.0 * b.cos_a + 0.0 * b.sin_a + grav * b.sin_a) - b.tau_new[0];
             cs.K2 = b.p_new[0] + mue * (0.0 * b.cos_a - 0.0 * b.sin_a + grav * b.cos_a);
         }
@@ -1161,7 +1176,7 @@ __global__ void __launch_bounds__(256) k_beam(BeamArgs b) {
         if (!need_factor && (mode & 2)) {
             const float4* g = reinterpret_cast<const float4*>(b.ws + beam_vec_doubles(ns) + beam_band_doubles(ns));
             float4* d = reinterpret_cast<float4*>(w.Uf);
-            for (size_t q = threadIdx.x; q < beam_fact_floats(ns) / 4; q += blockDim.x) d[q] = g[q];
+            copy_f4(d, g, beam_fact_floats(ns) / 4);
             __syncthreads();
         }
         int iter = 0;
@@ -1281,7 +1296,7 @@ __global__ void __launch_bounds__(256) k_beam(BeamArgs b) {
             if (mode & 2) {
                 float4* g = reinterpret_cast<float4*>(b.ws + beam_vec_doubles(ns) + beam_band_doubles(ns));
                 const float4* d = reinterpret_cast<const float4*>(w.Uf);
-                for (size_t q = threadIdx.x; q < beam_fact_floats(ns) / 4; q += blockDim.x) g[q] = d[q];
+                copy_f4(g, d, beam_fact_floats(ns) / 4);
             }
             if (threadIdx.x == 0) S->beam_fact = 1;
         }
@@ -1309,6 +1324,8 @@ __global__ void __launch_bounds__(256) k_beam(BeamArgs b) {
         w.cs[3 * (ns + 8) + i] = td * cn * ds;
     }
     __syncthreads();
+    // the four running sums in the reference's order: the positions decide grid-aligned
+    // boxes (mask, drag window), so their roundings must be the reference's
     if (threadIdx.x < 4) {
         const int q = threadIdx.x;
         const double* src = w.cs + q * (ns + 8);

@@ -66,6 +66,8 @@ struct DevScalars {
     int32_t run_row, run_cap;        // beam_data ring position / capacity of fsibe_run
     long long phase[32];             // beam kernel phase cycle counters (measurement)
     int32_t beam_fact;               // 1: the global copy of the beam's FP32 band factor is usable
+    int32_t etab_valid;              // 1: the integrating-factor tables hold exp of etab_cx, etab_cy
+    double etab_cx, etab_cy;
 };
 
 // Reduction slots written per block by the velocity/pressure kernel.

@@ -25,99 +25,135 @@ __device__ __forceinline__ void clip_box(int* bx, int nx, int ny) {
     bx[3] = min(bx[3], ny - 1);
 }
 
-// Per-primitive parameters in drawing order: segments, sharp end, hinges, dots.
-__global__ void k_mask_prep(MaskArgs a, double gerf) {
+// q / b correctly rounded from rb = RN(1/b): q0 = RN(q rb), then one FMA correction
+// (Markstein, IBM J. Res. Dev. 34 (1990) 111-119); three FP64 instructions instead of a
+// division sequence.  Valid away from overflow and underflow.
+__device__ __forceinline__ double div_cr(double q, double b, double rb) {
+    const double q0 = q * rb;
+    const double r = fma(-b, q0, q);
+    return fma(r, rb, q0);
+}
+
+// Per-primitive parameters in drawing order: segments, sharp end, hinges, dots (create_mask.f90:
+// 2-218, DrawBeamSegment/DrawHinge/DrawADot).  Thread i of the grid handles node i: segment i
+// (i < ns-1) and the hinge at node i (0 < i < ns-1); threads ns .. ns+2 the sharp end and the
+// dots.  The bounding box of all primitives is reduced with atomics; the last block publishes
+// it with its union with the previous step's box and resets the accumulator.
+__global__ void __launch_bounds__(32) k_mask_prep(MaskArgs a, double gerf) {
     const int ns = a.ns;
     const double dx = a.dx, dy = a.dy, mx = fmax(dx, dy), t = a.t_beam, N = a.N_smooth;
     const double t_star = t + 2.0 * N * mx;
-    const double alpha = a.angle_deg * a.pi / 180.0;  // mouvement case 0
+    const double rdx = a.rdx, rdy = a.rdy;
     const int nseg = ns - 1, nsharp = (a.sharp_trailing == 1) ? 1 : 0, nh = ns - 2;
     const int ndot = (a.sharp_trailing == 0) ? 2 : 1;
     const int total = nseg + nsharp + nh + ndot;
-    __shared__ int rect[4], prev[4];
-    if (threadIdx.x == 0) {
-        rect[0] = a.nx; rect[1] = -1; rect[2] = a.ny; rect[3] = -1;
-        for (int k = 0; k < 4; ++k) prev[k] = a.rect[k];
-    }
-    __syncthreads();
-    for (int q = threadIdx.x; q < total; q += blockDim.x) {
-        Prim P;
-        for (int k = 0; k < 12; ++k) P.p[k] = 0.0;
-        if (q < nseg) {
-            const int i = q;
-            const double p1x = a.x[i], p1y = a.y[i], p2x = a.x[i + 1], p2y = a.y[i + 1];
-            const double al = -atan2((p2y - p1y), (p2x - p1x));
-            P.type = PRIM_SEGMENT;
-            P.box[0] = dnint((fmin(p1x, p2x) - t_star) / dx);
-            P.box[1] = dnint((fmax(p1x, p2x) + t_star) / dx);
-            P.box[2] = dnint((fmin(p1y, p2y) - t_star) / dy);
-            P.box[3] = dnint((fmax(p1y, p2y) + t_star) / dy);
-            const double ca = cos(al), sa = sin(al);
-            P.p[0] = ca; P.p[1] = sa;
-            P.p[2] = ca * p1x - sa * p1y; P.p[3] = sa * p1x + ca * p1y;
-            P.p[4] = ca * p2x - sa * p2y; P.p[5] = sa * p2x + ca * p2y;
-            P.p[6] = a.vx[i]; P.p[7] = a.vy[i]; P.p[8] = a.vx[i + 1]; P.p[9] = a.vy[i + 1];
-        } else if (q < nseg + nsharp) {
-            const int e = ns - 1;
-            const double al = a.th[e] + alpha;
-            const double ca = cos(al), sa = sin(al);
-            const double p1x = a.x[e] - 2.0 * mx * ca, p1y = a.y[e] - 2.0 * mx * sa;
-            const double p2x = a.x[e] + 4.0 * mx * ca, p2y = a.y[e] + 4.0 * mx * sa;
-            P.type = PRIM_SHARP;
-            P.box[0] = dnint((fmin(p1x, p2x) - t_star) / dx);
-            P.box[1] = dnint((fmax(p1x, p2x) + t_star) / dx);
-            P.box[2] = dnint((fmin(p1y, p2y) - t_star) / dy);
-            P.box[3] = dnint((fmax(p1y, p2y) + t_star) / dy);
-            P.p[0] = ca; P.p[1] = sa;
-            P.p[2] = ca * p1x + sa * p1y; P.p[3] = -sa * p1x + ca * p1y;
-            P.p[4] = ca * p2x + sa * p2y; P.p[5] = -sa * p2x + ca * p2y;
-            P.p[6] = a.vx[e]; P.p[7] = a.vy[e];
-        } else if (q < nseg + nsharp + nh) {
-            const int i = q - nseg - nsharp + 1;
-            const double px = a.x[i], py = a.y[i];
-            const double a1 = atan2((a.y[i] - a.y[i - 1]), (a.x[i] - a.x[i - 1]));
-            const double a2 = atan2((a.y[i + 1] - a.y[i]), (a.x[i + 1] - a.x[i]));
-            P.type = PRIM_HINGE;
-            P.box[0] = dnint((px - t_star) / dx);
-            P.box[1] = dnint((px + t_star) / dx);
-            P.box[2] = dnint((py - t_star) / dy);
-            P.box[3] = dnint((py + t_star) / dy);
-            P.p[0] = px; P.p[1] = py;
-            P.p[2] = convert_angle(a1, a.pi) * 180.0 / a.pi;
-            P.p[3] = convert_angle(a2, a.pi) * 180.0 / a.pi;
-            P.p[4] = a.vx[i]; P.p[5] = a.vy[i];
-        } else {
-            // DrawADot runs over the whole grid in the reference; SmoothStep is exactly zero once
-            // both erf arguments exceed ~6 (erf rounds to 1), so the box is cut at t + 10 delta.
-            const int e = (q == total - ndot) ? 0 : ns - 1;
-            const double px = a.x[e], py = a.y[e];
-            if (py < 0.0) set_status(a.S, FSIBE_ERR_MASK_OOB);
-            const double rcut = t + 10.0 * (N * mx) * gerf;
-            P.type = PRIM_DOT;
-            P.box[0] = (int)floor((px - rcut) / dx) - 1;
-            P.box[1] = (int)ceil((px + rcut) / dx) + 1;
-            P.box[2] = (int)floor((py - rcut) / dy) - 1;
-            P.box[3] = (int)ceil((py + rcut) / dy) + 1;
-            P.p[0] = px; P.p[1] = py; P.p[2] = a.vx[e]; P.p[3] = a.vy[e];
-        }
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int bx0 = a.nx, bx1 = -1, by0 = a.ny, by1 = -1;
+    auto emit = [&](int q, Prim& P) {
         clip_box(P.box, a.nx, a.ny);
         a.prims[q] = P;
         if (P.box[0] <= P.box[1] && P.box[2] <= P.box[3]) {
-            atomicMin(&rect[0], P.box[0]);
-            atomicMax(&rect[1], P.box[1]);
-            atomicMin(&rect[2], P.box[2]);
-            atomicMax(&rect[3], P.box[3]);
+            bx0 = min(bx0, P.box[0]); bx1 = max(bx1, P.box[1]);
+            by0 = min(by0, P.box[2]); by1 = max(by1, P.box[3]);
         }
+    };
+    if (i < nseg) {
+        const double p1x = a.x[i], p1y = a.y[i], p2x = a.x[i + 1], p2y = a.y[i + 1];
+        // al = -atan2(p2y - p1y, p2x - p1x): cos(al), sin(al) from the normalised direction
+        const double ddx = p2x - p1x, ddy = p2y - p1y;
+        const double rl = 1.0 / sqrt(ddx * ddx + ddy * ddy);
+        Prim P;
+        for (int k = 0; k < 12; ++k) P.p[k] = 0.0;
+        P.type = PRIM_SEGMENT;
+        P.box[0] = dnint(div_cr(fmin(p1x, p2x) - t_star, dx, rdx));
+        P.box[1] = dnint(div_cr(fmax(p1x, p2x) + t_star, dx, rdx));
+        P.box[2] = dnint(div_cr(fmin(p1y, p2y) - t_star, dy, rdy));
+        P.box[3] = dnint(div_cr(fmax(p1y, p2y) + t_star, dy, rdy));
+        const double ca = ddx * rl, sa = -ddy * rl;
+        P.p[0] = ca; P.p[1] = sa;
+        P.p[2] = ca * p1x - sa * p1y; P.p[3] = sa * p1x + ca * p1y;
+        P.p[4] = ca * p2x - sa * p2y; P.p[5] = sa * p2x + ca * p2y;
+        P.p[6] = a.vx[i]; P.p[7] = a.vy[i]; P.p[8] = a.vx[i + 1]; P.p[9] = a.vy[i + 1];
+        emit(i, P);
     }
-    __syncthreads();
+    if (i >= 1 && i <= ns - 2) {
+        const double px = a.x[i], py = a.y[i];
+        const double a1 = atan2((a.y[i] - a.y[i - 1]), (a.x[i] - a.x[i - 1]));
+        const double a2 = atan2((a.y[i + 1] - a.y[i]), (a.x[i + 1] - a.x[i]));
+        Prim P;
+        for (int k = 0; k < 12; ++k) P.p[k] = 0.0;
+        P.type = PRIM_HINGE;
+        P.box[0] = dnint(div_cr(px - t_star, dx, rdx));
+        P.box[1] = dnint(div_cr(px + t_star, dx, rdx));
+        P.box[2] = dnint(div_cr(py - t_star, dy, rdy));
+        P.box[3] = dnint(div_cr(py + t_star, dy, rdy));
+        P.p[0] = px; P.p[1] = py;
+        P.p[2] = div_cr(convert_angle(a1, a.pi) * 180.0, a.pi, a.rpi);
+        P.p[3] = div_cr(convert_angle(a2, a.pi) * 180.0, a.pi, a.rpi);
+        P.p[4] = a.vx[i]; P.p[5] = a.vy[i];
+        emit(nseg + nsharp + (i - 1), P);
+    }
+    if (i == ns && nsharp) {
+        const int e = ns - 1;
+        const double al = a.th[e] + a.angle_rad;
+        double sa, ca;
+        sincos(al, &sa, &ca);
+        const double p1x = a.x[e] - 2.0 * mx * ca, p1y = a.y[e] - 2.0 * mx * sa;
+        const double p2x = a.x[e] + 4.0 * mx * ca, p2y = a.y[e] + 4.0 * mx * sa;
+        Prim P;
+        for (int k = 0; k < 12; ++k) P.p[k] = 0.0;
+        P.type = PRIM_SHARP;
+        P.box[0] = dnint(div_cr(fmin(p1x, p2x) - t_star, dx, rdx));
+        P.box[1] = dnint(div_cr(fmax(p1x, p2x) + t_star, dx, rdx));
+        P.box[2] = dnint(div_cr(fmin(p1y, p2y) - t_star, dy, rdy));
+        P.box[3] = dnint(div_cr(fmax(p1y, p2y) + t_star, dy, rdy));
+        P.p[0] = ca; P.p[1] = sa;
+        P.p[2] = ca * p1x + sa * p1y; P.p[3] = -sa * p1x + ca * p1y;
+        P.p[4] = ca * p2x + sa * p2y; P.p[5] = -sa * p2x + ca * p2y;
+        P.p[6] = a.vx[e]; P.p[7] = a.vy[e];
+        emit(nseg, P);
+    }
+    if (i >= ns + 1 && i < ns + 1 + ndot) {
+        // DrawADot runs over the whole grid in the reference; SmoothStep is exactly zero once
+        // both erf arguments exceed ~6 (erf rounds to 1), so the box is cut at t + 10 delta.
+        const int d = i - (ns + 1);
+        const int e = (d == 0) ? 0 : ns - 1;
+        const double px = a.x[e], py = a.y[e];
+        if (py < 0.0) set_status(a.S, FSIBE_ERR_MASK_OOB);
+        const double rcut = t + 10.0 * (N * mx) * gerf;
+        Prim P;
+        for (int k = 0; k < 12; ++k) P.p[k] = 0.0;
+        P.type = PRIM_DOT;
+        P.box[0] = (int)floor(div_cr(px - rcut, dx, rdx)) - 1;
+        P.box[1] = (int)ceil(div_cr(px + rcut, dx, rdx)) + 1;
+        P.box[2] = (int)floor(div_cr(py - rcut, dy, rdy)) - 1;
+        P.box[3] = (int)ceil(div_cr(py + rcut, dy, rdy)) + 1;
+        P.p[0] = px; P.p[1] = py; P.p[2] = a.vx[e]; P.p[3] = a.vy[e];
+        emit(nseg + nsharp + nh + d, P);
+    }
+    // the box of all primitives: warp reduction, then atomics on the accumulator rect[8..11]
+    bx0 = __reduce_min_sync(0xffffffffu, bx0);
+    bx1 = __reduce_max_sync(0xffffffffu, bx1);
+    by0 = __reduce_min_sync(0xffffffffu, by0);
+    by1 = __reduce_max_sync(0xffffffffu, by1);
     if (threadIdx.x == 0) {
-        // this step's box and its union with the previous one (whose cells must be cleared)
-        for (int k = 0; k < 4; ++k) a.rect[k] = rect[k];
-        a.rect[4] = min(rect[0], prev[0]);
-        a.rect[5] = max(rect[1], prev[1]);
-        a.rect[6] = min(rect[2], prev[2]);
-        a.rect[7] = max(rect[3], prev[3]);
-        *a.nprims = total;
+        if (bx0 <= bx1) {
+            atomicMin(&a.rect[8], bx0); atomicMax(&a.rect[9], bx1);
+            atomicMin(&a.rect[10], by0); atomicMax(&a.rect[11], by1);
+        }
+        __threadfence();
+        const unsigned done = atomicAdd(reinterpret_cast<unsigned*>(&a.rect[12]), 1u);
+        if (done == gridDim.x - 1) {
+            __threadfence();
+            volatile int* R = a.rect;
+            const int n0 = R[8], n1 = R[9], n2 = R[10], n3 = R[11];
+            const int p0 = R[0], p1 = R[1], p2 = R[2], p3 = R[3];
+            R[0] = n0; R[1] = n1; R[2] = n2; R[3] = n3;
+            R[4] = min(n0, p0); R[5] = max(n1, p1); R[6] = min(n2, p2); R[7] = max(n3, p3);
+            R[8] = a.nx; R[9] = -1; R[10] = a.ny; R[11] = -1;
+            R[12] = 0;
+            *a.nprims = total;
+        }
     }
 }
 
@@ -482,7 +518,9 @@ __global__ void __launch_bounds__(128) k_forces(ForceArgs a, double dxi, double 
 // ===================================================================================
 // Host launchers
 // ===================================================================================
-void launch_mask_prep(const MaskArgs& a, double gerf, cudaStream_t st) { k_mask_prep<<<1, 256, 0, st>>>(a, gerf); }
+void launch_mask_prep(const MaskArgs& a, double gerf, cudaStream_t st) {
+    k_mask_prep<<<(a.ns + 3 + 31) / 32, 32, 0, st>>>(a, gerf);
+}
 void launch_mask(const MaskArgs& a, double gerf, bool fp32, cudaStream_t st) {
     // one-warp blocks, four per SM: a tile per SMSP at a time, spread over the whole chip
     const int blocks = 4 * a.nsm;

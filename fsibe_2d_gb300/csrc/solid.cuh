@@ -20,7 +20,9 @@ struct MaskArgs {
     Prim* prims;
     int* nprims;
     int* rect;    // [0..3] union of this step's primitive boxes (x0, x1, y0, y1), [4..7] its union
-                  // with the previous step's box; every cell outside [0..3] is zero
+                  // with the previous step's box (every cell outside [0..3] is zero), [8..11] the
+                  // accumulator of the next box (empty between steps), [12] blocks done
+    double rdx, rdy, rpi, angle_rad;  // 1/dx, 1/dy, 1/pi (correctly rounded), angle_deg*pi/180
     int nsm;      // SMs of the device (raster grid size)
     void *mask, *mvx, *mvy;  // R*[ny][nx]
 };
@@ -37,11 +39,17 @@ struct ForceArgs {
     int fp32;
 };
 
+// Reciprocal constants of the beam's grid spacing ds (formed on the host).
+struct BeamConsts {
+    double ids, i2ds, ids2, i2ds2, ids4, e2ds3, eds4, e2ds4;
+};
+
 struct BeamArgs {
     DevScalars* S;
     int ns, iImpulse, maxit, iFLUSI;
     double ds, eta, mue, sigma, t_release, tau, tol, pi, x0, y0, angle_deg;
     double cos_a, sin_a;  // cos and sin of the beam angle (angle_deg * pi / 180), from the host
+    BeamConsts k;
     double *x, *y, *vx, *vy, *th, *thd, *ax, *ay, *p_old, *p_new, *tau_old, *tau_new, *oo;
     double* ws;      // global workspace (used when the shared-memory workspace does not fit)
     int use_smem;    // workspace parts in shared memory: 0 none, 1 FP32 factor, 2 + FP64 vectors, 3 + band
