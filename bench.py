@@ -97,13 +97,14 @@ class ClockSampler:
         sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
         mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[i] for s in self.samples for i in range(4) if len(s) > 3 + i and "Active" in s[3 + i]})
+        reasons = sorted({names[i] for s in self.samples for i in range(4) if len(s) > 3 + i and s[3 + i].strip() == "Active"})
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
                 "reasons": reasons, "samples": len(self.samples)}
 
 
 def algorithmic_bytes(kernel, nx, ny, rbytes):
-    """Bytes one launch must move (fields read + written once), per the kernel map in the design doc."""
+    """Bytes one launch must move: the fields it reads and writes, each once (one real field of
+    nx*ny values, or one half spectrum of nx/2*ny complex values, is nx*ny*rbytes bytes)."""
     field = nx * ny * rbytes  # one real field == one half spectrum of complex values
     passes = {"nl_y": 4 + 9, "nl_x": 7 + 2, "press_x": 9 + 9, "press_y": 3, "press_fin": 4, "mask": 3}
     return passes.get(kernel, 0) * field

@@ -79,6 +79,8 @@ struct XRows {
     static constexpr int TR = (G * TR0 >= 32) ? TR0 : 32 / G;
     static constexpr int PL = padded_len(H) + 1;  // row stride (complex) in shared memory
     static constexpr int THREADS = G * TR;
+    // blocks per SM that keep a thread at <= 128 registers
+    static constexpr int MINB128 = (65536 / (THREADS * 128)) > 0 ? 65536 / (THREADS * 128) : 1;
 };
 
 // ---- x-pass helpers -------------------------------------------------------------------
@@ -485,7 +487,9 @@ __global__ void __launch_bounds__(NY / 8) k_nl_y(KArgs<R> a) {
 // stresses to physical space.
 // ======================================================================================
 template <typename R, int H>
-__global__ void __launch_bounds__(XRows<R, H>::THREADS) k_press_x(KArgs<R> a) {
+// (FP32: at most 128 registers a thread, so that two 256-thread blocks share an SM and the
+// 1024^2 grid runs in one wave; FP64 is bound by its arithmetic and keeps its registers)
+__global__ void __launch_bounds__(XRows<R, H>::THREADS, (sizeof(R) == 4) ? XRows<R, H>::MINB128 : 1) k_press_x(KArgs<R> a) {
     using X = XRows<R, H>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C2<R>* bufA = reinterpret_cast<C2<R>*>(smem_raw);

@@ -40,7 +40,7 @@ extern "C" {
 #define FSIBE_ERR_SINGULAR       5  /* zero pivot in an LU (SolidSolver.f90:515-525,1074-1077) */
 #define FSIBE_ERR_INTERP_OOB     6  /* delta-interpolation target or stencil off the grid (Interpolation.f90:19-24) */
 #define FSIBE_ERR_TIMEOUT        7  /* a bounded device-side wait gave up              */
-#define FSIBE_ERR_UNSUPPORTED    8  /* size or option this build does not implement     */
+#define FSIBE_ERR_UNSUPPORTED    8  /* size or option the library does not implement    */
 #define FSIBE_ERR_MASK_OOB       9  /* beam point below the domain (create_mask.f90:685-688) */
 #define FSIBE_ERR_BRAKE         10  /* emergency brake |d theta_dot| > 100 (SolidSolver.f90:370-380);
                                        soft: the reference sets continue_timestep=.false. */
@@ -66,10 +66,10 @@ typedef struct fsibe_params {
     int32_t precision;           /* FSIBE_FP64 or FSIBE_FP32C                                 */
     double  xl, yl;              /* box size                                                  */
     double  nu;                  /* kinematic viscosity = 1/Re                                */
-    double  eps;                 /* penalization parameter (BASELINE's eta)                   */
+    double  eps;                 /* penalization parameter (often written eta)               */
     double  cfl, dt_fixed, time_end;
-    double  eta;                 /* beam stiffness (BASELINE's EI)                            */
-    double  mue;                 /* beam inertia (BASELINE's density ratio)                   */
+    double  eta;                 /* beam stiffness EI                                         */
+    double  mue;                 /* beam inertia (density ratio)                              */
     double  t_release, tau;      /* release time, soft-startup duration                       */
     double  angle_beam;          /* static beam angle, degrees (mouvement.f90:26)             */
     double  grav, sigma;         /* gravity, beam damping                                     */
