@@ -32,6 +32,13 @@ def library():
         L.fsibe_time_steps.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_float)]
         L.fsibe_launches_per_step.argtypes = [C.c_void_p, C.POINTER(C.c_int)]
         L.fsibe_use_graph.argtypes = [C.c_void_p, C.c_int]
+        L.fsibe_ensemble_create.argtypes = [C.POINTER(FsibeParams), C.c_int, C.POINTER(C.c_void_p)]
+        L.fsibe_ensemble_destroy.argtypes = [C.c_void_p]
+        L.fsibe_ensemble_get.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_void_p)]
+        L.fsibe_ensemble_step.argtypes = [C.c_void_p, C.c_int]
+        L.fsibe_ensemble_time_steps.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_float)]
+        L.fsibe_ensemble_last_error.argtypes = [C.c_void_p]
+        L.fsibe_ensemble_last_error.restype = C.c_char_p
         _lib = L
     return _lib
 
@@ -59,3 +66,65 @@ class Run(_Run):
 
     def use_graph(self, enable=True):
         self._call("use_graph", C.c_int(1 if enable else 0))
+
+
+class _EnsembleRun(Run):
+    """One run of an Ensemble: the ensemble owns its context."""
+
+    def __init__(self, ctx, params):
+        self._lib = library()
+        self._prefix = "fsibe_"
+        self.params = params
+        self.nx, self.ny, self.ns = params.nx, params.ny, params.ns
+        self._ctx = ctx
+
+    def close(self):
+        self._ctx = C.c_void_p()
+
+
+class Ensemble:
+    """Independent runs of any sizes advanced together (fsibe_ensemble_*): after the start-up
+    step, one CUDA graph launch per step carries every run's step on its own stream."""
+
+    def __init__(self, params_list):
+        L = library()
+        arr = (FsibeParams * len(params_list))(*params_list)
+        self._e = C.c_void_p()
+        st = L.fsibe_ensemble_create(arr, len(params_list), C.byref(self._e))
+        if st:
+            raise FsibeError(st, "fsibe_ensemble_create", self._err())
+        self.runs = []
+        for i, p in enumerate(params_list):
+            ctx = C.c_void_p()
+            L.fsibe_ensemble_get(self._e, i, C.byref(ctx))
+            self.runs.append(_EnsembleRun(ctx, p))
+
+    def _err(self):
+        m = library().fsibe_ensemble_last_error(self._e if getattr(self, "_e", None) else None)
+        return m.decode() if m else ""
+
+    def step(self, nsteps=1):
+        st = library().fsibe_ensemble_step(self._e, nsteps)
+        if st:
+            raise FsibeError(st, "fsibe_ensemble_step", self._err())
+
+    def time_steps(self, nsteps):
+        """Device milliseconds for nsteps steps of the whole ensemble."""
+        ms = C.c_float()
+        st = library().fsibe_ensemble_time_steps(self._e, nsteps, C.byref(ms))
+        if st:
+            raise FsibeError(st, "fsibe_ensemble_time_steps", self._err())
+        return ms.value
+
+    def close(self):
+        if getattr(self, "_e", None):
+            for r in self.runs:
+                r.close()
+            library().fsibe_ensemble_destroy(self._e)
+            self._e = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:  # pragma: no cover
+            pass

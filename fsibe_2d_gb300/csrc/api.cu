@@ -1448,6 +1448,182 @@ int fsibe_launches_per_step(fsibe_ctx* c, int* n) {
 }  // extern "C"
 
 // =====================================================================================
+// Ensembles: independent runs advanced together, one graph launch per step
+// =====================================================================================
+// Every run keeps its own context (fields, streams, beam workspace).  One step of the
+// ensemble is captured once as a CUDA graph: a fork from the ensemble's stream, each run's
+// whole step on its own stream (with its own predictor fork), and a join.  The runs' kernels
+// of different grid sizes then share the GPU in one launch; the single-CTA beam kernels of
+// many runs fill separate SMs at the same time.
+struct fsibe_ensemble {
+    std::vector<fsibe_ctx*> runs;
+    cudaStream_t master = nullptr;
+    cudaEvent_t fork = nullptr, ev0 = nullptr, ev1 = nullptr;
+    std::vector<cudaEvent_t> done;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t gexec = nullptr;
+    std::string err;
+};
+
+static void ens_free(fsibe_ensemble* e) {
+    if (e->gexec) cudaGraphExecDestroy(e->gexec);
+    if (e->graph) cudaGraphDestroy(e->graph);
+    for (cudaEvent_t ev : e->done) if (ev) cudaEventDestroy(ev);
+    if (e->fork) cudaEventDestroy(e->fork);
+    if (e->ev0) cudaEventDestroy(e->ev0);
+    if (e->ev1) cudaEventDestroy(e->ev1);
+    if (e->master) cudaStreamDestroy(e->master);
+    for (fsibe_ctx* c : e->runs) fsibe_destroy(c);
+    delete e;
+}
+
+#define CKE(ens, call)                                                                  \
+    do {                                                                                \
+        cudaError_t e_ = (call);                                                        \
+        if (e_ != cudaSuccess) {                                                        \
+            (ens)->err = std::string(#call) + ": " + cudaGetErrorString(e_);            \
+            g_err = (ens)->err;                                                         \
+            return FSIBE_ERR_CUDA;                                                      \
+        }                                                                               \
+    } while (0)
+
+// the ensemble's stream waits for every run's stream (work issued on the runs directly), or
+// every run's stream waits for the ensemble's stream
+static int ens_join_runs(fsibe_ensemble* e, bool runs_first) {
+    if (!runs_first) CKE(e, cudaEventRecord(e->fork, e->master));
+    for (size_t i = 0; i < e->runs.size(); ++i) {
+        fsibe_ctx* c = e->runs[i];
+        if (runs_first) {
+            CKE(e, cudaEventRecord(e->done[i], c->stream));
+            CKE(e, cudaStreamWaitEvent(e->master, e->done[i], 0));
+        } else {
+            CKE(e, cudaStreamWaitEvent(c->stream, e->fork, 0));
+        }
+    }
+    return FSIBE_OK;
+}
+
+static int ens_step(fsibe_ensemble* e) {
+    bool started = true;
+    for (fsibe_ctx* c : e->runs) {
+        if (!c->initialized) { e->err = "ensemble step before init_fields of every run"; g_err = e->err; return FSIBE_ERR_STATE; }
+        started = started && c->startup_done;
+    }
+    if (!started) {
+        // the Euler start-up steps, each run on its own stream
+        int st = ens_join_runs(e, false);
+        if (st) return st;
+        for (fsibe_ctx* c : e->runs) {
+            st = c->startup_done ? step_body(c, 0) : step_body(c, 1);
+            if (st) { e->err = c->err; g_err = e->err; return st; }
+            c->startup_done = true;
+        }
+        return ens_join_runs(e, true);
+    }
+    if (!e->gexec) {
+        CKE(e, cudaStreamBeginCapture(e->master, cudaStreamCaptureModeThreadLocal));
+        CKE(e, cudaEventRecord(e->fork, e->master));
+        int st = FSIBE_OK;
+        for (size_t i = 0; i < e->runs.size() && !st; ++i) {
+            fsibe_ctx* c = e->runs[i];
+            if (cudaStreamWaitEvent(c->stream, e->fork, 0) != cudaSuccess) { st = FSIBE_ERR_CUDA; break; }
+            const int before = c->launches;
+            st = step_body(c, 0);
+            c->launches = before;
+            if (st) { e->err = c->err; break; }
+            if (cudaEventRecord(e->done[i], c->stream) != cudaSuccess ||
+                cudaStreamWaitEvent(e->master, e->done[i], 0) != cudaSuccess) st = FSIBE_ERR_CUDA;
+        }
+        cudaGraph_t g = nullptr;
+        const cudaError_t ce = cudaStreamEndCapture(e->master, &g);
+        if (st) { if (g) cudaGraphDestroy(g); g_err = e->err; return st; }
+        if (ce != cudaSuccess) { e->err = std::string("ensemble capture: ") + cudaGetErrorString(ce); g_err = e->err; return FSIBE_ERR_CUDA; }
+        e->graph = g;
+        CKE(e, cudaGraphInstantiate(&e->gexec, g, 0));
+    }
+    CKE(e, cudaGraphLaunch(e->gexec, e->master));
+    return FSIBE_OK;
+}
+
+extern "C" {
+
+int fsibe_ensemble_create(const fsibe_params* params, int nruns, fsibe_ensemble** out) {
+    if (!params || nruns <= 0 || !out) { g_err = "null argument or nruns <= 0"; return FSIBE_ERR_PARAM; }
+    auto* e = new fsibe_ensemble;
+    for (int i = 0; i < nruns; ++i) {
+        fsibe_ctx* c = nullptr;
+        const int st = fsibe_create(&params[i], &c);
+        if (st) { ens_free(e); return st; }
+        e->runs.push_back(c);
+    }
+    cudaError_t ce = cudaStreamCreateWithFlags(&e->master, cudaStreamNonBlocking);
+    if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&e->fork, cudaEventDisableTiming);
+    if (ce == cudaSuccess) ce = cudaEventCreate(&e->ev0);
+    if (ce == cudaSuccess) ce = cudaEventCreate(&e->ev1);
+    e->done.assign(nruns, nullptr);
+    for (int i = 0; i < nruns && ce == cudaSuccess; ++i) ce = cudaEventCreateWithFlags(&e->done[i], cudaEventDisableTiming);
+    if (ce != cudaSuccess) { g_err = cudaGetErrorString(ce); ens_free(e); return FSIBE_ERR_CUDA; }
+    *out = e;
+    return FSIBE_OK;
+}
+
+int fsibe_ensemble_destroy(fsibe_ensemble* e) {
+    if (!e) return FSIBE_OK;
+    cudaStreamSynchronize(e->master);
+    ens_free(e);
+    return FSIBE_OK;
+}
+
+int fsibe_ensemble_size(fsibe_ensemble* e, int* nruns) {
+    if (!e || !nruns) return FSIBE_ERR_PARAM;
+    *nruns = (int)e->runs.size();
+    return FSIBE_OK;
+}
+
+int fsibe_ensemble_get(fsibe_ensemble* e, int run, fsibe_ctx** ctx) {
+    if (!e || !ctx || run < 0 || run >= (int)e->runs.size()) return FSIBE_ERR_PARAM;
+    *ctx = e->runs[run];
+    return FSIBE_OK;
+}
+
+int fsibe_ensemble_step(fsibe_ensemble* e, int nsteps) {
+    if (!e || nsteps < 0) return FSIBE_ERR_PARAM;
+    int st = ens_join_runs(e, true);
+    for (int s = 0; s < nsteps && !st; ++s) st = ens_step(e);
+    if (!st) st = ens_join_runs(e, false);
+    if (st) return st;
+    CKE(e, cudaStreamSynchronize(e->master));
+    for (fsibe_ctx* c : e->runs) {
+        const int rs = read_status(c);
+        if (rs) return rs;
+    }
+    return FSIBE_OK;
+}
+
+int fsibe_ensemble_time_steps(fsibe_ensemble* e, int nsteps, float* ms) {
+    if (!e || !ms || nsteps < 0) return FSIBE_ERR_PARAM;
+    int st = ens_join_runs(e, true);
+    if (st) return st;
+    CKE(e, cudaEventRecord(e->ev0, e->master));
+    for (int s = 0; s < nsteps && !st; ++s) st = ens_step(e);
+    if (st) return st;
+    CKE(e, cudaEventRecord(e->ev1, e->master));
+    CKE(e, cudaEventSynchronize(e->ev1));
+    CKE(e, cudaEventElapsedTime(ms, e->ev0, e->ev1));
+    st = ens_join_runs(e, false);
+    if (st) return st;
+    for (fsibe_ctx* c : e->runs) {
+        const int rs = read_status(c);
+        if (rs) return rs;
+    }
+    return FSIBE_OK;
+}
+
+const char* fsibe_ensemble_last_error(fsibe_ensemble* e) { return e ? e->err.c_str() : g_err.c_str(); }
+
+}  // extern "C"
+
+// =====================================================================================
 // coftxy on caller-owned device buffers with file-scope scratch (allocates nothing)
 // =====================================================================================
 // Scratch for one forward transform: the x-transformed half spectrum T and the result S

@@ -13,6 +13,8 @@
 // chains run in FP32, divisions are taken out of loops.
 #include <math.h>
 
+#include <mutex>
+
 #include "solid.cuh"
 
 namespace fsibe {
@@ -1459,11 +1461,23 @@ void launch_beam(const BeamArgs& b, cudaStream_t st) {
 void launch_beam_pre(const BeamArgs& b, cudaStream_t st) {
     k_beam_pre<<<1, 256, beam_smem_bytes(b.ns, b.use_smem), st>>>(b);
 }
+// The dynamic shared-memory limit of a kernel is one setting per function, shared by every
+// context of the process: it is only ever raised, to the largest size any context needs.
+static bool raise_smem_limit(const void* fn, size_t bytes, size_t* current) {
+    static std::mutex mu;
+    std::lock_guard<std::mutex> lock(mu);
+    if (bytes <= *current) return true;
+    if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) != cudaSuccess) return false;
+    *current = bytes;
+    return true;
+}
+static size_t g_pre_smem = 0, g_beam_smem = 0;
+
 // Shared-memory placement for the predictor kernel: the FP64 vectors when they fit.
 int beam_pre_smem_setup(int ns) {
     const size_t bytes = beam_part_bytes(ns, 2);
     if (bytes > 216 * 1024) return 0;
-    return cudaFuncSetAttribute(k_beam_pre, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) == cudaSuccess ? 4 : 0;
+    return raise_smem_limit((const void*)k_beam_pre, bytes, &g_pre_smem) ? 4 : 0;
 }
 // Shared-memory placement of the beam workspace: parts taken in the order scr, fact, vec,
 // band, each one kept when it still fits in 216 KB.
@@ -1474,7 +1488,7 @@ int beam_smem_setup(int ns) {
         const size_t pb = beam_part_bytes(ns, part);
         if (bytes + pb <= 216 * 1024) { mask |= 1 << part; bytes += pb; }
     }
-    if (mask && cudaFuncSetAttribute(k_beam, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) != cudaSuccess) mask = 0;
+    if (mask && !raise_smem_limit((const void*)k_beam, bytes, &g_beam_smem)) mask = 0;
     return mask;
 }
 void launch_init_beam(const BeamArgs& b, cudaStream_t st) { k_init_beam<<<1, 256, 0, st>>>(b); }

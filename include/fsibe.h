@@ -204,6 +204,24 @@ int fsibe_launches_per_step(fsibe_ctx* ctx, int* launches);
  * launch kernels directly (0, default). */
 int fsibe_use_graph(fsibe_ctx* ctx, int enable);
 
+/* ---- ensembles: independent runs advanced together (batched configuration) -------------
+ * No counterpart in the reference (its batch mode, dns.f90:76-100, runs the parameter sets
+ * one after another).  The runs may differ in grid size, beam size, parameters and precision.
+ * Each run is an ordinary context (fsibe_ensemble_get), initialised and read with the
+ * functions above.  fsibe_ensemble_step advances every run by nsteps; after the first step
+ * (every run's Euler start-up step) one step of all runs is one CUDA graph launch, with each
+ * run's step on its own stream.  Work issued on a run's context directly is ordered before
+ * and after the ensemble's steps. */
+typedef struct fsibe_ensemble fsibe_ensemble;
+int fsibe_ensemble_create(const fsibe_params* params, int nruns, fsibe_ensemble** out);
+int fsibe_ensemble_destroy(fsibe_ensemble* ens);
+int fsibe_ensemble_size(fsibe_ensemble* ens, int* nruns);
+int fsibe_ensemble_get(fsibe_ensemble* ens, int run, fsibe_ctx** ctx);
+int fsibe_ensemble_step(fsibe_ensemble* ens, int nsteps);
+/* Device milliseconds (CUDA events on the ensemble's stream) for nsteps ensemble steps. */
+int fsibe_ensemble_time_steps(fsibe_ensemble* ens, int nsteps, float* ms);
+const char* fsibe_ensemble_last_error(fsibe_ensemble* ens);
+
 /* ---- forward transform without any device allocation ------------------------------
  * No counterpart in the reference.  coftxy (the packed forward transform, same result as
  * fsibe_fft_forward) of a device field f_dev (nx*ny FP64, (0:nx-1,0:ny-1) column-major,
