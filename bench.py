@@ -214,6 +214,7 @@ def gpu_arm(args):
     del vfin
 
     ens = ensemble_c4(F, args) if rank == 0 else None
+    adj = adjoint_c3(F) if rank == 0 else None
 
     cells = NX * NY * world
     val32 = cells * args.steps / (results["fp32c"]["ms"] * 1e-3) / 1e6
@@ -246,7 +247,8 @@ def gpu_arm(args):
             "newton_iters_last_step": results["fp32c"]["newton_iters"],
             "kernel_ms_per_step_fp32c": {k: round(v, 5) for k, v in kt.items()},
             "kernel_ms_per_step_fp64": {k: round(v, 5) for k, v in results["fp64"]["kernels"].items()},
-            "adjoint_over_forward": None,
+            "adjoint_over_forward": adj["ratio_40_snapshots"] if adj else None,
+            "adjoint": adj,
             "measured_gemm_tflops": flops,
             "roofline": roof,
             "cpu_baseline": cpu,
@@ -259,6 +261,34 @@ def gpu_arm(args):
         print(json.dumps(line))
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def adjoint_c3(F):
+    """The adjoint configuration: flat plate of length 1 at 10 degrees incidence, 512^2 box
+    4x4, Re=200, eta=1e-3, dt=1e-4, 2000 steps, mean drag over the last 1000, seeded
+    band-limited initial vorticity (amplitude 1e-2).  Wall time of the gradient (with respect
+    to the initial vorticity, the mask field and nu) over the wall time of the forward run."""
+    n, steps, avg_from = 512, 2000, 1001
+    p = F.make_params(nx=n, ny=n, ns=n // 4, Re=200.0, dt=1e-4, eps=1e-3, cfl=10.0, precision=F.FSIBE_FP64,
+                      angle_beam=10.0, iFLUSI=0, iSaveBeam=0, iMotion=0)
+    r = F.Run(p)
+    w0 = seeded_vorticity(n, K=8, sigma=1e-2, seed=1)
+    r.init_fields(w0)
+    r.drag_objective(w0, 20, 11)
+    t0 = time.perf_counter()
+    J = r.drag_objective(w0, steps, avg_from)
+    t_fwd = time.perf_counter() - t0
+    out = {"workload": "512^2 flat plate at 10 deg, Re=200, eta=1e-3, dt=1e-4, 2000 steps, mean drag of the last 1000",
+           "forward_s": round(t_fwd, 4), "J": J}
+    for snaps, key in ((40, "40_snapshots"), (steps, "all_states")):
+        t0 = time.perf_counter()
+        Jg, gv, gm, gnu, info = r.drag_gradient(w0, steps, avg_from, snapshots=snaps)
+        t = time.perf_counter() - t0
+        out[f"gradient_s_{key}"] = round(t, 4)
+        out[f"ratio_{key}"] = round(t / t_fwd, 3)
+        out[f"forward_steps_{key}"] = info.forward_steps
+    r.close()
+    return out
 
 
 def ensemble_c4(F, args):

@@ -7,6 +7,8 @@ fallback: if the library is missing, `Run(...)` raises.
 import ctypes as C
 import os
 
+import numpy as np
+
 from ._abi import (FsibeParams, FsibeScalars, make_params, BEAM_DATA_COLUMNS, STATUS_NAMES,  # noqa: F401
                    FSIBE_FP64, FSIBE_FP32C, FSIBE_BDF2, FSIBE_CRANK_NICHOLSON, FSIBE_EULER_IMPLICIT)
 from ._binding import FsibeError, declare, Run as _Run  # noqa: F401
@@ -15,6 +17,11 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_lib", "libfsibe_gb300.so")
 
 _lib = None
+
+
+class AdjointInfo(C.Structure):
+    _fields_ = [("forward_steps", C.c_int32), ("adjoint_steps", C.c_int32), ("snapshots", C.c_int32),
+                ("ms_total", C.c_float)]
 
 
 def library():
@@ -39,6 +46,10 @@ def library():
         L.fsibe_ensemble_time_steps.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_float)]
         L.fsibe_ensemble_last_error.argtypes = [C.c_void_p]
         L.fsibe_ensemble_last_error.restype = C.c_char_p
+        _dp = C.POINTER(C.c_double)
+        L.fsibe_drag_objective.argtypes = [C.c_void_p, _dp, C.c_double, C.c_int, C.c_int, _dp]
+        L.fsibe_drag_gradient.argtypes = [C.c_void_p, _dp, C.c_double, C.c_int, C.c_int, C.c_int, _dp, _dp, _dp, _dp,
+                                          C.POINTER(AdjointInfo)]
         _lib = L
     return _lib
 
@@ -66,6 +77,26 @@ class Run(_Run):
 
     def use_graph(self, enable=True):
         self._call("use_graph", C.c_int(1 if enable else 0))
+
+    # -- adjoint on a prescribed rigid mask (FP64 form, iFLUSI = 0) -----------------------
+    def drag_objective(self, vort0, nsteps, avg_from, nu=0.0):
+        """Mean drag after steps avg_from..nsteps from the physical vorticity vort0 (ny, nx)."""
+        v = np.ascontiguousarray(vort0, dtype=np.float64)
+        J = C.c_double()
+        self._call("drag_objective", v.ctypes.data_as(C.POINTER(C.c_double)), C.c_double(nu), C.c_int(nsteps),
+                   C.c_int(avg_from), C.byref(J))
+        return J.value
+
+    def drag_gradient(self, vort0, nsteps, avg_from, nu=0.0, snapshots=40):
+        """(J, dJ/dvort0, dJ/dmask, dJ/dnu, info) by the discrete adjoint with checkpointing."""
+        v = np.ascontiguousarray(vort0, dtype=np.float64)
+        gv = np.empty((self.ny, self.nx))
+        gm = np.empty((self.ny, self.nx))
+        J, gnu, info = C.c_double(), C.c_double(), AdjointInfo()
+        dp = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
+        self._call("drag_gradient", dp(v), C.c_double(nu), C.c_int(nsteps), C.c_int(avg_from), C.c_int(snapshots),
+                   C.byref(J), dp(gv), dp(gm), C.byref(gnu), C.byref(info))
+        return J.value, gv, gm, gnu.value, info
 
 
 class _EnsembleRun(Run):

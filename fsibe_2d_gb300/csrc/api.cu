@@ -11,6 +11,7 @@
 #include <string>
 #include <vector>
 
+#include "adjoint.cuh"
 #include "fluid.cuh"
 #include "solid.cuh"
 
@@ -438,6 +439,7 @@ struct fsibe_ctx {
     cudaStream_t side = nullptr;  // the beam predictor runs here beside the fluid step
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     bool pre_launched = false;    // the predictor of the current step is in flight
+    struct AdjWork* adj = nullptr;  // adjoint buffers and checkpoints (allocated on first use)
     bool initialized = false, startup_done = false;
     bool use_graph = false, graph_ready = false;
     cudaGraphExec_t gexec = nullptr;
@@ -942,9 +944,12 @@ const char* fsibe_strerror(int s) {
 
 const char* fsibe_last_error(const fsibe_ctx* ctx) { return ctx ? ctx->err.c_str() : g_err.c_str(); }
 
+static void adj_free(fsibe_ctx* c);
+
 int fsibe_destroy(fsibe_ctx* c) {
     if (!c) return FSIBE_OK;
     free_graph(c);
+    adj_free(c);
     for (void* p : c->phys) if (p) cudaFree(p);
     for (void* p : c->spec) if (p) cudaFree(p);
     for (double* p : c->beam) if (p) cudaFree(p);
@@ -1151,8 +1156,9 @@ int fsibe_vis(fsibe_ctx* c, double dt, double* w) { return packed_op(c, nullptr,
 int fsibe_dealiase_mask(fsibe_ctx* c, double* d) { return packed_op(c, nullptr, d, PK_DEALIAS, 0.0); }
 
 // ---- the time step ------------------------------------------------------------------
-int fsibe_init_fields(fsibe_ctx* c, const double* vort) {
-    if (!c || !vort) return FSIBE_ERR_PARAM;
+// init_fields (inicond=111): vorticity, velocity, scalars, beam start state; the mask is
+// drawn unless keep_mask (a prescribed mask stays as it is).
+static int init_state(fsibe_ctx* c, const double* vort, bool keep_mask) {
     const size_t NN = (size_t)c->g.nx * c->g.ny;
     const size_t rs = c->fp32 ? 4 : 8;
     free_graph(c);
@@ -1178,12 +1184,19 @@ int fsibe_init_fields(fsibe_ctx* c, const double* vort) {
     CKL(c);
     st = c->fp32 ? init_velocity<float>(c) : init_velocity<double>(c);
     if (st) return st;
-    st = create_mask(c);
-    if (st) return st;
+    if (!keep_mask) {
+        st = create_mask(c);
+        if (st) return st;
+    }
     CK(c, cudaStreamSynchronize(c->stream));
     c->initialized = true;
     c->startup_done = false;
     return FSIBE_OK;
+}
+
+int fsibe_init_fields(fsibe_ctx* c, const double* vort) {
+    if (!c || !vort) return FSIBE_ERR_PARAM;
+    return init_state(c, vort, false);
 }
 
 int fsibe_create_mask(fsibe_ctx* c, double time) {
@@ -1442,6 +1455,417 @@ int fsibe_launches_per_step(fsibe_ctx* c, int* n) {
     if ((P.iFLUSI == 1 || P.iMotion > 0) && P.iBeam > 0) k += 2;  // mask prep + raster
     if (P.iFLUSI == 1) k += 2;  // beam predictor + beam
     *n = k;
+    return FSIBE_OK;
+}
+
+}  // extern "C"
+
+// =====================================================================================
+// Adjoint of the fluid step on a prescribed rigid mask, with binomial checkpointing
+// =====================================================================================
+// Objective: J = mean over the steps n in [avg_from, nsteps] of the drag after step n (the
+// first step is the Euler start-up step).  Gradients of J with respect to the initial
+// vorticity field, the mask field (the reference's `mask` array, chi / eta) and nu.  The
+// forward states (W, M, u, v, scalars) are kept in snapshot slots; the reverse sweep follows
+// the schedule that minimises recomputed forward steps for the given number of slots
+// (binomial checkpointing: C(t, s) = min_j j + C(t - j, s - 1) + C(j, s)).
+// A snapshot holds everything the next step reads: the state W, M, the velocity u, v, the
+// inverse-y derivative spectra Tdx, Tdy that k_nl_x transforms, and the scalars.
+struct AdjSlot {
+    void *W = nullptr, *M = nullptr, *u = nullptr, *v = nullptr, *Tdx = nullptr, *Tdy = nullptr;
+    DevScalars* S = nullptr;
+};
+struct AdjWork {
+    std::vector<void*> spec, phys;  // spectral / physical buffers (FP64)
+    std::vector<AdjSlot> slots;
+    double* part = nullptr;         // block partials
+    double* acc = nullptr;          // [0] J, [1] d J / d nu
+    int nparts = 0;
+    // schedule
+    std::vector<long long> cost;
+    std::vector<int> split;
+    int T = 0, S = 0;
+    // run state
+    int reached = 0, nsteps = 0, avg_from = 0;
+    double dt = 0.0, b10 = 0.0, b11 = 0.0, cobj = 0.0;
+    int win[4] = {0, 0, 0, 0};
+    long long fwd_steps = 0, adj_steps = 0;
+};
+enum AdjSpec { AS_LW = 0, AS_LM, AS_LN, AS_Q, AS_X0, AS_X1, AS_X2, AS_G1, AS_G2, AS_G3, AS_G4, AS_GD, AS_WN, AS_MN, AS_N };
+enum AdjPhys { AP_WX = 0, AP_WY, AP_LNL, AP_LP1, AP_LP2, AP_LU, AP_LV, AP_LWX, AP_LWY, AP_GMASK, AP_UBAR, AP_N };
+
+static void adj_free(fsibe_ctx* c) {
+    AdjWork* w = c->adj;
+    if (!w) return;
+    for (void* p : w->spec) if (p) cudaFree(p);
+    for (void* p : w->phys) if (p) cudaFree(p);
+    for (AdjSlot& sl : w->slots) {
+        for (void* p : {sl.W, sl.M, sl.u, sl.v, sl.Tdx, sl.Tdy}) if (p) cudaFree(p);
+        if (sl.S) cudaFree(sl.S);
+    }
+    if (w->part) cudaFree(w->part);
+    if (w->acc) cudaFree(w->acc);
+    delete w;
+    c->adj = nullptr;
+}
+
+static size_t adj_field_bytes(fsibe_ctx* c) { return 8 * (size_t)c->g.nx * c->g.ny; }
+
+static int adj_alloc(fsibe_ctx* c, int nslots) {
+    if (!c->adj) {
+        c->adj = new AdjWork;
+        AdjWork* w = c->adj;
+        const size_t b = adj_field_bytes(c);
+        w->spec.assign(AS_N, nullptr);
+        w->phys.assign(AP_N, nullptr);
+        for (auto& p : w->spec) CK(c, cudaMalloc(&p, b));
+        for (auto& p : w->phys) CK(c, cudaMalloc(&p, b));
+        w->nparts = 2 * c->nsm;
+        CK(c, cudaMalloc((void**)&w->part, 8 * (size_t)w->nparts));
+        CK(c, cudaMalloc((void**)&w->acc, 64));
+    }
+    AdjWork* w = c->adj;
+    const size_t b = adj_field_bytes(c);
+    while ((int)w->slots.size() < nslots) {
+        AdjSlot sl;
+        CK(c, cudaMalloc(&sl.W, b));
+        CK(c, cudaMalloc(&sl.M, b));
+        CK(c, cudaMalloc(&sl.u, b));
+        CK(c, cudaMalloc(&sl.v, b));
+        CK(c, cudaMalloc(&sl.Tdx, b));
+        CK(c, cudaMalloc(&sl.Tdy, b));
+        CK(c, cudaMalloc((void**)&sl.S, sizeof(DevScalars)));
+        w->slots.push_back(sl);
+    }
+    return FSIBE_OK;
+}
+
+static AdjArgs adj_args(fsibe_ctx* c) {
+    AdjWork* w = c->adj;
+    AdjArgs a;
+    std::memset(&a, 0, sizeof(a));
+    a.g = c->g;
+    a.etab = c->etab;
+    a.dcut = c->dcut;
+    a.b10 = w->b10; a.b11 = w->b11; a.dt = w->dt;
+    auto sp = [&](int i) { return reinterpret_cast<C2<double>*>(w->spec[i]); };
+    auto ph = [&](int i) { return reinterpret_cast<double*>(w->phys[i]); };
+    a.lW = sp(AS_LW); a.lM = sp(AS_LM); a.lN = sp(AS_LN); a.q = sp(AS_Q);
+    a.X0 = sp(AS_X0); a.X1 = sp(AS_X1); a.X2 = sp(AS_X2);
+    a.G1 = sp(AS_G1); a.G2 = sp(AS_G2); a.G3 = sp(AS_G3); a.G4 = sp(AS_G4); a.Gd = sp(AS_GD);
+    a.Wn = sp(AS_WN); a.Mn = sp(AS_MN);
+    a.u = reinterpret_cast<const double*>(c->phys[PH_U]);
+    a.v = reinterpret_cast<const double*>(c->phys[PH_V]);
+    a.mask = reinterpret_cast<const double*>(c->phys[PH_MASK]);
+    a.wx = ph(AP_WX); a.wy = ph(AP_WY); a.lnl = ph(AP_LNL); a.lp1 = ph(AP_LP1); a.lp2 = ph(AP_LP2);
+    a.lu = ph(AP_LU); a.lv = ph(AP_LV); a.lwx = ph(AP_LWX); a.lwy = ph(AP_LWY);
+    a.gmask = ph(AP_GMASK); a.ubar = ph(AP_UBAR);
+    a.part = w->part;
+    a.S = c->S;
+    a.J = w->acc;
+    return a;
+}
+
+// inverse 2D transform of op(spec) into a physical field, forward 2D transform of a physical
+// field into a half spectrum (the ordinary transform kernels, FP64)
+static int adj_inv2d(fsibe_ctx* c, const void* spec, int op, void* phys) {
+    KArgs<double> a = kargs<double>(c);
+    a.spec1 = reinterpret_cast<C2<double>*>(const_cast<void*>(spec));
+    a.spec0 = reinterpret_cast<C2<double>*>(c->spec[SP_0]);
+    a.op = op;
+    launch_y<double>(c, ky_of<double>(c).yinv, ky_of<double>(c).y_smem1, a, "adj_yinv");
+    a.phys0 = reinterpret_cast<double*>(phys);
+    launch_x<double>(c, kx_of<double>(c).xinv, kx_of<double>(c).x_smem1, a, "adj_xinv");
+    CKL(c);
+    return FSIBE_OK;
+}
+static int adj_invx(fsibe_ctx* c, const void* T, void* phys) {
+    KArgs<double> a = kargs<double>(c);
+    a.spec0 = reinterpret_cast<C2<double>*>(const_cast<void*>(T));
+    a.phys0 = reinterpret_cast<double*>(phys);
+    launch_x<double>(c, kx_of<double>(c).xinv, kx_of<double>(c).x_smem1, a, "adj_xinv");
+    CKL(c);
+    return FSIBE_OK;
+}
+static int adj_fwd2d(fsibe_ctx* c, const void* phys, void* spec) {
+    KArgs<double> a = kargs<double>(c);
+    a.phys0 = reinterpret_cast<double*>(const_cast<void*>(phys));
+    a.spec0 = reinterpret_cast<C2<double>*>(c->spec[SP_0]);
+    a.spec1 = reinterpret_cast<C2<double>*>(spec);
+    launch_x<double>(c, kx_of<double>(c).xfwd, kx_of<double>(c).x_smem1, a, "adj_xfwd");
+    launch_y<double>(c, ky_of<double>(c).yfwd, ky_of<double>(c).y_smem1, a, "adj_yfwd");
+    CKL(c);
+    return FSIBE_OK;
+}
+
+static int adj_grid(fsibe_ctx* c) { return 4 * c->nsm; }
+
+static int adj_save(fsibe_ctx* c, int slot) {
+    AdjSlot& sl = c->adj->slots[slot];
+    const size_t b = adj_field_bytes(c);
+    CK(c, cudaMemcpyAsync(sl.W, c->spec[SP_W], b, cudaMemcpyDeviceToDevice, c->stream));
+    CK(c, cudaMemcpyAsync(sl.M, c->spec[SP_M], b, cudaMemcpyDeviceToDevice, c->stream));
+    CK(c, cudaMemcpyAsync(sl.u, c->phys[PH_U], b, cudaMemcpyDeviceToDevice, c->stream));
+    CK(c, cudaMemcpyAsync(sl.v, c->phys[PH_V], b, cudaMemcpyDeviceToDevice, c->stream));
+    CK(c, cudaMemcpyAsync(sl.Tdx, c->spec[SP_TDX], b, cudaMemcpyDeviceToDevice, c->stream));
+    CK(c, cudaMemcpyAsync(sl.Tdy, c->spec[SP_TDY], b, cudaMemcpyDeviceToDevice, c->stream));
+    CK(c, cudaMemcpyAsync(sl.S, c->S, sizeof(DevScalars), cudaMemcpyDeviceToDevice, c->stream));
+    return FSIBE_OK;
+}
+static int adj_restore(fsibe_ctx* c, int slot, int k) {
+    AdjSlot& sl = c->adj->slots[slot];
+    const size_t b = adj_field_bytes(c);
+    CK(c, cudaMemcpyAsync(c->spec[SP_W], sl.W, b, cudaMemcpyDeviceToDevice, c->stream));
+    CK(c, cudaMemcpyAsync(c->spec[SP_M], sl.M, b, cudaMemcpyDeviceToDevice, c->stream));
+    CK(c, cudaMemcpyAsync(c->phys[PH_U], sl.u, b, cudaMemcpyDeviceToDevice, c->stream));
+    CK(c, cudaMemcpyAsync(c->phys[PH_V], sl.v, b, cudaMemcpyDeviceToDevice, c->stream));
+    CK(c, cudaMemcpyAsync(c->spec[SP_TDX], sl.Tdx, b, cudaMemcpyDeviceToDevice, c->stream));
+    CK(c, cudaMemcpyAsync(c->spec[SP_TDY], sl.Tdy, b, cudaMemcpyDeviceToDevice, c->stream));
+    CK(c, cudaMemcpyAsync(c->S, sl.S, sizeof(DevScalars), cudaMemcpyDeviceToDevice, c->stream));
+    c->startup_done = k > 0;
+    return FSIBE_OK;
+}
+
+// objective weight of the drag after step n
+static double adj_weight(const AdjWork* w, int n) {
+    return (n >= w->avg_from && n <= w->nsteps && n >= 1) ? w->cobj : 0.0;
+}
+
+// one forward step from state k; the first time a state is reached its drag (and velocity,
+// for the mask gradient's direct term) enters the objective sums; the final state is kept
+// for the viscosity term of the last step
+static int adj_advance(fsibe_ctx* c, int k, bool gradient) {
+    AdjWork* w = c->adj;
+    int st = do_step(c);
+    if (st) return st;
+    w->fwd_steps++;
+    const int n = k + 1;
+    if (n > w->reached) {
+        w->reached = n;
+        const double cw = adj_weight(w, n);
+        if (cw != 0.0) {
+            AdjArgs a = adj_args(c);
+            a.c_obj = cw;
+            k_adj_accum<<<adj_grid(c), 256, 0, c->stream>>>(a, (size_t)c->g.nx * c->g.ny);
+            CKL(c);
+        }
+        if (gradient && n == w->nsteps) {
+            const size_t b = adj_field_bytes(c);
+            CK(c, cudaMemcpyAsync(w->spec[AS_WN], c->spec[SP_W], b, cudaMemcpyDeviceToDevice, c->stream));
+            CK(c, cudaMemcpyAsync(w->spec[AS_MN], c->spec[SP_M], b, cudaMemcpyDeviceToDevice, c->stream));
+        }
+    }
+    return FSIBE_OK;
+}
+
+// the adjoint of step k (state k loaded): cotangents of state k+1 -> state k
+static int adj_step(fsibe_ctx* c, int k) {
+    AdjWork* w = c->adj;
+    AdjArgs a = adj_args(c);
+    const int G = adj_grid(c);
+    const size_t ncell = (size_t)c->g.nx * c->g.ny;
+    int st;
+    // viscosity term of step k: d W'/d nu = -dt |k|^2 W', d M'/d nu = -dt |k|^2 M'
+    k_adj_nu<<<w->nparts, 256, 0, c->stream>>>(a);
+    k_adj_reduce<<<1, 32, 0, c->stream>>>(w->part, w->nparts, -w->dt, w->acc + 1);
+    // linearisation point of step k: u, v and omega_x, omega_y exactly as k_nl_x forms them
+    // (the x inverse of the state's Tdx, Tdy)
+    if ((st = adj_invx(c, c->spec[SP_TDX], w->phys[AP_WX]))) return st;
+    if ((st = adj_invx(c, c->spec[SP_TDY], w->phys[AP_WY]))) return st;
+    a.euler = (k == 0);
+    k_adj_q<<<G, 256, 0, c->stream>>>(a);
+    k_adj_w3<<<G, 256, 0, c->stream>>>(a);
+    if ((st = adj_inv2d(c, w->spec[AS_X0], OP_ID, w->phys[AP_LNL]))) return st;
+    if ((st = adj_inv2d(c, w->spec[AS_X1], OP_ID, w->phys[AP_LP2]))) return st;
+    if ((st = adj_inv2d(c, w->spec[AS_X2], OP_ID, w->phys[AP_LP1]))) return st;
+    k_adj_phys<<<G, 256, 0, c->stream>>>(a, ncell);
+    if ((st = adj_fwd2d(c, w->phys[AP_LWX], w->spec[AS_G1]))) return st;
+    if ((st = adj_fwd2d(c, w->phys[AP_LWY], w->spec[AS_G2]))) return st;
+    if ((st = adj_fwd2d(c, w->phys[AP_LU], w->spec[AS_G3]))) return st;
+    if ((st = adj_fwd2d(c, w->phys[AP_LV], w->spec[AS_G4]))) return st;
+    a.c_obj = adj_weight(w, k);
+    k_adj_combine<<<G, 256, 0, c->stream>>>(a);
+    CKL(c);
+    // state k for the viscosity term of step k-1
+    const size_t b = adj_field_bytes(c);
+    CK(c, cudaMemcpyAsync(w->spec[AS_WN], c->spec[SP_W], b, cudaMemcpyDeviceToDevice, c->stream));
+    CK(c, cudaMemcpyAsync(w->spec[AS_MN], c->spec[SP_M], b, cudaMemcpyDeviceToDevice, c->stream));
+    w->adj_steps++;
+    return FSIBE_OK;
+}
+
+// binomial schedule: cost[t][s] forward steps to reverse t steps from a stored state with s
+// free slots; split[t][s] the steps to advance before the next snapshot
+static constexpr int kAdjMaxSched = 64;  // slots the schedule table covers (more: a slot per step)
+static void adj_schedule(AdjWork* w, int T, int S) {
+    S = S < kAdjMaxSched ? S : kAdjMaxSched;
+    if (w->T == T && w->S == S) return;
+    w->T = T;
+    w->S = S;
+    const size_t W = (size_t)S + 1;
+    w->cost.assign((size_t)(T + 1) * W, 0);
+    w->split.assign((size_t)(T + 1) * W, 1);
+    for (int t = 1; t <= T; ++t) w->cost[(size_t)t * W] = (long long)t * (t - 1) / 2;
+    for (int s = 1; s <= S; ++s)
+        for (int t = 2; t <= T; ++t) {
+            long long best = -1;
+            int bj = 1;
+            for (int j = 1; j < t; ++j) {
+                const long long v = j + w->cost[(size_t)(t - j) * W + s - 1] + w->cost[(size_t)j * W + s];
+                if (best < 0 || v < best) { best = v; bj = j; }
+            }
+            w->cost[(size_t)t * W + s] = best;
+            w->split[(size_t)t * W + s] = bj;
+        }
+}
+
+// reverse steps [a, a + t) with state a in slot `slot` and s free slots above it
+static int adj_reverse(fsibe_ctx* c, int a, int t, int s, int slot) {
+    AdjWork* w = c->adj;
+    int st;
+    if ((t == 1 || s == 0) && a + t == w->nsteps && w->reached < w->nsteps) {
+        // the last stretch of the first sweep: the final state's drag and fields come first
+        if ((st = adj_restore(c, slot, a))) return st;
+        for (int k = a; k < a + t; ++k)
+            if ((st = adj_advance(c, k, true))) return st;
+    }
+    if (t == 1) {
+        if ((st = adj_restore(c, slot, a))) return st;
+        return adj_step(c, a);
+    }
+    if (s == 0) {
+        for (int k = a + t - 1; k >= a; --k) {
+            if ((st = adj_restore(c, slot, a))) return st;
+            for (int i = a; i < k; ++i)
+                if ((st = adj_advance(c, i, true))) return st;
+            if ((st = adj_step(c, k))) return st;
+        }
+        return FSIBE_OK;
+    }
+    // a slot for every remaining step: advance one step at a time; else the schedule's split
+    const int j = (s >= t - 1) ? 1 : w->split[(size_t)t * (w->S + 1) + (s < w->S ? s : w->S)];
+    if ((st = adj_restore(c, slot, a))) return st;
+    for (int i = a; i < a + j; ++i)
+        if ((st = adj_advance(c, i, true))) return st;
+    if ((st = adj_save(c, slot + 1))) return st;
+    if ((st = adj_reverse(c, a + j, t - j, s - 1, slot + 1))) return st;
+    return adj_reverse(c, a, j, s, slot);
+}
+
+static int adj_check(fsibe_ctx* c, int nsteps, int avg_from) {
+    if (c->fp32) { c->err = "the adjoint runs in the FP64 form"; return FSIBE_ERR_UNSUPPORTED; }
+    if (c->P.iFLUSI != 0 || c->P.iMotion != 0 || c->P.iBeam <= 0) {
+        c->err = "the adjoint needs a prescribed rigid mask (iFLUSI = 0, iMotion = 0, iBeam > 0)";
+        return FSIBE_ERR_UNSUPPORTED;
+    }
+    if (nsteps < 1 || avg_from < 1 || avg_from > nsteps) { c->err = "need 1 <= avg_from <= nsteps"; return FSIBE_ERR_PARAM; }
+    return FSIBE_OK;
+}
+
+// state 0 from vort0 (the mask kept), nu set, the drag window known
+static int adj_begin(fsibe_ctx* c, const double* vort0, double nu, int nsteps, int avg_from, int nslots) {
+    int st = adj_alloc(c, nslots);
+    if (st) return st;
+    AdjWork* w = c->adj;
+    if (nu > 0.0 && nu != c->P.nu) {
+        c->P.nu = nu;
+        free_graph(c);
+    }
+    if ((st = init_state(c, vort0, true))) return st;
+    w->nsteps = nsteps;
+    w->avg_from = avg_from;
+    w->cobj = 1.0 / (double)(nsteps - avg_from + 1);
+    w->reached = 0;
+    w->fwd_steps = w->adj_steps = 0;
+    CK(c, cudaMemsetAsync(w->acc, 0, 64, c->stream));
+    CK(c, cudaMemsetAsync(w->phys[AP_UBAR], 0, adj_field_bytes(c), c->stream));
+    CK(c, cudaMemsetAsync(w->phys[AP_GMASK], 0, adj_field_bytes(c), c->stream));
+    return adj_save(c, 0);
+}
+
+extern "C" {
+
+int fsibe_drag_objective(fsibe_ctx* c, const double* vort0, double nu, int nsteps, int avg_from, double* J) {
+    if (!c || !vort0 || !J) return FSIBE_ERR_PARAM;
+    int st = adj_check(c, nsteps, avg_from);
+    if (st) return st;
+    if ((st = adj_begin(c, vort0, nu, nsteps, avg_from, 1))) return st;
+    for (int k = 0; k < nsteps; ++k)
+        if ((st = adj_advance(c, k, false))) return st;
+    CK(c, cudaMemcpyAsync(J, c->adj->acc, 8, cudaMemcpyDeviceToHost, c->stream));
+    CK(c, cudaStreamSynchronize(c->stream));
+    return read_status(c);
+}
+
+int fsibe_drag_gradient(fsibe_ctx* c, const double* vort0, double nu, int nsteps, int avg_from, int snapshots,
+                        double* J, double* g_vort0, double* g_mask, double* g_nu, fsibe_adjoint_info* info) {
+    if (!c || !vort0) return FSIBE_ERR_PARAM;
+    int st = adj_check(c, nsteps, avg_from);
+    if (st) return st;
+    if (snapshots < 1) snapshots = 1;
+    if (snapshots > nsteps) snapshots = nsteps;
+    CK(c, cudaEventRecord(c->ev0, c->stream));
+    if ((st = adj_begin(c, vort0, nu, nsteps, avg_from, snapshots + 1))) return st;
+    AdjWork* w = c->adj;
+    // time step and AB2 weights (fixed dt), the drag window: from one start-up step
+    if ((st = adj_advance(c, 0, true))) return st;
+    DevScalars h;
+    CK(c, cudaMemcpyAsync(&h, c->S, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+    CK(c, cudaStreamSynchronize(c->stream));
+    w->dt = h.dt1;
+    w->b10 = 1.5 * h.dt1;
+    w->b11 = -0.5 * h.dt1;
+    for (int q = 0; q < 4; ++q) w->win[q] = h.win[q];
+    // d drag / d W (constant: the mask and the window are fixed)
+    AdjArgs a = adj_args(c);
+    const int G = adj_grid(c);
+    k_adj_window<<<G, 256, 0, c->stream>>>(a, w->win[0], w->win[1], w->win[2], w->win[3], 0);
+    if ((st = adj_fwd2d(c, w->phys[AP_LU], w->spec[AS_G3]))) return st;
+    k_adj_gdrag<<<G, 256, 0, c->stream>>>(a);
+    CKL(c);
+    // the reverse sweep from the cotangents of the final state
+    if (snapshots < nsteps - 1) adj_schedule(w, nsteps, snapshots);
+    const size_t b = adj_field_bytes(c);
+    CK(c, cudaMemsetAsync(w->spec[AS_LW], 0, b, c->stream));
+    CK(c, cudaMemsetAsync(w->spec[AS_LM], 0, b, c->stream));
+    {
+        // lW(T) = c_T d drag / d W: q <- 0, G1..G4 <- 0 and one combine
+        for (int i : {AS_Q, AS_G1, AS_G2, AS_G3, AS_G4}) CK(c, cudaMemsetAsync(w->spec[i], 0, b, c->stream));
+        a.c_obj = adj_weight(w, nsteps);
+        k_adj_combine<<<G, 256, 0, c->stream>>>(a);
+        CKL(c);
+    }
+    if ((st = adj_reverse(c, 0, nsteps, snapshots, 0))) return st;
+    // the direct term of the mask gradient, then the outputs
+    k_adj_window<<<G, 256, 0, c->stream>>>(a, w->win[0], w->win[1], w->win[2], w->win[3], 1);
+    CKL(c);
+    CK(c, cudaEventRecord(c->ev1, c->stream));
+    double acc[2];
+    CK(c, cudaMemcpyAsync(acc, w->acc, 16, cudaMemcpyDeviceToHost, c->stream));
+    CK(c, cudaStreamSynchronize(c->stream));
+    if ((st = read_status(c))) return st;
+    if (J) *J = acc[0];
+    if (g_nu) *g_nu = acc[1];
+    const size_t NN = (size_t)c->g.nx * c->g.ny;
+    if (g_mask) {
+        if ((st = to_host(c, w->phys[AP_GMASK], NN, g_mask))) return st;
+    }
+    if (g_vort0) {
+        // W0 = F(omega0): d J / d omega0 = F^T lW(0) = Phi(w lW(0)) / (nx ny)
+        CK(c, cudaMemcpyAsync(w->spec[AS_LN], w->spec[AS_LW], b, cudaMemcpyDeviceToDevice, c->stream));
+        k_adj_w3<<<G, 256, 0, c->stream>>>(a);
+        CKL(c);
+        if ((st = adj_inv2d(c, w->spec[AS_X0], OP_ID, w->phys[AP_LNL]))) return st;
+        if ((st = to_host(c, w->phys[AP_LNL], NN, g_vort0))) return st;
+    }
+    if (info) {
+        info->forward_steps = (int32_t)w->fwd_steps;
+        info->adjoint_steps = (int32_t)w->adj_steps;
+        info->snapshots = snapshots;
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+        info->ms_total = ms;
+    }
     return FSIBE_OK;
 }
 

@@ -204,6 +204,29 @@ int fsibe_launches_per_step(fsibe_ctx* ctx, int* launches);
  * launch kernels directly (0, default). */
 int fsibe_use_graph(fsibe_ctx* ctx, int enable);
 
+/* ---- adjoint of the fluid step on a prescribed rigid mask --------------------------------
+ * No counterpart in the reference.  For a context with a prescribed rigid mask (iFLUSI = 0,
+ * iMotion = 0, iBeam > 0, FP64 form; the mask is drawn by fsibe_init_fields or set with
+ * fsibe_upload_mask and is kept by these calls):
+ *   J = mean of the drag (Force(1), cal_drag NavierStokes.f90:567) after the steps
+ *       avg_from .. nsteps, the first step being the Euler start-up step, starting from the
+ *       physical vorticity vort0 ((0:nx-1,0:ny-1) column-major) with viscosity nu (nu <= 0:
+ *       the context's).  fsibe_drag_objective returns J alone.
+ *   fsibe_drag_gradient also returns dJ/d vort0 (nx*ny), dJ/d mask (nx*ny, the reference's
+ *       `mask` array, chi/eta) and dJ/d nu, by the discrete adjoint of the step (transposed
+ *       transforms, linearised advection and penalization).  Forward states are kept in
+ *       `snapshots` slots and recomputed between them on the binomial schedule; with
+ *       snapshots >= nsteps - 1 every state is kept.  Any output pointer may be NULL. */
+typedef struct fsibe_adjoint_info {
+    int32_t forward_steps;   /* forward steps taken, recomputation included               */
+    int32_t adjoint_steps;
+    int32_t snapshots;
+    float   ms_total;        /* device time of the whole gradient computation            */
+} fsibe_adjoint_info;
+int fsibe_drag_objective(fsibe_ctx* ctx, const double* vort0, double nu, int nsteps, int avg_from, double* J);
+int fsibe_drag_gradient(fsibe_ctx* ctx, const double* vort0, double nu, int nsteps, int avg_from, int snapshots,
+                        double* J, double* g_vort0, double* g_mask, double* g_nu, fsibe_adjoint_info* info);
+
 /* ---- ensembles: independent runs advanced together (batched configuration) -------------
  * No counterpart in the reference (its batch mode, dns.f90:76-100, runs the parameter sets
  * one after another).  The runs may differ in grid size, beam size, parameters and precision.

@@ -1,0 +1,129 @@
+"""Adjoint of the fluid step on a prescribed rigid mask (fsibe_drag_gradient).
+
+The objective is the mean drag over the last steps of a run past a flat plate at 10 degrees
+incidence (the adjoint configuration, at a reduced size and step count).  The gradient with
+respect to the initial vorticity, the mask field and nu is checked against FP64 central
+finite differences of the objective along seeded random directions, through a
+torch.autograd.Function (the gradient-check harness), and against itself with different
+snapshot counts (the checkpointing schedule must not change the result)."""
+import numpy as np
+import pytest
+
+from conftest import seeded_vorticity
+from fsibe_2d_gb300 import make_params, FSIBE_FP64
+
+pytestmark = pytest.mark.gpu
+
+N, STEPS, AVG_FROM = 128, 40, 21
+
+
+def _run():
+    import fsibe_2d_gb300 as F
+    p = make_params(nx=N, ny=N, ns=N // 4, Re=200.0, dt=1e-4, eps=1e-3, cfl=10.0, precision=FSIBE_FP64,
+                    angle_beam=10.0, iFLUSI=0, iSaveBeam=0, iMotion=0)
+    r = F.Run(p)
+    w0 = seeded_vorticity(N, K=8, sigma=1e-2, seed=1)
+    r.init_fields(w0)   # draws the plate's mask; the adjoint calls keep it
+    return r, w0, p
+
+
+def _set_mask(r, m):
+    _, vx, vy = r.mask()
+    r.set_mask(m, vx, vy)
+
+
+def test_gradient_matches_central_differences_through_autograd():
+    torch = pytest.importorskip("torch")
+    r, w0, p = _run()
+    m0 = r.mask()[0].copy()
+    nu0 = p.nu
+
+    class DragObjective(torch.autograd.Function):
+        @staticmethod
+        def forward(ctx, vort, mask, nu):
+            _set_mask(r, mask.detach().numpy())
+            J, gv, gm, gnu, _ = r.drag_gradient(vort.detach().numpy(), STEPS, AVG_FROM, nu=float(nu), snapshots=6)
+            ctx.save_for_backward(torch.from_numpy(gv), torch.from_numpy(gm), torch.tensor(gnu, dtype=torch.float64))
+            return torch.tensor(J, dtype=torch.float64)
+
+        @staticmethod
+        def backward(ctx, g):
+            gv, gm, gnu = ctx.saved_tensors
+            return g * gv, g * gm, g * gnu
+
+    v = torch.tensor(w0, requires_grad=True)
+    m = torch.tensor(m0, requires_grad=True)
+    nu = torch.tensor(nu0, dtype=torch.float64, requires_grad=True)
+    J = DragObjective.apply(v, m, nu)
+    J.backward()
+    gv, gm, gnu = v.grad.numpy(), m.grad.numpy(), float(nu.grad)
+    assert np.isfinite(gv).all() and np.isfinite(gm).all() and np.isfinite(gnu)
+
+    def objective(vv, mm, nn):
+        _set_mask(r, mm)
+        return r.drag_objective(vv, STEPS, AVG_FROM, nu=nn)
+
+    J0 = objective(w0, m0, nu0)
+    assert abs(J0 - float(J)) <= 1e-13 * abs(J0)
+    rng = np.random.default_rng(20)
+    eps = 1e-6
+    for k in range(4):
+        dv = 1e-2 * rng.standard_normal(w0.shape)
+        dm = np.abs(m0).max() * rng.standard_normal(m0.shape)
+        dn = nu0 * rng.standard_normal()
+        if k == 0:
+            dm[:] = 0.0; dn = 0.0           # vorticity only
+        elif k == 1:
+            dv[:] = 0.0; dn = 0.0           # mask only
+        elif k == 2:
+            dv[:] = 0.0; dm[:] = 0.0        # viscosity only
+        jp = objective(w0 + eps * dv, m0 + eps * dm, nu0 + eps * dn)
+        jm = objective(w0 - eps * dv, m0 - eps * dm, nu0 - eps * dn)
+        fd = (jp - jm) / (2 * eps)
+        ad = float((gv * dv).sum() + (gm * dm).sum() + gnu * dn)
+        assert abs(ad - fd) <= 1e-6 * max(abs(fd), 1e-12 * abs(J0)), (k, ad, fd)
+    r.close()
+
+
+def test_snapshot_count_does_not_change_the_gradient():
+    r, w0, p = _run()
+    out = [r.drag_gradient(w0, STEPS, AVG_FROM, snapshots=s) for s in (1, 3, STEPS)]
+    J1, gv1, gm1, gn1, i1 = out[0]
+    for J, gv, gm, gn, info in out[1:]:
+        assert J == J1
+        assert np.array_equal(gv, gv1) and np.array_equal(gm, gm1) and gn == gn1
+    # fewer slots, more recomputation; with a slot per step no state is recomputed
+    assert out[0][4].forward_steps > out[1][4].forward_steps > out[2][4].forward_steps
+    assert out[2][4].adjoint_steps == STEPS
+    r.close()
+
+
+def test_adjoint_configuration_twenty_directions():
+    """The adjoint configuration at its stated size: 512^2, Re=200, eta=1e-3, dt=1e-4, 2000
+    steps, mean drag over the last 1000, binomial checkpointing with 40 snapshots; central
+    differences (eps = 1e-6) along 20 seeded random directions in (vort0, mask, nu)."""
+    import fsibe_2d_gb300 as F
+    n, steps, avg_from = 512, 2000, 1001
+    p = make_params(nx=n, ny=n, ns=n // 4, Re=200.0, dt=1e-4, eps=1e-3, cfl=10.0, precision=FSIBE_FP64,
+                    angle_beam=10.0, iFLUSI=0, iSaveBeam=0, iMotion=0)
+    r = F.Run(p)
+    w0 = seeded_vorticity(n, K=8, sigma=1e-2, seed=1)
+    r.init_fields(w0)
+    m0, vx, vy = (a.copy() for a in r.mask())
+    J, gv, gm, gnu, info = r.drag_gradient(w0, steps, avg_from, snapshots=40)
+    assert info.adjoint_steps == steps and info.forward_steps < 3 * steps
+    rng = np.random.default_rng(3)
+    eps, worst = 1e-6, 0.0
+    for k in range(20):
+        dv = 1e-2 * rng.standard_normal(w0.shape)
+        dm = np.abs(m0).max() * rng.standard_normal(m0.shape)
+        dn = p.nu * rng.standard_normal()
+        r.set_mask(m0 + eps * dm, vx, vy)
+        jp = r.drag_objective(w0 + eps * dv, steps, avg_from, nu=p.nu + eps * dn)
+        r.set_mask(m0 - eps * dm, vx, vy)
+        jm = r.drag_objective(w0 - eps * dv, steps, avg_from, nu=p.nu - eps * dn)
+        fd = (jp - jm) / (2 * eps)
+        ad = float((gv * dv).sum() + (gm * dm).sum() + gnu * dn)
+        worst = max(worst, abs(ad - fd) / abs(fd))
+    assert worst <= 1e-6, worst
+    r.close()
