@@ -385,20 +385,22 @@ def reference_arm(args):
         return
     threads = os.cpu_count() or 1
     total_dt = 0.0
-    for _ in range(args.warmup):
+    # a bounded sample: at most 200 CPU steps (about 10 s on 16 cores) whatever --steps says
+    K = min(args.steps, int(os.environ.get("FSIBE_REF_MAX_STEPS", "200")))
+    for _ in range(min(args.warmup, 3)):
         oracle_steps(1, threads)
-    dt, used = oracle_steps(args.steps, threads)
+    dt, used = oracle_steps(K, threads)
     total_dt += dt
-    val = NX * NY * args.steps / total_dt / 1e6
+    val = NX * NY * K / total_dt / 1e6
     line = {
         "impl": "reference", "metric": METRIC, "value": round(val, 3), "unit": "Mcell-steps/s", "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * total_dt / args.steps, 3),
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * total_dt / K, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp64",
         "data": "synthetic (seeded N(0,1e-3) vorticity, |k|<=8)",
         "config": {"workload": "precision form: 1024^2 box 4x4, ns=256, Re=500, dt=5e-5, clamped flexible beam EI=0.1, mu=1, eta=1e-3",
                    "nx": NX, "ny": NY, "ns": NS},
         "cpu_baseline": {"value": round(val, 3), "unit": "Mcell-steps/s", "cores": used, "kind": "port",
-                         "sample": f"{args.steps} FP64 AB2 steps at 1024^2 (CPU restatement; the Fortran/FFTW/MKL build is unavailable here)"},
+                         "sample": f"{K} FP64 AB2 steps at 1024^2 (CPU restatement; the Fortran/FFTW/MKL build is unavailable here)"},
         "e2e": {"value": round(val, 3), "unit": "Mcell-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
@@ -407,8 +409,9 @@ def reference_arm(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=50)
-    ap.add_argument("--warmup", type=int, default=5)
+    # 1000 steps keep the timed region (about 0.5 s) long enough for the clock sampler
+    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--err-steps", type=int, default=200)
     args = ap.parse_args()
