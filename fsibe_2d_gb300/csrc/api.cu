@@ -540,18 +540,20 @@ template <> SizeKernels<float>& ky_of<float>(fsibe_ctx* c) { return c->kyf; }
 
 // launch helpers (count launches for the bench's gpu_launches)
 template <typename R>
-static void launch_x(fsibe_ctx* c, void (*k)(KArgs<R>), int smem, const KArgs<R>& a, const char* name = "x_pass") {
+static void launch_x(fsibe_ctx* c, void (*k)(KArgs<R>), int smem, const KArgs<R>& a, const char* name = "x_pass",
+                     int nfields = 1) {
     const SizeKernels<R>& K = kx_of<R>(c);
     prof_begin(c, name);
-    k<<<c->g.ny / K.x_rows, K.x_threads, smem, c->stream>>>(a);
+    k<<<dim3(c->g.ny / K.x_rows, nfields), K.x_threads, smem, c->stream>>>(a);
     prof_end(c);
     c->launches++;
 }
 template <typename R>
-static void launch_y(fsibe_ctx* c, void (*k)(KArgs<R>), int smem, const KArgs<R>& a, const char* name = "y_pass") {
+static void launch_y(fsibe_ctx* c, void (*k)(KArgs<R>), int smem, const KArgs<R>& a, const char* name = "y_pass",
+                     int nfields = 1) {
     const SizeKernels<R>& K = ky_of<R>(c);
     prof_begin(c, name);
-    k<<<c->g.hx, K.y_threads, smem, c->stream>>>(a);
+    k<<<dim3(c->g.hx, nfields), K.y_threads, smem, c->stream>>>(a);
     prof_end(c);
     c->launches++;
 }
@@ -1491,8 +1493,13 @@ struct AdjWork {
     int win[4] = {0, 0, 0, 0};
     long long fwd_steps = 0, adj_steps = 0;
 };
-enum AdjSpec { AS_LW = 0, AS_LM, AS_LN, AS_Q, AS_X0, AS_X1, AS_X2, AS_G1, AS_G2, AS_G3, AS_G4, AS_GD, AS_WN, AS_MN, AS_N };
-enum AdjPhys { AP_WX = 0, AP_WY, AP_LNL, AP_LP1, AP_LP2, AP_LU, AP_LV, AP_LWX, AP_LWY, AP_GMASK, AP_UBAR, AP_N };
+// buffers (fields of nx*ny doubles); the blocks X (X0, X1, X2), G (G1..G4), T (transform
+// scratch), P (lnl, lp2, lp1) and L (lwx, lwy, lu, lv) are contiguous, so that one launch
+// transforms all of their fields
+enum AdjSpec { AS_LW = 0, AS_LM, AS_LN, AS_Q, AS_X, AS_G, AS_GD, AS_WN, AS_MN, AS_T, AS_N };
+enum AdjPhys { AP_WX = 0, AP_WY, AP_P, AP_L, AP_GMASK, AP_UBAR, AP_N };
+static int adj_spec_fields(int i) { return i == AS_X ? 3 : (i == AS_G || i == AS_T) ? 4 : 1; }
+static int adj_phys_fields(int i) { return i == AP_P ? 3 : i == AP_L ? 4 : 1; }
 
 static void adj_free(fsibe_ctx* c) {
     AdjWork* w = c->adj;
@@ -1518,8 +1525,8 @@ static int adj_alloc(fsibe_ctx* c, int nslots) {
         const size_t b = adj_field_bytes(c);
         w->spec.assign(AS_N, nullptr);
         w->phys.assign(AP_N, nullptr);
-        for (auto& p : w->spec) CK(c, cudaMalloc(&p, b));
-        for (auto& p : w->phys) CK(c, cudaMalloc(&p, b));
+        for (int i = 0; i < AS_N; ++i) CK(c, cudaMalloc(&w->spec[i], b * adj_spec_fields(i)));
+        for (int i = 0; i < AP_N; ++i) CK(c, cudaMalloc(&w->phys[i], b * adj_phys_fields(i)));
         w->nparts = 2 * c->nsm;
         CK(c, cudaMalloc((void**)&w->part, 8 * (size_t)w->nparts));
         CK(c, cudaMalloc((void**)&w->acc, 64));
@@ -1550,15 +1557,18 @@ static AdjArgs adj_args(fsibe_ctx* c) {
     a.b10 = w->b10; a.b11 = w->b11; a.dt = w->dt;
     auto sp = [&](int i) { return reinterpret_cast<C2<double>*>(w->spec[i]); };
     auto ph = [&](int i) { return reinterpret_cast<double*>(w->phys[i]); };
+    const size_t F = (size_t)c->g.hx * c->g.ny, N = (size_t)c->g.nx * c->g.ny;
     a.lW = sp(AS_LW); a.lM = sp(AS_LM); a.lN = sp(AS_LN); a.q = sp(AS_Q);
-    a.X0 = sp(AS_X0); a.X1 = sp(AS_X1); a.X2 = sp(AS_X2);
-    a.G1 = sp(AS_G1); a.G2 = sp(AS_G2); a.G3 = sp(AS_G3); a.G4 = sp(AS_G4); a.Gd = sp(AS_GD);
+    a.X0 = sp(AS_X); a.X1 = sp(AS_X) + F; a.X2 = sp(AS_X) + 2 * F;
+    a.G1 = sp(AS_G); a.G2 = sp(AS_G) + F; a.G3 = sp(AS_G) + 2 * F; a.G4 = sp(AS_G) + 3 * F;
+    a.Gd = sp(AS_GD);
     a.Wn = sp(AS_WN); a.Mn = sp(AS_MN);
     a.u = reinterpret_cast<const double*>(c->phys[PH_U]);
     a.v = reinterpret_cast<const double*>(c->phys[PH_V]);
     a.mask = reinterpret_cast<const double*>(c->phys[PH_MASK]);
-    a.wx = ph(AP_WX); a.wy = ph(AP_WY); a.lnl = ph(AP_LNL); a.lp1 = ph(AP_LP1); a.lp2 = ph(AP_LP2);
-    a.lu = ph(AP_LU); a.lv = ph(AP_LV); a.lwx = ph(AP_LWX); a.lwy = ph(AP_LWY);
+    a.wx = ph(AP_WX); a.wy = ph(AP_WY);
+    a.lnl = ph(AP_P); a.lp2 = ph(AP_P) + N; a.lp1 = ph(AP_P) + 2 * N;
+    a.lwx = ph(AP_L); a.lwy = ph(AP_L) + N; a.lu = ph(AP_L) + 2 * N; a.lv = ph(AP_L) + 3 * N;
     a.gmask = ph(AP_GMASK); a.ubar = ph(AP_UBAR);
     a.part = w->part;
     a.S = c->S;
@@ -1566,16 +1576,18 @@ static AdjArgs adj_args(fsibe_ctx* c) {
     return a;
 }
 
-// inverse 2D transform of op(spec) into a physical field, forward 2D transform of a physical
-// field into a half spectrum (the ordinary transform kernels, FP64)
-static int adj_inv2d(fsibe_ctx* c, const void* spec, int op, void* phys) {
+// inverse 2D transforms of nf consecutive half spectra into nf consecutive physical fields,
+// x inverses of given y-inverted spectra, and forward 2D transforms of nf consecutive physical
+// fields (the ordinary transform kernels, FP64, one launch per pass for all fields)
+static int adj_inv2d(fsibe_ctx* c, const void* spec, int nf, void* phys) {
     KArgs<double> a = kargs<double>(c);
+    a.bstride = (size_t)c->g.hx * c->g.ny;
     a.spec1 = reinterpret_cast<C2<double>*>(const_cast<void*>(spec));
-    a.spec0 = reinterpret_cast<C2<double>*>(c->spec[SP_0]);
-    a.op = op;
-    launch_y<double>(c, ky_of<double>(c).yinv, ky_of<double>(c).y_smem1, a, "adj_yinv");
+    a.spec0 = reinterpret_cast<C2<double>*>(c->adj->spec[AS_T]);
+    a.op = OP_ID;
+    launch_y<double>(c, ky_of<double>(c).yinv, ky_of<double>(c).y_smem1, a, "adj_yinv", nf);
     a.phys0 = reinterpret_cast<double*>(phys);
-    launch_x<double>(c, kx_of<double>(c).xinv, kx_of<double>(c).x_smem1, a, "adj_xinv");
+    launch_x<double>(c, kx_of<double>(c).xinv, kx_of<double>(c).x_smem1, a, "adj_xinv", nf);
     CKL(c);
     return FSIBE_OK;
 }
@@ -1587,13 +1599,14 @@ static int adj_invx(fsibe_ctx* c, const void* T, void* phys) {
     CKL(c);
     return FSIBE_OK;
 }
-static int adj_fwd2d(fsibe_ctx* c, const void* phys, void* spec) {
+static int adj_fwd2d(fsibe_ctx* c, const void* phys, int nf, void* spec) {
     KArgs<double> a = kargs<double>(c);
+    a.bstride = (size_t)c->g.hx * c->g.ny;
     a.phys0 = reinterpret_cast<double*>(const_cast<void*>(phys));
-    a.spec0 = reinterpret_cast<C2<double>*>(c->spec[SP_0]);
+    a.spec0 = reinterpret_cast<C2<double>*>(c->adj->spec[AS_T]);
     a.spec1 = reinterpret_cast<C2<double>*>(spec);
-    launch_x<double>(c, kx_of<double>(c).xfwd, kx_of<double>(c).x_smem1, a, "adj_xfwd");
-    launch_y<double>(c, ky_of<double>(c).yfwd, ky_of<double>(c).y_smem1, a, "adj_yfwd");
+    launch_x<double>(c, kx_of<double>(c).xfwd, kx_of<double>(c).x_smem1, a, "adj_xfwd", nf);
+    launch_y<double>(c, ky_of<double>(c).yfwd, ky_of<double>(c).y_smem1, a, "adj_yfwd", nf);
     CKL(c);
     return FSIBE_OK;
 }
@@ -1675,14 +1688,10 @@ static int adj_step(fsibe_ctx* c, int k) {
     a.euler = (k == 0);
     k_adj_q<<<G, 256, 0, c->stream>>>(a);
     k_adj_w3<<<G, 256, 0, c->stream>>>(a);
-    if ((st = adj_inv2d(c, w->spec[AS_X0], OP_ID, w->phys[AP_LNL]))) return st;
-    if ((st = adj_inv2d(c, w->spec[AS_X1], OP_ID, w->phys[AP_LP2]))) return st;
-    if ((st = adj_inv2d(c, w->spec[AS_X2], OP_ID, w->phys[AP_LP1]))) return st;
+    // (X0, X1, X2) -> (lnl, lp2, lp1); then (lwx, lwy, lu, lv) -> (G1, G2, G3, G4)
+    if ((st = adj_inv2d(c, w->spec[AS_X], 3, w->phys[AP_P]))) return st;
     k_adj_phys<<<G, 256, 0, c->stream>>>(a, ncell);
-    if ((st = adj_fwd2d(c, w->phys[AP_LWX], w->spec[AS_G1]))) return st;
-    if ((st = adj_fwd2d(c, w->phys[AP_LWY], w->spec[AS_G2]))) return st;
-    if ((st = adj_fwd2d(c, w->phys[AP_LU], w->spec[AS_G3]))) return st;
-    if ((st = adj_fwd2d(c, w->phys[AP_LV], w->spec[AS_G4]))) return st;
+    if ((st = adj_fwd2d(c, w->phys[AP_L], 4, w->spec[AS_G]))) return st;
     a.c_obj = adj_weight(w, k);
     k_adj_combine<<<G, 256, 0, c->stream>>>(a);
     CKL(c);
@@ -1820,7 +1829,7 @@ int fsibe_drag_gradient(fsibe_ctx* c, const double* vort0, double nu, int nsteps
     AdjArgs a = adj_args(c);
     const int G = adj_grid(c);
     k_adj_window<<<G, 256, 0, c->stream>>>(a, w->win[0], w->win[1], w->win[2], w->win[3], 0);
-    if ((st = adj_fwd2d(c, w->phys[AP_LU], w->spec[AS_G3]))) return st;
+    if ((st = adj_fwd2d(c, a.lu, 1, a.G3))) return st;
     k_adj_gdrag<<<G, 256, 0, c->stream>>>(a);
     CKL(c);
     // the reverse sweep from the cotangents of the final state
@@ -1830,7 +1839,8 @@ int fsibe_drag_gradient(fsibe_ctx* c, const double* vort0, double nu, int nsteps
     CK(c, cudaMemsetAsync(w->spec[AS_LM], 0, b, c->stream));
     {
         // lW(T) = c_T d drag / d W: q <- 0, G1..G4 <- 0 and one combine
-        for (int i : {AS_Q, AS_G1, AS_G2, AS_G3, AS_G4}) CK(c, cudaMemsetAsync(w->spec[i], 0, b, c->stream));
+        CK(c, cudaMemsetAsync(w->spec[AS_Q], 0, b, c->stream));
+        CK(c, cudaMemsetAsync(w->spec[AS_G], 0, 4 * b, c->stream));
         a.c_obj = adj_weight(w, nsteps);
         k_adj_combine<<<G, 256, 0, c->stream>>>(a);
         CKL(c);
@@ -1855,8 +1865,8 @@ int fsibe_drag_gradient(fsibe_ctx* c, const double* vort0, double nu, int nsteps
         CK(c, cudaMemcpyAsync(w->spec[AS_LN], w->spec[AS_LW], b, cudaMemcpyDeviceToDevice, c->stream));
         k_adj_w3<<<G, 256, 0, c->stream>>>(a);
         CKL(c);
-        if ((st = adj_inv2d(c, w->spec[AS_X0], OP_ID, w->phys[AP_LNL]))) return st;
-        if ((st = to_host(c, w->phys[AP_LNL], NN, g_vort0))) return st;
+        if ((st = adj_inv2d(c, w->spec[AS_X], 1, w->phys[AP_P]))) return st;
+        if ((st = to_host(c, w->phys[AP_P], NN, g_vort0))) return st;
     }
     if (info) {
         info->forward_steps = (int32_t)w->fwd_steps;

@@ -40,6 +40,8 @@ struct KArgs {
     const int* dcut;      // 2/3-rule: modes with |ky| >= dcut[kx] are removed (dealiase_mask.f90:9-26)
     int kcut;             // rows kx >= kcut hold no dealiased mode (dcut = 0): exact zeros after the update
     int viscous, pressure_on, penalize, op;
+    size_t bstride;       // generic transforms over several fields at once: blockIdx.y selects the
+                          // field, bstride complex values (= nx ny / 2) apart in every buffer
 };
 
 template <typename R> constexpr bool kIsF32 = std::is_same<R, float>::value;
@@ -131,14 +133,16 @@ __global__ void __launch_bounds__(XRows<R, H>::THREADS) k_xfwd(KArgs<R> a) {
     const int r = threadIdx.x / X::G, t = threadIdx.x % X::G;
     const int iy0 = blockIdx.x * X::TR, ny = a.g.ny;
     C2<R>* rb = buf + r * X::PL;
-    const C2<R>* f2 = reinterpret_cast<const C2<R>*>(a.phys0) + (size_t)(iy0 + r) * H;
+    const size_t boff = blockIdx.y * a.bstride;
+    const C2<R>* f2 = reinterpret_cast<const C2<R>*>(a.phys0) + boff + (size_t)(iy0 + r) * H;
 #pragma unroll
     for (int q = 0; q < 8; ++q) rb[pad8(t + q * X::G)] = f2[t + q * X::G];
     __syncthreads();
     row_r2c<R, H>(rb, a.twR, a.twX, t);
+    C2<R>* T = a.spec0 + boff;
     for (int i = threadIdx.x; i < H * X::TR; i += blockDim.x) {
         const int rr = i % X::TR, kx = i / X::TR;
-        a.spec0[(size_t)kx * ny + iy0 + rr] = buf[rr * X::PL + pad8(kx)];
+        T[(size_t)kx * ny + iy0 + rr] = buf[rr * X::PL + pad8(kx)];
     }
 }
 
@@ -151,10 +155,11 @@ __global__ void __launch_bounds__(XRows<R, H>::THREADS) k_xinv(KArgs<R> a) {
     const int r = threadIdx.x / X::G, t = threadIdx.x % X::G;
     const int iy0 = blockIdx.x * X::TR, ny = a.g.ny;
     C2<R>* rb = buf + r * X::PL;
-    load_tileT<R, H, X::TR, X::PL>(buf, a.spec0, ny, iy0);
+    const size_t boff = blockIdx.y * a.bstride;
+    load_tileT<R, H, X::TR, X::PL>(buf, a.spec0 + boff, ny, iy0);
     __syncthreads();
     row_c2r<R, H>(rb, a.twR, a.twX, t);
-    C2<R>* f2 = reinterpret_cast<C2<R>*>(a.phys0) + (size_t)(iy0 + r) * H;
+    C2<R>* f2 = reinterpret_cast<C2<R>*>(a.phys0) + boff + (size_t)(iy0 + r) * H;
 #pragma unroll
     for (int q = 0; q < 8; ++q) f2[t + q * X::G] = rb[pad8(t + q * X::G)];
 }
@@ -166,13 +171,14 @@ __global__ void __launch_bounds__(NY / 8) k_yfwd(KArgs<R> a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C2<R>* buf = reinterpret_cast<C2<R>*>(smem_raw);
     const int kx = blockIdx.x, t = threadIdx.x;
-    const C2<R>* in = a.spec0 + (size_t)kx * NY;
+    const size_t boff = blockIdx.y * a.bstride;
+    const C2<R>* in = a.spec0 + boff + (size_t)kx * NY;
 #pragma unroll
     for (int q = 0; q < 8; ++q) buf[pad8(t + q * G)] = in[t + q * G];
     __syncthreads();
     block_fft<R, NY, false>(buf, a.twY, t);
     const R norm = (R)(1.0 / ((double)a.g.nx * (double)a.g.ny));
-    C2<R>* out = a.spec1 + (size_t)kx * NY;
+    C2<R>* out = a.spec1 + boff + (size_t)kx * NY;
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
         const int ky = t + q * G;
@@ -188,7 +194,8 @@ __global__ void __launch_bounds__(NY / 8) k_yinv(KArgs<R> a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C2<R>* buf = reinterpret_cast<C2<R>*>(smem_raw);
     const int kx = blockIdx.x, t = threadIdx.x;
-    const C2<R>* in = a.spec1 + (size_t)kx * NY;
+    const size_t boff = blockIdx.y * a.bstride;
+    const C2<R>* in = a.spec1 + boff + (size_t)kx * NY;
     const Geometry& g = a.g;
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
@@ -211,7 +218,7 @@ __global__ void __launch_bounds__(NY / 8) k_yinv(KArgs<R> a) {
     }
     __syncthreads();
     block_fft<R, NY, true>(buf, a.twY, t);
-    C2<R>* out = a.spec0 + (size_t)kx * NY;
+    C2<R>* out = a.spec0 + boff + (size_t)kx * NY;
 #pragma unroll
     for (int q = 0; q < 8; ++q) out[t + q * G] = buf[pad8(t + q * G)];
 }
