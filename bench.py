@@ -182,7 +182,7 @@ def gpu_arm(args):
             raise RuntimeError(f"device status {s.status}")
         kt = kernel_times(run, 3)
         results[tag] = {"ms": ms, "clocks": clocks, "kernels": kt, "launches": run.launches_per_step(),
-                        "newton_iters": s.newton_iters}
+                        "newton_iters": s.newton_iters, "tiles": run.tiles()}
         run.close()
 
     # FP32-compensated vs FP64 on the GPU from the same seed (relative L2 of vorticity)
@@ -257,6 +257,8 @@ def gpu_arm(args):
             "gpu_launches": results["fp32c"]["launches"] * args.steps,
             "clocks": results["fp32c"]["clocks"],
             "ensemble": ens,
+            "autotuned_x_tiles": {tag: dict(zip(("nl_x", "press_x", "press_fin"), results[tag]["tiles"]))
+                                  for tag in ("fp32c", "fp64")},
         }
         print(json.dumps(line))
     if world > 1:

@@ -39,6 +39,7 @@ def library():
         L.fsibe_time_steps.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_float)]
         L.fsibe_launches_per_step.argtypes = [C.c_void_p, C.POINTER(C.c_int)]
         L.fsibe_use_graph.argtypes = [C.c_void_p, C.c_int]
+        L.fsibe_tiles.argtypes = [C.c_void_p, C.POINTER(C.c_int32)]
         L.fsibe_ensemble_create.argtypes = [C.POINTER(FsibeParams), C.c_int, C.POINTER(C.c_void_p)]
         L.fsibe_ensemble_destroy.argtypes = [C.c_void_p]
         L.fsibe_ensemble_get.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_void_p)]
@@ -77,6 +78,12 @@ class Run(_Run):
 
     def use_graph(self, enable=True):
         self._call("use_graph", C.c_int(1 if enable else 0))
+
+    def tiles(self):
+        """Rows per block the autotuner chose for (nl_x, press_x, press_fin)."""
+        out = (C.c_int32 * 3)()
+        self._call("tiles", out)
+        return tuple(out)
 
     # -- adjoint on a prescribed rigid mask (FP64 form, iFLUSI = 0) -----------------------
     def drag_objective(self, vort0, nsteps, avg_from, nu=0.0):

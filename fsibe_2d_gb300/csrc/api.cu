@@ -4,7 +4,9 @@
 // sequence of kernel launches whose time-dependent inputs (time, dt, AB2 weights, drag
 // window, status) live in a device struct, so a step needs no host round trip and can be
 // captured once in a CUDA graph and replayed.
+#include <array>
 #include <cmath>
+#include <cstdlib>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -102,10 +104,11 @@ __global__ void __launch_bounds__(256) k_step_begin(StepArgs a) {
     // quantity with shuffles): 0 max |u|^2, 1 sum u, 2 sum v, 3 min x, 4 max x, 5 min y, 6 max y
     __shared__ double q[8];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int nblk = ((volatile DevScalars*)a.S)->nred;  // partials of the last x-pass kernel
     if (warp < 3) {
         const int slot = (warp == 0) ? RED_UMAX2 : (warp == 1 ? RED_SUM_U : RED_SUM_V);
         double v = 0.0;
-        for (int b = lane; b < a.nblk; b += 32) {
+        for (int b = lane; b < nblk; b += 32) {
             const double r = a.red[(size_t)b * RED_NSLOTS + slot];
             v = (warp == 0) ? fmax(v, r) : v + r;
         }
@@ -195,9 +198,10 @@ __global__ void __launch_bounds__(256) k_fluid_finish(StepArgs a) {
     // one warp per slot group: warp w reduces slots w and w + 8 with shuffles
     __shared__ double sm[RED_NSLOTS][1];
     const int lane = threadIdx.x & 31;
+    const int nblk = ((volatile DevScalars*)a.S)->nred;  // partials of the last x-pass kernel
     for (int s = threadIdx.x >> 5; s < RED_NSLOTS; s += blockDim.x >> 5) {
         double v = 0.0;
-        for (int b = lane; b < a.nblk; b += 32) {
+        for (int b = lane; b < nblk; b += 32) {
             const double r = a.red[(size_t)b * RED_NSLOTS + s];
             v = (s == RED_UMAX2) ? fmax(v, r) : v + r;
         }
@@ -448,6 +452,7 @@ struct fsibe_ctx {
     std::string err;
     int launches = 0;
     int nsm = 152;                // SMs of the device
+    int xv_nl = 1, xv_px = 1, xv_fin = 1;  // tile-height variants of the fused x kernels (1: default)
     // per-kernel event timing (fsibe_kernel_times)
     bool profiling = false;
     std::vector<cudaEvent_t> pool;
@@ -558,6 +563,16 @@ static void launch_y(fsibe_ctx* c, void (*k)(KArgs<R>), int smem, const KArgs<R>
     c->launches++;
 }
 
+// a fused x kernel with one of its tile-height variants (nbuf row buffers of shared memory)
+template <typename R>
+static void launch_xv(fsibe_ctx* c, void (*k)(KArgs<R>), const typename SizeKernels<R>::XVariant& v, int nbuf,
+                      const KArgs<R>& a, const char* name) {
+    prof_begin(c, name);
+    k<<<c->g.ny / v.rows, v.threads, nbuf == 2 ? v.smem2 : v.smem1, c->stream>>>(a);
+    prof_end(c);
+    c->launches++;
+}
+
 static StepArgs step_args(fsibe_ctx* c, int explicit_step, int nblk) {
     StepArgs a;
     std::memset(&a, 0, sizeof(a));
@@ -664,16 +679,16 @@ static int fluid_step_t(fsibe_ctx* c, int explicit_step) {
     prof_end(c);
     c->launches++;
     if (c->P.iFLUSI == 1) { const int st = beam_predict(c); if (st) return st; }
-    launch_x<R>(c, KX.nl_x, KX.x_smem2, a, "nl_x");
+    launch_xv<R>(c, KX.xv[c->xv_nl].nl_x, KX.xv[c->xv_nl], 2, a, "nl_x");
     launch_y<R>(c, KY.nl_y, KY.y_smem2, a, "nl_y");
-    launch_x<R>(c, KX.press_x, KX.x_smem2, a, "press_x");
+    launch_xv<R>(c, KX.xv[c->xv_px].press_x, KX.xv[c->xv_px], 2, a, "press_x");
     prof_begin(c, "fluid_finish");
     k_fluid_finish<<<1, 256, 0, c->stream>>>(sa);
     prof_end(c);
     c->launches++;
     if (a.pressure_on) {
         launch_y<R>(c, KY.press_y, KY.y_smem2, a, "press_y");
-        launch_x<R>(c, KX.press_fin, KX.x_smem1, a, "press_fin");
+        launch_xv<R>(c, KX.xv[c->xv_fin].press_fin, KX.xv[c->xv_fin], 1, a, "press_fin");
     } else {
         CK(c, cudaMemsetAsync(c->phys[PH_PRESS], 0, sizeof(R) * (size_t)c->g.nx * c->g.ny, c->stream));
     }
@@ -946,6 +961,65 @@ const char* fsibe_strerror(int s) {
 
 const char* fsibe_last_error(const fsibe_ctx* ctx) { return ctx ? ctx->err.c_str() : g_err.c_str(); }
 
+}  // extern "C"
+
+// ---- autotuner ----------------------------------------------------------------------
+// The fused x kernels (k_nl_x, k_press_x, k_press_fin) come in three tile heights (rows of the
+// grid per block).  A new context times each candidate on its own freshly allocated buffers
+// (no state exists yet; fsibe_init_fields overwrites everything they touch) and keeps the
+// fastest per kernel.  The choice is cached per (precision, nx, ny) for the process, so an
+// ensemble of many runs of one size tunes once.  FSIBE_AUTOTUNE=0 keeps the default tiles.
+template <typename R>
+static float time_xv(fsibe_ctx* c, int kind, const typename SizeKernels<R>::XVariant& v) {
+    KArgs<R> a = kargs<R>(c);
+    void (*k)(KArgs<R>) = kind == 0 ? v.nl_x : (kind == 1 ? v.press_x : v.press_fin);
+    const int smem = kind == 2 ? v.smem1 : v.smem2;
+    const dim3 grid(c->g.ny / v.rows);
+    for (int i = 0; i < 2; ++i) k<<<grid, v.threads, smem, c->stream>>>(a);
+    cudaEventRecord(c->ev0, c->stream);
+    for (int i = 0; i < 5; ++i) k<<<grid, v.threads, smem, c->stream>>>(a);
+    cudaEventRecord(c->ev1, c->stream);
+    if (cudaEventSynchronize(c->ev1) != cudaSuccess) return 1e30f;
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+    return ms / 5.f;
+}
+
+template <typename R>
+static int autotune_x(fsibe_ctx* c) {
+    static std::mutex mu;
+    static std::vector<std::array<int, 6>> cache;  // fp32, nx, ny, nl, px, fin
+    const char* env = std::getenv("FSIBE_AUTOTUNE");
+    if (env && env[0] == '0') return FSIBE_OK;
+    std::lock_guard<std::mutex> lock(mu);
+    const int f32 = c->fp32 ? 1 : 0;
+    for (const auto& e : cache)
+        if (e[0] == f32 && e[1] == c->g.nx && e[2] == c->g.ny) {
+            c->xv_nl = e[3]; c->xv_px = e[4]; c->xv_fin = e[5];
+            return FSIBE_OK;
+        }
+    const SizeKernels<R>& K = kx_of<R>(c);
+    int choice[3];
+    for (int kind = 0; kind < 3; ++kind) {
+        // the default first; a candidate must be faster by 3% to replace it
+        int best = 1;
+        float tbest = time_xv<R>(c, kind, K.xv[1]);
+        for (int v : {0, 2}) {
+            if (K.xv[v].rows == K.xv[1].rows) continue;
+            const float t = time_xv<R>(c, kind, K.xv[v]);
+            if (t < 0.97f * tbest) { tbest = t; best = v; }
+        }
+        choice[kind] = best;
+    }
+    CKL(c);
+    CK(c, cudaStreamSynchronize(c->stream));
+    c->xv_nl = choice[0]; c->xv_px = choice[1]; c->xv_fin = choice[2];
+    cache.push_back({f32, c->g.nx, c->g.ny, choice[0], choice[1], choice[2]});
+    return FSIBE_OK;
+}
+
+extern "C" {
+
 static void adj_free(fsibe_ctx* c);
 
 int fsibe_destroy(fsibe_ctx* c) {
@@ -1090,6 +1164,10 @@ int fsibe_create(const fsibe_params* p, fsibe_ctx** out) {
     if (e != cudaSuccess) { g_err = cudaGetErrorString(e); fsibe_destroy(c); return FSIBE_ERR_CUDA; }
     cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming);
     cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming);
+    {
+        const int st = c->fp32 ? autotune_x<float>(c) : autotune_x<double>(c);
+        if (st) { g_err = c->err; fsibe_destroy(c); return st; }
+    }
     e = cudaDeviceSynchronize();
     if (e != cudaSuccess) { g_err = std::string("create: ") + cudaGetErrorString(e); fsibe_destroy(c); return FSIBE_ERR_CUDA; }
     *out = c;
@@ -1446,6 +1524,16 @@ int fsibe_beam_phase_cycles(fsibe_ctx* c, long long* out32, int reset) {
     CK(c, cudaMemcpyAsync(out32, c->S->phase, 32 * sizeof(long long), cudaMemcpyDeviceToHost, c->stream));
     if (reset) CK(c, cudaMemsetAsync(c->S->phase, 0, 32 * sizeof(long long), c->stream));
     CK(c, cudaStreamSynchronize(c->stream));
+    return FSIBE_OK;
+}
+
+int fsibe_tiles(fsibe_ctx* c, int32_t* rows3) {
+    if (!c || !rows3) return FSIBE_ERR_PARAM;
+    if (c->fp32) {
+        rows3[0] = c->kxf.xv[c->xv_nl].rows; rows3[1] = c->kxf.xv[c->xv_px].rows; rows3[2] = c->kxf.xv[c->xv_fin].rows;
+    } else {
+        rows3[0] = c->kxd.xv[c->xv_nl].rows; rows3[1] = c->kxd.xv[c->xv_px].rows; rows3[2] = c->kxd.xv[c->xv_fin].rows;
+    }
     return FSIBE_OK;
 }
 

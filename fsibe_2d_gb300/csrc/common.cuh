@@ -67,6 +67,7 @@ struct DevScalars {
     long long phase[32];             // beam kernel phase cycle counters (measurement)
     int32_t beam_fact;               // 1: the global copy of the beam's FP32 band factor is usable
     int32_t etab_valid;              // 1: the integrating-factor tables hold exp of etab_cx, etab_cy
+    int32_t nred;                    // per-block partial sums written by the last x-pass kernel
     double etab_cx, etab_cy;
 };
 

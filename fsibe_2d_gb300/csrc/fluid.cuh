@@ -72,18 +72,29 @@ enum SpecOp { OP_ID = 0, OP_DX = 1, OP_DY = 2, OP_U = 3, OP_V = 4 };
 
 __device__ __forceinline__ int signed_k(int k, int n) { return (k <= n / 2) ? k : k - n; }
 
-template <typename R, int H>
+template <typename R, int H, int TRV = 0>
 struct XRows {
     static constexpr int G = H / 8;
     // rows per block: keep the transposed chunks >= 32 bytes while bounding shared memory
     static constexpr int TR0 = (sizeof(R) == 8) ? (H <= 512 ? 4 : 2) : (H <= 256 ? 8 : (H <= 1024 ? 4 : 2));
     // at least one full warp per block (the block reductions use full-warp shuffles)
-    static constexpr int TR = (G * TR0 >= 32) ? TR0 : 32 / G;
+    static constexpr int TRD = (G * TR0 >= 32) ? TR0 : 32 / G;
+    // TRV > 0: an explicit tile height (the autotuner's candidates)
+    static constexpr int TR = TRV > 0 ? TRV : TRD;
     static constexpr int PL = padded_len(H) + 1;  // row stride (complex) in shared memory
     static constexpr int THREADS = G * TR;
     // blocks per SM that keep a thread at <= 128 registers
     static constexpr int MINB128 = (65536 / (THREADS * 128)) > 0 ? 65536 / (THREADS * 128) : 1;
 };
+
+// A tile height for the fused x-pass kernels: tr when it is valid (a full warp, at most 1024
+// threads, at most 200 KB of shared memory for two row buffers), else the default.
+template <typename R, int H>
+constexpr int xrows_valid(int tr) {
+    using X = XRows<R, H>;
+    return (tr >= 1 && X::G * tr >= 32 && X::G * tr <= 1024 &&
+            2 * tr * X::PL * (int)(2 * sizeof(R)) <= 200 * 1024) ? tr : X::TRD;
+}
 
 // ---- x-pass helpers -------------------------------------------------------------------
 // Rows kx >= kmax are known to be zero and are not read.
@@ -273,6 +284,7 @@ __global__ void __launch_bounds__(XRows<R, H>::THREADS) k_vel_x(KArgs<R> a) {
         double m0 = 0.0, s0 = 0.0, s1 = 0.0;
         for (int i = 0; i < X::THREADS / 32; ++i) { m0 = fmax(m0, red_s[0][i]); s0 += red_s[1][i]; s1 += red_s[2][i]; }
         double* out = a.red + (size_t)blockIdx.x * RED_NSLOTS;
+        if (blockIdx.x == 0) a.S->nred = (int)gridDim.x;
         for (int s = 0; s < RED_NSLOTS; ++s) out[s] = 0.0;
         out[RED_UMAX2] = m0;
         out[RED_SUM_U] = s0;
@@ -283,9 +295,9 @@ __global__ void __launch_bounds__(XRows<R, H>::THREADS) k_vel_x(KArgs<R> a) {
 // ======================================================================================
 // K2: nonlinear term and penalization in physical space (cal_nlk)
 // ======================================================================================
-template <typename R, int H>
-__global__ void __launch_bounds__(XRows<R, H>::THREADS) k_nl_x(KArgs<R> a) {
-    using X = XRows<R, H>;
+template <typename R, int H, int TRV>
+__global__ void __launch_bounds__(XRows<R, H, TRV>::THREADS) k_nl_x(KArgs<R> a) {
+    using X = XRows<R, H, TRV>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C2<R>* bufA = reinterpret_cast<C2<R>*>(smem_raw);
     C2<R>* bufB = bufA + X::TR * X::PL;
@@ -493,11 +505,11 @@ __global__ void __launch_bounds__(NY / 8) k_nl_y(KArgs<R> a) {
 // K4: velocity at n+1, penalty, drag/energy reductions, vor_mean, Poisson RHS (forward-x),
 // stresses to physical space.
 // ======================================================================================
-template <typename R, int H>
+template <typename R, int H, int TRV>
 // (FP32: at most 128 registers a thread, so that two 256-thread blocks share an SM and the
 // 1024^2 grid runs in one wave; FP64 is bound by its arithmetic and keeps its registers)
-__global__ void __launch_bounds__(XRows<R, H>::THREADS, (sizeof(R) == 4) ? XRows<R, H>::MINB128 : 1) k_press_x(KArgs<R> a) {
-    using X = XRows<R, H>;
+__global__ void __launch_bounds__(XRows<R, H, TRV>::THREADS, (sizeof(R) == 4) ? XRows<R, H, TRV>::MINB128 : 1) k_press_x(KArgs<R> a) {
+    using X = XRows<R, H, TRV>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C2<R>* bufA = reinterpret_cast<C2<R>*>(smem_raw);
     C2<R>* bufB = bufA + X::TR * X::PL;
@@ -656,6 +668,7 @@ __global__ void __launch_bounds__(XRows<R, H>::THREADS, (sizeof(R) == 4) ? XRows
         double v = 0.0;
         for (int i = 0; i < X::THREADS / 32; ++i) v = (s == RED_UMAX2) ? fmax(v, red_s[s][i]) : v + red_s[s][i];
         a.red[(size_t)blockIdx.x * RED_NSLOTS + s] = v;
+        if (blockIdx.x == 0 && s == 0) a.S->nred = (int)gridDim.x;
     }
     if (a.pressure_on) {
         row_r2c<R, H>(ra, a.twR, a.twX, t);
@@ -732,9 +745,9 @@ __global__ void __launch_bounds__(NY / 8) k_press_y(KArgs<R> a) {
 }
 
 // K6: inverse-x of q, p = q - |u|^2/2
-template <typename R, int H>
-__global__ void __launch_bounds__(XRows<R, H>::THREADS) k_press_fin(KArgs<R> a) {
-    using X = XRows<R, H>;
+template <typename R, int H, int TRV>
+__global__ void __launch_bounds__(XRows<R, H, TRV>::THREADS) k_press_fin(KArgs<R> a) {
+    using X = XRows<R, H, TRV>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C2<R>* buf = reinterpret_cast<C2<R>*>(smem_raw);
     const int r = threadIdx.x / X::G, t = threadIdx.x % X::G;
@@ -774,6 +787,13 @@ struct SizeKernels {
     void (*press_x)(KArgs<R>);
     void (*press_fin)(KArgs<R>);
     int x_threads, x_rows, x_smem1, x_smem2;
+    // tile-height candidates of the fused x kernels (index 1 is the default)
+    struct XVariant {
+        int rows, threads, smem1, smem2;
+        void (*nl_x)(KArgs<R>);
+        void (*press_x)(KArgs<R>);
+        void (*press_fin)(KArgs<R>);
+    } xv[3];
     // y-pass kernels for NY
     void (*yfwd)(KArgs<R>);
     void (*yinv)(KArgs<R>);
@@ -782,6 +802,21 @@ struct SizeKernels {
     int y_threads, y_smem1, y_smem2;
 };
 
+template <typename R, int H, int TR>
+inline void fill_xvariant(typename SizeKernels<R>::XVariant& v) {
+    using X = XRows<R, H, TR>;
+    v.rows = TR;
+    v.threads = X::THREADS;
+    v.smem1 = (int)(TR * X::PL * sizeof(C2<R>));
+    v.smem2 = 2 * v.smem1;
+    v.nl_x = k_nl_x<R, H, TR>;
+    v.press_x = k_press_x<R, H, TR>;
+    v.press_fin = k_press_fin<R, H, TR>;
+    cudaFuncSetAttribute(k_nl_x<R, H, TR>, cudaFuncAttributeMaxDynamicSharedMemorySize, v.smem2);
+    cudaFuncSetAttribute(k_press_x<R, H, TR>, cudaFuncAttributeMaxDynamicSharedMemorySize, v.smem2);
+    cudaFuncSetAttribute(k_press_fin<R, H, TR>, cudaFuncAttributeMaxDynamicSharedMemorySize, v.smem1);
+}
+
 template <typename R, int N>
 inline void fill_size_kernels(SizeKernels<R>& k) {
     constexpr int H = N / 2;
@@ -789,19 +824,20 @@ inline void fill_size_kernels(SizeKernels<R>& k) {
     k.xfwd = k_xfwd<R, H>;
     k.xinv = k_xinv<R, H>;
     k.vel_x = k_vel_x<R, H>;
-    k.nl_x = k_nl_x<R, H>;
-    k.press_x = k_press_x<R, H>;
-    k.press_fin = k_press_fin<R, H>;
     k.x_threads = X::THREADS;
     k.x_rows = X::TR;
     k.x_smem1 = (int)(X::TR * X::PL * sizeof(C2<R>));
     k.x_smem2 = 2 * k.x_smem1;
     cudaFuncSetAttribute(k_xfwd<R, H>, cudaFuncAttributeMaxDynamicSharedMemorySize, k.x_smem1);
     cudaFuncSetAttribute(k_xinv<R, H>, cudaFuncAttributeMaxDynamicSharedMemorySize, k.x_smem1);
-    cudaFuncSetAttribute(k_press_fin<R, H>, cudaFuncAttributeMaxDynamicSharedMemorySize, k.x_smem1);
     cudaFuncSetAttribute(k_vel_x<R, H>, cudaFuncAttributeMaxDynamicSharedMemorySize, k.x_smem2);
-    cudaFuncSetAttribute(k_nl_x<R, H>, cudaFuncAttributeMaxDynamicSharedMemorySize, k.x_smem2);
-    cudaFuncSetAttribute(k_press_x<R, H>, cudaFuncAttributeMaxDynamicSharedMemorySize, k.x_smem2);
+    constexpr int T0 = xrows_valid<R, H>(X::TRD / 2), T1 = X::TRD, T2 = xrows_valid<R, H>(X::TRD * 2);
+    fill_xvariant<R, H, T0>(k.xv[0]);
+    fill_xvariant<R, H, T1>(k.xv[1]);
+    fill_xvariant<R, H, T2>(k.xv[2]);
+    k.nl_x = k.xv[1].nl_x;
+    k.press_x = k.xv[1].press_x;
+    k.press_fin = k.xv[1].press_fin;
     k.yfwd = k_yfwd<R, N>;
     k.yinv = k_yinv<R, N>;
     k.nl_y = k_nl_y<R, N>;

@@ -198,6 +198,11 @@ int fsibe_kernel_times(fsibe_ctx* ctx, int nsteps, fsibe_kernel_time* out, int c
  * the Newton loop.  Parts of [4]: [23] Newton update and norms.  out32 receives 32 values;
  * reset != 0 zeroes them after reading. */
 int fsibe_beam_phase_cycles(fsibe_ctx* ctx, long long* out32, int reset);
+/* Rows per block chosen by the autotuner for the fused x-pass kernels (nl_x, press_x,
+ * press_fin).  fsibe_create times three tile heights per kernel on the new context's
+ * buffers and keeps the fastest (cached per precision and grid size for the process;
+ * FSIBE_AUTOTUNE=0 in the environment keeps the defaults). */
+int fsibe_tiles(fsibe_ctx* ctx, int32_t* rows3);
 /* Number of kernel launches one fsibe_step issues (for the bench's gpu_launches). */
 int fsibe_launches_per_step(fsibe_ctx* ctx, int* launches);
 /* Capture one fsibe_step in a CUDA graph and replay it for later steps (1) or
