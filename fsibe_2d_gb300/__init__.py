@@ -40,6 +40,7 @@ def library():
         L.fsibe_launches_per_step.argtypes = [C.c_void_p, C.POINTER(C.c_int)]
         L.fsibe_use_graph.argtypes = [C.c_void_p, C.c_int]
         L.fsibe_tiles.argtypes = [C.c_void_p, C.POINTER(C.c_int32)]
+        L.fsibe_beam_cluster.argtypes = [C.c_void_p, C.POINTER(C.c_int32)]
         L.fsibe_ensemble_create.argtypes = [C.POINTER(FsibeParams), C.c_int, C.POINTER(C.c_void_p)]
         L.fsibe_ensemble_destroy.argtypes = [C.c_void_p]
         L.fsibe_ensemble_get.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_void_p)]
@@ -84,6 +85,12 @@ class Run(_Run):
         out = (C.c_int32 * 3)()
         self._call("tiles", out)
         return tuple(out)
+
+    def beam_cluster(self):
+        """CTAs of the cluster running the beam's Newton step (0: the single-CTA kernel)."""
+        out = C.c_int32(0)
+        self._call("beam_cluster", C.byref(out))
+        return out.value
 
     # -- adjoint on a prescribed rigid mask (FP64 form, iFLUSI = 0) -----------------------
     def drag_objective(self, vort0, nsteps, avg_from, nu=0.0):

@@ -34,8 +34,12 @@ void launch_beam(const BeamArgs& b, cudaStream_t st);
 void launch_beam_pre(const BeamArgs& b, cudaStream_t st);
 int beam_pre_smem_setup(int ns);
 size_t beam_pred_doubles(int ns);
+void beam_d1d_table(double ds, double* out);
 void launch_init_beam(const BeamArgs& b, cudaStream_t st);
 int beam_smem_setup(int ns);
+int beam_cluster_setup(int ns, int want, size_t* smem_out);
+void launch_beam_cluster(const BeamArgs& b, int R, size_t smem, cudaStream_t st);
+size_t beam_cluster_minv_floats(int ns, int R);
 
 static bool get_sizes(int N, SizeKernels<double>& d, SizeKernels<float>& f) {
     switch (N) {
@@ -439,6 +443,11 @@ struct fsibe_ctx {
     double U_mean_true = 1.0;
     int beam_smem = 0;      // beam workspace parts in shared memory (bit mask, see k_beam)
     int beam_pre_smem = 0;  // the same for the predictor kernel
+    int beam_cl = 0;        // CTAs of the cluster form of the beam kernel (0: the single-CTA form)
+    size_t beam_cl_smem = 0;
+    float* minv = nullptr;  // cluster form: rows of the preconditioner inverse, kept between steps
+    int* minv_rse = nullptr;
+    double* d1d = nullptr;  // Differentiate1D table of the beam (4 x 3 x 8)
     double* pred = nullptr; // predictor output
     cudaStream_t side = nullptr;  // the beam predictor runs here beside the fluid step
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
@@ -641,6 +650,9 @@ static BeamArgs beam_args(fsibe_ctx* c) {
     b.ws = c->ws;
     b.use_smem = c->beam_smem;
     b.pred = c->pred;
+    b.minv = c->minv;
+    b.minv_rse = c->minv_rse;
+    b.d1d = c->d1d;
     return b;
 }
 
@@ -764,7 +776,8 @@ static int solid_step(fsibe_ctx* c) {
     CK(c, cudaStreamWaitEvent(c->stream, c->ev_join, 0));
     c->pre_launched = false;
     prof_begin(c, "beam");
-    launch_beam(beam_args(c), c->stream);
+    if (c->beam_cl) launch_beam_cluster(beam_args(c), c->beam_cl, c->beam_cl_smem, c->stream);
+    else launch_beam(beam_args(c), c->stream);
     prof_end(c);
     c->launches++;
     CKL(c);
@@ -1029,7 +1042,7 @@ int fsibe_destroy(fsibe_ctx* c) {
     for (void* p : c->phys) if (p) cudaFree(p);
     for (void* p : c->spec) if (p) cudaFree(p);
     for (double* p : c->beam) if (p) cudaFree(p);
-    void* others[] = {c->twX, c->twR, c->twY, c->S, c->red, c->oo, c->ws, c->pred, c->prims, c->nprims,
+    void* others[] = {c->twX, c->twR, c->twY, c->S, c->red, c->oo, c->ws, c->pred, c->minv, c->minv_rse, c->d1d, c->prims, c->nprims,
                       c->rect, c->counter, c->fterm, c->rows, c->dscratch, c->dscratch2, c->etab, c->etabf, c->dcut};
     for (void* p : others) if (p) cudaFree(p);
     for (cudaEvent_t e : c->pool) cudaEventDestroy(e);
@@ -1095,7 +1108,24 @@ int fsibe_create(const fsibe_params* p, fsibe_ctx** out) {
     ALLOC(c->oo, 8 * (size_t)ns * 6);
     ALLOC(c->ws, 8 * beam_ws_doubles(ns));
     ALLOC(c->pred, 8 * beam_pred_doubles(ns));
+    ALLOC(c->d1d, 8 * 96);
+    {
+        double tab[96];
+        beam_d1d_table(c->g.ds, tab);
+        cudaMemcpy(c->d1d, tab, sizeof(tab), cudaMemcpyHostToDevice);
+    }
     c->beam_smem = beam_smem_setup(ns);
+    {
+        // the beam's Newton step on a cluster of 16 (or 8) CTAs when the device places one;
+        // FSIBE_BEAM_CLUSTER = 0 / 8 / 16 caps the size (0: the single-CTA kernel)
+        const char* e = std::getenv("FSIBE_BEAM_CLUSTER");
+        const int want = e ? std::atoi(e) : 16;
+        c->beam_cl = (want >= 8) ? beam_cluster_setup(ns, want, &c->beam_cl_smem) : 0;
+        if (c->beam_cl) {
+            ALLOC(c->minv, 4 * beam_cluster_minv_floats(ns, c->beam_cl));
+            ALLOC(c->minv_rse, 4 * (size_t)(n + 16));
+        }
+    }
     c->beam_pre_smem = beam_pre_smem_setup(ns);
     ALLOC(c->prims, sizeof(Prim) * (size_t)(2 * ns + 8));
     ALLOC(c->nprims, 16);
@@ -1534,6 +1564,12 @@ int fsibe_tiles(fsibe_ctx* c, int32_t* rows3) {
     } else {
         rows3[0] = c->kxd.xv[c->xv_nl].rows; rows3[1] = c->kxd.xv[c->xv_px].rows; rows3[2] = c->kxd.xv[c->xv_fin].rows;
     }
+    return FSIBE_OK;
+}
+
+int fsibe_beam_cluster(fsibe_ctx* c, int32_t* ctas) {
+    if (!c || !ctas) return FSIBE_ERR_PARAM;
+    *ctas = c->beam_cl;
     return FSIBE_OK;
 }
 

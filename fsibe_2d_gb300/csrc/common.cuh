@@ -87,6 +87,15 @@ struct Geometry {
     int idealis;
 };
 
+// q / b correctly rounded from rb = RN(1/b): q0 = RN(q rb), then one FMA correction
+// (Markstein, IBM J. Res. Dev. 34 (1990) 111-119); three FP64 instructions instead of a
+// division sequence.  Valid away from overflow and underflow.
+__device__ __forceinline__ double div_cr(double q, double b, double rb) {
+    const double q0 = q * rb;
+    const double r = fma(-b, q0, q);
+    return fma(r, rb, q0);
+}
+
 __device__ __forceinline__ void set_status(DevScalars* S, int code) {
     atomicCAS(&S->status, 0, code);
 }

@@ -25,15 +25,6 @@ __device__ __forceinline__ void clip_box(int* bx, int nx, int ny) {
     bx[3] = min(bx[3], ny - 1);
 }
 
-// q / b correctly rounded from rb = RN(1/b): q0 = RN(q rb), then one FMA correction
-// (Markstein, IBM J. Res. Dev. 34 (1990) 111-119); three FP64 instructions instead of a
-// division sequence.  Valid away from overflow and underflow.
-__device__ __forceinline__ double div_cr(double q, double b, double rb) {
-    const double q0 = q * rb;
-    const double r = fma(-b, q0, q);
-    return fma(r, rb, q0);
-}
-
 // Per-primitive parameters in drawing order: segments, sharp end, hinges, dots (create_mask.f90:
 // 2-218, DrawBeamSegment/DrawHinge/DrawADot).  Thread i of the grid handles node i: segment i
 // (i < ns-1) and the hinge at node i (0 < i < ns-1); threads ns .. ns+2 the sharp end and the

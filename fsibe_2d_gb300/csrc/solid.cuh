@@ -54,8 +54,11 @@ struct BeamArgs {
     double* ws;      // global workspace (used when the shared-memory workspace does not fit)
     int use_smem;    // workspace parts in shared memory: 0 none, 1 FP32 factor, 2 + FP64 vectors, 3 + band
     double* pred;    // predictor output (beam_pred_doubles)
+    const double* d1d;  // Differentiate1D table (4 x 3 x 8 doubles, beam_d1d_table)
     double* rows;    // beam_data ring (21 per step) or nullptr
     int row_cap;
+    float* minv;     // cluster form: the rows of the preconditioner inverse, one slice per CTA
+    int* minv_rse;   // cluster form: the row-scale exponents of those rows
 };
 
 }  // namespace fsibe

@@ -195,14 +195,24 @@ int fsibe_kernel_times(fsibe_ctx* ctx, int nsteps, fsibe_kernel_time* out, int c
  * [10] is the number of refinement solves (a count, not cycles).  Parts of [12]: [16] local
  * forward eliminations, [17] window carry, [18] forward correction, [19] local back
  * substitutions, [20] state carry, [21] back correction.  Parts of [7]: [22] set-up before
- * the Newton loop.  Parts of [4]: [23] Newton update and norms.  out32 receives 32 values;
- * reset != 0 zeroes them after reading. */
+ * the Newton loop.  Parts of [4]: [23] Newton update and norms.  The cluster form of the
+ * Newton kernel (fsibe_beam_cluster > 0) records, on its first CTA: [22] set-up, [4] F +
+ * Jacobian, [5] row scaling, exchange, factorisation and inverse rows, [16] residuals and the
+ * all-gather of the right-hand side, [17] inverse products and solution updates, [18] the
+ * all-gather of the solution rows, [6] the refinement's decisions, [23] Newton update and
+ * norms, [7] saving the inverse, [8] position sums, [9] positions, brake and energies, [10]
+ * the solve count.  out32 receives 32 values; reset != 0 zeroes them after reading. */
 int fsibe_beam_phase_cycles(fsibe_ctx* ctx, long long* out32, int reset);
 /* Rows per block chosen by the autotuner for the fused x-pass kernels (nl_x, press_x,
  * press_fin).  fsibe_create times three tile heights per kernel on the new context's
  * buffers and keeps the fastest (cached per precision and grid size for the process;
  * FSIBE_AUTOTUNE=0 in the environment keeps the defaults). */
 int fsibe_tiles(fsibe_ctx* ctx, int32_t* rows3);
+
+/* CTAs of the thread-block cluster that runs the beam's Newton step (16 or 8; 0 when the
+ * single-CTA kernel runs it).  Chosen at fsibe_create from what the device can place;
+ * the environment variable FSIBE_BEAM_CLUSTER = 0, 8 or 16 caps it. */
+int fsibe_beam_cluster(fsibe_ctx* ctx, int32_t* ctas);
 /* Number of kernel launches one fsibe_step issues (for the bench's gpu_launches). */
 int fsibe_launches_per_step(fsibe_ctx* ctx, int* launches);
 /* Capture one fsibe_step in a CUDA graph and replay it for later steps (1) or
