@@ -26,19 +26,23 @@ __device__ __forceinline__ void clip_box(int* bx, int nx, int ny) {
 }
 
 // Per-primitive parameters in drawing order: segments, sharp end, hinges, dots (create_mask.f90:
-// 2-218, DrawBeamSegment/DrawHinge/DrawADot).  Thread i of the grid handles node i: segment i
-// (i < ns-1) and the hinge at node i (0 < i < ns-1); threads ns .. ns+2 the sharp end and the
-// dots.  The bounding box of all primitives is reduced with atomics; the last block publishes
-// it with its union with the previous step's box and resets the accumulator.
-__global__ void __launch_bounds__(32) k_mask_prep(MaskArgs a, double gerf) {
-    const int ns = a.ns;
+// 2-218, DrawBeamSegment/DrawHinge/DrawADot).  A block of two warps handles 32 nodes i: warp 0
+// segment i and the direction angle of segment i (the hinge's second angle), then the sharp end
+// and the dots; warp 1 the direction angle of segment i-1 (the hinge's first angle), then the
+// hinge at node i -- the FP64 work of a node is split over two SMSPs.  The bounding box of all
+// primitives is reduced with atomics; the last block publishes it with its union with the
+// previous step's box and resets the accumulator.
+__global__ void __launch_bounds__(64) k_mask_prep(MaskArgs a, double gerf) {
+    __shared__ double ang2[32];
+    __shared__ int wbox[2][4];
+    const int ns = a.ns, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const double dx = a.dx, dy = a.dy, mx = fmax(dx, dy), t = a.t_beam, N = a.N_smooth;
     const double t_star = t + 2.0 * N * mx;
     const double rdx = a.rdx, rdy = a.rdy;
     const int nseg = ns - 1, nsharp = (a.sharp_trailing == 1) ? 1 : 0, nh = ns - 2;
     const int ndot = (a.sharp_trailing == 0) ? 2 : 1;
     const int total = nseg + nsharp + nh + ndot;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = blockIdx.x * 32 + lane;
     int bx0 = a.nx, bx1 = -1, by0 = a.ny, by1 = -1;
     auto emit = [&](int q, Prim& P) {
         clip_box(P.box, a.nx, a.ny);
@@ -48,29 +52,36 @@ __global__ void __launch_bounds__(32) k_mask_prep(MaskArgs a, double gerf) {
             by0 = min(by0, P.box[2]); by1 = max(by1, P.box[3]);
         }
     };
-    if (i < nseg) {
-        const double p1x = a.x[i], p1y = a.y[i], p2x = a.x[i + 1], p2y = a.y[i + 1];
-        // al = -atan2(p2y - p1y, p2x - p1x): cos(al), sin(al) from the normalised direction
-        const double ddx = p2x - p1x, ddy = p2y - p1y;
-        const double rl = 1.0 / sqrt(ddx * ddx + ddy * ddy);
-        Prim P;
-        for (int k = 0; k < 12; ++k) P.p[k] = 0.0;
-        P.type = PRIM_SEGMENT;
-        P.box[0] = dnint(div_cr(fmin(p1x, p2x) - t_star, dx, rdx));
-        P.box[1] = dnint(div_cr(fmax(p1x, p2x) + t_star, dx, rdx));
-        P.box[2] = dnint(div_cr(fmin(p1y, p2y) - t_star, dy, rdy));
-        P.box[3] = dnint(div_cr(fmax(p1y, p2y) + t_star, dy, rdy));
-        const double ca = ddx * rl, sa = -ddy * rl;
-        P.p[0] = ca; P.p[1] = sa;
-        P.p[2] = ca * p1x - sa * p1y; P.p[3] = sa * p1x + ca * p1y;
-        P.p[4] = ca * p2x - sa * p2y; P.p[5] = sa * p2x + ca * p2y;
-        P.p[6] = a.vx[i]; P.p[7] = a.vy[i]; P.p[8] = a.vx[i + 1]; P.p[9] = a.vy[i + 1];
-        emit(i, P);
+    const bool hinge = (i >= 1 && i <= ns - 2);
+    double a1 = 0.0;
+    if (warp == 0) {
+        if (i < nseg) {
+            const double p1x = a.x[i], p1y = a.y[i], p2x = a.x[i + 1], p2y = a.y[i + 1];
+            // al = -atan2(p2y - p1y, p2x - p1x): cos(al), sin(al) from the normalised direction
+            const double ddx = p2x - p1x, ddy = p2y - p1y;
+            const double rl = 1.0 / sqrt(ddx * ddx + ddy * ddy);
+            Prim P;
+            for (int k = 0; k < 12; ++k) P.p[k] = 0.0;
+            P.type = PRIM_SEGMENT;
+            P.box[0] = dnint(div_cr(fmin(p1x, p2x) - t_star, dx, rdx));
+            P.box[1] = dnint(div_cr(fmax(p1x, p2x) + t_star, dx, rdx));
+            P.box[2] = dnint(div_cr(fmin(p1y, p2y) - t_star, dy, rdy));
+            P.box[3] = dnint(div_cr(fmax(p1y, p2y) + t_star, dy, rdy));
+            const double ca = ddx * rl, sa = -ddy * rl;
+            P.p[0] = ca; P.p[1] = sa;
+            P.p[2] = ca * p1x - sa * p1y; P.p[3] = sa * p1x + ca * p1y;
+            P.p[4] = ca * p2x - sa * p2y; P.p[5] = sa * p2x + ca * p2y;
+            P.p[6] = a.vx[i]; P.p[7] = a.vy[i]; P.p[8] = a.vx[i + 1]; P.p[9] = a.vy[i + 1];
+            emit(i, P);
+        }
+        if (hinge) ang2[lane] = atan2((a.y[i + 1] - a.y[i]), (a.x[i + 1] - a.x[i]));
+    } else if (hinge) {
+        a1 = atan2((a.y[i] - a.y[i - 1]), (a.x[i] - a.x[i - 1]));
     }
-    if (i >= 1 && i <= ns - 2) {
+    __syncthreads();
+    if (warp == 1 && hinge) {
         const double px = a.x[i], py = a.y[i];
-        const double a1 = atan2((a.y[i] - a.y[i - 1]), (a.x[i] - a.x[i - 1]));
-        const double a2 = atan2((a.y[i + 1] - a.y[i]), (a.x[i + 1] - a.x[i]));
+        const double a2 = ang2[lane];
         Prim P;
         for (int k = 0; k < 12; ++k) P.p[k] = 0.0;
         P.type = PRIM_HINGE;
@@ -84,7 +95,7 @@ __global__ void __launch_bounds__(32) k_mask_prep(MaskArgs a, double gerf) {
         P.p[4] = a.vx[i]; P.p[5] = a.vy[i];
         emit(nseg + nsharp + (i - 1), P);
     }
-    if (i == ns && nsharp) {
+    if (warp == 0 && i == ns && nsharp) {
         const int e = ns - 1;
         const double al = a.th[e] + a.angle_rad;
         double sa, ca;
@@ -104,7 +115,7 @@ __global__ void __launch_bounds__(32) k_mask_prep(MaskArgs a, double gerf) {
         P.p[6] = a.vx[e]; P.p[7] = a.vy[e];
         emit(nseg, P);
     }
-    if (i >= ns + 1 && i < ns + 1 + ndot) {
+    if (warp == 0 && i >= ns + 1 && i < ns + 1 + ndot) {
         // DrawADot runs over the whole grid in the reference; SmoothStep is exactly zero once
         // both erf arguments exceed ~6 (erf rounds to 1), so the box is cut at t + 10 delta.
         const int d = i - (ns + 1);
@@ -122,12 +133,17 @@ __global__ void __launch_bounds__(32) k_mask_prep(MaskArgs a, double gerf) {
         P.p[0] = px; P.p[1] = py; P.p[2] = a.vx[e]; P.p[3] = a.vy[e];
         emit(nseg + nsharp + nh + d, P);
     }
-    // the box of all primitives: warp reduction, then atomics on the accumulator rect[8..11]
+    // the box of all primitives: warp reductions, the block's two warps, then atomics on the
+    // accumulator rect[8..11]
     bx0 = __reduce_min_sync(0xffffffffu, bx0);
     bx1 = __reduce_max_sync(0xffffffffu, bx1);
     by0 = __reduce_min_sync(0xffffffffu, by0);
     by1 = __reduce_max_sync(0xffffffffu, by1);
+    if (lane == 0) { wbox[warp][0] = bx0; wbox[warp][1] = bx1; wbox[warp][2] = by0; wbox[warp][3] = by1; }
+    __syncthreads();
     if (threadIdx.x == 0) {
+        bx0 = min(wbox[0][0], wbox[1][0]); bx1 = max(wbox[0][1], wbox[1][1]);
+        by0 = min(wbox[0][2], wbox[1][2]); by1 = max(wbox[0][3], wbox[1][3]);
         if (bx0 <= bx1) {
             atomicMin(&a.rect[8], bx0); atomicMax(&a.rect[9], bx1);
             atomicMin(&a.rect[10], by0); atomicMax(&a.rect[11], by1);
@@ -148,13 +164,15 @@ __global__ void __launch_bounds__(32) k_mask_prep(MaskArgs a, double gerf) {
     }
 }
 
-// Raster tiles: 8 x 4 cells, one warp each; warps stride over the tiles of the union of this
-// step's and the previous step's primitive box, so every other cell keeps its zero.  The few
-// tiles along the beam carry all the FP64 work, so they are dealt out one per warp and
-// the warps are spread over every SMSP of the chip.
+// Raster tiles: 8 x 4 cells, one block of MASK_WARPS warps each; blocks stride over the tiles
+// of the union of this step's and the previous step's primitive box, so every other cell keeps
+// its zero.  The few tiles along the beam carry all the FP64 work: the primitives of a tile are
+// dealt to its warps round-robin by index (every warp holds all 32 cells), so a tile's work
+// spreads over the four SMSPs of its SM, and the warps' partial results are combined with the
+// draw-order rule.
 #define MASK_TX 8
 #define MASK_TY 4
-#define MASK_WARPS 1
+#define MASK_WARPS 4
 
 // DrawHinge's angular test (create_mask.f90:623-641): both half-circle sectors contain gamma.
 // near (optional) is set when gamma lies within `margin` degrees of an interval end.
@@ -202,15 +220,102 @@ __device__ __forceinline__ double smooth_step_d(double x, double t, double inv_d
     return 0.5 * (erf((t - x) * inv_delta) + erf((x + t) * inv_delta));
 }
 
-// The primitives in draw order, per cell: the largest SmoothStep wins (strict >, so the first
-// of equal values), the sharp end overwrites.  R = float: the FP32 form, SmoothStep in FP32.
-// R = double: SmoothStep in FP64, evaluated only when its FP32 estimate (within 1e-6) could
-// exceed the cell's current value by the margin 1e-5 -- a candidate that cannot win changes
-// nothing under the strict comparison.
+// Per-cell fold state of one warp over its share of the primitives: the largest SmoothStep so
+// far, its velocity and primitive index (INT_MAX: none yet), and an FP32 lower bound of m.
+struct MaskFold {
+    double m, vx, vy;
+    int idx;
+    float mlow;
+};
+
+// Draw order keeps the first of equal values (strict >); over a subset taken in any order the
+// same winner is the largest value with the smallest index among its ties.
+__device__ __forceinline__ void fold_take(MaskFold& f, double temp, double vx, double vy, int q) {
+    if (temp > f.m || (temp == f.m && f.idx != 0x7fffffff && q < f.idx)) {
+        f.m = temp; f.vx = vx; f.vy = vy; f.idx = q; f.mlow = __double2float_rd(temp);
+    }
+}
+
+// Segment, hinge or dot q for the lane's cell (i, j), FP32 pre-test first.  R = float: the FP32
+// form, SmoothStep in FP32.  R = double: SmoothStep in FP64, evaluated only when its FP32
+// estimate (within 1e-6) could exceed the cell's current value by the margin 1e-5 -- a
+// candidate that cannot win changes nothing under the draw-order rule.
+template <typename R>
+__device__ __forceinline__ void mask_prim(const MaskArgs& a, const Prim& Q, const PrimF& F, int q, int i, int j,
+                                          double xi, double yj, float xf, float yf, double t, double t_star,
+                                          double inv_delta, double inv_ds, MaskFold& f) {
+    if (i < Q.box[0] || i > Q.box[1] || j < Q.box[2] || j > Q.box[3]) return;
+    if (Q.type == PRIM_SEGMENT) {
+        const float xs_f = xf * F.a.x - yf * F.a.y, ys_f = xf * F.a.y + yf * F.a.x;
+        if (xs_f < F.a.z || xs_f > F.a.w || ys_f > F.b.x || ys_f < F.b.y) return;
+        const double ca = Q.p[0], sa = Q.p[1];
+        const double xs = xi * ca - yj * sa, ys = xi * sa + yj * ca;
+        if (xs >= Q.p[2] && xs <= Q.p[4] && ys <= (Q.p[3] + t_star) && ys >= (Q.p[5] - t_star)) {
+            const double dist = fabs(ys - Q.p[3]);
+            const float tf = smooth_step_f(dist, t, inv_delta, a.sharp);
+            double temp;
+            if (sizeof(R) == 4) temp = tf;
+            else {
+                if (tf + 1e-5f <= f.mlow) return;
+                temp = smooth_step_d(dist, t, inv_delta, a.sharp);
+            }
+            if (temp >= f.m)
+                fold_take(f, temp, (Q.p[6] + (xs - Q.p[2]) * (Q.p[8] - Q.p[6]) * inv_ds),
+                          (Q.p[7] + (xs - Q.p[2]) * (Q.p[9] - Q.p[7]) * inv_ds), q);
+        }
+        return;
+    }
+    const float ex = xf - F.a.x, ey = yf - F.a.y;
+    if (ex * ex + ey * ey > F.a.z) return;
+    const double ddx = xi - Q.p[0], ddy = yj - Q.p[1];
+    if (Q.type == PRIM_HINGE) {
+        // angular wedge first: FP32 atan2 of the FP64 offsets, exact FP64 only near an end
+        const float beta1f = (float)Q.p[2], beta2f = (float)Q.p[3];
+        float gf = atan2f((float)ddy, (float)ddx);
+        if (gf < 0.f) gf = 6.28318530717958647692f + gf;
+        gf = gf * 57.2957795130823208768f;
+        bool near = (fabsf(gf) < 1e-3f) || (fabsf(gf - 360.f) < 1e-3f) || (ddx == 0.0 && ddy == 0.0);
+        bool inw = hinge_inside<float>(gf, beta1f, beta2f, 1e-3f, &near);
+        if (near) {
+            const double gamma = convert_angle(atan2(ddy, ddx), a.pi) * 180.0 / a.pi;
+            inw = hinge_inside<double>(gamma, Q.p[2], Q.p[3], 0.0, nullptr);
+        }
+        if (!inw) return;
+        const double Rr = sqrt(ddx * ddx + ddy * ddy);
+        if (Rr <= t_star) {
+            const float tf = smooth_step_f(Rr, t, inv_delta, a.sharp);
+            double temp;
+            if (sizeof(R) == 4) temp = tf;
+            else {
+                if (tf + 1e-5f <= f.mlow) return;
+                temp = smooth_step_d(Rr, t, inv_delta, a.sharp);
+            }
+            fold_take(f, temp, Q.p[4], Q.p[5], q);
+        }
+        return;
+    }
+    const double Rr = sqrt(ddx * ddx + ddy * ddy);
+    const float tf = smooth_step_f(Rr, t, inv_delta, a.sharp);
+    double temp;
+    if (sizeof(R) == 4) temp = tf;
+    else {
+        if (tf + 1e-5f <= f.mlow) return;
+        temp = smooth_step_d(Rr, t, inv_delta, a.sharp);
+    }
+    fold_take(f, temp, Q.p[2], Q.p[3], q);
+}
+
+// The primitives in draw order, per cell (create_mask.f90:2-218): segments and then hinges and
+// dots keep the largest SmoothStep (the first of equal values); the sharp end between them
+// overwrites the value.  Each warp folds its share of a range of primitives; the block
+// combines the partial folds after the segments (then applies the sharp end) and after the
+// hinges and dots.
 template <typename R>
 __global__ void __launch_bounds__(32 * MASK_WARPS) k_mask_raster(MaskArgs a, double gerf) {
     __shared__ Prim sp[MASK_WARPS][32];
     __shared__ PrimF sf[MASK_WARPS][32];
+    __shared__ double cmv[MASK_WARPS][3][32];
+    __shared__ int cidx[MASK_WARPS][32];
     R* mk_ = reinterpret_cast<R*>(a.mask);
     R* vx_ = reinterpret_cast<R*>(a.mvx);
     R* vy_ = reinterpret_cast<R*>(a.mvy);
@@ -227,136 +332,103 @@ __global__ void __launch_bounds__(32 * MASK_WARPS) k_mask_raster(MaskArgs a, dou
     const double two_mxd = 2.0 * mxd;
     const float mg = 1.0e-5f * (float)fmax((double)a.nx * dx, (double)a.ny * dy);
     const int total = *a.nprims;
-    // tiles are dealt to warps block-first, so neighbouring tiles land on different SMs
-    const int nwarps = gridDim.x * MASK_WARPS;
-    for (int tile = blockIdx.x + gridDim.x * warp; tile < ntx * nty; tile += nwarps) {
+    const int nseg = a.ns - 1, nsharp = (a.sharp_trailing == 1) ? 1 : 0;
+    for (int tile = blockIdx.x; tile < ntx * nty; tile += gridDim.x) {
         const int ix0 = (tx0 + tile % ntx) * MASK_TX, iy0 = (ty0 + tile / ntx) * MASK_TY;
         const int ix1 = ix0 + MASK_TX - 1, iy1 = iy0 + MASK_TY - 1;
         const int i = ix0 + (lane % MASK_TX), j = iy0 + (lane / MASK_TX);
         const size_t cell = (size_t)j * a.nx + i;
         if (r1 < ix0 || r0 > ix1 || r3 < iy0 || r2 > iy1) {
-            mk_[cell] = (R)0; vx_[cell] = (R)0; vy_[cell] = (R)0;
+            if (warp == 0) { mk_[cell] = (R)0; vx_[cell] = (R)0; vy_[cell] = (R)0; }
             continue;
         }
         const double xi = (double)i * dx, yj = (double)j * dy;
         const float xf = (float)xi, yf = (float)yj;
-        double m = 0.0, vx = 0.0, vy = 0.0;
-        float mlow = 0.f;  // a lower bound of m in FP32
-        for (int base = 0; base < total; base += 32) {
-            const int q = base + lane;
-            bool hit = false;
-            Prim P;
-            if (q < total) {
-                P = a.prims[q];
-                const int* bx = P.box;
-                hit = !(bx[1] < ix0 || bx[0] > ix1 || bx[3] < iy0 || bx[2] > iy1) && bx[0] <= bx[1] && bx[2] <= bx[3];
-            }
-            const unsigned bal = __ballot_sync(0xffffffffu, hit);
-            if (hit) {
-                const int e = __popc(bal & ((1u << lane) - 1u));
-                sp[warp][e] = P;
-                PrimF F;
-                if (P.type == PRIM_SEGMENT || P.type == PRIM_SHARP) {
-                    F.a = make_float4((float)P.p[0], (float)P.p[1], (float)P.p[2] - mg, (float)P.p[4] + mg);
-                    F.b = make_float2((float)(P.p[3] + t_star) + mg, (float)(P.p[5] - t_star) - mg);
-                } else {
-                    const float lim = (float)((P.type == PRIM_HINGE) ? t_star : rcut) + mg;
-                    F.a = make_float4((float)P.p[0], (float)P.p[1], lim * lim, 0.f);
-                    F.b = make_float2(0.f, 0.f);
+        MaskFold f;
+        f.m = 0.0; f.vx = 0.0; f.vy = 0.0; f.idx = 0x7fffffff; f.mlow = 0.f;
+        // this warp's primitives of [q0, q1): q = q0 + MASK_WARPS (32 c + lane) + warp, staged
+        // per round of 32 with their FP32 pre-test data
+        auto fold_range = [&](int q0, int q1) {
+            for (int base = q0; base < q1; base += 32 * MASK_WARPS) {
+                const int q = base + MASK_WARPS * lane + warp;
+                bool hit = false;
+                Prim P;
+                if (q < q1) {
+                    P = a.prims[q];
+                    const int* bx = P.box;
+                    hit = !(bx[1] < ix0 || bx[0] > ix1 || bx[3] < iy0 || bx[2] > iy1) && bx[0] <= bx[1] && bx[2] <= bx[3];
                 }
-                sf[warp][e] = F;
-            }
-            __syncwarp();
-            const int nl = __popc(bal);
-            for (int e = 0; e < nl; ++e) {
-                const Prim& Q = sp[warp][e];
-                if (i < Q.box[0] || i > Q.box[1] || j < Q.box[2] || j > Q.box[3]) continue;
-                const PrimF F = sf[warp][e];
-                if (Q.type == PRIM_SEGMENT) {
-                    const float xs_f = xf * F.a.x - yf * F.a.y, ys_f = xf * F.a.y + yf * F.a.x;
-                    if (xs_f < F.a.z || xs_f > F.a.w || ys_f > F.b.x || ys_f < F.b.y) continue;
-                    const double ca = Q.p[0], sa = Q.p[1];
-                    const double xs = xi * ca - yj * sa, ys = xi * sa + yj * ca;
-                    if (xs >= Q.p[2] && xs <= Q.p[4] && ys <= (Q.p[3] + t_star) && ys >= (Q.p[5] - t_star)) {
-                        const double dist = fabs(ys - Q.p[3]);
-                        const float tf = smooth_step_f(dist, t, inv_delta, a.sharp);
-                        double temp;
-                        if (sizeof(R) == 4) temp = tf;
-                        else {
-                            if (tf + 1e-5f <= mlow) continue;
-                            temp = smooth_step_d(dist, t, inv_delta, a.sharp);
-                        }
-                        if (temp > m) {
-                            m = temp;
-                            mlow = __double2float_rd(m);
-                            vx = (Q.p[6] + (xs - Q.p[2]) * (Q.p[8] - Q.p[6]) * inv_ds);
-                            vy = (Q.p[7] + (xs - Q.p[2]) * (Q.p[9] - Q.p[7]) * inv_ds);
-                        }
-                    }
-                } else if (Q.type == PRIM_SHARP) {
-                    const float xs_f = xf * F.a.x + yf * F.a.y, ys_f = -xf * F.a.y + yf * F.a.x;
-                    if (xs_f < F.a.z || xs_f > F.a.w || ys_f > F.b.x || ys_f < F.b.y) continue;
-                    const double ca = Q.p[0], sa = Q.p[1];
-                    const double xs = xi * ca + yj * sa, ys = -xi * sa + yj * ca;
-                    if (xs >= Q.p[2] && xs <= Q.p[4] && ys <= (Q.p[3] + t_star) && ys >= (Q.p[5] - t_star)) {
-                        double tmp2, temp;
-                        if (sizeof(R) == 4) {
-                            tmp2 = smooth_step_f(xs - Q.p[2], two_mxd, inv_delta, a.sharp);
-                            temp = smooth_step_f(fabs(ys - Q.p[3]), t, inv_delta, a.sharp);
-                        } else {
-                            tmp2 = smooth_step_d(xs - Q.p[2], two_mxd, inv_delta, a.sharp);
-                            temp = smooth_step_d(fabs(ys - Q.p[3]), t, inv_delta, a.sharp);
-                        }
-                        m = temp * tmp2;
-                        mlow = __double2float_rd(m);
-                        if (xs - Q.p[2] >= two_mxd) { vx = Q.p[6]; vy = Q.p[7]; }
-                    }
-                } else {
-                    const float ex = xf - F.a.x, ey = yf - F.a.y;
-                    if (ex * ex + ey * ey > F.a.z) continue;
-                    const double ddx = xi - Q.p[0], ddy = yj - Q.p[1];
-                    if (Q.type == PRIM_HINGE) {
-                        // angular wedge first: FP32 atan2 of the FP64 offsets, exact FP64 only near an end
-                        const float beta1f = (float)Q.p[2], beta2f = (float)Q.p[3];
-                        float gf = atan2f((float)ddy, (float)ddx);
-                        if (gf < 0.f) gf = 6.28318530717958647692f + gf;
-                        gf = gf * 57.2957795130823208768f;
-                        bool near = (fabsf(gf) < 1e-3f) || (fabsf(gf - 360.f) < 1e-3f) || (ddx == 0.0 && ddy == 0.0);
-                        bool inw = hinge_inside<float>(gf, beta1f, beta2f, 1e-3f, &near);
-                        if (near) {
-                            const double gamma = convert_angle(atan2(ddy, ddx), a.pi) * 180.0 / a.pi;
-                            inw = hinge_inside<double>(gamma, Q.p[2], Q.p[3], 0.0, nullptr);
-                        }
-                        if (!inw) continue;
-                        const double Rr = sqrt(ddx * ddx + ddy * ddy);
-                        if (Rr <= t_star) {
-                            const float tf = smooth_step_f(Rr, t, inv_delta, a.sharp);
-                            double temp;
-                            if (sizeof(R) == 4) temp = tf;
-                            else {
-                                if (tf + 1e-5f <= mlow) continue;
-                                temp = smooth_step_d(Rr, t, inv_delta, a.sharp);
-                            }
-                            if (temp > m) { m = temp; mlow = __double2float_rd(m); vx = Q.p[4]; vy = Q.p[5]; }
-                        }
+                const unsigned bal = __ballot_sync(0xffffffffu, hit);
+                if (hit) {
+                    const int e = __popc(bal & ((1u << lane) - 1u));
+                    sp[warp][e] = P;
+                    PrimF F;
+                    if (P.type == PRIM_SEGMENT || P.type == PRIM_SHARP) {
+                        F.a = make_float4((float)P.p[0], (float)P.p[1], (float)P.p[2] - mg, (float)P.p[4] + mg);
+                        F.b = make_float2((float)(P.p[3] + t_star) + mg, (float)(P.p[5] - t_star) - mg);
                     } else {
-                        const double Rr = sqrt(ddx * ddx + ddy * ddy);
-                        const float tf = smooth_step_f(Rr, t, inv_delta, a.sharp);
-                        double temp;
-                        if (sizeof(R) == 4) temp = tf;
-                        else {
-                            if (tf + 1e-5f <= mlow) continue;
-                            temp = smooth_step_d(Rr, t, inv_delta, a.sharp);
-                        }
-                        if (temp > m) { m = temp; mlow = __double2float_rd(m); vx = Q.p[2]; vy = Q.p[3]; }
+                        const float lim = (float)((P.type == PRIM_HINGE) ? t_star : rcut) + mg;
+                        F.a = make_float4((float)P.p[0], (float)P.p[1], lim * lim, 0.f);
+                        F.b = make_float2(0.f, 0.f);
                     }
+                    sf[warp][e] = F;
+                    cidx[warp][e] = q;
+                }
+                __syncwarp();
+                const int nl = __popc(bal);
+                for (int e = 0; e < nl; ++e)
+                    mask_prim<R>(a, sp[warp][e], sf[warp][e], cidx[warp][e], i, j, xi, yj, xf, yf, t, t_star,
+                                 inv_delta, inv_ds, f);
+                __syncwarp();
+            }
+        };
+        // the block's partial folds -> the combined state in every warp
+        auto combine = [&]() {
+            cmv[warp][0][lane] = f.m; cmv[warp][1][lane] = f.vx; cmv[warp][2][lane] = f.vy;
+            const int my = f.idx;
+            __syncthreads();
+            cidx[warp][lane] = my;
+            __syncthreads();
+            for (int w = 0; w < MASK_WARPS; ++w) {
+                const double mw = cmv[w][0][lane];
+                const int iw = cidx[w][lane];
+                if (mw > f.m || (mw == f.m && iw < f.idx)) {
+                    f.m = mw; f.vx = cmv[w][1][lane]; f.vy = cmv[w][2][lane]; f.idx = iw;
                 }
             }
-            __syncwarp();
+            f.mlow = __double2float_rd(f.m);
+            __syncthreads();
+        };
+        fold_range(0, nseg);
+        combine();
+        if (nsharp) {
+            const Prim& Q = a.prims[nseg];
+            if (!(i < Q.box[0] || i > Q.box[1] || j < Q.box[2] || j > Q.box[3])) {
+                const double ca = Q.p[0], sa = Q.p[1];
+                const double xs = xi * ca + yj * sa, ys = -xi * sa + yj * ca;
+                if (xs >= Q.p[2] && xs <= Q.p[4] && ys <= (Q.p[3] + t_star) && ys >= (Q.p[5] - t_star)) {
+                    double tmp2, temp;
+                    if (sizeof(R) == 4) {
+                        tmp2 = smooth_step_f(xs - Q.p[2], two_mxd, inv_delta, a.sharp);
+                        temp = smooth_step_f(fabs(ys - Q.p[3]), t, inv_delta, a.sharp);
+                    } else {
+                        tmp2 = smooth_step_d(xs - Q.p[2], two_mxd, inv_delta, a.sharp);
+                        temp = smooth_step_d(fabs(ys - Q.p[3]), t, inv_delta, a.sharp);
+                    }
+                    f.m = temp * tmp2;
+                    f.mlow = __double2float_rd(f.m);
+                    if (xs - Q.p[2] >= two_mxd) { f.vx = Q.p[6]; f.vy = Q.p[7]; }
+                }
+            }
         }
-        mk_[cell] = (R)(m * inv_eps);
-        vx_[cell] = (R)vx;
-        vy_[cell] = (R)vy;
+        f.idx = 0x7fffffff;  // the state after the sharp end is no primitive of the next range
+        fold_range(nseg + nsharp, total);
+        combine();
+        if (warp == 0) {
+            mk_[cell] = (R)(f.m * inv_eps);
+            vx_[cell] = (R)f.vx;
+            vy_[cell] = (R)f.vy;
+        }
     }
 }
 
@@ -510,11 +582,11 @@ __global__ void __launch_bounds__(128) k_forces(ForceArgs a, double dxi, double 
 // Host launchers
 // ===================================================================================
 void launch_mask_prep(const MaskArgs& a, double gerf, cudaStream_t st) {
-    k_mask_prep<<<(a.ns + 3 + 31) / 32, 32, 0, st>>>(a, gerf);
+    k_mask_prep<<<(a.ns + 3 + 31) / 32, 64, 0, st>>>(a, gerf);
 }
 void launch_mask(const MaskArgs& a, double gerf, bool fp32, cudaStream_t st) {
-    // one-warp blocks, four per SM: a tile per SMSP at a time, spread over the whole chip
-    const int blocks = 4 * a.nsm;
+    // four-warp blocks, two per SM: a tile's primitives over the four SMSPs of an SM
+    const int blocks = 2 * a.nsm;
     if (fp32) k_mask_raster<float><<<blocks, 32 * MASK_WARPS, 0, st>>>(a, gerf);
     else k_mask_raster<double><<<blocks, 32 * MASK_WARPS, 0, st>>>(a, gerf);
 }
