@@ -65,6 +65,7 @@ struct StepArgs {
     double cfl, dx, dy, eps, dt_fixed, time_end, theta_inf, T_fullspeed, U_mean_true, pi, nu;
     double x0, y0, t_beam, NN, scalex, scaley;
     double cos_ti, sin_ti;  // cos and sin of theta_inf, from the host
+    double rdx, rdy, rNN;   // RN(1/dx), RN(1/dy), RN(1/NN)
     const double *bx, *by;
     double* etab;
     float2* etabf;
@@ -134,48 +135,65 @@ __global__ void __launch_bounds__(256) k_step_begin(StepArgs a) {
         if (lane == 0) q[warp] = v;
     }
     __syncthreads();
-    double smax[1] = {q[0]}, su[1] = {q[1]}, sv[1] = {q[2]};
-    double bmin[2][1] = {{q[3]}, {q[5]}}, bmax[2][1] = {{q[4]}, {q[6]}};
+    const double smax = q[0], su = q[1], sv = q[2];
+    const double bminx = q[3], bmaxx = q[4], bminy = q[5], bmaxy = q[6];
     DevScalars* S = a.S;
+    __shared__ double dts[2];
+    // the scalars, each chain on its own warp (SMSP): dt1 (warp 0), the mean velocities
+    // (warps 1, 2), the drag window (warps 3, 4); the quotients by constants use their host
+    // reciprocals (div_cr: the correctly rounded quotient, like the division)
     if (threadIdx.x == 0) {
-    if (!a.explicit_step) S->dt0 = S->dt1;
-    const double time = S->time;
-    const double u_max = sqrt(smax[0]);
-    double dt1 = a.cfl * fmin(a.dx, a.dy) / u_max;
-    if (u_max < 1.e-10) dt1 = 1.e-2;
-    if (a.iBeam > 0) dt1 = fmin(0.9 * a.eps, dt1);
-    if (a.dt_fixed > 0.0) dt1 = fmin(a.dt_fixed, dt1);
-    if ((a.time_end - time) < dt1) dt1 = a.time_end - time;
-    S->dt1 = dt1;
-    S->u_max = u_max;
-    S->umax2 = smax[0];
-    S->mean_ux = su[0] / a.NN;
-    S->mean_uy = sv[0] / a.NN;
-    S->explicit_step = a.explicit_step;
-    if (!a.explicit_step) {
-        const double dt0 = S->dt0;
-        S->b10 = dt1 / dt0 * (0.5 * dt1 + dt0);
-        S->b11 = -0.5 * (dt1 * dt1) / dt0;
-    } else {
-        S->b10 = dt1;
-        S->b11 = 0.0;
-    }
-    S->mean_u_next = a.U_mean_true * mean_ux(a.iMeanVelocity, time + dt1, a.cos_ti, a.T_fullspeed, a.pi);
-    S->mean_v_next = a.U_mean_true * mean_uy(a.iMeanVelocity, time + dt1, a.sin_ti, a.T_fullspeed, a.pi);
-    if (a.iBeam > 0) {
+        const double time = S->time;
+        const double dt0 = a.explicit_step ? S->dt0 : S->dt1;
+        const double u_max = sqrt(smax);
+        double dt1 = a.cfl * fmin(a.dx, a.dy) / u_max;
+        if (u_max < 1.e-10) dt1 = 1.e-2;
+        if (a.iBeam > 0) dt1 = fmin(0.9 * a.eps, dt1);
+        if (a.dt_fixed > 0.0) dt1 = fmin(a.dt_fixed, dt1);
+        if ((a.time_end - time) < dt1) dt1 = a.time_end - time;
+        if (!a.explicit_step) S->dt0 = dt0;
+        S->dt1 = dt1;
+        S->u_max = u_max;
+        S->umax2 = smax;
+        S->explicit_step = a.explicit_step;
+        dts[0] = dt1;
+        dts[1] = dt0;
+    } else if (threadIdx.x == 32) {
+        S->mean_ux = div_cr(su, a.NN, a.rNN);
+    } else if (threadIdx.x == 64) {
+        S->mean_uy = div_cr(sv, a.NN, a.rNN);
+    } else if (threadIdx.x == 96 || threadIdx.x == 128) {
         const double r_cyl = 0.0, tb = a.t_beam;
-        int iymax = (int)((fmax(bmax[1][0] + 1.5 * tb, a.y0 + 2.0 * r_cyl)) / a.dy);
-        int iymin = (int)((fmin(bmin[1][0] - 1.5 * tb, a.y0 - 2.0 * r_cyl)) / a.dy);
-        int ixmin = (int)(fmin((a.x0 - fmax(2.5 * r_cyl, 1.5 * tb)), (bmin[0][0] - 1.5 * tb)) / a.dx);
-        int ixmax = (int)((bmax[0][0] + 1.5 * tb) / a.dx);
-        if (ixmin < 0) ixmin = 0;
-        if (ixmax > a.nx - 1) ixmax = a.nx - 1;
-        if (iymin < 0) iymin = 0;
-        if (iymax > a.ny - 1) iymax = a.ny - 1;
-        S->win[0] = ixmin; S->win[1] = ixmax; S->win[2] = iymin; S->win[3] = iymax;
-    } else {
-        S->win[0] = 0; S->win[1] = a.nx - 1; S->win[2] = 0; S->win[3] = a.ny - 1;
+        if (threadIdx.x == 96) {
+            int ixmin = 0, ixmax = a.nx - 1;
+            if (a.iBeam > 0) {
+                ixmin = (int)div_cr(fmin((a.x0 - fmax(2.5 * r_cyl, 1.5 * tb)), (bminx - 1.5 * tb)), a.dx, a.rdx);
+                ixmax = (int)div_cr((bmaxx + 1.5 * tb), a.dx, a.rdx);
+                if (ixmin < 0) ixmin = 0;
+                if (ixmax > a.nx - 1) ixmax = a.nx - 1;
+            }
+            S->win[0] = ixmin; S->win[1] = ixmax;
+        } else {
+            int iymin = 0, iymax = a.ny - 1;
+            if (a.iBeam > 0) {
+                iymax = (int)div_cr((fmax(bmaxy + 1.5 * tb, a.y0 + 2.0 * r_cyl)), a.dy, a.rdy);
+                iymin = (int)div_cr((fmin(bminy - 1.5 * tb, a.y0 - 2.0 * r_cyl)), a.dy, a.rdy);
+                if (iymin < 0) iymin = 0;
+                if (iymax > a.ny - 1) iymax = a.ny - 1;
+            }
+            S->win[2] = iymin; S->win[3] = iymax;
+        }
     }
+    __syncthreads();
+    // after dt1: the AB2 weights (warps 0, 1) and the mean flow at time + dt1 (warps 2, 3)
+    {
+        const double dt1 = dts[0], dt0 = dts[1];
+        if (threadIdx.x == 0) S->b10 = a.explicit_step ? dt1 : dt1 / dt0 * (0.5 * dt1 + dt0);
+        else if (threadIdx.x == 32) S->b11 = a.explicit_step ? 0.0 : -0.5 * (dt1 * dt1) / dt0;
+        else if (threadIdx.x == 64)
+            S->mean_u_next = a.U_mean_true * mean_ux(a.iMeanVelocity, S->time + dt1, a.cos_ti, a.T_fullspeed, a.pi);
+        else if (threadIdx.x == 96)
+            S->mean_v_next = a.U_mean_true * mean_uy(a.iMeanVelocity, S->time + dt1, a.sin_ti, a.T_fullspeed, a.pi);
     }
     __syncthreads();
     // integrating factor exp(-nu dt |k|^2) = exp(coefx kx^2) exp(coefy ky^2) (cal_vis.f90:183-189),
@@ -215,64 +233,34 @@ __global__ void __launch_bounds__(256) k_fluid_finish(StepArgs a) {
         }
         if (lane == 0) sm[s][0] = v;
     }
-    __syncthreads();
-    if (threadIdx.x != 0) return;
     DevScalars* S = a.S;
-    S->mean_u_cur = S->mean_u_next;
-    S->mean_v_cur = S->mean_v_next;
+    const int ready = ((volatile DevScalars*)S)->unst_ready;
+    __syncthreads();
+    // the scalars on three warps (SMSPs): energies (warp 0), drag (warp 1), lift (warp 2)
     const double dx = a.dx, dy = a.dy, norm = dx * dy;
-    S->vor_rms = dx * dy * sqrt(sm[RED_OMEGA2][0]);
-    S->kinetic = 0.5 * dx * dy * sm[RED_KIN][0];
-    S->dissipation = a.nu * dx * dy * sm[RED_OMEGA2][0];
-    S->porous_diss = dx * dy * sm[RED_POROUS][0];
-    S->inflow_solid = dx * dy * sm[RED_INFLOW_SOLID][0];
-    S->inflow_mean = dx * dy * a.U_mean_true * sm[RED_INFLOW_MEAN][0];
-    if (a.iBeam > 0) {
-        S->force[0] = sm[RED_DRAG_X][0] * norm;
-        S->force[1] = sm[RED_DRAG_Y][0] * norm;
-        const double dn = sm[RED_UNST_X][0] * norm * a.eps, ln = sm[RED_UNST_Y][0] * norm * a.eps;
-        if (S->unst_ready) {
-            S->force_unst[0] = (dn - S->drag_unst_old) / S->dt1;
-            S->force_unst[1] = (ln - S->lift_unst_old) / S->dt1;
-        } else {
-            S->force_unst[0] = 0.0;
-            S->force_unst[1] = 0.0;
-        }
-        S->drag_unst_old = dn;
-        S->lift_unst_old = ln;
-        S->unst_ready = 1;
-    }
-}
-
-struct AdvArgs {
-    DevScalars* S;
-    int ns;
-    double *x, *y, *vx, *vy, *th, *thd, *p_old, *p_new, *tau_old, *tau_new;
-    double* rows;
-};
-
-// time_step.f90:152-161 / :222-236: swap, time += dt1, old <- new beam loads, beam_data row.
-__global__ void __launch_bounds__(256) k_advance(AdvArgs a) {
-    for (int i = threadIdx.x; i < a.ns; i += blockDim.x) {
-        a.p_old[i] = a.p_new[i];
-        a.tau_old[i] = a.tau_new[i];
-    }
     if (threadIdx.x == 0) {
-        DevScalars* S = a.S;
-        const int ns = a.ns;
-        S->time = S->time + S->dt1;
-        S->step += 1;
-        const double row[21] = {S->time, a.p_new[ns - 1], a.p_new[3 * ns / 4], a.p_new[ns / 2], a.x[ns - 1], a.y[ns - 1],
-                                a.vx[ns - 1], a.vy[ns - 1], a.th[ns - 1], a.thd[ns - 1], S->force[0], S->force[1],
-                                S->force_unst[0], S->force_unst[1], S->force_press[0], S->force_press[1],
-                                S->inertial_force[0], S->inertial_force[1], S->e_kinetic, S->e_elastic, S->e_pot};
-        for (int c = 0; c < 21; ++c) S->row[c] = row[c];
-        if (a.rows && S->run_row < S->run_cap) {
-            for (int c = 0; c < 21; ++c) a.rows[(size_t)S->run_row * 21 + c] = row[c];
-            S->run_row += 1;
-        }
+        S->mean_u_cur = S->mean_u_next;
+        S->mean_v_cur = S->mean_v_next;
+        S->vor_rms = dx * dy * sqrt(sm[RED_OMEGA2][0]);
+        S->kinetic = 0.5 * dx * dy * sm[RED_KIN][0];
+        S->dissipation = a.nu * dx * dy * sm[RED_OMEGA2][0];
+        S->porous_diss = dx * dy * sm[RED_POROUS][0];
+        S->inflow_solid = dx * dy * sm[RED_INFLOW_SOLID][0];
+        S->inflow_mean = dx * dy * a.U_mean_true * sm[RED_INFLOW_MEAN][0];
+    } else if (a.iBeam > 0 && (threadIdx.x == 32 || threadIdx.x == 64)) {
+        const int c = (threadIdx.x == 32) ? 0 : 1;
+        S->force[c] = sm[c == 0 ? RED_DRAG_X : RED_DRAG_Y][0] * norm;
+        const double dn = sm[c == 0 ? RED_UNST_X : RED_UNST_Y][0] * norm * a.eps;
+        double* old = (c == 0) ? &S->drag_unst_old : &S->lift_unst_old;
+        S->force_unst[c] = ready ? (dn - *old) / S->dt1 : 0.0;
+        *old = dn;
     }
+    __syncthreads();
+    if (threadIdx.x == 0 && a.iBeam > 0) S->unst_ready = 1;
 }
+
+// time_step.f90:152-161 / :222-236 (advance_state in solid.cuh) as its own kernel.
+__global__ void __launch_bounds__(256) k_advance(AdvArgs a) { advance_state(a); }
 
 // ---- the packed Temperton layout (ABI boundary only) ---------------------------------
 // unpack: fk (Fortran (0:nx-1,0:ny-1)) -> S[kx][ky]   (cof_fftw33.f90:214-233)
@@ -609,6 +597,9 @@ static StepArgs step_args(fsibe_ctx* c, int explicit_step, int nblk) {
     a.y0 = c->P.y0;
     a.t_beam = c->P.t_beam;
     a.NN = (double)c->P.nx * (double)c->P.ny;
+    a.rdx = 1.0 / a.dx;
+    a.rdy = 1.0 / a.dy;
+    a.rNN = 1.0 / a.NN;
     a.bx = c->beam[B_X];
     a.by = c->beam[B_Y];
     a.scalex = c->g.scalex;
@@ -763,6 +754,9 @@ static int get_forces(fsibe_ctx* c) {
     f.fp32 = c->fp32 ? 1 : 0;
     const double dxi = (c->P.xl - c->g.dx) / (double)(c->P.nx - 1);
     const double dyi = (c->P.yl - c->g.dy) / (double)(c->P.ny - 1);
+    f.alpha = f.angle_deg * f.pi / 180.0;
+    f.rdxi = 1.0 / dxi;
+    f.rdyi = 1.0 / dyi;
     prof_begin(c, "forces");
     launch_forces(f, dxi, dyi, c->stream);
     prof_end(c);
@@ -771,20 +765,7 @@ static int get_forces(fsibe_ctx* c) {
     return FSIBE_OK;
 }
 
-static int solid_step(fsibe_ctx* c) {
-    if (!c->pre_launched) { const int st = beam_predict(c); if (st) return st; }
-    CK(c, cudaStreamWaitEvent(c->stream, c->ev_join, 0));
-    c->pre_launched = false;
-    prof_begin(c, "beam");
-    if (c->beam_cl) launch_beam_cluster(beam_args(c), c->beam_cl, c->beam_cl_smem, c->stream);
-    else launch_beam(beam_args(c), c->stream);
-    prof_end(c);
-    c->launches++;
-    CKL(c);
-    return FSIBE_OK;
-}
-
-static int advance(fsibe_ctx* c) {
+static AdvArgs adv_args(fsibe_ctx* c) {
     AdvArgs a;
     a.S = c->S;
     a.ns = c->P.ns;
@@ -792,6 +773,35 @@ static int advance(fsibe_ctx* c) {
     a.th = c->beam[B_TH]; a.thd = c->beam[B_THD];
     a.p_old = c->beam[B_PO]; a.p_new = c->beam[B_PN]; a.tau_old = c->beam[B_TO]; a.tau_new = c->beam[B_TN];
     a.rows = c->rows;
+    return a;
+}
+
+// The solid step; with end_step and the cluster form, the cluster kernel also ends the time
+// step (advance_state) and *advanced is set.
+static int solid_step(fsibe_ctx* c, bool end_step = false, bool* advanced = nullptr) {
+    if (!c->pre_launched) { const int st = beam_predict(c); if (st) return st; }
+    CK(c, cudaStreamWaitEvent(c->stream, c->ev_join, 0));
+    c->pre_launched = false;
+    prof_begin(c, "beam");
+    if (c->beam_cl) {
+        BeamArgs b = beam_args(c);
+        if (end_step) {
+            b.fuse_adv = 1;
+            b.adv = adv_args(c);
+            if (advanced) *advanced = true;
+        }
+        launch_beam_cluster(b, c->beam_cl, c->beam_cl_smem, c->stream);
+    } else {
+        launch_beam(beam_args(c), c->stream);
+    }
+    prof_end(c);
+    c->launches++;
+    CKL(c);
+    return FSIBE_OK;
+}
+
+static int advance(fsibe_ctx* c) {
+    const AdvArgs a = adv_args(c);
     prof_begin(c, "advance");
     k_advance<<<1, 256, 0, c->stream>>>(a);
     prof_end(c);
@@ -808,8 +818,9 @@ static int step_body(fsibe_ctx* c, int explicit_step) {
     st = fluid_step(c, explicit_step);
     if (st) return st;
     if (P.iFLUSI == 1 || P.iSaveBeam > 0) { st = get_forces(c); if (st) return st; }
-    if (P.iFLUSI == 1) { st = solid_step(c); if (st) return st; }
-    return advance(c);
+    bool advanced = false;
+    if (P.iFLUSI == 1) { st = solid_step(c, true, &advanced); if (st) return st; }
+    return advanced ? FSIBE_OK : advance(c);
 }
 
 static int do_step(fsibe_ctx* c) {
@@ -1580,6 +1591,7 @@ int fsibe_launches_per_step(fsibe_ctx* c, int* n) {
     if (P.iFLUSI == 1 || P.iSaveBeam > 0) k += 2 + 1;  // press_y, press_fin, forces
     if ((P.iFLUSI == 1 || P.iMotion > 0) && P.iBeam > 0) k += 2;  // mask prep + raster
     if (P.iFLUSI == 1) k += 2;  // beam predictor + beam
+    if (P.iFLUSI == 1 && c->beam_cl) k -= 1;  // the cluster beam kernel ends the step itself
     *n = k;
     return FSIBE_OK;
 }

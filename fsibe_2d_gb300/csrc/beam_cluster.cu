@@ -76,7 +76,7 @@ __host__ __device__ inline void cl_layout(int ns, int R, ClLayout& Y) {
     Y.n = 2 * ns + 4;
     Y.L = ns + 8;
     Y.R = R;
-    Y.rmax = (Y.n + R - 1) / R;
+    Y.rmax = 4 * (((Y.n + 3) / 4 + R - 1) / R);  // rows are dealt in quads (cl_rows)
     Y.mld = cl_mld(Y.n);
     size_t o = 0;
     Y.x = o;     o = al16(o + 8 * (size_t)(Y.n + 8));
@@ -94,6 +94,16 @@ __host__ __device__ inline void cl_layout(int ns, int R, ClLayout& Y) {
     o = al16(o + (fact > post ? fact : post));
     Y.minv = o;  o = al16(o + 4 * (size_t)Y.rmax * Y.mld);
     Y.total = o;
+}
+
+// The rows [lo, hi) of CTA r: quads of rows dealt evenly, so that every CTA's slice of the FP32
+// right-hand side (and of the FP64 solution) starts on a 16-byte boundary.
+__host__ __device__ inline void cl_rows(int n, int R, int r, int& lo, int& hi) {
+    const int nq = (n + 3) / 4;
+    lo = 4 * (int)(((long long)r * nq) / R);
+    hi = 4 * (int)(((long long)(r + 1) * nq) / R);
+    lo = lo < n ? lo : n;
+    hi = hi < n ? hi : n;
 }
 
 // Fortran equation (1-based) of interleaved row r: the inverse of row_of.
@@ -175,7 +185,9 @@ __global__ void __launch_bounds__(256, 1) k_beam_cl(BeamArgs b) {
     ClLayout Y;
     cl_layout(ns, (int)R, Y);
     const int L = Y.L, mld = Y.mld, rmax = Y.rmax;
-    const int lo = (int)(((long long)rank * n) / R), hi = (int)(((long long)(rank + 1) * n) / R), nr = hi - lo;
+    int lo, hi;
+    cl_rows(n, (int)R, (int)rank, lo, hi);
+    const int nr = hi - lo;
     double* x = reinterpret_cast<double*>(cl_smem + Y.x);
     double* xdi = reinterpret_cast<double*>(cl_smem + Y.xdi);
     double* nd = reinterpret_cast<double*>(cl_smem + Y.node);
@@ -184,8 +196,9 @@ __global__ void __launch_bounds__(256, 1) k_beam_cl(BeamArgs b) {
     double* bvec = reinterpret_cast<double*>(cl_smem + Y.bvec);
     double* band = reinterpret_cast<double*>(cl_smem + Y.band);
     double* part = reinterpret_cast<double*>(cl_smem + Y.part);
-    // slots: [0, R) the passes' max |c| (FP32 bits), [R, 2R) max |x| (FP64 bits), [2R, 3R)
-    // flags sent with the right-hand side, [3R, 4R) flags sent with the factor rows
+    // exchange words, written by every CTA into every CTA: [0, R) the passes' max |c| (FP32
+    // bits), [R, 2R) max |x| (FP64 bits), [2R, 3R) the flags sent with the right-hand side,
+    // [3R, 4R) the flags sent with the factor rows
     unsigned long long* slots = reinterpret_cast<unsigned long long*>(cl_smem + Y.slots);
     float* yf = reinterpret_cast<float*>(cl_smem + Y.yf);
     float* Uf = reinterpret_cast<float*>(cl_smem + Y.fact);
@@ -196,7 +209,8 @@ __global__ void __launch_bounds__(256, 1) k_beam_cl(BeamArgs b) {
     __shared__ NewtonCtx cs;
     __shared__ double red[2][8];
     __shared__ unsigned long long redu[2][8];
-    __shared__ int flag_s, stop_s, info_s;
+    __shared__ int flag_s, stop_s, info_s, dec_s;
+    __shared__ float cprev_s;
 
     BeamWS w;
     memset(&w, 0, sizeof(w));
@@ -340,7 +354,6 @@ __global__ void __launch_bounds__(256, 1) k_beam_cl(BeamArgs b) {
                     factored = true;
                 }
                 PH(5);
-                float cprev = 0.f;
                 bool ok = false;
                 for (int pass = 0;; ++pass) {
                     // FP32 right-hand side of the own rows: -F, or the FP64 residual, its 15
@@ -370,10 +383,14 @@ __global__ void __launch_bounds__(256, 1) k_beam_cl(BeamArgs b) {
                         yf[k] = __double2float_rn(acc * row_scale(rse[k]));
                     }
                     __syncthreads();
-                    for (int e = tid; e < nr * ((int)R - 1); e += nthr) {
-                        const unsigned dst = (rank + 1 + (unsigned)(e / nr)) % R;
-                        const int k = lo + e % nr;
-                        *cl_map(yf + k, dst) = yf[k];
+                    // the own rows to every other CTA, 16 bytes a store (slices start on quads)
+                    {
+                        const int nq4 = (nr + 3) / 4;
+                        for (int e = tid; e < nq4 * ((int)R - 1); e += nthr) {
+                            const unsigned dst = (rank + 1 + (unsigned)(e / nq4)) % R;
+                            float4* p4 = reinterpret_cast<float4*>(yf + lo + 4 * (e % nq4));
+                            *cl_map(p4, dst) = *p4;
+                        }
                     }
                     if (tid < (int)R) *cl_map(slots + 2 * R + rank, (unsigned)tid) = (unsigned long long)flag_s;
                     cl_sync();
@@ -464,30 +481,39 @@ __global__ void __launch_bounds__(256, 1) k_beam_cl(BeamArgs b) {
                         *cl_map(slots + rank, (unsigned)tid) = c2;
                         *cl_map(slots + R + rank, (unsigned)tid) = x2;
                     }
-                    for (int e = tid; e < nr * ((int)R - 1); e += nthr) {
-                        const unsigned dst = (rank + 1 + (unsigned)(e / nr)) % R;
-                        const int k = lo + e % nr;
-                        *cl_map(xdi + k, dst) = xdi[k];
+                    // the own solution rows to every other CTA, 16 bytes a store
+                    {
+                        const int nq2 = (nr + 1) / 2;
+                        for (int e = tid; e < nq2 * ((int)R - 1); e += nthr) {
+                            const unsigned dst = (rank + 1 + (unsigned)(e / nq2)) % R;
+                            double2* p2 = reinterpret_cast<double2*>(xdi + lo + 2 * (e % nq2));
+                            *cl_map(p2, dst) = *p2;
+                        }
                     }
                     cl_sync();
                     PH(18);
                     ++solves;
-                    // the convergence decision of refine_step, from the cluster's maxima
-                    unsigned long long c2 = 0, x2 = 0;
-#pragma unroll
-                    for (int q = 0; q < 16; ++q)
-                        if (q < (int)R) {
+                    // the convergence decision of refine_step from the cluster's maxima, on one
+                    // thread (FP64 issue is per warp)
+                    if (tid == 0) {
+                        unsigned long long c2 = 0, x2 = 0;
+                        for (int q = 0; q < (int)R; ++q) {
                             c2 = (slots[q] > c2) ? slots[q] : c2;
                             x2 = (slots[R + q] > x2) ? slots[R + q] : x2;
                         }
-                    const double cmd = (double)__uint_as_float((unsigned)c2), cpd = (double)cprev;
-                    const double xmd = __longlong_as_double((long long)x2);
-                    const double tol = 0x1p-44 * xmd;
-                    const bool conv = !(cmd > tol) || (pass >= 1 && cmd * cmd <= tol * cpd);
-                    const bool stall = pass >= 2 && cmd > 0.5 * cpd;
-                    cprev = __uint_as_float((unsigned)c2);
-                    if (conv || (stall && cmd <= 0x1p-30 * xmd)) { ok = true; break; }
-                    if (stall || pass >= 9) break;
+                        const float cpf = (pass == 0) ? 0.f : cprev_s;
+                        const double cmd = (double)__uint_as_float((unsigned)c2), cpd = (double)cpf;
+                        const double xmd = __longlong_as_double((long long)x2);
+                        const double tol = 0x1p-44 * xmd;
+                        const bool conv = !(cmd > tol) || (pass >= 1 && cmd * cmd <= tol * cpd);
+                        const bool stall = pass >= 2 && cmd > 0.5 * cpd;
+                        cprev_s = __uint_as_float((unsigned)c2);
+                        dec_s = (conv || (stall && cmd <= 0x1p-30 * xmd)) ? 1 : ((stall || pass >= 9) ? -1 : 0);
+                    }
+                    __syncthreads();
+                    const int dec = dec_s;
+                    if (dec > 0) { ok = true; break; }
+                    if (dec < 0) break;
                 }
                 if (ok || fresh) break;
                 need_factor = true;
@@ -497,30 +523,41 @@ __global__ void __launch_bounds__(256, 1) k_beam_cl(BeamArgs b) {
             PH(6);
             // x += dx in Fortran order, the norms and the stopping test: the same data in every
             // CTA, so the same decisions without an exchange
+            // the stopping test needs iter > 2: before that the norms are not formed
+            const bool test = iter + 1 > 2;
             double sd = 0.0, sx = 0.0;
             for (int l = tid; l < n; l += nthr) {
                 const double d = xdi[col_of(ns, l + 1)];
                 if (isnan(d)) flag_s = FSIBE_ERR_NAN;
                 const double xn = x[l] + d;
                 x[l] = xn;
-                sd += d * d;
-                sx += xn * xn;
+                if (test) {
+                    sd += d * d;
+                    sx += xn * xn;
+                }
             }
-            for (int o = 16; o > 0; o >>= 1) {
-                sd += __shfl_xor_sync(0xffffffffu, sd, o);
-                sx += __shfl_xor_sync(0xffffffffu, sx, o);
+            if (test) {
+                for (int o = 16; o > 0; o >>= 1) {
+                    sd += __shfl_xor_sync(0xffffffffu, sd, o);
+                    sx += __shfl_xor_sync(0xffffffffu, sx, o);
+                }
+                if (lane == 0) { red[0][warp] = sd; red[1][warp] = sx; }
             }
-            if (lane == 0) { red[0][warp] = sd; red[1][warp] = sx; }
             __syncthreads();
             if (flag_s) { if (rank == 0 && tid == 0) set_status(S, flag_s); return; }
             iter = iter + 1;
-            if (tid < 32) {
-                double tsd = (lane < nwarp) ? red[0][lane] : 0.0, tsx = (lane < nwarp) ? red[1][lane] : 0.0;
-                for (int o = 4; o > 0; o >>= 1) {
-                    tsd += __shfl_xor_sync(0xffffffffu, tsd, o);
-                    tsx += __shfl_xor_sync(0xffffffffu, tsx, o);
+            if (test) {
+                if (tid < 32) {
+                    double tsd = (lane < nwarp) ? red[0][lane] : 0.0, tsx = (lane < nwarp) ? red[1][lane] : 0.0;
+                    for (int o = 4; o > 0; o >>= 1) {
+                        tsd += __shfl_xor_sync(0xffffffffu, tsd, o);
+                        tsx += __shfl_xor_sync(0xffffffffu, tsx, o);
+                    }
+                    if (lane == 0) stop_s = newton_stop(tsd, tsx, b.tol);
                 }
-                if (lane == 0) stop_s = (iter > 2) ? newton_stop(tsd, tsx, b.tol) : 0;
+                __syncthreads();
+            } else if (tid == 0) {
+                stop_s = 0;
             }
             __syncthreads();
             PH(23);
@@ -680,6 +717,11 @@ __global__ void __launch_bounds__(256, 1) k_beam_cl(BeamArgs b) {
     PH(9);
     if (tid == 0)
         for (int k = 4; k < 24; ++k) S->phase[k] += ph[k];
+    if (b.fuse_adv) {
+        // the end of the time step, which the host would otherwise launch next (k_advance)
+        __syncthreads();
+        advance_state(b.adv);
+    }
 }
 
 // ---- host side ------------------------------------------------------------------------

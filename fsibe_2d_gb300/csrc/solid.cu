@@ -435,15 +435,18 @@ __global__ void __launch_bounds__(32 * MASK_WARPS) k_mask_raster(MaskArgs a, dou
 // ===================================================================================
 // Forces: phi4* delta interpolation of p and the viscous stresses at the beam surface
 // ===================================================================================
-__device__ __forceinline__ double delta_phi4star(double x, double dx, double pi) {
-    const double r = fabs(x / dx);  // one division per thread, all threads in parallel
+// phi4* (BeamForces.f90): the branch of r = |x/dx| chosen arithmetically, so a warp whose lanes
+// fall in different branches runs one square root and one arcsine instead of one per branch;
+// each branch keeps the reference's expression.  rdx = RN(1/dx).
+__device__ __forceinline__ double delta_phi4star(double x, double dx, double rdx, double pi) {
+    const double r = fabs(div_cr(x, dx, rdx));
     if (r < 0.5) return (3. / 8.) + (pi / 32.) - 0.25 * (r * r);
-    if (r >= 0.5 && r <= 1.5)
-        return 0.25 + (1.0 - r) / 8. * sqrt(-2. + 8. * r - 4. * (r * r)) - asin(sqrt(2.) * (r - 1.)) / 8.;
-    if (r >= 1.5 && r <= 2.5)
-        return (17. / 16.) - (pi / 64.) - (3. * r / 4.) + ((r * r) / 8.) + (r - 2.) * sqrt(-14. + 16. * r - 4. * (r * r)) / 16. +
-               asin(sqrt(2.) * (r - 2.)) / 16.;
-    return 0.0;
+    if (!(r <= 2.5)) return 0.0;
+    const bool b2 = r <= 1.5;
+    const double sq = sqrt(b2 ? (-2. + 8. * r - 4. * (r * r)) : (-14. + 16. * r - 4. * (r * r)));
+    const double as = asin(b2 ? sqrt(2.) * (r - 1.) : sqrt(2.) * (r - 2.));
+    if (b2) return 0.25 + (1.0 - r) / 8. * sq - as / 8.;
+    return (17. / 16.) - (pi / 64.) - (3. * r / 4.) + ((r * r) / 8.) + (r - 2.) * sq / 16. + as / 16.;
 }
 
 __device__ __forceinline__ double fld(const void* f, int fp32, size_t k) {
@@ -462,28 +465,32 @@ __global__ void __launch_bounds__(128) k_forces(ForceArgs a, double dxi, double 
     __shared__ double trig[4];  // sin, cos of theta + alpha and of twice it
     __shared__ double px[4], py[4];
     __shared__ int last;
-    if (threadIdx.x == 0) {
-        const double alpha = a.angle_deg * a.pi / 180.0;
-        const double thn = a.th[n] + alpha;
-        double s, c, s2, c2;
-        sincos(thn, &s, &c);
-        sincos(2.0 * thn, &s2, &c2);
-        trig[0] = s; trig[1] = c; trig[2] = s2; trig[3] = c2;
-        const double mx = fmax(a.dy, a.dx);
-        const double off = a.t_beam + a.N_smooth * mx;
-        const double off1 = a.t_beam - 0.0 * a.N_smooth * mx;
-        const double x = a.x[n], y = a.y[n];
-        px[0] = x - off1 * s; py[0] = y + off1 * c;
-        px[1] = x + off1 * s; py[1] = y - off1 * c;
-        px[2] = x - off * s; py[2] = y + off * c;
-        px[3] = x + off * s; py[3] = y - off * c;
+    // the two sincos on two warps (SMSPs)
+    if (threadIdx.x == 0 || threadIdx.x == 32) {
+        const double thn = a.th[n] + a.alpha;
+        double sv, cv;
+        if (threadIdx.x == 0) {
+            sincos(thn, &sv, &cv);
+            trig[0] = sv; trig[1] = cv;
+            const double mx = fmax(a.dy, a.dx);
+            const double off = a.t_beam + a.N_smooth * mx;
+            const double off1 = a.t_beam - 0.0 * a.N_smooth * mx;
+            const double x = a.x[n], y = a.y[n];
+            px[0] = x - off1 * sv; py[0] = y + off1 * cv;
+            px[1] = x + off1 * sv; py[1] = y - off1 * cv;
+            px[2] = x - off * sv; py[2] = y + off * cv;
+            px[3] = x + off * sv; py[3] = y - off * cv;
+        } else {
+            sincos(2.0 * thn, &sv, &cv);
+            trig[2] = sv; trig[3] = cv;
+        }
     }
     __syncthreads();
     const double x2 = a.xl - a.dx, y2 = a.yl - a.dy;
     if (threadIdx.x < 4) {
         const int p = threadIdx.x;
         const double xt = px[p], yt = py[p];
-        const int i = (int)((xt - 0.0) / dxi), j = (int)((yt - 0.0) / dyi);
+        const int i = (int)div_cr((xt - 0.0), dxi, a.rdxi), j = (int)div_cr((yt - 0.0), dyi, a.rdyi);
         ij[p][0] = i; ij[p][1] = j;
         if (xt > x2 || xt < 0.0 || yt > y2 || yt < 0.0 || i - 4 < 0 || j - 4 < 0 || i + 4 > a.nx - 1 || j + 4 > a.ny - 1)
             set_status(a.S, FSIBE_ERR_INTERP_OOB);
@@ -493,10 +500,10 @@ __global__ void __launch_bounds__(128) k_forces(ForceArgs a, double dxi, double 
         const int p = threadIdx.x / 18, d = threadIdx.x % 18;
         if (d < 9) {
             const double xl_ = (double)(ij[p][0] - 4 + d) * dxi + 0.0;
-            dl[p][d] = delta_phi4star(fabs(xl_ - px[p]), dxi, a.pi);
+            dl[p][d] = delta_phi4star(fabs(xl_ - px[p]), dxi, a.rdxi, a.pi);
         } else {
             const double yl_ = (double)(ij[p][1] - 4 + d - 9) * dyi + 0.0;
-            dl[p][d] = delta_phi4star(fabs(yl_ - py[p]), dyi, a.pi);
+            dl[p][d] = delta_phi4star(fabs(yl_ - py[p]), dyi, a.rdyi, a.pi);
         }
     }
     __syncthreads();

@@ -31,6 +31,7 @@ struct ForceArgs {
     DevScalars* S;
     int nx, ny, ns, viscous;
     double xl, yl, dx, dy, ds, t_beam, N_smooth, pi, angle_deg, t_release, tau;
+    double alpha, rdxi, rdyi;  // angle_deg pi / 180, RN(1/dxi), RN(1/dyi) (host)
     const double *x, *y, *th;
     const void *press, *sa, *sb;   // R*[ny][nx]
     double *p_new, *tau_new;
@@ -38,6 +39,38 @@ struct ForceArgs {
     double* fterm;          // 2*ns per-node terms of the force integral
     int fp32;
 };
+
+// The end of a time step (time_step.f90:152-161 / :222-236): old <- new beam loads, time +=
+// dt1, the step count and the beam_data row (BeamIO.f90:193-216), kept in the scalars and, when
+// a ring is given, appended to it.  Run by one block after everything else of the step.
+struct AdvArgs {
+    DevScalars* S;
+    int ns;
+    double *x, *y, *vx, *vy, *th, *thd, *p_old, *p_new, *tau_old, *tau_new;
+    double* rows;
+};
+
+__device__ __forceinline__ void advance_state(const AdvArgs& a) {
+    for (int i = threadIdx.x; i < a.ns; i += blockDim.x) {
+        a.p_old[i] = a.p_new[i];
+        a.tau_old[i] = a.tau_new[i];
+    }
+    if (threadIdx.x == 0) {
+        DevScalars* S = a.S;
+        const int ns = a.ns;
+        S->time = S->time + S->dt1;
+        S->step += 1;
+        const double row[21] = {S->time, a.p_new[ns - 1], a.p_new[3 * ns / 4], a.p_new[ns / 2], a.x[ns - 1], a.y[ns - 1],
+                                a.vx[ns - 1], a.vy[ns - 1], a.th[ns - 1], a.thd[ns - 1], S->force[0], S->force[1],
+                                S->force_unst[0], S->force_unst[1], S->force_press[0], S->force_press[1],
+                                S->inertial_force[0], S->inertial_force[1], S->e_kinetic, S->e_elastic, S->e_pot};
+        for (int c = 0; c < 21; ++c) S->row[c] = row[c];
+        if (a.rows && S->run_row < S->run_cap) {
+            for (int c = 0; c < 21; ++c) a.rows[(size_t)S->run_row * 21 + c] = row[c];
+            S->run_row += 1;
+        }
+    }
+}
 
 // Reciprocal constants of the beam's grid spacing ds (formed on the host).
 struct BeamConsts {
@@ -59,6 +92,8 @@ struct BeamArgs {
     int row_cap;
     float* minv;     // cluster form: the rows of the preconditioner inverse, one slice per CTA
     int* minv_rse;   // cluster form: the row-scale exponents of those rows
+    int fuse_adv;    // cluster form: 1 = also end the time step (advance_state with adv)
+    AdvArgs adv;
 };
 
 }  // namespace fsibe
