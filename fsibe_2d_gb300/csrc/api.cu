@@ -565,7 +565,7 @@ template <typename R>
 static void launch_xv(fsibe_ctx* c, void (*k)(KArgs<R>), const typename SizeKernels<R>::XVariant& v, int nbuf,
                       const KArgs<R>& a, const char* name) {
     prof_begin(c, name);
-    k<<<c->g.ny / v.rows, v.threads, nbuf == 2 ? v.smem2 : v.smem1, c->stream>>>(a);
+    k<<<c->g.ny / v.rows, v.threads, nbuf == 3 ? v.smem3 : v.smem1, c->stream>>>(a);
     prof_end(c);
     c->launches++;
 }
@@ -682,9 +682,9 @@ static int fluid_step_t(fsibe_ctx* c, int explicit_step) {
     prof_end(c);
     c->launches++;
     if (c->P.iFLUSI == 1) { const int st = beam_predict(c); if (st) return st; }
-    launch_xv<R>(c, KX.xv[c->xv_nl].nl_x, KX.xv[c->xv_nl], 2, a, "nl_x");
-    launch_y<R>(c, KY.nl_y, KY.y_smem2, a, "nl_y");
-    launch_xv<R>(c, KX.xv[c->xv_px].press_x, KX.xv[c->xv_px], 2, a, "press_x");
+    launch_xv<R>(c, KX.xv[c->xv_nl].nl_x, KX.xv[c->xv_nl], 3, a, "nl_x");
+    launch_y<R>(c, KY.nl_y, KY.y_smem_nl, a, "nl_y");
+    launch_xv<R>(c, KX.xv[c->xv_px].press_x, KX.xv[c->xv_px], 3, a, "press_x");
     prof_begin(c, "fluid_finish");
     k_fluid_finish<<<1, 256, 0, c->stream>>>(sa);
     prof_end(c);
@@ -997,7 +997,7 @@ template <typename R>
 static float time_xv(fsibe_ctx* c, int kind, const typename SizeKernels<R>::XVariant& v) {
     KArgs<R> a = kargs<R>(c);
     void (*k)(KArgs<R>) = kind == 0 ? v.nl_x : (kind == 1 ? v.press_x : v.press_fin);
-    const int smem = kind == 2 ? v.smem1 : v.smem2;
+    const int smem = kind == 2 ? v.smem1 : v.smem3;
     const dim3 grid(c->g.ny / v.rows);
     for (int i = 0; i < 2; ++i) k<<<grid, v.threads, smem, c->stream>>>(a);
     cudaEventRecord(c->ev0, c->stream);

@@ -113,6 +113,66 @@ __device__ __forceinline__ void block_fft(C2<R>* buf, const C2<R>* __restrict__ 
     fft_run<R, N, INV>(buf, tw, t);
 }
 
+// NB independent transforms of the same length at buf + b * bstride, b < NB, stage by stage:
+// each stage loads all NB butterflies, synchronises once, and shares its twiddles between the
+// NB transforms.  Each transform's arithmetic is exactly that of block_fft.
+template <typename R, int N, int P, int NS, bool INV, int NB>
+__device__ __forceinline__ void fft_stage_m(C2<R>* buf, int bstride, const C2<R>* __restrict__ tw, int t) {
+    constexpr int G = N / 8, B = N / P, PER = 8 / P;
+    C2<R> v[NB][8];
+#pragma unroll
+    for (int b = 0; b < NB; ++b)
+#pragma unroll
+        for (int q = 0; q < PER; ++q) {
+            const int j = t + q * G;
+#pragma unroll
+            for (int r = 0; r < P; ++r) v[b][q * P + r] = buf[b * bstride + pad8(j + r * B)];
+        }
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < PER; ++q) {
+        const int j = t + q * G;
+        const int k = j & (NS - 1);
+        if constexpr (NS > 1) {
+#pragma unroll
+            for (int r = 1; r < P; ++r) {
+                C2<R> w = __ldg(&tw[r * k * (N / (NS * P))]);
+                if (INV) w.y = -w.y;
+#pragma unroll
+                for (int b = 0; b < NB; ++b) v[b][q * P + r] = cmul<R>(v[b][q * P + r], w);
+            }
+        }
+        const int base = (j - k) * P + k;
+#pragma unroll
+        for (int b = 0; b < NB; ++b) {
+            dftp<R, P, INV>(v[b] + q * P);
+#pragma unroll
+            for (int r = 0; r < P; ++r) buf[b * bstride + pad8(base + r * NS)] = v[b][q * P + r];
+        }
+    }
+    __syncthreads();
+}
+
+template <typename R, int N, bool INV, int NB, int NS = 1>
+__device__ __forceinline__ void fft_run_m(C2<R>* buf, int bstride, const C2<R>* __restrict__ tw, int t) {
+    if constexpr (NS * 8 <= N) {
+        fft_stage_m<R, N, 8, NS, INV, NB>(buf, bstride, tw, t);
+        fft_run_m<R, N, INV, NB, NS * 8>(buf, bstride, tw, t);
+    } else if constexpr (NS * 4 == N) {
+        fft_stage_m<R, N, 4, NS, INV, NB>(buf, bstride, tw, t);
+    } else if constexpr (NS * 2 == N) {
+        fft_stage_m<R, N, 2, NS, INV, NB>(buf, bstride, tw, t);
+    }
+}
+
+// NB in-place transforms (padded, natural order) at buf + b * bstride; the same contract as
+// block_fft.
+template <typename R, int N, bool INV, int NB>
+__device__ __forceinline__ void block_fft_m(C2<R>* buf, int bstride, const C2<R>* __restrict__ tw, int t) {
+    static_assert(N >= 16 && (N & (N - 1)) == 0, "power-of-two length >= 16");
+    fft_run_m<R, N, INV, NB>(buf, bstride, tw, t);
+}
+
 // ---- real <-> half-length complex split steps (x direction) -------------------------------
 // A real row x[0..2H) is handled as z[m] = x[2m] + i x[2m+1], m < H, transformed with a
 // length-H complex FFT.  twr[k] = exp(-2 pi i k / 2H), k <= H.
@@ -171,6 +231,74 @@ __device__ __forceinline__ void c2r_merge(C2<R>* buf, const C2<R>* __restrict__ 
         buf[pad8(0)] = mk<R>(x0.x, x0.x);
         C2<R> xh = buf[pad8(H / 2)];
         buf[pad8(H / 2)] = mk<R>((R)2 * xh.x, (R)-2 * xh.y);
+    }
+    __syncthreads();
+}
+
+// r2c_split and c2r_merge of NB rows at buf + b * bstride (each row's arithmetic unchanged;
+// the twiddles are loaded once for all rows).
+template <typename R, int H, int NB>
+__device__ __forceinline__ void r2c_split_m(C2<R>* buf, int bstride, const C2<R>* __restrict__ twr, int t) {
+    constexpr int G = H / 8;
+    for (int k = 1 + t; k < H / 2; k += G) {
+        const C2<R> wk = __ldg(&twr[k]), wm = __ldg(&twr[H - k]);
+#pragma unroll
+        for (int b = 0; b < NB; ++b) {
+            C2<R>* bb = buf + b * bstride;
+            const C2<R> zk = bb[pad8(k)], zm = bb[pad8(H - k)];
+            C2<R> e = mk<R>((R)0.5 * (zk.x + zm.x), (R)0.5 * (zk.y - zm.y));
+            C2<R> d = mk<R>(zk.x - zm.x, zk.y + zm.y);
+            C2<R> o = mk<R>((R)0.5 * d.y, (R)-0.5 * d.x);
+            C2<R> Xk = cadd<R>(e, cmul<R>(wk, o));
+            C2<R> e2 = mk<R>((R)0.5 * (zm.x + zk.x), (R)0.5 * (zm.y - zk.y));
+            C2<R> d2 = mk<R>(zm.x - zk.x, zm.y + zk.y);
+            C2<R> o2 = mk<R>((R)0.5 * d2.y, (R)-0.5 * d2.x);
+            C2<R> Xm = cadd<R>(e2, cmul<R>(wm, o2));
+            bb[pad8(k)] = Xk;
+            bb[pad8(H - k)] = Xm;
+        }
+    }
+    if (t == 0) {
+#pragma unroll
+        for (int b = 0; b < NB; ++b) {
+            C2<R>* bb = buf + b * bstride;
+            C2<R> z0 = bb[pad8(0)];
+            bb[pad8(0)] = mk<R>(z0.x + z0.y, (R)0);
+            C2<R> zh = bb[pad8(H / 2)];
+            bb[pad8(H / 2)] = mk<R>(zh.x, -zh.y);
+        }
+    }
+    __syncthreads();
+}
+
+template <typename R, int H, int NB>
+__device__ __forceinline__ void c2r_merge_m(C2<R>* buf, int bstride, const C2<R>* __restrict__ twr, int t) {
+    constexpr int G = H / 8;
+    for (int k = 1 + t; k < H / 2; k += G) {
+        const C2<R> wk = __ldg(&twr[k]), wm = __ldg(&twr[H - k]);
+#pragma unroll
+        for (int b = 0; b < NB; ++b) {
+            C2<R>* bb = buf + b * bstride;
+            const C2<R> xk = bb[pad8(k)], xm = bb[pad8(H - k)];
+            C2<R> e = mk<R>(xk.x + xm.x, xk.y - xm.y);
+            C2<R> o = cmul<R>(mk<R>(xk.x - xm.x, xk.y + xm.y), mk<R>(wk.x, -wk.y));
+            C2<R> Zk = mk<R>(e.x - o.y, e.y + o.x);
+            C2<R> e2 = mk<R>(xm.x + xk.x, xm.y - xk.y);
+            C2<R> o2 = cmul<R>(mk<R>(xm.x - xk.x, xm.y + xk.y), mk<R>(wm.x, -wm.y));
+            C2<R> Zm = mk<R>(e2.x - o2.y, e2.y + o2.x);
+            bb[pad8(k)] = Zk;
+            bb[pad8(H - k)] = Zm;
+        }
+    }
+    if (t == 0) {
+#pragma unroll
+        for (int b = 0; b < NB; ++b) {
+            C2<R>* bb = buf + b * bstride;
+            C2<R> x0 = bb[pad8(0)];
+            bb[pad8(0)] = mk<R>(x0.x, x0.x);
+            C2<R> xh = bb[pad8(H / 2)];
+            bb[pad8(H / 2)] = mk<R>((R)2 * xh.x, (R)-2 * xh.y);
+        }
     }
     __syncthreads();
 }

@@ -45,6 +45,8 @@ struct KArgs {
 };
 
 template <typename R> constexpr bool kIsF32 = std::is_same<R, float>::value;
+// shared-memory row buffers of k_nl_y: four inverse transforms at a time in FP32, two in FP64
+template <typename R> constexpr int nl_y_bufs() { return kIsF32<R> ? 4 : 2; }
 
 // Error-free transformations for the compensated (hi + lo) vorticity state of the FP32 form.
 __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
@@ -88,12 +90,12 @@ struct XRows {
 };
 
 // A tile height for the fused x-pass kernels: tr when it is valid (a full warp, at most 1024
-// threads, at most 200 KB of shared memory for two row buffers), else the default.
+// threads, at most 200 KB of shared memory for three row buffers), else the default.
 template <typename R, int H>
 constexpr int xrows_valid(int tr) {
     using X = XRows<R, H>;
     return (tr >= 1 && X::G * tr >= 32 && X::G * tr <= 1024 &&
-            2 * tr * X::PL * (int)(2 * sizeof(R)) <= 200 * 1024) ? tr : X::TRD;
+            3 * tr * X::PL * (int)(2 * sizeof(R)) <= 200 * 1024) ? tr : X::TRD;
 }
 
 // ---- x-pass helpers -------------------------------------------------------------------
@@ -117,6 +119,20 @@ template <typename R, int H>
 __device__ __forceinline__ void row_r2c(C2<R>* rb, const C2<R>* __restrict__ twR, const C2<R>* __restrict__ twX, int t) {
     block_fft<R, H, false>(rb, twX, t);
     r2c_split<R, H>(rb, twR, t);
+}
+
+// NB rows at rb + b * bstride at once (their stages share synchronisations and twiddles)
+template <typename R, int H, int NB>
+__device__ __forceinline__ void row_c2r_m(C2<R>* rb, int bstride, const C2<R>* __restrict__ twR,
+                                          const C2<R>* __restrict__ twX, int t) {
+    c2r_merge_m<R, H, NB>(rb, bstride, twR, t);
+    block_fft_m<R, H, true, NB>(rb, bstride, twX, t);
+}
+template <typename R, int H, int NB>
+__device__ __forceinline__ void row_r2c_m(C2<R>* rb, int bstride, const C2<R>* __restrict__ twR,
+                                          const C2<R>* __restrict__ twX, int t) {
+    block_fft_m<R, H, false, NB>(rb, bstride, twX, t);
+    r2c_split_m<R, H, NB>(rb, bstride, twR, t);
 }
 
 template <typename R>
@@ -300,18 +316,20 @@ __global__ void __launch_bounds__(XRows<R, H, TRV>::THREADS) k_nl_x(KArgs<R> a) 
     using X = XRows<R, H, TRV>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C2<R>* bufA = reinterpret_cast<C2<R>*>(smem_raw);
-    C2<R>* bufB = bufA + X::TR * X::PL;
+    constexpr int BS = X::TR * X::PL;  // one row buffer (TR rows)
+    C2<R>* bufB = bufA + BS;
+    C2<R>* bufC = bufB + BS;
     const int r = threadIdx.x / X::G, t = threadIdx.x % X::G;
     const int iy0 = blockIdx.x * X::TR, ny = a.g.ny;
     C2<R>* ra = bufA + r * X::PL;
     C2<R>* rb = bufB + r * X::PL;
+    C2<R>* rc = bufC + r * X::PL;
     // after the first AB2/Euler update the vorticity is dealiased: rows kx >= kcut are zero
     const int kin = a.S->explicit_step ? H : a.kcut;
     load_tileT<R, H, X::TR, X::PL>(bufA, a.Tdx, ny, iy0, kin);
     load_tileT<R, H, X::TR, X::PL>(bufB, a.Tdy, ny, iy0, kin);
     __syncthreads();
-    row_c2r<R, H>(ra, a.twR, a.twX, t);
-    row_c2r<R, H>(rb, a.twR, a.twX, t);
+    row_c2r_m<R, H, 2>(ra, BS, a.twR, a.twX, t);  // ra and rb together
     const int iy = iy0 + r;
     const size_t roff = (size_t)iy * H;
     const C2<R>* u2 = reinterpret_cast<const C2<R>*>(a.u) + roff;
@@ -346,25 +364,18 @@ __global__ void __launch_bounds__(XRows<R, H, TRV>::THREADS) k_nl_x(KArgs<R> a) 
         const int m = t + q * X::G;
         ra[pad8(m)] = wv[q];
         rb[pad8(m)] = pyv[q];
+        rc[pad8(m)] = pxv[q];
     }
     __syncthreads();
-    row_r2c<R, H>(ra, a.twR, a.twX, t);
-    row_r2c<R, H>(rb, a.twR, a.twX, t);
+    row_r2c_m<R, H, 3>(ra, BS, a.twR, a.twX, t);  // ra, rb and rc together
     // the right-hand side only matters where the update keeps modes (kx < kcut)
     for (int i = threadIdx.x; i < a.kcut * X::TR; i += blockDim.x) {
         const int rr = i % X::TR, kx = i / X::TR;
         const C2<R> xa = bufA[rr * X::PL + pad8(kx)], xb = bufB[rr * X::PL + pad8(kx)];
         const R kxs = (R)((double)kx * a.g.kxs);
-        a.A[(size_t)kx * ny + iy0 + rr] = cadd<R>(xa, cimul<R>(xb, kxs));
-    }
-    __syncthreads();
-#pragma unroll
-    for (int q = 0; q < 8; ++q) ra[pad8(t + q * X::G)] = pxv[q];
-    __syncthreads();
-    row_r2c<R, H>(ra, a.twR, a.twX, t);
-    for (int i = threadIdx.x; i < a.kcut * X::TR; i += blockDim.x) {
-        const int rr = i % X::TR, kx = i / X::TR;
-        a.B[(size_t)kx * ny + iy0 + rr] = bufA[rr * X::PL + pad8(kx)];
+        const size_t o = (size_t)kx * ny + iy0 + rr;
+        a.A[o] = cadd<R>(xa, cimul<R>(xb, kxs));
+        a.B[o] = bufC[rr * X::PL + pad8(kx)];
     }
 }
 
@@ -373,7 +384,9 @@ __global__ void __launch_bounds__(XRows<R, H, TRV>::THREADS) k_nl_x(KArgs<R> a) 
 // inverse-y transforms of everything the velocity/pressure/force kernels need.
 // ======================================================================================
 template <typename R, int NY>
-__global__ void __launch_bounds__(NY / 8) k_nl_y(KArgs<R> a) {
+// (FP32: at most 128 registers a thread, so that four blocks share an SM and the 512 rows of
+// 1024^2 run in one wave)
+__global__ void __launch_bounds__(NY / 8, kIsF32<R> ? 4 : 1) k_nl_y(KArgs<R> a) {
     constexpr int G = NY / 8;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C2<R>* bufA = reinterpret_cast<C2<R>*>(smem_raw);
@@ -398,8 +411,7 @@ __global__ void __launch_bounds__(NY / 8) k_nl_y(KArgs<R> a) {
         bufB[pad8(t + q * G)] = a.B[row + t + q * G];
     }
     __syncthreads();
-    block_fft<R, NY, false>(bufA, a.twY, t);
-    block_fft<R, NY, false>(bufB, a.twY, t);
+    block_fft_m<R, NY, false, 2>(bufA, padded_len(NY), a.twY, t);  // bufA and bufB together
     const DevScalars* S = a.S;
     const double dt1 = S->dt1, b10 = S->b10, b11 = S->b11;
     const bool expl = S->explicit_step != 0;
@@ -461,43 +473,64 @@ __global__ void __launch_bounds__(NY / 8) k_nl_y(KArgs<R> a) {
         else if constexpr (kIsF32<R>) ps[q] = cscale<R>(Wn, (R)1 / k2);
         else ps[q] = mk<R>(Wn.x / k2, Wn.y / k2);   // poisson.f90:159-162 divides
     }
-    // inverse-y outputs
+    // inverse-y outputs, NBO at a time: their transforms share the stages' synchronisations
+    // and twiddle loads (NBO buffers of shared memory)
+    constexpr int NBO = nl_y_bufs<R>();
+    constexpr int PLY = padded_len(NY);
     const R kxs = (R)kx * (R)g.kxs;
     const int nout = a.viscous ? 7 : 5;
-    for (int o = 0; o < nout; ++o) {
-        C2<R>* dst;
+    auto out_ptr = [&](int o) -> C2<R>* {
         switch (o) {
-            case 0: dst = a.Tu; break;
-            case 1: dst = a.Tv; break;
-            case 2: dst = a.Tw; break;
-            case 3: dst = a.Tdx; break;
-            case 4: dst = a.Tdy; break;
-            case 5: dst = a.Tsa; break;
-            default: dst = a.Tsb; break;
+            case 0: return a.Tu;
+            case 1: return a.Tv;
+            case 2: return a.Tw;
+            case 3: return a.Tdx;
+            case 4: return a.Tdy;
+            case 5: return a.Tsa;
+            default: return a.Tsb;
         }
+    };
+    for (int o0 = 0; o0 < nout; o0 += NBO) {
+        const int cnt = (nout - o0 < NBO) ? nout - o0 : NBO;
         __syncthreads();
+        for (int b = 0; b < cnt; ++b) {
+            const int o = o0 + b;
+            C2<R>* buf = bufA + b * PLY;
 #pragma unroll
-        for (int q = 0; q < 8; ++q) {
-            const int ky = t + q * G;
-            const int ks = signed_k(ky, NY);
-            const R kys = (R)ks * (R)g.kys;
-            C2<R> val;
-            switch (o) {
-                case 0: val = cimul<R>(ps[q], kys); break;                 // cofdy(psi)   -> u
-                case 1: val = cimul<R>(ps[q], kxs); break;                 // cofdx(psi)   -> -v
-                case 2: val = wn[q]; break;                                // omega
-                case 3: val = cimul<R>(wn[q], kxs); break;                 // cofdx(omega)
-                case 4: val = cimul<R>(wn[q], kys); break;                 // cofdy(omega)
-                case 5: val = cscale<R>(ps[q], -(kxs * kys)); break;       // d2psi/dxdy = du/dx
-                default: val = cscale<R>(ps[q], kxs * kxs - kys * kys); break;  // du/dy + dv/dx
+            for (int q = 0; q < 8; ++q) {
+                const int ky = t + q * G;
+                const int ks = signed_k(ky, NY);
+                const R kys = (R)ks * (R)g.kys;
+                C2<R> val;
+                switch (o) {
+                    case 0: val = cimul<R>(ps[q], kys); break;                 // cofdy(psi)   -> u
+                    case 1: val = cimul<R>(ps[q], kxs); break;                 // cofdx(psi)   -> -v
+                    case 2: val = wn[q]; break;                                // omega
+                    case 3: val = cimul<R>(wn[q], kxs); break;                 // cofdx(omega)
+                    case 4: val = cimul<R>(wn[q], kys); break;                 // cofdy(omega)
+                    case 5: val = cscale<R>(ps[q], -(kxs * kys)); break;       // d2psi/dxdy = du/dx
+                    default: val = cscale<R>(ps[q], kxs * kxs - kys * kys); break;  // du/dy + dv/dx
+                }
+                if (ky == NY / 2) val = mk<R>(0, 0);
+                buf[pad8(ky)] = val;
             }
-            if (ky == NY / 2) val = mk<R>(0, 0);
-            bufA[pad8(ky)] = val;
         }
         __syncthreads();
-        block_fft<R, NY, true>(bufA, a.twY, t);
+        if (cnt == 4) {
+            if constexpr (NBO >= 4) block_fft_m<R, NY, true, 4>(bufA, PLY, a.twY, t);
+        } else if (cnt == 3) {
+            if constexpr (NBO >= 3) block_fft_m<R, NY, true, 3>(bufA, PLY, a.twY, t);
+        } else if (cnt == 2) {
+            block_fft_m<R, NY, true, 2>(bufA, PLY, a.twY, t);
+        } else {
+            block_fft<R, NY, true>(bufA, a.twY, t);
+        }
+        for (int b = 0; b < cnt; ++b) {
+            C2<R>* dst = out_ptr(o0 + b);
+            const C2<R>* buf = bufA + b * PLY;
 #pragma unroll
-        for (int q = 0; q < 8; ++q) dst[row + t + q * G] = bufA[pad8(t + q * G)];
+            for (int q = 0; q < 8; ++q) dst[row + t + q * G] = buf[pad8(t + q * G)];
+        }
     }
 }
 
@@ -512,12 +545,15 @@ __global__ void __launch_bounds__(XRows<R, H, TRV>::THREADS, (sizeof(R) == 4) ? 
     using X = XRows<R, H, TRV>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C2<R>* bufA = reinterpret_cast<C2<R>*>(smem_raw);
-    C2<R>* bufB = bufA + X::TR * X::PL;
+    constexpr int BS = X::TR * X::PL;  // one row buffer (TR rows)
+    C2<R>* bufB = bufA + BS;
+    C2<R>* bufC = bufB + BS;
     __shared__ double red_s[RED_NSLOTS][X::THREADS / 32];
     const int r = threadIdx.x / X::G, t = threadIdx.x % X::G;
     const int iy0 = blockIdx.x * X::TR, ny = a.g.ny;
     C2<R>* ra = bufA + r * X::PL;
     C2<R>* rb = bufB + r * X::PL;
+    C2<R>* rc = bufC + r * X::PL;
     const DevScalars* S = a.S;
     const double time = S->time, dt1 = S->dt1;
     const R U = (R)S->mean_u_next, V = (R)S->mean_v_next;
@@ -525,9 +561,9 @@ __global__ void __launch_bounds__(XRows<R, H, TRV>::THREADS, (sizeof(R) == 4) ? 
 
     load_tileT<R, H, X::TR, X::PL>(bufA, a.Tu, ny, iy0, a.kcut);
     load_tileT<R, H, X::TR, X::PL>(bufB, a.Tv, ny, iy0, a.kcut);
+    load_tileT<R, H, X::TR, X::PL>(bufC, a.Tw, ny, iy0, a.kcut);
     __syncthreads();
-    row_c2r<R, H>(ra, a.twR, a.twX, t);
-    row_c2r<R, H>(rb, a.twR, a.twX, t);
+    row_c2r_m<R, H, 3>(ra, BS, a.twR, a.twX, t);  // u, v and omega together
     C2<R> uv[8], vv[8], wv[8];
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
@@ -541,12 +577,8 @@ __global__ void __launch_bounds__(XRows<R, H, TRV>::THREADS, (sizeof(R) == 4) ? 
             vv[q] = mk<R>(-vr.x + V, -vr.y + V);
         }
     }
-    __syncthreads();
-    load_tileT<R, H, X::TR, X::PL>(bufA, a.Tw, ny, iy0, a.kcut);
-    __syncthreads();
-    row_c2r<R, H>(ra, a.twR, a.twX, t);
 #pragma unroll
-    for (int q = 0; q < 8; ++q) wv[q] = ra[pad8(t + q * X::G)];
+    for (int q = 0; q < 8; ++q) wv[q] = rc[pad8(t + q * X::G)];
     __syncthreads();
 
     const int iy = iy0 + r;
@@ -671,8 +703,7 @@ __global__ void __launch_bounds__(XRows<R, H, TRV>::THREADS, (sizeof(R) == 4) ? 
         if (blockIdx.x == 0 && s == 0) a.S->nred = (int)gridDim.x;
     }
     if (a.pressure_on) {
-        row_r2c<R, H>(ra, a.twR, a.twX, t);
-        row_r2c<R, H>(rb, a.twR, a.twX, t);
+        row_r2c_m<R, H, 2>(ra, BS, a.twR, a.twX, t);  // ra and rb together
         for (int i = threadIdx.x; i < H * X::TR; i += blockDim.x) {
             const int rr = i % X::TR, kx = i / X::TR;
             const R kxs = (R)((double)kx * a.g.kxs);
@@ -686,8 +717,7 @@ __global__ void __launch_bounds__(XRows<R, H, TRV>::THREADS, (sizeof(R) == 4) ? 
         load_tileT<R, H, X::TR, X::PL>(bufA, a.Tsa, ny, iy0, a.kcut);
         load_tileT<R, H, X::TR, X::PL>(bufB, a.Tsb, ny, iy0, a.kcut);
         __syncthreads();
-        row_c2r<R, H>(ra, a.twR, a.twX, t);
-        row_c2r<R, H>(rb, a.twR, a.twX, t);
+        row_c2r_m<R, H, 2>(ra, BS, a.twR, a.twX, t);  // ra and rb together
         C2<R>* sa2 = reinterpret_cast<C2<R>*>(a.sa) + roff;
         C2<R>* sb2 = reinterpret_cast<C2<R>*>(a.sb) + roff;
         const R c2 = (R)(2.0 * a.nu), c1 = (R)a.nu;
@@ -717,8 +747,7 @@ __global__ void __launch_bounds__(NY / 8) k_press_y(KArgs<R> a) {
         bufB[pad8(t + q * G)] = a.P2[row + t + q * G];
     }
     __syncthreads();
-    block_fft<R, NY, false>(bufA, a.twY, t);
-    block_fft<R, NY, false>(bufB, a.twY, t);
+    block_fft_m<R, NY, false, 2>(bufA, padded_len(NY), a.twY, t);  // bufA and bufB together
     const R norm = (R)(1.0 / ((double)g.nx * (double)g.ny));
     C2<R> qv[8];
 #pragma unroll
@@ -789,7 +818,7 @@ struct SizeKernels {
     int x_threads, x_rows, x_smem1, x_smem2;
     // tile-height candidates of the fused x kernels (index 1 is the default)
     struct XVariant {
-        int rows, threads, smem1, smem2;
+        int rows, threads, smem1, smem3;  // smem3: the three row buffers of nl_x / press_x
         void (*nl_x)(KArgs<R>);
         void (*press_x)(KArgs<R>);
         void (*press_fin)(KArgs<R>);
@@ -799,7 +828,7 @@ struct SizeKernels {
     void (*yinv)(KArgs<R>);
     void (*nl_y)(KArgs<R>);
     void (*press_y)(KArgs<R>);
-    int y_threads, y_smem1, y_smem2;
+    int y_threads, y_smem1, y_smem2, y_smem_nl;
 };
 
 template <typename R, int H, int TR>
@@ -808,12 +837,12 @@ inline void fill_xvariant(typename SizeKernels<R>::XVariant& v) {
     v.rows = TR;
     v.threads = X::THREADS;
     v.smem1 = (int)(TR * X::PL * sizeof(C2<R>));
-    v.smem2 = 2 * v.smem1;
+    v.smem3 = 3 * v.smem1;
     v.nl_x = k_nl_x<R, H, TR>;
     v.press_x = k_press_x<R, H, TR>;
     v.press_fin = k_press_fin<R, H, TR>;
-    cudaFuncSetAttribute(k_nl_x<R, H, TR>, cudaFuncAttributeMaxDynamicSharedMemorySize, v.smem2);
-    cudaFuncSetAttribute(k_press_x<R, H, TR>, cudaFuncAttributeMaxDynamicSharedMemorySize, v.smem2);
+    cudaFuncSetAttribute(k_nl_x<R, H, TR>, cudaFuncAttributeMaxDynamicSharedMemorySize, v.smem3);
+    cudaFuncSetAttribute(k_press_x<R, H, TR>, cudaFuncAttributeMaxDynamicSharedMemorySize, v.smem3);
     cudaFuncSetAttribute(k_press_fin<R, H, TR>, cudaFuncAttributeMaxDynamicSharedMemorySize, v.smem1);
 }
 
@@ -845,9 +874,10 @@ inline void fill_size_kernels(SizeKernels<R>& k) {
     k.y_threads = N / 8;
     k.y_smem1 = (int)(padded_len(N) * sizeof(C2<R>));
     k.y_smem2 = 2 * k.y_smem1;
+    k.y_smem_nl = nl_y_bufs<R>() * k.y_smem1;
     cudaFuncSetAttribute(k_yfwd<R, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, k.y_smem1);
     cudaFuncSetAttribute(k_yinv<R, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, k.y_smem1);
-    cudaFuncSetAttribute(k_nl_y<R, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, k.y_smem2);
+    cudaFuncSetAttribute(k_nl_y<R, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, k.y_smem_nl);
     cudaFuncSetAttribute(k_press_y<R, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, k.y_smem2);
 }
 
