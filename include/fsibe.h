@@ -249,7 +249,9 @@ int fsibe_drag_gradient(fsibe_ctx* ctx, const double* vort0, double nu, int nste
  * functions above.  fsibe_ensemble_step advances every run by nsteps; after the first step
  * (every run's Euler start-up step) one step of all runs is one CUDA graph launch, with each
  * run's step on its own stream.  Work issued on a run's context directly is ordered before
- * and after the ensemble's steps. */
+ * and after the ensemble's steps.  Ensembles of 8 runs or more run each beam on one CTA
+ * (fsibe_beam_cluster reports 0) unless FSIBE_BEAM_CLUSTER is set: many runs fill the GPU by
+ * themselves, and the single-CTA kernel then gives the higher throughput. */
 typedef struct fsibe_ensemble fsibe_ensemble;
 int fsibe_ensemble_create(const fsibe_params* params, int nruns, fsibe_ensemble** out);
 int fsibe_ensemble_destroy(fsibe_ensemble* ens);
