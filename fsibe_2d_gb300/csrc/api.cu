@@ -439,6 +439,8 @@ struct fsibe_ctx {
     double* pred = nullptr; // predictor output
     cudaStream_t side = nullptr;  // the beam predictor runs here beside the fluid step
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    cudaStream_t side2 = nullptr;                     // the fluid step's scalar reductions run here
+    cudaEvent_t ev_ff = nullptr, ev_ffj = nullptr;
     bool pre_launched = false;    // the predictor of the current step is in flight
     struct AdjWork* adj = nullptr;  // adjoint buffers and checkpoints (allocated on first use)
     bool initialized = false, startup_done = false;
@@ -685,9 +687,14 @@ static int fluid_step_t(fsibe_ctx* c, int explicit_step) {
     launch_xv<R>(c, KX.xv[c->xv_nl].nl_x, KX.xv[c->xv_nl], 3, a, "nl_x");
     launch_y<R>(c, KY.nl_y, KY.y_smem_nl, a, "nl_y");
     launch_xv<R>(c, KX.xv[c->xv_px].press_x, KX.xv[c->xv_px], 3, a, "press_x");
-    prof_begin(c, "fluid_finish");
-    k_fluid_finish<<<1, 256, 0, c->stream>>>(sa);
-    prof_end(c);
+    // the energies, drag and unsteady forces from press_x's partial sums feed only scalars read
+    // after the fluid step: a second side stream runs them beside the pressure transforms
+    CK(c, cudaEventRecord(c->ev_ff, c->stream));
+    CK(c, cudaStreamWaitEvent(c->side2, c->ev_ff, 0));
+    prof_begin(c, "fluid_finish", c->side2);
+    k_fluid_finish<<<1, 256, 0, c->side2>>>(sa);
+    prof_end(c, c->side2);
+    CK(c, cudaEventRecord(c->ev_ffj, c->side2));
     c->launches++;
     if (a.pressure_on) {
         launch_y<R>(c, KY.press_y, KY.y_smem2, a, "press_y");
@@ -695,6 +702,7 @@ static int fluid_step_t(fsibe_ctx* c, int explicit_step) {
     } else {
         CK(c, cudaMemsetAsync(c->phys[PH_PRESS], 0, sizeof(R) * (size_t)c->g.nx * c->g.ny, c->stream));
     }
+    CK(c, cudaStreamWaitEvent(c->stream, c->ev_ffj, 0));
     CKL(c);
     return FSIBE_OK;
 }
@@ -1062,6 +1070,9 @@ int fsibe_destroy(fsibe_ctx* c) {
     if (c->ev_fork) cudaEventDestroy(c->ev_fork);
     if (c->ev_join) cudaEventDestroy(c->ev_join);
     if (c->side) { cudaStreamSynchronize(c->side); cudaStreamDestroy(c->side); }
+    if (c->side2) { cudaStreamSynchronize(c->side2); cudaStreamDestroy(c->side2); }
+    if (c->ev_ff) cudaEventDestroy(c->ev_ff);
+    if (c->ev_ffj) cudaEventDestroy(c->ev_ffj);
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return FSIBE_OK;
@@ -1205,6 +1216,10 @@ int fsibe_create(const fsibe_params* p, fsibe_ctx** out) {
     if (e != cudaSuccess) { g_err = cudaGetErrorString(e); fsibe_destroy(c); return FSIBE_ERR_CUDA; }
     cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming);
     cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming);
+    e = cudaStreamCreateWithFlags(&c->side2, cudaStreamNonBlocking);
+    if (e != cudaSuccess) { g_err = cudaGetErrorString(e); fsibe_destroy(c); return FSIBE_ERR_CUDA; }
+    cudaEventCreateWithFlags(&c->ev_ff, cudaEventDisableTiming);
+    cudaEventCreateWithFlags(&c->ev_ffj, cudaEventDisableTiming);
     {
         const int st = c->fp32 ? autotune_x<float>(c) : autotune_x<double>(c);
         if (st) { g_err = c->err; fsibe_destroy(c); return st; }

@@ -795,7 +795,9 @@ __global__ void __launch_bounds__(XRows<R, H, TRV>::THREADS) k_press_fin(KArgs<R
         const C2<R> qq = rb[pad8(m)];
         C2<R> uu = u2[m], vq = v2[m];
         if constexpr (kIsF32<R>) {
-            const R Uc = (R)a.S->mean_u_cur, Vc = (R)a.S->mean_v_cur;
+            // the velocity press_x stored holds the mean flow at time + dt1 (mean_u_next; the
+            // fluid step's last scalar kernel copies it to mean_u_cur, beside this kernel)
+            const R Uc = (R)a.S->mean_u_next, Vc = (R)a.S->mean_v_next;
             uu = mk<R>(uu.x + Uc, uu.y + Uc);
             vq = mk<R>(vq.x + Vc, vq.y + Vc);
         }

@@ -72,6 +72,7 @@ __global__ void __launch_bounds__(64) k_mask_prep(MaskArgs a, double gerf) {
             P.p[2] = ca * p1x - sa * p1y; P.p[3] = sa * p1x + ca * p1y;
             P.p[4] = ca * p2x - sa * p2y; P.p[5] = sa * p2x + ca * p2y;
             P.p[6] = a.vx[i]; P.p[7] = a.vy[i]; P.p[8] = a.vx[i + 1]; P.p[9] = a.vy[i + 1];
+            P.p[10] = p1x; P.p[11] = p1y;  // the FP32 raster works relative to the start point
             emit(i, P);
         }
         if (hinge) ang2[lane] = atan2((a.y[i + 1] - a.y[i]), (a.x[i + 1] - a.x[i]));
@@ -222,18 +223,66 @@ __device__ __forceinline__ double smooth_step_d(double x, double t, double inv_d
 
 // Per-cell fold state of one warp over its share of the primitives: the largest SmoothStep so
 // far, its velocity and primitive index (INT_MAX: none yet), and an FP32 lower bound of m.
+// T: double in the FP64 form, float in the FP32 form.
+template <typename T>
 struct MaskFold {
-    double m, vx, vy;
+    T m, vx, vy;
     int idx;
     float mlow;
 };
 
 // Draw order keeps the first of equal values (strict >); over a subset taken in any order the
 // same winner is the largest value with the smallest index among its ties.
-__device__ __forceinline__ void fold_take(MaskFold& f, double temp, double vx, double vy, int q) {
+template <typename T>
+__device__ __forceinline__ void fold_take(MaskFold<T>& f, T temp, T vx, T vy, int q) {
     if (temp > f.m || (temp == f.m && f.idx != 0x7fffffff && q < f.idx)) {
-        f.m = temp; f.vx = vx; f.vy = vy; f.idx = q; f.mlow = __double2float_rd(temp);
+        f.m = temp; f.vx = vx; f.vy = vy; f.idx = q;
+        if constexpr (sizeof(T) == 8) f.mlow = __double2float_rd(temp);
     }
+}
+
+// SmoothStep in FP32 from FP32 arguments (the FP32 form's raster).
+__device__ __forceinline__ float smooth_step_ff(float x, float t, float inv_delta, int sharp) {
+    if (sharp) return (x <= t) ? 1.f : 0.f;
+    return 0.5f * (erff((t - x) * inv_delta) + erff((x + t) * inv_delta));
+}
+
+// The FP32 form's per-primitive data, relative to the tile origin (x0, y0) so that every
+// coordinate is small and FP32 keeps it to ~1e-9:
+//   segment: a = (cos, sin, p1x - x0, p1y - y0), b = (length along the axis, lower bound of the
+//            normal offset, -, -), c = (v1x, v1y, (v2x - v1x)/ds, (v2y - v1y)/ds)
+//   hinge / dot: a = (px - x0, py - y0, R^2 limit, -), b = (beta1, beta2, -, -), c = (vx, vy, -, -)
+struct PrimG {
+    float4 a, b, c;
+};
+
+// Segment, hinge or dot q for the lane's cell at (cx, cy) from the tile origin, all in FP32:
+// the FP32 form's mask is continuous across every primitive's edge (a segment's end meets its
+// hinge's disc with the same value and velocity, the outer edges have SmoothStep ~ 0), so the
+// exact FP64 edge tests of the FP64 form are not needed for its tolerance.
+__device__ __forceinline__ void mask_prim_f(const MaskArgs& a, const Prim& Q, const PrimG& G, int q, int i, int j,
+                                            float cx, float cy, float tf, float tsf, float idf, MaskFold<float>& f) {
+    if (i < Q.box[0] || i > Q.box[1] || j < Q.box[2] || j > Q.box[3]) return;
+    if (Q.type == PRIM_SEGMENT) {
+        const float xr = cx - G.a.z, yr = cy - G.a.w;
+        const float u = G.a.x * xr - G.a.y * yr, w = G.a.y * xr + G.a.x * yr;
+        if (u < 0.f || u > G.b.x || w > tsf || w < G.b.y) return;
+        const float temp = smooth_step_ff(fabsf(w), tf, idf, a.sharp);
+        if (temp >= f.m) fold_take<float>(f, temp, G.c.x + u * G.c.z, G.c.y + u * G.c.w, q);
+        return;
+    }
+    const float ddx = cx - G.a.x, ddy = cy - G.a.y, r2 = ddx * ddx + ddy * ddy;
+    if (r2 > G.a.z) return;
+    if (Q.type == PRIM_HINGE) {
+        float gf = atan2f(ddy, ddx);
+        if (gf < 0.f) gf = 6.28318530717958647692f + gf;
+        gf = gf * 57.2957795130823208768f;
+        if (!hinge_inside<float>(gf, G.b.x, G.b.y, 0.f, nullptr)) return;
+        const float Rr = sqrtf(r2);
+        if (Rr <= tsf) fold_take<float>(f, smooth_step_ff(Rr, tf, idf, a.sharp), G.c.x, G.c.y, q);
+        return;
+    }
+    fold_take<float>(f, smooth_step_ff(sqrtf(r2), tf, idf, a.sharp), G.c.x, G.c.y, q);
 }
 
 // Segment, hinge or dot q for the lane's cell (i, j), FP32 pre-test first.  R = float: the FP32
@@ -243,7 +292,7 @@ __device__ __forceinline__ void fold_take(MaskFold& f, double temp, double vx, d
 template <typename R>
 __device__ __forceinline__ void mask_prim(const MaskArgs& a, const Prim& Q, const PrimF& F, int q, int i, int j,
                                           double xi, double yj, float xf, float yf, double t, double t_star,
-                                          double inv_delta, double inv_ds, MaskFold& f) {
+                                          double inv_delta, double inv_ds, MaskFold<double>& f) {
     if (i < Q.box[0] || i > Q.box[1] || j < Q.box[2] || j > Q.box[3]) return;
     if (Q.type == PRIM_SEGMENT) {
         const float xs_f = xf * F.a.x - yf * F.a.y, ys_f = xf * F.a.y + yf * F.a.x;
@@ -312,8 +361,11 @@ __device__ __forceinline__ void mask_prim(const MaskArgs& a, const Prim& Q, cons
 // hinges and dots.
 template <typename R>
 __global__ void __launch_bounds__(32 * MASK_WARPS) k_mask_raster(MaskArgs a, double gerf) {
+    constexpr bool F32 = sizeof(R) == 4;
+    using T = R;  // the fold's arithmetic: FP32 in the FP32 form, FP64 in the FP64 form
     __shared__ Prim sp[MASK_WARPS][32];
-    __shared__ PrimF sf[MASK_WARPS][32];
+    __shared__ PrimF sf[MASK_WARPS][F32 ? 1 : 32];
+    __shared__ PrimG sg[MASK_WARPS][F32 ? 32 : 1];
     __shared__ double cmv[MASK_WARPS][3][32];
     __shared__ int cidx[MASK_WARPS][32];
     R* mk_ = reinterpret_cast<R*>(a.mask);
@@ -333,6 +385,9 @@ __global__ void __launch_bounds__(32 * MASK_WARPS) k_mask_raster(MaskArgs a, dou
     const float mg = 1.0e-5f * (float)fmax((double)a.nx * dx, (double)a.ny * dy);
     const int total = *a.nprims;
     const int nseg = a.ns - 1, nsharp = (a.sharp_trailing == 1) ? 1 : 0;
+    // FP32 form: the cell's offset from its tile's origin and the SmoothStep constants
+    const float cx = (float)((double)(lane % MASK_TX) * dx), cy = (float)((double)(lane / MASK_TX) * dy);
+    const float tf = (float)t, tsf = (float)t_star, idf = (float)inv_delta;
     for (int tile = blockIdx.x; tile < ntx * nty; tile += gridDim.x) {
         const int ix0 = (tx0 + tile % ntx) * MASK_TX, iy0 = (ty0 + tile / ntx) * MASK_TY;
         const int ix1 = ix0 + MASK_TX - 1, iy1 = iy0 + MASK_TY - 1;
@@ -344,8 +399,9 @@ __global__ void __launch_bounds__(32 * MASK_WARPS) k_mask_raster(MaskArgs a, dou
         }
         const double xi = (double)i * dx, yj = (double)j * dy;
         const float xf = (float)xi, yf = (float)yj;
-        MaskFold f;
-        f.m = 0.0; f.vx = 0.0; f.vy = 0.0; f.idx = 0x7fffffff; f.mlow = 0.f;
+        const double x0 = (double)ix0 * dx, y0 = (double)iy0 * dy;
+        MaskFold<T> f;
+        f.m = (T)0; f.vx = (T)0; f.vy = (T)0; f.idx = 0x7fffffff; f.mlow = 0.f;
         // this warp's primitives of [q0, q1): q = q0 + MASK_WARPS (32 c + lane) + warp, staged
         // per round of 32 with their FP32 pre-test data
         auto fold_range = [&](int q0, int q1) {
@@ -362,23 +418,44 @@ __global__ void __launch_bounds__(32 * MASK_WARPS) k_mask_raster(MaskArgs a, dou
                 if (hit) {
                     const int e = __popc(bal & ((1u << lane) - 1u));
                     sp[warp][e] = P;
-                    PrimF F;
-                    if (P.type == PRIM_SEGMENT || P.type == PRIM_SHARP) {
-                        F.a = make_float4((float)P.p[0], (float)P.p[1], (float)P.p[2] - mg, (float)P.p[4] + mg);
-                        F.b = make_float2((float)(P.p[3] + t_star) + mg, (float)(P.p[5] - t_star) - mg);
+                    if constexpr (F32) {
+                        PrimG G;
+                        if (P.type == PRIM_SEGMENT) {
+                            G.a = make_float4((float)P.p[0], (float)P.p[1], (float)(P.p[10] - x0), (float)(P.p[11] - y0));
+                            G.b = make_float4((float)(P.p[4] - P.p[2]), (float)((P.p[5] - P.p[3]) - t_star), 0.f, 0.f);
+                            G.c = make_float4((float)P.p[6], (float)P.p[7], (float)((P.p[8] - P.p[6]) * inv_ds),
+                                              (float)((P.p[9] - P.p[7]) * inv_ds));
+                        } else {
+                            const float lim = (float)((P.type == PRIM_HINGE) ? t_star : rcut) + mg;
+                            G.a = make_float4((float)(P.p[0] - x0), (float)(P.p[1] - y0), lim * lim, 0.f);
+                            G.b = make_float4((float)P.p[2], (float)P.p[3], 0.f, 0.f);
+                            G.c = (P.type == PRIM_HINGE) ? make_float4((float)P.p[4], (float)P.p[5], 0.f, 0.f)
+                                                         : make_float4((float)P.p[2], (float)P.p[3], 0.f, 0.f);
+                        }
+                        sg[warp][e] = G;
                     } else {
-                        const float lim = (float)((P.type == PRIM_HINGE) ? t_star : rcut) + mg;
-                        F.a = make_float4((float)P.p[0], (float)P.p[1], lim * lim, 0.f);
-                        F.b = make_float2(0.f, 0.f);
+                        PrimF F;
+                        if (P.type == PRIM_SEGMENT || P.type == PRIM_SHARP) {
+                            F.a = make_float4((float)P.p[0], (float)P.p[1], (float)P.p[2] - mg, (float)P.p[4] + mg);
+                            F.b = make_float2((float)(P.p[3] + t_star) + mg, (float)(P.p[5] - t_star) - mg);
+                        } else {
+                            const float lim = (float)((P.type == PRIM_HINGE) ? t_star : rcut) + mg;
+                            F.a = make_float4((float)P.p[0], (float)P.p[1], lim * lim, 0.f);
+                            F.b = make_float2(0.f, 0.f);
+                        }
+                        sf[warp][e] = F;
                     }
-                    sf[warp][e] = F;
                     cidx[warp][e] = q;
                 }
                 __syncwarp();
                 const int nl = __popc(bal);
-                for (int e = 0; e < nl; ++e)
-                    mask_prim<R>(a, sp[warp][e], sf[warp][e], cidx[warp][e], i, j, xi, yj, xf, yf, t, t_star,
-                                 inv_delta, inv_ds, f);
+                for (int e = 0; e < nl; ++e) {
+                    if constexpr (F32)
+                        mask_prim_f(a, sp[warp][e], sg[warp][e], cidx[warp][e], i, j, cx, cy, tf, tsf, idf, f);
+                    else
+                        mask_prim<R>(a, sp[warp][e], sf[warp][e], cidx[warp][e], i, j, xi, yj, xf, yf, t, t_star,
+                                     inv_delta, inv_ds, f);
+                }
                 __syncwarp();
             }
         };
@@ -390,13 +467,13 @@ __global__ void __launch_bounds__(32 * MASK_WARPS) k_mask_raster(MaskArgs a, dou
             cidx[warp][lane] = my;
             __syncthreads();
             for (int w = 0; w < MASK_WARPS; ++w) {
-                const double mw = cmv[w][0][lane];
+                const T mw = (T)cmv[w][0][lane];
                 const int iw = cidx[w][lane];
                 if (mw > f.m || (mw == f.m && iw < f.idx)) {
-                    f.m = mw; f.vx = cmv[w][1][lane]; f.vy = cmv[w][2][lane]; f.idx = iw;
+                    f.m = mw; f.vx = (T)cmv[w][1][lane]; f.vy = (T)cmv[w][2][lane]; f.idx = iw;
                 }
             }
-            f.mlow = __double2float_rd(f.m);
+            if constexpr (!F32) f.mlow = __double2float_rd(f.m);
             __syncthreads();
         };
         fold_range(0, nseg);
@@ -415,9 +492,9 @@ __global__ void __launch_bounds__(32 * MASK_WARPS) k_mask_raster(MaskArgs a, dou
                         tmp2 = smooth_step_d(xs - Q.p[2], two_mxd, inv_delta, a.sharp);
                         temp = smooth_step_d(fabs(ys - Q.p[3]), t, inv_delta, a.sharp);
                     }
-                    f.m = temp * tmp2;
-                    f.mlow = __double2float_rd(f.m);
-                    if (xs - Q.p[2] >= two_mxd) { f.vx = Q.p[6]; f.vy = Q.p[7]; }
+                    f.m = (T)(temp * tmp2);
+                    f.mlow = __double2float_rd(temp * tmp2);
+                    if (xs - Q.p[2] >= two_mxd) { f.vx = (T)Q.p[6]; f.vy = (T)Q.p[7]; }
                 }
             }
         }
@@ -425,7 +502,7 @@ __global__ void __launch_bounds__(32 * MASK_WARPS) k_mask_raster(MaskArgs a, dou
         fold_range(nseg + nsharp, total);
         combine();
         if (warp == 0) {
-            mk_[cell] = (R)(f.m * inv_eps);
+            mk_[cell] = (R)((double)f.m * inv_eps);
             vx_[cell] = (R)f.vx;
             vy_[cell] = (R)f.vy;
         }
