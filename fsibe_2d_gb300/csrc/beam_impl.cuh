@@ -238,52 +238,79 @@ __device__ int refine_step(double* x, const float* cf, int n, int pass, float& c
     return 0;
 }
 
-// Tridiagonal system (dl, d, du) x = b (dl, du: n-1 entries) solved to the accuracy of
-// LAPACK dgttrf + dgttrs: dgttrf's elimination with partial pivoting, in FP32 on one thread,
-// preconditions an FP64 iterative refinement with block-cooperative residuals.  fs: 5n
-// floats of scratch, ip: n ints.  Returns non-zero on an exactly zero pivot.
+// One warp solves the first-order recurrence v_i = a_i v_(i-1) + c_i, v_(-1) = 0, over
+// i = 0..n-1 (rev: over i = n-1..0 with v_n = 0), and writes out_i = v_i (times scale_i when
+// scale is given).  Lane L takes a chunk of consecutive terms: it composes the chunk's affine
+// maps, a shuffle scan composes the chunks, and each lane replays its chunk from the value
+// that enters it.  out may alias c (each lane reads and writes only its own chunk).
+__device__ __forceinline__ void warp_affine_scan(const float* a, const float* c, float* out, const float* scale, int n,
+                                                 bool rev) {
+    const int lane = threadIdx.x & 31;
+    const int k = (n + 31) / 32;
+    const int s0 = lane * k < n ? lane * k : n, s1 = (s0 + k) < n ? s0 + k : n;
+    float A = 1.f, C = 0.f;
+    for (int s = s0; s < s1; ++s) {
+        const int i = rev ? n - 1 - s : s;
+        C = __fmaf_rn(a[i], C, c[i]);
+        A = __fmul_rn(a[i], A);
+    }
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const float Ap = __shfl_up_sync(0xffffffffu, A, o), Cp = __shfl_up_sync(0xffffffffu, C, o);
+        if (lane >= o) {
+            C = __fmaf_rn(A, Cp, C);
+            A = __fmul_rn(A, Ap);
+        }
+    }
+    float v = __shfl_up_sync(0xffffffffu, C, 1);
+    if (lane == 0) v = 0.f;
+    for (int s = s0; s < s1; ++s) {
+        const int i = rev ? n - 1 - s : s;
+        v = __fmaf_rn(a[i], v, c[i]);
+        out[i] = scale ? __fmul_rn(v, scale[i]) : v;
+    }
+}
+
+// Tridiagonal system (dl, d, du) x = b (dl, du: n-1 entries) solved to the accuracy of an FP64
+// factorisation (LAPACK dgttrf + dgttrs): an FP32 LU without interchanges (the scaled tension
+// system is diagonally dominant) preconditions an FP64 iterative refinement with
+// block-cooperative residuals.  The LU is formed by one thread; every refinement pass applies
+// it by two warp scans (forward y_i = b_i - l_i y_(i-1), backward x_i = y_i/u_i -
+// (du_i/u_i) x_(i+1)).  fs: 5n floats of scratch.  Returns non-zero on a zero pivot.
 __device__ int tri_solve(int n, const double* dl, const double* d, const double* du, const double* b, double* x,
-                         float* fs, int* ip) {
-    float* __restrict__ fl = fs;
-    float* __restrict__ fd = fs + n;
-    float* __restrict__ fu = fs + 2 * n;
-    float* __restrict__ fu2 = fs + 3 * n;
-    float* __restrict__ fy = fs + 4 * n;
+                         float* fs, int*) {
+    float* __restrict__ fa = fs;           // forward coefficients -l_i (fa_0 = 0); first the FP32 d
+    float* __restrict__ fr = fs + n;       // 1/u_i
+    float* __restrict__ fb = fs + 2 * n;   // backward coefficients -du_i/u_i (fb_(n-1) = 0); first dl
+    float* __restrict__ fu = fs + 3 * n;   // du (FP32)
+    float* __restrict__ fy = fs + 4 * n;   // right-hand side / correction
     __shared__ int info_s;
     __shared__ double rbuf[16];
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        fd[i] = __double2float_rn(d[i]);
-        if (i < n - 1) { fl[i] = __double2float_rn(dl[i]); fu[i] = __double2float_rn(du[i]); }
-        fu2[i] = 0.f;
+        fa[i] = __double2float_rn(d[i]);
+        fb[i] = (i < n - 1) ? __double2float_rn(dl[i]) : 0.f;
+        fu[i] = (i < n - 1) ? __double2float_rn(du[i]) : 0.f;
         fy[i] = __double2float_rn(b[i]);
     }
     __syncthreads();
     if (threadIdx.x == 0) {
         int info = 0;
-        for (int i = 0; i < n - 1; ++i) {
-            const float di = fd[i], li = fl[i];
-            if (fabsf(di) >= fabsf(li)) {
-                ip[i] = 0;
-                if (di != 0.f) {
-                    const float f = __fmul_rn(li, __frcp_rn(di));
-                    fl[i] = f;
-                    fd[i + 1] = __fmaf_rn(-f, fu[i], fd[i + 1]);
-                }
-            } else {
-                const float f = __fmul_rn(di, __frcp_rn(li));
-                fd[i] = li;
-                fl[i] = f;
-                const float t = fu[i];
-                fu[i] = fd[i + 1];
-                fd[i + 1] = __fmaf_rn(-f, fd[i + 1], t);
-                if (i < n - 2) { fu2[i] = fu[i + 1]; fu[i + 1] = -f * fu[i + 1]; }
-                ip[i] = 1;
-            }
+        float u = fa[0];
+        if (u == 0.f) info = 1;
+        float r = __frcp_rn(u);
+        fr[0] = r;
+        fa[0] = 0.f;
+        for (int i = 1; i < n && !info; ++i) {
+            const float l = __fmul_rn(fb[i - 1], r);
+            const float di = fa[i];
+            u = __fmaf_rn(-l, fu[i - 1], di);
+            if (u == 0.f) { info = i + 1; break; }
+            fb[i - 1] = -__fmul_rn(fu[i - 1], r);
+            r = __frcp_rn(u);
+            fr[i] = r;
+            fa[i] = -l;
         }
-        for (int i = 0; i < n; ++i) {
-            if (fd[i] == 0.f) { info = i + 1; break; }
-            fd[i] = __frcp_rn(fd[i]);
-        }
+        fb[n - 1] = 0.f;
         info_s = info;
     }
     __syncthreads();
@@ -292,32 +319,17 @@ __device__ int tri_solve(int n, const double* dl, const double* d, const double*
     for (int pass = 0;; ++pass) {
         if (pass > 0) {
             for (int i = threadIdx.x; i < n; i += blockDim.x) {
-                double r = fma(-d[i], x[i], b[i]);
-                if (i > 0) r = fma(-dl[i - 1], x[i - 1], r);
-                if (i < n - 1) r = fma(-du[i], x[i + 1], r);
-                fy[i] = __double2float_rn(r);
+                double rr = fma(-d[i], x[i], b[i]);
+                if (i > 0) rr = fma(-dl[i - 1], x[i - 1], rr);
+                if (i < n - 1) rr = fma(-du[i], x[i + 1], rr);
+                fy[i] = __double2float_rn(rr);
             }
             __syncthreads();
         }
-        if (threadIdx.x == 0) {
-            float bi = fy[0];
-            for (int i = 0; i < n - 1; ++i) {
-                const float bn = fy[i + 1];
-                if (ip[i] == 0) { fy[i] = bi; bi = __fmaf_rn(-fl[i], bi, bn); }
-                else { fy[i] = bn; bi = __fmaf_rn(-fl[i], bn, bi); }
-            }
-            float x1 = __fmul_rn(bi, fd[n - 1]);
-            fy[n - 1] = x1;
-            if (n > 1) {
-                float x0 = __fmul_rn(__fmaf_rn(-fu[n - 2], x1, fy[n - 2]), fd[n - 2]);
-                fy[n - 2] = x0;
-                for (int i = n - 3; i >= 0; --i) {
-                    const float xi = __fmul_rn(__fmaf_rn(-fu2[i], x1, __fmaf_rn(-fu[i], x0, fy[i])), fd[i]);
-                    fy[i] = xi;
-                    x1 = x0;
-                    x0 = xi;
-                }
-            }
+        if (threadIdx.x < 32) {
+            warp_affine_scan(fa, fy, fy, fr, n, false);  // y_i / u_i
+            __syncwarp();
+            warp_affine_scan(fb, fy, fy, nullptr, n, true);
         }
         __syncthreads();
         if (refine_step(x, fy, n, pass, cprev, rbuf) != 0) break;
