@@ -440,7 +440,7 @@ struct fsibe_ctx {
     cudaStream_t side = nullptr;  // the beam predictor runs here beside the fluid step
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     cudaStream_t side2 = nullptr;                     // the fluid step's scalar reductions run here
-    cudaEvent_t ev_ff = nullptr, ev_ffj = nullptr;
+    cudaEvent_t ev_ff = nullptr, ev_ffj = nullptr, ev_sb0 = nullptr, ev_sb = nullptr;
     bool pre_launched = false;    // the predictor of the current step is in flight
     struct AdjWork* adj = nullptr;  // adjoint buffers and checkpoints (allocated on first use)
     bool initialized = false, startup_done = false;
@@ -679,12 +679,19 @@ static int fluid_step_t(fsibe_ctx* c, int explicit_step) {
     SizeKernels<R>& KY = ky_of<R>(c);
     const int nblk = x_blocks<R>(c);
     StepArgs sa = step_args(c, explicit_step, nblk);
-    prof_begin(c, "step_begin");
-    k_step_begin<<<1, 256, 0, c->stream>>>(sa);
-    prof_end(c);
+    a.explicit_step = explicit_step;
+    // the step's scalars (dt, AB2 weights, mean flow, drag window, integrating factor) on the
+    // side stream beside nl_x, which reads none of them; the beam predictor follows them there
+    CK(c, cudaEventRecord(c->ev_sb0, c->stream));
+    CK(c, cudaStreamWaitEvent(c->side, c->ev_sb0, 0));
+    prof_begin(c, "step_begin", c->side);
+    k_step_begin<<<1, 256, 0, c->side>>>(sa);
+    prof_end(c, c->side);
+    CK(c, cudaEventRecord(c->ev_sb, c->side));
     c->launches++;
     if (c->P.iFLUSI == 1) { const int st = beam_predict(c); if (st) return st; }
     launch_xv<R>(c, KX.xv[c->xv_nl].nl_x, KX.xv[c->xv_nl], 3, a, "nl_x");
+    CK(c, cudaStreamWaitEvent(c->stream, c->ev_sb, 0));
     launch_y<R>(c, KY.nl_y, KY.y_smem_nl, a, "nl_y");
     launch_xv<R>(c, KX.xv[c->xv_px].press_x, KX.xv[c->xv_px], 3, a, "press_x");
     // the energies, drag and unsteady forces from press_x's partial sums feed only scalars read
@@ -1073,6 +1080,8 @@ int fsibe_destroy(fsibe_ctx* c) {
     if (c->side2) { cudaStreamSynchronize(c->side2); cudaStreamDestroy(c->side2); }
     if (c->ev_ff) cudaEventDestroy(c->ev_ff);
     if (c->ev_ffj) cudaEventDestroy(c->ev_ffj);
+    if (c->ev_sb0) cudaEventDestroy(c->ev_sb0);
+    if (c->ev_sb) cudaEventDestroy(c->ev_sb);
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return FSIBE_OK;
@@ -1220,6 +1229,8 @@ int fsibe_create(const fsibe_params* p, fsibe_ctx** out) {
     if (e != cudaSuccess) { g_err = cudaGetErrorString(e); fsibe_destroy(c); return FSIBE_ERR_CUDA; }
     cudaEventCreateWithFlags(&c->ev_ff, cudaEventDisableTiming);
     cudaEventCreateWithFlags(&c->ev_ffj, cudaEventDisableTiming);
+    cudaEventCreateWithFlags(&c->ev_sb0, cudaEventDisableTiming);
+    cudaEventCreateWithFlags(&c->ev_sb, cudaEventDisableTiming);
     {
         const int st = c->fp32 ? autotune_x<float>(c) : autotune_x<double>(c);
         if (st) { g_err = c->err; fsibe_destroy(c); return st; }

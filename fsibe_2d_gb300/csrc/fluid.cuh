@@ -40,6 +40,7 @@ struct KArgs {
     const int* dcut;      // 2/3-rule: modes with |ky| >= dcut[kx] are removed (dealiase_mask.f90:9-26)
     int kcut;             // rows kx >= kcut hold no dealiased mode (dcut = 0): exact zeros after the update
     int viscous, pressure_on, penalize, op;
+    int explicit_step;    // 1 on the Euler start-up step (the host's flag: nl_x runs beside k_step_begin)
     size_t bstride;       // generic transforms over several fields at once: blockIdx.y selects the
                           // field, bstride complex values (= nx ny / 2) apart in every buffer
 };
@@ -325,7 +326,7 @@ __global__ void __launch_bounds__(XRows<R, H, TRV>::THREADS) k_nl_x(KArgs<R> a) 
     C2<R>* rb = bufB + r * X::PL;
     C2<R>* rc = bufC + r * X::PL;
     // after the first AB2/Euler update the vorticity is dealiased: rows kx >= kcut are zero
-    const int kin = a.S->explicit_step ? H : a.kcut;
+    const int kin = a.explicit_step ? H : a.kcut;
     load_tileT<R, H, X::TR, X::PL>(bufA, a.Tdx, ny, iy0, kin);
     load_tileT<R, H, X::TR, X::PL>(bufB, a.Tdy, ny, iy0, kin);
     __syncthreads();
