@@ -30,6 +30,7 @@ size_t beam_ws_doubles(int ns);
 void launch_mask_prep(const MaskArgs& a, double gerf, cudaStream_t st);
 void launch_mask(const MaskArgs& a, double gerf, bool fp32, cudaStream_t st);
 void launch_forces(const ForceArgs& a, double dxi, double dyi, cudaStream_t st);
+void launch_forces_geo(const ForceArgs& a, double dxi, double dyi, cudaStream_t st);
 void launch_beam(const BeamArgs& b, cudaStream_t st);
 void launch_beam_pre(const BeamArgs& b, cudaStream_t st);
 int beam_pre_smem_setup(int ns);
@@ -436,6 +437,9 @@ struct fsibe_ctx {
     float* minv = nullptr;  // cluster form: rows of the preconditioner inverse, kept between steps
     int* minv_rse = nullptr;
     double* d1d = nullptr;  // Differentiate1D table of the beam (4 x 3 x 8)
+    double* fgeo = nullptr;  // interpolation geometry of the forces, 76 doubles a node
+    int* fgij = nullptr;     // its cells, 8 ints a node
+    cudaEvent_t ev_geo = nullptr;
     double* pred = nullptr; // predictor output
     cudaStream_t side = nullptr;  // the beam predictor runs here beside the fluid step
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
@@ -753,7 +757,7 @@ static int create_mask(fsibe_ctx* c) {
     return FSIBE_OK;
 }
 
-static int get_forces(fsibe_ctx* c) {
+static ForceArgs force_args(fsibe_ctx* c, double& dxi, double& dyi) {
     ForceArgs f;
     std::memset(&f, 0, sizeof(f));
     f.S = c->S;
@@ -767,11 +771,32 @@ static int get_forces(fsibe_ctx* c) {
     f.counter = c->counter;
     f.fterm = c->fterm;
     f.fp32 = c->fp32 ? 1 : 0;
-    const double dxi = (c->P.xl - c->g.dx) / (double)(c->P.nx - 1);
-    const double dyi = (c->P.yl - c->g.dy) / (double)(c->P.ny - 1);
+    dxi = (c->P.xl - c->g.dx) / (double)(c->P.nx - 1);
+    dyi = (c->P.yl - c->g.dy) / (double)(c->P.ny - 1);
+    f.geo = c->fgeo;
+    f.gij = c->fgij;
     f.alpha = f.angle_deg * f.pi / 180.0;
     f.rdxi = 1.0 / dxi;
     f.rdyi = 1.0 / dyi;
+    return f;
+}
+
+// The interpolation geometry of the forces (k_forces_geo), from the beam state alone.
+static void forces_geo(fsibe_ctx* c, cudaStream_t st) {
+    double dxi, dyi;
+    const ForceArgs f = force_args(c, dxi, dyi);
+    prof_begin(c, "forces_geo", st);
+    launch_forces_geo(f, dxi, dyi, st);
+    prof_end(c, st);
+    c->launches++;
+}
+
+// GetForces; geo_done: the step already formed the geometry beside the fluid kernels (ev_geo).
+static int get_forces(fsibe_ctx* c, bool geo_done = false) {
+    double dxi, dyi;
+    const ForceArgs f = force_args(c, dxi, dyi);
+    if (geo_done) CK(c, cudaStreamWaitEvent(c->stream, c->ev_geo, 0));
+    else forces_geo(c, c->stream);
     prof_begin(c, "forces");
     launch_forces(f, dxi, dyi, c->stream);
     prof_end(c);
@@ -830,9 +855,18 @@ static int step_body(fsibe_ctx* c, int explicit_step) {
     const fsibe_params& P = c->P;
     int st;
     if (P.iFLUSI == 1 || P.iMotion > 0) { st = create_mask(c); if (st) return st; }
+    const bool forces = P.iFLUSI == 1 || P.iSaveBeam > 0;
+    if (forces) {
+        // the forces' interpolation geometry needs only the beam state: it is formed on the
+        // second side stream beside the fluid step
+        CK(c, cudaEventRecord(c->ev_geo, c->stream));
+        CK(c, cudaStreamWaitEvent(c->side2, c->ev_geo, 0));
+        forces_geo(c, c->side2);
+        CK(c, cudaEventRecord(c->ev_geo, c->side2));
+    }
     st = fluid_step(c, explicit_step);
     if (st) return st;
-    if (P.iFLUSI == 1 || P.iSaveBeam > 0) { st = get_forces(c); if (st) return st; }
+    if (forces) { st = get_forces(c, true); if (st) return st; }
     bool advanced = false;
     if (P.iFLUSI == 1) { st = solid_step(c, true, &advanced); if (st) return st; }
     return advanced ? FSIBE_OK : advance(c);
@@ -1068,7 +1102,7 @@ int fsibe_destroy(fsibe_ctx* c) {
     for (void* p : c->phys) if (p) cudaFree(p);
     for (void* p : c->spec) if (p) cudaFree(p);
     for (double* p : c->beam) if (p) cudaFree(p);
-    void* others[] = {c->twX, c->twR, c->twY, c->S, c->red, c->oo, c->ws, c->pred, c->minv, c->minv_rse, c->d1d, c->prims, c->nprims,
+    void* others[] = {c->twX, c->twR, c->twY, c->S, c->red, c->oo, c->ws, c->pred, c->minv, c->minv_rse, c->d1d, c->fgeo, c->fgij, c->prims, c->nprims,
                       c->rect, c->counter, c->fterm, c->rows, c->dscratch, c->dscratch2, c->etab, c->etabf, c->dcut};
     for (void* p : others) if (p) cudaFree(p);
     for (cudaEvent_t e : c->pool) cudaEventDestroy(e);
@@ -1081,6 +1115,7 @@ int fsibe_destroy(fsibe_ctx* c) {
     if (c->ev_ff) cudaEventDestroy(c->ev_ff);
     if (c->ev_ffj) cudaEventDestroy(c->ev_ffj);
     if (c->ev_sb0) cudaEventDestroy(c->ev_sb0);
+    if (c->ev_geo) cudaEventDestroy(c->ev_geo);
     if (c->ev_sb) cudaEventDestroy(c->ev_sb);
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
     delete c;
@@ -1140,6 +1175,8 @@ int fsibe_create(const fsibe_params* p, fsibe_ctx** out) {
     ALLOC(c->ws, 8 * beam_ws_doubles(ns));
     ALLOC(c->pred, 8 * beam_pred_doubles(ns));
     ALLOC(c->d1d, 8 * 96);
+    ALLOC(c->fgeo, 8 * 76 * (size_t)ns);
+    ALLOC(c->fgij, 4 * 8 * (size_t)ns);
     {
         double tab[96];
         beam_d1d_table(c->g.ds, tab);
@@ -1230,6 +1267,7 @@ int fsibe_create(const fsibe_params* p, fsibe_ctx** out) {
     cudaEventCreateWithFlags(&c->ev_ff, cudaEventDisableTiming);
     cudaEventCreateWithFlags(&c->ev_ffj, cudaEventDisableTiming);
     cudaEventCreateWithFlags(&c->ev_sb0, cudaEventDisableTiming);
+    cudaEventCreateWithFlags(&c->ev_geo, cudaEventDisableTiming);
     cudaEventCreateWithFlags(&c->ev_sb, cudaEventDisableTiming);
     {
         const int st = c->fp32 ? autotune_x<float>(c) : autotune_x<double>(c);
@@ -1614,7 +1652,7 @@ int fsibe_launches_per_step(fsibe_ctx* c, int* n) {
     if (!c || !n) return FSIBE_ERR_PARAM;
     const fsibe_params& P = c->P;
     int k = 6;  // step_begin, nl_x, nl_y, press_x, fluid_finish, advance
-    if (P.iFLUSI == 1 || P.iSaveBeam > 0) k += 2 + 1;  // press_y, press_fin, forces
+    if (P.iFLUSI == 1 || P.iSaveBeam > 0) k += 2 + 2;  // press_y, press_fin, forces geometry, forces
     if ((P.iFLUSI == 1 || P.iMotion > 0) && P.iBeam > 0) k += 2;  // mask prep + raster
     if (P.iFLUSI == 1) k += 2;  // beam predictor + beam
     if (P.iFLUSI == 1 && c->beam_cl) k -= 1;  // the cluster beam kernel ends the step itself

@@ -534,14 +534,16 @@ __device__ __forceinline__ double fld(const void* f, int fp32, size_t k) {
 // 9 x 9 interpolation sums run as 54 nine-term partial sums; the force integral of all nodes
 // is a block reduction in the last block.  Summation orders differ from the reference's
 // sequential loops (relative differences of a few ulps).
-__global__ void __launch_bounds__(128) k_forces(ForceArgs a, double dxi, double dyi) {
+// The geometry of the interpolation at node n (BeamForces.f90:105-124): the trigonometric
+// values, the four surface points' cells and their phi4* weights.  It depends only on the beam
+// state, so the step computes it beside the fluid kernels; k_forces then reads it.
+// Per node in a.geo: trig[4], dl[4][18]; in a.gij: ij[4][2].
+__global__ void __launch_bounds__(128) k_forces_geo(ForceArgs a, double dxi, double dyi) {
     const int n = blockIdx.x;
     __shared__ double dl[4][18];
     __shared__ int ij[4][2];
-    __shared__ double part[6][9];
     __shared__ double trig[4];  // sin, cos of theta + alpha and of twice it
     __shared__ double px[4], py[4];
-    __shared__ int last;
     // the two sincos on two warps (SMSPs)
     if (threadIdx.x == 0 || threadIdx.x == 32) {
         const double thn = a.th[n] + a.alpha;
@@ -582,6 +584,26 @@ __global__ void __launch_bounds__(128) k_forces(ForceArgs a, double dxi, double 
             const double yl_ = (double)(ij[p][1] - 4 + d - 9) * dyi + 0.0;
             dl[p][d] = delta_phi4star(fabs(yl_ - py[p]), dyi, a.rdyi, a.pi);
         }
+    }
+    __syncthreads();
+    double* g = a.geo + (size_t)n * 76;
+    if (threadIdx.x < 4) g[threadIdx.x] = trig[threadIdx.x];
+    if (threadIdx.x < 72) g[4 + threadIdx.x] = dl[threadIdx.x / 18][threadIdx.x % 18];
+    if (threadIdx.x < 8) a.gij[(size_t)n * 8 + threadIdx.x] = ij[threadIdx.x / 2][threadIdx.x % 2];
+}
+
+__global__ void __launch_bounds__(128) k_forces(ForceArgs a, double dxi, double dyi) {
+    const int n = blockIdx.x;
+    __shared__ double dl[4][18];
+    __shared__ int ij[4][2];
+    __shared__ double part[6][9];
+    __shared__ double trig[4];  // sin, cos of theta + alpha and of twice it
+    __shared__ int last;
+    {
+        const double* g = a.geo + (size_t)n * 76;
+        if (threadIdx.x < 4) trig[threadIdx.x] = g[threadIdx.x];
+        if (threadIdx.x < 72) dl[threadIdx.x / 18][threadIdx.x % 18] = g[4 + threadIdx.x];
+        if (threadIdx.x < 8) ij[threadIdx.x / 2][threadIdx.x % 2] = a.gij[(size_t)n * 8 + threadIdx.x];
     }
     __syncthreads();
     if (threadIdx.x < 54) {
@@ -675,6 +697,9 @@ void launch_mask(const MaskArgs& a, double gerf, bool fp32, cudaStream_t st) {
     else k_mask_raster<double><<<blocks, 32 * MASK_WARPS, 0, st>>>(a, gerf);
 }
 
+void launch_forces_geo(const ForceArgs& a, double dxi, double dyi, cudaStream_t st) {
+    k_forces_geo<<<a.ns, 128, 0, st>>>(a, dxi, dyi);
+}
 void launch_forces(const ForceArgs& a, double dxi, double dyi, cudaStream_t st) {
     k_forces<<<a.ns, 128, 0, st>>>(a, dxi, dyi);
 }

@@ -32,6 +32,8 @@ struct ForceArgs {
     int nx, ny, ns, viscous;
     double xl, yl, dx, dy, ds, t_beam, N_smooth, pi, angle_deg, t_release, tau;
     double alpha, rdxi, rdyi;  // angle_deg pi / 180, RN(1/dxi), RN(1/dyi) (host)
+    double* geo;     // per node: trig[4], phi4* weights dl[4][18] (k_forces_geo)
+    int* gij;        // per node: the four surface points' cells ij[4][2]
     const double *x, *y, *th;
     const void *press, *sa, *sb;   // R*[ny][nx]
     double *p_new, *tau_new;
