@@ -218,7 +218,9 @@ __global__ void __launch_bounds__(256, 1) k_beam_cl(BeamArgs b) {
     w.old_rhs = old_rhs; w.taun_s = taun_s; w.dtab = &dtab; w.Uf = Uf; w.Lf = Lf; w.rse = rse;
 
     long long ph_t = clock64(), ph[24] = {};
-    cl_sync();  // every CTA of the cluster runs before the first DSMEM access
+    // the cluster barrier that guarantees every CTA runs before the first DSMEM access comes
+    // just before that access (cl_up), so the set-up overlaps the CTAs' start
+    bool cl_up = false;
     d1d_load(&dtab, b.d1d);
     const double time = S->time, dt = S->dt1, grav = S->grav;
     const double ds = b.ds, mue = b.mue, eta = b.eta;
@@ -269,9 +271,9 @@ __global__ void __launch_bounds__(256, 1) k_beam_cl(BeamArgs b) {
             cs.K1 = mue * (0.0 * b.cos_a + 0.0 * b.sin_a + grav * b.sin_a) - b.tau_new[0];
             cs.K2 = b.p_new[0] + mue * (0.0 * b.cos_a - 0.0 * b.sin_a + grav * b.cos_a);
         }
-        if (have_inv) cp_async_wait_all();
         __syncthreads();
         const NewtonCtx& c = cs;
+        bool inv_pending = have_inv;  // the stored inverse rows are still arriving (cp.async)
         bool need_factor = !have_inv, factored = false;
         // own rows: generic ones [glo, ghi); the boundary equations (rows 0..3: k = 1, 2, 3, 7;
         // rows 2ns..2ns+3: k = 8, 6, 5, 4) sit in the first and last CTA and take warps 4..7,
@@ -319,6 +321,11 @@ __global__ void __launch_bounds__(256, 1) k_beam_cl(BeamArgs b) {
             }
             __syncthreads();
             PH(4);
+            if (inv_pending) {
+                cp_async_wait_all();
+                inv_pending = false;
+            }
+            if (!cl_up) { cl_sync(); cl_up = true; }
             int solves = 0;
             for (int attempt = 0; attempt < 2; ++attempt) {
                 const bool fresh = need_factor;
@@ -586,6 +593,7 @@ __global__ void __launch_bounds__(256, 1) k_beam_cl(BeamArgs b) {
     // saving, start 96 (n + 16) > 80 L bytes in.  The third sum subtracts: its terms are
     // stored negated and added (s - a and s + (-a) round the same).
     double* pcs = reinterpret_cast<double*>(cl_smem + Y.fact);
+    if (!cl_up) { cl_sync(); cl_up = true; }
     {
         const int q0 = (int)(((long long)rank * ns) / R), q1 = (int)(((long long)(rank + 1) * ns) / R);
         double* dst = cl_map(pcs, 0u);

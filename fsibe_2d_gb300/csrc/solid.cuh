@@ -52,7 +52,8 @@ struct AdvArgs {
     double* rows;
 };
 
-__device__ __forceinline__ void advance_state(const AdvArgs& a) {
+// tip: x, y, vx, vy, theta, theta_dot of the last node when the caller has them (else read).
+__device__ __forceinline__ void advance_state(const AdvArgs& a, const double* tip = nullptr) {
     for (int i = threadIdx.x; i < a.ns; i += blockDim.x) {
         a.p_old[i] = a.p_new[i];
         a.tau_old[i] = a.tau_new[i];
@@ -62,8 +63,10 @@ __device__ __forceinline__ void advance_state(const AdvArgs& a) {
         const int ns = a.ns;
         S->time = S->time + S->dt1;
         S->step += 1;
-        const double row[21] = {S->time, a.p_new[ns - 1], a.p_new[3 * ns / 4], a.p_new[ns / 2], a.x[ns - 1], a.y[ns - 1],
-                                a.vx[ns - 1], a.vy[ns - 1], a.th[ns - 1], a.thd[ns - 1], S->force[0], S->force[1],
+        const double t0 = tip ? tip[0] : a.x[ns - 1], t1 = tip ? tip[1] : a.y[ns - 1], t2 = tip ? tip[2] : a.vx[ns - 1],
+                     t3 = tip ? tip[3] : a.vy[ns - 1], t4 = tip ? tip[4] : a.th[ns - 1], t5 = tip ? tip[5] : a.thd[ns - 1];
+        const double row[21] = {S->time, a.p_new[ns - 1], a.p_new[3 * ns / 4], a.p_new[ns / 2], t0, t1,
+                                t2, t3, t4, t5, S->force[0], S->force[1],
                                 S->force_unst[0], S->force_unst[1], S->force_press[0], S->force_press[1],
                                 S->inertial_force[0], S->inertial_force[1], S->e_kinetic, S->e_elastic, S->e_pot};
         for (int c = 0; c < 21; ++c) S->row[c] = row[c];
