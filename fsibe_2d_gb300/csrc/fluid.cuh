@@ -46,8 +46,19 @@ struct KArgs {
 };
 
 template <typename R> constexpr bool kIsF32 = std::is_same<R, float>::value;
-// shared-memory row buffers of k_nl_y: four inverse transforms at a time in FP32, two in FP64
-template <typename R> constexpr int nl_y_bufs() { return kIsF32<R> ? 4 : 2; }
+// shared-memory row buffers of k_nl_y: four inverse transforms at a time in FP32 (and a fifth
+// buffer for the prefetched state), two in FP64
+template <typename R> constexpr int nl_y_bufs() { return kIsF32<R> ? 5 : 2; }
+
+// 16-byte asynchronous global -> shared copies (the copy engine fills shared memory while the
+// threads compute); completed by cp_async_wait before use
+__device__ __forceinline__ void cp_async16_f(void* s, const void* g) {
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(s);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(sa), "l"(g) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_f() {
+    asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
+}
 
 // Error-free transformations for the compensated (hi + lo) vorticity state of the FP32 form.
 __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
@@ -406,6 +417,18 @@ __global__ void __launch_bounds__(NY / 8, kIsF32<R> ? 4 : 1) k_nl_y(KArgs<R> a) 
         }
         return;
     }
+    // FP32 form: the row's state (W, Wlo, M) flows into the spare buffers C, D, E while the
+    // forward transforms run (unpadded rows of NY complex values)
+    C2<R>* preW = bufA + 2 * padded_len(NY);
+    C2<R>* preWl = bufA + 3 * padded_len(NY);
+    C2<R>* preM = bufA + 4 * padded_len(NY);
+    if constexpr (kIsF32<R>) {
+        for (int e = t; e < NY / 2; e += G) {  // 16 bytes = two complex values per copy
+            cp_async16_f(preW + 2 * e, a.W + row + 2 * e);
+            cp_async16_f(preWl + 2 * e, a.Wlo + row + 2 * e);
+            cp_async16_f(preM + 2 * e, a.M + row + 2 * e);
+        }
+    }
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
         bufA[pad8(t + q * G)] = a.A[row + t + q * G];
@@ -413,6 +436,10 @@ __global__ void __launch_bounds__(NY / 8, kIsF32<R> ? 4 : 1) k_nl_y(KArgs<R> a) 
     }
     __syncthreads();
     block_fft_m<R, NY, false, 2>(bufA, padded_len(NY), a.twY, t);  // bufA and bufB together
+    if constexpr (kIsF32<R>) {
+        cp_async_wait_f();
+        __syncthreads();
+    }
     const DevScalars* S = a.S;
     const double dt1 = S->dt1, b10 = S->b10, b11 = S->b11;
     const bool expl = S->explicit_step != 0;
@@ -436,13 +463,13 @@ __global__ void __launch_bounds__(NY / 8, kIsF32<R> ? 4 : 1) k_nl_y(KArgs<R> a) 
             const float2 ex = a.etabf[kx], ey = a.etabf[g.hx + ka];
             const float Eh = __fmul_rn(ex.x, ey.x);
             const float El = __fadd_rn(__fmaf_rn(ex.x, ey.x, -Eh), __fmaf_rn(ex.x, ey.y, __fmul_rn(ex.y, ey.x)));
-            const C2<R> Wo = a.W[row + ky], Wl = a.Wlo[row + ky];
+            const C2<R> Wo = preW[ky], Wl = preWl[ky];
             float dx_, dy_;
             if (expl) {
                 dx_ = (float)dt1 * N.x;
                 dy_ = (float)dt1 * N.y;
             } else {
-                const C2<R> Mo = a.M[row + ky];
+                const C2<R> Mo = preM[ky];
                 dx_ = fmaf((float)b10, N.x, (float)b11 * Mo.x);
                 dy_ = fmaf((float)b10, N.y, (float)b11 * Mo.y);
             }
@@ -476,7 +503,7 @@ __global__ void __launch_bounds__(NY / 8, kIsF32<R> ? 4 : 1) k_nl_y(KArgs<R> a) 
     }
     // inverse-y outputs, NBO at a time: their transforms share the stages' synchronisations
     // and twiddle loads (NBO buffers of shared memory)
-    constexpr int NBO = nl_y_bufs<R>();
+    constexpr int NBO = kIsF32<R> ? 4 : 2;  // inverse transforms at a time (the fifth FP32 buffer holds the prefetched state)
     constexpr int PLY = padded_len(NY);
     const R kxs = (R)kx * (R)g.kxs;
     const int nout = a.viscous ? 7 : 5;
@@ -783,18 +810,22 @@ __global__ void __launch_bounds__(XRows<R, H, TRV>::THREADS) k_press_fin(KArgs<R
     const int r = threadIdx.x / X::G, t = threadIdx.x % X::G;
     const int iy0 = blockIdx.x * X::TR, ny = a.g.ny;
     C2<R>* rb = buf + r * X::PL;
-    load_tileT<R, H, X::TR, X::PL>(buf, a.Tq, ny, iy0);
-    __syncthreads();
-    row_c2r<R, H>(rb, a.twR, a.twX, t);
     const size_t roff = (size_t)(iy0 + r) * H;
     const C2<R>* u2 = reinterpret_cast<const C2<R>*>(a.u) + roff;
     const C2<R>* v2 = reinterpret_cast<const C2<R>*>(a.v) + roff;
     C2<R>* p2 = reinterpret_cast<C2<R>*>(a.press) + roff;
+    // the velocity loads are issued before the transform, which hides their latency
+    C2<R> ul[8], vl[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) { ul[q] = u2[t + q * X::G]; vl[q] = v2[t + q * X::G]; }
+    load_tileT<R, H, X::TR, X::PL>(buf, a.Tq, ny, iy0);
+    __syncthreads();
+    row_c2r<R, H>(rb, a.twR, a.twX, t);
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
         const int m = t + q * X::G;
         const C2<R> qq = rb[pad8(m)];
-        C2<R> uu = u2[m], vq = v2[m];
+        C2<R> uu = ul[q], vq = vl[q];
         if constexpr (kIsF32<R>) {
             // the velocity press_x stored holds the mean flow at time + dt1 (mean_u_next; the
             // fluid step's last scalar kernel copies it to mean_u_cur, beside this kernel)
