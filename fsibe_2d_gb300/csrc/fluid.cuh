@@ -576,7 +576,9 @@ __global__ void __launch_bounds__(XRows<R, H, TRV>::THREADS, (sizeof(R) == 4) ? 
     constexpr int BS = X::TR * X::PL;  // one row buffer (TR rows)
     C2<R>* bufB = bufA + BS;
     C2<R>* bufC = bufB + BS;
-    __shared__ double red_s[RED_NSLOTS][X::THREADS / 32];
+    __shared__ double red_s[RED_NSLOTS][X::THREADS / 32 > 2 ? X::THREADS / 32 : 2];
+    static_assert((kIsF32<R> ? (RED_NSLOTS + 1) * 4 : RED_NSLOTS * 8) * X::THREADS <= X::TR * X::PL * (int)sizeof(C2<R>),
+                  "the reduction columns fit the spare row buffer");
     const int r = threadIdx.x / X::G, t = threadIdx.x % X::G;
     const int iy0 = blockIdx.x * X::TR, ny = a.g.ny;
     C2<R>* ra = bufA + r * X::PL;
@@ -670,9 +672,12 @@ __global__ void __launch_bounds__(XRows<R, H, TRV>::THREADS, (sizeof(R) == 4) ? 
             ra[pad8(m)] = mk<R>(px[0], px[1]);
             rb[pad8(m)] = mk<R>(py[0], py[1]);
         }
+        // the FP32 partials go to the spare row buffer; the block reduces them in FP64 below
+        float* cols = reinterpret_cast<float*>(bufC);
 #pragma unroll
-        for (int s = 0; s < RED_NSLOTS; ++s) acc[s] = (double)f[s];
-        acc[RED_INFLOW_MEAN] = Ud * (double)spx + Vd * (double)spy;
+        for (int s = 0; s < RED_NSLOTS; ++s)
+            cols[s * X::THREADS + threadIdx.x] = (s == RED_INFLOW_MEAN) ? spx : f[s];
+        cols[RED_NSLOTS * X::THREADS + threadIdx.x] = spy;
     } else {
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
@@ -715,18 +720,39 @@ __global__ void __launch_bounds__(XRows<R, H, TRV>::THREADS, (sizeof(R) == 4) ? 
         rb[pad8(m)] = mk<R>(py[0], py[1]);
     }
     }
-    // block reduction (fixed order -> deterministic)
+    // block reduction in a fixed order: every thread's partials go to the spare row buffer as
+    // columns; one warp per column sums it in FP64 (its lanes over the column, then a shuffle
+    // tree), far fewer FP64 warp instructions than a shuffle tree per warp and column
     const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    constexpr int NW = X::THREADS / 32;
+    if constexpr (!kIsF32<R>) {
+        double* cols = reinterpret_cast<double*>(bufC);
 #pragma unroll
-    for (int s = 0; s < RED_NSLOTS; ++s) {
-        double v = (s == RED_UMAX2) ? warp_max(acc[s]) : warp_sum<R>(acc[s]);
-        if (l == 0) red_s[s][w] = v;
+        for (int s = 0; s < RED_NSLOTS; ++s) cols[s * X::THREADS + threadIdx.x] = acc[s];
+    }
+    __syncthreads();
+    constexpr int NCOL = kIsF32<R> ? RED_NSLOTS + 1 : RED_NSLOTS;  // FP32: spx and spy for INFLOW_MEAN
+    for (int cidx = w; cidx < NCOL; cidx += NW) {
+        const bool mx = cidx == RED_UMAX2;
+        double v = 0.0;
+        for (int i = l; i < X::THREADS; i += 32) {
+            double x;
+            if constexpr (kIsF32<R>) x = (double)reinterpret_cast<const float*>(bufC)[cidx * X::THREADS + i];
+            else x = reinterpret_cast<const double*>(bufC)[cidx * X::THREADS + i];
+            v = mx ? fmax(v, x) : v + x;
+        }
+        v = mx ? warp_max(v) : warp_sum<R>(v);
+        if (l == 0) {
+            if (cidx < RED_NSLOTS) red_s[cidx][0] = v;
+            else red_s[RED_INFLOW_MEAN][1] = v;  // FP32: the sum of spy (spx is in column INFLOW_MEAN)
+        }
     }
     __syncthreads();
     if (threadIdx.x < RED_NSLOTS) {
         const int s = threadIdx.x;
-        double v = 0.0;
-        for (int i = 0; i < X::THREADS / 32; ++i) v = (s == RED_UMAX2) ? fmax(v, red_s[s][i]) : v + red_s[s][i];
+        double v = red_s[s][0];
+        if constexpr (kIsF32<R>)
+            if (s == RED_INFLOW_MEAN) v = Ud * red_s[s][0] + Vd * red_s[s][1];
         a.red[(size_t)blockIdx.x * RED_NSLOTS + s] = v;
         if (blockIdx.x == 0 && s == 0) a.S->nred = (int)gridDim.x;
     }
