@@ -390,6 +390,7 @@ __global__ void __launch_bounds__(256, 1) k_beam_cl(BeamArgs b) {
                         yf[k] = __double2float_rn(acc * row_scale(rse[k]));
                     }
                     __syncthreads();
+                    PH(19);
                     // the own rows to every other CTA, 16 bytes a store (slices start on quads)
                     {
                         const int nq4 = (nr + 3) / 4;
@@ -400,6 +401,7 @@ __global__ void __launch_bounds__(256, 1) k_beam_cl(BeamArgs b) {
                         }
                     }
                     if (tid < (int)R) *cl_map(slots + 2 * R + rank, (unsigned)tid) = (unsigned long long)flag_s;
+                    PH(20);
                     cl_sync();
                     PH(16);
                     {
@@ -497,6 +499,7 @@ __global__ void __launch_bounds__(256, 1) k_beam_cl(BeamArgs b) {
                             *cl_map(p2, dst) = *p2;
                         }
                     }
+                    PH(21);
                     cl_sync();
                     PH(18);
                     ++solves;

@@ -197,9 +197,10 @@ int fsibe_kernel_times(fsibe_ctx* ctx, int nsteps, fsibe_kernel_time* out, int c
  * substitutions, [20] state carry, [21] back correction.  Parts of [7]: [22] set-up before
  * the Newton loop.  Parts of [4]: [23] Newton update and norms.  The cluster form of the
  * Newton kernel (fsibe_beam_cluster > 0) records, on its first CTA: [22] set-up, [4] F +
- * Jacobian, [5] row scaling, exchange, factorisation and inverse rows, [16] residuals and the
- * all-gather of the right-hand side, [17] inverse products and solution updates, [18] the
- * all-gather of the solution rows, [6] the refinement's decisions, [23] Newton update and
+ * Jacobian, [5] row scaling, exchange, factorisation and inverse rows, [19] residuals (with the
+ * previous pass's decision), [20] the push and [16] the barrier of the right-hand side's
+ * all-gather, [17] inverse products and solution updates, [21] the push and [18] the barrier
+ * of the solution rows' all-gather, [6] the refinement's decisions, [23] Newton update and
  * norms, [7] saving the inverse, [8] position sums, [9] positions, brake and energies, [10]
  * the solve count.  out32 receives 32 values; reset != 0 zeroes them after reading. */
 int fsibe_beam_phase_cycles(fsibe_ctx* ctx, long long* out32, int reset);
