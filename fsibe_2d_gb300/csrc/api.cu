@@ -440,6 +440,8 @@ struct fsibe_ctx {
     double* fgeo = nullptr;  // interpolation geometry of the forces, 76 doubles a node
     int* fgij = nullptr;     // its cells, 8 ints a node
     cudaEvent_t ev_geo = nullptr;
+    cudaEvent_t ev_adv = nullptr;  // the advection part of k_nl_x, run beside the mask kernels
+    bool nl_split = true;          // split k_nl_x in fsibe_step (FSIBE_NL_SPLIT=0: one launch)
     double* pred = nullptr; // predictor output
     cudaStream_t side = nullptr;  // the beam predictor runs here beside the fluid step
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
@@ -569,10 +571,11 @@ static void launch_y(fsibe_ctx* c, void (*k)(KArgs<R>), int smem, const KArgs<R>
 // a fused x kernel with one of its tile-height variants (nbuf row buffers of shared memory)
 template <typename R>
 static void launch_xv(fsibe_ctx* c, void (*k)(KArgs<R>), const typename SizeKernels<R>::XVariant& v, int nbuf,
-                      const KArgs<R>& a, const char* name) {
-    prof_begin(c, name);
-    k<<<c->g.ny / v.rows, v.threads, nbuf == 3 ? v.smem3 : v.smem1, c->stream>>>(a);
-    prof_end(c);
+                      const KArgs<R>& a, const char* name, cudaStream_t st = nullptr) {
+    if (!st) st = c->stream;
+    prof_begin(c, name, st);
+    k<<<c->g.ny / v.rows, v.threads, nbuf == 3 ? v.smem3 : nbuf * v.smem1, st>>>(a);
+    prof_end(c, st);
     c->launches++;
 }
 
@@ -675,9 +678,21 @@ static int beam_predict(fsibe_ctx* c) {
 template <typename R>
 static int x_blocks(fsibe_ctx* c) { return c->g.ny / kx_of<R>(c).x_rows; }
 
+// The advection part of cal_nlk (NavierStokes.f90:88-132 without the penalization) on the
+// second side stream, forked from the main stream at the start of the step: it reads the
+// state the previous step left (u, v, the vorticity's derivatives) and no mask, so it runs
+// beside the mask kernels.  fluid_step_t(adv_forked) joins it (ev_adv).
+template <typename R>
+static void nl_advect_t(fsibe_ctx* c, int explicit_step) {
+    KArgs<R> a = kargs<R>(c);
+    SizeKernels<R>& KX = kx_of<R>(c);
+    a.explicit_step = explicit_step;
+    launch_xv<R>(c, KX.xv[c->xv_nl].nl_adv, KX.xv[c->xv_nl], 2, a, "nl_adv", c->side2);
+}
+
 // EvolveFluidExplicit / EvolveFluidAB2 + pressure (NavierStokes.f90:422-508, 273-403)
 template <typename R>
-static int fluid_step_t(fsibe_ctx* c, int explicit_step) {
+static int fluid_step_t(fsibe_ctx* c, int explicit_step, bool adv_forked = false) {
     KArgs<R> a = kargs<R>(c);
     SizeKernels<R>& KX = kx_of<R>(c);
     SizeKernels<R>& KY = ky_of<R>(c);
@@ -694,7 +709,16 @@ static int fluid_step_t(fsibe_ctx* c, int explicit_step) {
     CK(c, cudaEventRecord(c->ev_sb, c->side));
     c->launches++;
     if (c->P.iFLUSI == 1) { const int st = beam_predict(c); if (st) return st; }
-    launch_xv<R>(c, KX.xv[c->xv_nl].nl_x, KX.xv[c->xv_nl], 3, a, "nl_x");
+    if (adv_forked) {
+        // the advection part ran beside the mask kernels: add the penalization on the rows
+        // of the mask's box
+        CK(c, cudaStreamWaitEvent(c->stream, c->ev_adv, 0));
+        KArgs<R> p = a;
+        p.rect = c->rect;
+        launch_xv<R>(c, KX.xv[c->xv_nl].nl_pen, KX.xv[c->xv_nl], 2, p, "nl_pen");
+    } else {
+        launch_xv<R>(c, KX.xv[c->xv_nl].nl_x, KX.xv[c->xv_nl], 3, a, "nl_x");
+    }
     CK(c, cudaStreamWaitEvent(c->stream, c->ev_sb, 0));
     launch_y<R>(c, KY.nl_y, KY.y_smem_nl, a, "nl_y");
     launch_xv<R>(c, KX.xv[c->xv_px].press_x, KX.xv[c->xv_px], 3, a, "press_x");
@@ -718,8 +742,8 @@ static int fluid_step_t(fsibe_ctx* c, int explicit_step) {
     return FSIBE_OK;
 }
 
-static int fluid_step(fsibe_ctx* c, int explicit_step) {
-    return c->fp32 ? fluid_step_t<float>(c, explicit_step) : fluid_step_t<double>(c, explicit_step);
+static int fluid_step(fsibe_ctx* c, int explicit_step, bool adv_forked = false) {
+    return c->fp32 ? fluid_step_t<float>(c, explicit_step, adv_forked) : fluid_step_t<double>(c, explicit_step, adv_forked);
 }
 
 static MaskArgs mask_args(fsibe_ctx* c) {
@@ -854,17 +878,27 @@ static int advance(fsibe_ctx* c) {
 static int step_body(fsibe_ctx* c, int explicit_step) {
     const fsibe_params& P = c->P;
     int st;
-    if (P.iFLUSI == 1 || P.iMotion > 0) { st = create_mask(c); if (st) return st; }
+    const bool mask = P.iFLUSI == 1 || P.iMotion > 0;
     const bool forces = P.iFLUSI == 1 || P.iSaveBeam > 0;
-    if (forces) {
-        // the forces' interpolation geometry needs only the beam state: it is formed on the
-        // second side stream beside the fluid step
+    // with a mask formed in the step, the advection part of the nonlinear term runs on the
+    // second side stream beside the mask kernels; the forces' interpolation geometry, which
+    // needs only the beam state, follows it there and runs beside the fluid step
+    const bool split = mask && P.iBeam > 0 && c->nl_split;
+    if (split || forces) {
         CK(c, cudaEventRecord(c->ev_geo, c->stream));
         CK(c, cudaStreamWaitEvent(c->side2, c->ev_geo, 0));
+    }
+    if (split) {
+        if (c->fp32) nl_advect_t<float>(c, explicit_step);
+        else nl_advect_t<double>(c, explicit_step);
+        CK(c, cudaEventRecord(c->ev_adv, c->side2));
+    }
+    if (forces) {
         forces_geo(c, c->side2);
         CK(c, cudaEventRecord(c->ev_geo, c->side2));
     }
-    st = fluid_step(c, explicit_step);
+    if (mask) { st = create_mask(c); if (st) return st; }
+    st = fluid_step(c, explicit_step, split);
     if (st) return st;
     if (forces) { st = get_forces(c, true); if (st) return st; }
     bool advanced = false;
@@ -1116,6 +1150,7 @@ int fsibe_destroy(fsibe_ctx* c) {
     if (c->ev_ffj) cudaEventDestroy(c->ev_ffj);
     if (c->ev_sb0) cudaEventDestroy(c->ev_sb0);
     if (c->ev_geo) cudaEventDestroy(c->ev_geo);
+    if (c->ev_adv) cudaEventDestroy(c->ev_adv);
     if (c->ev_sb) cudaEventDestroy(c->ev_sb);
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
     delete c;
@@ -1195,6 +1230,10 @@ int fsibe_create(const fsibe_params* p, fsibe_ctx** out) {
         }
     }
     c->beam_pre_smem = beam_pre_smem_setup(ns);
+    {
+        const char* e = std::getenv("FSIBE_NL_SPLIT");
+        c->nl_split = !(e && std::atoi(e) == 0);
+    }
     ALLOC(c->prims, sizeof(Prim) * (size_t)(2 * ns + 8));
     ALLOC(c->nprims, 16);
     ALLOC(c->rect, 64);
@@ -1268,6 +1307,7 @@ int fsibe_create(const fsibe_params* p, fsibe_ctx** out) {
     cudaEventCreateWithFlags(&c->ev_ffj, cudaEventDisableTiming);
     cudaEventCreateWithFlags(&c->ev_sb0, cudaEventDisableTiming);
     cudaEventCreateWithFlags(&c->ev_geo, cudaEventDisableTiming);
+    cudaEventCreateWithFlags(&c->ev_adv, cudaEventDisableTiming);
     cudaEventCreateWithFlags(&c->ev_sb, cudaEventDisableTiming);
     {
         const int st = c->fp32 ? autotune_x<float>(c) : autotune_x<double>(c);
@@ -1653,7 +1693,8 @@ int fsibe_launches_per_step(fsibe_ctx* c, int* n) {
     const fsibe_params& P = c->P;
     int k = 6;  // step_begin, nl_x, nl_y, press_x, fluid_finish, advance
     if (P.iFLUSI == 1 || P.iSaveBeam > 0) k += 2 + 2;  // press_y, press_fin, forces geometry, forces
-    if ((P.iFLUSI == 1 || P.iMotion > 0) && P.iBeam > 0) k += 2;  // mask prep + raster
+    // mask prep + raster, and nl_x split into its advection and penalization parts
+    if ((P.iFLUSI == 1 || P.iMotion > 0) && P.iBeam > 0) k += c->nl_split ? 3 : 2;
     if (P.iFLUSI == 1) k += 2;  // beam predictor + beam
     if (P.iFLUSI == 1 && c->beam_cl) k -= 1;  // the cluster beam kernel ends the step itself
     *n = k;

@@ -41,11 +41,17 @@ struct KArgs {
     int kcut;             // rows kx >= kcut hold no dealiased mode (dcut = 0): exact zeros after the update
     int viscous, pressure_on, penalize, op;
     int explicit_step;    // 1 on the Euler start-up step (the host's flag: nl_x runs beside k_step_begin)
+    const int* rect;      // the mask's box (rect[2..3]: its rows), written by k_mask_prep
     size_t bstride;       // generic transforms over several fields at once: blockIdx.y selects the
                           // field, bstride complex values (= nx ny / 2) apart in every buffer
 };
 
 template <typename R> constexpr bool kIsF32 = std::is_same<R, float>::value;
+
+// k_nl_x's parts.  The advection part needs no mask, so it can run beside the mask kernels;
+// the penalization part then adds the mask's term on the rows of the mask's box alone
+// (outside it the mask and the penalization are zero).
+enum { NL_WHOLE = 0, NL_ADVECT = 1, NL_PENAL = 2 };
 // shared-memory row buffers of k_nl_y: four inverse transforms at a time in FP32 (and a fifth
 // buffer for the prefetched state), two in FP64
 template <typename R> constexpr int nl_y_bufs() { return kIsF32<R> ? 5 : 2; }
@@ -323,7 +329,7 @@ __global__ void __launch_bounds__(XRows<R, H>::THREADS) k_vel_x(KArgs<R> a) {
 // ======================================================================================
 // K2: nonlinear term and penalization in physical space (cal_nlk)
 // ======================================================================================
-template <typename R, int H, int TRV>
+template <typename R, int H, int TRV, int PART = NL_WHOLE>
 __global__ void __launch_bounds__(XRows<R, H, TRV>::THREADS) k_nl_x(KArgs<R> a) {
     using X = XRows<R, H, TRV>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -333,15 +339,33 @@ __global__ void __launch_bounds__(XRows<R, H, TRV>::THREADS) k_nl_x(KArgs<R> a) 
     C2<R>* bufC = bufB + BS;
     const int r = threadIdx.x / X::G, t = threadIdx.x % X::G;
     const int iy0 = blockIdx.x * X::TR, ny = a.g.ny;
+    constexpr int part = PART;
+    // the penalization part: only the rows of the mask's box carry a non-zero term
+    if (part == NL_PENAL && (iy0 + X::TR - 1 < a.rect[2] || iy0 > a.rect[3])) return;
     C2<R>* ra = bufA + r * X::PL;
     C2<R>* rb = bufB + r * X::PL;
     C2<R>* rc = bufC + r * X::PL;
-    // after the first AB2/Euler update the vorticity is dealiased: rows kx >= kcut are zero
-    const int kin = a.explicit_step ? H : a.kcut;
-    load_tileT<R, H, X::TR, X::PL>(bufA, a.Tdx, ny, iy0, kin);
-    load_tileT<R, H, X::TR, X::PL>(bufB, a.Tdy, ny, iy0, kin);
-    __syncthreads();
-    row_c2r_m<R, H, 2>(ra, BS, a.twR, a.twX, t);  // ra and rb together
+    // the penalization part adds to the advection part's A: its values (kx < kcut <= H, at
+    // most H / G per thread) are loaded first, to arrive while the transforms run
+    static_assert(H % X::G == 0 && X::THREADS == X::TR * X::G, "one block: TR rows of G threads");
+    constexpr int NLA = H / X::G;
+    const int nout = a.kcut * X::TR;
+    C2<R> av[NLA];
+    if (part == NL_PENAL) {
+#pragma unroll
+        for (int u = 0; u < NLA; ++u) {
+            const int i = threadIdx.x + u * blockDim.x;
+            if (i < nout) av[u] = a.A[(size_t)(i / X::TR) * ny + iy0 + i % X::TR];
+        }
+    }
+    if (part != NL_PENAL) {
+        // after the first AB2/Euler update the vorticity is dealiased: rows kx >= kcut are zero
+        const int kin = a.explicit_step ? H : a.kcut;
+        load_tileT<R, H, X::TR, X::PL>(bufA, a.Tdx, ny, iy0, kin);
+        load_tileT<R, H, X::TR, X::PL>(bufB, a.Tdy, ny, iy0, kin);
+        __syncthreads();
+        row_c2r_m<R, H, 2>(ra, BS, a.twR, a.twX, t);  // ra and rb together
+    }
     const int iy = iy0 + r;
     const size_t roff = (size_t)iy * H;
     const C2<R>* u2 = reinterpret_cast<const C2<R>*>(a.u) + roff;
@@ -349,19 +373,22 @@ __global__ void __launch_bounds__(XRows<R, H, TRV>::THREADS) k_nl_x(KArgs<R> a) 
     const C2<R>* k2 = reinterpret_cast<const C2<R>*>(a.mask) + roff;
     const C2<R>* x2 = reinterpret_cast<const C2<R>*>(a.mvx) + roff;
     const C2<R>* y2 = reinterpret_cast<const C2<R>*>(a.mvy) + roff;
+    const bool adv = part != NL_PENAL, pen = part != NL_ADVECT && a.penalize;
     C2<R> wv[8], pyv[8], pxv[8];
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
         const int m = t + q * X::G;
-        const C2<R> dx = ra[pad8(m)], dy = rb[pad8(m)];
         C2<R> uu = u2[m], vv = v2[m];
         if constexpr (kIsF32<R>) {
             const R Uc = (R)a.S->mean_u_cur, Vc = (R)a.S->mean_v_cur;
             uu = mk<R>(uu.x + Uc, uu.y + Uc);
             vv = mk<R>(vv.x + Vc, vv.y + Vc);
         }
-        wv[q] = mk<R>(-uu.x * dx.x - vv.x * dy.x, -uu.y * dx.y - vv.y * dy.y);
-        if (a.penalize) {
+        if (adv) {
+            const C2<R> dx = ra[pad8(m)], dy = rb[pad8(m)];
+            wv[q] = mk<R>(-uu.x * dx.x - vv.x * dy.x, -uu.y * dx.y - vv.y * dy.y);
+        }
+        if (pen) {
             const C2<R> kk = k2[m], mx = x2[m], my = y2[m];
             pxv[q] = mk<R>(-kk.x * (uu.x - mx.x), -kk.y * (uu.y - mx.y));
             pyv[q] = mk<R>(-kk.x * (vv.x - my.x), -kk.y * (vv.y - my.y));
@@ -370,24 +397,63 @@ __global__ void __launch_bounds__(XRows<R, H, TRV>::THREADS) k_nl_x(KArgs<R> a) 
             pyv[q] = mk<R>(0, 0);
         }
     }
-    __syncthreads();
+    if (adv) __syncthreads();
+    if (part == NL_WHOLE) {
 #pragma unroll
-    for (int q = 0; q < 8; ++q) {
-        const int m = t + q * X::G;
-        ra[pad8(m)] = wv[q];
-        rb[pad8(m)] = pyv[q];
-        rc[pad8(m)] = pxv[q];
+        for (int q = 0; q < 8; ++q) {
+            const int m = t + q * X::G;
+            ra[pad8(m)] = wv[q];
+            rb[pad8(m)] = pyv[q];
+            rc[pad8(m)] = pxv[q];
+        }
+        __syncthreads();
+        row_r2c_m<R, H, 3>(ra, BS, a.twR, a.twX, t);  // ra, rb and rc together
+    } else if (part == NL_ADVECT) {
+#pragma unroll
+        for (int q = 0; q < 8; ++q) ra[pad8(t + q * X::G)] = wv[q];
+        __syncthreads();
+        row_r2c_m<R, H, 1>(ra, BS, a.twR, a.twX, t);
+    } else {
+        // the penalization's y and x components in the buffers A and B (the whole kernel's B
+        // and C)
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            const int m = t + q * X::G;
+            ra[pad8(m)] = pyv[q];
+            rb[pad8(m)] = pxv[q];
+        }
+        __syncthreads();
+        row_r2c_m<R, H, 2>(ra, BS, a.twR, a.twX, t);
     }
-    __syncthreads();
-    row_r2c_m<R, H, 3>(ra, BS, a.twR, a.twX, t);  // ra, rb and rc together
-    // the right-hand side only matters where the update keeps modes (kx < kcut)
-    for (int i = threadIdx.x; i < a.kcut * X::TR; i += blockDim.x) {
+    // the right-hand side only matters where the update keeps modes (kx < kcut):
+    // A = X(w) + i kx X(pen_y), B = X(pen_x); the advection part writes X(w) and a zero B,
+    // the penalization part adds its terms to that
+    if (part == NL_PENAL) {
+#pragma unroll
+        for (int u = 0; u < NLA; ++u) {
+            const int i = threadIdx.x + u * blockDim.x;
+            if (i < nout) {
+                const int rr = i % X::TR, kx = i / X::TR;
+                const size_t o = (size_t)kx * ny + iy0 + rr;
+                const R kxs = (R)((double)kx * a.g.kxs);
+                a.A[o] = cadd<R>(av[u], cimul<R>(bufA[rr * X::PL + pad8(kx)], kxs));
+                a.B[o] = bufB[rr * X::PL + pad8(kx)];
+            }
+        }
+        return;
+    }
+    for (int i = threadIdx.x; i < nout; i += blockDim.x) {
         const int rr = i % X::TR, kx = i / X::TR;
-        const C2<R> xa = bufA[rr * X::PL + pad8(kx)], xb = bufB[rr * X::PL + pad8(kx)];
-        const R kxs = (R)((double)kx * a.g.kxs);
         const size_t o = (size_t)kx * ny + iy0 + rr;
-        a.A[o] = cadd<R>(xa, cimul<R>(xb, kxs));
-        a.B[o] = bufC[rr * X::PL + pad8(kx)];
+        const C2<R> xa = bufA[rr * X::PL + pad8(kx)];
+        if (part == NL_WHOLE) {
+            const R kxs = (R)((double)kx * a.g.kxs);
+            a.A[o] = cadd<R>(xa, cimul<R>(bufB[rr * X::PL + pad8(kx)], kxs));
+            a.B[o] = bufC[rr * X::PL + pad8(kx)];
+        } else {
+            a.A[o] = xa;
+            a.B[o] = mk<R>(0, 0);
+        }
     }
 }
 
@@ -880,6 +946,8 @@ struct SizeKernels {
     struct XVariant {
         int rows, threads, smem1, smem3;  // smem3: the three row buffers of nl_x / press_x
         void (*nl_x)(KArgs<R>);
+        void (*nl_adv)(KArgs<R>);  // k_nl_x's advection and penalization parts (two buffers)
+        void (*nl_pen)(KArgs<R>);
         void (*press_x)(KArgs<R>);
         void (*press_fin)(KArgs<R>);
     } xv[3];
@@ -899,6 +967,10 @@ inline void fill_xvariant(typename SizeKernels<R>::XVariant& v) {
     v.smem1 = (int)(TR * X::PL * sizeof(C2<R>));
     v.smem3 = 3 * v.smem1;
     v.nl_x = k_nl_x<R, H, TR>;
+    v.nl_adv = k_nl_x<R, H, TR, NL_ADVECT>;
+    v.nl_pen = k_nl_x<R, H, TR, NL_PENAL>;
+    cudaFuncSetAttribute(k_nl_x<R, H, TR, NL_ADVECT>, cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * v.smem1);
+    cudaFuncSetAttribute(k_nl_x<R, H, TR, NL_PENAL>, cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * v.smem1);
     v.press_x = k_press_x<R, H, TR>;
     v.press_fin = k_press_fin<R, H, TR>;
     cudaFuncSetAttribute(k_nl_x<R, H, TR>, cudaFuncAttributeMaxDynamicSharedMemorySize, v.smem3);
