@@ -217,7 +217,7 @@ __global__ void __launch_bounds__(256, 1) k_beam_cl(BeamArgs b) {
     w.x = x; w.tdn = tdn; w.bo5 = bo5; w.bo6 = bo6; w.oo5 = oo5; w.oo6 = oo6;
     w.old_rhs = old_rhs; w.taun_s = taun_s; w.dtab = &dtab; w.Uf = Uf; w.Lf = Lf; w.rse = rse;
 
-    long long ph_t = clock64(), ph[24] = {};
+    long long ph_t = clock64(), ph[26] = {};
     // the cluster barrier that guarantees every CTA runs before the first DSMEM access comes
     // just before that access (cl_up), so the set-up overlaps the CTAs' start
     bool cl_up = false;
@@ -514,7 +514,8 @@ __global__ void __launch_bounds__(256, 1) k_beam_cl(BeamArgs b) {
                         const float cpf = (pass == 0) ? 0.f : cprev_s;
                         const double cmd = (double)__uint_as_float((unsigned)c2), cpd = (double)cpf;
                         const double xmd = __longlong_as_double((long long)x2);
-                        const double tol = 0x1p-44 * xmd;
+                        // 2^-30 in the two iterations without a stopping test (refine_step)
+                        const double tol = (iter + 1 > 2 ? 0x1p-44 : 0x1p-30) * xmd;
                         const bool conv = !(cmd > tol) || (pass >= 1 && cmd * cmd <= tol * cpd);
                         const bool stall = pass >= 2 && cmd > 0.5 * cpd;
                         cprev_s = __uint_as_float((unsigned)c2);
@@ -619,8 +620,10 @@ __global__ void __launch_bounds__(256, 1) k_beam_cl(BeamArgs b) {
             dst[9 * L + i] = td;
         }
     }
+    PH(24);
     cl_sync();  // the last DSMEM traffic; CTAs other than 0 are done
     if (rank != 0) return;
+    PH(25);
     const double* thv = pcs + 8 * L;
     const double* tdv = pcs + 9 * L;
     if (tid < 4) {
@@ -727,7 +730,7 @@ __global__ void __launch_bounds__(256, 1) k_beam_cl(BeamArgs b) {
     }
     PH(9);
     if (tid == 0)
-        for (int k = 4; k < 24; ++k) S->phase[k] += ph[k];
+        for (int k = 4; k < 26; ++k) S->phase[k] += ph[k];
     if (b.fuse_adv) {
         // the end of the time step, which the host would otherwise launch next (k_advance)
         __syncthreads();

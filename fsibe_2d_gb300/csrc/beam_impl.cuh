@@ -194,10 +194,16 @@ __device__ void solid_coeffs(int method, double dt, double dt_old, double& C1, d
 // One pass of an FP64 iterative refinement driven by an FP32 solve (block-cooperative):
 // x += c for the FP32 correction c in cf, then the block maxima of |c| and |x| decide.
 // Returns 1 when converged (the correction, or the next one predicted from the contraction
-// c_k / c_(k-1), is below 2^-44 of the solution, or the corrections stopped shrinking at the
-// FP64 residual's rounding floor below 2^-30), -1 on a failure (10 passes, or a stall above
-// that floor), 0 to go on.  rbuf: 16 doubles of shared memory.
-__device__ int refine_step(double* x, const float* cf, int n, int pass, float& cprev, double* rbuf) {
+// c_k / c_(k-1), is below tscale (2^-44) of the solution, or the corrections stopped shrinking
+// at the FP64 residual's rounding floor below 2^-30), -1 on a failure (10 passes, or a stall
+// above that floor), 0 to go on.  rbuf: 16 doubles of shared memory.
+//
+// The beam's Newton iteration passes tscale = 2^-30 in its first two iterations, which make no
+// stopping test: Newton's map is flat at the root, so the 2^-30-relative error these solves
+// leave in the second iterate moves the third by O(|x_2 - x*| 2^-30 |dx_2|), far below the
+// rounding of FP64 (and its stopping test, on dx_3 = x* - x_2, by the same 2^-30 |dx_2|).
+__device__ int refine_step(double* x, const float* cf, int n, int pass, float& cprev, double* rbuf,
+                           double tscale = 0x1p-44) {
     unsigned cm = 0;
     unsigned long long xm = 0;
     for (int k = threadIdx.x; k < n; k += blockDim.x) {
@@ -228,7 +234,7 @@ __device__ int refine_step(double* x, const float* cf, int n, int pass, float& c
     }
     const double cmd = (double)__uint_as_float(cm), cpd = (double)cprev;
     const double xmd = __longlong_as_double((long long)xm);
-    const double tol = 0x1p-44 * xmd;
+    const double tol = tscale * xmd;
     const bool conv = !(cmd > tol) || (pass >= 1 && cmd * cmd <= tol * cpd);
     const bool stall = pass >= 2 && cmd > 0.5 * cpd;
     cprev = __uint_as_float(cm);

@@ -201,7 +201,8 @@ int fsibe_kernel_times(fsibe_ctx* ctx, int nsteps, fsibe_kernel_time* out, int c
  * previous pass's decision), [20] the push and [16] the barrier of the right-hand side's
  * all-gather, [17] inverse products and solution updates, [21] the push and [18] the barrier
  * of the solution rows' all-gather, [6] the refinement's decisions, [23] Newton update and
- * norms, [7] saving the inverse, [8] position sums, [9] positions, brake and energies, [10]
+ * norms, [7] saving the inverse, [24] the angles' increments to the first CTA, [25] the
+ * cluster barrier after them, [8] position sums, [9] positions, brake and energies, [10]
  * the solve count.  out32 receives 32 values; reset != 0 zeroes them after reading. */
 int fsibe_beam_phase_cycles(fsibe_ctx* ctx, long long* out32, int reset);
 /* Rows per block chosen by the autotuner for the fused x-pass kernels (nl_x, press_x,
