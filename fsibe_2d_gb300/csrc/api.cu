@@ -27,9 +27,9 @@ void fill_sizes_1024(SizeKernels<double>&, SizeKernels<float>&);
 void fill_sizes_2048(SizeKernels<double>&, SizeKernels<float>&);
 void fill_sizes_4096(SizeKernels<double>&, SizeKernels<float>&);
 size_t beam_ws_doubles(int ns);
-void launch_mask_prep(const MaskArgs& a, double gerf, cudaStream_t st);
-void launch_mask(const MaskArgs& a, double gerf, bool fp32, cudaStream_t st);
-void launch_forces(const ForceArgs& a, double dxi, double dyi, cudaStream_t st);
+void launch_mask_prep(const MaskArgs& a, double gerf, cudaStream_t st, bool pdl);
+void launch_mask(const MaskArgs& a, double gerf, bool fp32, cudaStream_t st, bool pdl);
+void launch_forces(const ForceArgs& a, double dxi, double dyi, cudaStream_t st, bool pdl);
 void launch_forces_geo(const ForceArgs& a, double dxi, double dyi, cudaStream_t st);
 void launch_beam(const BeamArgs& b, cudaStream_t st);
 void launch_beam_pre(const BeamArgs& b, cudaStream_t st);
@@ -39,7 +39,7 @@ void beam_d1d_table(double ds, double* out);
 void launch_init_beam(const BeamArgs& b, cudaStream_t st);
 int beam_smem_setup(int ns);
 int beam_cluster_setup(int ns, int want, size_t* smem_out);
-void launch_beam_cluster(const BeamArgs& b, int R, size_t smem, cudaStream_t st);
+void launch_beam_cluster(const BeamArgs& b, int R, size_t smem, cudaStream_t st, bool pdl);
 size_t beam_cluster_minv_floats(int ns, int R);
 
 static bool get_sizes(int N, SizeKernels<double>& d, SizeKernels<float>& f) {
@@ -442,6 +442,9 @@ struct fsibe_ctx {
     cudaEvent_t ev_geo = nullptr;
     cudaEvent_t ev_adv = nullptr;  // the advection part of k_nl_x, run beside the mask kernels
     bool nl_split = true;          // split k_nl_x in fsibe_step (FSIBE_NL_SPLIT=0: one launch)
+    bool pdl = true;               // programmatic dependent launches on the main stream (FSIBE_PDL=0: off)
+    bool stress_split = true;      // viscous stresses in k_stress_x beside k_press_x (FSIBE_STRESS_SPLIT=0: off)
+    cudaEvent_t ev_ny = nullptr;   // k_nl_y done: k_stress_x may start
     double* pred = nullptr; // predictor output
     cudaStream_t side = nullptr;  // the beam predictor runs here beside the fluid step
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
@@ -559,22 +562,25 @@ static void launch_x(fsibe_ctx* c, void (*k)(KArgs<R>), int smem, const KArgs<R>
     c->launches++;
 }
 template <typename R>
+// pdl: a programmatic dependent launch (only for kernels that begin with pdl_wait)
 static void launch_y(fsibe_ctx* c, void (*k)(KArgs<R>), int smem, const KArgs<R>& a, const char* name = "y_pass",
-                     int nfields = 1) {
+                     int nfields = 1, bool pdl = false) {
     const SizeKernels<R>& K = ky_of<R>(c);
     prof_begin(c, name);
-    k<<<dim3(c->g.hx, nfields), K.y_threads, smem, c->stream>>>(a);
+    launch_k(k, dim3(c->g.hx, nfields), dim3(K.y_threads), smem, c->stream, pdl && c->pdl, a);
     prof_end(c);
     c->launches++;
 }
 
-// a fused x kernel with one of its tile-height variants (nbuf row buffers of shared memory)
+// a fused x kernel with one of its tile-height variants (nbuf row buffers of shared memory);
+// on the main stream a programmatic dependent launch (the fused x kernels begin with pdl_wait)
 template <typename R>
 static void launch_xv(fsibe_ctx* c, void (*k)(KArgs<R>), const typename SizeKernels<R>::XVariant& v, int nbuf,
                       const KArgs<R>& a, const char* name, cudaStream_t st = nullptr) {
     if (!st) st = c->stream;
     prof_begin(c, name, st);
-    k<<<c->g.ny / v.rows, v.threads, nbuf == 3 ? v.smem3 : nbuf * v.smem1, st>>>(a);
+    launch_k(k, dim3(c->g.ny / v.rows), dim3(v.threads), nbuf == 3 ? v.smem3 : nbuf * v.smem1, st,
+             c->pdl && st == c->stream, a);
     prof_end(c, st);
     c->launches++;
 }
@@ -691,8 +697,10 @@ static void nl_advect_t(fsibe_ctx* c, int explicit_step) {
 }
 
 // EvolveFluidExplicit / EvolveFluidAB2 + pressure (NavierStokes.f90:422-508, 273-403)
+// stress_rows: the forces that follow use this beam state, so k_stress_x may leave the rows
+// their stencils cannot reach
 template <typename R>
-static int fluid_step_t(fsibe_ctx* c, int explicit_step, bool adv_forked = false) {
+static int fluid_step_t(fsibe_ctx* c, int explicit_step, bool adv_forked = false, bool stress_rows = false) {
     KArgs<R> a = kargs<R>(c);
     SizeKernels<R>& KX = kx_of<R>(c);
     SizeKernels<R>& KY = ky_of<R>(c);
@@ -720,7 +728,21 @@ static int fluid_step_t(fsibe_ctx* c, int explicit_step, bool adv_forked = false
         launch_xv<R>(c, KX.xv[c->xv_nl].nl_x, KX.xv[c->xv_nl], 3, a, "nl_x");
     }
     CK(c, cudaStreamWaitEvent(c->stream, c->ev_sb, 0));
-    launch_y<R>(c, KY.nl_y, KY.y_smem_nl, a, "nl_y");
+    launch_y<R>(c, KY.nl_y, KY.y_smem_nl, a, "nl_y", 1, true);
+    if (a.viscous && c->stress_split) {
+        // the viscous stresses, read only by GetForces, on the second side stream beside the
+        // pressure kernels (joined with ev_ffj below)
+        CK(c, cudaEventRecord(c->ev_ny, c->stream));
+        CK(c, cudaStreamWaitEvent(c->side2, c->ev_ny, 0));
+        KArgs<R> s = a;
+        if (stress_rows && c->P.iBeam > 0) {
+            s.by = c->beam[B_Y];
+            s.soff = c->P.t_beam + c->P.N_smooth * std::fmax(c->g.dx, c->g.dy);
+            s.rdyi = (double)(c->P.ny - 1) / (c->P.yl - c->g.dy);
+        }
+        launch_xv<R>(c, KX.xv[c->xv_px].stress_x, KX.xv[c->xv_px], 2, s, "stress_x", c->side2);
+        a.stress_split = 1;
+    }
     launch_xv<R>(c, KX.xv[c->xv_px].press_x, KX.xv[c->xv_px], 3, a, "press_x");
     // the energies, drag and unsteady forces from press_x's partial sums feed only scalars read
     // after the fluid step: a second side stream runs them beside the pressure transforms
@@ -732,7 +754,7 @@ static int fluid_step_t(fsibe_ctx* c, int explicit_step, bool adv_forked = false
     CK(c, cudaEventRecord(c->ev_ffj, c->side2));
     c->launches++;
     if (a.pressure_on) {
-        launch_y<R>(c, KY.press_y, KY.y_smem2, a, "press_y");
+        launch_y<R>(c, KY.press_y, KY.y_smem2, a, "press_y", 1, true);
         launch_xv<R>(c, KX.xv[c->xv_fin].press_fin, KX.xv[c->xv_fin], 1, a, "press_fin");
     } else {
         CK(c, cudaMemsetAsync(c->phys[PH_PRESS], 0, sizeof(R) * (size_t)c->g.nx * c->g.ny, c->stream));
@@ -742,8 +764,9 @@ static int fluid_step_t(fsibe_ctx* c, int explicit_step, bool adv_forked = false
     return FSIBE_OK;
 }
 
-static int fluid_step(fsibe_ctx* c, int explicit_step, bool adv_forked = false) {
-    return c->fp32 ? fluid_step_t<float>(c, explicit_step, adv_forked) : fluid_step_t<double>(c, explicit_step, adv_forked);
+static int fluid_step(fsibe_ctx* c, int explicit_step, bool adv_forked = false, bool stress_rows = false) {
+    return c->fp32 ? fluid_step_t<float>(c, explicit_step, adv_forked, stress_rows)
+                   : fluid_step_t<double>(c, explicit_step, adv_forked, stress_rows);
 }
 
 static MaskArgs mask_args(fsibe_ctx* c) {
@@ -771,10 +794,10 @@ static int create_mask(fsibe_ctx* c) {
     }
     const MaskArgs m = mask_args(c);
     prof_begin(c, "mask_prep");
-    launch_mask_prep(m, c->gerf, c->stream);
+    launch_mask_prep(m, c->gerf, c->stream, c->pdl);
     prof_end(c);
     prof_begin(c, "mask");
-    launch_mask(m, c->gerf, c->fp32, c->stream);
+    launch_mask(m, c->gerf, c->fp32, c->stream, c->pdl);
     prof_end(c);
     c->launches += 2;
     CKL(c);
@@ -822,7 +845,7 @@ static int get_forces(fsibe_ctx* c, bool geo_done = false) {
     if (geo_done) CK(c, cudaStreamWaitEvent(c->stream, c->ev_geo, 0));
     else forces_geo(c, c->stream);
     prof_begin(c, "forces");
-    launch_forces(f, dxi, dyi, c->stream);
+    launch_forces(f, dxi, dyi, c->stream, c->pdl);
     prof_end(c);
     c->launches++;
     CKL(c);
@@ -854,7 +877,7 @@ static int solid_step(fsibe_ctx* c, bool end_step = false, bool* advanced = null
             b.adv = adv_args(c);
             if (advanced) *advanced = true;
         }
-        launch_beam_cluster(b, c->beam_cl, c->beam_cl_smem, c->stream);
+        launch_beam_cluster(b, c->beam_cl, c->beam_cl_smem, c->stream, c->pdl);
     } else {
         launch_beam(beam_args(c), c->stream);
     }
@@ -898,7 +921,7 @@ static int step_body(fsibe_ctx* c, int explicit_step) {
         CK(c, cudaEventRecord(c->ev_geo, c->side2));
     }
     if (mask) { st = create_mask(c); if (st) return st; }
-    st = fluid_step(c, explicit_step, split);
+    st = fluid_step(c, explicit_step, split, forces);
     if (st) return st;
     if (forces) { st = get_forces(c, true); if (st) return st; }
     bool advanced = false;
@@ -1151,6 +1174,7 @@ int fsibe_destroy(fsibe_ctx* c) {
     if (c->ev_sb0) cudaEventDestroy(c->ev_sb0);
     if (c->ev_geo) cudaEventDestroy(c->ev_geo);
     if (c->ev_adv) cudaEventDestroy(c->ev_adv);
+    if (c->ev_ny) cudaEventDestroy(c->ev_ny);
     if (c->ev_sb) cudaEventDestroy(c->ev_sb);
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
     delete c;
@@ -1233,6 +1257,10 @@ int fsibe_create(const fsibe_params* p, fsibe_ctx** out) {
     {
         const char* e = std::getenv("FSIBE_NL_SPLIT");
         c->nl_split = !(e && std::atoi(e) == 0);
+        e = std::getenv("FSIBE_PDL");
+        c->pdl = !(e && std::atoi(e) == 0);
+        e = std::getenv("FSIBE_STRESS_SPLIT");
+        c->stress_split = !(e && std::atoi(e) == 0);
     }
     ALLOC(c->prims, sizeof(Prim) * (size_t)(2 * ns + 8));
     ALLOC(c->nprims, 16);
@@ -1308,6 +1336,7 @@ int fsibe_create(const fsibe_params* p, fsibe_ctx** out) {
     cudaEventCreateWithFlags(&c->ev_sb0, cudaEventDisableTiming);
     cudaEventCreateWithFlags(&c->ev_geo, cudaEventDisableTiming);
     cudaEventCreateWithFlags(&c->ev_adv, cudaEventDisableTiming);
+    cudaEventCreateWithFlags(&c->ev_ny, cudaEventDisableTiming);
     cudaEventCreateWithFlags(&c->ev_sb, cudaEventDisableTiming);
     {
         const int st = c->fp32 ? autotune_x<float>(c) : autotune_x<double>(c);
@@ -1692,6 +1721,7 @@ int fsibe_launches_per_step(fsibe_ctx* c, int* n) {
     if (!c || !n) return FSIBE_ERR_PARAM;
     const fsibe_params& P = c->P;
     int k = 6;  // step_begin, nl_x, nl_y, press_x, fluid_finish, advance
+    if (P.iViscous == 1 && c->stress_split) k += 1;  // k_stress_x
     if (P.iFLUSI == 1 || P.iSaveBeam > 0) k += 2 + 2;  // press_y, press_fin, forces geometry, forces
     // mask prep + raster, and nl_x split into its advection and penalization parts
     if ((P.iFLUSI == 1 || P.iMotion > 0) && P.iBeam > 0) k += c->nl_split ? 3 : 2;

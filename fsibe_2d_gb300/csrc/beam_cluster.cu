@@ -176,6 +176,7 @@ __device__ void inv_row(const float* __restrict__ U, const float* __restrict__ L
 // The cluster form of k_beam (one cluster of R CTAs of 256 threads; R from the launch).
 // k_beam_pre of the same step ran before it and left the step's constants in b.pred.
 __global__ void __launch_bounds__(256, 1) k_beam_cl(BeamArgs b) {
+    pdl_wait();     // the previous kernel of the stream has completed
     extern __shared__ __align__(16) unsigned char cl_smem[];
     DevScalars* S = b.S;
     if (S->status != 0) return;  // the same value in every CTA
@@ -791,19 +792,21 @@ int beam_cluster_setup(int ns, int want, size_t* smem_out) {
     return 0;
 }
 
-void launch_beam_cluster(const BeamArgs& b, int R, size_t smem, cudaStream_t st) {
+void launch_beam_cluster(const BeamArgs& b, int R, size_t smem, cudaStream_t st, bool pdl) {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(R);
     cfg.blockDim = dim3(256);
     cfg.dynamicSmemBytes = smem;
     cfg.stream = st;
-    cudaLaunchAttribute at[1];
+    cudaLaunchAttribute at[2];
     at[0].id = cudaLaunchAttributeClusterDimension;
     at[0].val.clusterDim.x = R;
     at[0].val.clusterDim.y = 1;
     at[0].val.clusterDim.z = 1;
+    at[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[1].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = at;
-    cfg.numAttrs = 1;
+    cfg.numAttrs = pdl ? 2 : 1;
     cudaLaunchKernelEx(&cfg, k_beam_cl, b);
 }
 

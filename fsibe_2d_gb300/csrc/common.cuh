@@ -17,6 +17,31 @@
 
 namespace fsibe {
 
+// Programmatic dependent launch (PTX griddepcontrol).  A kernel launched with
+// cudaLaunchAttributeProgrammaticStreamSerialization may start while the previous kernel of its
+// stream still runs; pdl_wait() returns once that kernel has completed and its memory is
+// visible (at once for a kernel launched without the attribute), so it comes before the first
+// read of anything an earlier kernel wrote.  pdl_trigger() lets the next kernel of the stream
+// launch: its blocks become resident and wait in their own pdl_wait().
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
+// Launch k<<<g, b, smem, st>>>(args...), as a programmatic dependent launch when pdl is set.
+template <typename... P, typename... A>
+inline cudaError_t launch_k(void (*k)(P...), dim3 g, dim3 b, size_t smem, cudaStream_t st, bool pdl, A&&... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = g;
+    cfg.blockDim = b;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = pdl ? 1 : 0;
+    return cudaLaunchKernelEx(&cfg, k, static_cast<A&&>(args)...);
+}
+
 template <typename R> struct C2T;
 template <> struct C2T<double> { typedef double2 type; };
 template <> struct C2T<float> { typedef float2 type; };

@@ -42,6 +42,11 @@ struct KArgs {
     int viscous, pressure_on, penalize, op;
     int explicit_step;    // 1 on the Euler start-up step (the host's flag: nl_x runs beside k_step_begin)
     const int* rect;      // the mask's box (rect[2..3]: its rows), written by k_mask_prep
+    // the viscous stresses in their own kernel (k_stress_x) instead of k_press_x; with by set,
+    // only on the rows that the forces' stencils at the beam can reach
+    int stress_split;
+    const double* by;     // beam y (ns nodes)
+    double soff, rdyi;    // the stress points' offset from the centre line; 1 / interpolation spacing
     size_t bstride;       // generic transforms over several fields at once: blockIdx.y selects the
                           // field, bstride complex values (= nx ny / 2) apart in every buffer
 };
@@ -331,6 +336,7 @@ __global__ void __launch_bounds__(XRows<R, H>::THREADS) k_vel_x(KArgs<R> a) {
 // ======================================================================================
 template <typename R, int H, int TRV, int PART = NL_WHOLE>
 __global__ void __launch_bounds__(XRows<R, H, TRV>::THREADS) k_nl_x(KArgs<R> a) {
+    pdl_wait();     // the previous kernel of the stream has completed
     using X = XRows<R, H, TRV>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C2<R>* bufA = reinterpret_cast<C2<R>*>(smem_raw);
@@ -465,6 +471,7 @@ template <typename R, int NY>
 // (FP32: at most 128 registers a thread, so that four blocks share an SM and the 512 rows of
 // 1024^2 run in one wave)
 __global__ void __launch_bounds__(NY / 8, kIsF32<R> ? 4 : 1) k_nl_y(KArgs<R> a) {
+    pdl_wait();     // the previous kernel of the stream has completed
     constexpr int G = NY / 8;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C2<R>* bufA = reinterpret_cast<C2<R>*>(smem_raw);
@@ -636,6 +643,7 @@ template <typename R, int H, int TRV>
 // (FP32: at most 128 registers a thread, so that two 256-thread blocks share an SM and the
 // 1024^2 grid runs in one wave; FP64 is bound by its arithmetic and keeps its registers)
 __global__ void __launch_bounds__(XRows<R, H, TRV>::THREADS, (sizeof(R) == 4) ? XRows<R, H, TRV>::MINB128 : 1) k_press_x(KArgs<R> a) {
+    pdl_wait();     // the previous kernel of the stream has completed
     using X = XRows<R, H, TRV>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C2<R>* bufA = reinterpret_cast<C2<R>*>(smem_raw);
@@ -832,7 +840,7 @@ __global__ void __launch_bounds__(XRows<R, H, TRV>::THREADS, (sizeof(R) == 4) ? 
             a.P2[o] = bufB[rr * X::PL + pad8(kx)];
         }
     }
-    if (a.viscous) {
+    if (a.viscous && !a.stress_split) {
         __syncthreads();
         load_tileT<R, H, X::TR, X::PL>(bufA, a.Tsa, ny, iy0, a.kcut);
         load_tileT<R, H, X::TR, X::PL>(bufB, a.Tsb, ny, iy0, a.kcut);
@@ -851,9 +859,59 @@ __global__ void __launch_bounds__(XRows<R, H, TRV>::THREADS, (sizeof(R) == 4) ? 
     }
 }
 
+// The viscous stresses (NavierStokes.f90:354-370: 2 nu d2psi/dxdy, nu (d2psi/dy2 - d2psi/dx2))
+// to physical space, beside k_press_x on another stream: only GetForces reads them.  With
+// a.by set, a block whose rows no stencil of the forces reaches (rows j - 4 .. j + 4 of the
+// stress points' cells j, BeamForces.f90:105-124, which lie within soff of the beam's
+// y range) leaves them; every block forms the range from the beam state alone.
+template <typename R, int H, int TRV>
+__global__ void __launch_bounds__(XRows<R, H, TRV>::THREADS) k_stress_x(KArgs<R> a) {
+    using X = XRows<R, H, TRV>;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    C2<R>* bufA = reinterpret_cast<C2<R>*>(smem_raw);
+    constexpr int BS = X::TR * X::PL;
+    C2<R>* bufB = bufA + BS;
+    const int r = threadIdx.x / X::G, t = threadIdx.x % X::G;
+    const int iy0 = blockIdx.x * X::TR, ny = a.g.ny;
+    if (a.by) {
+        __shared__ double ymm[2][32];
+        double lo = 1e300, hi = -1e300;
+        for (int i = threadIdx.x; i < a.g.ns; i += blockDim.x) { lo = fmin(lo, a.by[i]); hi = fmax(hi, a.by[i]); }
+        for (int o = 16; o > 0; o >>= 1) {
+            lo = fmin(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+            hi = fmax(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+        }
+        if ((threadIdx.x & 31) == 0) { ymm[0][threadIdx.x >> 5] = lo; ymm[1][threadIdx.x >> 5] = hi; }
+        __syncthreads();
+        lo = ymm[0][0]; hi = ymm[1][0];
+        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) { lo = fmin(lo, ymm[0][w]); hi = fmax(hi, ymm[1][w]); }
+        // the cells' rows with two rows of margin for the rounding of the cell index
+        const double j0 = floor((lo - a.soff) * a.rdyi) - 6.0, j1 = floor((hi + a.soff) * a.rdyi) + 6.0;
+        if ((double)(iy0 + X::TR - 1) < j0 || (double)iy0 > j1) return;
+    }
+    C2<R>* ra = bufA + r * X::PL;
+    C2<R>* rb = bufB + r * X::PL;
+    load_tileT<R, H, X::TR, X::PL>(bufA, a.Tsa, ny, iy0, a.kcut);
+    load_tileT<R, H, X::TR, X::PL>(bufB, a.Tsb, ny, iy0, a.kcut);
+    __syncthreads();
+    row_c2r_m<R, H, 2>(ra, BS, a.twR, a.twX, t);  // ra and rb together
+    const size_t roff = (size_t)(iy0 + r) * H;
+    C2<R>* sa2 = reinterpret_cast<C2<R>*>(a.sa) + roff;
+    C2<R>* sb2 = reinterpret_cast<C2<R>*>(a.sb) + roff;
+    const R c2 = (R)(2.0 * a.nu), c1 = (R)a.nu;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+        const int m = t + q * X::G;
+        const C2<R> x = ra[pad8(m)], y = rb[pad8(m)];
+        sa2[m] = mk<R>(c2 * x.x, c2 * x.y);
+        sb2[m] = mk<R>(c1 * y.x, c1 * y.y);
+    }
+}
+
 // K5: forward-y of the Poisson right-hand side, divergence, poisson, inverse-y -> Tq
 template <typename R, int NY>
 __global__ void __launch_bounds__(NY / 8) k_press_y(KArgs<R> a) {
+    pdl_wait();     // the previous kernel of the stream has completed
     constexpr int G = NY / 8;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C2<R>* bufA = reinterpret_cast<C2<R>*>(smem_raw);
@@ -896,6 +954,7 @@ __global__ void __launch_bounds__(NY / 8) k_press_y(KArgs<R> a) {
 // K6: inverse-x of q, p = q - |u|^2/2
 template <typename R, int H, int TRV>
 __global__ void __launch_bounds__(XRows<R, H, TRV>::THREADS) k_press_fin(KArgs<R> a) {
+    pdl_wait();     // the previous kernel of the stream has completed
     using X = XRows<R, H, TRV>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C2<R>* buf = reinterpret_cast<C2<R>*>(smem_raw);
@@ -948,6 +1007,7 @@ struct SizeKernels {
         void (*nl_x)(KArgs<R>);
         void (*nl_adv)(KArgs<R>);  // k_nl_x's advection and penalization parts (two buffers)
         void (*nl_pen)(KArgs<R>);
+        void (*stress_x)(KArgs<R>);  // two buffers
         void (*press_x)(KArgs<R>);
         void (*press_fin)(KArgs<R>);
     } xv[3];
@@ -969,6 +1029,8 @@ inline void fill_xvariant(typename SizeKernels<R>::XVariant& v) {
     v.nl_x = k_nl_x<R, H, TR>;
     v.nl_adv = k_nl_x<R, H, TR, NL_ADVECT>;
     v.nl_pen = k_nl_x<R, H, TR, NL_PENAL>;
+    v.stress_x = k_stress_x<R, H, TR>;
+    cudaFuncSetAttribute(k_stress_x<R, H, TR>, cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * v.smem1);
     cudaFuncSetAttribute(k_nl_x<R, H, TR, NL_ADVECT>, cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * v.smem1);
     cudaFuncSetAttribute(k_nl_x<R, H, TR, NL_PENAL>, cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * v.smem1);
     v.press_x = k_press_x<R, H, TR>;

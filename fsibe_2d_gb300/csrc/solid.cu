@@ -33,6 +33,7 @@ __device__ __forceinline__ void clip_box(int* bx, int nx, int ny) {
 // primitives is reduced with atomics; the last block publishes it with its union with the
 // previous step's box and resets the accumulator.
 __global__ void __launch_bounds__(64) k_mask_prep(MaskArgs a, double gerf) {
+    pdl_wait();     // the previous kernel of the stream has completed
     __shared__ double ang2[32];
     __shared__ int wbox[2][4];
     const int ns = a.ns, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -361,6 +362,7 @@ __device__ __forceinline__ void mask_prim(const MaskArgs& a, const Prim& Q, cons
 // hinges and dots.
 template <typename R>
 __global__ void __launch_bounds__(32 * MASK_WARPS) k_mask_raster(MaskArgs a, double gerf) {
+    pdl_wait();     // the previous kernel of the stream has completed
     constexpr bool F32 = sizeof(R) == 4;
     using T = R;  // the fold's arithmetic: FP32 in the FP32 form, FP64 in the FP64 form
     __shared__ Prim sp[MASK_WARPS][32];
@@ -593,6 +595,7 @@ __global__ void __launch_bounds__(128) k_forces_geo(ForceArgs a, double dxi, dou
 }
 
 __global__ void __launch_bounds__(128) k_forces(ForceArgs a, double dxi, double dyi) {
+    pdl_wait();     // the previous kernel of the stream has completed
     const int n = blockIdx.x;
     __shared__ double dl[4][18];
     __shared__ int ij[4][2];
@@ -687,21 +690,21 @@ __global__ void __launch_bounds__(128) k_forces(ForceArgs a, double dxi, double 
 // ===================================================================================
 // Host launchers
 // ===================================================================================
-void launch_mask_prep(const MaskArgs& a, double gerf, cudaStream_t st) {
-    k_mask_prep<<<(a.ns + 3 + 31) / 32, 64, 0, st>>>(a, gerf);
+void launch_mask_prep(const MaskArgs& a, double gerf, cudaStream_t st, bool pdl) {
+    launch_k(k_mask_prep, dim3((a.ns + 3 + 31) / 32), dim3(64), 0, st, pdl, a, gerf);
 }
-void launch_mask(const MaskArgs& a, double gerf, bool fp32, cudaStream_t st) {
+void launch_mask(const MaskArgs& a, double gerf, bool fp32, cudaStream_t st, bool pdl) {
     // four-warp blocks, two per SM: a tile's primitives over the four SMSPs of an SM
     const int blocks = 2 * a.nsm;
-    if (fp32) k_mask_raster<float><<<blocks, 32 * MASK_WARPS, 0, st>>>(a, gerf);
-    else k_mask_raster<double><<<blocks, 32 * MASK_WARPS, 0, st>>>(a, gerf);
+    if (fp32) launch_k(k_mask_raster<float>, dim3(blocks), dim3(32 * MASK_WARPS), 0, st, pdl, a, gerf);
+    else launch_k(k_mask_raster<double>, dim3(blocks), dim3(32 * MASK_WARPS), 0, st, pdl, a, gerf);
 }
 
 void launch_forces_geo(const ForceArgs& a, double dxi, double dyi, cudaStream_t st) {
     k_forces_geo<<<a.ns, 128, 0, st>>>(a, dxi, dyi);
 }
-void launch_forces(const ForceArgs& a, double dxi, double dyi, cudaStream_t st) {
-    k_forces<<<a.ns, 128, 0, st>>>(a, dxi, dyi);
+void launch_forces(const ForceArgs& a, double dxi, double dyi, cudaStream_t st, bool pdl) {
+    launch_k(k_forces, dim3(a.ns), dim3(128), 0, st, pdl, a, dxi, dyi);
 }
 
 }  // namespace fsibe

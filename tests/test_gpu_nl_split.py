@@ -3,7 +3,11 @@
 alone (outside the box the mask, and with it the penalization, is zero).  The routine-by-routine
 path (create_mask, EvolveFluidAB2, GetForces, SolidSolverWrapper, advance) forms the whole
 right-hand side in one launch.  Both give the same state: the split changes no arithmetic,
-only which rows carry an exactly-zero penalization term."""
+only which rows carry an exactly-zero penalization term.
+
+The fused step also forms the viscous stresses only on the rows that the forces' stencils can
+reach (k_stress_x with the beam's y range); the routine-by-routine path forms them on every
+row, so equal forces show that the range covers every stencil."""
 import numpy as np
 import pytest
 
