@@ -102,12 +102,34 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(self.samples)}
 
 
+# Fields each fused fluid kernel reads + writes once per launch, FP32-compensated form with the
+# split launches of fsibe_step.  One real field of nx*ny values, or one half spectrum of
+# nx/2*ny complex values, is one pass; a spectrum touched only on its rows kx < kcut (every
+# row above is zero after the 2/3 rule) counts f = kcut / (nx/2) of a pass:
+#   nl_y      R A, B, W, Wlo, M (f)      W W, Wlo, M (1), Tu, Tv, Tw, Tdx, Tdy, Tsa, Tsb (f)
+#   nl_adv    R Tdx, Tdy (f), u, v       W A, B (f)
+#   nl_x      R Tdx, Tdy (f), u, v, mask, mvx, mvy      W A, B (f)   (one launch, FSIBE_NL_SPLIT=0)
+#   press_x   R Tu, Tv, Tw (f), mask, mvx, mvy, vor_mean      W u, v, vor_mean, P1, P2
+#   press_y   R P1, P2                   W Tq
+#   press_fin R Tq, u, v                 W press
+# (nl_pen and stress_x touch only the rows near the beam.)
+PASSES = {"nl_y": lambda f: 12 * f + 3, "nl_adv": lambda f: 4 * f + 2, "nl_x": lambda f: 4 * f + 5,
+          "press_x": lambda f: 3 * f + 9, "press_y": lambda f: 3, "press_fin": lambda f: 4}
+
+
+def kcut_fraction(nx, ny):
+    """kcut / (nx/2): the first kx whose modes the 2/3 rule removes for every ky
+    (dealiase_mask.f90:9-26, kx^2/kxt^2 >= 1 with kxt = 2/3 (nx/2 - 1))."""
+    kxt = 2.0 / 3.0 * (nx // 2 - 1)
+    kcut = next((kx for kx in range(nx // 2) if kx * kx / (kxt * kxt) >= 1.0), nx // 2)
+    return kcut / (nx // 2)
+
+
 def algorithmic_bytes(kernel, nx, ny, rbytes):
-    """Bytes one launch must move: the fields it reads and writes, each once (one real field of
-    nx*ny values, or one half spectrum of nx/2*ny complex values, is nx*ny*rbytes bytes)."""
-    field = nx * ny * rbytes  # one real field == one half spectrum of complex values
-    passes = {"nl_y": 4 + 9, "nl_x": 7 + 2, "press_x": 9 + 9, "press_y": 3, "press_fin": 4, "mask": 3}
-    return passes.get(kernel, 0) * field
+    """Bytes one launch must move: the fields it reads and writes, each once."""
+    if kernel not in PASSES:
+        return 0
+    return int(round(PASSES[kernel](kcut_fraction(nx, ny)) * nx * ny * rbytes))
 
 
 def measured_peaks():
@@ -221,7 +243,7 @@ def gpu_arm(args):
     val64 = cells * args.steps / (results["fp64"]["ms"] * 1e-3) / 1e6
     peaks, which = measured_peaks()
     kt = results["fp32c"]["kernels"]
-    top = max((k for k in kt if k in ("nl_y", "nl_x", "press_x", "press_y", "press_fin")), key=lambda k: kt[k])
+    top = max((k for k in kt if k in PASSES), key=lambda k: kt[k])
     top_ms = kt[top]
     ab = algorithmic_bytes(top, NX, NY, 4)
     achieved = ab / (top_ms * 1e-3) / 1e9

@@ -151,7 +151,12 @@ int fsibe_solid_step(fsibe_ctx* ctx, double time);
  * (time_step.f90:152-159, 222-228). */
 int fsibe_advance(fsibe_ctx* ctx);
 /* One whole step in the reference order (time_step.f90:120-162 when the
- * startup step is due, else :178-228). */
+ * startup step is due, else :178-228).  The same results as the five calls above, in fewer
+ * dependent launches: cal_nlk's advection part runs beside the mask kernels and its
+ * penalization part covers only the rows of the mask's box (FSIBE_NL_SPLIT=0: one kernel),
+ * the viscous stresses run beside the pressure kernels on the rows the forces' stencils reach
+ * (FSIBE_STRESS_SPLIT=0: inside the pressure kernel, every row), and the main stream's kernels
+ * are programmatic dependent launches (FSIBE_PDL=0: plain launches). */
 int fsibe_step(fsibe_ctx* ctx);
 /* nsteps calls of fsibe_step; when rows != NULL writes one 21-column beam_data
  * row per step (rows[s*21 + c]). Stops early on a non-zero status. */
@@ -253,7 +258,10 @@ int fsibe_drag_gradient(fsibe_ctx* ctx, const double* vort0, double nu, int nste
  * run's step on its own stream.  Work issued on a run's context directly is ordered before
  * and after the ensemble's steps.  Ensembles of 8 runs or more run each beam on one CTA
  * (fsibe_beam_cluster reports 0) unless FSIBE_BEAM_CLUSTER is set: many runs fill the GPU by
- * themselves, and the single-CTA kernel then gives the higher throughput. */
+ * themselves, and the single-CTA kernel then gives the higher throughput.  For the same reason
+ * their steps form the nonlinear term and the stresses in the fused kernels (the split launches
+ * of a single run, see fsibe_step, would only add graph nodes) unless FSIBE_NL_SPLIT or
+ * FSIBE_STRESS_SPLIT is set. */
 typedef struct fsibe_ensemble fsibe_ensemble;
 int fsibe_ensemble_create(const fsibe_params* params, int nruns, fsibe_ensemble** out);
 int fsibe_ensemble_destroy(fsibe_ensemble* ens);
