@@ -467,10 +467,16 @@ __global__ void __launch_bounds__(XRows<R, H, TRV>::THREADS) k_nl_x(KArgs<R> a) 
 // K3: forward-y of the right-hand side, AB2 / Euler integrating-factor update, and the
 // inverse-y transforms of everything the velocity/pressure/force kernels need.
 // ======================================================================================
+// Blocks per SM that k_nl_y's launch bounds ask for: in FP32 as many as 128 registers a thread
+// allow (four at NY = 1024, so that its 512 rows run in one wave; one at NY = 4096), never
+// fewer registers than that (fewer spill the transforms' state)
 template <typename R, int NY>
-// (FP32: at most 128 registers a thread, so that four blocks share an SM and the 512 rows of
-// 1024^2 run in one wave)
-__global__ void __launch_bounds__(NY / 8, kIsF32<R> ? 4 : 1) k_nl_y(KArgs<R> a) {
+constexpr int nl_y_minb() {
+    return !kIsF32<R> ? 1 : (65536 / ((NY / 8) * 128) >= 4 ? 4 : (65536 / ((NY / 8) * 128) >= 1 ? 65536 / ((NY / 8) * 128) : 1));
+}
+
+template <typename R, int NY>
+__global__ void __launch_bounds__(NY / 8, (nl_y_minb<R, NY>())) k_nl_y(KArgs<R> a) {
     pdl_wait();     // the previous kernel of the stream has completed
     constexpr int G = NY / 8;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -910,7 +916,7 @@ __global__ void __launch_bounds__(XRows<R, H, TRV>::THREADS) k_stress_x(KArgs<R>
 
 // K5: forward-y of the Poisson right-hand side, divergence, poisson, inverse-y -> Tq
 template <typename R, int NY>
-__global__ void __launch_bounds__(NY / 8) k_press_y(KArgs<R> a) {
+__global__ void __launch_bounds__(NY / 8, (kIsF32<R> && NY >= 4096) ? 2 : 1) k_press_y(KArgs<R> a) {
     pdl_wait();     // the previous kernel of the stream has completed
     constexpr int G = NY / 8;
     extern __shared__ __align__(16) unsigned char smem_raw[];
