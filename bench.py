@@ -237,6 +237,7 @@ def gpu_arm(args):
 
     ens = ensemble_c4(F, args) if rank == 0 else None
     adj = adjoint_c3(F) if rank == 0 else None
+    large = large_run_c5(F, measured_peaks()[0]) if rank == 0 and not args.no_large else None
 
     cells = NX * NY * world
     val32 = cells * args.steps / (results["fp32c"]["ms"] * 1e-3) / 1e6
@@ -279,12 +280,50 @@ def gpu_arm(args):
             "gpu_launches": results["fp32c"]["launches"] * args.steps,
             "clocks": results["fp32c"]["clocks"],
             "ensemble": ens,
+            "large_run": large,
             "autotuned_x_tiles": {tag: dict(zip(("nl_x", "press_x", "press_fin"), results[tag]["tiles"]))
                                   for tag in ("fp32c", "fp64")},
         }
         print(json.dumps(line))
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def large_run_c5(F, peaks, err_steps=1000):
+    """The large single run: 4096^2, box 8x8, Re=2000, clamped beam ns=1024, EI=0.05, mu=2,
+    eta=1e-4, dt=1e-5, seeded |k|<=32 noise of amplitude 1e-3, FP32-compensated form.  Cell-steps/s
+    from the CUDA graph (the working set, about 2 GB, exceeds L2: no flush is needed), each
+    fused fluid kernel's algorithmic bytes over its live time against the HBM peak, and the
+    drag/lift error against an FP64 run over the first err_steps steps."""
+    n = 4096
+    kw = dict(nx=n, ny=n, ns=1024, xl=8.0, yl=8.0, Re=2000.0, dt=1e-5, EI=0.05, mu=2.0, eps=1e-4, x0=2.0, y0=4.0)
+    w = seeded_vorticity(n, K=32, sigma=1e-3, seed=2)
+    g32 = F.Run(F.make_params(precision=F.FSIBE_FP32C, **kw))
+    g32.init_fields(w)
+    r32 = g32.time_step(err_steps)
+    kt = kernel_times(g32, 10)
+    g32.use_graph(True)
+    g32.time_step(3)
+    K = 50
+    ms = g32.time_steps(K) / K
+    g32.close()
+    g64 = F.Run(F.make_params(precision=F.FSIBE_FP64, **kw))
+    g64.init_fields(w)
+    r64 = g64.time_step(err_steps)
+    g64.close()
+    drag_err = float(np.linalg.norm(r32[:, 10] - r64[:, 10]) / np.linalg.norm(r64[:, 10]))
+    lift_err = float(np.linalg.norm(r32[:, 11] - r64[:, 11]) / np.linalg.norm(r64[:, 10:12]))
+    roof = {}
+    for k, v in kt.items():
+        ab = algorithmic_bytes(k, n, n, 4)
+        if ab:
+            gbs = ab / (v * 1e-3) / 1e9
+            roof[k] = {"us": round(v * 1e3, 1), "bytes": ab, "GB/s": round(gbs, 1), "frac": round(gbs / peaks["hbm_gbs"], 3)}
+    return {"workload": "4096^2 box 8x8, Re=2000, ns=1024, EI=0.05, mu=2, eta=1e-4, dt=1e-5, FP32-compensated",
+            "ms_per_step": round(ms, 4), "value": round(n * n / (ms * 1e-3) / 1e6, 1), "unit": "Mcell-steps/s",
+            "kernel_ms_per_step": {k: round(v, 4) for k, v in kt.items()},
+            "hbm_roofline": roof, "error_steps": err_steps,
+            "drag_rel_err_vs_fp64": drag_err, "lift_rel_err_at_force_scale_vs_fp64": lift_err}
 
 
 def adjoint_c3(F):
@@ -438,6 +477,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--err-steps", type=int, default=200)
+    ap.add_argument("--no-large", action="store_true", help="skip the 4096^2 large-run report")
     args = ap.parse_args()
     if args.impl == "reference":
         reference_arm(args)

@@ -18,7 +18,7 @@ namespace fsibe {
 // Workspace length (doubles) of the global copy of the beam workspace for ns nodes.
 __host__ size_t beam_ws_doubles(int ns) {
     return beam_vec_doubles(ns) + beam_band_doubles(ns) +
-           (beam_fact_floats(ns) + beam_scr_floats(ns) + beam_bulk_floats(ns) + 1) / 2;
+           (beam_lu_floats(ns) + beam_fact_floats(ns) + beam_scr_floats(ns) + beam_bulk_floats(ns) + 1) / 2;
 }
 
 // Doubles of the predictor's output: the initial guess x (n), the Crank-Nicolson right-hand
@@ -217,10 +217,13 @@ __global__ void __launch_bounds__(256) k_beam(BeamArgs b) {
         const NewtonCtx& c = cs;
         // the FP32 factor of an earlier step, when one is stored
         bool need_factor = (S->beam_fact == 0), factored = false;
-        if (!need_factor && (mode & 2)) {
-            const float4* g = reinterpret_cast<const float4*>(b.ws + beam_vec_doubles(ns) + beam_band_doubles(ns));
-            float4* d = reinterpret_cast<float4*>(w.Uf);
-            copy_f4(d, g, beam_fact_floats(ns) / 4);
+        if (!need_factor && (mode & (2 | 16))) {
+            // the global copy holds [lu | fact] at its place
+            const float* g = reinterpret_cast<const float*>(b.ws + beam_vec_doubles(ns) + beam_band_doubles(ns));
+            if (mode & 16) copy_f4(reinterpret_cast<float4*>(w.Uf), reinterpret_cast<const float4*>(g), beam_lu_floats(ns) / 4);
+            if (mode & 2)
+                copy_f4(reinterpret_cast<float4*>(w.rse), reinterpret_cast<const float4*>(g + beam_lu_floats(ns)),
+                        beam_fact_floats(ns) / 4);
             __syncthreads();
         }
         int iter = 0;
@@ -337,11 +340,11 @@ __global__ void __launch_bounds__(256) k_beam(BeamArgs b) {
             b.thd[i] = c.D * (th - c.C3 * w.bo5[i] - c.C4 * w.oo5[i]) - c.C2 * w.bo6[i];
         }
         if (factored) {
-            if (mode & 2) {
-                float4* g = reinterpret_cast<float4*>(b.ws + beam_vec_doubles(ns) + beam_band_doubles(ns));
-                const float4* d = reinterpret_cast<const float4*>(w.Uf);
-                copy_f4(g, d, beam_fact_floats(ns) / 4);
-            }
+            float* g = reinterpret_cast<float*>(b.ws + beam_vec_doubles(ns) + beam_band_doubles(ns));
+            if (mode & 16) copy_f4(reinterpret_cast<float4*>(g), reinterpret_cast<const float4*>(w.Uf), beam_lu_floats(ns) / 4);
+            if (mode & 2)
+                copy_f4(reinterpret_cast<float4*>(g + beam_lu_floats(ns)), reinterpret_cast<const float4*>(w.rse),
+                        beam_fact_floats(ns) / 4);
             if (threadIdx.x == 0) S->beam_fact = 1;
         }
         if (threadIdx.x == 0) {
@@ -371,13 +374,26 @@ __global__ void __launch_bounds__(256) k_beam(BeamArgs b) {
     // the four running sums in the reference's order: the positions decide grid-aligned
     // boxes (mask, drag window), so their roundings must be the reference's
     if (threadIdx.x < 4) {
+        // eight terms at a time, the next eight loaded before the current ones are added (the
+        // workspace is in global memory at large ns); the order of the additions is unchanged
         const int q = threadIdx.x;
         const double* src = w.cs + q * (ns + 8);
         double* dst = w.pre + q * (ns + 8);
-        double s = 0.0;
-        for (int i = 0; i < ns; ++i) {
-            dst[i] = s;
-            s = (q == 2) ? s - src[i] : s + src[i];
+        double s = 0.0, v[8], nv[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) v[u] = (u < ns) ? src[u] : 0.0;
+        for (int i = 0; i < ns; i += 8) {
+#pragma unroll
+            for (int u = 0; u < 8; ++u) nv[u] = (i + 8 + u < ns) ? src[i + 8 + u] : 0.0;
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                if (i + u < ns) {
+                    dst[i + u] = s;
+                    s = (q == 2) ? s - v[u] : s + v[u];
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < 8; ++u) v[u] = nv[u];
         }
     }
     __syncthreads();
@@ -493,7 +509,7 @@ __global__ void k_init_beam(BeamArgs b) {
 // ===================================================================================
 static size_t beam_smem_bytes(int ns, int mask) {
     size_t bytes = 0;
-    for (int part = 0; part < 4; ++part)
+    for (int part = 0; part < BEAM_PARTS; ++part)
         if (mask & (1 << part)) bytes += beam_part_bytes(ns, part);
     return bytes;
 }
@@ -521,14 +537,25 @@ int beam_pre_smem_setup(int ns) {
     if (bytes > 216 * 1024) return 0;
     return raise_smem_limit((const void*)k_beam_pre, bytes, &g_pre_smem) ? 4 : 0;
 }
-// Shared-memory placement of the beam workspace: parts taken in the order scr, fact, vec,
-// band, each one kept when it still fits in 216 KB.
+// Shared-memory placement of the beam workspace: parts taken in beam_part_at order (scratch,
+// LU factor, rest of the factor, FP64 vectors, band), each one kept when it still fits beside
+// the kernel's static shared memory (at ns = 1024 the 198 KB LU factor fits, so the chunk
+// sweeps' dependent loads come from shared memory).
 int beam_smem_setup(int ns) {
+    int dev = 0, optin = 0;
+    cudaFuncAttributes fa;
+    size_t budget = 216 * 1024;
+    if (cudaGetDevice(&dev) == cudaSuccess &&
+        cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) == cudaSuccess &&
+        cudaFuncGetAttributes(&fa, (const void*)k_beam) == cudaSuccess && (size_t)optin > fa.sharedSizeBytes + 1024)
+        budget = (size_t)optin - fa.sharedSizeBytes - 1024;
+    cudaGetLastError();
     int mask = 0;
     size_t bytes = 0;
-    for (int part = 0; part < 4; ++part) {
+    for (int o = 0; o < BEAM_PARTS; ++o) {
+        const int part = beam_part_at(o);
         const size_t pb = beam_part_bytes(ns, part);
-        if (bytes + pb <= 216 * 1024) { mask |= 1 << part; bytes += pb; }
+        if (bytes + pb <= budget) { mask |= 1 << part; bytes += pb; }
     }
     if (mask && !raise_smem_limit((const void*)k_beam, bytes, &g_beam_smem)) mask = 0;
     return mask;

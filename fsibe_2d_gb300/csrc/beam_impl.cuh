@@ -104,44 +104,61 @@ __host__ __device__ inline size_t beam_vec_doubles(int ns) {
     return (d + 1) & ~(size_t)1;
 }
 __host__ __device__ inline size_t beam_band_doubles(int ns) { return (size_t)(2 * ns + 4 + 16) * 16; }
+// the FP32 LU factor (U rows of 16, L rows of 8), which the sequential chunk sweeps read
+__host__ __device__ inline size_t beam_lu_floats(int ns) { return (size_t)(2 * ns + 4 + 16) * 24; }
+// the rest of the factor: row exponents and the chunk-boundary responses E, F
 __host__ __device__ inline size_t beam_fact_floats(int ns) {
     const int n = 2 * ns + 4, C = beam_chunks(n);
-    return r4((size_t)(n + 16) * 25 + (size_t)C * (64 + 224));
+    return r4((size_t)(n + 16) + (size_t)C * (64 + 224));
 }
 __host__ __device__ inline size_t beam_scr_floats(int ns) {
     const int n = 2 * ns + 4, C = beam_chunks(n);
     return r4((size_t)C * 48 + 2 * (size_t)(n + 16));
 }
 __host__ __device__ inline size_t beam_bulk_floats(int ns) { return (size_t)(2 * ns + 4 + 16) * 24; }
-// bytes of each part, in the order scr, fact, vec, band
+// The workspace parts: 0 scr, 1 fact, 2 vec, 3 band, 4 lu (mask bit 1 << part)
+constexpr int BEAM_PARTS = 5;
 __host__ __device__ inline size_t beam_part_bytes(int ns, int part) {
     switch (part) {
         case 0: return 4 * beam_scr_floats(ns);
         case 1: return 4 * beam_fact_floats(ns);
         case 2: return 8 * beam_vec_doubles(ns);
-        default: return 8 * beam_band_doubles(ns);
+        case 3: return 8 * beam_band_doubles(ns);
+        default: return 4 * beam_lu_floats(ns);
     }
 }
+// The o-th part in the order in which parts are offered shared memory (and packed there): the
+// small scratch vectors, the LU factor of the sequential sweeps, the rest of the factor, the
+// FP64 vectors, the FP64 band
+__host__ __device__ constexpr int beam_part_at(int o) { return o == 0 ? 0 : (o == 1 ? 4 : o - 1); }
 
-struct BeamParts { double* vec; double* band; float* fact; float* scr; float* bulk; };
+struct BeamParts { double* vec; double* band; float* lu; float* fact; float* scr; float* bulk; };
 
-// Part addresses: those whose bit is set in mask (1 scr, 2 fact, 4 vec, 8 band) packed in
-// shared memory in that order, the rest at their place in the global copy
-// [vec | band | fact | scr | bulk].
+// Part addresses: those whose bit is set in mask packed in shared memory in beam_part_at order,
+// the rest at their place in the global copy [vec | band | lu | fact | scr | bulk].
 __device__ BeamParts beam_parts(double* gws, double* smem, int mask, int ns) {
     BeamParts P;
     double* g = gws;
     P.vec = g; g += beam_vec_doubles(ns);
     P.band = g; g += beam_band_doubles(ns);
     float* gf = reinterpret_cast<float*>(g);
+    P.lu = gf; gf += beam_lu_floats(ns);
     P.fact = gf; gf += beam_fact_floats(ns);
     P.scr = gf; gf += beam_scr_floats(ns);
     P.bulk = gf;
     char* sp = reinterpret_cast<char*>(smem);
-    if (mask & 1) { P.scr = reinterpret_cast<float*>(sp); sp += beam_part_bytes(ns, 0); }
-    if (mask & 2) { P.fact = reinterpret_cast<float*>(sp); sp += beam_part_bytes(ns, 1); }
-    if (mask & 4) { P.vec = reinterpret_cast<double*>(sp); sp += beam_part_bytes(ns, 2); }
-    if (mask & 8) { P.band = reinterpret_cast<double*>(sp); }
+    for (int o = 0; o < BEAM_PARTS; ++o) {
+        const int part = beam_part_at(o);
+        if (!(mask & (1 << part))) continue;
+        switch (part) {
+            case 0: P.scr = reinterpret_cast<float*>(sp); break;
+            case 1: P.fact = reinterpret_cast<float*>(sp); break;
+            case 2: P.vec = reinterpret_cast<double*>(sp); break;
+            case 3: P.band = reinterpret_cast<double*>(sp); break;
+            default: P.lu = reinterpret_cast<float*>(sp); break;
+        }
+        sp += beam_part_bytes(ns, part);
+    }
     return P;
 }
 
@@ -160,9 +177,9 @@ __device__ BeamWS carve(const BeamParts& P, int ns) {
     w.tf = reinterpret_cast<float*>(p); p += 3 * L;
     w.ipiv = reinterpret_cast<int*>(p);
     w.band = P.band;
+    w.Uf = P.lu;
+    w.Lf = P.lu + (size_t)(n + 16) * 16;
     float* f = P.fact;
-    w.Uf = f; f += (size_t)(n + 16) * 16;
-    w.Lf = f; f += (size_t)(n + 16) * 8;
     w.rse = reinterpret_cast<int*>(f); f += n + 16;
     w.Ec = f; f += (size_t)C * 64;
     w.Fc = f;
@@ -900,6 +917,9 @@ __device__ void band_precompute(const BeamWS& w, int n) {
 // between chunks (D_(c+1) = d_c + E_c D_c), the correction y += G D; then local back
 // substitutions with zero incoming state, the carry of the 14-value states from the last
 // chunk down (S_(c-1) = head_c + F_c S_c), and the correction x += H S.
+// chunk rows of the boundary-carry sweeps in flight ahead of their use
+constexpr int CARRY_PD = 4;
+
 __device__ __forceinline__ void band_solve_chunked(const BeamWS& w, int n, long long* sub) {
     const int C = w.nch, lane = threadIdx.x & 31;
     long long t0 = clock64();
@@ -918,9 +938,25 @@ __device__ __forceinline__ void band_solve_chunked(const BeamWS& w, int n, long 
     if (threadIdx.x < 8) {
         float Di = 0.f;
         w.cD[lane] = 0.f;
+        // the E rows of the next CARRY_PD chunks are in flight in a register ring (they do not
+        // depend on the carry; at large ns they live in global memory)
+        float4 ea[CARRY_PD], eb[CARRY_PD];
+#pragma unroll
+        for (int d = 0; d < CARRY_PD; ++d) {
+            ea[d] = eb[d] = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (d < C - 1) {
+                ea[d] = *reinterpret_cast<const float4*>(w.Ec + d * 64 + lane * 8);
+                eb[d] = *reinterpret_cast<const float4*>(w.Ec + d * 64 + lane * 8 + 4);
+            }
+        }
         for (int c = 0; c + 1 < C; ++c) {
-            const float4 e0 = *reinterpret_cast<const float4*>(w.Ec + c * 64 + lane * 8);
-            const float4 e1 = *reinterpret_cast<const float4*>(w.Ec + c * 64 + lane * 8 + 4);
+            const float4 e0 = ea[0], e1 = eb[0];
+#pragma unroll
+            for (int d = 0; d + 1 < CARRY_PD; ++d) { ea[d] = ea[d + 1]; eb[d] = eb[d + 1]; }
+            if (c + CARRY_PD < C - 1) {
+                ea[CARRY_PD - 1] = *reinterpret_cast<const float4*>(w.Ec + (c + CARRY_PD) * 64 + lane * 8);
+                eb[CARRY_PD - 1] = *reinterpret_cast<const float4*>(w.Ec + (c + CARRY_PD) * 64 + lane * 8 + 4);
+            }
             const float d0 = __shfl_sync(0xffu, Di, 0), d1 = __shfl_sync(0xffu, Di, 1), d2 = __shfl_sync(0xffu, Di, 2),
                         d3 = __shfl_sync(0xffu, Di, 3), d4 = __shfl_sync(0xffu, Di, 4), d5 = __shfl_sync(0xffu, Di, 5),
                         d6 = __shfl_sync(0xffu, Di, 6), d7 = __shfl_sync(0xffu, Di, 7);
@@ -969,8 +1005,24 @@ __device__ __forceinline__ void band_solve_chunked(const BeamWS& w, int n, long 
     if (threadIdx.x < 14) {
         float Si = 0.f;
         w.cS[(C - 1) * 16 + lane] = 0.f;
+        // the F rows of the next CARRY_PD chunks in a register ring, as the E rows above
+        float Fq[CARRY_PD][14];
+#pragma unroll
+        for (int d = 0; d < CARRY_PD; ++d)
+#pragma unroll
+            for (int j = 0; j < 14; ++j) Fq[d][j] = (C - 1 - d >= 1) ? w.Fc[(C - 1 - d) * 224 + lane * 16 + j] : 0.f;
         for (int c = C - 1; c >= 1; --c) {
-            const float* Fr = w.Fc + c * 224 + lane * 16;
+            float Fr[14];
+#pragma unroll
+            for (int j = 0; j < 14; ++j) Fr[j] = Fq[0][j];
+#pragma unroll
+            for (int d = 0; d + 1 < CARRY_PD; ++d)
+#pragma unroll
+                for (int j = 0; j < 14; ++j) Fq[d][j] = Fq[d + 1][j];
+            if (c - CARRY_PD >= 1) {
+#pragma unroll
+                for (int j = 0; j < 14; ++j) Fq[CARRY_PD - 1][j] = w.Fc[(c - CARRY_PD) * 224 + lane * 16 + j];
+            }
             float sv[14];
 #pragma unroll
             for (int j = 0; j < 14; ++j) sv[j] = __shfl_sync(0x3fffu, Si, j);

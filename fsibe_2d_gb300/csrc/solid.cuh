@@ -90,7 +90,7 @@ struct BeamArgs {
     BeamConsts k;
     double *x, *y, *vx, *vy, *th, *thd, *ax, *ay, *p_old, *p_new, *tau_old, *tau_new, *oo;
     double* ws;      // global workspace (used when the shared-memory workspace does not fit)
-    int use_smem;    // workspace parts in shared memory: 0 none, 1 FP32 factor, 2 + FP64 vectors, 3 + band
+    int use_smem;    // workspace parts in shared memory: bit 1 << part of beam_part_bytes' parts
     double* pred;    // predictor output (beam_pred_doubles)
     const double* d1d;  // Differentiate1D table (4 x 3 x 8 doubles, beam_d1d_table)
     double* rows;    // beam_data ring (21 per step) or nullptr
