@@ -173,6 +173,93 @@ __device__ __forceinline__ void block_fft_m(C2<R>* buf, int bstride, const C2<R>
     fft_run_m<R, N, INV, NB>(buf, bstride, tw, t);
 }
 
+// ---- transforms of values held in registers ------------------------------------------------
+// A thread of the G = N/8 owns elements t + m G (m < 8) of each of the NB sequences.  These are
+// exactly the inputs of its first-stage butterfly and the outputs of its last-stage
+// butterflies, so a transform whose inputs are computed in registers and whose outputs go to
+// registers needs shared memory only between stages: stages - 1 exchanges instead of a load and
+// a store per stage plus the staging in and out.  Each stage's arithmetic (twiddles, radix-P
+// butterfly, operation order) is that of fft_stage_m, so the results are bitwise the same.
+
+// The butterflies of one stage on v[b][q P + r] (input r of butterfly q, j = t + q G), b < NB
+// of the NBA rows of v.
+template <typename R, int N, int P, int NS, bool INV, int NB, int NBA>
+__device__ __forceinline__ void fft_reg_compute(C2<R> (&v)[NBA][8], const C2<R>* __restrict__ tw, int t) {
+    constexpr int G = N / 8, PER = 8 / P;
+#pragma unroll
+    for (int q = 0; q < PER; ++q) {
+        const int j = t + q * G;
+        const int k = j & (NS - 1);
+        if constexpr (NS > 1) {
+#pragma unroll
+            for (int r = 1; r < P; ++r) {
+                C2<R> w = __ldg(&tw[r * k * (N / (NS * P))]);
+                if (INV) w.y = -w.y;
+#pragma unroll
+                for (int b = 0; b < NB; ++b) v[b][q * P + r] = cmul<R>(v[b][q * P + r], w);
+            }
+        }
+#pragma unroll
+        for (int b = 0; b < NB; ++b) dftp<R, P, INV>(v[b] + q * P);
+    }
+}
+
+template <typename R, int N, bool INV, int NB, int NS, int NBA>
+__device__ __forceinline__ void fft_reg_run(C2<R> (&v)[NBA][8], C2<R>* buf, int bstride, const C2<R>* __restrict__ tw,
+                                            int t) {
+    constexpr int G = N / 8;
+    constexpr int P = (NS * 8 <= N) ? 8 : ((NS * 4 == N) ? 4 : 2), PER = 8 / P;
+    fft_reg_compute<R, N, P, NS, INV, NB, NBA>(v, tw, t);
+    if constexpr (NS * P < N) {
+        // outputs to their autosorted positions, then the next stage's inputs
+#pragma unroll
+        for (int q = 0; q < PER; ++q) {
+            const int j = t + q * G;
+            const int k = j & (NS - 1);
+            const int base = (j - k) * P + k;
+#pragma unroll
+            for (int b = 0; b < NB; ++b)
+#pragma unroll
+                for (int r = 0; r < P; ++r) buf[b * bstride + pad8(base + r * NS)] = v[b][q * P + r];
+        }
+        __syncthreads();
+        constexpr int NS2 = NS * P;
+        constexpr int P2 = (NS2 * 8 <= N) ? 8 : ((NS2 * 4 == N) ? 4 : 2), PER2 = 8 / P2, B2 = N / P2;
+#pragma unroll
+        for (int b = 0; b < NB; ++b)
+#pragma unroll
+            for (int q = 0; q < PER2; ++q)
+#pragma unroll
+                for (int r = 0; r < P2; ++r) v[b][q * P2 + r] = buf[b * bstride + pad8(t + q * G + r * B2)];
+        __syncthreads();  // every thread has its inputs before the buffer is written again
+        fft_reg_run<R, N, INV, NB, NS2, NBA>(v, buf, bstride, tw, t);
+    } else if constexpr (PER > 1) {
+        // the last stage's butterfly q, output r is element t + (q + PER r) G: element order
+#pragma unroll
+        for (int b = 0; b < NB; ++b) {
+            C2<R> o[8];
+#pragma unroll
+            for (int q = 0; q < PER; ++q)
+#pragma unroll
+                for (int r = 0; r < P; ++r) o[q + PER * r] = v[b][q * P + r];
+#pragma unroll
+            for (int m = 0; m < 8; ++m) v[b][m] = o[m];
+        }
+    }
+}
+
+// NB transforms of the sequences v[b][m] = element t + m (N/8), b < NB (of the NBA rows of v);
+// buf + b * bstride are NB padded shared-memory rows for the exchanges, free when this is
+// called (the caller synchronises after their last use); they are free again on return.  All
+// threads of the block call it.
+template <typename R, int N, bool INV, int NB, int NBA>
+__device__ __forceinline__ void block_fft_reg_m(C2<R> (&v)[NBA][8], C2<R>* buf, int bstride,
+                                                const C2<R>* __restrict__ tw, int t) {
+    static_assert(N >= 16 && (N & (N - 1)) == 0, "power-of-two length >= 16");
+    static_assert(NB >= 1 && NB <= NBA, "NB of the NBA rows");
+    fft_reg_run<R, N, INV, NB, 1, NBA>(v, buf, bstride, tw, t);
+}
+
 // ---- real <-> half-length complex split steps (x direction) -------------------------------
 // A real row x[0..2H) is handled as z[m] = x[2m] + i x[2m+1], m < H, transformed with a
 // length-H complex FFT.  twr[k] = exp(-2 pi i k / 2H), k <= H.

@@ -508,13 +508,14 @@ __global__ void __launch_bounds__(NY / 8, (nl_y_minb<R, NY>())) k_nl_y(KArgs<R> 
             cp_async16_f(preM + 2 * e, a.M + row + 2 * e);
         }
     }
+    // forward-y of A and B from registers (this thread's elements ky = t + q G) to registers
+    C2<R> fab[2][8];
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
-        bufA[pad8(t + q * G)] = a.A[row + t + q * G];
-        bufB[pad8(t + q * G)] = a.B[row + t + q * G];
+        fab[0][q] = a.A[row + t + q * G];
+        fab[1][q] = a.B[row + t + q * G];
     }
-    __syncthreads();
-    block_fft_m<R, NY, false, 2>(bufA, padded_len(NY), a.twY, t);  // bufA and bufB together
+    block_fft_reg_m<R, NY, false, 2>(fab, bufA, padded_len(NY), a.twY, t);  // A and B together
     if constexpr (kIsF32<R>) {
         cp_async_wait_f();
         __syncthreads();
@@ -532,7 +533,7 @@ __global__ void __launch_bounds__(NY / 8, (nl_y_minb<R, NY>())) k_nl_y(KArgs<R> 
         const int ka = ks < 0 ? -ks : ks;
         const bool nyq = (ky == NY / 2);
         const R kys = (R)ks * (R)g.kys;
-        const C2<R> fa = bufA[pad8(ky)], fb = bufB[pad8(ky)];
+        const C2<R> fa = fab[0][q], fb = fab[1][q];
         C2<R> N = csub<R>(fa, cimul<R>(fb, kys));
         N = cscale<R>(N, (R)norm);
         if (nyq) N = mk<R>(0, 0);
@@ -599,10 +600,12 @@ __global__ void __launch_bounds__(NY / 8, (nl_y_minb<R, NY>())) k_nl_y(KArgs<R> 
     };
     for (int o0 = 0; o0 < nout; o0 += NBO) {
         const int cnt = (nout - o0 < NBO) ? nout - o0 : NBO;
-        __syncthreads();
-        for (int b = 0; b < cnt; ++b) {
+        // the outputs' spectra in registers (this thread's ky = t + q G), transformed with the
+        // shared-memory rows as exchange buffers, stored from registers
+        C2<R> ov[NBO][8];
+#pragma unroll
+        for (int b = 0; b < NBO; ++b) {
             const int o = o0 + b;
-            C2<R>* buf = bufA + b * PLY;
 #pragma unroll
             for (int q = 0; q < 8; ++q) {
                 const int ky = t + q * G;
@@ -619,24 +622,25 @@ __global__ void __launch_bounds__(NY / 8, (nl_y_minb<R, NY>())) k_nl_y(KArgs<R> 
                     default: val = cscale<R>(ps[q], kxs * kxs - kys * kys); break;  // du/dy + dv/dx
                 }
                 if (ky == NY / 2) val = mk<R>(0, 0);
-                buf[pad8(ky)] = val;
+                ov[b][q] = val;
             }
         }
+        // the buffers are free: the state loop above read the prefetched rows (buffers C..E),
+        // and a previous round's transform ended synchronised
         __syncthreads();
         if (cnt == 4) {
-            if constexpr (NBO >= 4) block_fft_m<R, NY, true, 4>(bufA, PLY, a.twY, t);
+            if constexpr (NBO >= 4) block_fft_reg_m<R, NY, true, 4>(ov, bufA, PLY, a.twY, t);
         } else if (cnt == 3) {
-            if constexpr (NBO >= 3) block_fft_m<R, NY, true, 3>(bufA, PLY, a.twY, t);
+            if constexpr (NBO >= 3) block_fft_reg_m<R, NY, true, 3>(ov, bufA, PLY, a.twY, t);
         } else if (cnt == 2) {
-            block_fft_m<R, NY, true, 2>(bufA, PLY, a.twY, t);
+            block_fft_reg_m<R, NY, true, 2>(ov, bufA, PLY, a.twY, t);
         } else {
-            block_fft<R, NY, true>(bufA, a.twY, t);
+            block_fft_reg_m<R, NY, true, 1>(ov, bufA, PLY, a.twY, t);
         }
         for (int b = 0; b < cnt; ++b) {
             C2<R>* dst = out_ptr(o0 + b);
-            const C2<R>* buf = bufA + b * PLY;
 #pragma unroll
-            for (int q = 0; q < 8; ++q) dst[row + t + q * G] = buf[pad8(t + q * G)];
+            for (int q = 0; q < 8; ++q) dst[row + t + q * G] = ov[b][q];
         }
     }
 }
@@ -925,36 +929,34 @@ __global__ void __launch_bounds__(NY / 8, (kIsF32<R> && NY >= 4096) ? 2 : 1) k_p
     const int kx = blockIdx.x, t = threadIdx.x;
     const Geometry& g = a.g;
     const size_t row = (size_t)kx * NY;
+    // forward-y of P1 and P2 from registers (this thread's ky = t + q G) to registers
+    C2<R> fp[2][8];
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
-        bufA[pad8(t + q * G)] = a.P1[row + t + q * G];
-        bufB[pad8(t + q * G)] = a.P2[row + t + q * G];
+        fp[0][q] = a.P1[row + t + q * G];
+        fp[1][q] = a.P2[row + t + q * G];
     }
-    __syncthreads();
-    block_fft_m<R, NY, false, 2>(bufA, padded_len(NY), a.twY, t);  // bufA and bufB together
+    block_fft_reg_m<R, NY, false, 2>(fp, bufA, padded_len(NY), a.twY, t);  // P1 and P2 together
     const R norm = (R)(1.0 / ((double)g.nx * (double)g.ny));
-    C2<R> qv[8];
+    C2<R> qv[1][8];
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
         const int ky = t + q * G;
         const int ks = signed_k(ky, NY);
         const R kys = (R)ks * (R)g.kys;
-        C2<R> Q = cadd<R>(cscale<R>(bufA[pad8(ky)], norm), cimul<R>(cscale<R>(bufB[pad8(ky)], norm), kys));
+        C2<R> Q = cadd<R>(cscale<R>(fp[0][q], norm), cimul<R>(cscale<R>(fp[1][q], norm), kys));
         const R k2 = (R)(kx * kx) * (R)g.scalex + (R)(ks * ks) * (R)g.scaley;
         C2<R> qh;
         if (kx == 0 && ky == 0) qh = mk<R>(0, 0);
         else if constexpr (kIsF32<R>) qh = cscale<R>(Q, (R)1 / k2);
         else qh = mk<R>(Q.x / k2, Q.y / k2);
         if (ky == NY / 2) qh = mk<R>(0, 0);
-        qv[q] = qh;
+        qv[0][q] = qh;
     }
-    __syncthreads();
+    // inverse-y of q from registers to registers (the forward transform left bufA free)
+    block_fft_reg_m<R, NY, true, 1>(qv, bufA, padded_len(NY), a.twY, t);
 #pragma unroll
-    for (int q = 0; q < 8; ++q) bufA[pad8(t + q * G)] = qv[q];
-    __syncthreads();
-    block_fft<R, NY, true>(bufA, a.twY, t);
-#pragma unroll
-    for (int q = 0; q < 8; ++q) a.Tq[row + t + q * G] = bufA[pad8(t + q * G)];
+    for (int q = 0; q < 8; ++q) a.Tq[row + t + q * G] = qv[0][q];
 }
 
 // K6: inverse-x of q, p = q - |u|^2/2
