@@ -158,6 +158,36 @@ __device__ __forceinline__ void row_r2c_m(C2<R>* rb, int bstride, const C2<R>* _
     r2c_split_m<R, H, NB>(rb, bstride, twR, t);
 }
 
+// row_c2r_m with the transform's output in registers: v[b][q] = element t + q (H/8) of row b
+// (the row buffers are free on return).  The merge runs in shared memory, the transform's
+// stages exchange through it; the arithmetic is row_c2r_m's.
+template <typename R, int H, int NB, int NBA>
+__device__ __forceinline__ void row_c2r_reg(C2<R>* rb, int bstride, const C2<R>* __restrict__ twR,
+                                            const C2<R>* __restrict__ twX, int t, C2<R> (&v)[NBA][8]) {
+    constexpr int G = H / 8;
+    c2r_merge_m<R, H, NB>(rb, bstride, twR, t);
+#pragma unroll
+    for (int b = 0; b < NB; ++b)
+#pragma unroll
+        for (int q = 0; q < 8; ++q) v[b][q] = rb[b * bstride + pad8(t + q * G)];
+    __syncthreads();
+    block_fft_reg_m<R, H, true, NB>(v, rb, bstride, twX, t);
+}
+// row_r2c_m of rows given in registers (v[b][q] = element t + q (H/8)); the rows must be free
+// (synchronised after their last use).  The result is in the row buffers, as from row_r2c_m.
+template <typename R, int H, int NB, int NBA>
+__device__ __forceinline__ void row_r2c_reg(C2<R> (&v)[NBA][8], C2<R>* rb, int bstride, const C2<R>* __restrict__ twR,
+                                            const C2<R>* __restrict__ twX, int t) {
+    constexpr int G = H / 8;
+    block_fft_reg_m<R, H, false, NB>(v, rb, bstride, twX, t);
+#pragma unroll
+    for (int b = 0; b < NB; ++b)
+#pragma unroll
+        for (int q = 0; q < 8; ++q) rb[b * bstride + pad8(t + q * G)] = v[b][q];
+    __syncthreads();
+    r2c_split_m<R, H, NB>(rb, bstride, twR, t);
+}
+
 template <typename R>
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
@@ -364,13 +394,14 @@ __global__ void __launch_bounds__(XRows<R, H, TRV>::THREADS) k_nl_x(KArgs<R> a) 
             if (i < nout) av[u] = a.A[(size_t)(i / X::TR) * ny + iy0 + i % X::TR];
         }
     }
+    C2<R> dxy[2][8];  // the vorticity's x and y derivatives at this thread's elements
     if (part != NL_PENAL) {
         // after the first AB2/Euler update the vorticity is dealiased: rows kx >= kcut are zero
         const int kin = a.explicit_step ? H : a.kcut;
         load_tileT<R, H, X::TR, X::PL>(bufA, a.Tdx, ny, iy0, kin);
         load_tileT<R, H, X::TR, X::PL>(bufB, a.Tdy, ny, iy0, kin);
         __syncthreads();
-        row_c2r_m<R, H, 2>(ra, BS, a.twR, a.twX, t);  // ra and rb together
+        row_c2r_reg<R, H, 2>(ra, BS, a.twR, a.twX, t, dxy);  // both together, to registers
     }
     const int iy = iy0 + r;
     const size_t roff = (size_t)iy * H;
@@ -380,6 +411,8 @@ __global__ void __launch_bounds__(XRows<R, H, TRV>::THREADS) k_nl_x(KArgs<R> a) 
     const C2<R>* x2 = reinterpret_cast<const C2<R>*>(a.mvx) + roff;
     const C2<R>* y2 = reinterpret_cast<const C2<R>*>(a.mvy) + roff;
     const bool adv = part != NL_PENAL, pen = part != NL_ADVECT && a.penalize;
+    // the rows to forward-transform: WHOLE w, pen_y, pen_x; ADVECT w; PENAL pen_y, pen_x
+    C2<R> fw[3][8];
     C2<R> wv[8], pyv[8], pxv[8];
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
@@ -391,7 +424,7 @@ __global__ void __launch_bounds__(XRows<R, H, TRV>::THREADS) k_nl_x(KArgs<R> a) 
             vv = mk<R>(vv.x + Vc, vv.y + Vc);
         }
         if (adv) {
-            const C2<R> dx = ra[pad8(m)], dy = rb[pad8(m)];
+            const C2<R> dx = dxy[0][q], dy = dxy[1][q];
             wv[q] = mk<R>(-uu.x * dx.x - vv.x * dy.x, -uu.y * dx.y - vv.y * dy.y);
         }
         if (pen) {
@@ -403,38 +436,27 @@ __global__ void __launch_bounds__(XRows<R, H, TRV>::THREADS) k_nl_x(KArgs<R> a) 
             pyv[q] = mk<R>(0, 0);
         }
     }
-    if (adv) __syncthreads();
-    if (part == NL_WHOLE) {
+    // the row buffers are free (the inverse transform returned them so; the penalization part
+    // used none)
+    if constexpr (PART == NL_WHOLE) {
 #pragma unroll
-        for (int q = 0; q < 8; ++q) {
-            const int m = t + q * X::G;
-            ra[pad8(m)] = wv[q];
-            rb[pad8(m)] = pyv[q];
-            rc[pad8(m)] = pxv[q];
-        }
-        __syncthreads();
-        row_r2c_m<R, H, 3>(ra, BS, a.twR, a.twX, t);  // ra, rb and rc together
-    } else if (part == NL_ADVECT) {
+        for (int q = 0; q < 8; ++q) { fw[0][q] = wv[q]; fw[1][q] = pyv[q]; fw[2][q] = pxv[q]; }
+        row_r2c_reg<R, H, 3>(fw, ra, BS, a.twR, a.twX, t);  // into buffers A, B and C together
+    } else if constexpr (PART == NL_ADVECT) {
 #pragma unroll
-        for (int q = 0; q < 8; ++q) ra[pad8(t + q * X::G)] = wv[q];
-        __syncthreads();
-        row_r2c_m<R, H, 1>(ra, BS, a.twR, a.twX, t);
+        for (int q = 0; q < 8; ++q) fw[0][q] = wv[q];
+        row_r2c_reg<R, H, 1>(fw, ra, BS, a.twR, a.twX, t);
     } else {
-        // the penalization's y and x components in the buffers A and B (the whole kernel's B
-        // and C)
+        // the penalization's y and x components into the buffers A and B (the whole kernel's
+        // B and C)
 #pragma unroll
-        for (int q = 0; q < 8; ++q) {
-            const int m = t + q * X::G;
-            ra[pad8(m)] = pyv[q];
-            rb[pad8(m)] = pxv[q];
-        }
-        __syncthreads();
-        row_r2c_m<R, H, 2>(ra, BS, a.twR, a.twX, t);
+        for (int q = 0; q < 8; ++q) { fw[0][q] = pyv[q]; fw[1][q] = pxv[q]; }
+        row_r2c_reg<R, H, 2>(fw, ra, BS, a.twR, a.twX, t);
     }
     // the right-hand side only matters where the update keeps modes (kx < kcut):
     // A = X(w) + i kx X(pen_y), B = X(pen_x); the advection part writes X(w) and a zero B,
     // the penalization part adds its terms to that
-    if (part == NL_PENAL) {
+    if constexpr (PART == NL_PENAL) {
 #pragma unroll
         for (int u = 0; u < NLA; ++u) {
             const int i = threadIdx.x + u * blockDim.x;
@@ -446,19 +468,19 @@ __global__ void __launch_bounds__(XRows<R, H, TRV>::THREADS) k_nl_x(KArgs<R> a) 
                 a.B[o] = bufB[rr * X::PL + pad8(kx)];
             }
         }
-        return;
-    }
-    for (int i = threadIdx.x; i < nout; i += blockDim.x) {
-        const int rr = i % X::TR, kx = i / X::TR;
-        const size_t o = (size_t)kx * ny + iy0 + rr;
-        const C2<R> xa = bufA[rr * X::PL + pad8(kx)];
-        if (part == NL_WHOLE) {
-            const R kxs = (R)((double)kx * a.g.kxs);
-            a.A[o] = cadd<R>(xa, cimul<R>(bufB[rr * X::PL + pad8(kx)], kxs));
-            a.B[o] = bufC[rr * X::PL + pad8(kx)];
-        } else {
-            a.A[o] = xa;
-            a.B[o] = mk<R>(0, 0);
+    } else {
+        for (int i = threadIdx.x; i < nout; i += blockDim.x) {
+            const int rr = i % X::TR, kx = i / X::TR;
+            const size_t o = (size_t)kx * ny + iy0 + rr;
+            const C2<R> xa = bufA[rr * X::PL + pad8(kx)];
+            if constexpr (PART == NL_WHOLE) {
+                const R kxs = (R)((double)kx * a.g.kxs);
+                a.A[o] = cadd<R>(xa, cimul<R>(bufB[rr * X::PL + pad8(kx)], kxs));
+                a.B[o] = bufC[rr * X::PL + pad8(kx)];
+            } else {
+                a.A[o] = xa;
+                a.B[o] = mk<R>(0, 0);
+            }
         }
     }
 }
@@ -677,12 +699,14 @@ __global__ void __launch_bounds__(XRows<R, H, TRV>::THREADS, (sizeof(R) == 4) ? 
     load_tileT<R, H, X::TR, X::PL>(bufB, a.Tv, ny, iy0, a.kcut);
     load_tileT<R, H, X::TR, X::PL>(bufC, a.Tw, ny, iy0, a.kcut);
     __syncthreads();
-    row_c2r_m<R, H, 3>(ra, BS, a.twR, a.twX, t);  // u, v and omega together
+    // u, v and omega together, this thread's elements m = t + q G to registers (the row buffers
+    // are free afterwards)
+    C2<R> uvw[3][8];
+    row_c2r_reg<R, H, 3>(ra, BS, a.twR, a.twX, t, uvw);
     C2<R> uv[8], vv[8], wv[8];
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
-        const int m = t + q * X::G;
-        const C2<R> ur = ra[pad8(m)], vr = rb[pad8(m)];
+        const C2<R> ur = uvw[0][q], vr = uvw[1][q];
         if constexpr (kIsF32<R>) {   // keep the raw perturbation; the mean is added in the FP32 path
             uv[q] = ur;
             vv[q] = mk<R>(-vr.x, -vr.y);
@@ -690,10 +714,9 @@ __global__ void __launch_bounds__(XRows<R, H, TRV>::THREADS, (sizeof(R) == 4) ? 
             uv[q] = mk<R>(ur.x + U, ur.y + U);
             vv[q] = mk<R>(-vr.x + V, -vr.y + V);
         }
+        wv[q] = uvw[2][q];
     }
-#pragma unroll
-    for (int q = 0; q < 8; ++q) wv[q] = rc[pad8(t + q * X::G)];
-    __syncthreads();
+    C2<R> pxy[2][8];  // the pressure right-hand side's x and y parts, for the forward transform
 
     const int iy = iy0 + r;
     const size_t roff = (size_t)iy * H;
@@ -753,8 +776,8 @@ __global__ void __launch_bounds__(XRows<R, H, TRV>::THREADS, (sizeof(R) == 4) ? 
                 py[e] = peny + wc[e] * uc;
             }
             vm2[m] = mk<R>(vmn[0], vmn[1]);
-            ra[pad8(m)] = mk<R>(px[0], px[1]);
-            rb[pad8(m)] = mk<R>(py[0], py[1]);
+            pxy[0][q] = mk<R>(px[0], px[1]);
+            pxy[1][q] = mk<R>(py[0], py[1]);
         }
         // the FP32 partials go to the spare row buffer; the block reduces them in FP64 below
         float* cols = reinterpret_cast<float*>(bufC);
@@ -800,8 +823,8 @@ __global__ void __launch_bounds__(XRows<R, H, TRV>::THREADS, (sizeof(R) == 4) ? 
             py[e] = peny + wc[e] * uc[e];
         }
         vm2[m] = mk<R>(vmn[0], vmn[1]);
-        ra[pad8(m)] = mk<R>(px[0], px[1]);
-        rb[pad8(m)] = mk<R>(py[0], py[1]);
+        pxy[0][q] = mk<R>(px[0], px[1]);
+        pxy[1][q] = mk<R>(py[0], py[1]);
     }
     }
     // block reduction in a fixed order: every thread's partials go to the spare row buffer as
@@ -841,7 +864,7 @@ __global__ void __launch_bounds__(XRows<R, H, TRV>::THREADS, (sizeof(R) == 4) ? 
         if (blockIdx.x == 0 && s == 0) a.S->nred = (int)gridDim.x;
     }
     if (a.pressure_on) {
-        row_r2c_m<R, H, 2>(ra, BS, a.twR, a.twX, t);  // ra and rb together
+        row_r2c_reg<R, H, 2>(pxy, ra, BS, a.twR, a.twX, t);  // x and y parts together
         for (int i = threadIdx.x; i < H * X::TR; i += blockDim.x) {
             const int rr = i % X::TR, kx = i / X::TR;
             const R kxs = (R)((double)kx * a.g.kxs);
@@ -904,7 +927,8 @@ __global__ void __launch_bounds__(XRows<R, H, TRV>::THREADS) k_stress_x(KArgs<R>
     load_tileT<R, H, X::TR, X::PL>(bufA, a.Tsa, ny, iy0, a.kcut);
     load_tileT<R, H, X::TR, X::PL>(bufB, a.Tsb, ny, iy0, a.kcut);
     __syncthreads();
-    row_c2r_m<R, H, 2>(ra, BS, a.twR, a.twX, t);  // ra and rb together
+    C2<R> sv[2][8];
+    row_c2r_reg<R, H, 2>(ra, BS, a.twR, a.twX, t, sv);  // both together, to registers
     const size_t roff = (size_t)(iy0 + r) * H;
     C2<R>* sa2 = reinterpret_cast<C2<R>*>(a.sa) + roff;
     C2<R>* sb2 = reinterpret_cast<C2<R>*>(a.sb) + roff;
@@ -912,7 +936,7 @@ __global__ void __launch_bounds__(XRows<R, H, TRV>::THREADS) k_stress_x(KArgs<R>
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
         const int m = t + q * X::G;
-        const C2<R> x = ra[pad8(m)], y = rb[pad8(m)];
+        const C2<R> x = sv[0][q], y = sv[1][q];
         sa2[m] = mk<R>(c2 * x.x, c2 * x.y);
         sb2[m] = mk<R>(c1 * y.x, c1 * y.y);
     }
@@ -979,11 +1003,12 @@ __global__ void __launch_bounds__(XRows<R, H, TRV>::THREADS) k_press_fin(KArgs<R
     for (int q = 0; q < 8; ++q) { ul[q] = u2[t + q * X::G]; vl[q] = v2[t + q * X::G]; }
     load_tileT<R, H, X::TR, X::PL>(buf, a.Tq, ny, iy0);
     __syncthreads();
-    row_c2r<R, H>(rb, a.twR, a.twX, t);
+    C2<R> qv[1][8];
+    row_c2r_reg<R, H, 1>(rb, X::PL, a.twR, a.twX, t, qv);  // to registers
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
         const int m = t + q * X::G;
-        const C2<R> qq = rb[pad8(m)];
+        const C2<R> qq = qv[0][q];
         C2<R> uu = ul[q], vq = vl[q];
         if constexpr (kIsF32<R>) {
             // the velocity press_x stored holds the mean flow at time + dt1 (mean_u_next; the
