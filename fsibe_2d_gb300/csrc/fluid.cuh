@@ -57,8 +57,8 @@ template <typename R> constexpr bool kIsF32 = std::is_same<R, float>::value;
 // the penalization part then adds the mask's term on the rows of the mask's box alone
 // (outside it the mask and the penalization are zero).
 enum { NL_WHOLE = 0, NL_ADVECT = 1, NL_PENAL = 2 };
-// shared-memory row buffers of k_nl_y: four inverse transforms at a time in FP32 (and a fifth
-// buffer for the prefetched state), two in FP64
+// shared-memory row buffers of k_nl_y: in FP32 two for the forward transforms and three for the
+// prefetched state, then all five for the inverse transforms; two in FP64
 template <typename R> constexpr int nl_y_bufs() { return kIsF32<R> ? 5 : 2; }
 
 // 16-byte asynchronous global -> shared copies (the copy engine fills shared memory while the
@@ -603,45 +603,46 @@ __global__ void __launch_bounds__(NY / 8, (nl_y_minb<R, NY>())) k_nl_y(KArgs<R> 
         else if constexpr (kIsF32<R>) ps[q] = cscale<R>(Wn, (R)1 / k2);
         else ps[q] = mk<R>(Wn.x / k2, Wn.y / k2);   // poisson.f90:159-162 divides
     }
-    // inverse-y outputs, NBO at a time: their transforms share the stages' synchronisations
-    // and twiddle loads (NBO buffers of shared memory)
-    constexpr int NBO = kIsF32<R> ? 4 : 2;  // inverse transforms at a time (the fifth FP32 buffer holds the prefetched state)
+    // inverse-y outputs, NBO at a time: their transforms share the stages' synchronisations and
+    // twiddle loads (NBO buffers of shared memory).  In the FP32 form the factor i kx, constant
+    // along a kx row, is applied after the transform where that saves one: cofdx(omega) =
+    // i kx T(omega) and d2psi/dxdy = i kx T(cofdy psi), so five spectra are transformed (cofdy
+    // psi, cofdx psi, omega, cofdy omega, (kx^2 - ky^2) psi).  The FP64 form transforms all seven
+    // in the reference's order (cofdx, then cofitxy), which keeps its roundings those of the
+    // operators its adjoint transposes.
+    // transforms at a time: the five FP32 buffers (the prefetched state they held is consumed),
+    // so the FP32 form's five spectra take one round; two in FP64
+    constexpr int NBO = kIsF32<R> ? 5 : 2;
+    static_assert(NBO <= nl_y_bufs<R>(), "one shared-memory row buffer per transform");
     constexpr int PLY = padded_len(NY);
     const R kxs = (R)kx * (R)g.kxs;
-    const int nout = a.viscous ? 7 : 5;
-    auto out_ptr = [&](int o) -> C2<R>* {
-        switch (o) {
-            case 0: return a.Tu;
-            case 1: return a.Tv;
-            case 2: return a.Tw;
-            case 3: return a.Tdx;
-            case 4: return a.Tdy;
-            case 5: return a.Tsa;
-            default: return a.Tsb;
-        }
-    };
-    for (int o0 = 0; o0 < nout; o0 += NBO) {
-        const int cnt = (nout - o0 < NBO) ? nout - o0 : NBO;
-        // the outputs' spectra in registers (this thread's ky = t + q G), transformed with the
+    // spectra: 0 cofdy psi, 1 cofdx psi, 2 omega, 3 cofdy omega, 4 (kx^2 - ky^2) psi, and in
+    // the FP64 form 5 cofdx omega, 6 d2psi/dxdy
+    const int ntr = kIsF32<R> ? (a.viscous ? 5 : 4) : (a.viscous ? 7 : 5);
+    for (int s0 = 0; s0 < ntr; s0 += NBO) {
+        const int cnt = (ntr - s0 < NBO) ? ntr - s0 : NBO;
+        // the spectra in registers (this thread's ky = t + q G), transformed with the
         // shared-memory rows as exchange buffers, stored from registers
         C2<R> ov[NBO][8];
 #pragma unroll
         for (int b = 0; b < NBO; ++b) {
-            const int o = o0 + b;
+            const int sp = s0 + b;
 #pragma unroll
             for (int q = 0; q < 8; ++q) {
                 const int ky = t + q * G;
                 const int ks = signed_k(ky, NY);
                 const R kys = (R)ks * (R)g.kys;
                 C2<R> val;
-                switch (o) {
+                // (FP64 without the stresses: spectra 0..3 and 5; sp 4 stands for 5 there)
+                const int spk = (!kIsF32<R> && !a.viscous && sp == 4) ? 5 : sp;
+                switch (spk) {
                     case 0: val = cimul<R>(ps[q], kys); break;                 // cofdy(psi)   -> u
                     case 1: val = cimul<R>(ps[q], kxs); break;                 // cofdx(psi)   -> -v
                     case 2: val = wn[q]; break;                                // omega
-                    case 3: val = cimul<R>(wn[q], kxs); break;                 // cofdx(omega)
-                    case 4: val = cimul<R>(wn[q], kys); break;                 // cofdy(omega)
-                    case 5: val = cscale<R>(ps[q], -(kxs * kys)); break;       // d2psi/dxdy = du/dx
-                    default: val = cscale<R>(ps[q], kxs * kxs - kys * kys); break;  // du/dy + dv/dx
+                    case 3: val = cimul<R>(wn[q], kys); break;                 // cofdy(omega)
+                    case 4: val = cscale<R>(ps[q], kxs * kxs - kys * kys); break;  // du/dy + dv/dx
+                    case 5: val = cimul<R>(wn[q], kxs); break;                 // cofdx(omega)
+                    default: val = cscale<R>(ps[q], -(kxs * kys)); break;      // d2psi/dxdy = du/dx
                 }
                 if (ky == NY / 2) val = mk<R>(0, 0);
                 ov[b][q] = val;
@@ -650,7 +651,9 @@ __global__ void __launch_bounds__(NY / 8, (nl_y_minb<R, NY>())) k_nl_y(KArgs<R> 
         // the buffers are free: the state loop above read the prefetched rows (buffers C..E),
         // and a previous round's transform ended synchronised
         __syncthreads();
-        if (cnt == 4) {
+        if (cnt == 5) {
+            if constexpr (NBO >= 5) block_fft_reg_m<R, NY, true, 5>(ov, bufA, PLY, a.twY, t);
+        } else if (cnt == 4) {
             if constexpr (NBO >= 4) block_fft_reg_m<R, NY, true, 4>(ov, bufA, PLY, a.twY, t);
         } else if (cnt == 3) {
             if constexpr (NBO >= 3) block_fft_reg_m<R, NY, true, 3>(ov, bufA, PLY, a.twY, t);
@@ -660,9 +663,18 @@ __global__ void __launch_bounds__(NY / 8, (nl_y_minb<R, NY>())) k_nl_y(KArgs<R> 
             block_fft_reg_m<R, NY, true, 1>(ov, bufA, PLY, a.twY, t);
         }
         for (int b = 0; b < cnt; ++b) {
-            C2<R>* dst = out_ptr(o0 + b);
+            const int sp = s0 + b;
+            const int spk = (!kIsF32<R> && !a.viscous && sp == 4) ? 5 : sp;
+            C2<R>* dst = (spk == 0) ? a.Tu : (spk == 1) ? a.Tv : (spk == 2) ? a.Tw : (spk == 3) ? a.Tdy
+                       : (spk == 4) ? a.Tsb : (spk == 5) ? a.Tdx : a.Tsa;
+            // FP32: the outputs i kx times a transformed one, cofdx(omega) = i kx Tw and
+            // du/dx = i kx Tu
+            C2<R>* dst2 = !kIsF32<R> ? nullptr : (sp == 2) ? a.Tdx : (sp == 0 && a.viscous) ? a.Tsa : nullptr;
 #pragma unroll
-            for (int q = 0; q < 8; ++q) dst[row + t + q * G] = ov[b][q];
+            for (int q = 0; q < 8; ++q) {
+                dst[row + t + q * G] = ov[b][q];
+                if (dst2) dst2[row + t + q * G] = cimul<R>(ov[b][q], kxs);
+            }
         }
     }
 }
