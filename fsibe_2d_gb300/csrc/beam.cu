@@ -283,7 +283,7 @@ __global__ void __launch_bounds__(256) k_beam(BeamArgs b) {
                     band_solve_chunked(w, n, ph + 16);
                     PH(12);
                     ++solves;
-                    const int rs = refine_step(w.xdi, w.yf, n, pass, cprev, &red[2][0], iter + 1 > 2 ? 0x1p-44 : 0x1p-30);
+                    const int rs = refine_step(w.xdi, w.yf, n, pass, cprev, &red[2][0], 0x1p-30);
                     PH(13);
                     if (rs != 0) { ok = rs > 0; break; }
                 }

@@ -515,8 +515,8 @@ __global__ void __launch_bounds__(256, 1) k_beam_cl(BeamArgs b) {
                         const float cpf = (pass == 0) ? 0.f : cprev_s;
                         const double cmd = (double)__uint_as_float((unsigned)c2), cpd = (double)cpf;
                         const double xmd = __longlong_as_double((long long)x2);
-                        // 2^-30 in the two iterations without a stopping test (refine_step)
-                        const double tol = (iter + 1 > 2 ? 0x1p-44 : 0x1p-30) * xmd;
+                        // 2^-30 of the correction (refine_step says why that suffices)
+                        const double tol = 0x1p-30 * xmd;
                         const bool conv = !(cmd > tol) || (pass >= 1 && cmd * cmd <= tol * cpd);
                         const bool stall = pass >= 2 && cmd > 0.5 * cpd;
                         cprev_s = __uint_as_float((unsigned)c2);

@@ -215,10 +215,11 @@ __device__ void solid_coeffs(int method, double dt, double dt_old, double& C1, d
 // at the FP64 residual's rounding floor below 2^-30), -1 on a failure (10 passes, or a stall
 // above that floor), 0 to go on.  rbuf: 16 doubles of shared memory.
 //
-// The beam's Newton iteration passes tscale = 2^-30 in its first two iterations, which make no
-// stopping test: Newton's map is flat at the root, so the 2^-30-relative error these solves
-// leave in the second iterate moves the third by O(|x_2 - x*| 2^-30 |dx_2|), far below the
-// rounding of FP64 (and its stopping test, on dx_3 = x* - x_2, by the same 2^-30 |dx_2|).
+// The beam's Newton iteration passes tscale = 2^-30: a solve's error enters the iterate as
+// 2^-30 |dx_k|.  Before convergence Newton's map is flat at the root, so that moves the next
+// iterate by O(|x_k - x*| 2^-30 |dx_k|); in the last iteration |dx_k| is below the Newton
+// tolerance, so the error is below FP64 rounding of the solution (the stopping test on |dx_k|
+// moves by the same relative 2^-30).
 __device__ int refine_step(double* x, const float* cf, int n, int pass, float& cprev, double* rbuf,
                            double tscale = 0x1p-44) {
     unsigned cm = 0;
