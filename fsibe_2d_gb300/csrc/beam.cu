@@ -249,7 +249,7 @@ __global__ void __launch_bounds__(256) k_beam(BeamArgs b) {
             if (flag) { if (threadIdx.x == 0) set_status(S, flag); return; }
             PH(4);
             // J dx = -F: FP32 LU of the row-scaled band as the preconditioner of an FP64
-            // iterative refinement, run to the accuracy of an FP64 factorisation.  The factor is
+            // iterative refinement, run to 2^-30 of the correction (refine_step).  The factor is
             // kept across Newton iterations and steps while it still contracts fast (<= 5
             // solves); a stale factor that stops converging is replaced and the solve redone.
             int solves = 0;

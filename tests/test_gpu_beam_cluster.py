@@ -1,9 +1,9 @@
 """The two forms of the beam's Newton kernel: the thread-block cluster form (16 or 8 CTAs,
 the default on a device that places the cluster) and the single-CTA form
 (FSIBE_BEAM_CLUSTER=0).  Both run FP64 Newton with an FP32-preconditioned FP64 iterative
-refinement to 2^-44; they differ only in the preconditioner's application (inverse rows
-against triangular solves), so they agree to refinement rounding, far inside the 1e-10 bar
-that both meet against the oracle."""
+refinement to 2^-30 of the correction; they differ only in the preconditioner's application
+(inverse rows against triangular solves), so they agree to refinement rounding, far inside
+the 1e-10 bar that both meet against the oracle."""
 import numpy as np
 import pytest
 
