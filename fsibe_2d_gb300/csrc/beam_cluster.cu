@@ -657,75 +657,60 @@ __global__ void __launch_bounds__(256, 1) k_beam_cl(BeamArgs b) {
     }
     __syncthreads();
     PH(8);
+    // positions and velocities, and in the same pass each thread's terms of the emergency brake
+    // (SolidSolver.f90:370-380) and of SolidEnergies (SolidSolver.f90:76-92); the block then
+    // reduces the six columns in FP64, one warp a column
     {
+        __shared__ double ecol[6][256];
+        static_assert(256 >= 32 * 6, "one warp a column");
         const double* pre = pcs + 4 * L;
         const double ca = b.cos_a, sa = b.sin_a, alpha_t = 0.0, idt = 1.0 / dt;
+        double sk = 0, sp = 0, se = 0, sax = 0, say = 0, mx = 0;
         for (int i = tid; i < ns; i += nthr) {
             const double xrel = pre[i], yrel = pre[L + i];
             const double vxrel = pre[2 * L + i], vyrel = pre[3 * L + i];
+            const double yi = b.y0 + yrel * ca + xrel * sa;
             b.x[i] = b.x0 + xrel * ca - yrel * sa;
-            b.y[i] = b.y0 + yrel * ca + xrel * sa;
+            b.y[i] = yi;
             const double vx = 0.0 + ca * (vxrel - alpha_t * yrel) - sa * (vyrel + alpha_t * xrel);
             const double vy = 0.0 + ca * (vyrel + alpha_t * xrel) + sa * (vxrel - alpha_t * yrel);
             b.vx[i] = vx;
             b.vy[i] = vy;
+            double ax, ay;
             if (released) {
-                b.ax[i] = (vx - bo3[i]) * idt;
-                b.ay[i] = (vy - bo4[i]) * idt;
+                ax = (vx - bo3[i]) * idt;
+                ay = (vy - bo4[i]) * idt;
+                b.ax[i] = ax;
+                b.ay[i] = ay;
+                mx = fmax(mx, fabs(tdv[i] - bo6[i]));
+            } else {
+                ax = b.ax[i];
+                ay = b.ay[i];
             }
-        }
-    }
-    __syncthreads();
-    // emergency brake (SolidSolver.f90:370-380)
-    if (released) {
-        double mx = 0.0;
-        for (int i = tid; i < ns; i += nthr) mx = fmax(mx, fabs(tdv[i] - bo6[i]));
-        for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-        if (lane == 0) red[0][warp] = mx;
-        __syncthreads();
-        if (tid == 0) {
-            double m = 0.0;
-            for (int q = 0; q < nwarp; ++q) m = fmax(m, red[0][q]);
-            if (m > 100.0) set_status(S, FSIBE_ERR_BRAKE);
-        }
-        __syncthreads();
-    }
-    // SolidEnergies (SolidSolver.f90:76-92) as block reductions
-    {
-        __shared__ double esum[5][8];
-        double sk = 0, sp = 0, se = 0, sax = 0, say = 0;
-        for (int i = tid; i < ns; i += nthr) {
             const double th_s = d1d(&dtab, thv, ns, 1, i);
-            const double vx = b.vx[i], vy = b.vy[i];
             sk += vx * vx + vy * vy;
-            sp += b.y[i] - b.y0;
+            sp += yi - b.y0;
             se += th_s * th_s;
-            sax += b.ax[i];
-            say += b.ay[i];
+            sax += ax;
+            say += ay;
         }
-        for (int o = 16; o > 0; o >>= 1) {
-            sk += __shfl_xor_sync(0xffffffffu, sk, o);
-            sp += __shfl_xor_sync(0xffffffffu, sp, o);
-            se += __shfl_xor_sync(0xffffffffu, se, o);
-            sax += __shfl_xor_sync(0xffffffffu, sax, o);
-            say += __shfl_xor_sync(0xffffffffu, say, o);
-        }
-        if (lane == 0) { esum[0][warp] = sk; esum[1][warp] = sp; esum[2][warp] = se; esum[3][warp] = sax; esum[4][warp] = say; }
+        ecol[0][tid] = sk; ecol[1][tid] = sp; ecol[2][tid] = se;
+        ecol[3][tid] = sax; ecol[4][tid] = say; ecol[5][tid] = mx;
         __syncthreads();
-        if (tid < 32) {
-            double v[5];
-#pragma unroll
-            for (int q = 0; q < 5; ++q) v[q] = (lane < nwarp) ? esum[q][lane] : 0.0;
-#pragma unroll
-            for (int o = 4; o > 0; o >>= 1)
-#pragma unroll
-                for (int q = 0; q < 5; ++q) v[q] += __shfl_xor_sync(0xffffffffu, v[q], o);
-            if (tid == 0) {
-                S->e_kinetic = mue * 0.5 * ds * v[0];
-                S->e_pot = mue * grav * ds * v[1];
-                S->e_elastic = eta * 0.5 * ds * v[2];
-                S->inertial_force[0] = mue * ds * v[3];
-                S->inertial_force[1] = mue * ds * v[4];
+        if (warp < 6) {
+            double v = 0.0;
+            for (int k = lane; k < nthr; k += 32) v = (warp == 5) ? fmax(v, ecol[5][k]) : v + ecol[warp][k];
+            for (int o = 16; o > 0; o >>= 1) {
+                const double u = __shfl_xor_sync(0xffffffffu, v, o);
+                v = (warp == 5) ? fmax(v, u) : v + u;
+            }
+            if (lane == 0) {
+                if (warp == 0) S->e_kinetic = mue * 0.5 * ds * v;
+                else if (warp == 1) S->e_pot = mue * grav * ds * v;
+                else if (warp == 2) S->e_elastic = eta * 0.5 * ds * v;
+                else if (warp == 3) S->inertial_force[0] = mue * ds * v;
+                else if (warp == 4) S->inertial_force[1] = mue * ds * v;
+                else if (released && v > 100.0) set_status(S, FSIBE_ERR_BRAKE);
             }
         }
     }
