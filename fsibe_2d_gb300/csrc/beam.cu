@@ -397,50 +397,43 @@ __global__ void __launch_bounds__(256) k_beam(BeamArgs b) {
         }
     }
     __syncthreads();
+    // positions and velocities, and in the same pass each thread's terms of the emergency brake
+    // (SolidSolver.f90:370-380) and of SolidEnergies (SolidSolver.f90:76-92); then block
+    // reductions (per-thread partials, a shuffle tree, one warp over the warps' results), since
+    // a serial FP64 loop costs a full warp issue slot per addition on this chip.  (The cluster
+    // kernel sums columns in shared memory instead; here those 12 KB would push the LU factor
+    // out of shared memory at ns = 1024.)
     {
+        __shared__ double esum[6][8];
         const double ca = b.cos_a, sa = b.sin_a, alpha_t = 0.0, idt = 1.0 / dt;
+        double sk = 0, sp = 0, se = 0, sax = 0, say = 0, mx = 0;
         for (int i = threadIdx.x; i < ns; i += blockDim.x) {
             const double xrel = w.pre[i], yrel = w.pre[(ns + 8) + i];
             const double vxrel = w.pre[2 * (ns + 8) + i], vyrel = w.pre[3 * (ns + 8) + i];
+            const double yi = b.y0 + yrel * ca + xrel * sa;
             b.x[i] = b.x0 + xrel * ca - yrel * sa;
-            b.y[i] = b.y0 + yrel * ca + xrel * sa;
-            b.vx[i] = 0.0 + ca * (vxrel - alpha_t * yrel) - sa * (vyrel + alpha_t * xrel);
-            b.vy[i] = 0.0 + ca * (vyrel + alpha_t * xrel) + sa * (vxrel - alpha_t * yrel);
+            b.y[i] = yi;
+            const double vx = 0.0 + ca * (vxrel - alpha_t * yrel) - sa * (vyrel + alpha_t * xrel);
+            const double vy = 0.0 + ca * (vyrel + alpha_t * xrel) + sa * (vxrel - alpha_t * yrel);
+            b.vx[i] = vx;
+            b.vy[i] = vy;
+            double ax, ay;
             if (released) {
-                b.ax[i] = (b.vx[i] - w.bo3[i]) * idt;
-                b.ay[i] = (b.vy[i] - w.bo4[i]) * idt;
+                ax = (vx - w.bo3[i]) * idt;
+                ay = (vy - w.bo4[i]) * idt;
+                b.ax[i] = ax;
+                b.ay[i] = ay;
+                mx = fmax(mx, fabs(b.thd[i] - w.bo6[i]));
+            } else {
+                ax = b.ax[i];
+                ay = b.ay[i];
             }
-        }
-    }
-    __syncthreads();
-    // emergency brake (SolidSolver.f90:370-380)
-    if (released) {
-        double mx = 0.0;
-        for (int i = threadIdx.x; i < ns; i += blockDim.x) mx = fmax(mx, fabs(b.thd[i] - w.bo6[i]));
-        for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-        if ((threadIdx.x & 31) == 0) red[2][threadIdx.x >> 5] = mx;
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            double m = 0.0;
-            for (int q = 0; q < (int)(blockDim.x >> 5); ++q) m = fmax(m, red[2][q]);
-            if (m > 100.0) set_status(S, FSIBE_ERR_BRAKE);
-        }
-    }
-    PH(8);
-    // SolidEnergies (SolidSolver.f90:76-92): the five sums as block reductions (per-thread
-    // partials, then a shuffle tree), since a serial FP64 loop costs a full warp issue slot
-    // per addition on this chip
-    {
-        __shared__ double esum[5][8];
-        double sk = 0, sp = 0, se = 0, sax = 0, say = 0;
-        for (int i = threadIdx.x; i < ns; i += blockDim.x) {
             const double th_s = d1d(w.dtab, b.th, ns, 1, i);
-            const double vx = b.vx[i], vy = b.vy[i];
             sk += vx * vx + vy * vy;
-            sp += b.y[i] - b.y0;
+            sp += yi - b.y0;
             se += th_s * th_s;
-            sax += b.ax[i];
-            say += b.ay[i];
+            sax += ax;
+            say += ay;
         }
         for (int o = 16; o > 0; o >>= 1) {
             sk += __shfl_xor_sync(0xffffffffu, sk, o);
@@ -448,27 +441,32 @@ __global__ void __launch_bounds__(256) k_beam(BeamArgs b) {
             se += __shfl_xor_sync(0xffffffffu, se, o);
             sax += __shfl_xor_sync(0xffffffffu, sax, o);
             say += __shfl_xor_sync(0xffffffffu, say, o);
+            mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
         }
-        if ((threadIdx.x & 31) == 0) {
-            const int wv = threadIdx.x >> 5;
-            esum[0][wv] = sk; esum[1][wv] = sp; esum[2][wv] = se; esum[3][wv] = sax; esum[4][wv] = say;
+        const int wv = threadIdx.x >> 5, ln = lane_id();
+        if (ln == 0) {
+            esum[0][wv] = sk; esum[1][wv] = sp; esum[2][wv] = se; esum[3][wv] = sax; esum[4][wv] = say; esum[5][wv] = mx;
         }
         __syncthreads();
+        PH(8);
         if (threadIdx.x < 32) {
             const int nw = blockDim.x >> 5;
-            double v[5];
+            double v[6];
 #pragma unroll
-            for (int q = 0; q < 5; ++q) v[q] = (lane_id() < nw) ? esum[q][lane_id()] : 0.0;
+            for (int q = 0; q < 6; ++q) v[q] = (ln < nw) ? esum[q][ln] : 0.0;
 #pragma unroll
-            for (int o = 4; o > 0; o >>= 1)
+            for (int o = 4; o > 0; o >>= 1) {
 #pragma unroll
                 for (int q = 0; q < 5; ++q) v[q] += __shfl_xor_sync(0xffffffffu, v[q], o);
+                v[5] = fmax(v[5], __shfl_xor_sync(0xffffffffu, v[5], o));
+            }
             if (threadIdx.x == 0) {
                 S->e_kinetic = mue * 0.5 * ds * v[0];
                 S->e_pot = mue * grav * ds * v[1];
                 S->e_elastic = eta * 0.5 * ds * v[2];
                 S->inertial_force[0] = mue * ds * v[3];
                 S->inertial_force[1] = mue * ds * v[4];
+                if (released && v[5] > 100.0) set_status(S, FSIBE_ERR_BRAKE);
             }
         }
     }
