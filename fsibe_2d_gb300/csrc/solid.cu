@@ -26,16 +26,17 @@ __device__ __forceinline__ void clip_box(int* bx, int nx, int ny) {
 }
 
 // Per-primitive parameters in drawing order: segments, sharp end, hinges, dots (create_mask.f90:
-// 2-218, DrawBeamSegment/DrawHinge/DrawADot).  A block of two warps handles 32 nodes i: warp 0
-// segment i and the direction angle of segment i (the hinge's second angle), then the sharp end
-// and the dots; warp 1 the direction angle of segment i-1 (the hinge's first angle), then the
-// hinge at node i -- the FP64 work of a node is split over two SMSPs.  The bounding box of all
-// primitives is reduced with atomics; the last block publishes it with its union with the
-// previous step's box and resets the accumulator.
-__global__ void __launch_bounds__(64) k_mask_prep(MaskArgs a, double gerf) {
+// 2-218, DrawBeamSegment/DrawHinge/DrawADot).  A block of four warps handles 32 nodes i, the
+// FP64 work of a node spread over the four SMSPs: warp 0 segment i; warp 1 the direction angle
+// of segment i-1 (the hinge's first angle); warp 2 that of segment i (its second); warp 3 the
+// hinge's box, then the sharp end and the dots.  After one barrier warp 1 finishes the hinge.
+// The bounding box of all primitives is reduced with atomics; the last block publishes it with
+// its union with the previous step's box and resets the accumulator.
+__global__ void __launch_bounds__(128) k_mask_prep(MaskArgs a, double gerf) {
     pdl_wait();     // the previous kernel of the stream has completed
     __shared__ double ang2[32];
-    __shared__ int wbox[2][4];
+    __shared__ int hbox[32][4];
+    __shared__ int wbox[4][4];
     const int ns = a.ns, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const double dx = a.dx, dy = a.dy, mx = fmax(dx, dy), t = a.t_beam, N = a.N_smooth;
     const double t_star = t + 2.0 * N * mx;
@@ -76,9 +77,56 @@ __global__ void __launch_bounds__(64) k_mask_prep(MaskArgs a, double gerf) {
             P.p[10] = p1x; P.p[11] = p1y;  // the FP32 raster works relative to the start point
             emit(i, P);
         }
+    } else if (warp == 1) {
+        if (hinge) a1 = atan2((a.y[i] - a.y[i - 1]), (a.x[i] - a.x[i - 1]));
+    } else if (warp == 2) {
         if (hinge) ang2[lane] = atan2((a.y[i + 1] - a.y[i]), (a.x[i + 1] - a.x[i]));
-    } else if (hinge) {
-        a1 = atan2((a.y[i] - a.y[i - 1]), (a.x[i] - a.x[i - 1]));
+    } else {
+        if (hinge) {
+            const double px = a.x[i], py = a.y[i];
+            hbox[lane][0] = dnint(div_cr(px - t_star, dx, rdx));
+            hbox[lane][1] = dnint(div_cr(px + t_star, dx, rdx));
+            hbox[lane][2] = dnint(div_cr(py - t_star, dy, rdy));
+            hbox[lane][3] = dnint(div_cr(py + t_star, dy, rdy));
+        }
+        if (i == ns && nsharp) {
+            const int e = ns - 1;
+            const double al = a.th[e] + a.angle_rad;
+            double sa, ca;
+            sincos(al, &sa, &ca);
+            const double p1x = a.x[e] - 2.0 * mx * ca, p1y = a.y[e] - 2.0 * mx * sa;
+            const double p2x = a.x[e] + 4.0 * mx * ca, p2y = a.y[e] + 4.0 * mx * sa;
+            Prim P;
+            for (int k = 0; k < 12; ++k) P.p[k] = 0.0;
+            P.type = PRIM_SHARP;
+            P.box[0] = dnint(div_cr(fmin(p1x, p2x) - t_star, dx, rdx));
+            P.box[1] = dnint(div_cr(fmax(p1x, p2x) + t_star, dx, rdx));
+            P.box[2] = dnint(div_cr(fmin(p1y, p2y) - t_star, dy, rdy));
+            P.box[3] = dnint(div_cr(fmax(p1y, p2y) + t_star, dy, rdy));
+            P.p[0] = ca; P.p[1] = sa;
+            P.p[2] = ca * p1x + sa * p1y; P.p[3] = -sa * p1x + ca * p1y;
+            P.p[4] = ca * p2x + sa * p2y; P.p[5] = -sa * p2x + ca * p2y;
+            P.p[6] = a.vx[e]; P.p[7] = a.vy[e];
+            emit(nseg, P);
+        }
+        if (i >= ns + 1 && i < ns + 1 + ndot) {
+            // DrawADot runs over the whole grid in the reference; SmoothStep is exactly zero once
+            // both erf arguments exceed ~6 (erf rounds to 1), so the box is cut at t + 10 delta.
+            const int d = i - (ns + 1);
+            const int e = (d == 0) ? 0 : ns - 1;
+            const double px = a.x[e], py = a.y[e];
+            if (py < 0.0) set_status(a.S, FSIBE_ERR_MASK_OOB);
+            const double rcut = t + 10.0 * (N * mx) * gerf;
+            Prim P;
+            for (int k = 0; k < 12; ++k) P.p[k] = 0.0;
+            P.type = PRIM_DOT;
+            P.box[0] = (int)floor(div_cr(px - rcut, dx, rdx)) - 1;
+            P.box[1] = (int)ceil(div_cr(px + rcut, dx, rdx)) + 1;
+            P.box[2] = (int)floor(div_cr(py - rcut, dy, rdy)) - 1;
+            P.box[3] = (int)ceil(div_cr(py + rcut, dy, rdy)) + 1;
+            P.p[0] = px; P.p[1] = py; P.p[2] = a.vx[e]; P.p[3] = a.vy[e];
+            emit(nseg + nsharp + nh + d, P);
+        }
     }
     __syncthreads();
     if (warp == 1 && hinge) {
@@ -87,55 +135,14 @@ __global__ void __launch_bounds__(64) k_mask_prep(MaskArgs a, double gerf) {
         Prim P;
         for (int k = 0; k < 12; ++k) P.p[k] = 0.0;
         P.type = PRIM_HINGE;
-        P.box[0] = dnint(div_cr(px - t_star, dx, rdx));
-        P.box[1] = dnint(div_cr(px + t_star, dx, rdx));
-        P.box[2] = dnint(div_cr(py - t_star, dy, rdy));
-        P.box[3] = dnint(div_cr(py + t_star, dy, rdy));
+        P.box[0] = hbox[lane][0]; P.box[1] = hbox[lane][1]; P.box[2] = hbox[lane][2]; P.box[3] = hbox[lane][3];
         P.p[0] = px; P.p[1] = py;
         P.p[2] = div_cr(convert_angle(a1, a.pi) * 180.0, a.pi, a.rpi);
         P.p[3] = div_cr(convert_angle(a2, a.pi) * 180.0, a.pi, a.rpi);
         P.p[4] = a.vx[i]; P.p[5] = a.vy[i];
         emit(nseg + nsharp + (i - 1), P);
     }
-    if (warp == 0 && i == ns && nsharp) {
-        const int e = ns - 1;
-        const double al = a.th[e] + a.angle_rad;
-        double sa, ca;
-        sincos(al, &sa, &ca);
-        const double p1x = a.x[e] - 2.0 * mx * ca, p1y = a.y[e] - 2.0 * mx * sa;
-        const double p2x = a.x[e] + 4.0 * mx * ca, p2y = a.y[e] + 4.0 * mx * sa;
-        Prim P;
-        for (int k = 0; k < 12; ++k) P.p[k] = 0.0;
-        P.type = PRIM_SHARP;
-        P.box[0] = dnint(div_cr(fmin(p1x, p2x) - t_star, dx, rdx));
-        P.box[1] = dnint(div_cr(fmax(p1x, p2x) + t_star, dx, rdx));
-        P.box[2] = dnint(div_cr(fmin(p1y, p2y) - t_star, dy, rdy));
-        P.box[3] = dnint(div_cr(fmax(p1y, p2y) + t_star, dy, rdy));
-        P.p[0] = ca; P.p[1] = sa;
-        P.p[2] = ca * p1x + sa * p1y; P.p[3] = -sa * p1x + ca * p1y;
-        P.p[4] = ca * p2x + sa * p2y; P.p[5] = -sa * p2x + ca * p2y;
-        P.p[6] = a.vx[e]; P.p[7] = a.vy[e];
-        emit(nseg, P);
-    }
-    if (warp == 0 && i >= ns + 1 && i < ns + 1 + ndot) {
-        // DrawADot runs over the whole grid in the reference; SmoothStep is exactly zero once
-        // both erf arguments exceed ~6 (erf rounds to 1), so the box is cut at t + 10 delta.
-        const int d = i - (ns + 1);
-        const int e = (d == 0) ? 0 : ns - 1;
-        const double px = a.x[e], py = a.y[e];
-        if (py < 0.0) set_status(a.S, FSIBE_ERR_MASK_OOB);
-        const double rcut = t + 10.0 * (N * mx) * gerf;
-        Prim P;
-        for (int k = 0; k < 12; ++k) P.p[k] = 0.0;
-        P.type = PRIM_DOT;
-        P.box[0] = (int)floor(div_cr(px - rcut, dx, rdx)) - 1;
-        P.box[1] = (int)ceil(div_cr(px + rcut, dx, rdx)) + 1;
-        P.box[2] = (int)floor(div_cr(py - rcut, dy, rdy)) - 1;
-        P.box[3] = (int)ceil(div_cr(py + rcut, dy, rdy)) + 1;
-        P.p[0] = px; P.p[1] = py; P.p[2] = a.vx[e]; P.p[3] = a.vy[e];
-        emit(nseg + nsharp + nh + d, P);
-    }
-    // the box of all primitives: warp reductions, the block's two warps, then atomics on the
+    // the box of all primitives: warp reductions, the block's four warps, then atomics on the
     // accumulator rect[8..11]
     bx0 = __reduce_min_sync(0xffffffffu, bx0);
     bx1 = __reduce_max_sync(0xffffffffu, bx1);
@@ -144,8 +151,10 @@ __global__ void __launch_bounds__(64) k_mask_prep(MaskArgs a, double gerf) {
     if (lane == 0) { wbox[warp][0] = bx0; wbox[warp][1] = bx1; wbox[warp][2] = by0; wbox[warp][3] = by1; }
     __syncthreads();
     if (threadIdx.x == 0) {
-        bx0 = min(wbox[0][0], wbox[1][0]); bx1 = max(wbox[0][1], wbox[1][1]);
-        by0 = min(wbox[0][2], wbox[1][2]); by1 = max(wbox[0][3], wbox[1][3]);
+        for (int q = 1; q < 4; ++q) {
+            bx0 = min(bx0, wbox[q][0]); bx1 = max(bx1, wbox[q][1]);
+            by0 = min(by0, wbox[q][2]); by1 = max(by1, wbox[q][3]);
+        }
         if (bx0 <= bx1) {
             atomicMin(&a.rect[8], bx0); atomicMax(&a.rect[9], bx1);
             atomicMin(&a.rect[10], by0); atomicMax(&a.rect[11], by1);
@@ -691,7 +700,7 @@ __global__ void __launch_bounds__(128) k_forces(ForceArgs a, double dxi, double 
 // Host launchers
 // ===================================================================================
 void launch_mask_prep(const MaskArgs& a, double gerf, cudaStream_t st, bool pdl) {
-    launch_k(k_mask_prep, dim3((a.ns + 3 + 31) / 32), dim3(64), 0, st, pdl, a, gerf);
+    launch_k(k_mask_prep, dim3((a.ns + 3 + 31) / 32), dim3(128), 0, st, pdl, a, gerf);
 }
 void launch_mask(const MaskArgs& a, double gerf, bool fp32, cudaStream_t st, bool pdl) {
     // four-warp blocks, two per SM: a tile's primitives over the four SMSPs of an SM
