@@ -576,10 +576,10 @@ static void launch_y(fsibe_ctx* c, void (*k)(KArgs<R>), int smem, const KArgs<R>
 // on the main stream a programmatic dependent launch (the fused x kernels begin with pdl_wait)
 template <typename R>
 static void launch_xv(fsibe_ctx* c, void (*k)(KArgs<R>), const typename SizeKernels<R>::XVariant& v, int nbuf,
-                      const KArgs<R>& a, const char* name, cudaStream_t st = nullptr) {
+                      const KArgs<R>& a, const char* name, cudaStream_t st = nullptr, int grid = 0) {
     if (!st) st = c->stream;
     prof_begin(c, name, st);
-    launch_k(k, dim3(c->g.ny / v.rows), dim3(v.threads), nbuf == 3 ? v.smem3 : nbuf * v.smem1, st,
+    launch_k(k, dim3(grid > 0 ? grid : c->g.ny / v.rows), dim3(v.threads), nbuf == 3 ? v.smem3 : nbuf * v.smem1, st,
              c->pdl && st == c->stream, a);
     prof_end(c, st);
     c->launches++;
@@ -693,7 +693,11 @@ static void nl_advect_t(fsibe_ctx* c, int explicit_step) {
     KArgs<R> a = kargs<R>(c);
     SizeKernels<R>& KX = kx_of<R>(c);
     a.explicit_step = explicit_step;
-    launch_xv<R>(c, KX.xv[c->xv_nl].nl_adv, KX.xv[c->xv_nl], 2, a, "nl_adv", c->side2);
+    // one block a SM, each taking tiles in turn (k_nl_x), so that the mask raster launched
+    // after it finds room on every SM
+    const int tiles = c->g.ny / KX.xv[c->xv_nl].rows;
+    launch_xv<R>(c, KX.xv[c->xv_nl].nl_adv, KX.xv[c->xv_nl], 2, a, "nl_adv", c->side2,
+                 tiles < c->nsm ? tiles : c->nsm);
 }
 
 // EvolveFluidExplicit / EvolveFluidAB2 + pressure (NavierStokes.f90:422-508, 273-403)

@@ -364,9 +364,9 @@ __global__ void __launch_bounds__(XRows<R, H>::THREADS) k_vel_x(KArgs<R> a) {
 // ======================================================================================
 // K2: nonlinear term and penalization in physical space (cal_nlk)
 // ======================================================================================
-template <typename R, int H, int TRV, int PART = NL_WHOLE>
-__global__ void __launch_bounds__(XRows<R, H, TRV>::THREADS) k_nl_x(KArgs<R> a) {
-    pdl_wait();     // the previous kernel of the stream has completed
+// One tile of TR rows from iy0 (the whole kernel's work for one block)
+template <typename R, int H, int TRV, int PART>
+__device__ __forceinline__ void nl_x_tile(const KArgs<R>& a, const int iy0) {
     using X = XRows<R, H, TRV>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C2<R>* bufA = reinterpret_cast<C2<R>*>(smem_raw);
@@ -374,7 +374,7 @@ __global__ void __launch_bounds__(XRows<R, H, TRV>::THREADS) k_nl_x(KArgs<R> a) 
     C2<R>* bufB = bufA + BS;
     C2<R>* bufC = bufB + BS;
     const int r = threadIdx.x / X::G, t = threadIdx.x % X::G;
-    const int iy0 = blockIdx.x * X::TR, ny = a.g.ny;
+    const int ny = a.g.ny;
     constexpr int part = PART;
     // the penalization part: only the rows of the mask's box carry a non-zero term
     if (part == NL_PENAL && (iy0 + X::TR - 1 < a.rect[2] || iy0 > a.rect[3])) return;
@@ -482,6 +482,24 @@ __global__ void __launch_bounds__(XRows<R, H, TRV>::THREADS) k_nl_x(KArgs<R> a) 
                 a.B[o] = mk<R>(0, 0);
             }
         }
+    }
+}
+
+template <typename R, int H, int TRV, int PART = NL_WHOLE>
+__global__ void __launch_bounds__(XRows<R, H, TRV>::THREADS) k_nl_x(KArgs<R> a) {
+    pdl_wait();     // the previous kernel of the stream has completed
+    using X = XRows<R, H, TRV>;
+    if constexpr (PART == NL_ADVECT) {
+        // the advection part runs beside the mask kernels on fewer blocks than tiles (the
+        // launch gives one a SM), each taking tiles in turn, so that the raster launched after
+        // it still finds room on every SM
+        const int ntile = a.g.ny / X::TR;
+        for (int tile = blockIdx.x; tile < ntile; tile += gridDim.x) {
+            nl_x_tile<R, H, TRV, PART>(a, tile * X::TR);
+            __syncthreads();  // the next tile reuses the row buffers
+        }
+    } else {
+        nl_x_tile<R, H, TRV, PART>(a, blockIdx.x * X::TR);
     }
 }
 
