@@ -9,6 +9,7 @@ spectral fields in the packed Temperton layout of coftxy.
 Errors follow the reference's "stop" semantics by raising FsibeError with the status code.
 """
 import ctypes as C
+import os
 
 import numpy as np
 
@@ -70,6 +71,8 @@ def declare(lib, prefix, ctx_type=C.c_void_p):
     f("upload_beam", P, _dp, _dp, _dp, _dp, _dp)
     f("download_beam", P, _dp, _dp, _dp, _dp, _dp)
     f("get_scalars", P, C.POINTER(FsibeScalars))
+    f("write_backup", P, C.c_char_p)
+    f("read_backup", P, C.c_char_p)
     f("last_error", P, res=C.c_char_p)
 
 
@@ -177,6 +180,17 @@ class Run:
         plus init_beams / InitializeSolidSolver / the start-up create_mask (time_step.f90:60-84)."""
         v = _f64(vort, self.shape)
         self._call("init_fields", _ptr(v))
+
+    def MakeRuntimeBackup(self, path):
+        """Write the state between two steps as runtime_backup<n>.in (save_fields.f90:109-152):
+        Fortran sequential unformatted records, reals 8 bytes, integers 4."""
+        self._call("write_backup", os.fsencode(os.fspath(path)))
+
+    def resume(self, path):
+        """init_fields with inicond=2 (init_fields.f90:44-100) plus init_beams /
+        InitializeSolidSolver / the start-up create_mask (time_step.f90:60-84); the next step
+        is an AB2 step with a Crank-Nicolson solid step."""
+        self._call("read_backup", os.fsencode(os.fspath(path)))
 
     def create_mask(self, time):
         self._call("create_mask", C.c_double(time))

@@ -4,6 +4,7 @@
 // sequence of kernel launches whose time-dependent inputs (time, dt, AB2 weights, drag
 // window, status) live in a device struct, so a step needs no host round trip and can be
 // captured once in a CUDA graph and replayed.
+#include <algorithm>
 #include <array>
 #include <cmath>
 #include <cstdlib>
@@ -1625,6 +1626,207 @@ int fsibe_download_beam(fsibe_ctx* c, double* beam, double* po, double* pn, doub
     if (to) CK(c, cudaMemcpyAsync(to, c->beam[B_TO], 8 * ns, cudaMemcpyDeviceToHost, c->stream));
     if (tn) CK(c, cudaMemcpyAsync(tn, c->beam[B_TN], 8 * ns, cudaMemcpyDeviceToHost, c->stream));
     CK(c, cudaStreamSynchronize(c->stream));
+    return FSIBE_OK;
+}
+
+// ---- runtime backup (save_fields.f90:109-152, init_fields.f90:44-100) ------------------
+// Fortran sequential unformatted records: a 4-byte length before and after each record;
+// reals are 8 bytes, integers and logicals 4.
+namespace {
+struct BackupOut {
+    FILE* f = nullptr;
+    std::vector<char> rec;
+    bool ok = true;
+    void put(const void* p, size_t n) { const char* q = static_cast<const char*>(p); rec.insert(rec.end(), q, q + n); }
+    void d(double v) { put(&v, 8); }
+    void i(int32_t v) { put(&v, 4); }
+    void dv(const double* p, size_t n) { put(p, 8 * n); }
+    void end() {
+        const int32_t n = (int32_t)rec.size();
+        ok = ok && fwrite(&n, 4, 1, f) == 1 && (rec.empty() || fwrite(rec.data(), 1, rec.size(), f) == rec.size()) &&
+             fwrite(&n, 4, 1, f) == 1;
+        rec.clear();
+    }
+};
+struct BackupIn {
+    FILE* f = nullptr;
+    std::vector<char> rec;
+    size_t pos = 0;
+    bool ok = true;
+    void next() {
+        int32_t n = -1, m = -2;
+        ok = ok && fread(&n, 4, 1, f) == 1 && n >= 0;
+        if (ok) rec.resize((size_t)n);
+        ok = ok && (n == 0 || fread(rec.data(), 1, (size_t)n, f) == (size_t)n) && fread(&m, 4, 1, f) == 1 && m == n;
+        pos = 0;
+    }
+    void get(void* p, size_t n) {
+        ok = ok && pos + n <= rec.size();
+        if (ok) std::memcpy(p, rec.data() + pos, n);
+        pos += n;
+    }
+    double d() { double v = 0.0; get(&v, 8); return v; }
+    int32_t i() { int32_t v = 0; get(&v, 4); return v; }
+    void dv(double* p, size_t n) { get(p, 8 * n); }
+};
+}  // namespace
+
+// The state between two steps as MakeRuntimeBackup writes it.  The AB2 history is stored as
+// the product the next step forms first (nlk(n1) workvis(n0), NavierStokes.f90:480): nlk(n1)
+// holds it and workvis(n0) is one, so the reference and this library both resume from the
+// same history.
+int fsibe_write_backup(fsibe_ctx* c, const char* path) {
+    if (!c || !path) return FSIBE_ERR_PARAM;
+    if (!c->initialized) { c->err = "write_backup before init_fields"; return FSIBE_ERR_STATE; }
+    const size_t NN = (size_t)c->g.nx * c->g.ny, ns = (size_t)c->P.ns;
+    std::vector<double> W(NN), M(NN), zero(NN, 0.0), one(NN, 1.0), mk(3 * NN), u(2 * NN), vm(NN);
+    int st = spec_to_packed(c, c->spec[SP_W], W.data(), c->fp32 ? c->spec[SP_WLO] : nullptr);
+    if (!st) st = spec_to_packed(c, c->spec[SP_M], M.data());
+    if (!st) st = fsibe_download_mask(c, mk.data(), mk.data() + NN, mk.data() + 2 * NN);
+    if (!st) st = fsibe_download_u(c, u.data());
+    if (!st) st = fsibe_download_vor_mean(c, vm.data());
+    if (st) return st;
+    std::vector<double> bm(B_N * ns), oo(6 * ns);
+    for (int q = 0; q < B_N; ++q) CK(c, cudaMemcpyAsync(bm.data() + q * ns, c->beam[q], 8 * ns, cudaMemcpyDeviceToHost, c->stream));
+    CK(c, cudaMemcpyAsync(oo.data(), c->oo, 8 * 6 * ns, cudaMemcpyDeviceToHost, c->stream));
+    DevScalars h;
+    CK(c, cudaMemcpyAsync(&h, c->S, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+    CK(c, cudaStreamSynchronize(c->stream));
+    BackupOut o;
+    o.f = std::fopen(path, "wb");
+    if (!o.f) { c->err = "cannot open the backup file for writing"; return FSIBE_ERR_PARAM; }
+    o.d(h.time); o.end();
+    o.d(123.0); o.end();
+    o.i(1); o.d(h.dt1);
+    o.dv(W.data(), NN); o.dv(zero.data(), NN);   // vortk(n0 = 0) current, vortk(n1) unused
+    o.dv(zero.data(), NN); o.dv(M.data(), NN);   // nlk(n0) unused, nlk(n1) the history
+    o.dv(one.data(), NN); o.dv(zero.data(), NN); // workvis(n0) = 1
+    o.dv(mk.data(), 3 * NN);
+    o.i(1);  // ivideo
+    o.dv(u.data(), 2 * NN);
+    o.end();
+    o.i(c->P.ns); o.end();
+    o.d(0.0); o.i(0); o.end();  // colorscale, colorscale_done
+    if (c->P.iBeam > 0) {
+        for (int q : {B_X, B_Y, B_VX, B_VY, B_TH, B_THD}) o.dv(bm.data() + q * ns, ns);
+        o.end();
+        for (int q : {B_PN, B_PO, B_TN, B_TO}) o.dv(bm.data() + q * ns, ns);
+        o.end();
+        o.dv(h.force, 2); o.dv(h.force_unst, 2); o.dv(h.force_press, 2);
+        o.d(h.e_kinetic); o.d(h.e_pot); o.d(h.e_elastic); o.d(c->P.x0); o.d(c->P.y0);
+        o.end();
+        o.d(c->P.angle_beam); o.i(c->P.iMotion);
+        o.d(h.drag_unst_old); o.d(h.drag_unst_old); o.d(h.lift_unst_old); o.d(h.lift_unst_old);
+        o.end();
+        o.i(h.unst_ready ? 1 : 0); o.d(h.dt_old); o.dv(oo.data(), 6 * ns);
+        o.end();
+        o.dv(bm.data() + B_AX * ns, ns); o.dv(bm.data() + B_AY * ns, ns); o.dv(h.inertial_force, 2);
+        o.end();
+    }
+    o.dv(vm.data(), NN); o.end();
+    const bool ok = (std::fclose(o.f) == 0) && o.ok;
+    if (!ok) { c->err = "writing the backup file failed"; return FSIBE_ERR_PARAM; }
+    return FSIBE_OK;
+}
+
+// Resume: init_beams and InitializeSolidSolver (the next solid step is a Crank-Nicolson
+// start-up step), the records, n0 = 1 - n1, the start-up mask (time_step.f90:60-84); no Euler
+// start-up step follows.  The velocity statistics of the first step come from the file's u.
+int fsibe_read_backup(fsibe_ctx* c, const char* path) {
+    if (!c || !path) return FSIBE_ERR_PARAM;
+    const size_t NN = (size_t)c->g.nx * c->g.ny, ns = (size_t)c->P.ns;
+    BackupIn in;
+    in.f = std::fopen(path, "rb");
+    if (!in.f) { c->err = "cannot open the backup file"; return FSIBE_ERR_PARAM; }
+    std::vector<double> vortk(2 * NN), nlk(2 * NN), workvis(2 * NN), mk(3 * NN), u(2 * NN), vm(NN);
+    std::vector<double> bm(B_N * ns, 0.0), oo(6 * ns, 0.0);
+    double force[2] = {0, 0}, force_unst[2] = {0, 0}, force_press[2] = {0, 0}, inertial[2] = {0, 0};
+    double ek = 0, ep = 0, ee = 0, dun = 0, duo = 0, lun = 0, luo = 0, dt_old = 0;
+    int32_t ready = 0;
+    in.next(); const double time = in.d();
+    in.next(); const bool sum_ok = in.d() == 123.0;
+    in.next();
+    const int32_t n1 = in.i();
+    const double dt1 = in.d();
+    in.dv(vortk.data(), 2 * NN); in.dv(nlk.data(), 2 * NN); in.dv(workvis.data(), 2 * NN);
+    in.dv(mk.data(), 3 * NN);
+    (void)in.i();  // ivideo
+    in.dv(u.data(), 2 * NN);
+    in.next(); const bool ns_ok = in.i() == c->P.ns;
+    in.next(); (void)in.d(); (void)in.i();  // colorscale, colorscale_done
+    if (in.ok && ns_ok && c->P.iBeam > 0) {
+        in.next();
+        for (int q : {B_X, B_Y, B_VX, B_VY, B_TH, B_THD}) in.dv(bm.data() + q * ns, ns);
+        in.next();
+        for (int q : {B_PN, B_PO, B_TN, B_TO}) in.dv(bm.data() + q * ns, ns);
+        in.next();
+        in.dv(force, 2); in.dv(force_unst, 2); in.dv(force_press, 2);
+        ek = in.d(); ep = in.d(); ee = in.d(); (void)in.d(); (void)in.d();  // x0, y0 come from the parameters
+        in.next();
+        (void)in.d(); (void)in.i();  // AngleBeam, iMouvement come from the parameters
+        dun = in.d(); duo = in.d(); lun = in.d(); luo = in.d();
+        in.next();
+        ready = in.i(); dt_old = in.d(); in.dv(oo.data(), 6 * ns);
+        in.next();
+        in.dv(bm.data() + B_AX * ns, ns); in.dv(bm.data() + B_AY * ns, ns); in.dv(inertial, 2);
+    }
+    in.next(); in.dv(vm.data(), NN);
+    std::fclose(in.f);
+    (void)dun; (void)lun;
+    if (!in.ok || !sum_ok || !ns_ok || (n1 != 0 && n1 != 1)) {
+        c->err = "not a runtime backup of this configuration (record, checksum or ns)";
+        return FSIBE_ERR_PARAM;
+    }
+    const int n0 = 1 - n1;
+    // the AB2 history nlk(n1) workvis(n0), formed as the next step would
+    std::vector<double> M(NN);
+    for (size_t i = 0; i < NN; ++i) M[i] = nlk[n1 * NN + i] * workvis[n0 * NN + i];
+    free_graph(c);
+    const size_t rs = c->fp32 ? 4 : 8;
+    int st = packed_to_spec(c, vortk.data() + n0 * NN, c->spec[SP_W], c->fp32 ? c->spec[SP_WLO] : nullptr);
+    if (!st) st = packed_to_spec(c, M.data(), c->spec[SP_M]);
+    if (st) return st;
+    for (int q : {PH_PRESS, PH_SA, PH_SB}) CK(c, cudaMemsetAsync(c->phys[q], 0, rs * NN, c->stream));
+    if ((st = from_host(c, vm.data(), NN, c->phys[PH_VORMEAN]))) return st;
+    DevScalars h;
+    std::memset(&h, 0, sizeof(h));
+    h.time = time; h.dt1 = dt1; h.dt0 = dt1; h.dt_old = dt_old;
+    h.startup_step = 1;
+    h.method = c->P.time_method_solid;
+    h.grav = c->P.grav;
+    h.unst_ready = ready ? 1 : 0;
+    h.drag_unst_old = duo; h.lift_unst_old = luo;
+    for (int k = 0; k < 2; ++k) {
+        h.force[k] = force[k]; h.force_unst[k] = force_unst[k]; h.force_press[k] = force_press[k]; h.inertial_force[k] = inertial[k];
+    }
+    h.e_kinetic = ek; h.e_pot = ep; h.e_elastic = ee;
+    c->U_mean_true = 1.0;
+    h.mean_u_next = h.mean_u_cur = c->U_mean_true * host_mean(c->P, time, true);
+    h.mean_v_next = h.mean_v_cur = c->U_mean_true * host_mean(c->P, time, false);
+    CK(c, cudaMemcpyAsync(c->S, &h, sizeof(h), cudaMemcpyHostToDevice, c->stream));
+    c->pre_launched = false;
+    if (c->P.iBeam > 0) {
+        for (int q = 0; q < B_N; ++q) CK(c, cudaMemcpyAsync(c->beam[q], bm.data() + q * ns, 8 * ns, cudaMemcpyHostToDevice, c->stream));
+        CK(c, cudaMemcpyAsync(c->oo, oo.data(), 8 * 6 * ns, cudaMemcpyHostToDevice, c->stream));
+    }
+    // the spectra the first step's x-pass reads, then the file's velocity over the one formed here
+    st = c->fp32 ? init_velocity<float>(c) : init_velocity<double>(c);
+    if (!st) st = fsibe_upload_u(c, u.data());
+    if (st) return st;
+    // the first step's dt and mean velocity (cal_nlk's statistics of u) from the file's u
+    std::vector<double> red(RED_NSLOTS, 0.0);
+    for (size_t i = 0; i < NN; ++i) {
+        red[RED_UMAX2] = std::max(red[RED_UMAX2], u[i] * u[i] + u[NN + i] * u[NN + i]);
+        red[RED_SUM_U] += u[i];
+        red[RED_SUM_V] += u[NN + i];
+    }
+    const int32_t one_block = 1;
+    CK(c, cudaMemcpyAsync(c->red, red.data(), 8 * RED_NSLOTS, cudaMemcpyHostToDevice, c->stream));
+    CK(c, cudaMemcpyAsync(&c->S->nred, &one_block, 4, cudaMemcpyHostToDevice, c->stream));
+    if ((st = create_mask(c))) return st;
+    CK(c, cudaStreamSynchronize(c->stream));
+    c->initialized = true;
+    c->startup_done = true;
     return FSIBE_OK;
 }
 

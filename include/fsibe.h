@@ -180,6 +180,21 @@ int fsibe_download_beam(fsibe_ctx* ctx, double* beam, double* p_old, double* p_n
                         double* tau_old, double* tau_new);
 int fsibe_get_scalars(fsibe_ctx* ctx, fsibe_scalars* out);
 
+/* ---- runtime backup ----------------------------------------------------------
+ * The file runtime_backup<n>.in of MakeRuntimeBackup (save_fields.f90:109-152): Fortran
+ * sequential unformatted records (a 4-byte record length before and after each record),
+ * reals 8 bytes, integers and logicals 4; one beam.
+ *
+ * fsibe_write_backup: the state between two steps (after fsibe_step / fsibe_run / advance).
+ *   Replaces the MakeRuntimeBackup call of time_step.f90:249.  The AB2 history is stored as
+ *   nlk(n1) = the product nlk workvis that the next step forms first, with workvis(n0) = 1.
+ * fsibe_read_backup: resume, as inicond = 2 (init_fields.f90:44-100) with the init_beams /
+ *   InitializeSolidSolver / create_mask around it (time_step.f90:60-84).  The next fsibe_step
+ *   is an AB2 step with a Crank-Nicolson solid step.  Reads files of either writer.
+ * Both return FSIBE_ERR_PARAM on an I/O error, a wrong checksum or a different ns. */
+int fsibe_write_backup(fsibe_ctx* ctx, const char* path);
+int fsibe_read_backup(fsibe_ctx* ctx, const char* path);
+
 /* ---- measurement helpers ---------------------------------------------------- */
 /* Device time (ms, CUDA events on ctx's stream) of nsteps whole steps. */
 int fsibe_time_steps(fsibe_ctx* ctx, int nsteps, float* ms);

@@ -1487,6 +1487,48 @@ static void fill_scalars(orc_ctx* c) {
 
 static bool is_pow2(int v) { return v >= 8 && (v & (v - 1)) == 0; }
 
+/* Fortran sequential unformatted records (gfortran framing: a 4-byte length before and after
+ * each record), as MakeRuntimeBackup writes them with -r8 (reals 8 bytes, integers and
+ * logicals 4). */
+struct RecWriter {
+    std::vector<char> rec;
+    FILE* f;
+    void put(const void* p, size_t n) { const char* q = static_cast<const char*>(p); rec.insert(rec.end(), q, q + n); }
+    void d(double v) { put(&v, 8); }
+    void i(int32_t v) { put(&v, 4); }
+    void dv(const double* p, size_t n) { put(p, 8 * n); }
+    bool end() {
+        const int32_t n = (int32_t)rec.size();
+        const bool ok = fwrite(&n, 4, 1, f) == 1 && (rec.empty() || fwrite(rec.data(), 1, rec.size(), f) == rec.size()) &&
+                        fwrite(&n, 4, 1, f) == 1;
+        rec.clear();
+        return ok;
+    }
+};
+struct RecReader {
+    std::vector<char> rec;
+    size_t pos = 0;
+    FILE* f;
+    bool next() {
+        int32_t n = 0, m = 0;
+        if (fread(&n, 4, 1, f) != 1 || n < 0) return false;
+        rec.resize((size_t)n);
+        if (n > 0 && fread(rec.data(), 1, (size_t)n, f) != (size_t)n) return false;
+        if (fread(&m, 4, 1, f) != 1 || m != n) return false;
+        pos = 0;
+        return true;
+    }
+    bool get(void* p, size_t n) {
+        if (pos + n > rec.size()) return false;
+        std::memcpy(p, rec.data() + pos, n);
+        pos += n;
+        return true;
+    }
+    bool d(double& v) { return get(&v, 8); }
+    bool i(int32_t& v) { return get(&v, 4); }
+    bool dv(double* p, size_t n) { return get(p, 8 * n); }
+};
+
 }  // namespace
 
 /* ==================================================================================
@@ -1709,5 +1751,116 @@ int orc_newton_system(orc_ctx* c, double time, double dt, double dt_old, int met
     return st;
 }
 double orc_time(orc_ctx* c) { return c->time; }
+
+/* MakeRuntimeBackup (save_fields.f90:109-152): the records of runtime_backup<n>.in for the
+ * state between two steps (n0 the current level, n1 the previous one, after the level
+ * switch of time_step.f90:152/222). */
+int orc_write_backup(orc_ctx* c, const char* path) {
+    if (!c || !path) return FSIBE_ERR_PARAM;
+    if (!c->initialized) return fail(c, FSIBE_ERR_STATE, "write_backup before init_fields");
+    FILE* f = std::fopen(path, "wb");
+    if (!f) return fail(c, FSIBE_ERR_PARAM, "cannot open the backup file for writing");
+    const size_t NN = (size_t)c->nx * c->ny;
+    RecWriter w;
+    w.f = f;
+    bool ok = true;
+    w.d(c->time); ok = ok && w.end();
+    w.d(123.0); ok = ok && w.end();  /* checksum */
+    w.i(c->n1); w.d(c->dt1);
+    for (int q = 0; q < 2; ++q) w.dv(c->vortk[q].data(), NN);
+    for (int q = 0; q < 2; ++q) w.dv(c->nlk[q].data(), NN);
+    for (int q = 0; q < 2; ++q) w.dv(c->workvis[q].data(), NN);
+    w.dv(c->mask.data(), NN); w.dv(c->maskvx.data(), NN); w.dv(c->maskvy.data(), NN);
+    w.i(1);  /* ivideo */
+    w.dv(c->u.data(), 2 * NN);
+    ok = ok && w.end();
+    w.i(c->ns); ok = ok && w.end();
+    w.d(0.0); w.i(0); ok = ok && w.end();  /* colorscale, colorscale_done */
+    if (c->P.iBeam > 0) {
+        const Beam& b = c->beam;
+        const size_t ns = (size_t)c->ns;
+        for (const auto* v : {&b.x, &b.y, &b.vx, &b.vy, &b.theta, &b.theta_dot}) w.dv(v->data(), ns);
+        ok = ok && w.end();
+        for (const auto* v : {&b.p_new, &b.p_old, &b.tau_new, &b.tau_old}) w.dv(v->data(), ns);
+        ok = ok && w.end();
+        w.dv(b.Force, 2); w.dv(b.Force_unst, 2); w.dv(b.Force_press, 2);
+        w.d(b.E_kin); w.d(b.E_pot); w.d(b.E_el); w.d(b.x0); w.d(b.y0);
+        ok = ok && w.end();
+        w.d(b.AngleBeam); w.i(b.iMouvement); w.d(b.drag_unst_new); w.d(b.drag_unst_old);
+        w.d(b.lift_unst_new); w.d(b.lift_unst_old);
+        ok = ok && w.end();
+        w.i(b.UnstReady ? 1 : 0); w.d(b.dt_old); w.dv(b.oldold.data(), 6 * ns);
+        ok = ok && w.end();
+        w.dv(b.ax.data(), ns); w.dv(b.ay.data(), ns); w.dv(b.Inertial, 2);
+        ok = ok && w.end();
+    }
+    w.dv(c->vor_mean.data(), NN); ok = ok && w.end();
+    ok = (std::fclose(f) == 0) && ok;
+    return ok ? FSIBE_OK : fail(c, FSIBE_ERR_PARAM, "writing the backup file failed");
+}
+
+/* Resume from a backup: init_fields with inicond = 2 (init_fields.f90:44-100) and what
+ * time_step does around it (time_step.f90:60-84): init_beams, InitializeSolidSolver (the next
+ * solid step is a start-up step), the records, n0 = 1 - n1, the start-up mask; no Euler
+ * start-up step follows. */
+int orc_read_backup(orc_ctx* c, const char* path) {
+    if (!c || !path) return FSIBE_ERR_PARAM;
+    FILE* f = std::fopen(path, "rb");
+    if (!f) return fail(c, FSIBE_ERR_PARAM, "cannot open the backup file");
+    const size_t NN = (size_t)c->nx * c->ny;
+    c->TimeMethodSolid = c->P.time_method_solid;
+    c->ActuallyBDF2 = false;
+    c->grav = c->P.grav;
+    init_beams(c);
+    c->beam.StartupStep = true;
+    RecReader r;
+    r.f = f;
+    bool ok = true;
+    double time = 0.0, checksum = 0.0, dt1 = 0.0, colorscale = 0.0;
+    int32_t n1 = 1, ivideo = 0, ns = 0, cdone = 0;
+    ok = ok && r.next() && r.d(time);
+    ok = ok && r.next() && r.d(checksum) && checksum == 123.0;
+    ok = ok && r.next() && r.i(n1) && r.d(dt1) && (n1 == 0 || n1 == 1);
+    for (int q = 0; q < 2 && ok; ++q) ok = r.dv(c->vortk[q].data(), NN);
+    for (int q = 0; q < 2 && ok; ++q) ok = r.dv(c->nlk[q].data(), NN);
+    for (int q = 0; q < 2 && ok; ++q) ok = r.dv(c->workvis[q].data(), NN);
+    ok = ok && r.dv(c->mask.data(), NN) && r.dv(c->maskvx.data(), NN) && r.dv(c->maskvy.data(), NN);
+    ok = ok && r.i(ivideo) && r.dv(c->u.data(), 2 * NN);
+    ok = ok && r.next() && r.i(ns) && ns == c->ns;
+    ok = ok && r.next() && r.d(colorscale) && r.i(cdone);
+    if (ok && c->P.iBeam > 0) {
+        Beam& b = c->beam;
+        const size_t nsz = (size_t)c->ns;
+        int32_t imv = 0, ready = 0;
+        ok = r.next();
+        for (auto* v : {&b.x, &b.y, &b.vx, &b.vy, &b.theta, &b.theta_dot}) ok = ok && r.dv(v->data(), nsz);
+        ok = ok && r.next();
+        for (auto* v : {&b.p_new, &b.p_old, &b.tau_new, &b.tau_old}) ok = ok && r.dv(v->data(), nsz);
+        ok = ok && r.next() && r.dv(b.Force, 2) && r.dv(b.Force_unst, 2) && r.dv(b.Force_press, 2) && r.d(b.E_kin) &&
+             r.d(b.E_pot) && r.d(b.E_el) && r.d(b.x0) && r.d(b.y0);
+        ok = ok && r.next() && r.d(b.AngleBeam) && r.i(imv) && r.d(b.drag_unst_new) && r.d(b.drag_unst_old) &&
+             r.d(b.lift_unst_new) && r.d(b.lift_unst_old);
+        ok = ok && r.next() && r.i(ready) && r.d(b.dt_old) && r.dv(b.oldold.data(), 6 * nsz);
+        ok = ok && r.next() && r.dv(b.ax.data(), nsz) && r.dv(b.ay.data(), nsz) && r.dv(b.Inertial, 2);
+        b.iMouvement = imv;
+        b.UnstReady = ready != 0;
+    }
+    ok = ok && r.next() && r.dv(c->vor_mean.data(), NN);
+    std::fclose(f);
+    if (!ok) return fail(c, FSIBE_ERR_PARAM, "not a runtime backup of this configuration (record, checksum or ns)");
+    c->time = time;
+    c->dt1 = dt1;
+    c->dt0 = dt1;
+    c->n1 = n1;
+    c->n0 = 1 - n1;
+    c->U_mean_true = 1.0;
+    const int st = create_mask(c, c->time);
+    if (st) return st;
+    c->initialized = true;
+    c->startup_done = true;
+    std::memset(&c->sc, 0, sizeof(c->sc));
+    fill_scalars(c);
+    return FSIBE_OK;
+}
 
 }  // extern "C"
