@@ -11,7 +11,7 @@ import numpy as np
 
 from ._abi import (FsibeParams, FsibeScalars, make_params, BEAM_DATA_COLUMNS, STATUS_NAMES,  # noqa: F401
                    FSIBE_FP64, FSIBE_FP32C, FSIBE_BDF2, FSIBE_CRANK_NICHOLSON, FSIBE_EULER_IMPLICIT)
-from ._binding import FsibeError, declare, Run as _Run  # noqa: F401
+from ._binding import FsibeError, declare, backup_time, Run as _Run  # noqa: F401
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_lib", "libfsibe_gb300.so")

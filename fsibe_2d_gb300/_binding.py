@@ -10,6 +10,7 @@ Errors follow the reference's "stop" semantics by raising FsibeError with the st
 """
 import ctypes as C
 import os
+import struct
 
 import numpy as np
 
@@ -74,6 +75,20 @@ def declare(lib, prefix, ctx_type=C.c_void_p):
     f("write_backup", P, C.c_char_p)
     f("read_backup", P, C.c_char_p)
     f("last_error", P, res=C.c_char_p)
+
+
+def backup_time(path):
+    """The time in the first record of a runtime backup (a Fortran sequential record of one
+    8-byte real), or None when the file is missing or its first record is not that."""
+    try:
+        with open(path, "rb") as f:
+            head = f.read(16)
+    except OSError:
+        return None
+    if len(head) < 16:
+        return None
+    n, t, m = struct.unpack("<id", head[:12]) + struct.unpack("<i", head[12:16])
+    return t if n == 8 and m == 8 else None
 
 
 class Run:
@@ -191,6 +206,31 @@ class Run:
         InitializeSolidSolver / the start-up create_mask (time_step.f90:60-84); the next step
         is an AB2 step with a Crank-Nicolson solid step."""
         self._call("read_backup", os.fsencode(os.fspath(path)))
+
+    def make_runtime_backup(self, directory, nbackup):
+        """MakeRuntimeBackup's file naming (save_fields.f90:122-147): write
+        <directory>/runtime_backup<nbackup>.in and return the next nbackup (1 - nbackup),
+        so that successive backups alternate between two files."""
+        if nbackup not in (0, 1):
+            raise ValueError("nbackup is 0 or 1")
+        self.MakeRuntimeBackup(os.path.join(os.fspath(directory), "runtime_backup%d.in" % nbackup))
+        return 1 - nbackup
+
+    def resume_latest(self, directory):
+        """inicond = 2 (init_fields.f90:44-92): of runtime_backup0.in and runtime_backup1.in,
+        resume from the one whose first record holds the later time (a time above zero);
+        missing files are skipped.  Raises FileNotFoundError when neither holds one
+        ("Unable to resume").  Returns the path used."""
+        best, tbest = None, 0.0
+        for i in (0, 1):
+            path = os.path.join(os.fspath(directory), "runtime_backup%d.in" % i)
+            t = backup_time(path)
+            if t is not None and t > tbest:
+                best, tbest = path, t
+        if best is None:
+            raise FileNotFoundError("unable to resume: no runtime backup with a time above zero in %s" % directory)
+        self.resume(best)
+        return best
 
     def create_mask(self, time):
         self._call("create_mask", C.c_double(time))

@@ -98,6 +98,16 @@ module fsibe_iso_c
       import :: c_int, c_ptr
       type(c_ptr), value :: ctx
     end function
+    integer(c_int) function fsibe_write_backup(ctx, path) bind(C, name="fsibe_write_backup")
+      import :: c_int, c_ptr, c_char
+      type(c_ptr), value :: ctx
+      character(kind=c_char), intent(in) :: path(*)
+    end function
+    integer(c_int) function fsibe_read_backup(ctx, path) bind(C, name="fsibe_read_backup")
+      import :: c_int, c_ptr, c_char
+      type(c_ptr), value :: ctx
+      character(kind=c_char), intent(in) :: path(*)
+    end function
     integer(c_int) function fsibe_run(ctx, nsteps, rows) bind(C, name="fsibe_run")
       import :: c_int, c_ptr, c_double
       type(c_ptr), value :: ctx
@@ -203,6 +213,29 @@ contains
     use share_vars
     real(kind=pr), dimension(0:nx-1,0:ny-1), intent(in) :: vort
     call fsibe_check(fsibe_init_fields(gctx, vort), "init_fields")
+  end subroutine
+
+  ! MakeRuntimeBackup (save_fields.f90:109-152): the same file, written from the device state;
+  ! nbackup alternates between 0 and 1 as in the reference
+  subroutine makeruntimebackup_gb300(nbackup)
+    use share_vars
+    integer, intent(inout) :: nbackup
+    character(len=1) :: name1
+    write (name1, '(I1)') nbackup
+    call fsibe_check(fsibe_write_backup(gctx, trim(dir_name)//'/runtime_backup'//name1//'.in'//c_null_char), &
+                     "MakeRuntimeBackup")
+    nbackup = 1 - nbackup
+  end subroutine
+
+  ! inicond = 2: resume from runtime_backup<ibackup>.in (the caller picks the later file, as
+  ! init_fields.f90:44-92 does); replaces init_fields + init_beams + create_mask
+  subroutine resume_gb300(ibackup)
+    use share_vars
+    integer, intent(in) :: ibackup
+    character(len=1) :: name1
+    write (name1, '(I1)') ibackup
+    call fsibe_check(fsibe_read_backup(gctx, trim(dir_name)//'/runtime_backup'//name1//'.in'//c_null_char), &
+                     "init_fields (inicond=2)")
   end subroutine
 
   subroutine create_mask_gb300(time)

@@ -96,3 +96,32 @@ def test_resume_refusals(oracle, tmp_path):
         oracle.OracleRun(p).resume(bad)
     with pytest.raises(Exception):
         oracle.OracleRun(p).resume(tmp_path / "missing.in")
+
+
+def test_alternating_files_and_latest(oracle, tmp_path):
+    """MakeRuntimeBackup alternates between runtime_backup0.in and runtime_backup1.in;
+    inicond = 2 resumes from the later of the two (init_fields.f90:44-92)."""
+    from fsibe_2d_gb300 import backup_time
+    p = make_params(nx=64, ny=64, ns=32)
+    with pytest.raises(FileNotFoundError):
+        oracle.OracleRun(p).resume_latest(tmp_path)
+    o = oracle.OracleRun(p)
+    o.init_fields(seeded_vorticity(64, seed=3))
+    o.time_step(2)
+    nb = o.make_runtime_backup(tmp_path, 0)
+    assert nb == 1
+    t0 = o.scalars().time
+    o.time_step(2)
+    assert o.make_runtime_backup(tmp_path, nb) == 0
+    t1 = o.scalars().time
+    assert backup_time(tmp_path / "runtime_backup0.in") == t0
+    assert backup_time(tmp_path / "runtime_backup1.in") == t1 > t0
+    r = oracle.OracleRun(p)
+    assert r.resume_latest(tmp_path).endswith("runtime_backup1.in")
+    assert r.scalars().time == t1
+    assert np.array_equal(r.vortk(), o.vortk())
+    # the older file wins once it is rewritten later
+    o.time_step(1)
+    o.make_runtime_backup(tmp_path, 0)
+    assert r.resume_latest(tmp_path).endswith("runtime_backup0.in")
+    o.close(); r.close()
