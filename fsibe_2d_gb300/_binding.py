@@ -73,6 +73,7 @@ def declare(lib, prefix, ctx_type=C.c_void_p):
     f("download_beam", P, _dp, _dp, _dp, _dp, _dp)
     f("get_scalars", P, C.POINTER(FsibeScalars))
     f("write_backup", P, C.c_char_p)
+    f("surface_integral", P, C.c_double, _dp)
     f("read_backup", P, C.c_char_p)
     f("last_error", P, res=C.c_char_p)
 
@@ -195,6 +196,13 @@ class Run:
         plus init_beams / InitializeSolidSolver / the start-up create_mask (time_step.f90:60-84)."""
         v = _f64(vort, self.shape)
         self._call("init_fields", _ptr(v))
+
+    def BeamSurfaceIntegral(self, time):
+        """BeamForces.f90:306-509: returns the 11 columns of the 'surface' file (time, drag,
+        lift, drag_surf, lift_surf, Ft(1), Fn(1), Fp(1), Ft(2), Fn(2), Fp(2))."""
+        out = np.zeros(11)
+        self._call("surface_integral", C.c_double(time), _ptr(out))
+        return out
 
     def MakeRuntimeBackup(self, path):
         """Write the state between two steps as runtime_backup<n>.in (save_fields.f90:109-152):

@@ -7,6 +7,7 @@
 #include <algorithm>
 #include <array>
 #include <cmath>
+#include <cstddef>
 #include <cstdlib>
 #include <cstdio>
 #include <cstring>
@@ -32,6 +33,7 @@ void launch_mask_prep(const MaskArgs& a, double gerf, cudaStream_t st, bool pdl)
 void launch_mask(const MaskArgs& a, double gerf, bool fp32, cudaStream_t st, bool pdl);
 void launch_forces(const ForceArgs& a, double dxi, double dyi, cudaStream_t st, bool pdl);
 void launch_forces_geo(const ForceArgs& a, double dxi, double dyi, cudaStream_t st);
+void launch_surface_integral(const ForceArgs& a, const SurfArgs& s, double dxi, double dyi, double time, cudaStream_t st);
 void launch_beam(const BeamArgs& b, cudaStream_t st);
 void launch_beam_pre(const BeamArgs& b, cudaStream_t st);
 int beam_pre_smem_setup(int ns);
@@ -1629,6 +1631,30 @@ int fsibe_download_beam(fsibe_ctx* c, double* beam, double* po, double* pn, doub
     if (tn) CK(c, cudaMemcpyAsync(tn, c->beam[B_TN], 8 * ns, cudaMemcpyDeviceToHost, c->stream));
     CK(c, cudaStreamSynchronize(c->stream));
     return FSIBE_OK;
+}
+
+// ---- BeamSurfaceIntegral (BeamForces.f90:306-509) ---------------------------------------
+// From the stresses and pressure of the last fluid step and the current beam: between
+// GetForces and the solid step this is the reference's call (:129).
+int fsibe_surface_integral(fsibe_ctx* c, double time, double* out) {
+    if (!c || !out) return FSIBE_ERR_PARAM;
+    if (!c->initialized) { c->err = "surface_integral before init_fields"; return FSIBE_ERR_STATE; }
+    if (c->P.iViscous != 1 || c->P.iBeam <= 0) { c->err = "BeamSurfaceIntegral needs iViscous = 1 and a beam"; return FSIBE_ERR_PARAM; }
+    double dxi, dyi;
+    const ForceArgs f = force_args(c, dxi, dyi);
+    SurfArgs s;
+    s.nx = c->g.nx; s.ny = c->g.ny; s.fp32 = c->fp32 ? 1 : 0;
+    s.nblk = 2 * c->nsm;
+    s.u = c->phys[PH_U]; s.v = c->phys[PH_V];
+    s.mask = c->phys[PH_MASK]; s.mvx = c->phys[PH_MVX]; s.mvy = c->phys[PH_MVY];
+    static_assert(offsetof(DevScalars, mean_v_cur) == offsetof(DevScalars, mean_u_cur) + sizeof(double), "U, V adjacent");
+    s.mean = &c->S->mean_u_cur;  // mean_u_cur, mean_v_cur
+    s.part = c->dscratch;          // 2 nblk + 11 doubles of the nx ny scratch
+    s.out = c->dscratch + 2 * s.nblk;
+    launch_surface_integral(f, s, dxi, dyi, time, c->stream);
+    CKL(c);
+    CK(c, cudaMemcpyAsync(out, s.out, 8 * 11, cudaMemcpyDeviceToHost, c->stream));
+    return read_status(c);
 }
 
 // ---- runtime backup (save_fields.f90:109-152, init_fields.f90:44-100) ------------------

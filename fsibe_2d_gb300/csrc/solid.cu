@@ -709,6 +709,131 @@ void launch_mask(const MaskArgs& a, double gerf, bool fp32, cudaStream_t st, boo
     else launch_k(k_mask_raster<double>, dim3(blocks), dim3(32 * MASK_WARPS), 0, st, pdl, a, gerf);
 }
 
+// BeamSurfaceIntegral (BeamForces.f90:306-509)
+// ===================================================================================
+// phi4* interpolation of one field at (xt, yt) on the box (0,0)-(xl-dx, yl-dy)
+// (Interpolation.f90:6-48); false when the 9 x 9 stencil leaves the field.
+__device__ bool surf_interp(const ForceArgs& a, const void* f, double xt, double yt, double dxi, double dyi,
+                            double& out) {
+    const double x2 = a.xl - a.dx, y2 = a.yl - a.dy;
+    const int i = (int)div_cr(xt, dxi, a.rdxi), j = (int)div_cr(yt, dyi, a.rdyi);
+    if (xt > x2 || xt < 0.0 || yt > y2 || yt < 0.0 || i - 4 < 0 || j - 4 < 0 || i + 4 > a.nx - 1 || j + 4 > a.ny - 1)
+        return false;
+    double dlx[9], r = 0.0;
+    for (int d = 0; d < 9; ++d) dlx[d] = delta_phi4star(fabs((double)(i - 4 + d) * dxi - xt), dxi, a.rdxi, a.pi);
+    for (int e = 0; e < 9; ++e) {
+        const double dly = delta_phi4star(fabs((double)(j - 4 + e) * dyi - yt), dyi, a.rdyi, a.pi);
+        const size_t row = (size_t)(j - 4 + e) * a.nx + (i - 4);
+        for (int d = 0; d < 9; ++d) r += dlx[d] * dly * fld(f, a.fp32, row + d);
+    }
+    out = r;
+    return true;
+}
+
+// The penalization drag / lift sums over the grid, one partial pair per block:
+// sum mask (u - maskvx), sum mask (v - maskvy) (:483-486).  The FP32 form stores u - U.
+__global__ void __launch_bounds__(256) k_surface_fields(SurfArgs s) {
+    const size_t NN = (size_t)s.nx * s.ny;
+    const double Uc = s.fp32 ? s.mean[0] : 0.0, Vc = s.fp32 ? s.mean[1] : 0.0;
+    double d = 0.0, l = 0.0;
+    for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < NN; k += (size_t)gridDim.x * blockDim.x) {
+        const double m = fld(s.mask, s.fp32, k);
+        d += m * ((fld(s.u, s.fp32, k) + Uc) - fld(s.mvx, s.fp32, k));
+        l += m * ((fld(s.v, s.fp32, k) + Vc) - fld(s.mvy, s.fp32, k));
+    }
+    __shared__ double sm[2][8];
+    for (int o = 16; o > 0; o >>= 1) { d += __shfl_xor_sync(0xffffffffu, d, o); l += __shfl_xor_sync(0xffffffffu, l, o); }
+    if ((threadIdx.x & 31) == 0) { sm[0][threadIdx.x >> 5] = d; sm[1][threadIdx.x >> 5] = l; }
+    __syncthreads();
+    if (threadIdx.x < 2) {
+        double t = 0.0;
+        for (int w = 0; w < 8; ++w) t += sm[threadIdx.x][w];
+        s.part[2 * blockIdx.x + threadIdx.x] = t;
+    }
+}
+
+// The contour: two half circles of nc points at the ends (:341-420), the top and bottom lines
+// (:426-480), a point a thread; six force sums reduced over the block; out[11] as the
+// 'surface' file's columns.  One block of 256 threads.
+__global__ void __launch_bounds__(256) k_surface_integral(ForceArgs a, SurfArgs s, double dxi, double dyi, double time) {
+    const int nc = 128, ns = a.ns, npts = 2 * nc + 2 * ns;
+    const double pi = a.pi;
+    const double R = a.t_beam + a.N_smooth * fmax(a.dx, a.dy);
+    const double dphi = pi / (double)(nc - 1), dL = dphi * R;
+    double F[6] = {0, 0, 0, 0, 0, 0};  // Ft(1), Fn(1), Fp(1), Ft(2), Fn(2), Fp(2)
+    bool ok = true;
+    for (int p = threadIdx.x; p < npts; p += blockDim.x) {
+        double A = 0.0, B = 0.0, P = 0.0;
+        if (p < 2 * nc) {
+            const int end = p / nc, i = p % nc, node = end == 0 ? ns - 1 : 0;
+            const double beta = a.th[end == 0 ? ns - 1 : 1] + a.alpha;
+            const double phi = (end == 0 ? -(0.5 * pi - beta) : (0.5 * pi + beta)) + (double)i * dphi;
+            double sp_, cp_, s2, c2;
+            sincos(phi, &sp_, &cp_);
+            sincos(2.0 * phi, &s2, &c2);
+            const double xc = a.x[node] + R * cp_, yc = a.y[node] + R * sp_;
+            ok &= surf_interp(a, a.sa, xc, yc, dxi, dyi, A);
+            ok &= surf_interp(a, a.sb, xc, yc, dxi, dyi, B);
+            ok &= surf_interp(a, a.press, xc, yc, dxi, dyi, P);
+            const double sn = +A * c2 + B * s2, st = -A * s2 + B * c2, sp = -P;
+            F[0] += dL * st * (-sp_); F[3] += dL * st * (+cp_);
+            F[1] += dL * sn * (+cp_); F[4] += dL * sn * (+sp_);
+            F[2] += dL * sp * (+cp_); F[5] += dL * sp * (+sp_);
+        } else {
+            const int q = p - 2 * nc, i = q % ns;
+            const double sg = q < ns ? 1.0 : -1.0;
+            const double th = a.th[i] + a.alpha;
+            double sn_, cs_, s2, c2;
+            sincos(th, &sn_, &cs_);
+            sincos(2.0 * th, &s2, &c2);
+            const double x = a.x[i] - sg * R * sn_, y = a.y[i] + sg * R * cs_;
+            const double x1 = a.x[i] - sg * a.t_beam * sn_, y1 = a.y[i] + sg * a.t_beam * cs_;
+            ok &= surf_interp(a, a.sa, x, y, dxi, dyi, A);
+            ok &= surf_interp(a, a.sb, x, y, dxi, dyi, B);
+            ok &= surf_interp(a, a.press, x1, y1, dxi, dyi, P);
+            const double sn = -A * c2 - B * s2, st = -A * s2 + B * c2, sp = -P;
+            F[0] += a.ds * st * (sg * cs_); F[3] += a.ds * st * (sg * sn_);
+            F[1] += a.ds * sn * (-sg * sn_); F[4] += a.ds * sn * (sg * cs_);
+            F[2] += a.ds * sp * (-sg * sn_); F[5] += a.ds * sp * (sg * cs_);
+        }
+    }
+    if (!ok) set_status(a.S, FSIBE_ERR_INTERP_OOB);
+    __shared__ double sm[8][8];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int k = 0; k < 6; ++k) {
+        double v = F[k];
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (lane == 0) sm[k][warp] = v;
+    }
+    // the grid sums of k_surface_fields, one warp each
+    if (warp < 2) {
+        double v = 0.0;
+        for (int b = lane; b < s.nblk; b += 32) v += s.part[2 * b + warp];
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (lane == 0) sm[6 + warp][0] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t[6];
+        for (int k = 0; k < 6; ++k) {
+            t[k] = 0.0;
+            for (int w = 0; w < 8; ++w) t[k] += sm[k][w];
+        }
+        double* o = s.out;
+        o[0] = time;
+        o[1] = sm[6][0] * a.dx * a.dy;
+        o[2] = sm[7][0] * a.dx * a.dy;
+        o[3] = t[0] + t[1] + t[2];
+        o[4] = t[3] + t[4] + t[5];
+        for (int k = 0; k < 6; ++k) o[5 + k] = t[k];
+    }
+}
+
+void launch_surface_integral(const ForceArgs& a, const SurfArgs& s, double dxi, double dyi, double time, cudaStream_t st) {
+    k_surface_fields<<<s.nblk, 256, 0, st>>>(s);
+    k_surface_integral<<<1, 256, 0, st>>>(a, s, dxi, dyi, time);
+}
+
 void launch_forces_geo(const ForceArgs& a, double dxi, double dyi, cudaStream_t st) {
     k_forces_geo<<<a.ns, 128, 0, st>>>(a, dxi, dyi);
 }

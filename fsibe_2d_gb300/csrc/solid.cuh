@@ -42,6 +42,15 @@ struct ForceArgs {
     int fp32;
 };
 
+// BeamSurfaceIntegral's grid sums (BeamForces.f90:483-486) and its output.
+struct SurfArgs {
+    int nx, ny, nblk, fp32;
+    const void *u, *v, *mask, *mvx, *mvy;  // R*[ny][nx]; the FP32 form stores u - U
+    const double* mean;                     // U, V of the stored velocity (FP32 form)
+    double* part;                           // 2 nblk block partials
+    double* out;                            // 11 values
+};
+
 // The end of a time step (time_step.f90:152-161 / :222-236): old <- new beam loads, time +=
 // dt1, the step count and the beam_data row (BeamIO.f90:193-216), kept in the scalars and, when
 // a ring is given, appended to it.  Run by one block after everything else of the step.

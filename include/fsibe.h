@@ -180,6 +180,15 @@ int fsibe_download_beam(fsibe_ctx* ctx, double* beam, double* p_old, double* p_n
                         double* tau_old, double* tau_new);
 int fsibe_get_scalars(fsibe_ctx* ctx, fsibe_scalars* out);
 
+/* BeamSurfaceIntegral (BeamForces.f90:306-509): the stresses and pressure of the last fluid
+ * step, phi4*-interpolated on the contour around the beam (half circles of 128 points at the
+ * ends, the top and bottom lines), and the penalization drag/lift over the grid.
+ * out[11] = time, drag, lift, drag_surf, lift_surf, Ft(1), Fn(1), Fp(1), Ft(2), Fn(2), Fp(2),
+ * the columns of the reference's 'surface' file.  Replaces the call of BeamForces.f90:129; called
+ * between fsibe_get_forces and fsibe_solid_step it sees the reference's state.  Needs
+ * iViscous = 1 and a beam (else FSIBE_ERR_PARAM). */
+int fsibe_surface_integral(fsibe_ctx* ctx, double time, double* out);
+
 /* ---- runtime backup ----------------------------------------------------------
  * The file runtime_backup<n>.in of MakeRuntimeBackup (save_fields.f90:109-152): Fortran
  * sequential unformatted records (a 4-byte record length before and after each record),

@@ -853,8 +853,8 @@ static int DeltaInterpolation(const orc_ctx* c, double xt, double yt, const doub
     return FSIBE_OK;
 }
 
-/* GetForces + GetForcesInterp with SPL=3 (BeamForces.f90:6-288); BeamSurfaceIntegral (:306-509)
- * only writes a diagnostic file and is not restated. */
+/* GetForces + GetForcesInterp with SPL=3 (BeamForces.f90:6-288); BeamSurfaceIntegral
+ * (:306-509) is orc_surface_integral. */
 static int GetForces(orc_ctx* c, double time) {
     const size_t NN = (size_t)c->nx * c->ny;
     const int ns = c->ns;
@@ -1751,6 +1751,93 @@ int orc_newton_system(orc_ctx* c, double time, double dt, double dt_old, int met
     return st;
 }
 double orc_time(orc_ctx* c) { return c->time; }
+
+/* BeamSurfaceIntegral (BeamForces.f90:306-509), the diagnostic GetForces runs when
+ * viscous_tensions (:129): the stresses (as GetForces forms them from u, :105-118) and the
+ * pressure interpolated with phi4* on the contour around the beam -- two half circles of
+ * nc = 128 points at the ends, the top and bottom lines at t_beam + N_smooth max(dx,dy)
+ * (pressure at t_beam) -- and the penalization drag/lift over the whole grid.
+ * out[11]: time, drag, lift, drag_surf, lift_surf, Ft(1), Fn(1), Fp(1), Ft(2), Fn(2), Fp(2)
+ * (the columns of the 'surface' file, :492-499). */
+int orc_surface_integral(orc_ctx* c, double time, double* out) {
+    if (!c || !out) return FSIBE_ERR_PARAM;
+    if (!c->initialized) return fail(c, FSIBE_ERR_STATE, "surface_integral before init_fields");
+    if (c->P.iViscous != 1 || c->P.iBeam <= 0) return fail(c, FSIBE_ERR_PARAM, "BeamSurfaceIntegral needs iViscous = 1 and a beam");
+    const size_t NN = (size_t)c->nx * c->ny;
+    const int ns = c->ns, nc = 128;
+    const Beam& b = c->beam;
+    const double pi = c->pi, dx = c->dx, dy = c->dy;
+    std::vector<double> sa(NN), sb(NN), w1(NN), w2(NN), w3(NN);
+    const double* u1 = c->u.data();
+    const double* u2 = c->u.data() + NN;
+    coftxy(c, u1, w1.data()); cofdx(c, w1.data(), w2.data()); cofitxy(c, w2.data(), sa.data());
+    for (size_t k = 0; k < NN; ++k) sa[k] = 2.0 * c->P.nu * sa[k];
+    coftxy(c, u1, w1.data()); cofdy(c, w1.data(), w2.data()); cofitxy(c, w2.data(), w3.data());
+    coftxy(c, u2, w1.data()); cofdx(c, w1.data(), w2.data()); cofitxy(c, w2.data(), sb.data());
+    for (size_t k = 0; k < NN; ++k) sb[k] = c->P.nu * (w3[k] + sb[k]);
+    double alpha, alpha_t, alpha_tt, LE[6];
+    mouvement(c, time, alpha, alpha_t, alpha_tt, LE, b);
+    double Ft[2] = {0, 0}, Fn[2] = {0, 0}, Fp[2] = {0, 0};
+    int st = FSIBE_OK;
+    const double R = c->P.t_beam + c->P.N_smooth * std::max(dx, dy);
+    const double dphi = pi / (double)(nc - 1), dL = dphi * R;
+    for (int end = 0; end < 2; ++end) {  /* trailing edge (:341-377), leading edge (:379-420) */
+        const int node = end == 0 ? ns - 1 : 0;
+        const double beta = (end == 0 ? b.theta[ns - 1] : b.theta[1]) + alpha;
+        for (int i = 0; i < nc; ++i) {
+            const double phi = (end == 0 ? -(0.5 * pi - beta) : (0.5 * pi + beta)) + (double)i * dphi;
+            const double xc = b.x[node] + R * std::cos(phi), yc = b.y[node] + R * std::sin(phi);
+            double A, B, P;
+            st |= DeltaInterpolation(c, xc, yc, sa.data(), A);
+            st |= DeltaInterpolation(c, xc, yc, sb.data(), B);
+            st |= DeltaInterpolation(c, xc, yc, c->press.data(), P);
+            const double sn = +A * std::cos(2.0 * phi) + B * std::sin(2.0 * phi);
+            const double stt = -A * std::sin(2.0 * phi) + B * std::cos(2.0 * phi);
+            const double sp = -P;
+            Ft[0] = Ft[0] + dL * stt * (-std::sin(phi));
+            Ft[1] = Ft[1] + dL * stt * (+std::cos(phi));
+            Fn[0] = Fn[0] + dL * sn * (+std::cos(phi));
+            Fn[1] = Fn[1] + dL * sn * (+std::sin(phi));
+            Fp[0] = Fp[0] + dL * sp * (+std::cos(phi));
+            Fp[1] = Fp[1] + dL * sp * (+std::sin(phi));
+        }
+    }
+    for (int side = 0; side < 2; ++side) {  /* top (:426-451), bottom (:456-480) */
+        const double sg = side == 0 ? 1.0 : -1.0;
+        for (int i = 0; i < ns; ++i) {
+            const double th = b.theta[i] + alpha, s = std::sin(th), co = std::cos(th);
+            const double x = b.x[i] - sg * R * s, y = b.y[i] + sg * R * co;
+            const double x1 = b.x[i] - sg * c->P.t_beam * s, y1 = b.y[i] + sg * c->P.t_beam * co;
+            double A, B, P;
+            st |= DeltaInterpolation(c, x, y, sa.data(), A);
+            st |= DeltaInterpolation(c, x, y, sb.data(), B);
+            st |= DeltaInterpolation(c, x1, y1, c->press.data(), P);
+            const double sn = -A * std::cos(2.0 * th) - B * std::sin(2.0 * th);
+            const double stt = -A * std::sin(2.0 * th) + B * std::cos(2.0 * th);
+            const double sp = -P;
+            Ft[0] = Ft[0] + c->ds * stt * (sg * co);
+            Ft[1] = Ft[1] + c->ds * stt * (sg * s);
+            Fn[0] = Fn[0] + c->ds * sn * (-sg * s);
+            Fn[1] = Fn[1] + c->ds * sn * (sg * co);
+            Fp[0] = Fp[0] + c->ds * sp * (-sg * s);
+            Fp[1] = Fp[1] + c->ds * sp * (sg * co);
+        }
+    }
+    if (st) return fail(c, FSIBE_ERR_INTERP_OOB, "DeltaInterpolation: target coordinates not in the field");
+    double drag = 0.0, lift = 0.0;
+    for (size_t k = 0; k < NN; ++k) {
+        drag += c->mask[k] * (u1[k] - c->maskvx[k]);
+        lift += c->mask[k] * (u2[k] - c->maskvy[k]);
+    }
+    out[0] = time;
+    out[1] = drag * dx * dy;
+    out[2] = lift * dx * dy;
+    out[3] = Ft[0] + Fn[0] + Fp[0];
+    out[4] = Ft[1] + Fn[1] + Fp[1];
+    out[5] = Ft[0]; out[6] = Fn[0]; out[7] = Fp[0];
+    out[8] = Ft[1]; out[9] = Fn[1]; out[10] = Fp[1];
+    return FSIBE_OK;
+}
 
 /* MakeRuntimeBackup (save_fields.f90:109-152): the records of runtime_backup<n>.in for the
  * state between two steps (n0 the current level, n1 the previous one, after the level

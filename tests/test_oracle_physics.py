@@ -124,3 +124,26 @@ def test_short_fsi_run_is_deterministic_and_sane(oracle):
     assert np.array_equal(rows[0], rows[1])
     assert np.all(np.isfinite(rows[0]))
     assert rows[0][-1, 10] > 0.0  # drag of an impulsively started plate is positive
+
+
+def test_surface_integral_oracle(oracle):
+    """BeamSurfaceIntegral (BeamForces.f90:306-509) on the oracle: finite, its time column,
+    and the penalization drag/lift over the grid equal to the sum of mask (u - us) dx dy."""
+    import numpy as np
+    from conftest import seeded_vorticity
+    from fsibe_2d_gb300 import make_params
+    n = 128
+    p = make_params(nx=n, ny=n, ns=32)
+    o = oracle.OracleRun(p)
+    o.init_fields(seeded_vorticity(n, seed=4))
+    o.time_step(3)
+    t = o.scalars().time
+    o.create_mask(t); o.EvolveFluidAB2(); o.GetForces(t)
+    out = o.BeamSurfaceIntegral(t)
+    assert out.shape == (11,) and np.all(np.isfinite(out)) and out[0] == t
+    m, mvx, mvy = o.mask()
+    u = o.u().reshape(2, n, n)
+    dx = p.xl / n
+    assert abs(out[1] - np.sum(m * (u[0] - mvx)) * dx * dx) <= 1e-12 * max(1.0, abs(out[1]))
+    assert out[3] == out[5] + out[6] + out[7] and out[4] == out[8] + out[9] + out[10]
+    o.close()
