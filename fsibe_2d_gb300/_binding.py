@@ -14,7 +14,7 @@ import struct
 
 import numpy as np
 
-from ._abi import FsibeParams, FsibeScalars, STATUS_NAMES, FSIBE_ERR_BRAKE
+from ._abi import FsibeParams, FsibeScalars, STATUS_NAMES, FSIBE_ERR_BRAKE, FSIBE_RECORD_COLS
 
 _dp = C.POINTER(C.c_double)
 
@@ -59,6 +59,7 @@ def declare(lib, prefix, ctx_type=C.c_void_p):
     f("advance", P)
     f("step", P)
     f("run", P, C.c_int, _dp)
+    f("run_records", P, C.c_int, _dp)
     f("upload_vortk", P, _dp)
     f("download_vortk", P, _dp)
     f("download_vort", P, _dp)
@@ -267,6 +268,14 @@ class Run:
         rows = np.zeros((nsteps, 21))
         self._call("run", C.c_int(nsteps), _ptr(rows), soft=(FSIBE_ERR_BRAKE,))
         return rows
+
+    def run_records(self, nsteps):
+        """nsteps iterations of the time loop with its per-step output (time_step.f90:178-236):
+        an (nsteps, FSIBE_RECORD_COLS) array of the beam_data, u_max, energies and IBES_iter
+        rows; fsibe_2d_gb300.outputs.write_step_files writes them in the reference's files."""
+        rec = np.zeros((nsteps, FSIBE_RECORD_COLS))
+        self._call("run_records", C.c_int(nsteps), _ptr(rec), soft=(FSIBE_ERR_BRAKE,))
+        return rec
 
     # -- state -----------------------------------------------------------------------
     def vortk(self):

@@ -1457,6 +1457,8 @@ static int init_state(fsibe_ctx* c, const double* vort, bool keep_mask) {
     return FSIBE_OK;
 }
 
+static int read_status(fsibe_ctx* c);
+
 int fsibe_init_fields(fsibe_ctx* c, const double* vort) {
     if (!c || !vort) return FSIBE_ERR_PARAM;
     return init_state(c, vort, false);
@@ -1467,8 +1469,7 @@ int fsibe_create_mask(fsibe_ctx* c, double time) {
     (void)time;  // mouvement case 0 does not depend on time
     int st = create_mask(c);
     if (st) return st;
-    CK(c, cudaStreamSynchronize(c->stream));
-    return FSIBE_OK;
+    return read_status(c);  // a beam point below the domain: FSIBE_ERR_MASK_OOB
 }
 
 static int read_status(fsibe_ctx* c) {
@@ -1523,13 +1524,15 @@ int fsibe_step(fsibe_ctx* c) {
     return do_step(c);
 }
 
-int fsibe_run(fsibe_ctx* c, int nsteps, double* rows) {
+// nsteps steps with the per-step records kept in the device ring (FSIBE_RECORD_COLS a step);
+// cols = 21 copies the beam_data rows alone (a pitched copy of the ring's first columns)
+static int run_steps(fsibe_ctx* c, int nsteps, double* out, int cols) {
     if (!c || nsteps < 0) return FSIBE_ERR_PARAM;
-    if (rows) {
+    if (out) {
         if (c->rows_cap < nsteps) {
             if (c->rows) cudaFree(c->rows);
             c->rows = nullptr;
-            CK(c, cudaMalloc((void**)&c->rows, 8 * 21 * (size_t)(nsteps > 0 ? nsteps : 1)));
+            CK(c, cudaMalloc((void**)&c->rows, 8 * FSIBE_RECORD_COLS * (size_t)(nsteps > 0 ? nsteps : 1)));
             c->rows_cap = nsteps;
             free_graph(c);  // the graph captured the old ring pointer
         }
@@ -1543,8 +1546,16 @@ int fsibe_run(fsibe_ctx* c, int nsteps, double* rows) {
         int st = do_step(c);
         if (st) return st;
     }
-    if (rows && nsteps > 0) CK(c, cudaMemcpyAsync(rows, c->rows, 8 * 21 * (size_t)nsteps, cudaMemcpyDeviceToHost, c->stream));
+    if (out && nsteps > 0)
+        CK(c, cudaMemcpy2DAsync(out, 8 * (size_t)cols, c->rows, 8 * (size_t)FSIBE_RECORD_COLS, 8 * (size_t)cols,
+                                (size_t)nsteps, cudaMemcpyDeviceToHost, c->stream));
     return read_status(c);
+}
+
+int fsibe_run(fsibe_ctx* c, int nsteps, double* rows) { return run_steps(c, nsteps, rows, 21); }
+
+int fsibe_run_records(fsibe_ctx* c, int nsteps, double* records) {
+    return run_steps(c, nsteps, records, FSIBE_RECORD_COLS);
 }
 
 // ---- state transfer -------------------------------------------------------------------
@@ -2588,10 +2599,19 @@ const char* fsibe_ensemble_last_error(fsibe_ensemble* e) { return e ? e->err.c_s
 static __device__ __align__(256) double g_static_scratch[2 * FSIBE_STATIC_MAX_CELLS + FSIBE_STATIC_TABLES];
 
 namespace {
-// Device address of g_static_scratch, looked up once per device (host code may not use the
-// symbol itself: on the host it names a stand-in, not device memory).
-double* g_static_dev[128] = {};
+// Device address of g_static_scratch per device (host code may not use the symbol itself: on
+// the host it names a stand-in, not device memory), and the transform kernels per
+// (device, length), filled on first use.  The address is looked up again on every call made
+// outside a stream capture, so a device reset or another context made current since the last
+// call cannot leave a stale address behind; during a capture the last looked-up address of
+// the device is used.
+constexpr int kStaticDevs = 128;
+double* g_static_dev[kStaticDevs] = {};
+SizeKernels<double> g_static_k[kStaticDevs][7];  // lengths 32 .. 2048
+bool g_static_k_ok[kStaticDevs][7] = {};
 std::mutex g_static_mu;
+
+int static_log2_index(int n) { int i = 0; while ((32 << i) < n) ++i; return i; }
 
 __global__ void k_static_twiddles(double2* twY, int ny, double2* twX, int hx, double2* twR, int nx) {
     const int total = ny + hx + hx + 1;
@@ -2623,11 +2643,16 @@ extern "C" int fsibe_coftxy_static(const double* f_dev, double* fk_dev, int32_t 
     }
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess || dev < 0 || dev >= 128) { g_err = "fsibe_coftxy_static: cudaGetDevice failed"; return FSIBE_ERR_CUDA; }
+    if (e != cudaSuccess || dev < 0 || dev >= kStaticDevs) { g_err = "fsibe_coftxy_static: cudaGetDevice failed"; return FSIBE_ERR_CUDA; }
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    e = cudaStreamIsCapturing(st, &cap);
+    if (e != cudaSuccess) { g_err = std::string("fsibe_coftxy_static: cudaStreamIsCapturing: ") + cudaGetErrorString(e); return FSIBE_ERR_CUDA; }
     double* base;
+    SizeKernels<double> kx, ky;
     {
         std::lock_guard<std::mutex> lk(g_static_mu);
-        if (!g_static_dev[dev]) {
+        if (cap == cudaStreamCaptureStatusNone) {
             void* p = nullptr;
             e = cudaGetSymbolAddress(&p, g_static_scratch);
             if (e != cudaSuccess || !p) {
@@ -2635,19 +2660,28 @@ extern "C" int fsibe_coftxy_static(const double* f_dev, double* fk_dev, int32_t 
                 return FSIBE_ERR_CUDA;
             }
             g_static_dev[dev] = static_cast<double*>(p);
+        } else if (!g_static_dev[dev]) {
+            g_err = "fsibe_coftxy_static: the first call on a device must come before any stream capture";
+            return FSIBE_ERR_STATE;
         }
         base = g_static_dev[dev];
+        for (int n : {nx, ny}) {
+            const int li = static_log2_index(n);
+            if (!g_static_k_ok[dev][li]) {
+                SizeKernels<float> unused;
+                if (!get_sizes(n, g_static_k[dev][li], unused)) { g_err = "fsibe_coftxy_static: size"; return FSIBE_ERR_UNSUPPORTED; }
+                g_static_k_ok[dev][li] = true;
+            }
+        }
+        kx = g_static_k[dev][static_log2_index(nx)];
+        ky = g_static_k[dev][static_log2_index(ny)];
     }
-    SizeKernels<double> kx, ky;
-    SizeKernels<float> fx, fy;
-    if (!get_sizes(nx, kx, fx) || !get_sizes(ny, ky, fy)) { g_err = "fsibe_coftxy_static: size"; return FSIBE_ERR_UNSUPPORTED; }
     const int hx = nx / 2;
     double2* T = reinterpret_cast<double2*>(base);
     double2* Sx = reinterpret_cast<double2*>(base + FSIBE_STATIC_MAX_CELLS);
     double2* twY = reinterpret_cast<double2*>(base + 2 * FSIBE_STATIC_MAX_CELLS);
     double2* twX = twY + ny;
     double2* twR = twX + hx;
-    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
     k_static_twiddles<<<16, 256, 0, st>>>(twY, ny, twX, hx, twR, nx);
     KArgs<double> a;
     std::memset(&a, 0, sizeof(a));

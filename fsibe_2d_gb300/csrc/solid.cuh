@@ -53,7 +53,10 @@ struct SurfArgs {
 
 // The end of a time step (time_step.f90:152-161 / :222-236): old <- new beam loads, time +=
 // dt1, the step count and the beam_data row (BeamIO.f90:193-216), kept in the scalars and, when
-// a ring is given, appended to it.  Run by one block after everything else of the step.
+// a ring is given, appended to it as one record of FSIBE_RECORD_COLS values: the beam_data row,
+// then the step's u_max row (NavierStokes.f90:80-82), energies row (:259-261) and IBES_iter row
+// (SolidSolver.f90:392-394), which the reference writes with the time before the step.  Run by
+// one block after everything else of the step.
 struct AdvArgs {
     DevScalars* S;
     int ns;
@@ -70,6 +73,7 @@ __device__ __forceinline__ void advance_state(const AdvArgs& a, const double* ti
     if (threadIdx.x == 0) {
         DevScalars* S = a.S;
         const int ns = a.ns;
+        const double t_before = S->time;
         S->time = S->time + S->dt1;
         S->step += 1;
         const double t0 = tip ? tip[0] : a.x[ns - 1], t1 = tip ? tip[1] : a.y[ns - 1], t2 = tip ? tip[2] : a.vx[ns - 1],
@@ -80,7 +84,13 @@ __device__ __forceinline__ void advance_state(const AdvArgs& a, const double* ti
                                 S->inertial_force[0], S->inertial_force[1], S->e_kinetic, S->e_elastic, S->e_pot};
         for (int c = 0; c < 21; ++c) S->row[c] = row[c];
         if (a.rows && S->run_row < S->run_cap) {
-            for (int c = 0; c < 21; ++c) a.rows[(size_t)S->run_row * 21 + c] = row[c];
+            double* rec = a.rows + (size_t)S->run_row * FSIBE_RECORD_COLS;
+            for (int c = 0; c < 21; ++c) rec[c] = row[c];
+            const double tail[FSIBE_RECORD_COLS - 21] = {
+                t_before, S->dt1, S->u_max, S->mean_ux, S->mean_uy,
+                t_before, S->dt1, S->vor_rms, S->kinetic, S->dissipation, S->porous_diss, S->inflow_solid, S->inflow_mean,
+                t_before, (double)S->newton_iters};
+            for (int c = 21; c < FSIBE_RECORD_COLS; ++c) rec[c] = tail[c - 21];
             S->run_row += 1;
         }
     }

@@ -162,6 +162,20 @@ int fsibe_step(fsibe_ctx* ctx);
  * row per step (rows[s*21 + c]). Stops early on a non-zero status. */
 int fsibe_run(fsibe_ctx* ctx, int nsteps, double* rows);
 
+/* Per-step records of fsibe_run_records: everything the reference appends to its
+ * per-step text files in one time step, FSIBE_RECORD_COLS values a step.  The device keeps
+ * them in a ring during the run; one copy to the host at the end.
+ *   [0..20]  the beam_data row, written after the step (BeamIO.f90:193-216, SaveBeamData)
+ *   [21..25] the u_max row: time, dt1, u_max, mean u, mean v (NavierStokes.f90:80-82)
+ *   [26..33] the energies row: time, dt1, vor_rms, kinetic, dissipation, porous_diss,
+ *            inflow_solid, inflow_mean (NavierStokes.f90:259-261)
+ *   [34..35] the IBES_iter row: time, Newton iterations (SolidSolver.f90:392-394)
+ * The last three carry the time before the step, as the reference writes them during it. */
+#define FSIBE_RECORD_COLS 36
+/* nsteps calls of fsibe_step with one record per step (records[s*FSIBE_RECORD_COLS + c]);
+ * the time loop of time_step.f90:178-236 with its per-step output. */
+int fsibe_run_records(fsibe_ctx* ctx, int nsteps, double* records);
+
 /* ---- state transfer (host <-> HBM) --------------------------------------- */
 int fsibe_upload_vortk(fsibe_ctx* ctx, const double* vortk_packed);
 int fsibe_download_vortk(fsibe_ctx* ctx, double* vortk_packed);
@@ -313,7 +327,11 @@ const char* fsibe_ensemble_last_error(fsibe_ensemble* ens);
  * FSIBE_ERR_UNSUPPORTED (message in fsibe_last_error(NULL)) without launching anything.
  * The first call on a device looks up the scratch's device address
  * (cudaGetSymbolAddress) with that device current; make that first call before any stream
- * capture.  All calls share the one scratch array, so calls that overlap on the GPU
+ * capture.  Every later call made outside a capture looks the address up again, so a
+ * device reset or another context made current in between leaves no stale address; a call
+ * made during a capture uses the address of the device's last uncaptured call (a capture
+ * on a device with no earlier call returns FSIBE_ERR_STATE).
+ * All calls share the one scratch array, so calls that overlap on the GPU
  * (different streams, or different host threads) race; every call rewrites all the
  * scratch it reads, so nothing carries over from the previous call. */
 int fsibe_coftxy_static(const double* f_dev, double* fk_dev, int32_t nx, int32_t ny, void* cuda_stream);

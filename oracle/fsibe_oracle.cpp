@@ -1676,6 +1676,29 @@ int orc_run(orc_ctx* c, int nsteps, double* rows) {
     return FSIBE_OK;
 }
 
+/* The time loop with its per-step output (time_step.f90:178-236): per step the beam_data row
+ * (BeamIO.f90:193-216), then the rows the step appends to u_max (NavierStokes.f90:80-82),
+ * energies (:259-261) and IBES_iter (SolidSolver.f90:392-394), which carry the time before
+ * the step. */
+int orc_run_records(orc_ctx* c, int nsteps, double* rec) {
+    for (int s = 0; s < nsteps; ++s) {
+        const double t_before = c->time;
+        int st = orc_step(c);
+        if (rec) {
+            double* r = rec + (size_t)s * FSIBE_RECORD_COLS;
+            std::memcpy(r, c->sc.beam_data, 21 * sizeof(double));
+            const fsibe_scalars& q = c->sc;
+            const double tail[FSIBE_RECORD_COLS - 21] = {
+                t_before, q.dt1, q.u_max, q.mean_ux, q.mean_uy,
+                t_before, q.dt1, q.vor_rms, q.kinetic, q.dissipation, q.porous_diss, q.inflow_solid, q.inflow_mean,
+                t_before, (double)q.newton_iters};
+            std::memcpy(r + 21, tail, sizeof(tail));
+        }
+        if (st) return st;
+    }
+    return FSIBE_OK;
+}
+
 int orc_upload_vortk(orc_ctx* c, const double* v) { std::memcpy(c->vortk[c->n0].data(), v, c->vortk[0].size() * 8); return FSIBE_OK; }
 int orc_download_vortk(orc_ctx* c, double* v) { std::memcpy(v, c->vortk[c->n0].data(), c->vortk[0].size() * 8); return FSIBE_OK; }
 int orc_download_vort(orc_ctx* c, double* v) { cofitxy(c, c->vortk[c->n0].data(), v); return FSIBE_OK; }

@@ -1,0 +1,52 @@
+"""The per-step text files in the reference's Fortran formats (fsibe_2d_gb300.outputs):
+ESw.d edits of known values, the line layouts of beam_data, u_max, energies and IBES_iter,
+and the files the oracle's records produce (append mode, one line per step)."""
+import numpy as np
+
+from fsibe_2d_gb300 import make_params
+from fsibe_2d_gb300 import outputs as O
+from fsibe_2d_gb300._abi import FSIBE_RECORD_COLS
+
+
+def test_es_edit_descriptor():
+    assert O.es(1.0, 15, 8) == " 1.00000000E+00"
+    assert O.es(-0.00123, 15, 8) == "-1.23000000E-03"
+    assert O.es(0.0, 12, 4) == "  0.0000E+00"
+    assert O.es(123456.0, 11, 4) == " 1.2346E+05"
+    assert O.es(2.5e-5, 12, 4) == "  2.5000E-05"
+    assert O.es(1e-100, 15, 8) == " 1.00000000-100"     # three-digit exponents drop the E
+    assert O.es(-9.99999999999e99, 12, 4) == " -1.0000+100"
+    assert O.es(1.0, 5, 4) == "*****"                   # does not fit
+
+
+def test_line_layouts():
+    r = np.arange(1, FSIBE_RECORD_COLS + 1, dtype=float) * 0.5
+    assert O.beam_data_line(r[O.BEAM]).count("E") == 21 and len(O.beam_data_line(r[O.BEAM])) == 21 * 16
+    assert O.u_max_line(r[O.UMAX]).startswith("  ") and len(O.u_max_line(r[O.UMAX])) == 1 + 5 * 13
+    assert len(O.energies_line(r[O.ENERGIES])) == 8 * 16
+    assert O.ibes_iter_line([0.25, 3]) == " 2.5000E-01   3"
+
+
+def test_oracle_records_write_the_reference_files(oracle, tmp_path):
+    from conftest import seeded_vorticity
+    p = make_params(nx=64, ny=64, ns=16)
+    o = oracle.OracleRun(p)
+    o.init_fields(seeded_vorticity(64))
+    rec = o.run_records(5)
+    rows = oracle.OracleRun(p)
+    rows.init_fields(seeded_vorticity(64))
+    assert np.array_equal(rows.time_step(5), rec[:, :21])       # beam_data: the same rows as fsibe_run
+    # the u_max, energies and IBES_iter rows carry the time before the step
+    assert np.array_equal(rec[1:, 21], rec[:-1, 0]) and rec[0, 21] == 0.0
+    assert np.array_equal(rec[:, 26], rec[:, 21]) and np.array_equal(rec[:, 34], rec[:, 21])
+    assert rec[0, 35] == 0 and np.all(rec[1:, 35] >= 3)     # no solve at time 0 (not released)
+    paths = O.write_step_files(str(tmp_path), rec[:3])
+    O.write_step_files(str(tmp_path), rec[3:])                  # appended
+    names = sorted(f.name for f in tmp_path.iterdir())
+    assert names == ["IBES_iter", "beam_data1", "energies", "u_max"]
+    for path in paths:
+        lines = open(path).read().splitlines()
+        assert len(lines) == (4 if path.endswith("IBES_iter") else 5)
+    first = open(tmp_path / "beam_data1").read().splitlines()[0].split()
+    assert np.allclose([float(v) for v in first], rec[0, :21], rtol=1e-8, atol=0)
+    o.close(); rows.close()

@@ -34,6 +34,15 @@ def test_static_scratch_transform_matches_fft_forward_twice():
         torch.cuda.synchronize()
         assert st == 0, lib.fsibe_last_error(None)
         assert rel(out.cpu().numpy(), ref) < 1e-13
+        # the defining property: once its kernels are loaded (the call above), further calls
+        # take no device memory at all
+        torch.cuda.synchronize()
+        free0 = torch.cuda.mem_get_info()[0]
+        for _ in range(5):
+            assert fn(fd.data_ptr(), out.data_ptr(), nx, ny, None) == 0
+        torch.cuda.synchronize()
+        assert torch.cuda.mem_get_info()[0] == free0
+        assert rel(out.cpu().numpy(), ref) < 1e-13
 
 
 def test_static_scratch_rejects_sizes_beyond_its_maximum():
