@@ -243,7 +243,7 @@ def gpu_arm(args):
     e2e_val = NX * NY * e2e_steps / (t1 - t0) / 1e6
     del vfin
 
-    ens = ensemble_c4(F, args) if rank == 0 else None
+    ens = ensemble_c4(F, args, rank, world)
     adj = adjoint_c3(F) if rank == 0 else None
     large = large_run_c5(F, measured_peaks()[0]) if rank == 0 and not args.no_large else None
 
@@ -374,10 +374,13 @@ def adjoint_c3(F):
     return out
 
 
-def ensemble_c4(F, args):
+def ensemble_c4(F, args, rank=0, world=1):
     """The batched configuration: 48 runs at 256^2, 12 at 512^2 and 4 at 1024^2, ns = nx/4,
     FP32-compensated, seeded parameters (Re uniform in [100, 1000], EI log-uniform in [0.01, 1],
-    density ratio uniform in [0.5, 5]); one graph launch advances all 64 runs by one step."""
+    density ratio uniform in [0.5, 5]); one graph launch advances a rank's runs by one step.
+    With several ranks the runs are shared out by cost (fsibe_2d_gb300.sharding, no exchange
+    on the data path) and the step time is the slowest rank's."""
+    from fsibe_2d_gb300.sharding import ShardedEnsemble
     rng = np.random.default_rng(4)
     ps = []
     for n, count in ((256, 48), (512, 12), (1024, 4)):
@@ -385,16 +388,21 @@ def ensemble_c4(F, args):
             ps.append(F.make_params(nx=n, ny=n, ns=n // 4, precision=F.FSIBE_FP32C, dt=5e-5,
                                     Re=float(rng.uniform(100, 1000)), EI=float(10 ** rng.uniform(-2, 0)),
                                     mu=float(rng.uniform(0.5, 5))))
-    ens = F.Ensemble(ps)
-    for k, (p, r) in enumerate(zip(ps, ens.runs)):
-        r.init_fields(seeded_vorticity(p.nx, seed=100 + k))
+    ens = ShardedEnsemble(ps, rank, world)
+    ens.init_fields(lambda i: seeded_vorticity(ps[i].nx, seed=100 + i))
     ens.step(max(args.warmup, 3))
     K = max(args.steps // 2, 5)
-    ms = ens.time_steps(K)
+    ms = ens.ens.time_steps(K) if ens.ens else 0.0
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        t = torch.tensor([ms], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX, group=dist.new_group(backend="gloo"))
+        ms = float(t.item())
     cells = sum(p.nx * p.ny for p in ps)
     ens.close()
     return {"workload": "48 x 256^2 + 12 x 512^2 + 4 x 1024^2 runs, ns=nx/4, FP32-compensated, seeded parameters",
-            "runs": len(ps), "steps": K, "ms_per_step": round(ms / K, 5),
+            "runs": len(ps), "ranks": world, "steps": K, "ms_per_step": round(ms / K, 5),
             "value": round(cells * K / (ms * 1e-3) / 1e6, 2), "unit": "Mcell-steps/s"}
 
 

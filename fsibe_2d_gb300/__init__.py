@@ -52,6 +52,9 @@ def library():
         L.fsibe_drag_objective.argtypes = [C.c_void_p, _dp, C.c_double, C.c_int, C.c_int, _dp]
         L.fsibe_drag_gradient.argtypes = [C.c_void_p, _dp, C.c_double, C.c_int, C.c_int, C.c_int, _dp, _dp, _dp, _dp,
                                           C.POINTER(AdjointInfo)]
+        L.fsibe_force_objective.argtypes = [C.c_void_p, C.c_int, _dp, C.c_double, C.c_int, C.c_int, _dp]
+        L.fsibe_force_gradient.argtypes = [C.c_void_p, C.c_int, _dp, C.c_double, C.c_int, C.c_int, C.c_int, _dp, _dp,
+                                           _dp, _dp, C.POINTER(AdjointInfo)]
         _lib = L
     return _lib
 
@@ -93,6 +96,33 @@ class Run(_Run):
         return out.value
 
     # -- adjoint on a prescribed rigid mask (FP64 form, iFLUSI = 0) -----------------------
+    def force_objective(self, component, vort0, nsteps, avg_from, nu=0.0):
+        """Mean of Force(component + 1) -- 0 drag, 1 lift -- after steps avg_from..nsteps from the
+        physical vorticity vort0 (ny, nx)."""
+        v = np.ascontiguousarray(vort0, dtype=np.float64)
+        J = C.c_double()
+        self._call("force_objective", C.c_int(component), v.ctypes.data_as(C.POINTER(C.c_double)), C.c_double(nu),
+                   C.c_int(nsteps), C.c_int(avg_from), C.byref(J))
+        return J.value
+
+    def force_gradient(self, component, vort0, nsteps, avg_from, nu=0.0, snapshots=40):
+        """(J, dJ/dvort0, dJ/dmask, dJ/dnu, info) of force_objective by the discrete adjoint with
+        checkpointing."""
+        v = np.ascontiguousarray(vort0, dtype=np.float64)
+        gv = np.empty((self.ny, self.nx))
+        gm = np.empty((self.ny, self.nx))
+        J, gnu, info = C.c_double(), C.c_double(), AdjointInfo()
+        dp = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
+        self._call("force_gradient", C.c_int(component), dp(v), C.c_double(nu), C.c_int(nsteps), C.c_int(avg_from),
+                   C.c_int(snapshots), C.byref(J), dp(gv), dp(gm), C.byref(gnu), C.byref(info))
+        return J.value, gv, gm, gnu.value, info
+
+    def lift_objective(self, vort0, nsteps, avg_from, nu=0.0):
+        return self.force_objective(1, vort0, nsteps, avg_from, nu)
+
+    def lift_gradient(self, vort0, nsteps, avg_from, nu=0.0, snapshots=40):
+        return self.force_gradient(1, vort0, nsteps, avg_from, nu, snapshots)
+
     def drag_objective(self, vort0, nsteps, avg_from, nu=0.0):
         """Mean drag after steps avg_from..nsteps from the physical vorticity vort0 (ny, nx)."""
         v = np.ascontiguousarray(vort0, dtype=np.float64)

@@ -6,7 +6,7 @@
 //   u = Phi(i ky Pi W) + U,  v = -Phi(i kx Pi W) + V,  wx = Phi(i kx W),  wy = Phi(i ky W)
 //   N = F(-(u wx + v wy)) + i kx F(-chi v) - i ky F(-chi u)
 //   W' = (W + b10 N + b11 M) E D,  M' = N E           (Euler start-up: W' = (W + dt N) E D)
-//   drag' = dx dy sum_window chi u'
+//   drag' = dx dy sum_window chi u',  lift' = dx dy sum_window chi v'
 // with F the forward transform (1/(nx ny), Nyquist row dropped), Phi the inverse (Im of the
 // kx = 0 column ignored, X[nx/2] = 0), Pi = 1/|k|^2 (0 at k = 0), E = exp(-nu dt |k|^2), D the
 // 2/3 rule.  Their exact transposes, in the real-pair inner product over the stored modes:
@@ -31,6 +31,7 @@ struct AdjArgs {
     double *lu, *lv, *lwx, *lwy, *gmask, *ubar, *part;
     const DevScalars* S;
     double* J;
+    int comp;            // the objective's force component: 0 drag (Force(1)), 1 lift (Force(2))
 };
 
 __device__ __forceinline__ void adj_mode(const Geometry& g, int i, int& kx, int& ky, int& ks) {
@@ -105,18 +106,20 @@ __global__ void k_adj_combine(AdjArgs a) {
     }
 }
 
-// Gd = nx ny (1 + [kx > 0]) Pi (-i ky) G3   (G3 = F(dx dy chi 1_window)): d drag / d W
+// G3 = F(dx dy chi 1_window).  Drag = dx dy sum_window chi (u - u_s) with u = Phi(i ky Pi W) + U:
+// Gd = nx ny (1 + [kx > 0]) Pi (-i ky) G3 = d drag / d W.  Lift uses v = -Phi(i kx Pi W) + V:
+// Gd = nx ny (1 + [kx > 0]) Pi (i kx) G3 = d lift / d W.
 __global__ void k_adj_gdrag(AdjArgs a) {
     const int n = a.g.hx * a.g.ny;
     const double N = (double)a.g.nx * (double)a.g.ny;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         int kx, ky, ks;
         adj_mode(a.g, i, kx, ky, ks);
-        const double kys = (double)ks * a.g.kys;
+        const double kys = (double)ks * a.g.kys, kxs = (double)kx * a.g.kxs;
         const double k2 = (double)(kx * kx) * a.g.scalex + (double)(ks * ks) * a.g.scaley;
         const double pi = (kx == 0 && ky == 0) ? 0.0 : 1.0 / k2;
         const double s = N * (kx == 0 ? 1.0 : 2.0);
-        a.Gd[i] = cscale<double>(cimul<double>(a.G3[i], -kys), s * pi);
+        a.Gd[i] = cscale<double>(cimul<double>(a.G3[i], a.comp ? kxs : -kys), s * pi);
     }
 }
 
@@ -151,15 +154,16 @@ __global__ void k_adj_reduce(const double* part, int nparts, double scale, doubl
     }
 }
 
-// forward sweep: ubar += c u, J += c drag
+// forward sweep: ubar += c u (drag) or c v (lift), J += c Force(comp)
 __global__ void k_adj_accum(AdjArgs a, size_t ncell) {
+    const double* vel = a.comp ? a.v : a.u;
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < ncell; i += (size_t)gridDim.x * blockDim.x)
-        a.ubar[i] += a.c_obj * a.u[i];
-    if (blockIdx.x == 0 && threadIdx.x == 0) *a.J += a.c_obj * a.S->force[0];
+        a.ubar[i] += a.c_obj * vel[i];
+    if (blockIdx.x == 0 && threadIdx.x == 0) *a.J += a.c_obj * a.S->force[a.comp];
 }
 
 // h = dx dy chi 1_window (physical, into lu), and the final mask gradient
-// gmask += dx dy ubar 1_window
+// gmask += dx dy ubar 1_window (ubar: the weighted sum of u for the drag, of v for the lift)
 __global__ void k_adj_window(AdjArgs a, int ix0, int ix1, int iy0, int iy1, int final_pass) {
     const int nx = a.g.nx, ny = a.g.ny;
     const double dxdy = a.g.dx * a.g.dy;

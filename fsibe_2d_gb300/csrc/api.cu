@@ -1755,6 +1755,8 @@ int fsibe_write_backup(fsibe_ctx* c, const char* path) {
         o.d(h.e_kinetic); o.d(h.e_pot); o.d(h.e_elastic); o.d(c->P.x0); o.d(c->P.y0);
         o.end();
         o.d(c->P.angle_beam); o.i(c->P.iMotion);
+        // drag_unst_new, _old, lift_unst_new, _old: cal_drag ends every step with old = new
+        // (NavierStokes.f90:583-584), so between steps both slots hold the one tracked value
         o.d(h.drag_unst_old); o.d(h.drag_unst_old); o.d(h.lift_unst_old); o.d(h.lift_unst_old);
         o.end();
         o.i(h.unst_ready ? 1 : 0); o.d(h.dt_old); o.dv(oo.data(), 6 * ns);
@@ -2005,6 +2007,7 @@ struct AdjWork {
     int T = 0, S = 0;
     // run state
     int reached = 0, nsteps = 0, avg_from = 0;
+    int comp = 0;                   // objective: 0 mean drag, 1 mean lift
     double dt = 0.0, b10 = 0.0, b11 = 0.0, cobj = 0.0;
     int win[4] = {0, 0, 0, 0};
     long long fwd_steps = 0, adj_steps = 0;
@@ -2089,6 +2092,7 @@ static AdjArgs adj_args(fsibe_ctx* c) {
     a.part = w->part;
     a.S = c->S;
     a.J = w->acc;
+    a.comp = w->comp;
     return a;
 }
 
@@ -2288,10 +2292,11 @@ static int adj_check(fsibe_ctx* c, int nsteps, int avg_from) {
 }
 
 // state 0 from vort0 (the mask kept), nu set, the drag window known
-static int adj_begin(fsibe_ctx* c, const double* vort0, double nu, int nsteps, int avg_from, int nslots) {
+static int adj_begin(fsibe_ctx* c, int comp, const double* vort0, double nu, int nsteps, int avg_from, int nslots) {
     int st = adj_alloc(c, nslots);
     if (st) return st;
     AdjWork* w = c->adj;
+    w->comp = comp;
     if (nu > 0.0 && nu != c->P.nu) {
         c->P.nu = nu;
         free_graph(c);
@@ -2310,11 +2315,13 @@ static int adj_begin(fsibe_ctx* c, const double* vort0, double nu, int nsteps, i
 
 extern "C" {
 
-int fsibe_drag_objective(fsibe_ctx* c, const double* vort0, double nu, int nsteps, int avg_from, double* J) {
+int fsibe_force_objective(fsibe_ctx* c, int component, const double* vort0, double nu, int nsteps, int avg_from,
+                          double* J) {
     if (!c || !vort0 || !J) return FSIBE_ERR_PARAM;
+    if (component != 0 && component != 1) { c->err = "component: 0 (drag) or 1 (lift)"; return FSIBE_ERR_PARAM; }
     int st = adj_check(c, nsteps, avg_from);
     if (st) return st;
-    if ((st = adj_begin(c, vort0, nu, nsteps, avg_from, 1))) return st;
+    if ((st = adj_begin(c, component, vort0, nu, nsteps, avg_from, 1))) return st;
     for (int k = 0; k < nsteps; ++k)
         if ((st = adj_advance(c, k, false))) return st;
     CK(c, cudaMemcpyAsync(J, c->adj->acc, 8, cudaMemcpyDeviceToHost, c->stream));
@@ -2322,15 +2329,21 @@ int fsibe_drag_objective(fsibe_ctx* c, const double* vort0, double nu, int nstep
     return read_status(c);
 }
 
-int fsibe_drag_gradient(fsibe_ctx* c, const double* vort0, double nu, int nsteps, int avg_from, int snapshots,
-                        double* J, double* g_vort0, double* g_mask, double* g_nu, fsibe_adjoint_info* info) {
+int fsibe_drag_objective(fsibe_ctx* c, const double* vort0, double nu, int nsteps, int avg_from, double* J) {
+    return fsibe_force_objective(c, 0, vort0, nu, nsteps, avg_from, J);
+}
+
+int fsibe_force_gradient(fsibe_ctx* c, int component, const double* vort0, double nu, int nsteps, int avg_from,
+                         int snapshots, double* J, double* g_vort0, double* g_mask, double* g_nu,
+                         fsibe_adjoint_info* info) {
     if (!c || !vort0) return FSIBE_ERR_PARAM;
+    if (component != 0 && component != 1) { c->err = "component: 0 (drag) or 1 (lift)"; return FSIBE_ERR_PARAM; }
     int st = adj_check(c, nsteps, avg_from);
     if (st) return st;
     if (snapshots < 1) snapshots = 1;
     if (snapshots > nsteps) snapshots = nsteps;
     CK(c, cudaEventRecord(c->ev0, c->stream));
-    if ((st = adj_begin(c, vort0, nu, nsteps, avg_from, snapshots + 1))) return st;
+    if ((st = adj_begin(c, component, vort0, nu, nsteps, avg_from, snapshots + 1))) return st;
     AdjWork* w = c->adj;
     // time step and AB2 weights (fixed dt), the drag window: from one start-up step
     if ((st = adj_advance(c, 0, true))) return st;
@@ -2393,6 +2406,11 @@ int fsibe_drag_gradient(fsibe_ctx* c, const double* vort0, double nu, int nsteps
         info->ms_total = ms;
     }
     return FSIBE_OK;
+}
+
+int fsibe_drag_gradient(fsibe_ctx* c, const double* vort0, double nu, int nsteps, int avg_from, int snapshots,
+                        double* J, double* g_vort0, double* g_mask, double* g_nu, fsibe_adjoint_info* info) {
+    return fsibe_force_gradient(c, 0, vort0, nu, nsteps, avg_from, snapshots, J, g_vort0, g_mask, g_nu, info);
 }
 
 }  // extern "C"

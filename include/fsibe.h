@@ -200,7 +200,9 @@ int fsibe_get_scalars(fsibe_ctx* ctx, fsibe_scalars* out);
  * out[11] = time, drag, lift, drag_surf, lift_surf, Ft(1), Fn(1), Fp(1), Ft(2), Fn(2), Fp(2),
  * the columns of the reference's 'surface' file.  Replaces the call of BeamForces.f90:129; called
  * between fsibe_get_forces and fsibe_solid_step it sees the reference's state.  Needs
- * iViscous = 1 and a beam (else FSIBE_ERR_PARAM). */
+ * iViscous = 1 and a beam (else FSIBE_ERR_PARAM).  `time` fills column 0 and the soft
+ * start-up factor; the contour follows the device's current beam (angle and positions of the
+ * step), which is the reference's mouvement(time) when time is the context's current time. */
 int fsibe_surface_integral(fsibe_ctx* ctx, double time, double* out);
 
 /* ---- runtime backup ----------------------------------------------------------
@@ -286,6 +288,14 @@ typedef struct fsibe_adjoint_info {
 int fsibe_drag_objective(fsibe_ctx* ctx, const double* vort0, double nu, int nsteps, int avg_from, double* J);
 int fsibe_drag_gradient(fsibe_ctx* ctx, const double* vort0, double nu, int nsteps, int avg_from, int snapshots,
                         double* J, double* g_vort0, double* g_mask, double* g_nu, fsibe_adjoint_info* info);
+/* The same for either force component: component 0 is the drag above, 1 the lift, the mean of
+ * Force(2) (cal_drag NavierStokes.f90:568, the window sum of chi (v - v_s)).  The drag calls
+ * are these with component 0. */
+int fsibe_force_objective(fsibe_ctx* ctx, int component, const double* vort0, double nu, int nsteps, int avg_from,
+                          double* J);
+int fsibe_force_gradient(fsibe_ctx* ctx, int component, const double* vort0, double nu, int nsteps, int avg_from,
+                         int snapshots, double* J, double* g_vort0, double* g_mask, double* g_nu,
+                         fsibe_adjoint_info* info);
 
 /* ---- ensembles: independent runs advanced together (batched configuration) -------------
  * No counterpart in the reference (its batch mode, dns.f90:76-100, runs the parameter sets

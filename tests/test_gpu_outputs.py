@@ -1,7 +1,10 @@
 """The per-step files of a GPU run against the oracle's (C1 configuration, first 100 steps):
 the records of fsibe_run_records written by fsibe_2d_gb300.outputs in the reference's
 formats (beam_data1, u_max, energies, IBES_iter) must read the same, line for line and field
-for field, except in the last printed digit (FP64 parity is 1e-10, far inside es15.8)."""
+for field: identical, or apart by one unit of the last printed digit, or -- for a value far
+below its column's scale, whose printed digits are rounding noise -- within the FP64 parity
+bar, 1e-10 of the column's largest magnitude, or at the FP64 rounding level of the file's
+largest value (a mean that is zero up to rounding, such as the mean of v)."""
 import numpy as np
 import pytest
 
@@ -20,13 +23,14 @@ def _value(field):
     return float(field[:k] + "E" + field[k:])
 
 
-def _fields_agree(a, b, digits):
-    """Two ES-formatted fields equal, or apart by at most one unit of their last digit."""
+def _fields_agree(a, b, digits, col_scale, file_scale):
+    """Two ES-formatted fields equal, apart by at most one unit of their last digit, within
+    1e-10 of their column's scale, or both at the FP64 rounding level of the file's scale."""
     if a == b:
         return True
     va, vb = _value(a), _value(b)
-    scale = 10.0 ** (np.floor(np.log10(max(abs(va), abs(vb), 1e-300))) - digits)
-    return abs(va - vb) <= 1.01 * scale
+    ulp = 10.0 ** (np.floor(np.log10(max(abs(va), abs(vb), 1e-300))) - digits)
+    return abs(va - vb) <= max(1.01 * ulp, 1e-10 * col_scale, 1e-15 * file_scale)
 
 
 def test_c1_step_files_match_the_oracle(oracle, tmp_path):
@@ -46,6 +50,9 @@ def test_c1_step_files_match_the_oracle(oracle, tmp_path):
         name = a.rsplit("/", 1)[1]
         la, lb = open(a).read().splitlines(), open(b).read().splitlines()
         assert len(la) == len(lb) == (steps - 1 if name == "IBES_iter" else steps)
+        vals = np.abs(np.array([[_value(f) for f in line.split()] for line in lb]))
+        scale = vals.max(axis=0)
+        file_scale = vals[:, 1:].max()      # column 0 is the time
         for x, y in zip(la, lb):
             if x == y:
                 identical += 1
@@ -53,7 +60,7 @@ def test_c1_step_files_match_the_oracle(oracle, tmp_path):
             differ += 1
             fx, fy = x.split(), y.split()
             assert len(fx) == len(fy)
-            for u, v in zip(fx, fy):
-                assert _fields_agree(u, v, digits[name]), (name, x, y)
+            for c, (u, v) in enumerate(zip(fx, fy)):
+                assert _fields_agree(u, v, digits[name], scale[c], file_scale), (name, c, u, v)
     print(f"step files: {identical} lines identical, {differ} within the last digit")
     g.close(); o.close()
