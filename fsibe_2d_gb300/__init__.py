@@ -40,6 +40,7 @@ def library():
         L.fsibe_launches_per_step.argtypes = [C.c_void_p, C.POINTER(C.c_int)]
         L.fsibe_use_graph.argtypes = [C.c_void_p, C.c_int]
         L.fsibe_tiles.argtypes = [C.c_void_p, C.POINTER(C.c_int32)]
+        L.fsibe_tile_config.argtypes = [C.c_void_p, C.POINTER(C.c_int32)]
         L.fsibe_beam_cluster.argtypes = [C.c_void_p, C.POINTER(C.c_int32)]
         L.fsibe_ensemble_create.argtypes = [C.POINTER(FsibeParams), C.c_int, C.POINTER(C.c_void_p)]
         L.fsibe_ensemble_destroy.argtypes = [C.c_void_p]
@@ -88,6 +89,13 @@ class Run(_Run):
         out = (C.c_int32 * 3)()
         self._call("tiles", out)
         return tuple(out)
+
+    def tile_config(self):
+        """(rows, blocks-per-SM bound) of the fused x kernels nl_x, press_x, press_fin as the
+        autotuner chose them (bound 0: the kernel's default)."""
+        out = (C.c_int32 * 6)()
+        self._call("tile_config", out)
+        return [(out[2 * q], out[2 * q + 1]) for q in range(3)]
 
     def beam_cluster(self):
         """CTAs of the cluster running the beam's Newton step (0: the single-CTA kernel)."""

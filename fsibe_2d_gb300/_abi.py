@@ -50,6 +50,8 @@ class FsibeParams(C.Structure):
         ("x0", C.c_double), ("y0", C.c_double), ("length", C.c_double),
         ("t_beam", C.c_double), ("N_smooth", C.c_double),
         ("newton_tol", C.c_double), ("newton_maxit", C.c_int32), ("reserved", C.c_int32),
+        ("iWalls", C.c_int32), ("iCylinder", C.c_int32), ("iSponge", C.c_int32), ("reserved2", C.c_int32),
+        ("h_channel", C.c_double), ("R_cylinder", C.c_double), ("SpongeSize", C.c_double), ("eps_sponge", C.c_double),
     ]
 
 
@@ -89,7 +91,8 @@ def make_params(nx=256, ny=256, ns=64, xl=4.0, yl=4.0, Re=100.0, eps=1.0e-3, dt=
                 N_smooth=2.0, newton_tol=1.0e-10, newton_maxit=50, precision=FSIBE_FP64,
                 angle_beam=0.0, iFLUSI=1, iViscous=1, iSaveBeam=3, iSharpTrailing=0,
                 time_method_solid=FSIBE_BDF2, theta_inf=0.0, iMeanVelocity=3, idealis=1,
-                t_release=0.0, tau=0.0, grav=0.0, sigma=0.0, iImpulse=0, iMotion=0, iBeam=1):
+                t_release=0.0, tau=0.0, grav=0.0, sigma=0.0, iImpulse=0, iMotion=0, iBeam=1,
+                iWalls=0, h_channel=0.0, iCylinder=0, R_cylinder=0.0, iSponge=0, SpongeSize=0.0, eps_sponge=1.0):
     """Parameters in the reference's units (params.f90): nu = 1/Re, t_beam is the HALF
     thickness = thickness_cells/2 * dx, eps is the penalization parameter, eta = EI,
     mue = density ratio."""
@@ -109,4 +112,6 @@ def make_params(nx=256, ny=256, ns=64, xl=4.0, yl=4.0, Re=100.0, eps=1.0e-3, dt=
     p.t_beam = 0.5 * thickness_cells * xl / nx
     p.N_smooth = N_smooth
     p.newton_tol, p.newton_maxit = newton_tol, newton_maxit
+    p.iWalls, p.iCylinder, p.iSponge = iWalls, iCylinder, iSponge
+    p.h_channel, p.R_cylinder, p.SpongeSize, p.eps_sponge = h_channel, R_cylinder, SpongeSize, eps_sponge
     return p

@@ -32,6 +32,8 @@ size_t beam_ws_doubles(int ns);
 void launch_mask_prep(const MaskArgs& a, double gerf, cudaStream_t st, bool pdl);
 void launch_mask(const MaskArgs& a, double gerf, bool fp32, cudaStream_t st, bool pdl);
 void launch_forces(const ForceArgs& a, double dxi, double dyi, cudaStream_t st, bool pdl);
+void launch_static_masks(const StaticMaskArgs& a, double gerf, cudaStream_t st);
+void launch_sponge_mask(const StaticMaskArgs& a, double gerf, cudaStream_t st);
 void launch_forces_geo(const ForceArgs& a, double dxi, double dyi, cudaStream_t st);
 void launch_surface_integral(const ForceArgs& a, const SurfArgs& s, double dxi, double dyi, double time, cudaStream_t st);
 void launch_beam(const BeamArgs& b, cudaStream_t st);
@@ -74,6 +76,10 @@ struct StepArgs {
     double* etab;
     float2* etabf;
     int hx;
+    double soff, rdyi;      // the stress points' offset from the beam; 1 / interpolation spacing
+    int walls_or_cyl;       // walls or a cylinder clamp the step like a beam (NavierStokes.f90:71)
+    double r_cyl;           // R_cylinder in the drag window (NavierStokes.f90:538-545)
+    int wall_row0, wall_row1;  // iWalls: the window's rows stay within [row0, row1] (:546-552)
 };
 
 __device__ double mean_ux(int mode, double time, double cos_ti, double Tf, double pi) {  // mean_velocity.f90:4-42
@@ -152,7 +158,7 @@ __global__ void __launch_bounds__(256) k_step_begin(StepArgs a) {
         const double u_max = sqrt(smax);
         double dt1 = a.cfl * fmin(a.dx, a.dy) / u_max;
         if (u_max < 1.e-10) dt1 = 1.e-2;
-        if (a.iBeam > 0) dt1 = fmin(0.9 * a.eps, dt1);
+        if (a.iBeam > 0 || a.walls_or_cyl) dt1 = fmin(0.9 * a.eps, dt1);
         if (a.dt_fixed > 0.0) dt1 = fmin(a.dt_fixed, dt1);
         if ((a.time_end - time) < dt1) dt1 = a.time_end - time;
         if (!a.explicit_step) S->dt0 = dt0;
@@ -167,7 +173,7 @@ __global__ void __launch_bounds__(256) k_step_begin(StepArgs a) {
     } else if (threadIdx.x == 64) {
         S->mean_uy = div_cr(sv, a.NN, a.rNN);
     } else if (threadIdx.x == 96 || threadIdx.x == 128) {
-        const double r_cyl = 0.0, tb = a.t_beam;
+        const double r_cyl = a.r_cyl, tb = a.t_beam;
         if (threadIdx.x == 96) {
             int ixmin = 0, ixmax = a.nx - 1;
             if (a.iBeam > 0) {
@@ -184,6 +190,18 @@ __global__ void __launch_bounds__(256) k_step_begin(StepArgs a) {
                 iymin = (int)div_cr((fmin(bminy - 1.5 * tb, a.y0 - 2.0 * r_cyl)), a.dy, a.rdy);
                 if (iymin < 0) iymin = 0;
                 if (iymax > a.ny - 1) iymax = a.ny - 1;
+                // the rows of the cells j of the forces' stress points (within soff of the
+                // beam's y range, BeamForces.f90:105-124) and their 9 x 9 stencils, with two rows
+                // of margin for the rounding of the cell index: k_stress_x leaves the others
+                const double j0 = floor((bminy - a.soff) * a.rdyi) - 6.0, j1 = floor((bmaxy + a.soff) * a.rdyi) + 6.0;
+                S->srow[0] = (int)fmax(j0, -1.0);
+                S->srow[1] = (int)fmin(j1, (double)a.ny);
+            } else {
+                S->srow[0] = 0; S->srow[1] = a.ny - 1;
+            }
+            if (a.wall_row1 >= 0) {
+                if (iymin < a.wall_row0) iymin = a.wall_row0;
+                if (iymax > a.wall_row1) iymax = a.wall_row1;
             }
             S->win[2] = iymin; S->win[3] = iymax;
         }
@@ -433,6 +451,12 @@ struct fsibe_ctx {
     double* dscratch2 = nullptr;  // nx*ny doubles
     double gerf = 0.0;
     double U_mean_true = 1.0;
+    // walls, cylinder and sponges: static fields, formed once (null when not used)
+    bool full_mask = false;       // every cell of the mask is drawn each step
+    double* bg = nullptr;         // walls + cylinder, unscaled
+    double* frame = nullptr;      // iSponge = 22
+    void* spg = nullptr;          // vorticity sponge / eps_sponge (R)
+    int* rect_full = nullptr;     // rows of the whole grid, for the penalization part of cal_nlk
     int beam_smem = 0;      // beam workspace parts in shared memory (bit mask, see k_beam)
     int beam_pre_smem = 0;  // the same for the predictor kernel
     int beam_cl = 0;        // CTAs of the cluster form of the beam kernel (0: the single-CTA form)
@@ -540,6 +564,7 @@ static KArgs<R> kargs(fsibe_ctx* c) {
     a.etabf = c->etabf;
     a.dcut = c->dcut;
     a.kcut = c->kcut;
+    a.spg = reinterpret_cast<const R*>(c->spg);
     a.viscous = c->P.iViscous == 1;
     a.pressure_on = (c->P.iFLUSI == 1 || c->P.iSaveBeam > 0);
     a.penalize = c->P.iBeam > 0;
@@ -567,10 +592,10 @@ static void launch_x(fsibe_ctx* c, void (*k)(KArgs<R>), int smem, const KArgs<R>
 template <typename R>
 // pdl: a programmatic dependent launch (only for kernels that begin with pdl_wait)
 static void launch_y(fsibe_ctx* c, void (*k)(KArgs<R>), int smem, const KArgs<R>& a, const char* name = "y_pass",
-                     int nfields = 1, bool pdl = false) {
+                     int nfields = 1, bool pdl = false, int threads = 0) {
     const SizeKernels<R>& K = ky_of<R>(c);
     prof_begin(c, name);
-    launch_k(k, dim3(c->g.hx, nfields), dim3(K.y_threads), smem, c->stream, pdl && c->pdl, a);
+    launch_k(k, dim3(c->g.hx, nfields), dim3(threads > 0 ? threads : K.y_threads), smem, c->stream, pdl && c->pdl, a);
     prof_end(c);
     c->launches++;
 }
@@ -627,6 +652,16 @@ static StepArgs step_args(fsibe_ctx* c, int explicit_step, int nblk) {
     a.etab = c->etab;
     a.etabf = c->etabf;
     a.hx = c->g.hx;
+    a.soff = c->P.t_beam + c->P.N_smooth * std::fmax(c->g.dx, c->g.dy);
+    a.rdyi = (double)(c->P.ny - 1) / (c->P.yl - c->g.dy);
+    a.walls_or_cyl = (c->P.iWalls > 0 || c->P.iCylinder > 0) ? 1 : 0;
+    a.r_cyl = c->P.R_cylinder;
+    a.wall_row0 = 0; a.wall_row1 = -1;
+    if (c->P.iWalls > 0) {
+        const double h_star = c->P.h_channel + c->P.N_smooth * c->g.dy;
+        a.wall_row0 = (int)std::lround(h_star / c->g.dy) + 2;
+        a.wall_row1 = (int)std::lround((c->P.yl - h_star) / c->g.dy) - 2;
+    }
     return a;
 }
 
@@ -700,8 +735,10 @@ static void nl_advect_t(fsibe_ctx* c, int explicit_step) {
     // mask raster launched after it finds room on every SM.  Beyond that the kernel is long
     // beside the raster, and a block a tile keeps more of it in flight (4096²: 281 µs against
     // 513 µs with one block a SM).
-    const int tiles = c->g.ny / KX.xv[c->xv_nl].rows;
-    launch_xv<R>(c, KX.xv[c->xv_nl].nl_adv, KX.xv[c->xv_nl], 2, a, "nl_adv", c->side2,
+    // a run with the vorticity sponge takes the default tile, the one instantiated with it
+    const auto& V = c->spg ? KX.xv[1] : KX.xv[c->xv_nl];
+    const int tiles = c->g.ny / V.rows;
+    launch_xv<R>(c, c->spg ? V.nl_adv_spg : V.nl_adv, V, 2, a, "nl_adv", c->side2,
                  tiles <= 2 * c->nsm ? (tiles < c->nsm ? tiles : c->nsm) : tiles);
 }
 
@@ -731,8 +768,10 @@ static int fluid_step_t(fsibe_ctx* c, int explicit_step, bool adv_forked = false
         // of the mask's box
         CK(c, cudaStreamWaitEvent(c->stream, c->ev_adv, 0));
         KArgs<R> p = a;
-        p.rect = c->rect;
+        p.rect = c->full_mask ? c->rect_full : c->rect;  // walls and sponges: every row is penalized
         launch_xv<R>(c, KX.xv[c->xv_nl].nl_pen, KX.xv[c->xv_nl], 2, p, "nl_pen");
+    } else if (c->spg) {
+        launch_xv<R>(c, KX.xv[1].nl_x_spg, KX.xv[1], 3, a, "nl_x");  // the default tile carries the sponge
     } else {
         launch_xv<R>(c, KX.xv[c->xv_nl].nl_x, KX.xv[c->xv_nl], 3, a, "nl_x");
     }
@@ -744,11 +783,7 @@ static int fluid_step_t(fsibe_ctx* c, int explicit_step, bool adv_forked = false
         CK(c, cudaEventRecord(c->ev_ny, c->stream));
         CK(c, cudaStreamWaitEvent(c->side2, c->ev_ny, 0));
         KArgs<R> s = a;
-        if (stress_rows && c->P.iBeam > 0) {
-            s.by = c->beam[B_Y];
-            s.soff = c->P.t_beam + c->P.N_smooth * std::fmax(c->g.dx, c->g.dy);
-            s.rdyi = (double)(c->P.ny - 1) / (c->P.yl - c->g.dy);
-        }
+        s.srows = (stress_rows && c->P.iBeam > 0) ? 1 : 0;  // the row range k_step_begin formed
         launch_xv<R>(c, KX.xv[c->xv_px].stress_x, KX.xv[c->xv_px], 2, s, "stress_x", c->side2);
         a.stress_split = 1;
     }
@@ -763,7 +798,7 @@ static int fluid_step_t(fsibe_ctx* c, int explicit_step, bool adv_forked = false
     CK(c, cudaEventRecord(c->ev_ffj, c->side2));
     c->launches++;
     if (a.pressure_on) {
-        launch_y<R>(c, KY.press_y, KY.y_smem2, a, "press_y", 1, true);
+        launch_y<R>(c, KY.press_y, KY.y_smem2, a, "press_y", 1, true, KY.press_y_threads);
         launch_xv<R>(c, KX.xv[c->xv_fin].press_fin, KX.xv[c->xv_fin], 1, a, "press_fin");
     } else {
         CK(c, cudaMemsetAsync(c->phys[PH_PRESS], 0, sizeof(R) * (size_t)c->g.nx * c->g.ny, c->stream));
@@ -792,7 +827,50 @@ static MaskArgs mask_args(fsibe_ctx* c) {
     m.prims = c->prims; m.nprims = c->nprims; m.rect = c->rect; m.nsm = c->nsm;
     m.rdx = 1.0 / m.dx; m.rdy = 1.0 / m.dy; m.rpi = 1.0 / m.pi; m.angle_rad = m.angle_deg * m.pi / 180.0;
     m.mask = c->phys[PH_MASK]; m.mvx = c->phys[PH_MVX]; m.mvy = c->phys[PH_MVY];
+    m.full = c->full_mask ? 1 : 0;
+    m.bg = c->bg;
+    m.frame = c->frame;
+    m.frame_c = c->P.eps / std::max(1.0e-3, c->P.eps);
+    m.sponge4 = c->P.iSponge == 4 ? 1 : 0;
+    if (m.sponge4) {
+        const double sss = c->P.SpongeSize;
+        m.s4_star = sss;
+        m.s4_size = sss - 2.0 * c->P.N_smooth * c->g.dx;
+        m.s4_l1 = (int)std::lround((0.5 * sss) / c->g.dx);
+        m.s4_r0 = m.s4_l1;
+        m.s4_r1 = (int)std::lround((1.0 * sss) / c->g.dx);
+        m.h_channel = c->P.h_channel;
+        m.H_eff = c->P.yl - 2.0 * c->P.h_channel;
+    }
+    m.iMeanVelocity = c->P.iMeanVelocity;
+    m.T_fullspeed = c->P.T_fullspeed;
+    m.cos_ti = std::cos(c->P.theta_inf);
+    m.sin_ti = std::sin(c->P.theta_inf);
     return m;
+}
+
+static StaticMaskArgs static_mask_args(fsibe_ctx* c) {
+    StaticMaskArgs a;
+    std::memset(&a, 0, sizeof(a));
+    a.nx = c->P.nx; a.ny = c->P.ny;
+    a.sharp = std::fabs(c->P.N_smooth) < 1e-4;
+    a.iWalls = c->P.iWalls; a.iCylinder = c->P.iCylinder; a.iSponge = c->P.iSponge;
+    a.dx = c->g.dx; a.dy = c->g.dy; a.xl = c->P.xl; a.yl = c->P.yl; a.N = c->P.N_smooth; a.pi = c->g.pi;
+    a.h_channel = c->P.h_channel; a.R_cylinder = c->P.R_cylinder; a.x0 = c->P.x0; a.y0 = c->P.y0;
+    a.t_beam = c->P.t_beam; a.SpongeSize = c->P.SpongeSize; a.eps = c->P.eps; a.eps_sponge = c->P.eps_sponge;
+    a.bg = c->bg; a.frame = c->frame; a.spg = c->spg; a.mask = c->phys[PH_MASK];
+    a.fp32 = c->fp32 ? 1 : 0;
+    return a;
+}
+
+// create_sponge_mask (create_mask.f90:223-364) from the start-up mask, once per start
+static int sponge_mask(fsibe_ctx* c) {
+    if (!c->spg) return FSIBE_OK;
+    StaticMaskArgs a = static_mask_args(c);
+    a.bg = nullptr; a.frame = nullptr;
+    launch_sponge_mask(a, c->gerf, c->stream);
+    CKL(c);
+    return FSIBE_OK;
 }
 
 static int create_mask(fsibe_ctx* c) {
@@ -1055,6 +1133,7 @@ static int init_velocity(fsibe_ctx* c) {
     if ((st = inv_y<R>(c, c->spec[SP_W], c->spec[SP_TV], OP_V))) return st;
     if ((st = inv_y<R>(c, c->spec[SP_W], c->spec[SP_TDX], OP_DX))) return st;
     if ((st = inv_y<R>(c, c->spec[SP_W], c->spec[SP_TDY], OP_DY))) return st;
+    if ((st = inv_y<R>(c, c->spec[SP_W], c->spec[SP_TW], OP_ID))) return st;  // the sponge's vorticity
     KArgs<R> a = kargs<R>(c);
     launch_x<R>(c, kx_of<R>(c).vel_x, kx_of<R>(c).x_smem2, a);
     CKL(c);
@@ -1143,8 +1222,8 @@ static int autotune_x(fsibe_ctx* c) {
         // the default first; a candidate must be faster by 3% to replace it
         int best = 1;
         float tbest = time_xv<R>(c, kind, K.xv[1]);
-        for (int v : {0, 2}) {
-            if (K.xv[v].rows == K.xv[1].rows) continue;
+        for (int v : {0, 2, 3}) {
+            if (K.xv[v].rows == K.xv[1].rows && K.xv[v].minb == K.xv[1].minb) continue;
             const float t = time_xv<R>(c, kind, K.xv[v]);
             if (t < 0.97f * tbest) { tbest = t; best = v; }
         }
@@ -1169,7 +1248,8 @@ int fsibe_destroy(fsibe_ctx* c) {
     for (void* p : c->spec) if (p) cudaFree(p);
     for (double* p : c->beam) if (p) cudaFree(p);
     void* others[] = {c->twX, c->twR, c->twY, c->S, c->red, c->oo, c->ws, c->pred, c->minv, c->minv_rse, c->d1d, c->fgeo, c->fgij, c->prims, c->nprims,
-                      c->rect, c->counter, c->fterm, c->rows, c->dscratch, c->dscratch2, c->etab, c->etabf, c->dcut};
+                      c->rect, c->counter, c->fterm, c->rows, c->dscratch, c->dscratch2, c->etab, c->etabf, c->dcut,
+                      c->bg, c->frame, c->spg, c->rect_full};
     for (void* p : others) if (p) cudaFree(p);
     for (cudaEvent_t e : c->pool) cudaEventDestroy(e);
     if (c->ev0) cudaEventDestroy(c->ev0);
@@ -1199,6 +1279,22 @@ int fsibe_create(const fsibe_params* p, fsibe_ctx** out) {
     if (p->iMotion != 0) { g_err = "only the clamped leading edge (iMotion = 0) is implemented"; return FSIBE_ERR_UNSUPPORTED; }
     if (p->precision != FSIBE_FP64 && p->precision != FSIBE_FP32C) { g_err = "precision"; return FSIBE_ERR_PARAM; }
     if (p->iMeanVelocity == 11) { g_err = "iMeanVelocity = 11 is not implemented"; return FSIBE_ERR_UNSUPPORTED; }
+    {
+        const int isp = p->iSponge;
+        if (p->iWalls < 0 || p->iWalls > 1 || p->iCylinder < 0 || p->iCylinder > 1 ||
+            !(isp == 0 || isp == 1 || isp == 2 || isp == 3 || isp == 4 || isp == 22 || isp == 10)) {
+            g_err = "iWalls, iCylinder in {0, 1}; iSponge in {0, 1, 2, 3, 4, 22}"; return FSIBE_ERR_PARAM;
+        }
+        if (isp == 10) { g_err = "iSponge = 10 (the sharp outflow test sponge) is not implemented"; return FSIBE_ERR_UNSUPPORTED; }
+        if ((p->iWalls || p->iCylinder || isp) && p->iBeam != 1) {
+            g_err = "walls, the cylinder and the sponges run with the beam (iBeam = 1)"; return FSIBE_ERR_UNSUPPORTED;
+        }
+        if (isp > 0 && isp != 4 && !(p->eps_sponge >= 1.0e-9)) { g_err = "eps_sponge (params.f90:185-188)"; return FSIBE_ERR_PARAM; }
+        if ((isp == 4 || isp == 22 || isp == 1 || isp == 2 || isp == 3) && !(p->SpongeSize > 0.0)) {
+            g_err = "SpongeSize must be positive"; return FSIBE_ERR_PARAM;
+        }
+        if (p->iWalls == 1 && p->theta_inf != 0.0) { g_err = "walls need theta_inf = 0 (params.f90:199-203)"; return FSIBE_ERR_PARAM; }
+    }
     if (p->time_method_solid != FSIBE_BDF2 && p->time_method_solid != FSIBE_CRANK_NICHOLSON &&
         p->time_method_solid != FSIBE_EULER_IMPLICIT) { g_err = "time_method_solid"; return FSIBE_ERR_PARAM; }
     fsibe_ctx* c = new fsibe_ctx();
@@ -1303,6 +1399,26 @@ int fsibe_create(const fsibe_params* p, fsibe_ctx** out) {
     }
     ALLOC(c->dscratch, 8 * 2 * NN);
     ALLOC(c->dscratch2, 8 * NN);
+    {
+        // walls, cylinder and sponges (create_mask.f90:21-68, 120-204, 223-364): the static
+        // fields, and every cell drawn each step
+        const int isp = p->iSponge;
+        c->full_mask = p->iWalls > 0 || p->iCylinder > 0 || isp == 4 || isp == 22;
+        if (p->iWalls > 0 || p->iCylinder > 0) ALLOC(c->bg, 8 * NN);
+        if (isp == 22) ALLOC(c->frame, 8 * NN);
+        if (isp == 1 || isp == 2 || isp == 3 || isp == 22) ALLOC(c->spg, rs * NN);
+        if (c->full_mask) {
+            ALLOC(c->rect_full, 16);
+            const int rf[4] = {0, p->nx - 1, 0, p->ny - 1};
+            cudaMemcpy(c->rect_full, rf, sizeof(rf), cudaMemcpyHostToDevice);
+        }
+        if (c->bg || c->frame) {
+            launch_static_masks(static_mask_args(c), c->gerf, 0);
+            cudaError_t e_ = cudaGetLastError();
+            if (e_ == cudaSuccess) e_ = cudaStreamSynchronize(0);  // the run's streams do not wait on stream 0
+            if (e_ != cudaSuccess) { g_err = std::string("static masks: ") + cudaGetErrorString(e_); fsibe_destroy(c); return FSIBE_ERR_CUDA; }
+        }
+    }
     if (c->fp32) {
         std::vector<float2> tX, tR, tY;
         make_table(tX, p->nx / 2, p->nx / 2);
@@ -1436,7 +1552,7 @@ static int init_state(fsibe_ctx* c, const double* vort, bool keep_mask) {
     h.startup_step = 1;
     h.method = c->P.time_method_solid;
     h.grav = c->P.grav;
-    c->U_mean_true = 1.0;
+    c->U_mean_true = (c->P.iWalls == 1) ? 1.0 - 2.0 * c->P.h_channel / c->P.yl : 1.0;  // time_step.f90:95-100
     h.mean_u_next = c->U_mean_true * host_mean(c->P, 0.0, true);
     h.mean_v_next = c->U_mean_true * host_mean(c->P, 0.0, false);
     h.mean_u_cur = h.mean_u_next;
@@ -1450,6 +1566,7 @@ static int init_state(fsibe_ctx* c, const double* vort, bool keep_mask) {
     if (!keep_mask) {
         st = create_mask(c);
         if (st) return st;
+        if ((st = sponge_mask(c))) return st;
     }
     CK(c, cudaStreamSynchronize(c->stream));
     c->initialized = true;
@@ -1841,7 +1958,7 @@ int fsibe_read_backup(fsibe_ctx* c, const char* path) {
         h.force[k] = force[k]; h.force_unst[k] = force_unst[k]; h.force_press[k] = force_press[k]; h.inertial_force[k] = inertial[k];
     }
     h.e_kinetic = ek; h.e_pot = ep; h.e_elastic = ee;
-    c->U_mean_true = 1.0;
+    c->U_mean_true = (c->P.iWalls == 1) ? 1.0 - 2.0 * c->P.h_channel / c->P.yl : 1.0;
     h.mean_u_next = h.mean_u_cur = c->U_mean_true * host_mean(c->P, time, true);
     h.mean_v_next = h.mean_v_cur = c->U_mean_true * host_mean(c->P, time, false);
     CK(c, cudaMemcpyAsync(c->S, &h, sizeof(h), cudaMemcpyHostToDevice, c->stream));
@@ -1865,6 +1982,7 @@ int fsibe_read_backup(fsibe_ctx* c, const char* path) {
     CK(c, cudaMemcpyAsync(c->red, red.data(), 8 * RED_NSLOTS, cudaMemcpyHostToDevice, c->stream));
     CK(c, cudaMemcpyAsync(&c->S->nred, &one_block, 4, cudaMemcpyHostToDevice, c->stream));
     if ((st = create_mask(c))) return st;
+    if ((st = sponge_mask(c))) return st;
     CK(c, cudaStreamSynchronize(c->stream));
     c->initialized = true;
     c->startup_done = true;
@@ -1945,6 +2063,16 @@ int fsibe_beam_phase_cycles(fsibe_ctx* c, long long* out32, int reset) {
     CK(c, cudaMemcpyAsync(out32, c->S->phase, 32 * sizeof(long long), cudaMemcpyDeviceToHost, c->stream));
     if (reset) CK(c, cudaMemsetAsync(c->S->phase, 0, 32 * sizeof(long long), c->stream));
     CK(c, cudaStreamSynchronize(c->stream));
+    return FSIBE_OK;
+}
+
+int fsibe_tile_config(fsibe_ctx* c, int32_t* out6) {
+    if (!c || !out6) return FSIBE_ERR_PARAM;
+    const int idx[3] = {c->xv_nl, c->xv_px, c->xv_fin};
+    for (int q = 0; q < 3; ++q) {
+        out6[2 * q] = c->fp32 ? c->kxf.xv[idx[q]].rows : c->kxd.xv[idx[q]].rows;
+        out6[2 * q + 1] = c->fp32 ? c->kxf.xv[idx[q]].minb : c->kxd.xv[idx[q]].minb;
+    }
     return FSIBE_OK;
 }
 
@@ -2287,6 +2415,7 @@ static int adj_check(fsibe_ctx* c, int nsteps, int avg_from) {
         c->err = "the adjoint needs a prescribed rigid mask (iFLUSI = 0, iMotion = 0, iBeam > 0)";
         return FSIBE_ERR_UNSUPPORTED;
     }
+    if (c->spg || c->full_mask) { c->err = "the adjoint runs without walls, cylinder and sponges"; return FSIBE_ERR_UNSUPPORTED; }
     if (nsteps < 1 || avg_from < 1 || avg_from > nsteps) { c->err = "need 1 <= avg_from <= nsteps"; return FSIBE_ERR_PARAM; }
     return FSIBE_OK;
 }

@@ -94,6 +94,7 @@ struct DevScalars {
     int32_t etab_valid;              // 1: the integrating-factor tables hold exp of etab_cx, etab_cy
     int32_t nred;                    // per-block partial sums written by the last x-pass kernel
     double etab_cx, etab_cy;
+    int32_t srow[2];                 // rows the forces' stencils can reach this step (k_step_begin)
 };
 
 // Reduction slots written per block by the velocity/pressure kernel.

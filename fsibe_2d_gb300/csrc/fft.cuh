@@ -260,6 +260,123 @@ __device__ __forceinline__ void block_fft_reg_m(C2<R> (&v)[NBA][8], C2<R>* buf, 
     fft_reg_run<R, N, INV, NB, 1, NBA>(v, buf, bstride, tw, t);
 }
 
+// ---- paired transforms (FP32): a thread owns two adjacent butterflies -----------------------
+// A length-N transform runs on N/16 threads.  Thread u owns the elements 2u + h + m G (G = N/8,
+// h < 2, m < 8), held as v[2m + h]: the inputs of its two first-stage butterflies j = 2u and
+// 2u + 1, and the outputs of its last-stage butterflies.  The two butterflies of a stage have
+// adjacent outputs (k and k + 1 of the same group), so between stages every exchange moves a
+// pair (2p, 2p + 1) as one 16-byte shared-memory access, half the accesses of one butterfly a
+// thread.  With one pad slot after every eight pairs, the eight 16-byte accesses of every
+// quarter warp fall in distinct bank groups in every stage, for every length 16..4096.  A radix-8
+// butterfly loads the twiddles w, w^2, w^3, w^4 and forms w^5 = w w^4, w^6 = w^2 w^4,
+// w^7 = w^3 w^4 (a product of two correctly rounded FP32 twiddles: within 2 ulp).
+__host__ __device__ constexpr int pair_slots(int n) { return n / 2 + n / 16 + 1; }  // float4 slots of a row
+__device__ __forceinline__ int padp(int p) { return p + (p >> 3); }
+
+template <int P, bool INV>
+__device__ __forceinline__ void tw_powers(float2 (&w)[8], const float2* __restrict__ tw, int e) {
+    if constexpr (P == 8) {
+        w[1] = __ldg(&tw[e]); w[2] = __ldg(&tw[2 * e]); w[3] = __ldg(&tw[3 * e]); w[4] = __ldg(&tw[4 * e]);
+        w[5] = cmul<float>(w[1], w[4]); w[6] = cmul<float>(w[2], w[4]); w[7] = cmul<float>(w[3], w[4]);
+    } else {
+#pragma unroll
+        for (int r = 1; r < P; ++r) w[r] = __ldg(&tw[r * e]);
+    }
+    if (INV) {
+#pragma unroll
+        for (int r = 1; r < P; ++r) w[r].y = -w[r].y;
+    }
+}
+
+// The butterflies of one stage (radix P, NS = product of the radices applied) on v[b][..],
+// b < NB of the NBA rows.  Butterfly (q, h) takes its inputs from, and leaves its outputs in,
+// v[b][2 (q + r PER) + h], r < P.
+template <int N, int P, int NS, bool INV, int NB, int NBA>
+__device__ __forceinline__ void fft2_compute(float2 (&v)[NBA][16], const float2* __restrict__ tw, int u) {
+    constexpr int G = N / 8, PER = 8 / P;
+#pragma unroll
+    for (int q = 0; q < PER; ++q) {
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            if constexpr (NS > 1) {
+                const int j = 2 * u + h + q * G;
+                const int k = j & (NS - 1);
+                float2 w[8];
+                tw_powers<P, INV>(w, tw, k * (N / (NS * P)));
+#pragma unroll
+                for (int r = 1; r < P; ++r)
+#pragma unroll
+                    for (int b = 0; b < NB; ++b) v[b][2 * (q + r * PER) + h] = cmul<float>(v[b][2 * (q + r * PER) + h], w[r]);
+            }
+#pragma unroll
+            for (int b = 0; b < NB; ++b) {
+                float2 x[P];
+#pragma unroll
+                for (int r = 0; r < P; ++r) x[r] = v[b][2 * (q + r * PER) + h];
+                dftp<float, P, INV>(x);
+#pragma unroll
+                for (int r = 0; r < P; ++r) v[b][2 * (q + r * PER) + h] = x[r];
+            }
+        }
+    }
+}
+
+template <int N, bool INV, int NB, int NS, int NBA>
+__device__ __forceinline__ void fft2_run(float2 (&v)[NBA][16], float4* buf, int bstride, const float2* __restrict__ tw,
+                                         int u) {
+    constexpr int G = N / 8;
+    constexpr int P = (NS * 8 <= N) ? 8 : ((NS * 4 == N) ? 4 : 2);
+    fft2_compute<N, P, NS, INV, NB, NBA>(v, tw, u);
+    if constexpr (NS * P < N) {
+        static_assert(P == 8, "only the last stage has a radix below 8");
+        // outputs r of butterfly h at base_h + r NS: with NS = 1 a butterfly's eight outputs are
+        // contiguous (base_h = 8 (2u + h)); else base_1 = base_0 + 1 (k and k + 1)
+#pragma unroll
+        for (int b = 0; b < NB; ++b) {
+            float4* rb = buf + b * bstride;
+            if constexpr (NS == 1) {
+#pragma unroll
+                for (int h = 0; h < 2; ++h)
+#pragma unroll
+                    for (int r = 0; r < 8; r += 2) {
+                        const float2 a = v[b][2 * r + h], c = v[b][2 * (r + 1) + h];
+                        rb[padp(8 * u + 4 * h + r / 2)] = make_float4(a.x, a.y, c.x, c.y);
+                    }
+            } else {
+                const int j0 = 2 * u, k0 = j0 & (NS - 1), base0 = (j0 - k0) * 8 + k0;
+#pragma unroll
+                for (int r = 0; r < 8; ++r) {
+                    const float2 a = v[b][2 * r], c = v[b][2 * r + 1];
+                    rb[padp((base0 + r * NS) >> 1)] = make_float4(a.x, a.y, c.x, c.y);
+                }
+            }
+        }
+        __syncthreads();
+        // the next stage's inputs: elements 2u + h + m G, the pair u + m G / 2
+#pragma unroll
+        for (int b = 0; b < NB; ++b)
+#pragma unroll
+            for (int m = 0; m < 8; ++m) {
+                const float4 t = buf[b * bstride + padp(u + m * (G / 2))];
+                v[b][2 * m] = make_float2(t.x, t.y);
+                v[b][2 * m + 1] = make_float2(t.z, t.w);
+            }
+        __syncthreads();  // every thread has its inputs before the rows are written again
+        fft2_run<N, INV, NB, NS * 8, NBA>(v, buf, bstride, tw, u);
+    }
+}
+
+// NB paired transforms (FP32) of v[b][2m + h] = element 2u + h + m (N/8), b < NB of NBA; buf +
+// b * bstride are NB exchange rows of pair_slots(N) float4, free when called (the caller
+// synchronises after their last use) and free again on return.  All N/16 threads call it.
+template <int N, bool INV, int NB, int NBA>
+__device__ __forceinline__ void block_fft2_m(float2 (&v)[NBA][16], float4* buf, int bstride,
+                                             const float2* __restrict__ tw, int u) {
+    static_assert(N >= 16 && (N & (N - 1)) == 0, "power-of-two length >= 16");
+    static_assert(NB >= 1 && NB <= NBA, "NB of the NBA rows");
+    fft2_run<N, INV, NB, 1, NBA>(v, buf, bstride, tw, u);
+}
+
 // ---- real <-> half-length complex split steps (x direction) -------------------------------
 // A real row x[0..2H) is handled as z[m] = x[2m] + i x[2m+1], m < H, transformed with a
 // length-H complex FFT.  twr[k] = exp(-2 pi i k / 2H), k <= H.

@@ -20,6 +20,8 @@
 //   k_press_y  pressure :366-383: forward-y, divergence, poisson, inverse-y
 //   k_press_fin pressure :383-392: inverse-x, p = q - |u|^2/2
 #pragma once
+#include <algorithm>
+
 #include "fft.cuh"
 
 namespace fsibe {
@@ -42,11 +44,11 @@ struct KArgs {
     int viscous, pressure_on, penalize, op;
     int explicit_step;    // 1 on the Euler start-up step (the host's flag: nl_x runs beside k_step_begin)
     const int* rect;      // the mask's box (rect[2..3]: its rows), written by k_mask_prep
-    // the viscous stresses in their own kernel (k_stress_x) instead of k_press_x; with by set,
-    // only on the rows that the forces' stencils at the beam can reach
+    // the viscous stresses in their own kernel (k_stress_x) instead of k_press_x; with srows
+    // set, only on the rows that the forces' stencils at the beam can reach (S->srow)
     int stress_split;
-    const double* by;     // beam y (ns nodes)
-    double soff, rdyi;    // the stress points' offset from the centre line; 1 / interpolation spacing
+    int srows;
+    const R* spg;         // the vorticity sponge / eps_sponge (NavierStokes.f90:142-160), or null
     size_t bstride;       // generic transforms over several fields at once: blockIdx.y selects the
                           // field, bstride complex values (= nx ny / 2) apart in every buffer
 };
@@ -365,7 +367,9 @@ __global__ void __launch_bounds__(XRows<R, H>::THREADS) k_vel_x(KArgs<R> a) {
 // K2: nonlinear term and penalization in physical space (cal_nlk)
 // ======================================================================================
 // One tile of TR rows from iy0 (the whole kernel's work for one block)
-template <typename R, int H, int TRV, int PART>
+// SPG: the run has a vorticity sponge (a separate instantiation, so that the plain step keeps
+// its registers)
+template <typename R, int H, int TRV, int PART, bool SPG>
 __device__ __forceinline__ void nl_x_tile(const KArgs<R>& a, const int iy0) {
     using X = XRows<R, H, TRV>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -403,6 +407,15 @@ __device__ __forceinline__ void nl_x_tile(const KArgs<R>& a, const int iy0) {
         __syncthreads();
         row_c2r_reg<R, H, 2>(ra, BS, a.twR, a.twX, t, dxy);  // both together, to registers
     }
+    // the vorticity sponge: the vorticity itself (x inverse of Tw, the inverse-y transform of the
+    // state that k_nl_y left), for the term -F(mask_sponge omega) of cal_nlk
+    C2<R> om[1][8];
+    if constexpr (SPG && PART != NL_PENAL) {
+        const int kin = a.explicit_step ? H : a.kcut;
+        load_tileT<R, H, X::TR, X::PL>(bufA, a.Tw, ny, iy0, kin);
+        __syncthreads();
+        row_c2r_reg<R, H, 1>(ra, BS, a.twR, a.twX, t, om);
+    }
     const int iy = iy0 + r;
     const size_t roff = (size_t)iy * H;
     const C2<R>* u2 = reinterpret_cast<const C2<R>*>(a.u) + roff;
@@ -426,6 +439,10 @@ __device__ __forceinline__ void nl_x_tile(const KArgs<R>& a, const int iy0) {
         if (adv) {
             const C2<R> dx = dxy[0][q], dy = dxy[1][q];
             wv[q] = mk<R>(-uu.x * dx.x - vv.x * dy.x, -uu.y * dx.y - vv.y * dy.y);
+            if constexpr (SPG) {
+                const C2<R> sg = reinterpret_cast<const C2<R>*>(a.spg)[roff + m], w = om[0][q];
+                wv[q] = mk<R>(wv[q].x - sg.x * w.x, wv[q].y - sg.y * w.y);
+            }
         }
         if (pen) {
             const C2<R> kk = k2[m], mx = x2[m], my = y2[m];
@@ -485,8 +502,13 @@ __device__ __forceinline__ void nl_x_tile(const KArgs<R>& a, const int iy0) {
     }
 }
 
-template <typename R, int H, int TRV, int PART = NL_WHOLE>
-__global__ void __launch_bounds__(XRows<R, H, TRV>::THREADS) k_nl_x(KArgs<R> a) {
+// Blocks per SM that the fused x kernels' launch bounds ask for: MB > 0 an explicit count (the
+// autotuner's "two blocks an SM" candidates cap the registers for it), else the kernel's default.
+template <int MB, int DEF>
+constexpr int xminb() { return MB > 0 ? MB : DEF; }
+
+template <typename R, int H, int TRV, int PART = NL_WHOLE, int MB = 0, bool SPG = false>
+__global__ void __launch_bounds__(XRows<R, H, TRV>::THREADS, (xminb<MB, 1>())) k_nl_x(KArgs<R> a) {
     pdl_wait();     // the previous kernel of the stream has completed
     using X = XRows<R, H, TRV>;
     if constexpr (PART == NL_ADVECT) {
@@ -495,11 +517,11 @@ __global__ void __launch_bounds__(XRows<R, H, TRV>::THREADS) k_nl_x(KArgs<R> a) 
         // it still finds room on every SM
         const int ntile = a.g.ny / X::TR;
         for (int tile = blockIdx.x; tile < ntile; tile += gridDim.x) {
-            nl_x_tile<R, H, TRV, PART>(a, tile * X::TR);
+            nl_x_tile<R, H, TRV, PART, SPG>(a, tile * X::TR);
             __syncthreads();  // the next tile reuses the row buffers
         }
     } else {
-        nl_x_tile<R, H, TRV, PART>(a, blockIdx.x * X::TR);
+        nl_x_tile<R, H, TRV, PART, SPG>(a, blockIdx.x * X::TR);
     }
 }
 
@@ -701,10 +723,11 @@ __global__ void __launch_bounds__(NY / 8, (nl_y_minb<R, NY>())) k_nl_y(KArgs<R> 
 // K4: velocity at n+1, penalty, drag/energy reductions, vor_mean, Poisson RHS (forward-x),
 // stresses to physical space.
 // ======================================================================================
-template <typename R, int H, int TRV>
+template <typename R, int H, int TRV, int MB = 0>
 // (FP32: at most 128 registers a thread, so that two 256-thread blocks share an SM and the
 // 1024^2 grid runs in one wave; FP64 is bound by its arithmetic and keeps its registers)
-__global__ void __launch_bounds__(XRows<R, H, TRV>::THREADS, (sizeof(R) == 4) ? XRows<R, H, TRV>::MINB128 : 1) k_press_x(KArgs<R> a) {
+__global__ void __launch_bounds__(XRows<R, H, TRV>::THREADS,
+                                  (xminb<MB, (sizeof(R) == 4) ? XRows<R, H, TRV>::MINB128 : 1>())) k_press_x(KArgs<R> a) {
     pdl_wait();     // the previous kernel of the stream has completed
     using X = XRows<R, H, TRV>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -924,11 +947,11 @@ __global__ void __launch_bounds__(XRows<R, H, TRV>::THREADS, (sizeof(R) == 4) ? 
 
 // The viscous stresses (NavierStokes.f90:354-370: 2 nu d2psi/dxdy, nu (d2psi/dy2 - d2psi/dx2))
 // to physical space, beside k_press_x on another stream: only GetForces reads them.  With
-// a.by set, a block whose rows no stencil of the forces reaches (rows j - 4 .. j + 4 of the
-// stress points' cells j, BeamForces.f90:105-124, which lie within soff of the beam's
-// y range) leaves them; every block forms the range from the beam state alone.
-template <typename R, int H, int TRV>
-__global__ void __launch_bounds__(XRows<R, H, TRV>::THREADS) k_stress_x(KArgs<R> a) {
+// a.srows set, a block whose rows no stencil of the forces reaches (rows j - 4 .. j + 4 of the
+// stress points' cells j, BeamForces.f90:105-124, which lie within the stress points' offset
+// of the beam's y range; k_step_begin forms the range into S->srow) leaves them.
+template <typename R, int H, int TRV, int MB = 0>
+__global__ void __launch_bounds__(XRows<R, H, TRV>::THREADS, (xminb<MB, 1>())) k_stress_x(KArgs<R> a) {
     using X = XRows<R, H, TRV>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C2<R>* bufA = reinterpret_cast<C2<R>*>(smem_raw);
@@ -936,21 +959,9 @@ __global__ void __launch_bounds__(XRows<R, H, TRV>::THREADS) k_stress_x(KArgs<R>
     C2<R>* bufB = bufA + BS;
     const int r = threadIdx.x / X::G, t = threadIdx.x % X::G;
     const int iy0 = blockIdx.x * X::TR, ny = a.g.ny;
-    if (a.by) {
-        __shared__ double ymm[2][32];
-        double lo = 1e300, hi = -1e300;
-        for (int i = threadIdx.x; i < a.g.ns; i += blockDim.x) { lo = fmin(lo, a.by[i]); hi = fmax(hi, a.by[i]); }
-        for (int o = 16; o > 0; o >>= 1) {
-            lo = fmin(lo, __shfl_xor_sync(0xffffffffu, lo, o));
-            hi = fmax(hi, __shfl_xor_sync(0xffffffffu, hi, o));
-        }
-        if ((threadIdx.x & 31) == 0) { ymm[0][threadIdx.x >> 5] = lo; ymm[1][threadIdx.x >> 5] = hi; }
-        __syncthreads();
-        lo = ymm[0][0]; hi = ymm[1][0];
-        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) { lo = fmin(lo, ymm[0][w]); hi = fmax(hi, ymm[1][w]); }
-        // the cells' rows with two rows of margin for the rounding of the cell index
-        const double j0 = floor((lo - a.soff) * a.rdyi) - 6.0, j1 = floor((hi + a.soff) * a.rdyi) + 6.0;
-        if ((double)(iy0 + X::TR - 1) < j0 || (double)iy0 > j1) return;
+    if (a.srows) {
+        const int j0 = a.S->srow[0], j1 = a.S->srow[1];
+        if (iy0 + X::TR - 1 < j0 || iy0 > j1) return;
     }
     C2<R>* ra = bufA + r * X::PL;
     C2<R>* rb = bufB + r * X::PL;
@@ -972,10 +983,61 @@ __global__ void __launch_bounds__(XRows<R, H, TRV>::THREADS) k_stress_x(KArgs<R>
     }
 }
 
+// Threads of k_press_y: the paired FP32 engine (two butterflies a thread) or the one-butterfly
+// engine (FP64).
+template <typename R, int NY> constexpr int press_y_threads() { return kIsF32<R> ? NY / 16 : NY / 8; }
+
+// K5, FP32: the paired engine.  Thread u holds the row's elements 2u + h + m (NY/8) as v[2m + h];
+// the pairs are loaded from and stored to global memory as 16-byte accesses.  The arithmetic of
+// each element is that of the one-butterfly form below.
+template <int NY>
+__device__ __forceinline__ void press_y_paired(const KArgs<float>& a) {
+    constexpr int G = NY / 8, HG = G / 2;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float4* buf = reinterpret_cast<float4*>(smem_raw);
+    const int kx = blockIdx.x, u = threadIdx.x;
+    const Geometry& g = a.g;
+    const size_t row = (size_t)kx * NY;
+    const float4* p1 = reinterpret_cast<const float4*>(a.P1 + row);
+    const float4* p2 = reinterpret_cast<const float4*>(a.P2 + row);
+    float2 fp[2][16];
+#pragma unroll
+    for (int m = 0; m < 8; ++m) {
+        const float4 x = p1[u + m * HG], y = p2[u + m * HG];
+        fp[0][2 * m] = make_float2(x.x, x.y); fp[0][2 * m + 1] = make_float2(x.z, x.w);
+        fp[1][2 * m] = make_float2(y.x, y.y); fp[1][2 * m + 1] = make_float2(y.z, y.w);
+    }
+    block_fft2_m<NY, false, 2>(fp, buf, pair_slots(NY), a.twY, u);  // P1 and P2 together
+    const float norm = (float)(1.0 / ((double)g.nx * (double)g.ny));
+    float2 qv[1][16];
+#pragma unroll
+    for (int m = 0; m < 8; ++m)
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int ky = 2 * u + h + m * G;
+            const int ks = signed_k(ky, NY);
+            const float kys = (float)ks * (float)g.kys;
+            const float2 Q = cadd<float>(cscale<float>(fp[0][2 * m + h], norm), cimul<float>(cscale<float>(fp[1][2 * m + h], norm), kys));
+            const float k2 = (float)(kx * kx) * (float)g.scalex + (float)(ks * ks) * (float)g.scaley;
+            float2 qh = (kx == 0 && ky == 0) ? mk<float>(0, 0) : cscale<float>(Q, 1.0f / k2);
+            if (ky == NY / 2) qh = mk<float>(0, 0);
+            qv[0][2 * m + h] = qh;
+        }
+    block_fft2_m<NY, true, 1>(qv, buf, pair_slots(NY), a.twY, u);  // the forward transform left the rows free
+    float4* tq = reinterpret_cast<float4*>(a.Tq + row);
+#pragma unroll
+    for (int m = 0; m < 8; ++m)
+        tq[u + m * HG] = make_float4(qv[0][2 * m].x, qv[0][2 * m].y, qv[0][2 * m + 1].x, qv[0][2 * m + 1].y);
+}
+
 // K5: forward-y of the Poisson right-hand side, divergence, poisson, inverse-y -> Tq
 template <typename R, int NY>
-__global__ void __launch_bounds__(NY / 8, (kIsF32<R> && NY >= 4096) ? 2 : 1) k_press_y(KArgs<R> a) {
+__global__ void __launch_bounds__(press_y_threads<R, NY>(), (kIsF32<R> && NY >= 4096) ? 2 : 1) k_press_y(KArgs<R> a) {
     pdl_wait();     // the previous kernel of the stream has completed
+    if constexpr (kIsF32<R>) {
+        press_y_paired<NY>(a);
+        return;
+    }
     constexpr int G = NY / 8;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C2<R>* bufA = reinterpret_cast<C2<R>*>(smem_raw);
@@ -1014,8 +1076,8 @@ __global__ void __launch_bounds__(NY / 8, (kIsF32<R> && NY >= 4096) ? 2 : 1) k_p
 }
 
 // K6: inverse-x of q, p = q - |u|^2/2
-template <typename R, int H, int TRV>
-__global__ void __launch_bounds__(XRows<R, H, TRV>::THREADS) k_press_fin(KArgs<R> a) {
+template <typename R, int H, int TRV, int MB = 0>
+__global__ void __launch_bounds__(XRows<R, H, TRV>::THREADS, (xminb<MB, 1>())) k_press_fin(KArgs<R> a) {
     pdl_wait();     // the previous kernel of the stream has completed
     using X = XRows<R, H, TRV>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -1067,40 +1129,52 @@ struct SizeKernels {
     // tile-height candidates of the fused x kernels (index 1 is the default)
     struct XVariant {
         int rows, threads, smem1, smem3;  // smem3: the three row buffers of nl_x / press_x
+        int minb;                         // blocks per SM asked of the launch bounds (0: default)
         void (*nl_x)(KArgs<R>);
         void (*nl_adv)(KArgs<R>);  // k_nl_x's advection and penalization parts (two buffers)
         void (*nl_pen)(KArgs<R>);
+        void (*nl_x_spg)(KArgs<R>);   // nl_x and its advection part with the vorticity sponge
+        void (*nl_adv_spg)(KArgs<R>); // (the default tile only; null elsewhere)
         void (*stress_x)(KArgs<R>);  // two buffers
         void (*press_x)(KArgs<R>);
         void (*press_fin)(KArgs<R>);
-    } xv[3];
+    } xv[4];  // [0..2]: half, the default and twice the default tile height; [3]: the default, two blocks an SM
     // y-pass kernels for NY
     void (*yfwd)(KArgs<R>);
     void (*yinv)(KArgs<R>);
     void (*nl_y)(KArgs<R>);
     void (*press_y)(KArgs<R>);
     int y_threads, y_smem1, y_smem2, y_smem_nl;
+    int press_y_threads;  // the paired FP32 engine runs NY/16 threads
 };
 
-template <typename R, int H, int TR>
+template <typename R, int H, int TR, int MB = 0, bool SPG = false>
 inline void fill_xvariant(typename SizeKernels<R>::XVariant& v) {
     using X = XRows<R, H, TR>;
     v.rows = TR;
+    v.minb = MB;
     v.threads = X::THREADS;
     v.smem1 = (int)(TR * X::PL * sizeof(C2<R>));
     v.smem3 = 3 * v.smem1;
-    v.nl_x = k_nl_x<R, H, TR>;
-    v.nl_adv = k_nl_x<R, H, TR, NL_ADVECT>;
-    v.nl_pen = k_nl_x<R, H, TR, NL_PENAL>;
-    v.stress_x = k_stress_x<R, H, TR>;
-    cudaFuncSetAttribute(k_stress_x<R, H, TR>, cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * v.smem1);
-    cudaFuncSetAttribute(k_nl_x<R, H, TR, NL_ADVECT>, cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * v.smem1);
-    cudaFuncSetAttribute(k_nl_x<R, H, TR, NL_PENAL>, cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * v.smem1);
-    v.press_x = k_press_x<R, H, TR>;
-    v.press_fin = k_press_fin<R, H, TR>;
-    cudaFuncSetAttribute(k_nl_x<R, H, TR>, cudaFuncAttributeMaxDynamicSharedMemorySize, v.smem3);
-    cudaFuncSetAttribute(k_press_x<R, H, TR>, cudaFuncAttributeMaxDynamicSharedMemorySize, v.smem3);
-    cudaFuncSetAttribute(k_press_fin<R, H, TR>, cudaFuncAttributeMaxDynamicSharedMemorySize, v.smem1);
+    v.nl_x = k_nl_x<R, H, TR, NL_WHOLE, MB>;
+    v.nl_adv = k_nl_x<R, H, TR, NL_ADVECT, MB>;
+    v.nl_pen = k_nl_x<R, H, TR, NL_PENAL, MB>;
+    v.nl_x_spg = v.nl_adv_spg = nullptr;
+    if constexpr (SPG) {
+        v.nl_x_spg = k_nl_x<R, H, TR, NL_WHOLE, MB, true>;
+        v.nl_adv_spg = k_nl_x<R, H, TR, NL_ADVECT, MB, true>;
+        cudaFuncSetAttribute(k_nl_x<R, H, TR, NL_WHOLE, MB, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, v.smem3);
+        cudaFuncSetAttribute(k_nl_x<R, H, TR, NL_ADVECT, MB, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * v.smem1);
+    }
+    v.stress_x = k_stress_x<R, H, TR, MB>;
+    cudaFuncSetAttribute(k_stress_x<R, H, TR, MB>, cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * v.smem1);
+    cudaFuncSetAttribute(k_nl_x<R, H, TR, NL_ADVECT, MB>, cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * v.smem1);
+    cudaFuncSetAttribute(k_nl_x<R, H, TR, NL_PENAL, MB>, cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * v.smem1);
+    v.press_x = k_press_x<R, H, TR, MB>;
+    v.press_fin = k_press_fin<R, H, TR, MB>;
+    cudaFuncSetAttribute(k_nl_x<R, H, TR, NL_WHOLE, MB>, cudaFuncAttributeMaxDynamicSharedMemorySize, v.smem3);
+    cudaFuncSetAttribute(k_press_x<R, H, TR, MB>, cudaFuncAttributeMaxDynamicSharedMemorySize, v.smem3);
+    cudaFuncSetAttribute(k_press_fin<R, H, TR, MB>, cudaFuncAttributeMaxDynamicSharedMemorySize, v.smem1);
 }
 
 template <typename R, int N>
@@ -1119,8 +1193,11 @@ inline void fill_size_kernels(SizeKernels<R>& k) {
     cudaFuncSetAttribute(k_vel_x<R, H>, cudaFuncAttributeMaxDynamicSharedMemorySize, k.x_smem2);
     constexpr int T0 = xrows_valid<R, H>(X::TRD / 2), T1 = X::TRD, T2 = xrows_valid<R, H>(X::TRD * 2);
     fill_xvariant<R, H, T0>(k.xv[0]);
-    fill_xvariant<R, H, T1>(k.xv[1]);
+    fill_xvariant<R, H, T1, 0, true>(k.xv[1]);
     fill_xvariant<R, H, T2>(k.xv[2]);
+    // the default tile with the registers capped for two resident blocks (when two fit an SM)
+    constexpr int MB2 = (2 * XRows<R, H, T1>::THREADS <= 2048) ? 2 : 1;
+    fill_xvariant<R, H, T1, MB2>(k.xv[3]);
     k.nl_x = k.xv[1].nl_x;
     k.press_x = k.xv[1].press_x;
     k.press_fin = k.xv[1].press_fin;
@@ -1131,6 +1208,8 @@ inline void fill_size_kernels(SizeKernels<R>& k) {
     k.y_threads = N / 8;
     k.y_smem1 = (int)(padded_len(N) * sizeof(C2<R>));
     k.y_smem2 = 2 * k.y_smem1;
+    if (kIsF32<R>) k.y_smem2 = std::max(k.y_smem2, 2 * pair_slots(N) * 16);
+    k.press_y_threads = press_y_threads<R, N>();
     k.y_smem_nl = nl_y_bufs<R>() * k.y_smem1;
     cudaFuncSetAttribute(k_yfwd<R, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, k.y_smem1);
     cudaFuncSetAttribute(k_yinv<R, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, k.y_smem1);

@@ -168,6 +168,7 @@ __global__ void __launch_bounds__(128) k_mask_prep(MaskArgs a, double gerf) {
             const int p0 = R[0], p1 = R[1], p2 = R[2], p3 = R[3];
             R[0] = n0; R[1] = n1; R[2] = n2; R[3] = n3;
             R[4] = min(n0, p0); R[5] = max(n1, p1); R[6] = min(n2, p2); R[7] = max(n3, p3);
+            if (a.full) { R[4] = 0; R[5] = a.nx - 1; R[6] = 0; R[7] = a.ny - 1; }  // walls, sponges: every cell
             R[8] = a.nx; R[9] = -1; R[10] = a.ny; R[11] = -1;
             R[12] = 0;
             *a.nprims = total;
@@ -364,6 +365,41 @@ __device__ __forceinline__ void mask_prim(const MaskArgs& a, const Prim& Q, cons
     fold_take(f, temp, Q.p[2], Q.p[3], q);
 }
 
+// SmoothStep (create_mask.f90:475-520) with the reference's divisions, for the static parts.
+__device__ __forceinline__ double smooth_step_div(double x, double t, double h, int sharp, double gerf) {
+    if (sharp) return (x <= t) ? 1.0 : 0.0;
+    const double delta = h * gerf;
+    return 0.5 * (erf((t - x) / delta) + erf((x + t) / delta));
+}
+// SmoothStep2 (create_mask.f90:523-545)
+__device__ __forceinline__ double smooth_step2(double x, double t, double h, double pi) {
+    if (x <= t - h) return 1.0;
+    if ((t - h) < x && x < (t + h)) return 0.5 * (1. + cos((x - t + h) * pi / (2.0 * h)));
+    return 0.0;
+}
+
+// The parts drawn after the beam (create_mask.f90:131-204) on the unscaled value m and the
+// velocity of cell (i, j): the velocity sponge of iSponge = 4 (both halves, in the reference's
+// order) and the frame of iSponge = 22.  U, V: Mean_ux, Mean_uy of the time.
+__device__ __forceinline__ void mask_finish(const MaskArgs& a, double gerf, int i, int j, size_t cell, double U, double V,
+                                            double& m, double& vx, double& vy) {
+    if (a.sponge4) {
+        auto column = [&](double x, double t, double h) {
+            const double tmp = smooth_step_div(x, t, h, a.sharp, gerf);
+            if (m < tmp) m = tmp;
+            const double yc = (double)j * a.dy - a.h_channel;
+            vx = (yc > 0.0 && yc < a.H_eff) ? 1.5 * U * yc * (a.H_eff - yc) / ((0.5 * a.H_eff) * (0.5 * a.H_eff)) : 0.0;
+        };
+        if (i <= a.s4_l1) column(0.75 * a.s4_star - (double)i * a.dx, a.s4_size * 0.5, 0.25 * a.s4_size);
+        if (i >= a.s4_r0 && i <= a.s4_r1) column((double)i * a.dx - 0.5 * a.s4_star, a.s4_size * 0.5, a.N_smooth * a.dx);
+    }
+    if (a.frame) {
+        const double fr = a.frame[cell];
+        m = m + fr * a.frame_c;
+        if (fr > 0.0) { vx = U; vy = V; }
+    }
+}
+
 // The primitives in draw order, per cell (create_mask.f90:2-218): segments and then hinges and
 // dots keep the largest SmoothStep (the first of equal values); the sharp end between them
 // overwrites the value.  Each warp folds its share of a range of primitives; the block
@@ -395,6 +431,9 @@ __global__ void __launch_bounds__(32 * MASK_WARPS) k_mask_raster(MaskArgs a, dou
     const double two_mxd = 2.0 * mxd;
     const float mg = 1.0e-5f * (float)fmax((double)a.nx * dx, (double)a.ny * dy);
     const int total = *a.nprims;
+    // Mean_ux, Mean_uy of the time, for the velocity sponge and the frame
+    const double Um = a.full ? mean_flow_x(a.iMeanVelocity, a.S->time, a.cos_ti, a.T_fullspeed, a.pi) : 0.0;
+    const double Vm = a.full ? mean_flow_y(a.iMeanVelocity, a.S->time, a.sin_ti, a.T_fullspeed, a.pi) : 0.0;
     const int nseg = a.ns - 1, nsharp = (a.sharp_trailing == 1) ? 1 : 0;
     // FP32 form: the cell's offset from its tile's origin and the SmoothStep constants
     const float cx = (float)((double)(lane % MASK_TX) * dx), cy = (float)((double)(lane / MASK_TX) * dy);
@@ -405,7 +444,15 @@ __global__ void __launch_bounds__(32 * MASK_WARPS) k_mask_raster(MaskArgs a, dou
         const int i = ix0 + (lane % MASK_TX), j = iy0 + (lane / MASK_TX);
         const size_t cell = (size_t)j * a.nx + i;
         if (r1 < ix0 || r0 > ix1 || r3 < iy0 || r2 > iy1) {
-            if (warp == 0) { mk_[cell] = (R)0; vx_[cell] = (R)0; vy_[cell] = (R)0; }
+            if (warp == 0) {
+                if (a.full) {
+                    double m = a.bg ? a.bg[cell] : 0.0, vx = 0.0, vy = 0.0;
+                    mask_finish(a, gerf, i, j, cell, Um, Vm, m, vx, vy);
+                    mk_[cell] = (R)(m * inv_eps); vx_[cell] = (R)vx; vy_[cell] = (R)vy;
+                } else {
+                    mk_[cell] = (R)0; vx_[cell] = (R)0; vy_[cell] = (R)0;
+                }
+            }
             continue;
         }
         const double xi = (double)i * dx, yj = (double)j * dy;
@@ -413,6 +460,11 @@ __global__ void __launch_bounds__(32 * MASK_WARPS) k_mask_raster(MaskArgs a, dou
         const double x0 = (double)ix0 * dx, y0 = (double)iy0 * dy;
         MaskFold<T> f;
         f.m = (T)0; f.vx = (T)0; f.vy = (T)0; f.idx = 0x7fffffff; f.mlow = 0.f;
+        if (a.bg) {  // walls and cylinder come first in the draw order (velocity 0)
+            const double b0 = a.bg[cell];
+            f.m = (T)b0;
+            f.mlow = __double2float_rd(b0);
+        }
         // this warp's primitives of [q0, q1): q = q0 + MASK_WARPS (32 c + lane) + warp, staged
         // per round of 32 with their FP32 pre-test data
         auto fold_range = [&](int q0, int q1) {
@@ -513,9 +565,11 @@ __global__ void __launch_bounds__(32 * MASK_WARPS) k_mask_raster(MaskArgs a, dou
         fold_range(nseg + nsharp, total);
         combine();
         if (warp == 0) {
-            mk_[cell] = (R)((double)f.m * inv_eps);
-            vx_[cell] = (R)f.vx;
-            vy_[cell] = (R)f.vy;
+            double m = (double)f.m, vx = (double)f.vx, vy = (double)f.vy;
+            if (a.full) mask_finish(a, gerf, i, j, cell, Um, Vm, m, vx, vy);
+            mk_[cell] = (R)(m * inv_eps);
+            vx_[cell] = (R)vx;
+            vy_[cell] = (R)vy;
         }
     }
 }
@@ -702,6 +756,107 @@ __global__ void __launch_bounds__(128) k_forces(ForceArgs a, double dxi, double 
 void launch_mask_prep(const MaskArgs& a, double gerf, cudaStream_t st, bool pdl) {
     launch_k(k_mask_prep, dim3((a.ns + 3 + 31) / 32), dim3(128), 0, st, pdl, a, gerf);
 }
+// The walls (create_mask.f90:30-54: each wall row assigned its SmoothStep) and the leading-edge
+// cylinder (:66-68, DrawADot with the strict > rule), and the frame of iSponge = 22
+// (SmoothFrameAroundDomain, :370-470: the level set of the distance to the domain's edges with
+// rounded corners, each pass of the reference applied to the cell in its order), per cell.
+__global__ void k_static_masks(StaticMaskArgs a, double gerf) {
+    const size_t n = (size_t)a.nx * a.ny;
+    for (size_t cell = blockIdx.x * (size_t)blockDim.x + threadIdx.x; cell < n; cell += (size_t)gridDim.x * blockDim.x) {
+        const int i = (int)(cell % a.nx), j = (int)(cell / a.nx);
+        const double x = (double)i * a.dx, y = (double)j * a.dy, mx = fmax(a.dx, a.dy);
+        if (a.bg) {
+            double m = 0.0;
+            if (a.iWalls > 0) {
+                const double h = a.h_channel, hs = h + a.N * a.dy;
+                if (j <= (int)llround(hs / a.dy)) m = smooth_step_div(y, h, a.N * a.dy, a.sharp, gerf);
+                if (j >= (int)llround((a.yl - hs) / a.dy)) m = smooth_step_div(fabs(y - a.yl), h, a.N * a.dy, a.sharp, gerf);
+            }
+            if (a.iCylinder == 1) {
+                const double px = a.x0 - a.R_cylinder, py = a.y0;
+                const double Rr = sqrt((x - px) * (x - px) + (y - py) * (y - py));
+                const double temp = smooth_step_div(Rr, a.R_cylinder, a.N * mx, a.sharp, gerf);
+                if (temp > m) m = temp;
+            }
+            a.bg[cell] = m;
+        }
+        if (a.frame) {
+            const double th = 4.0 * a.t_beam, R1 = 0.0, R2 = 2.0 * th, RR = R1 + R2;
+            const int ixmin = (int)llround(RR / a.dx), ixmax = a.nx - (int)llround(RR / a.dx);
+            const int iymin = (int)llround(RR / a.dy), iymax = a.ny - (int)llround(RR / a.dy);
+            double phi = 1000.0;
+            if (i >= ixmin && i <= ixmax) {
+                const double m = fmin(phi, fmin(fabs(y - R1), fabs(y - (a.yl - R1))));
+                phi = ((j <= (int)llround(R1 / a.dy)) || (j >= a.ny - 1 - (int)llround(R1 / a.dy))) ? -m : +m;
+            }
+            if (j >= iymin && j <= iymax) {
+                const double m = fmin(phi, fmin(fabs(x - R1), fabs(x - (a.xl - R1))));
+                phi = ((i <= (int)llround(R1 / a.dx)) || (i >= a.nx - 1 - (int)llround(R1 / a.dx))) ? -m : +m;
+            }
+            auto corner = [&](int x0_, int x1_, int y0_, int y1_, double cx, double cy) {
+                if (i >= x0_ && i <= x1_ && j >= y0_ && j <= y1_)
+                    phi = fmin(phi, -(sqrt((x - cx) * (x - cx) + (y - cy) * (y - cy)) - R2));
+            };
+            corner(0, ixmin, 0, iymin, RR, RR);
+            corner(0, ixmin, iymax, a.ny - 1, RR, a.yl - RR);
+            corner(ixmax, a.nx - 1, iymax, a.ny - 1, a.xl - RR, a.yl - RR);
+            corner(ixmax, a.nx - 1, 0, iymin, a.xl - RR, RR);
+            a.frame[cell] = smooth_step2(phi, th / 2., th / 2., a.pi);
+        }
+    }
+}
+
+// The vorticity sponge (create_sponge_mask, create_mask.f90:223-364) after the start-up mask:
+// iSponge 1 (outflow), 2 (inflow, reduced inside the obstacle), 3 (around the domain), 22 (a
+// frame with a hole, zero on the obstacle); divided by eps_sponge.
+template <typename Rt>
+__global__ void k_sponge_mask(StaticMaskArgs a, double gerf) {
+    const size_t n = (size_t)a.nx * a.ny;
+    Rt* out = reinterpret_cast<Rt*>(a.spg);
+    const Rt* mk = reinterpret_cast<const Rt*>(a.mask);
+    const double dx = a.dx, dy = a.dy, N = a.N, sss = a.SpongeSize, xl = a.xl, yl = a.yl;
+    for (size_t cell = blockIdx.x * (size_t)blockDim.x + threadIdx.x; cell < n; cell += (size_t)gridDim.x * blockDim.x) {
+        const int i = (int)(cell % a.nx), j = (int)(cell / a.nx);
+        double v = 0.0;
+        if (a.iSponge == 1) {
+            const double ss = sss - 2.0 * N * dx;
+            const int l0 = (int)llround((xl - sss) / dx), l1 = (int)llround((xl - 0.5 * sss) / dx);
+            if (i >= l0 && i <= l1) v = smooth_step_div(xl - 0.5 * sss - (double)i * dx, ss * 0.5, N * dx, a.sharp, gerf);
+            if (i >= l1) v = smooth_step_div((double)i * dx - xl + 0.5 * sss - 1.0 * dx, ss * 0.4, N * dx, a.sharp, gerf);
+        } else if (a.iSponge == 2) {
+            const double ss = sss - 2.0 * N * dx;
+            const int l1 = (int)llround((0.5 * sss) / dx), r1 = (int)llround((1.0 * sss) / dx);
+            if (i <= l1) v = smooth_step_div(0.5 * sss - (double)i * dx, ss * 0.5, N * dx, a.sharp, gerf);
+            if (i >= l1 && i <= r1) v = smooth_step_div((double)i * dx - 0.5 * sss, ss * 0.5, N * dx, a.sharp, gerf);
+            if (i <= r1) {
+                const double me = (double)mk[cell] * a.eps;
+                if (me > 0.0) v = v * (1.0 - me);
+            }
+        } else if (a.iSponge == 3) {
+            const double ss = sss - N * dx;
+            const double t1 = smooth_step_div((double)i * dx, ss, N * dx, a.sharp, gerf);
+            const double t2 = smooth_step_div(xl - (double)i * dx, ss, N * dx, a.sharp, gerf);
+            const double t3 = smooth_step_div((double)j * dy, ss, N * dy, a.sharp, gerf);
+            const double t4 = smooth_step_div(yl - (double)j * dy, ss, N * dy, a.sharp, gerf);
+            v = fmin(t1 + t2 + t3 + t4, 1.0);
+        } else if (a.iSponge == 22) {
+            const int x0 = (int)llround(sss / dx), y0 = (int)llround(sss / dy);
+            const int x1 = (int)llround((xl - sss) / dx), y1 = (int)llround((yl - sss) / dy);
+            const bool hole = i >= x0 && i <= x1 && j >= y0 && j <= y1;
+            v = (hole || mk[cell] > (Rt)0) ? 0.0 : 1.0;
+        }
+        out[cell] = (Rt)(v / a.eps_sponge);
+    }
+}
+
+void launch_static_masks(const StaticMaskArgs& a, double gerf, cudaStream_t st) {
+    k_static_masks<<<1024, 256, 0, st>>>(a, gerf);
+}
+void launch_sponge_mask(const StaticMaskArgs& a, double gerf, cudaStream_t st) {
+    if (a.fp32) k_sponge_mask<float><<<1024, 256, 0, st>>>(a, gerf);
+    else k_sponge_mask<double><<<1024, 256, 0, st>>>(a, gerf);
+}
+
 void launch_mask(const MaskArgs& a, double gerf, bool fp32, cudaStream_t st, bool pdl) {
     // four-warp blocks, two per SM: a tile's primitives over the four SMSPs of an SM
     const int blocks = 2 * a.nsm;

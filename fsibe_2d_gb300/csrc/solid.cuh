@@ -25,6 +25,48 @@ struct MaskArgs {
     double rdx, rdy, rpi, angle_rad;  // 1/dx, 1/dy, 1/pi (correctly rounded), angle_deg*pi/180
     int nsm;      // SMs of the device (raster grid size)
     void *mask, *mvx, *mvy;  // R*[ny][nx]
+    // the parts of the mask that are not the beam (create_mask.f90:21-68, 120-204); with `full`
+    // set every cell is drawn each step (the box is the grid)
+    int full;
+    const double* bg;        // walls and the leading-edge cylinder (unscaled, velocity 0), or null
+    const double* frame;     // iSponge = 22: the smoothed frame around the domain, or null
+    double frame_c;          // its weight eps / max(1e-3, eps)
+    int sponge4;             // iSponge = 4: the velocity sponge at the inflow
+    int s4_l1, s4_r0, s4_r1; // its columns: [0, s4_l1] (left half), [s4_r0, s4_r1] (right half)
+    double s4_star, s4_size, h_channel, H_eff;
+    int iMeanVelocity;       // Mean_ux / Mean_uy of the time (mean_velocity.f90:4-84)
+    double T_fullspeed, cos_ti, sin_ti;
+};
+
+// Mean_ux / Mean_uy (mean_velocity.f90:4-84) for iMeanVelocity 1, 2, 3, 4, 6, 22.
+__device__ __forceinline__ double mean_flow_x(int mode, double time, double cos_ti, double Tf, double pi) {
+    switch (mode) {
+        case 1: return cos_ti * ((time < Tf) ? (time * time * time) / (-0.5 * Tf * Tf * Tf) + 3.0 * (time * time) / (Tf * Tf) : 1.0);
+        case 2: return cos_ti * ((time < Tf) ? 0.5 * (1.0 - cos(0.5 * pi * time / Tf)) : 1.0);
+        case 3: return cos_ti;
+        case 6: return time;
+        case 22: return 0.1;
+        default: return 0.0;
+    }
+}
+__device__ __forceinline__ double mean_flow_y(int mode, double time, double sin_ti, double Tf, double pi) {
+    switch (mode) {
+        case 1: return sin_ti * ((time < Tf) ? (time * time * time) / (-0.5 * Tf * Tf * Tf) + 3.0 * (time * time) / (Tf * Tf) : 1.0);
+        case 2: return sin_ti * ((time < Tf) ? 0.5 * (1.0 - cos(0.5 * pi * time / Tf)) : 1.0);
+        case 3: return sin_ti;
+        default: return 0.0;
+    }
+}
+
+// The static fields of the walls, cylinder, frame and vorticity sponge (solid.cu).
+struct StaticMaskArgs {
+    int nx, ny, sharp, iWalls, iCylinder, iSponge;
+    double dx, dy, xl, yl, N, pi, h_channel, R_cylinder, x0, y0, t_beam, SpongeSize, eps, eps_sponge;
+    double* bg;              // out: walls + cylinder
+    double* frame;           // out: iSponge = 22
+    void* spg;               // out: R*[ny][nx] the vorticity sponge / eps_sponge
+    const void* mask;        // in (sponge): the start-up mask (R, divided by eps)
+    int fp32;
 };
 
 struct ForceArgs {

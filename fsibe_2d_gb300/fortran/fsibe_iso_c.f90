@@ -22,6 +22,8 @@ module fsibe_iso_c
     integer(c_int32_t) :: iBeam, iSharpTrailing, iMeanVelocity, idealis
     real(c_double) :: T_fullspeed, theta_inf, x0, y0, length, t_beam, N_smooth, newton_tol
     integer(c_int32_t) :: newton_maxit, reserved
+    integer(c_int32_t) :: iWalls, iCylinder, iSponge, reserved2
+    real(c_double) :: h_channel, R_cylinder, SpongeSize, eps_sponge
   end type
 
   type, bind(C) :: fsibe_scalars_t
@@ -155,6 +157,8 @@ contains
     p%T_fullspeed = T_fullspeed; p%theta_inf = theta_inf; p%x0 = x0; p%y0 = y0
     p%length = length; p%t_beam = t_beam; p%N_smooth = N_smooth
     p%newton_tol = 1.0d-7; p%newton_maxit = 50; p%reserved = 0
+    p%iWalls = iWalls; p%iCylinder = iCylinder; p%iSponge = iSponge; p%reserved2 = 0
+    p%h_channel = h_channel; p%R_cylinder = R_cylinder; p%SpongeSize = SpongeSize; p%eps_sponge = eps_sponge
     st = fsibe_create(p, gctx)
     call fsibe_check(st, "fsibe_create")
   end subroutine

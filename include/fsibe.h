@@ -84,6 +84,13 @@ typedef struct fsibe_params {
     double  newton_tol;          /* reference hard-codes 1e-7 (SolidSolver.f90:126)           */
     int32_t newton_maxit;        /* reference stops after iteration 49 (SolidSolver.f90:298)  */
     int32_t reserved;
+    /* channel walls, a cylinder at the leading edge and sponges (share_vars.f90:11-21, read by
+     * params.f90:32-78); all zero leaves the beam alone in the periodic box */
+    int32_t iWalls;              /* 1: walls of half thickness h_channel at y = 0 and y = yl   */
+    int32_t iCylinder;           /* 1: a cylinder of radius R_cylinder touching the leading edge */
+    int32_t iSponge;             /* 1, 2, 3, 22: vorticity sponges; 4: velocity sponge (inflow)  */
+    int32_t reserved2;
+    double  h_channel, R_cylinder, SpongeSize, eps_sponge;
 } fsibe_params;
 
 /* Per-step scalar outputs: the columns of beam_data (BeamIO.f90:193-216),
@@ -251,10 +258,14 @@ int fsibe_kernel_times(fsibe_ctx* ctx, int nsteps, fsibe_kernel_time* out, int c
  * the solve count.  out32 receives 32 values; reset != 0 zeroes them after reading. */
 int fsibe_beam_phase_cycles(fsibe_ctx* ctx, long long* out32, int reset);
 /* Rows per block chosen by the autotuner for the fused x-pass kernels (nl_x, press_x,
- * press_fin).  fsibe_create times three tile heights per kernel on the new context's
- * buffers and keeps the fastest (cached per precision and grid size for the process;
- * FSIBE_AUTOTUNE=0 in the environment keeps the defaults). */
+ * press_fin).  fsibe_create times four candidates per kernel on the new context's buffers --
+ * half, the default and twice the default tile height, and the default tile with its
+ * registers capped for two resident blocks an SM -- and keeps the fastest (cached per
+ * precision and grid size for the process; FSIBE_AUTOTUNE=0 in the environment keeps the
+ * defaults).  fsibe_tile_config gives the rows and the blocks-per-SM bound (0: the kernel's
+ * default) of each: out6 = {rows, bound} for nl_x, press_x, press_fin. */
 int fsibe_tiles(fsibe_ctx* ctx, int32_t* rows3);
+int fsibe_tile_config(fsibe_ctx* ctx, int32_t* out6);
 
 /* CTAs of the thread-block cluster that runs the beam's Newton step (16 or 8; 0 when the
  * single-CTA kernel runs it).  Chosen at fsibe_create from what the device can place;

@@ -153,6 +153,7 @@ struct orc_ctx {
     bool sharp;
     double U_mean_true = 1.0;
     std::vector<double> dealiase, mask, maskvx, maskvy, vor_mean;
+    std::vector<double> mask_sponge, mask_frame;  /* vorticity sponge / eps_sponge; the frame of iSponge 22 */
     int n0 = 0, n1 = 1;
     double time = 0, dt0 = 0, dt1 = 0;
     std::vector<double> vortk[2], nlk[2], workvis[2], u, press;
@@ -472,6 +473,12 @@ static inline double SmoothStep(const orc_ctx* c, double x, double t, double h) 
     return (x <= t) ? 1.0 : 0.0;
 }
 
+static inline double SmoothStep2(const orc_ctx* c, double x, double t, double h) {  /* create_mask.f90:523-545 */
+    if (x <= t - h) return 1.0;
+    if ((t - h) < x && x < (t + h)) return 0.5 * (1. + std::cos((x - t + h) * c->pi / (2.0 * h)));
+    return 0.0;
+}
+
 static inline double ConvertAngle(const orc_ctx* c, double a) { return (a < 0.0) ? 2.0 * c->pi + a : a; }
 
 static inline long nint(double v) { return std::lround(v); }
@@ -594,11 +601,62 @@ static int DrawADot(orc_ctx* c, double px, double py, double vx, double vy, doub
     return FSIBE_OK;
 }
 
-static int create_mask(orc_ctx* c, double time) {  /* create_mask.f90:2-218 (beam branch) */
-    const double N = c->P.N_smooth;
+/* SmoothFrameAroundDomain (create_mask.f90:370-470): a level set phi of the distance to the
+ * domain's edges with rounded corners, smoothed into a frame mask of the thickness 4 t_beam. */
+static void SmoothFrameAroundDomain(orc_ctx* c, std::vector<double>& mask1) {
+    const int nx = c->nx, ny = c->ny;
+    const double dx = c->dx, dy = c->dy, xl = c->P.xl, yl = c->P.yl;
+    std::vector<double> phi((size_t)nx * ny, 1000.0);
+    const double thickness = 4.0 * c->P.t_beam, R1 = 0.0, R2 = 2.0 * thickness, RR = R1 + R2;
+    const long ixmin = nint(RR / dx), ixmax = nx - nint(RR / dx), iymin = nint(RR / dy), iymax = ny - nint(RR / dy);
+#define PHI(ix, iy) phi[(size_t)(iy) * nx + (ix)]
+    for (long ix = ixmin; ix <= ixmax; ++ix)
+        for (long iy = 0; iy <= ny - 1; ++iy) {
+            const double y = (double)iy * dy;
+            const double m = std::min(PHI(ix, iy), std::min(std::fabs(y - R1), std::fabs(y - (yl - R1))));
+            PHI(ix, iy) = ((iy <= nint(R1 / dy)) || (iy >= ny - 1 - nint(R1 / dy))) ? -m : +m;
+        }
+    for (long ix = 0; ix <= nx - 1; ++ix)
+        for (long iy = iymin; iy <= iymax; ++iy) {
+            const double x = (double)ix * dx;
+            const double m = std::min(PHI(ix, iy), std::min(std::fabs(x - R1), std::fabs(x - (xl - R1))));
+            PHI(ix, iy) = ((ix <= nint(R1 / dx)) || (ix >= nx - 1 - nint(R1 / dx))) ? -m : +m;
+        }
+    auto corner = [&](long x0_, long x1_, long y0_, long y1_, double cx, double cy) {
+        for (long ix = x0_; ix <= x1_; ++ix)
+            for (long iy = y0_; iy <= y1_; ++iy) {
+                const double x = (double)ix * dx, y = (double)iy * dy;
+                PHI(ix, iy) = std::min(PHI(ix, iy), -(std::sqrt((x - cx) * (x - cx) + (y - cy) * (y - cy)) - R2));
+            }
+    };
+    corner(0, ixmin, 0, iymin, RR, RR);
+    corner(0, ixmin, iymax, ny - 1, RR, yl - RR);
+    corner(ixmax, nx - 1, iymax, ny - 1, xl - RR, yl - RR);
+    corner(ixmax, nx - 1, 0, iymin, xl - RR, RR);
+    for (size_t k = 0; k < phi.size(); ++k) mask1[k] = SmoothStep2(c, phi[k], thickness / 2., thickness / 2.);
+#undef PHI
+}
+
+static int create_mask(orc_ctx* c, double time) {  /* create_mask.f90:2-218 */
+    const double N = c->P.N_smooth, dx = c->dx, dy = c->dy, yl = c->P.yl;
     std::fill(c->mask.begin(), c->mask.end(), 0.0);
     std::fill(c->maskvx.begin(), c->maskvx.end(), 0.0);
     std::fill(c->maskvy.begin(), c->maskvy.end(), 0.0);
+    if (c->P.iWalls > 0) {  /* :30-54, walls in the y direction */
+        const double h = c->P.h_channel, h_star = h + N * dy;
+        for (long j = 0; j <= nint(h_star / dy); ++j) {
+            const double temp = SmoothStep(c, (double)j * dy, h, N * dy);
+            for (int i = 0; i < c->nx; ++i) F2(c->mask, i, j) = temp;
+        }
+        for (long j = c->ny - 1; j >= nint((yl - h_star) / dy); --j) {
+            const double temp = SmoothStep(c, std::fabs((double)j * dy - yl), h, N * dy);
+            for (int i = 0; i < c->nx; ++i) F2(c->mask, i, j) = temp;
+        }
+    }
+    if (c->P.iCylinder == 1) {  /* :66-68 */
+        const int st = DrawADot(c, c->P.x0 - c->P.R_cylinder, c->P.y0, 0.0, 0.0, c->P.R_cylinder, N);
+        if (st) return st;
+    }
     if (c->P.iBeam > 0) {
         Beam& b = c->beam;
         double alpha, alpha_t, alpha_tt, LE[6];
@@ -620,8 +678,84 @@ static int create_mask(orc_ctx* c, double time) {  /* create_mask.f90:2-218 (bea
             if (st) return st;
         }
     }
+    if (c->P.iSponge == 4) {  /* :131-181, velocity sponge at the inflow with a channel profile */
+        const double sss = c->P.SpongeSize, ss = sss - 2.0 * N * dx, H_eff = yl - 2.0 * c->P.h_channel;
+        const double U = Mean_Ux(c, time);
+        auto column = [&](long ix, double x, double t, double h) {
+            const double tmp = SmoothStep(c, x, t, h);
+            for (int iy = 0; iy < c->ny; ++iy) {
+                const double y_chan = (double)iy * dy - c->P.h_channel;
+                if (F2(c->mask, ix, iy) < tmp) F2(c->mask, ix, iy) = tmp;
+                F2(c->maskvx, ix, iy) = (y_chan > 0.0 && y_chan < H_eff)
+                    ? 1.5 * U * y_chan * (H_eff - y_chan) / ((0.5 * H_eff) * (0.5 * H_eff)) : 0.0;
+            }
+        };
+        for (long ix = 0; ix <= nint((0.5 * sss) / dx); ++ix) column(ix, 0.75 * sss - (double)ix * dx, ss * 0.5, 0.25 * ss);
+        for (long ix = nint((0.5 * sss) / dx); ix <= nint((1.0 * sss) / dx); ++ix)
+            column(ix, (double)ix * dx - 0.5 * sss, ss * 0.5, N * dx);
+    }
+    if (c->P.iSponge == 22) {  /* :188-204, the frame around the domain */
+        if (*std::max_element(c->mask_frame.begin(), c->mask_frame.end()) < 1.0) SmoothFrameAroundDomain(c, c->mask_frame);
+        const double f = c->P.eps / std::max(1.0e-3, c->P.eps);
+        const double U = Mean_Ux(c, time), V = Mean_Uy(c, time);
+        for (size_t k = 0; k < c->mask.size(); ++k) {
+            c->mask[k] = c->mask[k] + c->mask_frame[k] * f;
+            if (c->mask_frame[k] > 0.0) { c->maskvx[k] = U; c->maskvy[k] = V; }
+        }
+    }
     for (size_t k = 0; k < c->mask.size(); ++k) c->mask[k] = c->mask[k] / c->P.eps;
     return FSIBE_OK;
+}
+
+/* create_sponge_mask (create_mask.f90:223-364), once after the start-up mask: the vorticity
+ * sponge of iSponge 1 (outflow), 2 (inflow, outside the obstacle), 3 (around the domain) and
+ * 22 (a frame with a hole, outside the obstacle), divided by eps_sponge. */
+static void create_sponge_mask(orc_ctx* c) {
+    const double N = c->P.N_smooth, dx = c->dx, dy = c->dy, xl = c->P.xl, yl = c->P.yl, sss = c->P.SpongeSize;
+    std::vector<double>& ms = c->mask_sponge;
+    std::fill(ms.begin(), ms.end(), 0.0);
+    const int isp = c->P.iSponge;
+    if (isp == 1) {
+        const double ss = sss - 2.0 * N * dx, begin = xl - sss;
+        for (long ix = nint(begin / dx); ix <= nint((xl - 0.5 * sss) / dx); ++ix) {
+            const double tmp = SmoothStep(c, xl - 0.5 * sss - (double)ix * dx, ss * 0.5, N * dx);
+            for (int iy = 0; iy < c->ny; ++iy) F2(ms, ix, iy) = tmp;
+        }
+        for (long ix = nint((xl - 0.5 * sss) / dx); ix <= c->nx - 1; ++ix) {
+            const double tmp = SmoothStep(c, (double)ix * dx - xl + 0.5 * sss - 1.0 * dx, ss * 0.4, N * dx);
+            for (int iy = 0; iy < c->ny; ++iy) F2(ms, ix, iy) = tmp;
+        }
+    } else if (isp == 2) {
+        const double ss = sss - 2.0 * N * dx;
+        const long ixmax = nint((1.0 * sss) / dx);
+        for (long ix = 0; ix <= nint((0.5 * sss) / dx); ++ix) {
+            const double tmp = SmoothStep(c, 0.5 * sss - (double)ix * dx, ss * 0.5, N * dx);
+            for (int iy = 0; iy < c->ny; ++iy) F2(ms, ix, iy) = tmp;
+        }
+        for (long ix = nint((0.5 * sss) / dx); ix <= ixmax; ++ix) {
+            const double tmp = SmoothStep(c, (double)ix * dx - 0.5 * sss, ss * 0.5, N * dx);
+            for (int iy = 0; iy < c->ny; ++iy) F2(ms, ix, iy) = tmp;
+        }
+        for (long ix = 0; ix <= ixmax; ++ix)
+            for (int iy = 0; iy < c->ny; ++iy)
+                if (F2(c->mask, ix, iy) * c->P.eps > 0.0) F2(ms, ix, iy) = F2(ms, ix, iy) * (1.0 - F2(c->mask, ix, iy) * c->P.eps);
+    } else if (isp == 3) {
+        const double ss = sss - N * dx;
+        for (int ix = 0; ix < c->nx; ++ix)
+            for (int iy = 0; iy < c->ny; ++iy) {
+                const double t1 = SmoothStep(c, (double)ix * dx, ss, N * dx), t2 = SmoothStep(c, xl - (double)ix * dx, ss, N * dx);
+                const double t3 = SmoothStep(c, (double)iy * dy, ss, N * dy), t4 = SmoothStep(c, yl - (double)iy * dy, ss, N * dy);
+                F2(ms, ix, iy) = std::min(t1 + t2 + t3 + t4, 1.0);
+            }
+    } else if (isp == 22) {
+        const long ixmin = nint(sss / dx), iymin = nint(sss / dy), ixmax = nint((xl - sss) / dx), iymax = nint((yl - sss) / dy);
+        for (int ix = 0; ix < c->nx; ++ix)
+            for (int iy = 0; iy < c->ny; ++iy) {
+                const bool hole = ix >= ixmin && ix <= ixmax && iy >= iymin && iy <= iymax;
+                F2(ms, ix, iy) = (hole || F2(c->mask, ix, iy) > 0.0) ? 0.0 : 1.0;
+            }
+    }
+    for (double& v : ms) v = v / c->P.eps_sponge;
 }
 
 /* ------------------------------------------------------------------------------
@@ -664,13 +798,13 @@ static void cal_nlk(orc_ctx* c, double time, double& dt1, double* nlk, const dou
     const double u_max = std::sqrt(m);
     dt1 = c->P.cfl * std::min(dx, dy) / u_max;
     if (u_max < 1.e-10) dt1 = 1.e-2;
-    if (c->P.iBeam > 0) dt1 = std::min(0.9 * c->P.eps, dt1);
+    if (c->P.iBeam > 0 || c->P.iWalls > 0 || c->P.iCylinder > 0) dt1 = std::min(0.9 * c->P.eps, dt1);
     if (c->P.dt_fixed > 0.0) dt1 = std::min(c->P.dt_fixed, dt1);
     if ((c->P.time_end - time) < dt1) dt1 = c->P.time_end - time;
     c->sc.u_max = u_max;
     c->sc.mean_ux = su / (double)NN;
     c->sc.mean_uy = sv / (double)NN;
-    if (c->P.iBeam > 0) {
+    if (c->P.iBeam > 0 || c->P.iWalls > 0 || c->P.iCylinder > 0 || c->P.iSponge == 22) {
 #pragma omp parallel for schedule(static)
         for (size_t k = 0; k < NN; ++k) {
             pen1[k] = -c->mask[k] * (u[k] - c->maskvx[k]);
@@ -687,6 +821,16 @@ static void cal_nlk(orc_ctx* c, double time, double& dt1, double* nlk, const dou
     }
 #pragma omp parallel for schedule(static)
     for (size_t k = 0; k < NN; ++k) nlk[k] = nlk[k] + (pen2[k] - pen1[k]);
+    const int isp = c->P.iSponge;
+    if ((isp > 0 && isp < 4) || isp == 22) {  /* :142-160, the vorticity sponge */
+        std::vector<double> penvortk(NN);
+        cofitxy(c, vortk, work2.data());
+#pragma omp parallel for schedule(static)
+        for (size_t k = 0; k < NN; ++k) work2[k] = c->mask_sponge[k] * work2[k];
+        coftxy(c, work2.data(), penvortk.data());
+#pragma omp parallel for schedule(static)
+        for (size_t k = 0; k < NN; ++k) nlk[k] = nlk[k] - penvortk[k];
+    }
 }
 
 static void cal_energy(orc_ctx* c, double time, double dt1, const double* vor, const double* u, const double* pen) {  /* :222-263 */
@@ -716,13 +860,20 @@ static void cal_drag(orc_ctx* c, double time, double dt1, const double* pen) {  
     Beam& b = c->beam;
     double alpha, alpha_t, alpha_tt, LE[6];
     mouvement(c, time, alpha, alpha_t, alpha_tt, LE, b);
-    const double r_cylinder = 0.0, tb = c->P.t_beam;
+    const double r_cylinder = c->P.R_cylinder, tb = c->P.t_beam;
     double ymax = *std::max_element(b.y.begin(), b.y.end()), ymin = *std::min_element(b.y.begin(), b.y.end());
     double xmax = *std::max_element(b.x.begin(), b.x.end()), xmin = *std::min_element(b.x.begin(), b.x.end());
     long iymax = (long)((std::max(ymax + 1.5 * tb, LE[1] + 2.0 * r_cylinder)) / dy);
     long iymin = (long)((std::min(ymin - 1.5 * tb, LE[1] - 2.0 * r_cylinder)) / dy);
     long ixmin = (long)(std::min((LE[0] - std::max(2.5 * r_cylinder, 1.5 * tb)), (xmin - 1.5 * tb)) / dx);
     long ixmax = (long)((xmax + 1.5 * tb) / dx);
+    if (c->P.iWalls > 0) {  /* :546-552, the window stays off the walls */
+        const double h_star = c->P.h_channel + c->P.N_smooth * dy;
+        if (ixmin < 0) ixmin = 0;
+        if (ixmax > c->nx - 1) ixmax = c->nx - 1;
+        if (iymin < nint(h_star / dy) + 2) iymin = nint(h_star / dy) + 2;
+        if (iymax > nint((c->P.yl - h_star) / dy) - 2) iymax = nint((c->P.yl - h_star) / dy) - 2;
+    }
     if (ixmin < 0) ixmin = 0;
     if (ixmax > c->nx - 1) ixmax = c->nx - 1;
     if (iymin < 0) iymin = 0;
@@ -1554,7 +1705,8 @@ int orc_create(const fsibe_params* p, orc_ctx** out) {
     if (c->P.newton_tol <= 0.0) c->P.newton_tol = 1.0e-7;
     if (c->P.newton_maxit <= 0) c->P.newton_maxit = 50;
     const size_t NN = (size_t)c->nx * c->ny;
-    for (auto* v : {&c->dealiase, &c->mask, &c->maskvx, &c->maskvy, &c->vor_mean, &c->press}) v->assign(NN, 0.0);
+    for (auto* v : {&c->dealiase, &c->mask, &c->maskvx, &c->maskvy, &c->vor_mean, &c->press, &c->mask_sponge, &c->mask_frame})
+        v->assign(NN, 0.0);
     for (int q = 0; q < 2; ++q) { c->vortk[q].assign(NN, 0.0); c->nlk[q].assign(NN, 0.0); c->workvis[q].assign(NN, 0.0); }
     c->u.assign(2 * NN, 0.0);
     c->ft.assign((size_t)(c->nx / 2) * c->ny, cplx{0, 0});
@@ -1602,10 +1754,11 @@ int orc_init_fields(orc_ctx* c, const double* vort) {  /* time_step.f90:29-113 w
     c->n1 = 1; c->n0 = 0;
     coftxy(c, vort, c->vortk[0].data());
     std::vector<double> stream(NN);
-    c->U_mean_true = 1.0;
+    c->U_mean_true = (c->P.iWalls == 1) ? 1.0 - 2.0 * c->P.h_channel / c->P.yl : 1.0;  /* time_step.f90:95-100 */
     cal_velocity(c, 0.0, c->vortk[0].data(), c->u.data(), stream.data());
     int st = create_mask(c, c->time);
     if (st) return st;
+    create_sponge_mask(c);
     c->initialized = true;
     c->startup_done = false;
     std::memset(&c->sc, 0, sizeof(c->sc));
@@ -1963,9 +2116,10 @@ int orc_read_backup(orc_ctx* c, const char* path) {
     c->dt0 = dt1;
     c->n1 = n1;
     c->n0 = 1 - n1;
-    c->U_mean_true = 1.0;
+    c->U_mean_true = (c->P.iWalls == 1) ? 1.0 - 2.0 * c->P.h_channel / c->P.yl : 1.0;
     const int st = create_mask(c, c->time);
     if (st) return st;
+    create_sponge_mask(c);
     c->initialized = true;
     c->startup_done = true;
     std::memset(&c->sc, 0, sizeof(c->sc));

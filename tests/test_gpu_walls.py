@@ -1,0 +1,76 @@
+"""Channel walls, the leading-edge cylinder and the sponges on the GPU against the oracle.
+
+The reference's optional solid features (create_mask.f90:21-210 walls and cylinder, 223-470
+the sponges; NavierStokes.f90:142-164 the vorticity-sponge term) at 128^2 with a flexible beam:
+the mask and its velocity field after the start-up, then 40 steps of the coupled run.  The FP64
+form must match the oracle within 1e-10 (relative L2) in the mask, the vorticity, the beam's
+deflection and the drag/lift series; the FP32-compensated form within 1e-5."""
+import numpy as np
+import pytest
+
+from conftest import rel, seeded_vorticity
+from fsibe_2d_gb300 import make_params, FSIBE_FP32C
+
+pytestmark = pytest.mark.gpu
+
+N, NS, STEPS = 128, 32, 40
+
+CASES = {
+    "walls": dict(iWalls=1, h_channel=0.3),
+    "cylinder": dict(iCylinder=1, R_cylinder=0.1),
+    "walls+cylinder": dict(iWalls=1, h_channel=0.3, iCylinder=1, R_cylinder=0.1),
+    "sponge1": dict(iSponge=1, SpongeSize=0.5, eps_sponge=1e-2),
+    "sponge2": dict(iSponge=2, SpongeSize=0.5, eps_sponge=1e-2),
+    "sponge3": dict(iSponge=3, SpongeSize=0.3, eps_sponge=1e-2),
+    "sponge22": dict(iSponge=22, SpongeSize=0.3, eps_sponge=1e-2),
+    "walls+sponge4": dict(iWalls=1, h_channel=0.3, iSponge=4, SpongeSize=0.5),
+}
+
+
+def _run_pair(oracle, precision, kw):
+    import fsibe_2d_gb300 as F
+    p = make_params(nx=N, ny=N, ns=NS, dt=1e-3, precision=precision, **kw)
+    g, o = F.Run(p), oracle.OracleRun(make_params(nx=N, ny=N, ns=NS, dt=1e-3, **kw))
+    w = seeded_vorticity(N, seed=7)
+    g.init_fields(w); o.init_fields(w)
+    return g, o
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_features_fp64_match_the_oracle(oracle, name):
+    g, o = _run_pair(oracle, 0, CASES[name])
+    mg, mo = g.mask(), o.mask()
+    for a, b in zip(mg, mo):                              # mask, us(:,:,1), us(:,:,2)
+        assert np.abs(a - b).max() <= 1e-10 * max(1.0, np.abs(b).max()), name
+    rg, ro = g.time_step(STEPS), o.time_step(STEPS)
+    assert g.scalars().status == 0 and o.scalars().status == 0
+    err = {"vorticity": rel(g.vort(), o.vort()), "deflection": rel(g.beam()[0][1], o.beam()[0][1]),
+           "drag": rel(rg[:, 10], ro[:, 10]), "lift": rel(rg[:, 11], ro[:, 11])}
+    print(name, "FP64 against the oracle after", STEPS, "steps:", err)
+    assert max(err.values()) < 1e-10, (name, err)
+    g.close(); o.close()
+
+
+@pytest.mark.parametrize("name", ["walls+cylinder", "sponge22", "walls+sponge4", "sponge1"])
+def test_features_fp32c_match_the_oracle(oracle, name):
+    g, o = _run_pair(oracle, FSIBE_FP32C, CASES[name])
+    rg, ro = g.time_step(STEPS), o.time_step(STEPS)
+    assert g.scalars().status == 0
+    err = {"vorticity": rel(g.vort(), o.vort()), "deflection": rel(g.beam()[0][1], o.beam()[0][1]),
+           "drag": rel(rg[:, 10], ro[:, 10])}
+    print(name, "FP32C against the oracle after", STEPS, "steps:", err)
+    assert max(err.values()) < 1e-5, (name, err)
+    g.close(); o.close()
+
+
+def test_feature_parameters_are_checked():
+    import fsibe_2d_gb300 as F
+    from fsibe_2d_gb300._binding import FsibeError
+    from fsibe_2d_gb300._abi import FSIBE_ERR_PARAM, FSIBE_ERR_UNSUPPORTED
+    for kw, code in ((dict(iSponge=10, SpongeSize=0.5), FSIBE_ERR_UNSUPPORTED),   # the penalised-
+                     (dict(iSponge=5, SpongeSize=0.5), FSIBE_ERR_PARAM),          # field sponge
+                     (dict(iSponge=1, SpongeSize=0.0), FSIBE_ERR_PARAM),
+                     (dict(iWalls=2), FSIBE_ERR_PARAM)):
+        with pytest.raises(FsibeError) as ex:
+            F.Run(make_params(nx=64, ny=64, ns=16, **kw))
+        assert ex.value.status == code, (kw, ex.value.status)
