@@ -262,6 +262,8 @@ def gpu_arm(args):
             "algorithmic_bytes_per_launch": ab, "avg_launch_ms": round(top_ms, 5)}
     flops = measure_gemm_peaks(dev)
     cpu = cpu_baseline_sample() if rank == 0 else None
+    if cpu is not None and os.environ.get("FSIBE_CPU_CONFIGS", "1") != "0":
+        cpu["configs_median_of_3"] = cpu_baseline_configs()
     if rank == 0:
         line = {
             "metric": METRIC, "value": round(val32, 2), "unit": "Mcell-steps/s", "n_gpus": world, "steps": args.steps,
@@ -447,13 +449,15 @@ def kernel_times(run, nsteps):
     return {out[i].name.decode(): out[i].ms_total / nsteps for i in range(n.value)}
 
 
-def oracle_steps(nsteps, threads):
+def oracle_steps(nsteps, threads, p=None, w=None):
+    """Wall time of nsteps AB2 steps of the oracle (after the start-up step), default the
+    headline workload."""
     sys.path.insert(0, os.path.join(HERE, "oracle"))
     import pyoracle
     from fsibe_2d_gb300 import FSIBE_FP64
     used = pyoracle.set_threads(threads)
-    r = pyoracle.OracleRun(params(FSIBE_FP64))
-    r.init_fields(seeded_vorticity(NX))
+    r = pyoracle.OracleRun(p if p is not None else params(FSIBE_FP64))
+    r.init_fields(w if w is not None else seeded_vorticity(NX))
     r.time_step(1)  # start-up step outside the timing
     t0 = time.perf_counter()
     r.time_step(nsteps)
@@ -468,6 +472,34 @@ def cpu_baseline_sample():
     dt, used = oracle_steps(n, threads)
     return {"value": round(NX * NY * n / dt / 1e6, 3), "unit": "Mcell-steps/s", "cores": used, "kind": "port",
             "sample": f"{n} FP64 AB2 steps of the same 1024^2 workload (after the start-up step), oracle/ C++ OpenMP"}
+
+
+# The benchmark table's single-run workloads for the CPU samples: (name, make_params keywords,
+# seed field (n, K, seed), AB2 steps a sample)
+CPU_CONFIGS = (
+    ("C1 256^2 plain FP64", dict(nx=256, ny=256, ns=64, Re=100.0, dt=2e-4), (256, 8, 0), 60),
+    ("C2 1024^2 precision form", dict(nx=NX, ny=NY, ns=NS, Re=RE, dt=DT), (NX, 8, 0), 8),
+    ("C5 4096^2 large run", dict(nx=4096, ny=4096, ns=1024, xl=8.0, yl=8.0, Re=2000.0, dt=1e-5, EI=0.05,
+                                 mu=2.0, eps=1e-4, x0=2.0, y0=4.0), (4096, 32, 2), 2),
+)
+
+
+def cpu_baseline_configs(repeats=3):
+    """The oracle's throughput on the host cores at C1, C2 and C5: the median of `repeats`
+    samples each (a bounded sample: a few seconds of CPU work per configuration)."""
+    from fsibe_2d_gb300 import make_params, FSIBE_FP64
+    threads = os.cpu_count() or 1
+    out = {}
+    for name, kw, (n, K, seed), steps in CPU_CONFIGS:
+        p = make_params(precision=FSIBE_FP64, **kw)
+        w = seeded_vorticity(n, K=K, seed=seed)
+        vals, used = [], 1
+        for _ in range(repeats):
+            dt, used = oracle_steps(steps, threads, p, w)
+            vals.append(kw["nx"] * kw["ny"] * steps / dt / 1e6)
+        out[name] = {"value": round(statistics.median(vals), 3), "unit": "Mcell-steps/s", "samples": [round(v, 3) for v in vals],
+                     "steps_per_sample": steps, "cores": used}
+    return out
 
 
 def reference_arm(args):

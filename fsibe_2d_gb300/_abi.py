@@ -92,7 +92,8 @@ def make_params(nx=256, ny=256, ns=64, xl=4.0, yl=4.0, Re=100.0, eps=1.0e-3, dt=
                 angle_beam=0.0, iFLUSI=1, iViscous=1, iSaveBeam=3, iSharpTrailing=0,
                 time_method_solid=FSIBE_BDF2, theta_inf=0.0, iMeanVelocity=3, idealis=1,
                 t_release=0.0, tau=0.0, grav=0.0, sigma=0.0, iImpulse=0, iMotion=0, iBeam=1,
-                iWalls=0, h_channel=0.0, iCylinder=0, R_cylinder=0.0, iSponge=0, SpongeSize=0.0, eps_sponge=1.0):
+                iWalls=0, h_channel=0.0, iCylinder=0, R_cylinder=0.0, iSponge=0, SpongeSize=0.0, eps_sponge=1.0,
+                T_fullspeed=0.0):
     """Parameters in the reference's units (params.f90): nu = 1/Re, t_beam is the HALF
     thickness = thickness_cells/2 * dx, eps is the penalization parameter, eta = EI,
     mue = density ratio."""
@@ -107,7 +108,7 @@ def make_params(nx=256, ny=256, ns=64, xl=4.0, yl=4.0, Re=100.0, eps=1.0e-3, dt=
     p.iImpulse, p.time_method_solid = iImpulse, time_method_solid
     p.iFLUSI, p.iMotion, p.iViscous, p.iSaveBeam = iFLUSI, iMotion, iViscous, iSaveBeam
     p.iBeam, p.iSharpTrailing, p.iMeanVelocity, p.idealis = iBeam, iSharpTrailing, iMeanVelocity, idealis
-    p.T_fullspeed, p.theta_inf = 0.0, theta_inf
+    p.T_fullspeed, p.theta_inf = T_fullspeed, theta_inf
     p.x0, p.y0, p.length = x0, y0, length
     p.t_beam = 0.5 * thickness_cells * xl / nx
     p.N_smooth = N_smooth

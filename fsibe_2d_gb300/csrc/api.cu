@@ -873,13 +873,16 @@ static int sponge_mask(fsibe_ctx* c) {
     return FSIBE_OK;
 }
 
-static int create_mask(fsibe_ctx* c) {
+// until_full: the step's redraw for the velocity sponge or the frame of a run whose beam does
+// not move; the kernels keep the previous mask from T_fullspeed on (time_step.f90:187)
+static int create_mask(fsibe_ctx* c, bool until_full = false) {
     if (c->P.iBeam <= 0) {
         const size_t bytes = (c->fp32 ? 4 : 8) * (size_t)c->g.nx * c->g.ny;
         for (int q : {PH_MASK, PH_MVX, PH_MVY}) CK(c, cudaMemsetAsync(c->phys[q], 0, bytes, c->stream));
         return FSIBE_OK;
     }
-    const MaskArgs m = mask_args(c);
+    MaskArgs m = mask_args(c);
+    m.until_full = until_full ? 1 : 0;
     prof_begin(c, "mask_prep");
     launch_mask_prep(m, c->gerf, c->stream, c->pdl);
     prof_end(c);
@@ -988,7 +991,10 @@ static int advance(fsibe_ctx* c) {
 static int step_body(fsibe_ctx* c, int explicit_step) {
     const fsibe_params& P = c->P;
     int st;
-    const bool mask = P.iFLUSI == 1 || P.iMotion > 0;
+    // time_step.f90:187: the mask is drawn every step for a moving beam, and while the mean flow
+    // accelerates for the velocity sponge (iSponge = 4) and the frame (22)
+    const bool moving = P.iFLUSI == 1 || P.iMotion > 0;
+    const bool mask = moving || P.iSponge >= 4;
     const bool forces = P.iFLUSI == 1 || P.iSaveBeam > 0;
     // with a mask formed in the step, the advection part of the nonlinear term runs on the
     // second side stream beside the mask kernels; the forces' interpolation geometry, which
@@ -1007,7 +1013,7 @@ static int step_body(fsibe_ctx* c, int explicit_step) {
         forces_geo(c, c->side2);
         CK(c, cudaEventRecord(c->ev_geo, c->side2));
     }
-    if (mask) { st = create_mask(c); if (st) return st; }
+    if (mask) { st = create_mask(c, !moving); if (st) return st; }
     st = fluid_step(c, explicit_step, split, forces);
     if (st) return st;
     if (forces) { st = get_forces(c, true); if (st) return st; }
@@ -1768,6 +1774,8 @@ int fsibe_surface_integral(fsibe_ctx* c, double time, double* out) {
     if (!c || !out) return FSIBE_ERR_PARAM;
     if (!c->initialized) { c->err = "surface_integral before init_fields"; return FSIBE_ERR_STATE; }
     if (c->P.iViscous != 1 || c->P.iBeam <= 0) { c->err = "BeamSurfaceIntegral needs iViscous = 1 and a beam"; return FSIBE_ERR_PARAM; }
+    // BeamForces.f90:331-336: no surface integral with the leading-edge cylinder
+    if (c->P.iCylinder == 1) { c->err = "BeamSurfaceIntegral is not computed with a cylinder at the leading edge"; return FSIBE_ERR_UNSUPPORTED; }
     double dxi, dyi;
     const ForceArgs f = force_args(c, dxi, dyi);
     SurfArgs s;
@@ -1782,7 +1790,9 @@ int fsibe_surface_integral(fsibe_ctx* c, double time, double* out) {
     launch_surface_integral(f, s, dxi, dyi, time, c->stream);
     CKL(c);
     CK(c, cudaMemcpyAsync(out, s.out, 8 * 11, cudaMemcpyDeviceToHost, c->stream));
-    return read_status(c);
+    const int st = read_status(c);
+    if (c->P.iWalls > 0) out[1] = out[2] = 0.0;  // with walls the file's drag and lift are 0 (BeamForces.f90:494-502)
+    return st;
 }
 
 // ---- runtime backup (save_fields.f90:109-152, init_fields.f90:44-100) ------------------
@@ -2099,7 +2109,7 @@ int fsibe_launches_per_step(fsibe_ctx* c, int* n) {
     if (P.iViscous == 1 && c->stress_split) k += 1;  // k_stress_x
     if (P.iFLUSI == 1 || P.iSaveBeam > 0) k += 2 + 2;  // press_y, press_fin, forces geometry, forces
     // mask prep + raster, and nl_x split into its advection and penalization parts
-    if ((P.iFLUSI == 1 || P.iMotion > 0) && P.iBeam > 0) k += c->nl_split ? 3 : 2;
+    if ((P.iFLUSI == 1 || P.iMotion > 0 || P.iSponge >= 4) && P.iBeam > 0) k += c->nl_split ? 3 : 2;
     if (P.iFLUSI == 1) k += 2;  // beam predictor + beam
     if (P.iFLUSI == 1 && c->beam_cl) k -= 1;  // the cluster beam kernel ends the step itself
     *n = k;

@@ -34,6 +34,7 @@ __device__ __forceinline__ void clip_box(int* bx, int nx, int ny) {
 // its union with the previous step's box and resets the accumulator.
 __global__ void __launch_bounds__(128) k_mask_prep(MaskArgs a, double gerf) {
     pdl_wait();     // the previous kernel of the stream has completed
+    if (a.until_full && a.S->time >= a.T_fullspeed) return;
     __shared__ double ang2[32];
     __shared__ int hbox[32][4];
     __shared__ int wbox[4][4];
@@ -408,6 +409,7 @@ __device__ __forceinline__ void mask_finish(const MaskArgs& a, double gerf, int 
 template <typename R>
 __global__ void __launch_bounds__(32 * MASK_WARPS) k_mask_raster(MaskArgs a, double gerf) {
     pdl_wait();     // the previous kernel of the stream has completed
+    if (a.until_full && a.S->time >= a.T_fullspeed) return;
     constexpr bool F32 = sizeof(R) == 4;
     using T = R;  // the fold's arithmetic: FP32 in the FP32 form, FP64 in the FP64 form
     __shared__ Prim sp[MASK_WARPS][32];

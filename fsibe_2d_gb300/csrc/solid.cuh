@@ -14,6 +14,8 @@ struct Prim {
 
 struct MaskArgs {
     DevScalars* S;
+    int until_full;  // 1: keep the previous mask once the time reaches T_fullspeed (the step's
+                     // redraw for the velocity sponge and the frame, time_step.f90:187)
     int nx, ny, ns, sharp_trailing, sharp;
     double dx, dy, ds, t_beam, N_smooth, eps, pi, angle_deg;
     const double *x, *y, *vx, *vy, *th;

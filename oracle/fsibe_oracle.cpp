@@ -1797,7 +1797,7 @@ int orc_step(orc_ctx* c) {  /* time_step.f90:120-162 (startup) or :178-228 */
     const fsibe_params& P = c->P;
     int st = FSIBE_OK;
     if (!c->startup_done) {
-        if (P.iFLUSI == 1 || P.iMotion > 0) { st = create_mask(c, c->time); if (st) return st; }
+        if (P.iFLUSI == 1 || P.iMotion > 0 || (P.iSponge >= 4 && c->time < P.T_fullspeed)) { st = create_mask(c, c->time); if (st) return st; }
         EvolveFluidExplicit(c);
         if (P.iFLUSI == 1 || P.iSaveBeam > 0) { st = GetForces(c, c->time); if (st) return st; }
         if (P.iFLUSI == 1) {
@@ -1809,7 +1809,7 @@ int orc_step(orc_ctx* c) {  /* time_step.f90:120-162 (startup) or :178-228 */
         return st;
     }
     c->dt0 = c->dt1;
-    if (P.iFLUSI == 1 || P.iMotion > 0) { st = create_mask(c, c->time); if (st) return st; }
+    if (P.iFLUSI == 1 || P.iMotion > 0 || (P.iSponge >= 4 && c->time < P.T_fullspeed)) { st = create_mask(c, c->time); if (st) return st; }
     EvolveFluidAB2(c);
     if (P.iFLUSI == 1 || P.iSaveBeam > 0) { st = GetForces(c, c->time); if (st) return st; }
     if (P.iFLUSI == 1) {
@@ -1939,6 +1939,8 @@ int orc_surface_integral(orc_ctx* c, double time, double* out) {
     if (!c || !out) return FSIBE_ERR_PARAM;
     if (!c->initialized) return fail(c, FSIBE_ERR_STATE, "surface_integral before init_fields");
     if (c->P.iViscous != 1 || c->P.iBeam <= 0) return fail(c, FSIBE_ERR_PARAM, "BeamSurfaceIntegral needs iViscous = 1 and a beam");
+    // BeamForces.f90:331-336: no surface integral with the leading-edge cylinder
+    if (c->P.iCylinder == 1) return fail(c, FSIBE_ERR_UNSUPPORTED, "BeamSurfaceIntegral is not computed with a cylinder at the leading edge");
     const size_t NN = (size_t)c->nx * c->ny;
     const int ns = c->ns, nc = 128;
     const Beam& b = c->beam;
@@ -2006,8 +2008,8 @@ int orc_surface_integral(orc_ctx* c, double time, double* out) {
         lift += c->mask[k] * (u2[k] - c->maskvy[k]);
     }
     out[0] = time;
-    out[1] = drag * dx * dy;
-    out[2] = lift * dx * dy;
+    out[1] = c->P.iWalls > 0 ? 0.0 : drag * dx * dy;  // with walls the file's drag and lift are 0 (:494-502)
+    out[2] = c->P.iWalls > 0 ? 0.0 : lift * dx * dy;
     out[3] = Ft[0] + Fn[0] + Fp[0];
     out[4] = Ft[1] + Fn[1] + Fp[1];
     out[5] = Ft[0]; out[6] = Fn[0]; out[7] = Fp[0];

@@ -24,6 +24,11 @@ CASES = {
     "sponge3": dict(iSponge=3, SpongeSize=0.3, eps_sponge=1e-2),
     "sponge22": dict(iSponge=22, SpongeSize=0.3, eps_sponge=1e-2),
     "walls+sponge4": dict(iWalls=1, h_channel=0.3, iSponge=4, SpongeSize=0.5),
+    # a fixed beam in an accelerating flow: the mask is redrawn until T_fullspeed, then kept
+    "sponge4-accelerating": dict(iWalls=1, h_channel=0.3, iSponge=4, SpongeSize=0.5, iFLUSI=0,
+                                 iMeanVelocity=1, T_fullspeed=0.02),
+    "sponge22-accelerating": dict(iSponge=22, SpongeSize=0.3, eps_sponge=1e-2, iFLUSI=0,
+                                  iMeanVelocity=2, T_fullspeed=0.02),
 }
 
 
@@ -74,3 +79,24 @@ def test_feature_parameters_are_checked():
         with pytest.raises(FsibeError) as ex:
             F.Run(make_params(nx=64, ny=64, ns=16, **kw))
         assert ex.value.status == code, (kw, ex.value.status)
+
+
+def test_surface_integral_with_walls_and_cylinder(oracle):
+    """BeamForces.f90:331-336, 494-502: no surface integral with the leading-edge cylinder; with
+    walls the file's penalization drag and lift columns are zero, the contour columns remain."""
+    import ctypes as C
+    from fsibe_2d_gb300._abi import FSIBE_ERR_UNSUPPORTED
+    from fsibe_2d_gb300._binding import _ptr
+    g, o = _run_pair(oracle, 0, CASES["walls"])
+    g.time_step(5); o.time_step(5)
+    t = g.scalars().time
+    sg, so = g.BeamSurfaceIntegral(t), o.BeamSurfaceIntegral(t)
+    assert sg[1] == 0.0 and sg[2] == 0.0 and so[1] == 0.0 and so[2] == 0.0
+    scale = np.abs(so[3:]).max()
+    assert np.abs(np.asarray(sg[3:]) - np.asarray(so[3:])).max() <= 1e-10 * scale
+    g.close(); o.close()
+    g, o = _run_pair(oracle, 0, CASES["cylinder"])
+    out = np.zeros(11)
+    for r in (g, o):
+        assert getattr(r._lib, r._prefix + "surface_integral")(r._ctx, C.c_double(0.0), _ptr(out)) == FSIBE_ERR_UNSUPPORTED
+    g.close(); o.close()

@@ -44,3 +44,23 @@ def test_cylinder_and_sponges_change_the_flow(oracle):
         assert np.abs(rows[:, 10] - ref[:, 10]).max() > 1e-8, kw        # the drag moved
         o.close()
     base.close()
+
+
+def test_fixed_beam_mask_is_redrawn_only_while_the_flow_accelerates(oracle):
+    """time_step.f90:124,187: with the velocity sponge and a beam that does not move, the mask
+    follows the mean flow until T_fullspeed and is kept from then on."""
+    n = 64
+    p = make_params(nx=n, ny=n, ns=16, dt=1e-3, iWalls=1, h_channel=0.3, iSponge=4, SpongeSize=0.5,
+                    iFLUSI=0, iMeanVelocity=1, T_fullspeed=0.01)
+    o = oracle.OracleRun(p)
+    o.init_fields(seeded_vorticity(n, seed=2))
+    o.time_step(3)
+    early = o.mask()[1].copy()
+    o.time_step(12)
+    t_late = o.scalars().time
+    late = o.mask()[1].copy()
+    o.time_step(10)
+    assert t_late > p.T_fullspeed
+    assert np.abs(late - early).max() > 1e-3          # the sponge's inflow profile grew
+    assert np.array_equal(o.mask()[1], late)            # and is frozen after T_fullspeed
+    o.close()
