@@ -19,7 +19,7 @@ FSIBE_ERR_BRAKE = 10
 FSIBE_ERR_STATE = 11
 
 # values per step of fsibe_run_records (include/fsibe.h)
-FSIBE_RECORD_COLS = 36
+FSIBE_RECORD_COLS = 46
 
 STATUS_NAMES = {
     0: "FSIBE_OK", 1: "FSIBE_ERR_PARAM", 2: "FSIBE_ERR_CUDA", 3: "FSIBE_ERR_NAN",

@@ -75,6 +75,7 @@ def declare(lib, prefix, ctx_type=C.c_void_p):
     f("get_scalars", P, C.POINTER(FsibeScalars))
     f("write_backup", P, C.c_char_p)
     f("surface_integral", P, C.c_double, _dp)
+    f("pressure_snapshot", P, C.c_double, _dp)
     f("read_backup", P, C.c_char_p)
     f("last_error", P, res=C.c_char_p)
 
@@ -204,6 +205,15 @@ class Run:
         out = np.zeros(11)
         self._call("surface_integral", C.c_double(time), _ptr(out))
         return out
+
+    def ComputePressureSnapshot(self, time):
+        """NavierStokes.f90:598-665: the static pressure of the current vorticity with the
+        velocity at `time` and the current mask, (ny, nx); the state is not changed."""
+        out = np.empty(self.shape)
+        self._call("pressure_snapshot", C.c_double(time), _ptr(out))
+        return out
+
+    pressure_snapshot = ComputePressureSnapshot
 
     def MakeRuntimeBackup(self, path):
         """Write the state between two steps as runtime_backup<n>.in (save_fields.f90:109-152):

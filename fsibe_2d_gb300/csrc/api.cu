@@ -42,6 +42,7 @@ int beam_pre_smem_setup(int ns);
 size_t beam_pred_doubles(int ns);
 void beam_d1d_table(double ds, double* out);
 void launch_init_beam(const BeamArgs& b, cudaStream_t st);
+void launch_move_beam(const BeamArgs& b, cudaStream_t st);
 int beam_smem_setup(int ns);
 int beam_cluster_setup(int ns, int want, size_t* smem_out);
 void launch_beam_cluster(const BeamArgs& b, int R, size_t smem, cudaStream_t st, bool pdl);
@@ -71,6 +72,7 @@ struct StepArgs {
     double cfl, dx, dy, eps, dt_fixed, time_end, theta_inf, T_fullspeed, U_mean_true, pi, nu;
     double x0, y0, t_beam, NN, scalex, scaley;
     double cos_ti, sin_ti;  // cos and sin of theta_inf, from the host
+    MotionArgs mo;          // the leading edge's motion (the drag window follows it)
     double rdx, rdy, rNN;   // RN(1/dx), RN(1/dy), RN(1/NN)
     const double *bx, *by;
     double* etab;
@@ -174,10 +176,11 @@ __global__ void __launch_bounds__(256) k_step_begin(StepArgs a) {
         S->mean_uy = div_cr(sv, a.NN, a.rNN);
     } else if (threadIdx.x == 96 || threadIdx.x == 128) {
         const double r_cyl = a.r_cyl, tb = a.t_beam;
+        const Motion mo = motion_at(a.mo, S->time);  // LeadingEdge (NavierStokes.f90:532)
         if (threadIdx.x == 96) {
             int ixmin = 0, ixmax = a.nx - 1;
             if (a.iBeam > 0) {
-                ixmin = (int)div_cr(fmin((a.x0 - fmax(2.5 * r_cyl, 1.5 * tb)), (bminx - 1.5 * tb)), a.dx, a.rdx);
+                ixmin = (int)div_cr(fmin((mo.le[0] - fmax(2.5 * r_cyl, 1.5 * tb)), (bminx - 1.5 * tb)), a.dx, a.rdx);
                 ixmax = (int)div_cr((bmaxx + 1.5 * tb), a.dx, a.rdx);
                 if (ixmin < 0) ixmin = 0;
                 if (ixmax > a.nx - 1) ixmax = a.nx - 1;
@@ -186,8 +189,8 @@ __global__ void __launch_bounds__(256) k_step_begin(StepArgs a) {
         } else {
             int iymin = 0, iymax = a.ny - 1;
             if (a.iBeam > 0) {
-                iymax = (int)div_cr((fmax(bmaxy + 1.5 * tb, a.y0 + 2.0 * r_cyl)), a.dy, a.rdy);
-                iymin = (int)div_cr((fmin(bminy - 1.5 * tb, a.y0 - 2.0 * r_cyl)), a.dy, a.rdy);
+                iymax = (int)div_cr((fmax(bmaxy + 1.5 * tb, mo.le[1] + 2.0 * r_cyl)), a.dy, a.rdy);
+                iymin = (int)div_cr((fmin(bminy - 1.5 * tb, mo.le[1] - 2.0 * r_cyl)), a.dy, a.rdy);
                 if (iymin < 0) iymin = 0;
                 if (iymax > a.ny - 1) iymax = a.ny - 1;
                 // the rows of the cells j of the forces' stress points (within soff of the
@@ -442,6 +445,7 @@ struct fsibe_ctx {
     unsigned* counter = nullptr;
     double* fterm = nullptr;
     double* rows = nullptr;
+    void* snap = nullptr;   // ComputePressureSnapshot's workspace (5 fields and 2 spectra of R), on first use
     int rows_cap = 0;
     double* etab = nullptr;       // integrating-factor tables (hx + ny/2 + 1)
     float2* etabf = nullptr;
@@ -456,6 +460,9 @@ struct fsibe_ctx {
     double* bg = nullptr;         // walls + cylinder, unscaled
     double* frame = nullptr;      // iSponge = 22
     void* spg = nullptr;          // vorticity sponge / eps_sponge (R)
+    void* s10 = nullptr;          // iSponge = 10: the integral term of the x penalization (R)
+    void* s10_dudx = nullptr;     // and du/dx in physical space (R)
+    int s10_ixmin = 0, s10_ixmax = -1;
     int* rect_full = nullptr;     // rows of the whole grid, for the penalization part of cal_nlk
     int beam_smem = 0;      // beam workspace parts in shared memory (bit mask, see k_beam)
     int beam_pre_smem = 0;  // the same for the predictor kernel
@@ -565,6 +572,7 @@ static KArgs<R> kargs(fsibe_ctx* c) {
     a.dcut = c->dcut;
     a.kcut = c->kcut;
     a.spg = reinterpret_cast<const R*>(c->spg);
+    a.s10 = reinterpret_cast<const R*>(c->s10);
     a.viscous = c->P.iViscous == 1;
     a.pressure_on = (c->P.iFLUSI == 1 || c->P.iSaveBeam > 0);
     a.penalize = c->P.iBeam > 0;
@@ -613,6 +621,20 @@ static void launch_xv(fsibe_ctx* c, void (*k)(KArgs<R>), const typename SizeKern
     c->launches++;
 }
 
+// The leading edge's motion (mouvement.f90:5-200): the case, its fixed position and angle (the
+// angle's cosine and sine from the host), and the phase of the single beam (init_beam.f90:48).
+static MotionArgs motion_args(const fsibe_ctx* c) {
+    MotionArgs m;
+    m.iMotion = c->P.iMotion;
+    m.x0 = c->P.x0; m.y0 = c->P.y0;
+    m.pi = c->g.pi;
+    m.alpha0 = c->P.angle_beam * c->g.pi / 180.0;
+    m.cos0 = std::cos(m.alpha0);
+    m.sin0 = std::sin(m.alpha0);
+    m.phase = 0.0;
+    return m;
+}
+
 static StepArgs step_args(fsibe_ctx* c, int explicit_step, int nblk) {
     StepArgs a;
     std::memset(&a, 0, sizeof(a));
@@ -638,6 +660,7 @@ static StepArgs step_args(fsibe_ctx* c, int explicit_step, int nblk) {
     a.nu = c->P.nu;
     a.x0 = c->P.x0;
     a.y0 = c->P.y0;
+    a.mo = motion_args(c);
     a.t_beam = c->P.t_beam;
     a.NN = (double)c->P.nx * (double)c->P.ny;
     a.rdx = 1.0 / a.dx;
@@ -673,10 +696,8 @@ static BeamArgs beam_args(fsibe_ctx* c) {
     b.ds = c->g.ds; b.eta = c->P.eta; b.mue = c->P.mue; b.sigma = c->P.sigma;
     b.t_release = c->P.t_release; b.tau = c->P.tau; b.tol = c->P.newton_tol; b.pi = c->g.pi;
     b.x0 = c->P.x0; b.y0 = c->P.y0; b.angle_deg = c->P.angle_beam;
+    b.mo = motion_args(c);
     {
-        const double alpha = c->P.angle_beam * c->g.pi / 180.0;
-        b.cos_a = std::cos(alpha);
-        b.sin_a = std::sin(alpha);
         const double ds = b.ds, eta = b.eta, ds2 = ds * ds, ds3 = ds * ds * ds, ds4 = (ds * ds) * (ds * ds);
         b.k.ids = 1.0 / ds;
         b.k.i2ds = 1.0 / (2.0 * ds);
@@ -722,6 +743,9 @@ static int beam_predict(fsibe_ctx* c) {
 template <typename R>
 static int x_blocks(fsibe_ctx* c) { return c->g.ny / kx_of<R>(c).x_rows; }
 
+template <typename R>
+static int sponge10_term(fsibe_ctx* c);  // the sharp outflow sponge's integral (below)
+
 // The advection part of cal_nlk (NavierStokes.f90:88-132 without the penalization) on the
 // second side stream, forked from the main stream at the start of the step: it reads the
 // state the previous step left (u, v, the vorticity's derivatives) and no mask, so it runs
@@ -763,15 +787,20 @@ static int fluid_step_t(fsibe_ctx* c, int explicit_step, bool adv_forked = false
     CK(c, cudaEventRecord(c->ev_sb, c->side));
     c->launches++;
     if (c->P.iFLUSI == 1) { const int st = beam_predict(c); if (st) return st; }
+    if (c->s10) { const int st = sponge10_term<R>(c); if (st) return st; }
     if (adv_forked) {
         // the advection part ran beside the mask kernels: add the penalization on the rows
         // of the mask's box
         CK(c, cudaStreamWaitEvent(c->stream, c->ev_adv, 0));
         KArgs<R> p = a;
-        p.rect = c->full_mask ? c->rect_full : c->rect;  // walls and sponges: every row is penalized
-        launch_xv<R>(c, KX.xv[c->xv_nl].nl_pen, KX.xv[c->xv_nl], 2, p, "nl_pen");
+        // walls, sponges and the outflow sponge's integral: every row is penalized
+        p.rect = (c->full_mask || c->s10) ? c->rect_full : c->rect;
+        if (c->s10) launch_xv<R>(c, KX.xv[1].nl_pen_s10, KX.xv[1], 2, p, "nl_pen");
+        else launch_xv<R>(c, KX.xv[c->xv_nl].nl_pen, KX.xv[c->xv_nl], 2, p, "nl_pen");
     } else if (c->spg) {
         launch_xv<R>(c, KX.xv[1].nl_x_spg, KX.xv[1], 3, a, "nl_x");  // the default tile carries the sponge
+    } else if (c->s10) {
+        launch_xv<R>(c, KX.xv[1].nl_x_s10, KX.xv[1], 3, a, "nl_x");
     } else {
         launch_xv<R>(c, KX.xv[c->xv_nl].nl_x, KX.xv[c->xv_nl], 3, a, "nl_x");
     }
@@ -825,7 +854,8 @@ static MaskArgs mask_args(fsibe_ctx* c) {
     m.angle_deg = c->P.angle_beam;
     m.x = c->beam[B_X]; m.y = c->beam[B_Y]; m.vx = c->beam[B_VX]; m.vy = c->beam[B_VY]; m.th = c->beam[B_TH];
     m.prims = c->prims; m.nprims = c->nprims; m.rect = c->rect; m.nsm = c->nsm;
-    m.rdx = 1.0 / m.dx; m.rdy = 1.0 / m.dy; m.rpi = 1.0 / m.pi; m.angle_rad = m.angle_deg * m.pi / 180.0;
+    m.rdx = 1.0 / m.dx; m.rdy = 1.0 / m.dy; m.rpi = 1.0 / m.pi;
+    m.mo = motion_args(c);
     m.mask = c->phys[PH_MASK]; m.mvx = c->phys[PH_MVX]; m.mvy = c->phys[PH_MVY];
     m.full = c->full_mask ? 1 : 0;
     m.bg = c->bg;
@@ -912,7 +942,7 @@ static ForceArgs force_args(fsibe_ctx* c, double& dxi, double& dyi) {
     dyi = (c->P.yl - c->g.dy) / (double)(c->P.ny - 1);
     f.geo = c->fgeo;
     f.gij = c->fgij;
-    f.alpha = f.angle_deg * f.pi / 180.0;
+    f.mo = motion_args(c);
     f.rdxi = 1.0 / dxi;
     f.rdyi = 1.0 / dyi;
     return f;
@@ -950,6 +980,7 @@ static AdvArgs adv_args(fsibe_ctx* c) {
     a.th = c->beam[B_TH]; a.thd = c->beam[B_THD];
     a.p_old = c->beam[B_PO]; a.p_new = c->beam[B_PN]; a.tau_old = c->beam[B_TO]; a.tau_new = c->beam[B_TN];
     a.rows = c->rows;
+    a.mo = motion_args(c);
     return a;
 }
 
@@ -1019,6 +1050,12 @@ static int step_body(fsibe_ctx* c, int explicit_step) {
     if (forces) { st = get_forces(c, true); if (st) return st; }
     bool advanced = false;
     if (P.iFLUSI == 1) { st = solid_step(c, true, &advanced); if (st) return st; }
+    else if (P.iMotion > 0) {
+        // the prescribed motion alone: integrate_position(time) (time_step.f90:211-216)
+        launch_move_beam(beam_args(c), c->stream);
+        c->launches++;
+        CKL(c);
+    }
     return advanced ? FSIBE_OK : advance(c);
 }
 
@@ -1131,6 +1168,26 @@ static int inv_x(fsibe_ctx* c) {
     return FSIBE_OK;
 }
 
+// The sharp outflow sponge (iSponge = 10, NavierStokes.f90:103-122): du/dx of the state's
+// velocity (i kx i ky psi from the vorticity spectrum, inverse y into the free spectrum SP_0,
+// inverse x), then its integral along each row (k_sponge10), which the penalization part of
+// k_nl_x adds to its x component.
+template <typename R>
+static int sponge10_term(fsibe_ctx* c) {
+    int st;
+    if ((st = inv_y<R>(c, c->spec[SP_W], c->spec[SP_0], OP_UX))) return st;
+    KArgs<R> a = kargs<R>(c);
+    a.spec0 = reinterpret_cast<C2<R>*>(c->spec[SP_0]);
+    a.phys0 = reinterpret_cast<R*>(c->s10_dudx);
+    launch_x<R>(c, kx_of<R>(c).xinv, kx_of<R>(c).x_smem1, a);
+    k_sponge10<R><<<(c->g.ny + 127) / 128, 128, 0, c->stream>>>(reinterpret_cast<const R*>(c->s10_dudx),
+                                                               reinterpret_cast<R*>(c->s10), c->g.nx, c->g.ny,
+                                                               c->s10_ixmin, c->s10_ixmax, c->g.dx, 1.0 / c->P.eps_sponge);
+    c->launches += 3;
+    CKL(c);
+    return FSIBE_OK;
+}
+
 // cal_velocity at time (init) : u, v and the velocity statistics for the first cal_nlk
 template <typename R>
 static int init_velocity(fsibe_ctx* c) {
@@ -1163,6 +1220,93 @@ static double host_mean(const fsibe_params& P, double t, bool x) {
 // =====================================================================================
 // C ABI
 // =====================================================================================
+// ---- ComputePressureSnapshot (NavierStokes.f90:598-665) ------------------------------
+// u, v at `time` (the state's velocity plus the mean flow of the time), the penalization and
+// the nonlinear term's divergence as two fields, forward 2-D, the Poisson divide, inverse 2-D,
+// p = q - |u|^2 / 2.  Outside the time step; the state is not changed.
+template <typename R>
+__global__ void k_snap_terms(R* u, R* v, const R* w, const R* mask, const R* mvx, const R* mvy, R* px, R* py,
+                             size_t n, double U, double V) {
+    for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x) {
+        const R uk = u[k] + (R)U, vk = -v[k] + (R)V, wk = w[k], m = mask[k];  // v = -d psi/dx + V
+        u[k] = uk;
+        v[k] = vk;
+        px[k] = m * (uk - mvx[k]) + (-wk * vk);  // the penalization (positive here) and -omega v
+        py[k] = m * (vk - mvy[k]) + wk * uk;     // and +omega u
+    }
+}
+// q^ = (i kx P^x + i ky P^y) / k^2 (zero at k = 0 and ky = ny/2), in place of P^x
+template <typename R>
+__global__ void k_snap_poisson(C2<R>* sx, const C2<R>* sy, Geometry g) {
+    const size_t n = (size_t)g.hx * g.ny;
+    for (size_t o = blockIdx.x * (size_t)blockDim.x + threadIdx.x; o < n; o += (size_t)gridDim.x * blockDim.x) {
+        const int kx = (int)(o / g.ny), ky = (int)(o % g.ny);
+        const int ks = signed_k(ky, g.ny);
+        const R kxs = (R)((double)kx * g.kxs), kys = (R)ks * (R)g.kys;
+        const C2<R> Q = cadd<R>(cimul<R>(sx[o], kxs), cimul<R>(sy[o], kys));
+        const R k2 = (R)(kx * kx) * (R)g.scalex + (R)(ks * ks) * (R)g.scaley;
+        C2<R> q;
+        if ((kx == 0 && ky == 0) || ky == g.ny / 2) q = mk<R>(0, 0);
+        else if constexpr (kIsF32<R>) q = cscale<R>(Q, (R)1 / k2);
+        else q = mk<R>(Q.x / k2, Q.y / k2);
+        sx[o] = q;
+    }
+}
+template <typename R>
+__global__ void k_snap_fin(const R* q, const R* u, const R* v, double* out, size_t n) {
+    for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x)
+        out[k] = (double)(q[k] - (R)0.5 * (u[k] * u[k] + v[k] * v[k]));
+}
+
+template <typename R>
+static int pressure_snapshot_t(fsibe_ctx* c, double time, double* host_out) {
+    const size_t NN = (size_t)c->g.nx * c->g.ny, rs = sizeof(R);
+    if (!c->snap) CK(c, cudaMalloc(&c->snap, 7 * rs * NN));
+    R* f = reinterpret_cast<R*>(c->snap);
+    R *pu = f, *pv = f + NN, *pw = f + 2 * NN, *px = f + 3 * NN, *py = f + 4 * NN;
+    C2<R>* s0 = reinterpret_cast<C2<R>*>(f + 5 * NN);
+    C2<R>* s1 = reinterpret_cast<C2<R>*>(f + 6 * NN);
+    C2<R>* T = reinterpret_cast<C2<R>*>(c->spec[SP_0]);
+    const SizeKernels<R>& KX = kx_of<R>(c);
+    const SizeKernels<R>& KY = ky_of<R>(c);
+    auto to_phys = [&](const void* spec, int op, R* out) {
+        int st = inv_y<R>(c, spec, T, op);
+        if (st) return st;
+        KArgs<R> a = kargs<R>(c);
+        a.spec0 = T;
+        a.phys0 = out;
+        launch_x<R>(c, KX.xinv, KX.x_smem1, a);
+        return FSIBE_OK;
+    };
+    auto to_spec = [&](R* in, C2<R>* out) {
+        KArgs<R> a = kargs<R>(c);
+        a.phys0 = in;
+        a.spec0 = T;
+        a.spec1 = out;
+        launch_x<R>(c, KX.xfwd, KX.x_smem1, a);
+        launch_y<R>(c, KY.yfwd, KY.y_smem1, a);
+    };
+    int st;
+    if ((st = to_phys(c->spec[SP_W], OP_U, pu))) return st;
+    if ((st = to_phys(c->spec[SP_W], OP_V, pv))) return st;
+    if ((st = to_phys(c->spec[SP_W], OP_ID, pw))) return st;
+    const double U = c->U_mean_true * host_mean(c->P, time, true), V = c->U_mean_true * host_mean(c->P, time, false);
+    const int grid = 4 * c->nsm;
+    k_snap_terms<R><<<grid, 256, 0, c->stream>>>(pu, pv, pw, reinterpret_cast<const R*>(c->phys[PH_MASK]),
+                                                 reinterpret_cast<const R*>(c->phys[PH_MVX]),
+                                                 reinterpret_cast<const R*>(c->phys[PH_MVY]), px, py, NN, U, V);
+    to_spec(px, s0);
+    to_spec(py, s1);
+    k_snap_poisson<R><<<grid, 256, 0, c->stream>>>(s0, s1, c->g);
+    if ((st = to_phys(s0, OP_ID, pw))) return st;
+    double* out = c->dscratch;  // nx ny doubles
+    k_snap_fin<R><<<grid, 256, 0, c->stream>>>(pw, pu, pv, out, NN);
+    CKL(c);
+    CK(c, cudaMemcpyAsync(host_out, out, 8 * NN, cudaMemcpyDeviceToHost, c->stream));
+    CK(c, cudaStreamSynchronize(c->stream));
+    return FSIBE_OK;
+}
+
 extern "C" {
 
 const char* fsibe_strerror(int s) {
@@ -1255,7 +1399,7 @@ int fsibe_destroy(fsibe_ctx* c) {
     for (double* p : c->beam) if (p) cudaFree(p);
     void* others[] = {c->twX, c->twR, c->twY, c->S, c->red, c->oo, c->ws, c->pred, c->minv, c->minv_rse, c->d1d, c->fgeo, c->fgij, c->prims, c->nprims,
                       c->rect, c->counter, c->fterm, c->rows, c->dscratch, c->dscratch2, c->etab, c->etabf, c->dcut,
-                      c->bg, c->frame, c->spg, c->rect_full};
+                      c->bg, c->frame, c->spg, c->s10, c->s10_dudx, c->rect_full, c->snap};
     for (void* p : others) if (p) cudaFree(p);
     for (cudaEvent_t e : c->pool) cudaEventDestroy(e);
     if (c->ev0) cudaEventDestroy(c->ev0);
@@ -1282,22 +1426,30 @@ int fsibe_create(const fsibe_params* p, fsibe_ctx** out) {
     if (!pow2_ok(p->nx) || !pow2_ok(p->ny)) { g_err = "nx, ny must be powers of two in [32, 4096]"; return FSIBE_ERR_UNSUPPORTED; }
     if (p->iBeam > 0 && p->ns < 8) { g_err = "ns must be >= 8"; return FSIBE_ERR_PARAM; }
     if (p->iBeam > 1) { g_err = "one beam per run"; return FSIBE_ERR_UNSUPPORTED; }
-    if (p->iMotion != 0) { g_err = "only the clamped leading edge (iMotion = 0) is implemented"; return FSIBE_ERR_UNSUPPORTED; }
+    {
+        // mouvement.f90:17-155: fixed (0), heaving (2), flapping (3), impulsive translation (4),
+        // heaving with a soft start (201-213, 300-350), the Paraz heaving cases (401-413: the
+        // reference indexes its 13 periods with iMotion - 400, so 400 and 414-450 read outside them)
+        const int m = p->iMotion;
+        const bool ok = m == 0 || m == 2 || m == 3 || m == 4 || (m >= 201 && m <= 213) || (m >= 300 && m <= 350) ||
+                        (m >= 401 && m <= 413);
+        if (!ok) { g_err = "iMotion in {0, 2, 3, 4, 201-213, 300-350, 401-413} (mouvement.f90)"; return FSIBE_ERR_PARAM; }
+        if (m != 0 && p->iBeam != 1) { g_err = "a prescribed motion needs the beam (iBeam = 1)"; return FSIBE_ERR_UNSUPPORTED; }
+    }
     if (p->precision != FSIBE_FP64 && p->precision != FSIBE_FP32C) { g_err = "precision"; return FSIBE_ERR_PARAM; }
     if (p->iMeanVelocity == 11) { g_err = "iMeanVelocity = 11 is not implemented"; return FSIBE_ERR_UNSUPPORTED; }
     {
         const int isp = p->iSponge;
         if (p->iWalls < 0 || p->iWalls > 1 || p->iCylinder < 0 || p->iCylinder > 1 ||
             !(isp == 0 || isp == 1 || isp == 2 || isp == 3 || isp == 4 || isp == 22 || isp == 10)) {
-            g_err = "iWalls, iCylinder in {0, 1}; iSponge in {0, 1, 2, 3, 4, 22}"; return FSIBE_ERR_PARAM;
+            g_err = "iWalls, iCylinder in {0, 1}; iSponge in {0, 1, 2, 3, 4, 10, 22}"; return FSIBE_ERR_PARAM;
         }
-        if (isp == 10) { g_err = "iSponge = 10 (the sharp outflow test sponge) is not implemented"; return FSIBE_ERR_UNSUPPORTED; }
         if ((p->iWalls || p->iCylinder || isp) && p->iBeam != 1) {
             g_err = "walls, the cylinder and the sponges run with the beam (iBeam = 1)"; return FSIBE_ERR_UNSUPPORTED;
         }
         if (isp > 0 && isp != 4 && !(p->eps_sponge >= 1.0e-9)) { g_err = "eps_sponge (params.f90:185-188)"; return FSIBE_ERR_PARAM; }
-        if ((isp == 4 || isp == 22 || isp == 1 || isp == 2 || isp == 3) && !(p->SpongeSize > 0.0)) {
-            g_err = "SpongeSize must be positive"; return FSIBE_ERR_PARAM;
+        if (isp > 0 && !(p->SpongeSize > 0.0 && p->SpongeSize < std::min(p->xl, p->yl))) {
+            g_err = "SpongeSize must lie in (0, min(xl, yl))"; return FSIBE_ERR_PARAM;
         }
         if (p->iWalls == 1 && p->theta_inf != 0.0) { g_err = "walls need theta_inf = 0 (params.f90:199-203)"; return FSIBE_ERR_PARAM; }
     }
@@ -1305,6 +1457,11 @@ int fsibe_create(const fsibe_params* p, fsibe_ctx** out) {
         p->time_method_solid != FSIBE_EULER_IMPLICIT) { g_err = "time_method_solid"; return FSIBE_ERR_PARAM; }
     fsibe_ctx* c = new fsibe_ctx();
     c->P = *p;
+    if (c->P.iMotion >= 401 && c->P.iMotion <= 413) {
+        // mouvement.f90:102-104: these cases set the forces' soft start-up to one period
+        static const double periods[13] = {0.51, 0.34, 0.25, 0.20, 0.17, 0.14, 0.13, 0.11, 0.10, 0.09, 0.08, 0.08, 0.07};
+        c->P.tau = periods[c->P.iMotion - 401];
+    }
     if (c->P.newton_tol <= 0.0) c->P.newton_tol = 1.0e-7;
     if (c->P.newton_maxit <= 0) c->P.newton_maxit = 50;
     c->fp32 = p->precision == FSIBE_FP32C;
@@ -1413,7 +1570,15 @@ int fsibe_create(const fsibe_params* p, fsibe_ctx** out) {
         if (p->iWalls > 0 || p->iCylinder > 0) ALLOC(c->bg, 8 * NN);
         if (isp == 22) ALLOC(c->frame, 8 * NN);
         if (isp == 1 || isp == 2 || isp == 3 || isp == 22) ALLOC(c->spg, rs * NN);
-        if (c->full_mask) {
+        if (isp == 10) {
+            // NavierStokes.f90:107-108: ixmin = nint((xl - SpongeSize)/dx), ixmax = nx - 1 - 15
+            c->s10_ixmin = (int)std::lround((p->xl - p->SpongeSize) / c->g.dx);
+            c->s10_ixmax = p->nx - 1 - 15;
+            ALLOC(c->s10, rs * NN);
+            ALLOC(c->s10_dudx, rs * NN);
+            cudaMemset(c->s10, 0, rs * NN);
+        }
+        if (c->full_mask || isp == 10) {
             ALLOC(c->rect_full, 16);
             const int rf[4] = {0, p->nx - 1, 0, p->ny - 1};
             cudaMemcpy(c->rect_full, rf, sizeof(rf), cudaMemcpyHostToDevice);
@@ -1581,6 +1746,7 @@ static int init_state(fsibe_ctx* c, const double* vort, bool keep_mask) {
 }
 
 static int read_status(fsibe_ctx* c);
+static int set_time(fsibe_ctx* c, double time);
 
 int fsibe_init_fields(fsibe_ctx* c, const double* vort) {
     if (!c || !vort) return FSIBE_ERR_PARAM;
@@ -1589,8 +1755,9 @@ int fsibe_init_fields(fsibe_ctx* c, const double* vort) {
 
 int fsibe_create_mask(fsibe_ctx* c, double time) {
     if (!c) return FSIBE_ERR_PARAM;
-    (void)time;  // mouvement case 0 does not depend on time
-    int st = create_mask(c);
+    int st = set_time(c, time);  // the motion and the mean flow of the time
+    if (st) return st;
+    st = create_mask(c);
     if (st) return st;
     return read_status(c);  // a beam point below the domain: FSIBE_ERR_MASK_OOB
 }
@@ -1770,6 +1937,12 @@ int fsibe_download_beam(fsibe_ctx* c, double* beam, double* po, double* pn, doub
 // ---- BeamSurfaceIntegral (BeamForces.f90:306-509) ---------------------------------------
 // From the stresses and pressure of the last fluid step and the current beam: between
 // GetForces and the solid step this is the reference's call (:129).
+int fsibe_pressure_snapshot(fsibe_ctx* c, double time, double* press) {
+    if (!c || !press) return FSIBE_ERR_PARAM;
+    if (!c->initialized) { c->err = "pressure snapshot before init_fields"; return FSIBE_ERR_STATE; }
+    return c->fp32 ? pressure_snapshot_t<float>(c, time, press) : pressure_snapshot_t<double>(c, time, press);
+}
+
 int fsibe_surface_integral(fsibe_ctx* c, double time, double* out) {
     if (!c || !out) return FSIBE_ERR_PARAM;
     if (!c->initialized) { c->err = "surface_integral before init_fields"; return FSIBE_ERR_STATE; }
@@ -2110,7 +2283,9 @@ int fsibe_launches_per_step(fsibe_ctx* c, int* n) {
     if (P.iFLUSI == 1 || P.iSaveBeam > 0) k += 2 + 2;  // press_y, press_fin, forces geometry, forces
     // mask prep + raster, and nl_x split into its advection and penalization parts
     if ((P.iFLUSI == 1 || P.iMotion > 0 || P.iSponge >= 4) && P.iBeam > 0) k += c->nl_split ? 3 : 2;
+    if (c->s10) k += 3;  // du/dx (inverse y, inverse x) and the outflow sponge's integral
     if (P.iFLUSI == 1) k += 2;  // beam predictor + beam
+    if (P.iFLUSI == 0 && P.iMotion > 0) k += 1;  // k_move_beam
     if (P.iFLUSI == 1 && c->beam_cl) k -= 1;  // the cluster beam kernel ends the step itself
     *n = k;
     return FSIBE_OK;
@@ -2425,7 +2600,7 @@ static int adj_check(fsibe_ctx* c, int nsteps, int avg_from) {
         c->err = "the adjoint needs a prescribed rigid mask (iFLUSI = 0, iMotion = 0, iBeam > 0)";
         return FSIBE_ERR_UNSUPPORTED;
     }
-    if (c->spg || c->full_mask) { c->err = "the adjoint runs without walls, cylinder and sponges"; return FSIBE_ERR_UNSUPPORTED; }
+    if (c->spg || c->full_mask || c->s10) { c->err = "the adjoint runs without walls, cylinder and sponges"; return FSIBE_ERR_UNSUPPORTED; }
     if (nsteps < 1 || avg_from < 1 || avg_from > nsteps) { c->err = "need 1 <= avg_from <= nsteps"; return FSIBE_ERR_PARAM; }
     return FSIBE_OK;
 }

@@ -101,7 +101,8 @@ __global__ void __launch_bounds__(256) k_beam_pre(BeamArgs b) {
     const int method = S->method;
     PH(0);
     // EE1 predictor: th1 = theta, td1 = theta_dot -> RHS
-    int st = rhs_beameqn(b, w, w.th1, w.td1, b.p_old, w.T, b.tau_old, grav);
+    const Motion mo = motion_at(b.mo, time);  // mouvement(time) of EE1 and the CN right-hand side
+    int st = rhs_beameqn(b, w, w.th1, w.td1, b.p_old, w.T, b.tau_old, grav, mo);
     PH(1);
     if (st) { if (threadIdx.x == 0) set_status(S, FSIBE_ERR_SINGULAR); return; }
     double* px = b.pred;
@@ -130,7 +131,7 @@ __global__ void __launch_bounds__(256) k_beam_pre(BeamArgs b) {
     if (method == FSIBE_CRANK_NICHOLSON) {
         for (int i = threadIdx.x; i < ns; i += blockDim.x) { w.th1[i] = b.th[i]; w.old_rhs[i] = b.thd[i]; }
         __syncthreads();
-        st = rhs_beameqn(b, w, w.th1, w.old_rhs, b.p_old, w.T, b.tau_old, grav);
+        st = rhs_beameqn(b, w, w.th1, w.old_rhs, b.p_old, w.T, b.tau_old, grav, mo);
         if (st) { if (threadIdx.x == 0) set_status(S, FSIBE_ERR_SINGULAR); return; }
         for (int i = threadIdx.x; i < ns; i += blockDim.x) p_old_rhs[i] = w.old_rhs[i];
     }
@@ -180,6 +181,7 @@ __global__ void __launch_bounds__(256) k_beam(BeamArgs b) {
     __syncthreads();
 
     bool released = time > b.t_release;
+    const Motion mo = motion_at(b.mo, time + dt);  // mouvement(time + dt) of the new level
     if (released) {
         const double dt_old = S->dt_old;
         const int method = S->method;
@@ -193,10 +195,10 @@ __global__ void __launch_bounds__(256) k_beam(BeamArgs b) {
             const double* g5 = b.pred + n + ns;
             const double* T = g5 + ns;
             const double ds2 = ds * ds;
-            const double K2 = b.p_new[0] + mue * (0.0 * b.cos_a - 0.0 * b.sin_a + grav * b.cos_a);
+            const double K2 = b.p_new[0] + mue * (mo.le[5] * mo.ca - mo.le[4] * mo.sa + grav * mo.ca);
             const double C2v = 2.0 * ds * K2 - T[0] * g5[1] + (eta / ds2) * (10.0 * g5[0] - 12.0 * g5[1] + 6.0 * g5[2] - g5[3]);
             w.x[xi_th(-1)] = C2v / ((3.0 * eta / ds2) - T[0]);
-            const double K1 = mue * (0.0 * b.cos_a + 0.0 * b.sin_a + grav * b.sin_a) - b.tau_new[0];
+            const double K1 = mue * (mo.le[4] * mo.ca + mo.le[5] * mo.sa + grav * mo.sa) - b.tau_new[0];
             const double th_ss0 = (2.0 * g5[0] - 5.0 * g5[1] + 4.0 * g5[2] - 1.0 * g5[3]) * b.k.ids2;
             const double th_s0 = (-1.5 * g5[0] + 2.0 * g5[1] - 0.5 * g5[2]) * b.k.ids;
             const double T_s0 = -eta * th_ss0 * th_s0 + K1;
@@ -206,12 +208,12 @@ __global__ void __launch_bounds__(256) k_beam(BeamArgs b) {
         // the step's Newton constants, evaluated once (divisions are long FP64 sequences here)
         __shared__ NewtonCtx cs;
         if (threadIdx.x == 0) {
-            cs.time = time; cs.dt = dt; cs.dt_old = dt_old; cs.alpha_t = 0.0; cs.alpha_tt = 0.0; cs.grav = grav;
+            cs.time = time; cs.dt = dt; cs.dt_old = dt_old; cs.alpha_t = mo.alpha_t; cs.alpha_tt = mo.alpha_tt; cs.grav = grav;
             solid_coeffs(method, dt, dt_old, cs.C1, cs.C2, cs.C3, cs.C4);
             cs.D = cs.C1 / dt;
             newton_consts(cs, b);
-            cs.K1 = mue * (0.0 * b.cos_a + 0.0 * b.sin_a + grav * b.sin_a) - b.tau_new[0];
-            cs.K2 = b.p_new[0] + mue * (0.0 * b.cos_a - 0.0 * b.sin_a + grav * b.cos_a);
+            cs.K1 = mue * (mo.le[4] * mo.ca + mo.le[5] * mo.sa + grav * mo.sa) - b.tau_new[0];
+            cs.K2 = b.p_new[0] + mue * (mo.le[5] * mo.ca - mo.le[4] * mo.sa + grav * mo.ca);
         }
         __syncthreads();
         const NewtonCtx& c = cs;
@@ -405,16 +407,16 @@ __global__ void __launch_bounds__(256) k_beam(BeamArgs b) {
     // out of shared memory at ns = 1024.)
     {
         __shared__ double esum[6][8];
-        const double ca = b.cos_a, sa = b.sin_a, alpha_t = 0.0, idt = 1.0 / dt;
+        const double ca = mo.ca, sa = mo.sa, alpha_t = mo.alpha_t, idt = 1.0 / dt;
         double sk = 0, sp = 0, se = 0, sax = 0, say = 0, mx = 0;
         for (int i = threadIdx.x; i < ns; i += blockDim.x) {
             const double xrel = w.pre[i], yrel = w.pre[(ns + 8) + i];
             const double vxrel = w.pre[2 * (ns + 8) + i], vyrel = w.pre[3 * (ns + 8) + i];
-            const double yi = b.y0 + yrel * ca + xrel * sa;
-            b.x[i] = b.x0 + xrel * ca - yrel * sa;
+            const double yi = mo.le[1] + yrel * ca + xrel * sa;
+            b.x[i] = mo.le[0] + xrel * ca - yrel * sa;
             b.y[i] = yi;
-            const double vx = 0.0 + ca * (vxrel - alpha_t * yrel) - sa * (vyrel + alpha_t * xrel);
-            const double vy = 0.0 + ca * (vyrel + alpha_t * xrel) + sa * (vxrel - alpha_t * yrel);
+            const double vx = mo.le[2] + ca * (vxrel - alpha_t * yrel) - sa * (vyrel + alpha_t * xrel);
+            const double vy = mo.le[3] + ca * (vyrel + alpha_t * xrel) + sa * (vxrel - alpha_t * yrel);
             b.vx[i] = vx;
             b.vy[i] = vy;
             double ax, ay;
@@ -475,11 +477,34 @@ __global__ void __launch_bounds__(256) k_beam(BeamArgs b) {
         for (int k = 4; k < 24; ++k) S->phase[k] += ph[k];
 }
 
-// Beam start state (init_beam.f90:83-120): straight beam at the leading edge, at rest.
+// integrate_position (integrate_position.f90:14-44) by one thread: the four running sums in the
+// reference's order and the positions and velocities of the motion mo.
+__device__ void integrate_position_seq(const BeamArgs& b, const Motion& mo) {
+    const int ns = b.ns;
+    const double ds = b.ds, ca = mo.ca, sa = mo.sa, alpha_t = mo.alpha_t;
+    double xrel = 0.0, yrel = 0.0, vxrel = 0.0, vyrel = 0.0;
+    for (int s = 0; s < ns; ++s) {
+        if (s > 0) {
+            double sn, cn;
+            sincos(b.th[s - 1], &sn, &cn);
+            const double td = b.thd[s - 1];
+            xrel = xrel + cn * ds;
+            yrel = yrel + sn * ds;
+            vxrel = vxrel - td * sn * ds;
+            vyrel = vyrel + td * cn * ds;
+        }
+        b.x[s] = mo.le[0] + xrel * ca - yrel * sa;
+        b.y[s] = mo.le[1] + yrel * ca + xrel * sa;
+        b.vx[s] = mo.le[2] + ca * (vxrel - alpha_t * yrel) - sa * (vyrel + alpha_t * xrel);
+        b.vy[s] = mo.le[3] + ca * (vyrel + alpha_t * xrel) + sa * (vxrel - alpha_t * yrel);
+    }
+}
+
+// Beam start state (init_beam.f90:83-120): straight beam at the leading edge, at rest relative
+// to it, placed by integrate_position(0).
 __global__ void k_init_beam(BeamArgs b) {
     const int ns = b.ns;
     if (threadIdx.x == 0) b.S->beam_fact = 0;
-    const double ca = b.cos_a, sa = b.sin_a;
     for (int i = threadIdx.x; i < ns; i += blockDim.x) {
         b.th[i] = 0.0; b.thd[i] = 0.0; b.ax[i] = 0.0; b.ay[i] = 0.0;
         b.p_old[i] = 0.0; b.p_new[i] = 0.0; b.tau_old[i] = 0.0; b.tau_new[i] = 0.0;
@@ -487,19 +512,14 @@ __global__ void k_init_beam(BeamArgs b) {
         b.vx[i] = 0.0; b.vy[i] = 0.0;
     }
     __syncthreads();
-    if (threadIdx.x == 0) {
-        double xrel = 0.0, yrel = 0.0;
-        for (int s = 0; s < ns; ++s) {
-            if (s > 0) {
-                xrel = xrel + cos(0.0) * b.ds;
-                yrel = yrel + sin(0.0) * b.ds;
-            }
-            b.x[s] = b.x0 + xrel * ca - yrel * sa;
-            b.y[s] = b.y0 + yrel * ca + xrel * sa;
-            b.vx[s] = 0.0;
-            b.vy[s] = 0.0;
-        }
-    }
+    if (threadIdx.x == 0) integrate_position_seq(b, motion_at(b.mo, 0.0));
+}
+
+// A prescribed motion without the beam solver (iFLUSI = 0, iMotion > 0; time_step.f90:211-216):
+// integrate_position at the step's time.
+__global__ void k_move_beam(BeamArgs b) {
+    pdl_wait();     // the previous kernel of the stream has completed
+    if (threadIdx.x == 0) integrate_position_seq(b, motion_at(b.mo, b.S->time));
 }
 
 // ===================================================================================
@@ -559,5 +579,6 @@ int beam_smem_setup(int ns) {
     return mask;
 }
 void launch_init_beam(const BeamArgs& b, cudaStream_t st) { k_init_beam<<<1, 256, 0, st>>>(b); }
+void launch_move_beam(const BeamArgs& b, cudaStream_t st) { k_move_beam<<<1, 32, 0, st>>>(b); }
 
 }  // namespace fsibe

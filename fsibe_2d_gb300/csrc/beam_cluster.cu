@@ -234,6 +234,7 @@ __global__ void __launch_bounds__(256, 1) k_beam_cl(BeamArgs b) {
     __syncthreads();
 
     const bool released = time > b.t_release;
+    const Motion mo = motion_at(b.mo, time + dt);  // mouvement(time + dt) of the new level
     int iter = 0;
     if (released) {
         const bool have_inv = S->beam_fact != 0;
@@ -257,20 +258,20 @@ __global__ void __launch_bounds__(256, 1) k_beam_cl(BeamArgs b) {
             const double* g5 = b.pred + n + ns;
             const double* T = g5 + ns;
             const double ds2 = ds * ds;
-            const double K2 = b.p_new[0] + mue * (0.0 * b.cos_a - 0.0 * b.sin_a + grav * b.cos_a);
+            const double K2 = b.p_new[0] + mue * (mo.le[5] * mo.ca - mo.le[4] * mo.sa + grav * mo.ca);
             const double C2v = 2.0 * ds * K2 - T[0] * g5[1] + (eta / ds2) * (10.0 * g5[0] - 12.0 * g5[1] + 6.0 * g5[2] - g5[3]);
             x[xi_th(-1)] = div_cr(C2v, K[8], K[9]);  // C2v / (3 eta/ds^2 - T_0), correctly rounded
-            const double K1 = mue * (0.0 * b.cos_a + 0.0 * b.sin_a + grav * b.sin_a) - b.tau_new[0];
+            const double K1 = mue * (mo.le[4] * mo.ca + mo.le[5] * mo.sa + grav * mo.sa) - b.tau_new[0];
             const double th_ss0 = (2.0 * g5[0] - 5.0 * g5[1] + 4.0 * g5[2] - 1.0 * g5[3]) * b.k.ids2;
             const double th_s0 = (-1.5 * g5[0] + 2.0 * g5[1] - 0.5 * g5[2]) * b.k.ids;
             const double T_s0 = -eta * th_ss0 * th_s0 + K1;
             x[xi_T(ns, -1)] = T[1] - 2.0 * ds * T_s0;
         }
         if (tid == 32) {
-            cs.time = time; cs.dt = dt; cs.dt_old = S->dt_old; cs.alpha_t = 0.0; cs.alpha_tt = 0.0; cs.grav = grav;
+            cs.time = time; cs.dt = dt; cs.dt_old = S->dt_old; cs.alpha_t = mo.alpha_t; cs.alpha_tt = mo.alpha_tt; cs.grav = grav;
             newton_consts_pre(cs, b, K);
-            cs.K1 = mue * (0.0 * b.cos_a + 0.0 * b.sin_a + grav * b.sin_a) - b.tau_new[0];
-            cs.K2 = b.p_new[0] + mue * (0.0 * b.cos_a - 0.0 * b.sin_a + grav * b.cos_a);
+            cs.K1 = mue * (mo.le[4] * mo.ca + mo.le[5] * mo.sa + grav * mo.sa) - b.tau_new[0];
+            cs.K2 = b.p_new[0] + mue * (mo.le[5] * mo.ca - mo.le[4] * mo.sa + grav * mo.ca);
         }
         __syncthreads();
         const NewtonCtx& c = cs;
@@ -664,16 +665,16 @@ __global__ void __launch_bounds__(256, 1) k_beam_cl(BeamArgs b) {
         __shared__ double ecol[6][256];
         static_assert(256 >= 32 * 6, "one warp a column");
         const double* pre = pcs + 4 * L;
-        const double ca = b.cos_a, sa = b.sin_a, alpha_t = 0.0, idt = 1.0 / dt;
+        const double ca = mo.ca, sa = mo.sa, alpha_t = mo.alpha_t, idt = 1.0 / dt;
         double sk = 0, sp = 0, se = 0, sax = 0, say = 0, mx = 0;
         for (int i = tid; i < ns; i += nthr) {
             const double xrel = pre[i], yrel = pre[L + i];
             const double vxrel = pre[2 * L + i], vyrel = pre[3 * L + i];
-            const double yi = b.y0 + yrel * ca + xrel * sa;
-            b.x[i] = b.x0 + xrel * ca - yrel * sa;
+            const double yi = mo.le[1] + yrel * ca + xrel * sa;
+            b.x[i] = mo.le[0] + xrel * ca - yrel * sa;
             b.y[i] = yi;
-            const double vx = 0.0 + ca * (vxrel - alpha_t * yrel) - sa * (vyrel + alpha_t * xrel);
-            const double vy = 0.0 + ca * (vyrel + alpha_t * xrel) + sa * (vxrel - alpha_t * yrel);
+            const double vx = mo.le[2] + ca * (vxrel - alpha_t * yrel) - sa * (vyrel + alpha_t * xrel);
+            const double vy = mo.le[3] + ca * (vyrel + alpha_t * xrel) + sa * (vxrel - alpha_t * yrel);
             b.vx[i] = vx;
             b.vy[i] = vy;
             double ax, ay;

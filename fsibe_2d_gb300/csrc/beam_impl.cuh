@@ -362,12 +362,13 @@ __device__ int tri_solve(int n, const double* dl, const double* d, const double*
 }
 
 // Tension (SolidSolver.f90:1000-1081), block-cooperative.
+// mo: the leading edge's motion at the time of the call (mouvement(time))
 __device__ int tension(const BeamArgs& b, BeamWS& w, double* T, double* T_s, const double* th, const double* thd,
-                       const double* p, const double* tau, double grav) {
+                       const double* p, const double* tau, double grav, const Motion& mo) {
     const int ns = b.ns;
     const double ds = b.ds, eta = b.eta, mue = b.mue;
-    const double alpha_t = 0.0;
-    const double LE4 = 0.0, LE5 = 0.0;  // leading-edge accelerations, mouvement case 0
+    const double alpha_t = mo.alpha_t;
+    const double LE4 = mo.le[4], LE5 = mo.le[5];  // leading-edge accelerations
     for (int i = threadIdx.x; i < ns; i += blockDim.x) {
         w.th_s[i] = d1d(w.dtab, th, ns, 1, i);
         w.th_ss[i] = d1d(w.dtab, th, ns, 2, i);
@@ -375,7 +376,7 @@ __device__ int tension(const BeamArgs& b, BeamWS& w, double* T, double* T_s, con
         w.tau_s[i] = d1d(w.dtab, tau, ns, 1, i);
     }
     __syncthreads();
-    const double K1 = mue * (LE4 * b.cos_a + LE5 * b.sin_a + grav * b.sin_a) - tau[0];
+    const double K1 = mue * (LE4 * mo.ca + LE5 * mo.sa + grav * mo.sa) - tau[0];
     const double T_s0 = -eta * w.th_ss[0] * w.th_s[0] + K1;
     const double ds2 = ds * ds;
     for (int i = threadIdx.x; i < ns; i += blockDim.x) {
@@ -404,18 +405,18 @@ __device__ int tension(const BeamArgs& b, BeamWS& w, double* T, double* T_s, con
 
 // RHS_beameqn (SolidSolver.f90:918-994): on return th := theta_dot, thd := theta_ddot.
 __device__ int rhs_beameqn(const BeamArgs& b, BeamWS& w, double* th, double* thd, const double* p, double* T,
-                           const double* tau, double grav) {
+                           const double* tau, double grav, const Motion& mo) {
     const int ns = b.ns;
     const double ds = b.ds, eta = b.eta, mue = b.mue, sigma = b.sigma;
-    const double alpha_tt = 0.0;
-    const double LE4 = 0.0, LE5 = 0.0;
+    const double alpha_tt = mo.alpha_tt;
+    const double LE4 = mo.le[4], LE5 = mo.le[5];
     if (threadIdx.x == 0) { th[0] = 0.0; thd[0] = 0.0; }
     __syncthreads();
-    int st = tension(b, w, T, w.T_s, th, thd, p, tau, grav);
+    int st = tension(b, w, T, w.T_s, th, thd, p, tau, grav, mo);
     if (st) return st;
     const double ds2 = ds * ds;
     if (threadIdx.x == 0) {
-        const double K2 = p[0] + mue * (LE5 * b.cos_a - LE4 * b.sin_a + grav * b.cos_a);
+        const double K2 = p[0] + mue * (LE5 * mo.ca - LE4 * mo.sa + grav * mo.ca);
         const double C2 = 2.0 * ds * K2 - T[0] * th[1] + (eta / ds2) * (10.0 * th[0] - 12.0 * th[1] + 6.0 * th[2] - th[3]);
         w.te[0] = C2 / ((3.0 * eta / ds2) - T[0]);
         const double A1 = th[ns - 3] / 12. - 2. * th[ns - 2] / 3.;

@@ -49,6 +49,7 @@ struct KArgs {
     int stress_split;
     int srows;
     const R* spg;         // the vorticity sponge / eps_sponge (NavierStokes.f90:142-160), or null
+    const R* s10;         // iSponge = 10: the integral added to the x penalization (:103-122), or null
     size_t bstride;       // generic transforms over several fields at once: blockIdx.y selects the
                           // field, bstride complex values (= nx ny / 2) apart in every buffer
 };
@@ -95,7 +96,7 @@ __device__ __forceinline__ void ff_update(float wh, float wl, float d, float Eh,
 }
 
 // Operators the generic inverse-y kernel applies before the transform.
-enum SpecOp { OP_ID = 0, OP_DX = 1, OP_DY = 2, OP_U = 3, OP_V = 4 };
+enum SpecOp { OP_ID = 0, OP_DX = 1, OP_DY = 2, OP_U = 3, OP_V = 4, OP_UX = 5 };  // OP_UX: du/dx
 
 __device__ __forceinline__ int signed_k(int k, int n) { return (k <= n / 2) ? k : k - n; }
 
@@ -292,7 +293,7 @@ __global__ void __launch_bounds__(NY / 8) k_yinv(KArgs<R> a) {
             else if (a.op == OP_DY) o = cimul<R>(s, kys);
             else {
                 C2<R> psi = (kx == 0 && ky == 0) ? mk<R>(0, 0) : cscale<R>(s, (R)(1.0 / k2));
-                o = (a.op == OP_U) ? cimul<R>(psi, kys) : cimul<R>(psi, kxs);
+                o = (a.op == OP_U) ? cimul<R>(psi, kys) : (a.op == OP_V) ? cimul<R>(psi, kxs) : cimul<R>(cimul<R>(psi, kys), kxs);
             }
         }
         if (ky == NY / 2) o = mk<R>(0, 0);
@@ -367,9 +368,9 @@ __global__ void __launch_bounds__(XRows<R, H>::THREADS) k_vel_x(KArgs<R> a) {
 // K2: nonlinear term and penalization in physical space (cal_nlk)
 // ======================================================================================
 // One tile of TR rows from iy0 (the whole kernel's work for one block)
-// SPG: the run has a vorticity sponge (a separate instantiation, so that the plain step keeps
-// its registers)
-template <typename R, int H, int TRV, int PART, bool SPG>
+// SPG: 1 the run has a vorticity sponge, 2 the sharp outflow sponge's integral (separate
+// instantiations, so that the plain step keeps its registers)
+template <typename R, int H, int TRV, int PART, int SPG>
 __device__ __forceinline__ void nl_x_tile(const KArgs<R>& a, const int iy0) {
     using X = XRows<R, H, TRV>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -410,7 +411,7 @@ __device__ __forceinline__ void nl_x_tile(const KArgs<R>& a, const int iy0) {
     // the vorticity sponge: the vorticity itself (x inverse of Tw, the inverse-y transform of the
     // state that k_nl_y left), for the term -F(mask_sponge omega) of cal_nlk
     C2<R> om[1][8];
-    if constexpr (SPG && PART != NL_PENAL) {
+    if constexpr (SPG == 1 && PART != NL_PENAL) {
         const int kin = a.explicit_step ? H : a.kcut;
         load_tileT<R, H, X::TR, X::PL>(bufA, a.Tw, ny, iy0, kin);
         __syncthreads();
@@ -439,7 +440,7 @@ __device__ __forceinline__ void nl_x_tile(const KArgs<R>& a, const int iy0) {
         if (adv) {
             const C2<R> dx = dxy[0][q], dy = dxy[1][q];
             wv[q] = mk<R>(-uu.x * dx.x - vv.x * dy.x, -uu.y * dx.y - vv.y * dy.y);
-            if constexpr (SPG) {
+            if constexpr (SPG == 1) {
                 const C2<R> sg = reinterpret_cast<const C2<R>*>(a.spg)[roff + m], w = om[0][q];
                 wv[q] = mk<R>(wv[q].x - sg.x * w.x, wv[q].y - sg.y * w.y);
             }
@@ -448,6 +449,10 @@ __device__ __forceinline__ void nl_x_tile(const KArgs<R>& a, const int iy0) {
             const C2<R> kk = k2[m], mx = x2[m], my = y2[m];
             pxv[q] = mk<R>(-kk.x * (uu.x - mx.x), -kk.y * (uu.y - mx.y));
             pyv[q] = mk<R>(-kk.x * (vv.x - my.x), -kk.y * (vv.y - my.y));
+            if constexpr (SPG == 2) {
+                const C2<R> si = reinterpret_cast<const C2<R>*>(a.s10)[roff + m];
+                pxv[q] = mk<R>(pxv[q].x + si.x, pxv[q].y + si.y);
+            }
         } else {
             pxv[q] = mk<R>(0, 0);
             pyv[q] = mk<R>(0, 0);
@@ -507,7 +512,7 @@ __device__ __forceinline__ void nl_x_tile(const KArgs<R>& a, const int iy0) {
 template <int MB, int DEF>
 constexpr int xminb() { return MB > 0 ? MB : DEF; }
 
-template <typename R, int H, int TRV, int PART = NL_WHOLE, int MB = 0, bool SPG = false>
+template <typename R, int H, int TRV, int PART = NL_WHOLE, int MB = 0, int SPG = 0>
 __global__ void __launch_bounds__(XRows<R, H, TRV>::THREADS, (xminb<MB, 1>())) k_nl_x(KArgs<R> a) {
     pdl_wait();     // the previous kernel of the stream has completed
     using X = XRows<R, H, TRV>;
@@ -522,6 +527,27 @@ __global__ void __launch_bounds__(XRows<R, H, TRV>::THREADS, (xminb<MB, 1>())) k
         }
     } else {
         nl_x_tile<R, H, TRV, PART, SPG>(a, blockIdx.x * X::TR);
+    }
+}
+
+// The sharp outflow sponge (iSponge = 10, NavierStokes.f90:103-122): per row iy, the term added
+// to the x penalization at ix in [ixmin, ixmax] is the trapezoid integral from ixmin to ix of
+// w = -mask_sponge du/dx, mask_sponge = 1 / eps_sponge there.  One thread a row sums in the
+// reference's order (the running sum adds the same terms as its sum from ixmin for every ix);
+// the rest of the output stays zero.
+template <typename R>
+__global__ void __launch_bounds__(128) k_sponge10(const R* __restrict__ dudx, R* __restrict__ out, int nx, int ny,
+                                                  int ixmin, int ixmax, double dx, double inv_eps) {
+    const int iy = blockIdx.x * blockDim.x + threadIdx.x;
+    if (iy >= ny || ixmin < 0 || ixmax >= nx) return;
+    const R* d = dudx + (size_t)iy * nx;
+    R* o = out + (size_t)iy * nx;
+    double summe = 0.0, wprev = 0.0;
+    for (int ix = ixmin; ix <= ixmax; ++ix) {
+        const double w = -(inv_eps * (double)d[ix]);
+        if (ix > ixmin) summe = summe + 0.5 * (wprev + w) * dx;
+        o[ix] = (R)summe;
+        wprev = w;
     }
 }
 
@@ -1133,8 +1159,10 @@ struct SizeKernels {
         void (*nl_x)(KArgs<R>);
         void (*nl_adv)(KArgs<R>);  // k_nl_x's advection and penalization parts (two buffers)
         void (*nl_pen)(KArgs<R>);
-        void (*nl_x_spg)(KArgs<R>);   // nl_x and its advection part with the vorticity sponge
-        void (*nl_adv_spg)(KArgs<R>); // (the default tile only; null elsewhere)
+        void (*nl_x_spg)(KArgs<R>);   // nl_x and its advection part with the vorticity sponge,
+        void (*nl_adv_spg)(KArgs<R>); // nl_x and its penalization part with the sharp outflow
+        void (*nl_x_s10)(KArgs<R>);   // sponge's integral (the default tile only; null
+        void (*nl_pen_s10)(KArgs<R>); // elsewhere)
         void (*stress_x)(KArgs<R>);  // two buffers
         void (*press_x)(KArgs<R>);
         void (*press_fin)(KArgs<R>);
@@ -1159,12 +1187,16 @@ inline void fill_xvariant(typename SizeKernels<R>::XVariant& v) {
     v.nl_x = k_nl_x<R, H, TR, NL_WHOLE, MB>;
     v.nl_adv = k_nl_x<R, H, TR, NL_ADVECT, MB>;
     v.nl_pen = k_nl_x<R, H, TR, NL_PENAL, MB>;
-    v.nl_x_spg = v.nl_adv_spg = nullptr;
+    v.nl_x_spg = v.nl_adv_spg = v.nl_x_s10 = v.nl_pen_s10 = nullptr;
     if constexpr (SPG) {
-        v.nl_x_spg = k_nl_x<R, H, TR, NL_WHOLE, MB, true>;
-        v.nl_adv_spg = k_nl_x<R, H, TR, NL_ADVECT, MB, true>;
-        cudaFuncSetAttribute(k_nl_x<R, H, TR, NL_WHOLE, MB, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, v.smem3);
-        cudaFuncSetAttribute(k_nl_x<R, H, TR, NL_ADVECT, MB, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * v.smem1);
+        v.nl_x_spg = k_nl_x<R, H, TR, NL_WHOLE, MB, 1>;
+        v.nl_adv_spg = k_nl_x<R, H, TR, NL_ADVECT, MB, 1>;
+        v.nl_x_s10 = k_nl_x<R, H, TR, NL_WHOLE, MB, 2>;
+        v.nl_pen_s10 = k_nl_x<R, H, TR, NL_PENAL, MB, 2>;
+        cudaFuncSetAttribute(k_nl_x<R, H, TR, NL_WHOLE, MB, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, v.smem3);
+        cudaFuncSetAttribute(k_nl_x<R, H, TR, NL_ADVECT, MB, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * v.smem1);
+        cudaFuncSetAttribute(k_nl_x<R, H, TR, NL_WHOLE, MB, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, v.smem3);
+        cudaFuncSetAttribute(k_nl_x<R, H, TR, NL_PENAL, MB, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * v.smem1);
     }
     v.stress_x = k_stress_x<R, H, TR, MB>;
     cudaFuncSetAttribute(k_stress_x<R, H, TR, MB>, cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * v.smem1);

@@ -92,7 +92,7 @@ __global__ void __launch_bounds__(128) k_mask_prep(MaskArgs a, double gerf) {
         }
         if (i == ns && nsharp) {
             const int e = ns - 1;
-            const double al = a.th[e] + a.angle_rad;
+            const double al = a.th[e] + motion_at(a.mo, a.S->time).alpha;  // mouvement(time)
             double sa, ca;
             sincos(al, &sa, &ca);
             const double p1x = a.x[e] - 2.0 * mx * ca, p1y = a.y[e] - 2.0 * mx * sa;
@@ -613,7 +613,7 @@ __global__ void __launch_bounds__(128) k_forces_geo(ForceArgs a, double dxi, dou
     __shared__ double px[4], py[4];
     // the two sincos on two warps (SMSPs)
     if (threadIdx.x == 0 || threadIdx.x == 32) {
-        const double thn = a.th[n] + a.alpha;
+        const double thn = a.th[n] + motion_at(a.mo, a.S->time).alpha;  // mouvement(time)
         double sv, cv;
         if (threadIdx.x == 0) {
             sincos(thn, &sv, &cv);
@@ -917,13 +917,14 @@ __global__ void __launch_bounds__(256) k_surface_integral(ForceArgs a, SurfArgs 
     const double pi = a.pi;
     const double R = a.t_beam + a.N_smooth * fmax(a.dx, a.dy);
     const double dphi = pi / (double)(nc - 1), dL = dphi * R;
+    const double alpha = motion_at(a.mo, time).alpha;  // mouvement(time) (BeamForces.f90:344)
     double F[6] = {0, 0, 0, 0, 0, 0};  // Ft(1), Fn(1), Fp(1), Ft(2), Fn(2), Fp(2)
     bool ok = true;
     for (int p = threadIdx.x; p < npts; p += blockDim.x) {
         double A = 0.0, B = 0.0, P = 0.0;
         if (p < 2 * nc) {
             const int end = p / nc, i = p % nc, node = end == 0 ? ns - 1 : 0;
-            const double beta = a.th[end == 0 ? ns - 1 : 1] + a.alpha;
+            const double beta = a.th[end == 0 ? ns - 1 : 1] + alpha;
             const double phi = (end == 0 ? -(0.5 * pi - beta) : (0.5 * pi + beta)) + (double)i * dphi;
             double sp_, cp_, s2, c2;
             sincos(phi, &sp_, &cp_);
@@ -939,7 +940,7 @@ __global__ void __launch_bounds__(256) k_surface_integral(ForceArgs a, SurfArgs 
         } else {
             const int q = p - 2 * nc, i = q % ns;
             const double sg = q < ns ? 1.0 : -1.0;
-            const double th = a.th[i] + a.alpha;
+            const double th = a.th[i] + alpha;
             double sn_, cs_, s2, c2;
             sincos(th, &sn_, &cs_);
             sincos(2.0 * th, &s2, &c2);

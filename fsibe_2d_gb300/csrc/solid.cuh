@@ -4,6 +4,67 @@
 
 namespace fsibe {
 
+// The leading edge's prescribed motion (mouvement.f90:5-200).  alpha0 = angle_deg pi / 180 and
+// its cosine and sine come from the host; every case but flapping (3) keeps alpha = alpha0.
+struct MotionArgs {
+    int iMotion;
+    double x0, y0, alpha0, cos0, sin0, phase, pi;
+};
+struct Motion {
+    double alpha, alpha_t, alpha_tt, ca, sa;
+    double le[6];  // x, y, vx, vy, ax, ay of the leading edge
+};
+
+__device__ __forceinline__ Motion motion_at(const MotionArgs& m, double time) {
+    Motion o;
+    const double pi = m.pi;
+    const int k = m.iMotion;
+    o.alpha = m.alpha0; o.alpha_t = 0.0; o.alpha_tt = 0.0; o.ca = m.cos0; o.sa = m.sin0;
+    o.le[0] = m.x0; o.le[1] = m.y0;
+    o.le[2] = 0.0; o.le[3] = 0.0; o.le[4] = 0.0; o.le[5] = 0.0;
+    if ((k >= 201 && k <= 213) || (k >= 300 && k <= 350)) {
+        // heaving with the soft start k(t) = -20 t^7 + 70 t^6 - 84 t^5 + 35 t^4 over t <= 1
+        const double periods[13] = {1.0, 1.09, 1.20, 1.29, 1.33, 1.4, 1.5, 1.71, 2.0, 2.4, 3.0, 4.0, 1.62};
+        const double y_max = 0.5, t_max = (k < 300) ? periods[k - 201] : 1.62;
+        double s = 1.0, st = 0.0, stt = 0.0;
+        if (time <= 1.0) {
+            const double t = time, t2 = t * t, t3 = t2 * t, t4 = t3 * t, t5 = t4 * t, t6 = t5 * t, t7 = t6 * t;
+            s = -20.0 * t7 + 70.0 * t6 + -84.0 * t5 + 35.0 * t4;
+            st = 7.0 * -20.0 * t6 + 6.0 * 70.0 * t5 + 5.0 * -84.0 * t4 + 4.0 * 35.0 * t3;
+            stt = 42. * -20.0 * t5 + 30. * 70.0 * t4 + 20. * -84.0 * t3 + 12. * 35.0 * t2;
+        }
+        const double w = 2.0 * pi / t_max, arg = 2.0 * pi * time / t_max + pi / 2. + m.phase;
+        const double sn = sin(arg), cn = cos(arg);
+        const double y = y_max * sn, yt = y_max * w * cn, ytt = -y_max * (w * w) * sn;
+        o.le[1] = m.y0 + s * y;
+        o.le[3] = st * y + yt * s;
+        o.le[5] = stt * y + ytt * s + 2. * st * yt;
+    } else if ((k >= 401 && k <= 413) || k == 2) {
+        // heaving without a soft start (2) and the cases compared with experiments (401-413)
+        const double periods[13] = {0.51, 0.34, 0.25, 0.20, 0.17, 0.14, 0.13, 0.11, 0.10, 0.09, 0.08, 0.08, 0.07};
+        const double y_max = (k == 2) ? 0.5 : 0.0333, t_max = (k == 2) ? 2.5 : periods[k - 401];
+        const double w = 2.0 * pi / t_max, arg = 2.0 * pi * time / t_max + pi / 2;
+        const double sn = sin(arg), cn = cos(arg);
+        o.le[1] = m.y0 + y_max * sn;
+        o.le[3] = y_max * w * cn;
+        o.le[5] = -y_max * (w * w) * sn;
+    } else if (k == 3) {
+        // flapping: alpha = 80 deg sin(2 pi f t), f = 0.5
+        const double amax = 80.0 * pi / 180.0, w = 2.0 * pi * 0.5;
+        const double sn = sin(w * time), cn = cos(w * time);
+        o.alpha = amax * sn;
+        o.alpha_t = amax * cn * w;
+        o.alpha_tt = -1.0 * amax * sn * (w * w);
+        o.ca = cos(o.alpha);
+        o.sa = sin(o.alpha);
+    } else if (k == 4) {
+        // impulsive translation at u0 = -1
+        o.le[0] = m.x0 + -1.0 * time;
+        o.le[2] = -1.0;
+    }
+    return o;
+}
+
 // One drawing primitive of create_mask (create_mask.f90:91-117), in drawing order.
 enum PrimType { PRIM_SEGMENT = 0, PRIM_SHARP = 1, PRIM_HINGE = 2, PRIM_DOT = 3 };
 struct Prim {
@@ -24,7 +85,8 @@ struct MaskArgs {
     int* rect;    // [0..3] union of this step's primitive boxes (x0, x1, y0, y1), [4..7] its union
                   // with the previous step's box (every cell outside [0..3] is zero), [8..11] the
                   // accumulator of the next box (empty between steps), [12] blocks done
-    double rdx, rdy, rpi, angle_rad;  // 1/dx, 1/dy, 1/pi (correctly rounded), angle_deg*pi/180
+    double rdx, rdy, rpi;  // 1/dx, 1/dy, 1/pi (correctly rounded)
+    MotionArgs mo;         // the leading edge's motion (alpha of the time)
     int nsm;      // SMs of the device (raster grid size)
     void *mask, *mvx, *mvy;  // R*[ny][nx]
     // the parts of the mask that are not the beam (create_mask.f90:21-68, 120-204); with `full`
@@ -75,7 +137,8 @@ struct ForceArgs {
     DevScalars* S;
     int nx, ny, ns, viscous;
     double xl, yl, dx, dy, ds, t_beam, N_smooth, pi, angle_deg, t_release, tau;
-    double alpha, rdxi, rdyi;  // angle_deg pi / 180, RN(1/dxi), RN(1/dyi) (host)
+    double rdxi, rdyi;  // RN(1/dxi), RN(1/dyi) (host)
+    MotionArgs mo;      // the leading edge's motion (alpha of the time)
     double* geo;     // per node: trig[4], phi4* weights dl[4][18] (k_forces_geo)
     int* gij;        // per node: the four surface points' cells ij[4][2]
     const double *x, *y, *th;
@@ -104,6 +167,7 @@ struct SurfArgs {
 struct AdvArgs {
     DevScalars* S;
     int ns;
+    MotionArgs mo;   // the leading edge's motion, for the record's mouvement row
     double *x, *y, *vx, *vy, *th, *thd, *p_old, *p_new, *tau_old, *tau_new;
     double* rows;
 };
@@ -130,10 +194,12 @@ __device__ __forceinline__ void advance_state(const AdvArgs& a, const double* ti
         if (a.rows && S->run_row < S->run_cap) {
             double* rec = a.rows + (size_t)S->run_row * FSIBE_RECORD_COLS;
             for (int c = 0; c < 21; ++c) rec[c] = row[c];
+            const Motion m = motion_at(a.mo, S->time);
             const double tail[FSIBE_RECORD_COLS - 21] = {
                 t_before, S->dt1, S->u_max, S->mean_ux, S->mean_uy,
                 t_before, S->dt1, S->vor_rms, S->kinetic, S->dissipation, S->porous_diss, S->inflow_solid, S->inflow_mean,
-                t_before, (double)S->newton_iters};
+                t_before, (double)S->newton_iters,
+                S->time, m.alpha, m.alpha_t, m.alpha_tt, m.le[0], m.le[1], m.le[2], m.le[3], m.le[4], m.le[5]};
             for (int c = 21; c < FSIBE_RECORD_COLS; ++c) rec[c] = tail[c - 21];
             S->run_row += 1;
         }
@@ -149,7 +215,7 @@ struct BeamArgs {
     DevScalars* S;
     int ns, iImpulse, maxit, iFLUSI;
     double ds, eta, mue, sigma, t_release, tau, tol, pi, x0, y0, angle_deg;
-    double cos_a, sin_a;  // cos and sin of the beam angle (angle_deg * pi / 180), from the host
+    MotionArgs mo;        // the leading edge's motion
     BeamConsts k;
     double *x, *y, *vx, *vy, *th, *thd, *ax, *ay, *p_old, *p_new, *tau_old, *tau_new, *oo;
     double* ws;      // global workspace (used when the shared-memory workspace does not fit)

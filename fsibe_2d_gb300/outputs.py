@@ -7,8 +7,9 @@ simulation name as a prefix), each with its own Fortran format:
     u_max         '(1x,5(es12.4,1x))'  NavierStokes.f90:80-82 (cal_nlk)
     energies      '(8(es15.8,1x))'     NavierStokes.f90:259-261 (cal_energy)
     IBES_iter     '(es11.4,1x,i3)'     SolidSolver.f90:392-394 (IBES_solver, iFLUSI = 1)
+    mouvement<i>  '(10(es15.8,1x))'    BeamIO.f90:229-238 (SaveBeamData, every step)
 
-A record (FSIBE_RECORD_COLS values) holds the four rows of one step in that order; the
+A record (FSIBE_RECORD_COLS values) holds the five rows of one step in that order; the
 column layout is documented at fsibe_run_records in include/fsibe.h.  The files are opened
 in append mode, as the reference opens them (status='unknown', access='append')."""
 import math
@@ -22,6 +23,7 @@ BEAM = slice(0, 21)
 UMAX = slice(21, 26)
 ENERGIES = slice(26, 34)
 IBES = slice(34, 36)
+MOUVEMENT = slice(36, 46)
 
 
 def es(v, w, d):
@@ -54,6 +56,10 @@ def energies_line(row):
     return "".join(es(v, 15, 8) + " " for v in row)
 
 
+def mouvement_line(row):
+    return "".join(es(v, 15, 8) + " " for v in row)
+
+
 def ibes_iter_line(row):
     it = int(round(row[1]))
     return es(row[0], 11, 4) + " " + ("%3d" % it if -99 <= it <= 999 else "***")
@@ -63,7 +69,7 @@ def write_step_files(directory, records, simulation_name="", beam=1, iFLUSI=1, i
     """Append the lines of every record to the reference's per-step files in directory.
     beam_data<beam> is written when iSaveBeam = 3 and IBES_iter when iFLUSI = 1, for the steps
     that start after t_release (SolidSolverWrapper calls IBES_solver only then,
-    SolidSolver.f90:20-27); u_max and energies every step.  Returns the paths written."""
+    SolidSolver.f90:20-27); u_max, energies and mouvement<beam> every step.  Returns the paths written."""
     rec = np.asarray(records, dtype=np.float64).reshape(-1, FSIBE_RECORD_COLS)
     os.makedirs(directory, exist_ok=True)
     base = os.path.join(directory, simulation_name)
@@ -73,6 +79,7 @@ def write_step_files(directory, records, simulation_name="", beam=1, iFLUSI=1, i
         files.insert(0, (f"beam_data{beam}", BEAM, beam_data_line, every))
     if iFLUSI == 1:
         files.append(("IBES_iter", IBES, ibes_iter_line, rec[:, IBES.start] > t_release))
+    files.append((f"mouvement{beam}", MOUVEMENT, mouvement_line, every))
     paths = []
     for name, cols, fmt, which in files:
         path = base + name

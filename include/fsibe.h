@@ -177,8 +177,11 @@ int fsibe_run(fsibe_ctx* ctx, int nsteps, double* rows);
  *   [26..33] the energies row: time, dt1, vor_rms, kinetic, dissipation, porous_diss,
  *            inflow_solid, inflow_mean (NavierStokes.f90:259-261)
  *   [34..35] the IBES_iter row: time, Newton iterations (SolidSolver.f90:392-394)
- * The last three carry the time before the step, as the reference writes them during it. */
-#define FSIBE_RECORD_COLS 36
+ *   [36..45] the mouvement row: time, alpha, alpha_t, alpha_tt, the leading edge's x, y, vx,
+ *            vy, ax, ay (BeamIO.f90:229-238, SaveBeamData)
+ * The u_max, energies and IBES_iter rows carry the time before the step, as the reference
+ * writes them during it; beam_data and mouvement the time after it. */
+#define FSIBE_RECORD_COLS 46
 /* nsteps calls of fsibe_step with one record per step (records[s*FSIBE_RECORD_COLS + c]);
  * the time loop of time_step.f90:178-236 with its per-step output. */
 int fsibe_run_records(fsibe_ctx* ctx, int nsteps, double* records);
@@ -209,8 +212,18 @@ int fsibe_get_scalars(fsibe_ctx* ctx, fsibe_scalars* out);
  * between fsibe_get_forces and fsibe_solid_step it sees the reference's state.  Needs
  * iViscous = 1 and a beam (else FSIBE_ERR_PARAM).  `time` fills column 0 and the soft
  * start-up factor; the contour follows the device's current beam (angle and positions of the
- * step), which is the reference's mouvement(time) when time is the context's current time. */
+ * step) and the leading edge's angle mouvement(time).  With the leading-edge cylinder the
+ * reference computes no surface integral (FSIBE_ERR_UNSUPPORTED); with walls its drag and lift
+ * columns are zero (BeamForces.f90:331-336, 494-502). */
 int fsibe_surface_integral(fsibe_ctx* ctx, double time, double* out);
+
+/* ComputePressureSnapshot (NavierStokes.f90:598-665): the static pressure of the current
+ * vorticity, with the velocity at `time` (the state's velocity plus the mean flow of the
+ * time) and the current mask: p = q - |u|^2/2, q from the Poisson equation of the divergence
+ * of the penalization and of the nonlinear term.  press: (0:nx-1, 0:ny-1) column-major FP64.
+ * Outside the time step; the state is not changed.  After a step at the context's time it
+ * equals that step's pressure up to rounding. */
+int fsibe_pressure_snapshot(fsibe_ctx* ctx, double time, double* press);
 
 /* ---- runtime backup ----------------------------------------------------------
  * The file runtime_backup<n>.in of MakeRuntimeBackup (save_fields.f90:109-152): Fortran

@@ -406,14 +406,52 @@ static double Mean_Uy(const orc_ctx* c, double time) {
  * ------------------------------------------------------------------------------ */
 
 /* mouvement case 0, clamped leading edge (mouvement.f90:19-28). */
-static void mouvement(const orc_ctx* c, double /*time*/, double& alpha, double& alpha_t, double& alpha_tt, double LE[6],
+/* The heaving periods of mouvement cases 201-213 (and 300-350: 1.62) and 401-413. */
+static const double kHeaveT[13] = {1.0, 1.09, 1.20, 1.29, 1.33, 1.4, 1.5, 1.71, 2.0, 2.4, 3.0, 4.0, 1.62};
+static const double kParazT[13] = {0.51, 0.34, 0.25, 0.20, 0.17, 0.14, 0.13, 0.11, 0.10, 0.09, 0.08, 0.08, 0.07};
+
+/* mouvement.f90:5-200: the leading edge's prescribed motion.  LE = x, y, vx, vy, ax, ay. */
+static void mouvement(const orc_ctx* c, double time, double& alpha, double& alpha_t, double& alpha_tt, double LE[6],
                       const Beam& b) {
+    const double pi = c->pi;
+    const int m = c->P.iMotion;
     for (int i = 0; i < 6; ++i) LE[i] = 0.0;
     LE[0] = b.x0;
     LE[1] = b.y0;
-    alpha = b.AngleBeam * c->pi / 180.0;
+    alpha = b.AngleBeam * pi / 180.0;
     alpha_t = 0.0;
     alpha_tt = 0.0;
+    if ((m >= 201 && m <= 213) || (m >= 300 && m <= 350)) {  /* :29-76, heaving with a soft start */
+        const double y_max = 0.5, t_max = (m < 300) ? kHeaveT[m - 201] : 1.62;
+        double k = 1.0, kt = 0.0, ktt = 0.0;
+        if (time <= 1.0) {
+            const double a = -20.0, bb = 70.0, cc = -84.0, d = 35.0, t = time;
+            const double t2 = t * t, t3 = t2 * t, t4 = t3 * t, t5 = t4 * t, t6 = t5 * t, t7 = t6 * t;
+            k = a * t7 + bb * t6 + cc * t5 + d * t4;
+            kt = 7.0 * a * t6 + 6.0 * bb * t5 + 5.0 * cc * t4 + 4.0 * d * t3;
+            ktt = 42. * a * t5 + 30. * bb * t4 + 20. * cc * t3 + 12. * d * t2;
+        }
+        const double w = 2.0 * pi / t_max, arg = 2.0 * pi * time / t_max + pi / 2. + b.phase;
+        const double y = y_max * std::sin(arg), yt = y_max * w * std::cos(arg), ytt = -y_max * (w * w) * std::sin(arg);
+        LE[1] = b.y0 + k * y;
+        LE[3] = kt * y + yt * k;
+        LE[5] = ktt * y + ytt * k + 2. * kt * yt;
+    } else if ((m >= 401 && m <= 413) || m == 2) {  /* :77-114 (Paraz), :116-130 (hard start) */
+        const double y_max = (m == 2) ? 0.5 : 0.0333, t_max = (m == 2) ? 2.5 : kParazT[m - 401];
+        const double w = 2.0 * pi / t_max, arg = 2.0 * pi * time / t_max + pi / 2;
+        LE[1] = b.y0 + y_max * std::sin(arg);
+        LE[3] = y_max * w * std::cos(arg);
+        LE[5] = -y_max * (w * w) * std::sin(arg);
+    } else if (m == 3) {  /* :131-143, flapping */
+        const double angle_max = 80.0 * pi / 180.0, f = 0.5, w = 2.0 * pi * f;
+        alpha = angle_max * std::sin(w * time);
+        alpha_t = angle_max * std::cos(w * time) * w;
+        alpha_tt = -1.0 * angle_max * std::sin(w * time) * (w * w);
+    } else if (m == 4) {  /* :144-155, impulsive translation */
+        const double u0 = -1.0;
+        LE[0] = b.x0 + u0 * time;
+        LE[2] = u0;
+    }
 }
 
 /* integrate_position.f90:14-44: running sums of cos/sin(theta)*ds, rotated by alpha. */
@@ -754,6 +792,9 @@ static void create_sponge_mask(orc_ctx* c) {
                 const bool hole = ix >= ixmin && ix <= ixmax && iy >= iymin && iy <= iymax;
                 F2(ms, ix, iy) = (hole || F2(c->mask, ix, iy) > 0.0) ? 0.0 : 1.0;
             }
+    } else if (isp == 10) {  /* :276-281, the sharp outflow sponge */
+        for (long ix = nint((xl - sss) / dx); ix <= c->nx - 1; ++ix)
+            for (int iy = 0; iy < c->ny; ++iy) F2(ms, ix, iy) = 1.0;
     }
     for (double& v : ms) v = v / c->P.eps_sponge;
 }
@@ -810,7 +851,24 @@ static void cal_nlk(orc_ctx* c, double time, double& dt1, double* nlk, const dou
             pen1[k] = -c->mask[k] * (u[k] - c->maskvx[k]);
             pen2[k] = -c->mask[k] * (u[NN + k] - c->maskvy[k]);
         }
-        std::vector<double> tmp(NN);
+        if (c->P.iSponge == 10) {  /* :103-122: the integral along x of -mask_sponge du/dx */
+            std::vector<double> wk(NN), dk(NN);
+            coftxy(c, u, wk.data());
+            cofdx(c, wk.data(), dk.data());
+            cofitxy(c, dk.data(), work2.data());
+            for (size_t k = 0; k < NN; ++k) work2[k] = -c->mask_sponge[k] * work2[k];
+            const long ixmin = nint((c->P.xl - c->P.SpongeSize) / dx), ixmax = c->nx - 1 - 15;
+#pragma omp parallel for schedule(static)
+            for (int iy = 0; iy < c->ny; ++iy) {
+                // the reference sums from ixmin for every ix; the running sum adds the same
+                // terms in the same order
+                double summe = 0.0;
+                for (long ix = ixmin; ix <= ixmax; ++ix) {
+                    if (ix > ixmin) summe = summe + 0.5 * (F2(work2, ix - 1, iy) + F2(work2, ix, iy)) * dx;
+                    F2(pen1, ix, iy) = F2(pen1, ix, iy) + summe;
+                }
+            }
+        }
         coftxy(c, pen2.data(), work2.data());
         cofdx(c, work2.data(), pen2.data());
         coftxy(c, pen1.data(), work2.data());
@@ -1704,6 +1762,8 @@ int orc_create(const fsibe_params* p, orc_ctx** out) {
     c->sharp = std::fabs(p->N_smooth) < 1e-4;
     if (c->P.newton_tol <= 0.0) c->P.newton_tol = 1.0e-7;
     if (c->P.newton_maxit <= 0) c->P.newton_maxit = 50;
+    /* mouvement.f90:102-104: the Paraz cases set the forces' soft start-up to one period */
+    if (c->P.iMotion >= 401 && c->P.iMotion <= 413) c->P.tau = kParazT[c->P.iMotion - 401];
     const size_t NN = (size_t)c->nx * c->ny;
     for (auto* v : {&c->dealiase, &c->mask, &c->maskvx, &c->maskvy, &c->vor_mean, &c->press, &c->mask_sponge, &c->mask_frame})
         v->assign(NN, 0.0);
@@ -1841,10 +1901,13 @@ int orc_run_records(orc_ctx* c, int nsteps, double* rec) {
             double* r = rec + (size_t)s * FSIBE_RECORD_COLS;
             std::memcpy(r, c->sc.beam_data, 21 * sizeof(double));
             const fsibe_scalars& q = c->sc;
+            double al, al_t, al_tt, LE[6];  /* BeamIO.f90:229-238: mouvement(time) after the step */
+            mouvement(c, c->time, al, al_t, al_tt, LE, c->beam);
             const double tail[FSIBE_RECORD_COLS - 21] = {
                 t_before, q.dt1, q.u_max, q.mean_ux, q.mean_uy,
                 t_before, q.dt1, q.vor_rms, q.kinetic, q.dissipation, q.porous_diss, q.inflow_solid, q.inflow_mean,
-                t_before, (double)q.newton_iters};
+                t_before, (double)q.newton_iters,
+                c->time, al, al_t, al_tt, LE[0], LE[1], LE[2], LE[3], LE[4], LE[5]};
             std::memcpy(r + 21, tail, sizeof(tail));
         }
         if (st) return st;
@@ -1935,6 +1998,40 @@ double orc_time(orc_ctx* c) { return c->time; }
  * (pressure at t_beam) -- and the penalization drag/lift over the whole grid.
  * out[11]: time, drag, lift, drag_surf, lift_surf, Ft(1), Fn(1), Fp(1), Ft(2), Fn(2), Fp(2)
  * (the columns of the 'surface' file, :492-499). */
+/* ComputePressureSnapshot (NavierStokes.f90:598-665): the static pressure of the state's
+ * vorticity at `time` (its mean flow) and the current mask, outside the time step. */
+int orc_pressure_snapshot(orc_ctx* c, double time, double* press) {
+    if (!c || !press) return FSIBE_ERR_PARAM;
+    if (!c->initialized) return fail(c, FSIBE_ERR_STATE, "pressure snapshot before init_fields");
+    const size_t NN = (size_t)c->nx * c->ny;
+    std::vector<double> u(2 * NN), work1(NN), work2(NN), work_dx(NN), work_dy(NN), pen1(NN), pen2(NN);
+    const double* vortk = c->vortk[c->n0].data();
+    cal_velocity(c, time, vortk, u.data(), work1.data());
+    for (size_t k = 0; k < NN; ++k) {
+        pen1[k] = c->mask[k] * (u[k] - c->maskvx[k]);
+        pen2[k] = c->mask[k] * (u[NN + k] - c->maskvy[k]);
+    }
+    cofitxy(c, vortk, work1.data());
+    coftxy(c, pen1.data(), work2.data());
+    cofdx(c, work2.data(), pen1.data());
+    coftxy(c, pen2.data(), work2.data());
+    cofdy(c, work2.data(), pen2.data());
+    for (size_t k = 0; k < NN; ++k) {
+        work_dx[k] = -work1[k] * u[NN + k];
+        work_dy[k] = +work1[k] * u[k];
+    }
+    coftxy(c, work_dx.data(), work1.data());
+    cofdx(c, work1.data(), work_dx.data());
+    coftxy(c, work_dy.data(), work1.data());
+    cofdy(c, work1.data(), work_dy.data());
+    for (size_t k = 0; k < NN; ++k) work1[k] = pen1[k] + pen2[k] + work_dy[k] + work_dx[k];
+    std::vector<double> q(NN);
+    poisson(c, work1.data(), q.data());
+    cofitxy(c, q.data(), work1.data());
+    for (size_t k = 0; k < NN; ++k) press[k] = work1[k] - 0.5 * (u[k] * u[k] + u[NN + k] * u[NN + k]);
+    return FSIBE_OK;
+}
+
 int orc_surface_integral(orc_ctx* c, double time, double* out) {
     if (!c || !out) return FSIBE_ERR_PARAM;
     if (!c->initialized) return fail(c, FSIBE_ERR_STATE, "surface_integral before init_fields");

@@ -1,6 +1,6 @@
 """The per-step files of a GPU run against the oracle's (C1 configuration, first 100 steps):
 the records of fsibe_run_records written by fsibe_2d_gb300.outputs in the reference's
-formats (beam_data1, u_max, energies, IBES_iter) must read the same, line for line and field
+formats (beam_data1, u_max, energies, IBES_iter, mouvement1) must read the same, line for line and field
 for field: identical, or apart by one unit of the last printed digit, or -- for a value far
 below its column's scale, whose printed digits are rounding noise -- within the FP64 parity
 bar, 1e-10 of the column's largest magnitude, or at the FP64 rounding level of the file's
@@ -44,7 +44,7 @@ def test_c1_step_files_match_the_oracle(oracle, tmp_path):
     assert np.allclose(rg[:, 35], ro[:, 35])                   # Newton iterations, exactly
     pg = O.write_step_files(str(tmp_path / "gpu"), rg)
     po = O.write_step_files(str(tmp_path / "oracle"), ro)
-    digits = {"beam_data1": 8, "u_max": 4, "energies": 8, "IBES_iter": 4}
+    digits = {"beam_data1": 8, "u_max": 4, "energies": 8, "IBES_iter": 4, "mouvement1": 8}
     identical = differ = 0
     for a, b in zip(pg, po):
         name = a.rsplit("/", 1)[1]

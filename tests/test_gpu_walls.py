@@ -1,7 +1,8 @@
 """Channel walls, the leading-edge cylinder and the sponges on the GPU against the oracle.
 
 The reference's optional solid features (create_mask.f90:21-210 walls and cylinder, 223-470
-the sponges; NavierStokes.f90:142-164 the vorticity-sponge term) at 128^2 with a flexible beam:
+the sponges; NavierStokes.f90:142-164 the vorticity-sponge term, :103-122 the sharp outflow
+sponge's integral) at 128^2 with a flexible beam:
 the mask and its velocity field after the start-up, then 40 steps of the coupled run.  The FP64
 form must match the oracle within 1e-10 (relative L2) in the mask, the vorticity, the beam's
 deflection and the drag/lift series; the FP32-compensated form within 1e-5."""
@@ -24,6 +25,7 @@ CASES = {
     "sponge3": dict(iSponge=3, SpongeSize=0.3, eps_sponge=1e-2),
     "sponge22": dict(iSponge=22, SpongeSize=0.3, eps_sponge=1e-2),
     "walls+sponge4": dict(iWalls=1, h_channel=0.3, iSponge=4, SpongeSize=0.5),
+    "sponge10": dict(iSponge=10, SpongeSize=1.0, eps_sponge=0.1),   # columns 96..112 of 128
     # a fixed beam in an accelerating flow: the mask is redrawn until T_fullspeed, then kept
     "sponge4-accelerating": dict(iWalls=1, h_channel=0.3, iSponge=4, SpongeSize=0.5, iFLUSI=0,
                                  iMeanVelocity=1, T_fullspeed=0.02),
@@ -56,7 +58,7 @@ def test_features_fp64_match_the_oracle(oracle, name):
     g.close(); o.close()
 
 
-@pytest.mark.parametrize("name", ["walls+cylinder", "sponge22", "walls+sponge4", "sponge1"])
+@pytest.mark.parametrize("name", ["walls+cylinder", "sponge22", "walls+sponge4", "sponge1", "sponge10"])
 def test_features_fp32c_match_the_oracle(oracle, name):
     g, o = _run_pair(oracle, FSIBE_FP32C, CASES[name])
     rg, ro = g.time_step(STEPS), o.time_step(STEPS)
@@ -72,9 +74,10 @@ def test_feature_parameters_are_checked():
     import fsibe_2d_gb300 as F
     from fsibe_2d_gb300._binding import FsibeError
     from fsibe_2d_gb300._abi import FSIBE_ERR_PARAM, FSIBE_ERR_UNSUPPORTED
-    for kw, code in ((dict(iSponge=10, SpongeSize=0.5), FSIBE_ERR_UNSUPPORTED),   # the penalised-
-                     (dict(iSponge=5, SpongeSize=0.5), FSIBE_ERR_PARAM),          # field sponge
+    for kw, code in ((dict(iSponge=5, SpongeSize=0.5), FSIBE_ERR_PARAM),
                      (dict(iSponge=1, SpongeSize=0.0), FSIBE_ERR_PARAM),
+                     (dict(iSponge=10, SpongeSize=4.0), FSIBE_ERR_PARAM),           # not inside the box
+                     (dict(iSponge=1, iBeam=0, SpongeSize=0.5), FSIBE_ERR_UNSUPPORTED),
                      (dict(iWalls=2), FSIBE_ERR_PARAM)):
         with pytest.raises(FsibeError) as ex:
             F.Run(make_params(nx=64, ny=64, ns=16, **kw))

@@ -36,7 +36,8 @@ def test_cylinder_and_sponges_change_the_flow(oracle):
     ref = base.time_step(5)
     for kw in (dict(iCylinder=1, R_cylinder=0.1), dict(iSponge=1, SpongeSize=0.5, eps_sponge=1e-2),
                dict(iSponge=3, SpongeSize=0.3, eps_sponge=1e-2), dict(iSponge=22, SpongeSize=0.3, eps_sponge=1e-2),
-               dict(iWalls=1, h_channel=0.3, iSponge=4, SpongeSize=0.5)):
+               dict(iWalls=1, h_channel=0.3, iSponge=4, SpongeSize=0.5),
+               dict(iSponge=10, SpongeSize=1.5, eps_sponge=0.1)):
         o = oracle.OracleRun(make_params(nx=n, ny=n, ns=16, **kw))
         o.init_fields(w)
         rows = o.time_step(5)

@@ -1,5 +1,6 @@
 """The per-step text files in the reference's Fortran formats (fsibe_2d_gb300.outputs):
-ESw.d edits of known values, the line layouts of beam_data, u_max, energies and IBES_iter,
+ESw.d edits of known values, the line layouts of beam_data, u_max, energies, IBES_iter and
+mouvement,
 and the files the oracle's records produce (append mode, one line per step)."""
 import numpy as np
 
@@ -24,6 +25,7 @@ def test_line_layouts():
     assert O.beam_data_line(r[O.BEAM]).count("E") == 21 and len(O.beam_data_line(r[O.BEAM])) == 21 * 16
     assert O.u_max_line(r[O.UMAX]).startswith("  ") and len(O.u_max_line(r[O.UMAX])) == 1 + 5 * 13
     assert len(O.energies_line(r[O.ENERGIES])) == 8 * 16
+    assert len(O.mouvement_line(r[O.MOUVEMENT])) == 10 * 16
     assert O.ibes_iter_line([0.25, 3]) == " 2.5000E-01   3"
 
 
@@ -43,7 +45,10 @@ def test_oracle_records_write_the_reference_files(oracle, tmp_path):
     paths = O.write_step_files(str(tmp_path), rec[:3])
     O.write_step_files(str(tmp_path), rec[3:])                  # appended
     names = sorted(f.name for f in tmp_path.iterdir())
-    assert names == ["IBES_iter", "beam_data1", "energies", "u_max"]
+    assert names == ["IBES_iter", "beam_data1", "energies", "mouvement1", "u_max"]
+    # the mouvement row: the time after the step, the fixed angle and leading edge (case 0)
+    assert np.array_equal(rec[:, 36], rec[:, 0])
+    assert np.all(rec[:, 37] == 0.0) and np.all(rec[:, 40] == p.x0) and np.all(rec[:, 41] == p.y0)
     for path in paths:
         lines = open(path).read().splitlines()
         assert len(lines) == (4 if path.endswith("IBES_iter") else 5)
