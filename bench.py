@@ -528,6 +528,27 @@ def reference_arm(args):
     print(json.dumps(line))
 
 
+# The workloads of --profile-case: (make_params keywords, seed field (n, K, seed))
+PROFILE_CASES = {
+    "c2": (dict(nx=NX, ny=NY, ns=NS, Re=RE, dt=DT), (NX, 8, 0)),
+    "c5": (dict(nx=4096, ny=4096, ns=1024, xl=8.0, yl=8.0, Re=2000.0, dt=1e-5, EI=0.05, mu=2.0, eps=1e-4,
+                x0=2.0, y0=4.0), (4096, 32, 2)),
+}
+
+
+def profile_case(name, precision, steps):
+    """A short run of one workload with the CUDA graph off (every kernel its own launch, the
+    start-up step first), for ncu captures: `python bench.py --profile-case c5 --precision 1
+    --steps 3`.  Prints the status and the autotuned tile heights."""
+    import fsibe_2d_gb300 as F
+    kw, (n, K, seed) = PROFILE_CASES[name]
+    r = F.Run(F.make_params(precision=precision, **kw))
+    r.init_fields(seeded_vorticity(n, K=K, seed=seed))
+    r.time_step(steps)
+    print("status", r.scalars().status, "tiles", r.tiles())
+    r.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -537,7 +558,12 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--err-steps", type=int, default=2000)
     ap.add_argument("--no-large", action="store_true", help="skip the 4096^2 large-run report")
+    ap.add_argument("--profile-case", choices=sorted(PROFILE_CASES), help="run --steps steps of a workload for ncu")
+    ap.add_argument("--precision", type=int, default=1, help="with --profile-case: 0 FP64, 1 FP32-compensated")
     args = ap.parse_args()
+    if args.profile_case:
+        profile_case(args.profile_case, args.precision, args.steps)
+        return
     if args.impl == "reference":
         reference_arm(args)
     else:

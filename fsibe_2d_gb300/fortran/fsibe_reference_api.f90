@@ -34,7 +34,7 @@ module fsibe_reference_api
   implicit none
   private
   public :: create_mask, EvolveFluidExplicit, EvolveFluidAB2, GetForces, GravityImpulse, &
-            SolidSolverWrapper, fsibe_sync_fields
+            SolidSolverWrapper, fsibe_sync_fields, ComputePressureSnapshot
 
   interface
     integer(c_int) function fsibe_download_beam(ctx, beam, po, pn, to, tn) bind(C, name="fsibe_download_beam")
@@ -46,6 +46,12 @@ module fsibe_reference_api
       import :: c_int, c_ptr, c_double
       type(c_ptr), value :: ctx
       real(c_double), intent(out) :: v(*)
+    end function
+    integer(c_int) function fsibe_pressure_snapshot(ctx, time, p) bind(C, name="fsibe_pressure_snapshot")
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: ctx
+      real(c_double), value :: time
+      real(c_double), intent(out) :: p(*)
     end function
   end interface
 
@@ -209,6 +215,17 @@ contains
     call fsibe_check(fsibe_download_vortk(gctx, vortk(:,:,n0)), "download_vortk")
     call fsibe_check(fsibe_download_u(gctx, u), "download_u")
     call fsibe_check(fsibe_download_press(gctx, press), "download_press")
+  end subroutine
+
+  ! ComputePressureSnapshot (NavierStokes.f90:598-665): the static pressure of the run's current
+  ! vorticity with the velocity at `time` and the current mask.  vortk must be the run's
+  ! current vorticity (the device's copy is the one used).
+  subroutine ComputePressureSnapshot(time, vortk, press)
+    use share_vars
+    real(kind=pr), intent(in) :: time
+    real(kind=pr), dimension(0:nx-1,0:ny-1), intent(in) :: vortk
+    real(kind=pr), dimension(0:nx-1,0:ny-1), intent(out) :: press
+    call fsibe_check(fsibe_pressure_snapshot(gctx, time, press), "pressure_snapshot")
   end subroutine
 
 end module fsibe_reference_api

@@ -88,3 +88,26 @@ def write_step_files(directory, records, simulation_name="", beam=1, iFLUSI=1, i
                 f.write(fmt(r[cols]) + "\n")
         paths.append(path)
     return paths
+
+
+def write_field(filename, field, nsave=1, lx=None, ly=None, fieldtype="pressure", header=()):
+    """SaveField (FieldExport.f90:612-648), '%format1': the header lines (the reference writes its
+    PARAMS file there; pass them as `header`), '%format1', nx and ny of the field as i5.5, the
+    domain sizes as es11.4, the type line, then one value a line, es11.4 (es16.9 for the type
+    "precision"): rows from the top (y index ny - 1) down in steps of nsave, each row from
+    x index 0 in steps of nsave.  field: (ny, nx), the layout of the library's fields."""
+    f = np.asarray(field, dtype=np.float64)
+    ny1, nx1 = f.shape
+    fmt = (lambda v: es(v, 16, 9)) if fieldtype == "precision" else (lambda v: es(v, 11, 4))
+    lines = list(header)
+    lines += ["%format1", "%05d   %% nx" % nx1, "%05d   %% ny" % ny1,
+              es(lx, 11, 4) + "   % xl, domain size in x-direction",
+              es(ly, 11, 4) + "   % yl, domain size in y-direction",
+              "% The next entry can be used to identify the type of the field: ",
+              "% " + fieldtype]
+    for iy in range(0, ny1, nsave):
+        row = f[ny1 - 1 - iy]
+        lines += [fmt(v) for v in row[0:nx1:nsave]]
+    with open(filename, "w") as out:
+        out.write("\n".join(lines) + "\n")
+    return filename

@@ -65,3 +65,15 @@ def test_fixed_beam_mask_is_redrawn_only_while_the_flow_accelerates(oracle):
     assert np.abs(late - early).max() > 1e-3          # the sponge's inflow profile grew
     assert np.array_equal(o.mask()[1], late)            # and is frozen after T_fullspeed
     o.close()
+
+
+def test_pressure_snapshot_is_the_steps_pressure(oracle):
+    """NavierStokes.f90:598-665 at the time after a step gives that step's pressure."""
+    n = 64
+    o = oracle.OracleRun(make_params(nx=n, ny=n, ns=16))
+    o.init_fields(seeded_vorticity(n, seed=9))
+    o.time_step(4)
+    snap = o.ComputePressureSnapshot(o.scalars().time)
+    p = o.press()
+    assert np.abs(snap - p).max() <= 1e-12 * np.abs(p).max()
+    o.close()

@@ -55,3 +55,18 @@ def test_oracle_records_write_the_reference_files(oracle, tmp_path):
     first = open(tmp_path / "beam_data1").read().splitlines()[0].split()
     assert np.allclose([float(v) for v in first], rec[0, :21], rtol=1e-8, atol=0)
     o.close(); rows.close()
+
+
+def test_save_field_format1(tmp_path):
+    """FieldExport.f90:612-648: the %format1 header and one value a line, top row first."""
+    f = np.arange(4 * 8, dtype=float).reshape(4, 8)      # (ny, nx)
+    path = O.write_field(str(tmp_path / "p_0.0000E+00"), f, nsave=2, lx=4.0, ly=2.0, header=["% PARAMS"])
+    lines = open(path).read().splitlines()
+    assert lines[:8] == ["% PARAMS", "%format1", "00008   % nx", "00004   % ny", " 4.0000E+00   % xl, domain size in x-direction",
+                         " 2.0000E+00   % yl, domain size in y-direction",
+                         "% The next entry can be used to identify the type of the field: ", "% pressure"]
+    vals = [float(v) for v in lines[8:]]
+    # rows y = 3, 1 (nsave 2 from the top), columns x = 0, 2, 4, 6
+    assert vals == [24.0, 26.0, 28.0, 30.0, 8.0, 10.0, 12.0, 14.0]
+    p2 = O.write_field(str(tmp_path / "q"), f, 1, 4.0, 2.0, "precision")
+    assert open(p2).read().splitlines()[7] == " 2.400000000E+01"
