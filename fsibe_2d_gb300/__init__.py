@@ -92,7 +92,7 @@ class Run(_Run):
 
     def tile_config(self):
         """(rows, blocks-per-SM bound) of the fused x kernels nl_x, press_x, press_fin as the
-        autotuner chose them (bound 0: the kernel's default)."""
+        autotuner chose them (bound 0: the kernel's default; 16: the paired FP32 press_x)."""
         out = (C.c_int32 * 6)()
         self._call("tile_config", out)
         return [(out[2 * q], out[2 * q + 1]) for q in range(3)]

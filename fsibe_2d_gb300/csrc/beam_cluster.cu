@@ -21,6 +21,11 @@
 // memory under the single-CTA kernel's reuse rule (kept while <= 5 passes per Newton step).
 // The iterate update, the norms and the stopping test run redundantly in every CTA on
 // identical data, so they need no exchange.
+// Large beams (ns >= 512: M^-1's rows and the factor exceed a CTA's shared memory) run the
+// same algorithm with both in global memory, where they stay L2-resident: each CTA reads its
+// rows of M^-1 from its slice of the persistent copy, and factors its own copy of the band
+// (the all-gather of the scaled rows writes every CTA's copy directly; the cluster barrier's
+// release/acquire orders those global stores as it orders the DSMEM ones).
 #include <math.h>
 
 #include <mutex>
@@ -72,7 +77,16 @@ struct ClLayout {
     size_t x, xdi, node, bvec, band, part, slots, yf, fact, minv, total;  // byte offsets
 };
 
-__host__ __device__ inline void cl_layout(int ns, int R, ClLayout& Y) {
+// Floats of one CTA's global copy of the factor area in the large-beam form (the factor, or
+// after the Newton loop the position sums, as in shared memory), a multiple of 4.
+__host__ __device__ inline size_t cl_fact_floats(int ns) {
+    const int n = 2 * ns + 4, L = ns + 8;
+    const size_t fact = 25 * (size_t)(n + 16), post = 20 * (size_t)L;
+    return ((fact > post ? fact : post) + 3) & ~(size_t)3;
+}
+
+// big: the factor area and M^-1 live in global memory (not in the shared-memory layout)
+__host__ __device__ inline void cl_layout(int ns, int R, ClLayout& Y, bool big = false) {
     Y.n = 2 * ns + 4;
     Y.L = ns + 8;
     Y.R = R;
@@ -87,6 +101,7 @@ __host__ __device__ inline void cl_layout(int ns, int R, ClLayout& Y) {
     Y.part = o;  o = al16(o + 8 * 4 * (size_t)Y.rmax);
     Y.slots = o; o = al16(o + 8 * 4 * (size_t)R);
     Y.yf = o;    o = al16(o + 4 * (size_t)(Y.mld + 16));
+    if (big) { Y.fact = Y.minv = Y.total = o; return; }
     Y.fact = o;
     // the factor (U 16, L 8 floats and a row-scale exponent per row); after the Newton loop
     // CTA 0 reuses it for the position sums (cs, pre: 4 L each) and th, thd (L each)
@@ -183,8 +198,10 @@ __global__ void __launch_bounds__(256, 1) k_beam_cl(BeamArgs b) {
     const unsigned rank = cl_rank(), R = cl_nrank();
     const int ns = b.ns, n = 2 * ns + 4;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nthr = blockDim.x, nwarp = nthr >> 5;
+    const bool big = b.cl_big != 0;
+    const size_t fstride = cl_fact_floats(ns);
     ClLayout Y;
-    cl_layout(ns, (int)R, Y);
+    cl_layout(ns, (int)R, Y, big);
     const int L = Y.L, mld = Y.mld, rmax = Y.rmax;
     int lo, hi;
     cl_rows(n, (int)R, (int)rank, lo, hi);
@@ -202,10 +219,10 @@ __global__ void __launch_bounds__(256, 1) k_beam_cl(BeamArgs b) {
     // [3R, 4R) the flags sent with the factor rows
     unsigned long long* slots = reinterpret_cast<unsigned long long*>(cl_smem + Y.slots);
     float* yf = reinterpret_cast<float*>(cl_smem + Y.yf);
-    float* Uf = reinterpret_cast<float*>(cl_smem + Y.fact);
+    float* Uf = big ? b.clws + (size_t)rank * fstride : reinterpret_cast<float*>(cl_smem + Y.fact);
     float* Lf = Uf + (size_t)16 * (n + 16);
     int* rse = reinterpret_cast<int*>(Lf + (size_t)8 * (n + 16));
-    float* minv = reinterpret_cast<float*>(cl_smem + Y.minv);
+    float* minv = big ? b.minv + (size_t)rank * rmax * mld : reinterpret_cast<float*>(cl_smem + Y.minv);
     __shared__ D1DTab dtab;
     __shared__ NewtonCtx cs;
     __shared__ double red[2][8];
@@ -242,7 +259,8 @@ __global__ void __launch_bounds__(256, 1) k_beam_cl(BeamArgs b) {
             // this CTA's rows of M^-1 and their row-scale exponents, kept from an earlier step
             const float* g = b.minv + (size_t)rank * rmax * mld;
             const int nv = nr * mld / 4;
-            for (int q = tid; q < nv; q += nthr) cp_async16(minv + 4 * q, g + 4 * q);
+            if (!big)  // the large-beam form reads its rows where they are
+                for (int q = tid; q < nv; q += nthr) cp_async16(minv + 4 * q, g + 4 * q);
             for (int k = lo + tid; k < hi; k += nthr) rse[k] = b.minv_rse[k];
         }
         const double* K = b.pred + pred_consts(ns);
@@ -275,7 +293,7 @@ __global__ void __launch_bounds__(256, 1) k_beam_cl(BeamArgs b) {
         }
         __syncthreads();
         const NewtonCtx& c = cs;
-        bool inv_pending = have_inv;  // the stored inverse rows are still arriving (cp.async)
+        bool inv_pending = have_inv && !big;  // the stored inverse rows are still arriving (cp.async)
         bool need_factor = !have_inv, factored = false;
         // own rows: generic ones [glo, ghi); the boundary equations (rows 0..3: k = 1, 2, 3, 7;
         // rows 2ns..2ns+3: k = 8, 6, 5, 4) sit in the first and last CTA and take warps 4..7,
@@ -339,11 +357,14 @@ __global__ void __launch_bounds__(256, 1) k_beam_cl(BeamArgs b) {
                     for (int e = tid; e < nr * 5 * ((int)R - 1); e += nthr) {
                         const unsigned dst = (rank + 1 + (unsigned)(e / (nr * 5))) % R;
                         const int q = e % (nr * 5), r = lo + q / 5, part5 = q % 5;
+                        float* Ud = big ? b.clws + (size_t)dst * fstride : nullptr;  // dst's global copy
                         if (part5 < 4) {
                             float4* s4 = reinterpret_cast<float4*>(Uf + (size_t)r * 16) + part5;
-                            *cl_map(s4, dst) = *s4;
+                            if (big) reinterpret_cast<float4*>(Ud + (size_t)r * 16)[part5] = *s4;
+                            else *cl_map(s4, dst) = *s4;
                         } else {
-                            *cl_map(rse + r, dst) = rse[r];
+                            if (big) reinterpret_cast<int*>(Ud + (size_t)24 * (n + 16))[r] = rse[r];
+                            else *cl_map(rse + r, dst) = rse[r];
                         }
                     }
                     if (tid < (int)R) *cl_map(slots + 3 * R + rank, (unsigned)tid) = (unsigned long long)flag_s;
@@ -585,8 +606,9 @@ __global__ void __launch_bounds__(256, 1) k_beam_cl(BeamArgs b) {
         if (factored) {
             float* g = b.minv + (size_t)rank * rmax * mld;
             const int nv = nr * mld / 4;
-            for (int q = tid; q < nv; q += nthr)
-                reinterpret_cast<float4*>(g)[q] = reinterpret_cast<const float4*>(minv)[q];
+            if (!big)  // the large-beam form formed its rows in place
+                for (int q = tid; q < nv; q += nthr)
+                    reinterpret_cast<float4*>(g)[q] = reinterpret_cast<const float4*>(minv)[q];
             for (int k = lo + tid; k < hi; k += nthr) b.minv_rse[k] = rse[k];
             if (rank == 0 && tid == 0) S->beam_fact = 1;
         }
@@ -598,11 +620,11 @@ __global__ void __launch_bounds__(256, 1) k_beam_cl(BeamArgs b) {
     // bytes), which its factor no longer needs; its row exponents, which it may still be
     // saving, start 96 (n + 16) > 80 L bytes in.  The third sum subtracts: its terms are
     // stored negated and added (s - a and s + (-a) round the same).
-    double* pcs = reinterpret_cast<double*>(cl_smem + Y.fact);
+    double* pcs = big ? reinterpret_cast<double*>(b.clws) : reinterpret_cast<double*>(cl_smem + Y.fact);
     if (!cl_up) { cl_sync(); cl_up = true; }
     {
         const int q0 = (int)(((long long)rank * ns) / R), q1 = (int)(((long long)(rank + 1) * ns) / R);
-        double* dst = cl_map(pcs, 0u);
+        double* dst = big ? pcs : cl_map(pcs, 0u);  // CTA 0's area (its global copy when big)
         for (int i = q0 + tid; i < q1; i += nthr) {
             double th, td;
             if (released) {
@@ -735,8 +757,9 @@ size_t beam_cluster_minv_floats(int ns, int R) {
 
 // The cluster size for a beam of ns nodes: 16 when the device places a 16-CTA cluster with
 // this kernel's shared memory and every CTA gets at least 8 rows, else 8 under the same
-// conditions, else 0 (the single-CTA kernel).  want caps it.
-int beam_cluster_setup(int ns, int want, size_t* smem_out) {
+// conditions, else 0 (the single-CTA kernel).  want caps it.  *big_out = 1 when only the
+// large-beam form (factor and M^-1 in global memory) fits.
+int beam_cluster_setup(int ns, int want, size_t* smem_out, int* big_out) {
     static std::mutex mu;
     std::lock_guard<std::mutex> lock(mu);
     int dev = 0, optin = 0;
@@ -747,36 +770,42 @@ int beam_cluster_setup(int ns, int want, size_t* smem_out) {
     static size_t cur = 0;
     for (int R = 16; R >= 8; R /= 2) {
         if (R > want || 2 * ns + 4 < 8 * R) continue;  // at least 8 rows per CTA
-        ClLayout Y;
-        cl_layout(ns, R, Y);
-        if (Y.total + fa.sharedSizeBytes > (size_t)optin) continue;
-        if (Y.total > cur) {
-            if (cudaFuncSetAttribute((const void*)k_beam_cl, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Y.total) != cudaSuccess) continue;
-            cur = Y.total;
+        for (int big = 0; big <= 1; ++big) {
+            ClLayout Y;
+            cl_layout(ns, R, Y, big != 0);
+            if (Y.total + fa.sharedSizeBytes > (size_t)optin) continue;
+            if (Y.total > cur) {
+                if (cudaFuncSetAttribute((const void*)k_beam_cl, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Y.total) != cudaSuccess) continue;
+                cur = Y.total;
+            }
+            if (R > 8 && cudaFuncSetAttribute((const void*)k_beam_cl, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) continue;
+            cudaLaunchConfig_t cfg = {};
+            cfg.gridDim = dim3(R);
+            cfg.blockDim = dim3(256);
+            cfg.dynamicSmemBytes = Y.total;
+            cudaLaunchAttribute at[1];
+            at[0].id = cudaLaunchAttributeClusterDimension;
+            at[0].val.clusterDim.x = R;
+            at[0].val.clusterDim.y = 1;
+            at[0].val.clusterDim.z = 1;
+            cfg.attrs = at;
+            cfg.numAttrs = 1;
+            int nclusters = 0;
+            if (cudaOccupancyMaxActiveClusters(&nclusters, (const void*)k_beam_cl, &cfg) != cudaSuccess || nclusters < 1) {
+                cudaGetLastError();
+                continue;
+            }
+            *smem_out = Y.total;
+            *big_out = big;
+            return R;
         }
-        if (R > 8 && cudaFuncSetAttribute((const void*)k_beam_cl, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) continue;
-        cudaLaunchConfig_t cfg = {};
-        cfg.gridDim = dim3(R);
-        cfg.blockDim = dim3(256);
-        cfg.dynamicSmemBytes = Y.total;
-        cudaLaunchAttribute at[1];
-        at[0].id = cudaLaunchAttributeClusterDimension;
-        at[0].val.clusterDim.x = R;
-        at[0].val.clusterDim.y = 1;
-        at[0].val.clusterDim.z = 1;
-        cfg.attrs = at;
-        cfg.numAttrs = 1;
-        int nclusters = 0;
-        if (cudaOccupancyMaxActiveClusters(&nclusters, (const void*)k_beam_cl, &cfg) != cudaSuccess || nclusters < 1) {
-            cudaGetLastError();
-            continue;
-        }
-        *smem_out = Y.total;
-        return R;
     }
     cudaGetLastError();
     return 0;
 }
+
+// Floats of the large-beam form's global factor copies (one a CTA).
+size_t beam_cluster_fact_floats(int ns, int R) { return (size_t)R * cl_fact_floats(ns); }
 
 void launch_beam_cluster(const BeamArgs& b, int R, size_t smem, cudaStream_t st, bool pdl) {
     cudaLaunchConfig_t cfg = {};

@@ -507,4 +507,110 @@ __device__ __forceinline__ void c2r_merge_m(C2<R>* buf, int bstride, const C2<R>
     __syncthreads();
 }
 
+// ---- the x direction's split steps on paired rows (FP32) -----------------------------------
+// A row of H complex values in the paired layout: element e is half e & 1 of the float4 slot
+// padp(e >> 1) (pair_slots(H) slots a row).  The arithmetic is that of r2c_split_m and
+// c2r_merge_m; nthr threads a row share the pairs (k, H - k).
+__device__ __forceinline__ float2& pel(float4* row, int e) {
+    return reinterpret_cast<float2*>(row + padp(e >> 1))[e & 1];
+}
+
+template <int H, int NB>
+__device__ __forceinline__ void r2c_split_p(float4* buf, int bstride, const float2* __restrict__ twr, int t, int nthr) {
+    for (int k = 1 + t; k < H / 2; k += nthr) {
+        const float2 wk = __ldg(&twr[k]), wm = __ldg(&twr[H - k]);
+#pragma unroll
+        for (int b = 0; b < NB; ++b) {
+            float4* bb = buf + b * bstride;
+            const float2 zk = pel(bb, k), zm = pel(bb, H - k);
+            float2 e = mk<float>(0.5f * (zk.x + zm.x), 0.5f * (zk.y - zm.y));
+            float2 d = mk<float>(zk.x - zm.x, zk.y + zm.y);
+            float2 o = mk<float>(0.5f * d.y, -0.5f * d.x);
+            float2 Xk = cadd<float>(e, cmul<float>(wk, o));
+            float2 e2 = mk<float>(0.5f * (zm.x + zk.x), 0.5f * (zm.y - zk.y));
+            float2 d2 = mk<float>(zm.x - zk.x, zm.y + zk.y);
+            float2 o2 = mk<float>(0.5f * d2.y, -0.5f * d2.x);
+            float2 Xm = cadd<float>(e2, cmul<float>(wm, o2));
+            pel(bb, k) = Xk;
+            pel(bb, H - k) = Xm;
+        }
+    }
+    if (t == 0) {
+#pragma unroll
+        for (int b = 0; b < NB; ++b) {
+            float4* bb = buf + b * bstride;
+            const float2 z0 = pel(bb, 0);
+            pel(bb, 0) = mk<float>(z0.x + z0.y, 0.f);
+            const float2 zh = pel(bb, H / 2);
+            pel(bb, H / 2) = mk<float>(zh.x, -zh.y);
+        }
+    }
+    __syncthreads();
+}
+
+template <int H, int NB>
+__device__ __forceinline__ void c2r_merge_p(float4* buf, int bstride, const float2* __restrict__ twr, int t, int nthr) {
+    for (int k = 1 + t; k < H / 2; k += nthr) {
+        const float2 wk = __ldg(&twr[k]), wm = __ldg(&twr[H - k]);
+#pragma unroll
+        for (int b = 0; b < NB; ++b) {
+            float4* bb = buf + b * bstride;
+            const float2 xk = pel(bb, k), xm = pel(bb, H - k);
+            float2 e = mk<float>(xk.x + xm.x, xk.y - xm.y);
+            float2 o = cmul<float>(mk<float>(xk.x - xm.x, xk.y + xm.y), mk<float>(wk.x, -wk.y));
+            float2 Zk = mk<float>(e.x - o.y, e.y + o.x);
+            float2 e2 = mk<float>(xm.x + xk.x, xm.y - xk.y);
+            float2 o2 = cmul<float>(mk<float>(xm.x - xk.x, xm.y + xk.y), mk<float>(wm.x, -wm.y));
+            float2 Zm = mk<float>(e2.x - o2.y, e2.y + o2.x);
+            pel(bb, k) = Zk;
+            pel(bb, H - k) = Zm;
+        }
+    }
+    if (t == 0) {
+#pragma unroll
+        for (int b = 0; b < NB; ++b) {
+            float4* bb = buf + b * bstride;
+            const float2 x0 = pel(bb, 0);
+            pel(bb, 0) = mk<float>(x0.x, x0.x);
+            const float2 xh = pel(bb, H / 2);
+            pel(bb, H / 2) = mk<float>(2.f * xh.x, -2.f * xh.y);
+        }
+    }
+    __syncthreads();
+}
+
+// Paired row transforms with the values in registers: v[b][2m + h] = element 2u + h + m (H/8)
+// of row b (u < H/16).  c2r: merge in the rows (loaded by the caller, synchronised), then the
+// inverse transform to registers; the rows are free on return.  r2c: the forward transform of
+// registers into the rows, then the split; the rows must be free when called.
+template <int H, int NB, int NBA>
+__device__ __forceinline__ void row_c2r_reg2(float4* rb, int bstride, const float2* __restrict__ twR,
+                                             const float2* __restrict__ twX, int u, float2 (&v)[NBA][16]) {
+    constexpr int HG = H / 16;
+    c2r_merge_p<H, NB>(rb, bstride, twR, u, HG);
+#pragma unroll
+    for (int b = 0; b < NB; ++b)
+#pragma unroll
+        for (int m = 0; m < 8; ++m) {
+            const float4 q = rb[b * bstride + padp(u + m * HG)];
+            v[b][2 * m] = make_float2(q.x, q.y);
+            v[b][2 * m + 1] = make_float2(q.z, q.w);
+        }
+    __syncthreads();
+    block_fft2_m<H, true, NB>(v, rb, bstride, twX, u);
+}
+template <int H, int NB, int NBA>
+__device__ __forceinline__ void row_r2c_reg2(float2 (&v)[NBA][16], float4* rb, int bstride,
+                                             const float2* __restrict__ twR, const float2* __restrict__ twX, int u) {
+    constexpr int HG = H / 16;
+    block_fft2_m<H, false, NB>(v, rb, bstride, twX, u);
+#pragma unroll
+    for (int b = 0; b < NB; ++b)
+#pragma unroll
+        for (int m = 0; m < 8; ++m)
+            rb[b * bstride + padp(u + m * HG)] = make_float4(v[b][2 * m].x, v[b][2 * m].y, v[b][2 * m + 1].x, v[b][2 * m + 1].y);
+    __syncthreads();
+    r2c_split_p<H, NB>(rb, bstride, twR, u, HG);
+}
+
 }  // namespace fsibe

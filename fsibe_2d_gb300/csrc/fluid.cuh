@@ -971,6 +971,174 @@ __global__ void __launch_bounds__(XRows<R, H, TRV>::THREADS,
     }
 }
 
+// ---- k_press_x on paired rows (FP32) ---------------------------------------------------------
+// The same work as k_press_x's FP32 form (the stresses in their own kernel), with the row
+// transforms of the paired engine: H/16 threads a row, each holding two adjacent butterflies,
+// 16-byte exchanges between the stages.  Rows of pair_slots(H) float4 slots; element e of a row
+// sits at half e & 1 of slot padp(e >> 1).
+template <int H, int TR>
+struct XPairs {
+    static constexpr int U = H / 16;                 // threads a row
+    static constexpr int THREADS = U * TR;
+    static constexpr int PS = pair_slots(H);         // float4 slots a row
+    // three 128-thread blocks an SM: up to 170 registers a thread (the pairs' transforms of two
+    // rows and the elementwise state need about 160)
+    static constexpr int MINB = 3;
+};
+// The tile height of the paired kernel: 128 threads a block (H / 16 a row), at least one row.
+template <int H>
+constexpr int xpairs_rows() {
+    return (128 / (H / 16)) > 0 ? 128 / (H / 16) : 1;
+}
+
+template <int H, int TR>
+__device__ __forceinline__ void load_tileP(float4* buf, const float2* __restrict__ T, int ny, int iy0, int kmax) {
+    constexpr int PS = pair_slots(H);
+    for (int i = threadIdx.x; i < H * TR; i += blockDim.x) {
+        const int r = i % TR, kx = i / TR;
+        pel(buf + r * PS, kx) = (kx < kmax) ? T[(size_t)kx * ny + iy0 + r] : make_float2(0.f, 0.f);
+    }
+}
+
+template <int H, int TR>
+__global__ void __launch_bounds__(XPairs<H, TR>::THREADS, XPairs<H, TR>::MINB) k_press_x2(KArgs<float> a) {
+    pdl_wait();     // the previous kernel of the stream has completed
+    using X = XPairs<H, TR>;
+    constexpr int G = H / 8, HG = X::U;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float4* bufA = reinterpret_cast<float4*>(smem_raw);
+    constexpr int BS = TR * X::PS;  // one row buffer (TR rows)
+    float4* bufB = bufA + BS;
+    float4* bufC = bufB + BS;
+    __shared__ double red_s[RED_NSLOTS][X::THREADS / 32 > 2 ? X::THREADS / 32 : 2];
+    static_assert((RED_NSLOTS + 1) * 4 * X::THREADS <= BS * 16, "the reduction columns fit the spare row buffer");
+    const int r = threadIdx.x / HG, u = threadIdx.x % HG;
+    const int iy0 = blockIdx.x * TR, ny = a.g.ny;
+    float4* ra = bufA + r * X::PS;
+    const DevScalars* S = a.S;
+    const double time = S->time, dt1 = S->dt1;
+    const int ixmin = S->win[0], ixmax = S->win[1], iymin = S->win[2], iymax = S->win[3];
+
+    load_tileP<H, TR>(bufA, a.Tu, ny, iy0, a.kcut);
+    load_tileP<H, TR>(bufB, a.Tv, ny, iy0, a.kcut);
+    load_tileP<H, TR>(bufC, a.Tw, ny, iy0, a.kcut);
+    __syncthreads();
+    // u and v together, then omega (three rows at once would not fit 128 registers):
+    // v[f][2m + h] = element 2u + h + m G (the rows are free afterwards)
+    float2 uvw[2][16], ww[1][16];
+    row_c2r_reg2<H, 2>(ra, BS, a.twR, a.twX, u, uvw);
+    row_c2r_reg2<H, 1>(ra + 2 * BS, BS, a.twR, a.twX, u, ww);
+    float2 pxy[2][16];  // the pressure right-hand side's x and y parts, for the forward transform
+
+    const int iy = iy0 + r;
+    const size_t roff = (size_t)iy * H;
+    float2* u2 = reinterpret_cast<float2*>(a.u) + roff;
+    float2* v2 = reinterpret_cast<float2*>(a.v) + roff;
+    float2* vm2 = reinterpret_cast<float2*>(a.vor_mean) + roff;
+    const float2* k2 = reinterpret_cast<const float2*>(a.mask) + roff;
+    const float2* x2 = reinterpret_cast<const float2*>(a.mvx) + roff;
+    const float2* y2 = reinterpret_cast<const float2*>(a.mvy) + roff;
+    const bool in_rows = (iy >= iymin && iy <= iymax);
+    const double Ud = S->mean_u_next, Vd = S->mean_v_next;
+    // stored velocity is the perturbation u' (the mean flow U, V kept in FP64 scalars); per-thread
+    // partial sums in FP32 over 32 cells, FP64 across threads and blocks
+    float f[RED_NSLOTS];
+#pragma unroll
+    for (int s = 0; s < RED_NSLOTS; ++s) f[s] = 0.f;
+    float spx = 0.f, spy = 0.f;
+    const float Uf = (float)Ud, Vf = (float)Vd;
+    const float ca = (float)(time / (time + dt1)), cb = (float)(dt1 / (time + dt1));
+#pragma unroll
+    for (int m = 0; m < 8; ++m) {
+        const int e0 = 2 * u + m * G;  // elements e0 and e0 + 1: 16-byte accesses of the rows
+        const float4 kk4 = *reinterpret_cast<const float4*>(k2 + e0), mx4 = *reinterpret_cast<const float4*>(x2 + e0);
+        const float4 my4 = *reinterpret_cast<const float4*>(y2 + e0), vm4 = *reinterpret_cast<const float4*>(vm2 + e0);
+        float out_u[4], out_v[4], out_vm[4];
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const float2 ur = uvw[0][2 * m + h], vr = uvw[1][2 * m + h], w = ww[0][2 * m + h];
+            const float upc[2] = {ur.x, ur.y}, vpc[2] = {-vr.x, -vr.y}, wc[2] = {w.x, w.y};
+            const float kc[2] = {h ? kk4.z : kk4.x, h ? kk4.w : kk4.y};
+            const float xc[2] = {h ? mx4.z : mx4.x, h ? mx4.w : mx4.y};
+            const float yc[2] = {h ? my4.z : my4.x, h ? my4.w : my4.y};
+            const float vmc[2] = {h ? vm4.z : vm4.x, h ? vm4.w : vm4.y};
+            float px[2], py[2];
+#pragma unroll
+            for (int e = 0; e < 2; ++e) {
+                const int ix = 2 * (e0 + h) + e;
+                const float uc = upc[e] + Uf, vc = vpc[e] + Vf;
+                const float rx = uc - xc[e], ry = vc - yc[e];
+                const float penx = kc[e] * rx, peny = kc[e] * ry;
+                f[RED_OMEGA2] += wc[e] * wc[e];
+                f[RED_KIN] += upc[e] * upc[e] + vpc[e] * vpc[e];
+                f[RED_POROUS] += kc[e] * (rx * rx + ry * ry);
+                f[RED_INFLOW_SOLID] += kc[e] * (xc[e] * rx + yc[e] * ry);
+                spx += penx;
+                spy += peny;
+                f[RED_SUM_U] += uc;
+                f[RED_SUM_V] += vc;
+                f[RED_UMAX2] = fmaxf(f[RED_UMAX2], uc * uc + vc * vc);
+                if (in_rows && ix >= ixmin && ix <= ixmax) {
+                    f[RED_DRAG_X] += penx;
+                    f[RED_DRAG_Y] += peny;
+                    f[RED_UNST_X] += xc[e] * kc[e];
+                    f[RED_UNST_Y] += yc[e] * kc[e];
+                }
+                out_u[2 * h + e] = upc[e];
+                out_v[2 * h + e] = vpc[e];
+                out_vm[2 * h + e] = vmc[e] * ca + wc[e] * cb;
+                px[e] = penx - wc[e] * vc;
+                py[e] = peny + wc[e] * uc;
+            }
+            pxy[0][2 * m + h] = make_float2(px[0], px[1]);
+            pxy[1][2 * m + h] = make_float2(py[0], py[1]);
+        }
+        *reinterpret_cast<float4*>(u2 + e0) = make_float4(out_u[0], out_u[1], out_u[2], out_u[3]);
+        *reinterpret_cast<float4*>(v2 + e0) = make_float4(out_v[0], out_v[1], out_v[2], out_v[3]);
+        *reinterpret_cast<float4*>(vm2 + e0) = make_float4(out_vm[0], out_vm[1], out_vm[2], out_vm[3]);
+    }
+    // the FP32 partials go to the spare row buffer; the block reduces them in FP64 in a fixed
+    // order (one warp a column)
+    float* cols = reinterpret_cast<float*>(bufC);
+#pragma unroll
+    for (int s = 0; s < RED_NSLOTS; ++s) cols[s * X::THREADS + threadIdx.x] = (s == RED_INFLOW_MEAN) ? spx : f[s];
+    cols[RED_NSLOTS * X::THREADS + threadIdx.x] = spy;
+    __syncthreads();
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    constexpr int NW = X::THREADS / 32;
+    for (int cidx = w; cidx < RED_NSLOTS + 1; cidx += NW) {
+        const bool mx = cidx == RED_UMAX2;
+        double v = 0.0;
+        for (int i = l; i < X::THREADS; i += 32) {
+            const double x = (double)cols[cidx * X::THREADS + i];
+            v = mx ? fmax(v, x) : v + x;
+        }
+        v = mx ? warp_max(v) : warp_sum<float>(v);
+        if (l == 0) {
+            if (cidx < RED_NSLOTS) red_s[cidx][0] = v;
+            else red_s[RED_INFLOW_MEAN][1] = v;  // the sum of spy (spx is in column INFLOW_MEAN)
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x < RED_NSLOTS) {
+        const int s = threadIdx.x;
+        double v = red_s[s][0];
+        if (s == RED_INFLOW_MEAN) v = Ud * red_s[s][0] + Vd * red_s[s][1];
+        a.red[(size_t)blockIdx.x * RED_NSLOTS + s] = v;
+        if (blockIdx.x == 0 && s == 0) a.S->nred = (int)gridDim.x;
+    }
+    if (a.pressure_on) {
+        row_r2c_reg2<H, 2>(pxy, ra, BS, a.twR, a.twX, u);  // x and y parts together (buffers A and B)
+        for (int i = threadIdx.x; i < H * TR; i += blockDim.x) {
+            const int rr = i % TR, kx = i / TR;
+            const float kxs = (float)((double)kx * a.g.kxs);
+            const size_t o = (size_t)kx * ny + iy0 + rr;
+            a.P1[o] = cimul<float>(pel(bufA + rr * X::PS, kx), kxs);
+            a.P2[o] = pel(bufB + rr * X::PS, kx);
+        }
+    }
+}
+
 // The viscous stresses (NavierStokes.f90:354-370: 2 nu d2psi/dxdy, nu (d2psi/dy2 - d2psi/dx2))
 // to physical space, beside k_press_x on another stream: only GetForces reads them.  With
 // a.srows set, a block whose rows no stencil of the forces reaches (rows j - 4 .. j + 4 of the
@@ -1110,6 +1278,12 @@ __global__ void __launch_bounds__(XRows<R, H, TRV>::THREADS, (xminb<MB, 1>())) k
     C2<R>* buf = reinterpret_cast<C2<R>*>(smem_raw);
     const int r = threadIdx.x / X::G, t = threadIdx.x % X::G;
     const int iy0 = blockIdx.x * X::TR, ny = a.g.ny;
+    // in the fused step only the rows the forces' stencils reach (k_step_begin's S->srow, as
+    // in k_stress_x); the host forms the other rows when the whole field is read
+    if (a.srows) {
+        const int j0 = a.S->srow[0], j1 = a.S->srow[1];
+        if (iy0 + X::TR - 1 < j0 || iy0 > j1) return;
+    }
     C2<R>* rb = buf + r * X::PL;
     const size_t roff = (size_t)(iy0 + r) * H;
     const C2<R>* u2 = reinterpret_cast<const C2<R>*>(a.u) + roff;
@@ -1167,6 +1341,7 @@ struct SizeKernels {
         void (*press_x)(KArgs<R>);
         void (*press_fin)(KArgs<R>);
     } xv[4];  // [0..2]: half, the default and twice the default tile height; [3]: the default, two blocks an SM
+    XVariant xp;  // FP32: k_press_x on paired rows (press_x only; null in the FP64 form)
     // y-pass kernels for NY
     void (*yfwd)(KArgs<R>);
     void (*yinv)(KArgs<R>);
@@ -1230,6 +1405,17 @@ inline void fill_size_kernels(SizeKernels<R>& k) {
     // the default tile with the registers capped for two resident blocks (when two fit an SM)
     constexpr int MB2 = (2 * XRows<R, H, T1>::THREADS <= 2048) ? 2 : 1;
     fill_xvariant<R, H, T1, MB2>(k.xv[3]);
+    k.xp = typename SizeKernels<R>::XVariant{};
+    if constexpr (kIsF32<R>) {
+        constexpr int TP = xpairs_rows<H>();
+        k.xp.rows = TP;
+        k.xp.threads = XPairs<H, TP>::THREADS;
+        k.xp.smem3 = 3 * TP * pair_slots(H) * 16;
+        k.xp.smem1 = k.xp.smem3 / 3;
+        k.xp.minb = 16;  // the marker of the paired kernel in fsibe_tile_config
+        k.xp.press_x = k_press_x2<H, TP>;
+        cudaFuncSetAttribute(k_press_x2<H, TP>, cudaFuncAttributeMaxDynamicSharedMemorySize, k.xp.smem3);
+    }
     k.nl_x = k.xv[1].nl_x;
     k.press_x = k.xv[1].press_x;
     k.press_fin = k.xv[1].press_fin;

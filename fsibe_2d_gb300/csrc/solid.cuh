@@ -226,6 +226,8 @@ struct BeamArgs {
     int row_cap;
     float* minv;     // cluster form: the rows of the preconditioner inverse, one slice per CTA
     int* minv_rse;   // cluster form: the row-scale exponents of those rows
+    int cl_big;      // cluster form for large beams: the factor and M^-1 in global memory
+    float* clws;     // its per-CTA factor copies (beam_cluster_fact_floats)
     int fuse_adv;    // cluster form: 1 = also end the time step (advance_state with adv)
     AdvArgs adv;
 };

@@ -273,10 +273,12 @@ int fsibe_beam_phase_cycles(fsibe_ctx* ctx, long long* out32, int reset);
 /* Rows per block chosen by the autotuner for the fused x-pass kernels (nl_x, press_x,
  * press_fin).  fsibe_create times four candidates per kernel on the new context's buffers --
  * half, the default and twice the default tile height, and the default tile with its
- * registers capped for two resident blocks an SM -- and keeps the fastest (cached per
+ * registers capped for two resident blocks an SM -- and, for press_x in the FP32 form, the
+ * paired kernel (two adjacent butterflies a thread) -- and keeps the fastest (cached per
  * precision and grid size for the process; FSIBE_AUTOTUNE=0 in the environment keeps the
- * defaults).  fsibe_tile_config gives the rows and the blocks-per-SM bound (0: the kernel's
- * default) of each: out6 = {rows, bound} for nl_x, press_x, press_fin. */
+ * defaults; FSIBE_PX_PAIRED=1 / 0 forces / forbids the paired press_x).  fsibe_tile_config
+ * gives the rows and the blocks-per-SM bound (0: the kernel's default; 16 marks the paired
+ * press_x) of each: out6 = {rows, bound} for nl_x, press_x, press_fin. */
 int fsibe_tiles(fsibe_ctx* ctx, int32_t* rows3);
 int fsibe_tile_config(fsibe_ctx* ctx, int32_t* out6);
 

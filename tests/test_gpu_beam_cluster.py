@@ -44,6 +44,26 @@ def test_cluster_form_matches_single_cta_form(monkeypatch, n, ns, steps, prec):
     a.close(); s.close()
 
 
+@pytest.mark.parametrize("n,ns,steps", [(512, 512, 12), (1024, 1024, 12)])
+def test_large_beam_cluster_form_matches_single_cta_form(monkeypatch, n, ns, steps):
+    """ns >= 512: the factor and M^-1 exceed a CTA's shared memory; the cluster form keeps them
+    in global memory (L2-resident) and must agree with the single-CTA form as at small ns."""
+    p = make_params(nx=n, ny=n, ns=ns, Re=500.0, dt=5e-5)
+    w = seeded_vorticity(n, seed=1)
+    a, ra = _run(p, w, steps, monkeypatch, None)
+    s, rs = _run(p, w, steps, monkeypatch, 0)
+    assert a.beam_cluster() in (8, 16) and s.beam_cluster() == 0
+    assert rel(a.beam()[0], s.beam()[0]) < 1e-12
+    assert rel(a.vortk(), s.vortk()) < 1e-12
+    # the rows: both forms stop Newton at the 1e-10 tolerance, and at ns = 1024 the rates
+    # (theta_dot, the tip velocity: differences over dt) carry that to 2e-10 of their column
+    scale = np.abs(rs).max(axis=0) + 1e-12
+    assert (np.abs(ra - rs) / scale).max() < 1e-9
+    sa, ss = a.scalars(), s.scalars()
+    assert sa.status == 0 and ss.status == 0 and sa.newton_iters == ss.newton_iters
+    a.close(); s.close()
+
+
 def test_cluster_sizes_agree(monkeypatch):
     """16 and 8 CTAs split the rows differently; the results agree to refinement rounding."""
     n, ns, steps = 256, 64, 30
