@@ -121,8 +121,10 @@ class ClockSampler:
 #   press_y   R P1, P2                   W Tq
 #   press_fin R Tq, u, v                 W press
 # (nl_pen and stress_x touch only the rows near the beam.)
+# (k_press_fin has no line: in the step it forms only the rows the forces' stencils reach, so
+# its bytes depend on where the beam is)
 PASSES = {"nl_y": lambda f: 12 * f + 3, "nl_adv": lambda f: 4 * f + 2, "nl_x": lambda f: 4 * f + 5,
-          "press_x": lambda f: 3 * f + 9, "press_y": lambda f: 3, "press_fin": lambda f: 4}
+          "press_x": lambda f: 3 * f + 9, "press_y": lambda f: 3}
 
 
 def kcut_fraction(nx, ny):

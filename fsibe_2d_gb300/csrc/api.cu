@@ -447,6 +447,8 @@ struct fsibe_ctx {
     double* fterm = nullptr;
     double* rows = nullptr;
     bool press_partial = false;  // the last fused step formed the pressure on the forces' rows only
+    bool adv_ready = false;      // the next step's advection part ran (launched by the previous fused step)
+    bool adv_pipe = false;       // fused steps launch the next step's advection part (from 2048^2)
     void* snap = nullptr;   // ComputePressureSnapshot's workspace (5 fields and 2 spectra of R), on first use
     int rows_cap = 0;
     double* etab = nullptr;       // integrating-factor tables (hx + ny/2 + 1)
@@ -775,8 +777,13 @@ static void nl_advect_t(fsibe_ctx* c, int explicit_step) {
 // EvolveFluidExplicit / EvolveFluidAB2 + pressure (NavierStokes.f90:422-508, 273-403)
 // stress_rows: the forces that follow use this beam state, so k_stress_x may leave the rows
 // their stencils cannot reach
+// adv_forked: the advection part of k_nl_x ran on the second side stream (ev_adv: this step's
+// launch, joined here; or, with adv_prev, the previous step's launch, already ordered before
+// this step).  adv_next: launch the next step's advection part on that stream after the
+// fluid step's scalars, beside the pressure, the forces and the beam (the caller joins it).
 template <typename R>
-static int fluid_step_t(fsibe_ctx* c, int explicit_step, bool adv_forked = false, bool stress_rows = false) {
+static int fluid_step_t(fsibe_ctx* c, int explicit_step, bool adv_forked = false, bool stress_rows = false,
+                        bool adv_prev = false, bool adv_next = false) {
     KArgs<R> a = kargs<R>(c);
     SizeKernels<R>& KX = kx_of<R>(c);
     SizeKernels<R>& KY = ky_of<R>(c);
@@ -797,7 +804,7 @@ static int fluid_step_t(fsibe_ctx* c, int explicit_step, bool adv_forked = false
     if (adv_forked) {
         // the advection part ran beside the mask kernels: add the penalization on the rows
         // of the mask's box
-        CK(c, cudaStreamWaitEvent(c->stream, c->ev_adv, 0));
+        if (!adv_prev) CK(c, cudaStreamWaitEvent(c->stream, c->ev_adv, 0));
         KArgs<R> p = a;
         // walls, sponges and the outflow sponge's integral: every row is penalized
         p.rect = (c->full_mask || c->s10) ? c->rect_full : c->rect;
@@ -838,6 +845,13 @@ static int fluid_step_t(fsibe_ctx* c, int explicit_step, bool adv_forked = false
     prof_end(c, c->side2);
     CK(c, cudaEventRecord(c->ev_ffj, c->side2));
     c->launches++;
+    if (adv_next) {
+        // the next step's advection part: it reads this step's new state (u, v from k_press_x,
+        // the vorticity's derivatives from k_nl_y, the mean flow k_fluid_finish just stored) and
+        // writes the spectra A, B, which k_nl_y has consumed
+        nl_advect_t<R>(c, 0);
+        CK(c, cudaEventRecord(c->ev_adv, c->side2));
+    }
     if (a.pressure_on) {
         launch_y<R>(c, KY.press_y, KY.y_smem2, a, "press_y", 1, true, KY.press_y_threads);
         KArgs<R> f = a;
@@ -851,9 +865,10 @@ static int fluid_step_t(fsibe_ctx* c, int explicit_step, bool adv_forked = false
     return FSIBE_OK;
 }
 
-static int fluid_step(fsibe_ctx* c, int explicit_step, bool adv_forked = false, bool stress_rows = false) {
-    return c->fp32 ? fluid_step_t<float>(c, explicit_step, adv_forked, stress_rows)
-                   : fluid_step_t<double>(c, explicit_step, adv_forked, stress_rows);
+static int fluid_step(fsibe_ctx* c, int explicit_step, bool adv_forked = false, bool stress_rows = false,
+                      bool adv_prev = false, bool adv_next = false) {
+    return c->fp32 ? fluid_step_t<float>(c, explicit_step, adv_forked, stress_rows, adv_prev, adv_next)
+                   : fluid_step_t<double>(c, explicit_step, adv_forked, stress_rows, adv_prev, adv_next);
 }
 
 static MaskArgs mask_args(fsibe_ctx* c) {
@@ -1066,11 +1081,17 @@ static int step_body(fsibe_ctx* c, int explicit_step) {
     // second side stream beside the mask kernels; the forces' interpolation geometry, which
     // needs only the beam state, follows it there and runs beside the fluid step
     const bool split = mask && P.iBeam > 0 && c->nl_split;
+    // the advection part is pipelined: each fused step launches the next step's beside its own
+    // pressure and beam; a step that finds none ready (the first, or after the host changed the
+    // state) launches its own first
+    const bool adv_prev = split && c->adv_ready;
+    const bool adv_next = split && c->adv_pipe;
+    c->adv_ready = false;
     if (split || forces) {
         CK(c, cudaEventRecord(c->ev_geo, c->stream));
         CK(c, cudaStreamWaitEvent(c->side2, c->ev_geo, 0));
     }
-    if (split) {
+    if (split && !adv_prev) {
         if (c->fp32) nl_advect_t<float>(c, explicit_step);
         else nl_advect_t<double>(c, explicit_step);
         CK(c, cudaEventRecord(c->ev_adv, c->side2));
@@ -1080,7 +1101,7 @@ static int step_body(fsibe_ctx* c, int explicit_step) {
         CK(c, cudaEventRecord(c->ev_geo, c->side2));
     }
     if (mask) { st = create_mask(c, !moving); if (st) return st; }
-    st = fluid_step(c, explicit_step, split, forces);
+    st = fluid_step(c, explicit_step, split, forces, adv_prev, adv_next);
     if (st) return st;
     if (forces) { st = get_forces(c, true); if (st) return st; }
     bool advanced = false;
@@ -1091,7 +1112,23 @@ static int step_body(fsibe_ctx* c, int explicit_step) {
         c->launches++;
         CKL(c);
     }
-    return advanced ? FSIBE_OK : advance(c);
+    st = advanced ? FSIBE_OK : advance(c);
+    if (st) return st;
+    if (adv_next) {
+        // join the next step's advection part: what follows on the main stream (the next step)
+        // is ordered after it
+        CK(c, cudaStreamWaitEvent(c->stream, c->ev_adv, 0));
+        c->adv_ready = true;
+    }
+    return FSIBE_OK;
+}
+
+// The fused step pipelines the advection part (step_body): true when its graph expects the
+// previous step to have launched it.
+static bool adv_pipelined(const fsibe_ctx* c) {
+    const fsibe_params& P = c->P;
+    const bool mask = P.iFLUSI == 1 || P.iMotion > 0 || P.iSponge >= 4;
+    return mask && P.iBeam > 0 && c->nl_split && c->adv_pipe;
 }
 
 static int do_step(fsibe_ctx* c) {
@@ -1103,7 +1140,9 @@ static int do_step(fsibe_ctx* c) {
         c->startup_done = true;
         return FSIBE_OK;
     }
-    if (c->use_graph) {
+    // the graph is the steady step: the previous step launched this one's advection part; a
+    // step after the host changed the state runs directly once
+    if (c->use_graph && (!adv_pipelined(c) || c->adv_ready)) {
         if (!c->graph_ready) {
             CK(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
             const int before = c->launches;
@@ -1113,12 +1152,13 @@ static int do_step(fsibe_ctx* c) {
             if (st) return st;
             if (e != cudaSuccess) { c->err = std::string("capture: ") + cudaGetErrorString(e); return FSIBE_ERR_CUDA; }
             c->graph = g;
-            CK(c, cudaGraphInstantiate(&c->gexec, g, 0));
+            CK(c, cudaGraphInstantiate(&c->gexec, g, cudaGraphInstantiateFlagUseNodePriority));
             c->graph_ready = true;
             c->launches = before;
         }
         CK(c, cudaGraphLaunch(c->gexec, c->stream));
         c->launches += 0;
+        c->adv_ready = adv_pipelined(c);  // the graph launched the next step's advection part
         return FSIBE_OK;
     }
     return step_body(c, 0);
@@ -1419,7 +1459,9 @@ static int autotune_x(fsibe_ctx* c) {
             const float t = time_xv<R>(c, kind, K.xv[v]);
             if (t < 0.97f * tbest) { tbest = t; best = v; }
         }
-        if (kind == 1 && K.xp.press_x) {  // FP32: the paired press_x (index 4)
+        // FP32: the paired press_x (index 4), when its tile (128 threads: 128 / (H/16) rows)
+        // divides the grid's rows
+        if (kind == 1 && K.xp.press_x && c->g.ny % K.xp.rows == 0) {
             const float t = time_xv<R>(c, kind, K.xp);
             if (t < 0.97f * tbest) { tbest = t; best = 4; }
         }
@@ -1576,6 +1618,7 @@ int fsibe_create(const fsibe_params* p, fsibe_ctx** out) {
         c->pdl = !(e && std::atoi(e) == 0);
         e = std::getenv("FSIBE_STRESS_SPLIT");
         c->stress_split = !(e && std::atoi(e) == 0);
+
     }
     ALLOC(c->prims, sizeof(Prim) * (size_t)(2 * ns + 8));
     ALLOC(c->nprims, 16);
@@ -1663,7 +1706,21 @@ int fsibe_create(const fsibe_params* p, fsibe_ctx** out) {
         cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, dev);
         if (c->nsm <= 0) c->nsm = 152;
     }
-    cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    // with the advection part pipelined, the main stream has the greatest priority and the
+    // second side stream the least: the next step's advection part then fills the SMs that the
+    // pressure and beam kernels leave, without holding them back (the graph keeps the
+    // priorities: cudaGraphInstantiateFlagUseNodePriority)
+    int prio_lo = 0, prio_hi = 0;
+    cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi);
+    {
+        // on by default from 2048^2 on, where the advection part outlasts the mask kernels it
+        // otherwise runs beside (4096^2: the step 1.61 -> 1.46 ms); at 1024^2 it is hidden there
+        // already and the pipelined form was 2.5% slower.  FSIBE_ADV_PIPE = 0 / 1 overrides.
+        const char* pe = std::getenv("FSIBE_ADV_PIPE");
+        c->adv_pipe = pe ? std::atoi(pe) != 0 : (long long)p->nx * p->ny >= 2048LL * 2048LL;
+    }
+    if (!c->adv_pipe) prio_lo = prio_hi = 0;
+    cudaError_t e = cudaStreamCreateWithPriority(&c->stream, cudaStreamNonBlocking, prio_hi);
     if (e != cudaSuccess) { g_err = cudaGetErrorString(e); fsibe_destroy(c); return FSIBE_ERR_CUDA; }
     c->own_stream = true;
     cudaEventCreate(&c->ev0);
@@ -1672,7 +1729,7 @@ int fsibe_create(const fsibe_params* p, fsibe_ctx** out) {
     if (e != cudaSuccess) { g_err = cudaGetErrorString(e); fsibe_destroy(c); return FSIBE_ERR_CUDA; }
     cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming);
     cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming);
-    e = cudaStreamCreateWithFlags(&c->side2, cudaStreamNonBlocking);
+    e = cudaStreamCreateWithPriority(&c->side2, cudaStreamNonBlocking, prio_lo);
     if (e != cudaSuccess) { g_err = cudaGetErrorString(e); fsibe_destroy(c); return FSIBE_ERR_CUDA; }
     cudaEventCreateWithFlags(&c->ev_ff, cudaEventDisableTiming);
     cudaEventCreateWithFlags(&c->ev_ffj, cudaEventDisableTiming);
@@ -1687,7 +1744,7 @@ int fsibe_create(const fsibe_params* p, fsibe_ctx** out) {
         // FSIBE_PX_PAIRED = 1 / 0 forces / forbids the paired FP32 press_x (tests of both forms)
         const char* pe = std::getenv("FSIBE_PX_PAIRED");
         if (pe && c->fp32) {
-            if (pe[0] == '1') c->xv_px = 4;
+            if (pe[0] == '1' && c->g.ny % c->kxf.xp.rows == 0) c->xv_px = 4;
             else if (pe[0] == '0' && c->xv_px == 4) c->xv_px = 1;
         }
     }
@@ -1765,6 +1822,7 @@ static int init_state(fsibe_ctx* c, const double* vort, bool keep_mask) {
     const size_t NN = (size_t)c->g.nx * c->g.ny;
     const size_t rs = c->fp32 ? 4 : 8;
     free_graph(c);
+    c->adv_ready = false;  // a new state: the next step forms its own advection part
     int st = from_host(c, vort, NN, c->phys[PH_0]);
     if (st) return st;
     for (int q : {SP_W, SP_M, SP_WLO}) CK(c, cudaMemsetAsync(c->spec[q], 0, rs * NN, c->stream));
@@ -1826,6 +1884,7 @@ static int read_status(fsibe_ctx* c) {
 int fsibe_fluid_step(fsibe_ctx* c, int explicit_step) {
     if (!c) return FSIBE_ERR_PARAM;
     if (!c->initialized) return FSIBE_ERR_STATE;
+    c->adv_ready = false;  // the routine's fluid step forms its nonlinear term whole
     int st = fluid_step(c, explicit_step ? 1 : 0);
     if (st) return st;
     return read_status(c);
@@ -1903,7 +1962,9 @@ int fsibe_run_records(fsibe_ctx* c, int nsteps, double* records) {
 
 // ---- state transfer -------------------------------------------------------------------
 int fsibe_upload_vortk(fsibe_ctx* c, const double* v) {
-    return c ? packed_to_spec(c, v, c->spec[SP_W], c->fp32 ? c->spec[SP_WLO] : nullptr) : FSIBE_ERR_PARAM;
+    if (!c) return FSIBE_ERR_PARAM;
+    c->adv_ready = false;
+    return packed_to_spec(c, v, c->spec[SP_W], c->fp32 ? c->spec[SP_WLO] : nullptr);
 }
 int fsibe_download_vortk(fsibe_ctx* c, double* v) {
     return c ? spec_to_packed(c, c->spec[SP_W], v, c->fp32 ? c->spec[SP_WLO] : nullptr) : FSIBE_ERR_PARAM;
@@ -1923,6 +1984,7 @@ int fsibe_download_vort(fsibe_ctx* c, double* v) {
 // The FP32 form stores u - U (U = mean flow of that velocity, kept as FP64 scalars).
 int fsibe_upload_u(fsibe_ctx* c, const double* u) {
     if (!c) return FSIBE_ERR_PARAM;
+    c->adv_ready = false;
     const size_t NN = (size_t)c->g.nx * c->g.ny;
     const double* ou = c->fp32 ? &c->S->mean_u_cur : nullptr;
     const double* ov = c->fp32 ? &c->S->mean_v_cur : nullptr;
@@ -2138,6 +2200,7 @@ int fsibe_write_backup(fsibe_ctx* c, const char* path) {
 // start-up step follows.  The velocity statistics of the first step come from the file's u.
 int fsibe_read_backup(fsibe_ctx* c, const char* path) {
     if (!c || !path) return FSIBE_ERR_PARAM;
+    c->adv_ready = false;
     const size_t NN = (size_t)c->g.nx * c->g.ny, ns = (size_t)c->P.ns;
     BackupIn in;
     in.f = std::fopen(path, "rb");
@@ -2673,6 +2736,7 @@ static int adj_check(fsibe_ctx* c, int nsteps, int avg_from) {
 
 // state 0 from vort0 (the mask kept), nu set, the drag window known
 static int adj_begin(fsibe_ctx* c, int comp, const double* vort0, double nu, int nsteps, int avg_from, int nslots) {
+    c->adv_ready = false;  // the adjoint's runs replace the state
     int st = adj_alloc(c, nslots);
     if (st) return st;
     AdjWork* w = c->adj;
@@ -2855,7 +2919,8 @@ static int ens_step(fsibe_ensemble* e) {
     bool started = true;
     for (fsibe_ctx* c : e->runs) {
         if (!c->initialized) { e->err = "ensemble step before init_fields of every run"; g_err = e->err; return FSIBE_ERR_STATE; }
-        started = started && c->startup_done;
+        // a run whose next advection part is not in place steps directly once (do_step's rule)
+        started = started && c->startup_done && (!adv_pipelined(c) || c->adv_ready);
     }
     if (!started) {
         // the Euler start-up steps, each run on its own stream
@@ -2888,10 +2953,13 @@ static int ens_step(fsibe_ensemble* e) {
         if (st) { if (g) cudaGraphDestroy(g); g_err = e->err; return st; }
         if (ce != cudaSuccess) { e->err = std::string("ensemble capture: ") + cudaGetErrorString(ce); g_err = e->err; return FSIBE_ERR_CUDA; }
         e->graph = g;
-        CKE(e, cudaGraphInstantiate(&e->gexec, g, 0));
+        CKE(e, cudaGraphInstantiate(&e->gexec, g, cudaGraphInstantiateFlagUseNodePriority));
     }
     CKE(e, cudaGraphLaunch(e->gexec, e->master));
-    for (fsibe_ctx* c : e->runs) c->press_partial = press_rows_only(c);
+    for (fsibe_ctx* c : e->runs) {
+        c->press_partial = press_rows_only(c);
+        c->adv_ready = adv_pipelined(c);
+    }
     return FSIBE_OK;
 }
 
