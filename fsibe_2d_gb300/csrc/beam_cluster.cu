@@ -190,11 +190,12 @@ __device__ void inv_row(const float* __restrict__ U, const float* __restrict__ L
 
 // The cluster form of k_beam (one cluster of R CTAs of 256 threads; R from the launch).
 // k_beam_pre of the same step ran before it and left the step's constants in b.pred.
+// k_forces lets it start early (pdl_trigger): the set-up that reads only what earlier kernels
+// wrote (the beam state, the predictor's output, the stored inverse rows) runs before its
+// pdl_wait, which precedes every read of the forces' loads and of the status.
 __global__ void __launch_bounds__(256, 1) k_beam_cl(BeamArgs b) {
-    pdl_wait();     // the previous kernel of the stream has completed
     extern __shared__ __align__(16) unsigned char cl_smem[];
     DevScalars* S = b.S;
-    if (S->status != 0) return;  // the same value in every CTA
     const unsigned rank = cl_rank(), R = cl_nrank();
     const int ns = b.ns, n = 2 * ns + 4;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nthr = blockDim.x, nwarp = nthr >> 5;
@@ -253,8 +254,8 @@ __global__ void __launch_bounds__(256, 1) k_beam_cl(BeamArgs b) {
     const bool released = time > b.t_release;
     const Motion mo = motion_at(b.mo, time + dt);  // mouvement(time + dt) of the new level
     int iter = 0;
+    const bool have_inv = released && S->beam_fact != 0;
     if (released) {
-        const bool have_inv = S->beam_fact != 0;
         if (have_inv) {
             // this CTA's rows of M^-1 and their row-scale exponents, kept from an earlier step
             const float* g = b.minv + (size_t)rank * rmax * mld;
@@ -263,9 +264,16 @@ __global__ void __launch_bounds__(256, 1) k_beam_cl(BeamArgs b) {
                 for (int q = tid; q < nv; q += nthr) cp_async16(minv + 4 * q, g + 4 * q);
             for (int k = lo + tid; k < hi; k += nthr) rse[k] = b.minv_rse[k];
         }
-        const double* K = b.pred + pred_consts(ns);
         for (int i = tid; i < n; i += nthr)
             if (i != xi_th(-1) && i != xi_T(ns, -1)) x[i] = b.pred[i];
+    }
+    pdl_wait();     // k_forces has completed: its loads and any status it raised are visible
+    if (S->status != 0) {  // the same value in every CTA: they all return here
+        cp_async_wait_all();
+        return;
+    }
+    if (released) {
+        const double* K = b.pred + pred_consts(ns);
         for (int i = tid; i < ns; i += nthr) {
             old_rhs[i] = b.pred[n + i];
             taun_s[i] = d1d(&dtab, b.tau_new, ns, 1, i);

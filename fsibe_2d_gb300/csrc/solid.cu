@@ -661,6 +661,7 @@ __global__ void __launch_bounds__(128) k_forces_geo(ForceArgs a, double dxi, dou
 
 __global__ void __launch_bounds__(128) k_forces(ForceArgs a, double dxi, double dyi) {
     pdl_wait();     // the previous kernel of the stream has completed
+    pdl_trigger();  // the beam kernel may start its set-up (it waits for this kernel's results)
     const int n = blockIdx.x;
     __shared__ double dl[4][18];
     __shared__ int ij[4][2];
