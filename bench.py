@@ -123,7 +123,9 @@ class ClockSampler:
 # (nl_pen and stress_x touch only the rows near the beam.)
 # (k_press_fin has no line: in the step it forms only the rows the forces' stencils reach, so
 # its bytes depend on where the beam is)
-PASSES = {"nl_y": lambda f: 12 * f + 3, "nl_adv": lambda f: 4 * f + 2, "nl_x": lambda f: 4 * f + 5,
+# k_nl_y (FP32C): reads A, B, W, W_lo, M (f), writes W, W_lo, M and the five spectra Tu, Tv,
+# Tw, T dy(omega), T sigma_b (f); the readers form i kx Tw and i kx Tu as they load
+PASSES = {"nl_y": lambda f: 10 * f + 3, "nl_adv": lambda f: 4 * f + 2, "nl_x": lambda f: 4 * f + 5,
           "press_x": lambda f: 3 * f + 9, "press_y": lambda f: 3}
 
 

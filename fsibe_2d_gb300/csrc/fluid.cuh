@@ -134,6 +134,17 @@ __device__ __forceinline__ void load_tileT(C2<R>* buf, const C2<R>* __restrict__
     }
 }
 
+// load_tileT of i kx T (kx's wavenumber kx kxs0 as k_nl_y forms it, in R): the FP32 form keeps
+// only T and forms the x derivative as it loads (cofdx of omega from Tw, du/dx from Tu)
+template <typename R, int H, int TR, int PL>
+__device__ __forceinline__ void load_tileT_dx(C2<R>* buf, const C2<R>* __restrict__ T, int ny, int iy0, int kmax,
+                                              double kxs0) {
+    for (int i = threadIdx.x; i < H * TR; i += blockDim.x) {
+        const int r = i % TR, kx = i / TR;
+        buf[r * PL + pad8(kx)] = (kx < kmax) ? cimul<R>(T[(size_t)kx * ny + iy0 + r], (R)kx * (R)kxs0) : mk<R>(0, 0);
+    }
+}
+
 // inverse x transform of one row buffer (after load + __syncthreads)
 template <typename R, int H>
 __device__ __forceinline__ void row_c2r(C2<R>* rb, const C2<R>* __restrict__ twR, const C2<R>* __restrict__ twX, int t) {
@@ -403,7 +414,8 @@ __device__ __forceinline__ void nl_x_tile(const KArgs<R>& a, const int iy0) {
     if (part != NL_PENAL) {
         // after the first AB2/Euler update the vorticity is dealiased: rows kx >= kcut are zero
         const int kin = a.explicit_step ? H : a.kcut;
-        load_tileT<R, H, X::TR, X::PL>(bufA, a.Tdx, ny, iy0, kin);
+        if constexpr (kIsF32<R>) load_tileT_dx<R, H, X::TR, X::PL>(bufA, a.Tw, ny, iy0, kin, a.g.kxs);
+        else load_tileT<R, H, X::TR, X::PL>(bufA, a.Tdx, ny, iy0, kin);
         load_tileT<R, H, X::TR, X::PL>(bufB, a.Tdy, ny, iy0, kin);
         __syncthreads();
         row_c2r_reg<R, H, 2>(ra, BS, a.twR, a.twX, t, dxy);  // both together, to registers
@@ -733,14 +745,10 @@ __global__ void __launch_bounds__(NY / 8, (nl_y_minb<R, NY>())) k_nl_y(KArgs<R> 
             const int spk = (!kIsF32<R> && !a.viscous && sp == 4) ? 5 : sp;
             C2<R>* dst = (spk == 0) ? a.Tu : (spk == 1) ? a.Tv : (spk == 2) ? a.Tw : (spk == 3) ? a.Tdy
                        : (spk == 4) ? a.Tsb : (spk == 5) ? a.Tdx : a.Tsa;
-            // FP32: the outputs i kx times a transformed one, cofdx(omega) = i kx Tw and
-            // du/dx = i kx Tu
-            C2<R>* dst2 = !kIsF32<R> ? nullptr : (sp == 2) ? a.Tdx : (sp == 0 && a.viscous) ? a.Tsa : nullptr;
+            // (FP32: cofdx(omega) = i kx Tw and du/dx = i kx Tu are formed by their readers as
+            // they load Tw and Tu, load_tileT_dx)
 #pragma unroll
-            for (int q = 0; q < 8; ++q) {
-                dst[row + t + q * G] = ov[b][q];
-                if (dst2) dst2[row + t + q * G] = cimul<R>(ov[b][q], kxs);
-            }
+            for (int q = 0; q < 8; ++q) dst[row + t + q * G] = ov[b][q];
         }
     }
 }
@@ -954,7 +962,8 @@ __global__ void __launch_bounds__(XRows<R, H, TRV>::THREADS,
     }
     if (a.viscous && !a.stress_split) {
         __syncthreads();
-        load_tileT<R, H, X::TR, X::PL>(bufA, a.Tsa, ny, iy0, a.kcut);
+        if constexpr (kIsF32<R>) load_tileT_dx<R, H, X::TR, X::PL>(bufA, a.Tu, ny, iy0, a.kcut, a.g.kxs);
+        else load_tileT<R, H, X::TR, X::PL>(bufA, a.Tsa, ny, iy0, a.kcut);
         load_tileT<R, H, X::TR, X::PL>(bufB, a.Tsb, ny, iy0, a.kcut);
         __syncthreads();
         row_c2r_m<R, H, 2>(ra, BS, a.twR, a.twX, t);  // ra and rb together
@@ -1159,7 +1168,8 @@ __global__ void __launch_bounds__(XRows<R, H, TRV>::THREADS, (xminb<MB, 1>())) k
     }
     C2<R>* ra = bufA + r * X::PL;
     C2<R>* rb = bufB + r * X::PL;
-    load_tileT<R, H, X::TR, X::PL>(bufA, a.Tsa, ny, iy0, a.kcut);
+    if constexpr (kIsF32<R>) load_tileT_dx<R, H, X::TR, X::PL>(bufA, a.Tu, ny, iy0, a.kcut, a.g.kxs);  // du/dx
+    else load_tileT<R, H, X::TR, X::PL>(bufA, a.Tsa, ny, iy0, a.kcut);
     load_tileT<R, H, X::TR, X::PL>(bufB, a.Tsb, ny, iy0, a.kcut);
     __syncthreads();
     C2<R> sv[2][8];
