@@ -73,6 +73,14 @@ __device__ __forceinline__ void cp_async16_f(void* s, const void* g) {
 __device__ __forceinline__ void cp_async_wait_f() {
     asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
 }
+// one complex value global -> shared without a register round trip (8 bytes in FP32 through
+// L1, 16 in FP64 bypassing it): a thread issues all of a tile's copies before waiting
+template <typename R>
+__device__ __forceinline__ void cp_async_el(C2<R>* s, const C2<R>* g) {
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(s);
+    if constexpr (sizeof(C2<R>) == 8) asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(sa), "l"(g) : "memory");
+    else asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(sa), "l"(g) : "memory");
+}
 
 // Error-free transformations for the compensated (hi + lo) vorticity state of the FP32 form.
 __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
@@ -127,10 +135,12 @@ constexpr int xrows_valid(int tr) {
 // ---- x-pass helpers -------------------------------------------------------------------
 // Rows kx >= kmax are known to be zero and are not read.
 template <typename R, int H, int TR, int PL>
+// Asynchronous: the caller completes the copies (cp_async_wait_f) before its __syncthreads.
 __device__ __forceinline__ void load_tileT(C2<R>* buf, const C2<R>* __restrict__ T, int ny, int iy0, int kmax = H) {
     for (int i = threadIdx.x; i < H * TR; i += blockDim.x) {
         const int r = i % TR, kx = i / TR;
-        buf[r * PL + pad8(kx)] = (kx < kmax) ? T[(size_t)kx * ny + iy0 + r] : mk<R>(0, 0);
+        if (kx < kmax) cp_async_el<R>(&buf[r * PL + pad8(kx)], &T[(size_t)kx * ny + iy0 + r]);
+        else buf[r * PL + pad8(kx)] = mk<R>(0, 0);
     }
 }
 
@@ -251,6 +261,7 @@ __global__ void __launch_bounds__(XRows<R, H>::THREADS) k_xinv(KArgs<R> a) {
     C2<R>* rb = buf + r * X::PL;
     const size_t boff = blockIdx.y * a.bstride;
     load_tileT<R, H, X::TR, X::PL>(buf, a.spec0 + boff, ny, iy0);
+    cp_async_wait_f();
     __syncthreads();
     row_c2r<R, H>(rb, a.twR, a.twX, t);
     C2<R>* f2 = reinterpret_cast<C2<R>*>(a.phys0) + boff + (size_t)(iy0 + r) * H;
@@ -332,6 +343,7 @@ __global__ void __launch_bounds__(XRows<R, H>::THREADS) k_vel_x(KArgs<R> a) {
     const int iy0 = blockIdx.x * X::TR, ny = a.g.ny;
     load_tileT<R, H, X::TR, X::PL>(bufA, a.Tu, ny, iy0);
     load_tileT<R, H, X::TR, X::PL>(bufB, a.Tv, ny, iy0);
+    cp_async_wait_f();
     __syncthreads();
     row_c2r<R, H>(bufA + r * X::PL, a.twR, a.twX, t);
     row_c2r<R, H>(bufB + r * X::PL, a.twR, a.twX, t);
@@ -417,6 +429,7 @@ __device__ __forceinline__ void nl_x_tile(const KArgs<R>& a, const int iy0) {
         if constexpr (kIsF32<R>) load_tileT_dx<R, H, X::TR, X::PL>(bufA, a.Tw, ny, iy0, kin, a.g.kxs);
         else load_tileT<R, H, X::TR, X::PL>(bufA, a.Tdx, ny, iy0, kin);
         load_tileT<R, H, X::TR, X::PL>(bufB, a.Tdy, ny, iy0, kin);
+        cp_async_wait_f();
         __syncthreads();
         row_c2r_reg<R, H, 2>(ra, BS, a.twR, a.twX, t, dxy);  // both together, to registers
     }
@@ -426,6 +439,7 @@ __device__ __forceinline__ void nl_x_tile(const KArgs<R>& a, const int iy0) {
     if constexpr (SPG == 1 && PART != NL_PENAL) {
         const int kin = a.explicit_step ? H : a.kcut;
         load_tileT<R, H, X::TR, X::PL>(bufA, a.Tw, ny, iy0, kin);
+        cp_async_wait_f();
         __syncthreads();
         row_c2r_reg<R, H, 1>(ra, BS, a.twR, a.twX, t, om);
     }
@@ -785,6 +799,7 @@ __global__ void __launch_bounds__(XRows<R, H, TRV>::THREADS,
     load_tileT<R, H, X::TR, X::PL>(bufA, a.Tu, ny, iy0, a.kcut);
     load_tileT<R, H, X::TR, X::PL>(bufB, a.Tv, ny, iy0, a.kcut);
     load_tileT<R, H, X::TR, X::PL>(bufC, a.Tw, ny, iy0, a.kcut);
+    cp_async_wait_f();
     __syncthreads();
     // u, v and omega together, this thread's elements m = t + q G to registers (the row buffers
     // are free afterwards)
@@ -965,6 +980,7 @@ __global__ void __launch_bounds__(XRows<R, H, TRV>::THREADS,
         if constexpr (kIsF32<R>) load_tileT_dx<R, H, X::TR, X::PL>(bufA, a.Tu, ny, iy0, a.kcut, a.g.kxs);
         else load_tileT<R, H, X::TR, X::PL>(bufA, a.Tsa, ny, iy0, a.kcut);
         load_tileT<R, H, X::TR, X::PL>(bufB, a.Tsb, ny, iy0, a.kcut);
+        cp_async_wait_f();
         __syncthreads();
         row_c2r_m<R, H, 2>(ra, BS, a.twR, a.twX, t);  // ra and rb together
         C2<R>* sa2 = reinterpret_cast<C2<R>*>(a.sa) + roff;
@@ -1003,9 +1019,10 @@ constexpr int xpairs_rows() {
 template <int H, int TR>
 __device__ __forceinline__ void load_tileP(float4* buf, const float2* __restrict__ T, int ny, int iy0, int kmax) {
     constexpr int PS = pair_slots(H);
-    for (int i = threadIdx.x; i < H * TR; i += blockDim.x) {
+    for (int i = threadIdx.x; i < H * TR; i += blockDim.x) {  // asynchronous, as load_tileT
         const int r = i % TR, kx = i / TR;
-        pel(buf + r * PS, kx) = (kx < kmax) ? T[(size_t)kx * ny + iy0 + r] : make_float2(0.f, 0.f);
+        if (kx < kmax) cp_async_el<float>(&pel(buf + r * PS, kx), &T[(size_t)kx * ny + iy0 + r]);
+        else pel(buf + r * PS, kx) = make_float2(0.f, 0.f);
     }
 }
 
@@ -1031,6 +1048,7 @@ __global__ void __launch_bounds__(XPairs<H, TR>::THREADS, XPairs<H, TR>::MINB) k
     load_tileP<H, TR>(bufA, a.Tu, ny, iy0, a.kcut);
     load_tileP<H, TR>(bufB, a.Tv, ny, iy0, a.kcut);
     load_tileP<H, TR>(bufC, a.Tw, ny, iy0, a.kcut);
+    cp_async_wait_f();
     __syncthreads();
     // u and v together, then omega (three rows at once would not fit 128 registers):
     // v[f][2m + h] = element 2u + h + m G (the rows are free afterwards)
@@ -1171,6 +1189,7 @@ __global__ void __launch_bounds__(XRows<R, H, TRV>::THREADS, (xminb<MB, 1>())) k
     if constexpr (kIsF32<R>) load_tileT_dx<R, H, X::TR, X::PL>(bufA, a.Tu, ny, iy0, a.kcut, a.g.kxs);  // du/dx
     else load_tileT<R, H, X::TR, X::PL>(bufA, a.Tsa, ny, iy0, a.kcut);
     load_tileT<R, H, X::TR, X::PL>(bufB, a.Tsb, ny, iy0, a.kcut);
+    cp_async_wait_f();
     __syncthreads();
     C2<R> sv[2][8];
     row_c2r_reg<R, H, 2>(ra, BS, a.twR, a.twX, t, sv);  // both together, to registers
@@ -1304,6 +1323,7 @@ __global__ void __launch_bounds__(XRows<R, H, TRV>::THREADS, (xminb<MB, 1>())) k
 #pragma unroll
     for (int q = 0; q < 8; ++q) { ul[q] = u2[t + q * X::G]; vl[q] = v2[t + q * X::G]; }
     load_tileT<R, H, X::TR, X::PL>(buf, a.Tq, ny, iy0);
+    cp_async_wait_f();
     __syncthreads();
     C2<R> qv[1][8];
     row_c2r_reg<R, H, 1>(rb, X::PL, a.twR, a.twX, t, qv);  // to registers
