@@ -42,6 +42,7 @@ def library():
         L.fsibe_tiles.argtypes = [C.c_void_p, C.POINTER(C.c_int32)]
         L.fsibe_tile_config.argtypes = [C.c_void_p, C.POINTER(C.c_int32)]
         L.fsibe_beam_cluster.argtypes = [C.c_void_p, C.POINTER(C.c_int32)]
+        L.fsibe_press_y_engine.argtypes = [C.c_void_p, C.POINTER(C.c_int32)]
         L.fsibe_ensemble_create.argtypes = [C.POINTER(FsibeParams), C.c_int, C.POINTER(C.c_void_p)]
         L.fsibe_ensemble_destroy.argtypes = [C.c_void_p]
         L.fsibe_ensemble_get.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_void_p)]
@@ -96,6 +97,12 @@ class Run(_Run):
         out = (C.c_int32 * 6)()
         self._call("tile_config", out)
         return [(out[2 * q], out[2 * q + 1]) for q in range(3)]
+
+    def press_y_engine(self):
+        """k_press_y's transform engine: 0 paired (FP32), 1 one butterfly a thread."""
+        out = C.c_int32(0)
+        self._call("press_y_engine", C.byref(out))
+        return out.value
 
     def beam_cluster(self):
         """CTAs of the cluster running the beam's Newton step (0: the single-CTA kernel)."""

@@ -501,6 +501,7 @@ struct fsibe_ctx {
     int launches = 0;
     int nsm = 152;                // SMs of the device
     int xv_nl = 1, xv_px = 1, xv_fin = 1;  // tile-height variants of the fused x kernels (1: default)
+    int py_eng = 0;                        // k_press_y's transform engine (FP32: 0 paired, 1 one butterfly)
     // per-kernel event timing (fsibe_kernel_times)
     bool profiling = false;
     std::vector<cudaEvent_t> pool;
@@ -853,7 +854,10 @@ static int fluid_step_t(fsibe_ctx* c, int explicit_step, bool adv_forked = false
         CK(c, cudaEventRecord(c->ev_adv, c->side2));
     }
     if (a.pressure_on) {
-        launch_y<R>(c, KY.press_y, KY.y_smem2, a, "press_y", 1, true, KY.press_y_threads);
+        if (c->py_eng == 1 && KY.press_y1)  // the one-butterfly engine, where the autotuner found it faster
+            launch_y<R>(c, KY.press_y1, KY.press_y1_smem, a, "press_y", 1, true, KY.y_threads);
+        else
+            launch_y<R>(c, KY.press_y, KY.y_smem2, a, "press_y", 1, true, KY.press_y_threads);
         KArgs<R> f = a;
         f.srows = (stress_rows && c->P.iBeam > 0) ? 1 : 0;  // the forces' rows only (k_press_fin)
         launch_xv<R>(c, KX.xv[c->xv_fin].press_fin, KX.xv[c->xv_fin], 1, f, "press_fin");
@@ -1435,17 +1439,36 @@ static float time_xv(fsibe_ctx* c, int kind, const typename SizeKernels<R>::XVar
     return best;
 }
 
+// One y-pass kernel over the kx rows, timed as time_xv times the x-pass candidates.
+template <typename R>
+static float time_y(fsibe_ctx* c, void (*k)(KArgs<R>), int smem, int threads) {
+    KArgs<R> a = kargs<R>(c);
+    const dim3 grid(c->g.hx);
+    for (int i = 0; i < 2; ++i) k<<<grid, threads, smem, c->stream>>>(a);
+    float best = 1e30f;
+    for (int round = 0; round < 3; ++round) {
+        cudaEventRecord(c->ev0, c->stream);
+        for (int i = 0; i < 5; ++i) k<<<grid, threads, smem, c->stream>>>(a);
+        cudaEventRecord(c->ev1, c->stream);
+        if (cudaEventSynchronize(c->ev1) != cudaSuccess) return 1e30f;
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+        best = ms / 5.f < best ? ms / 5.f : best;
+    }
+    return best;
+}
+
 template <typename R>
 static int autotune_x(fsibe_ctx* c) {
     static std::mutex mu;
-    static std::vector<std::array<int, 6>> cache;  // fp32, nx, ny, nl, px, fin
+    static std::vector<std::array<int, 7>> cache;  // fp32, nx, ny, nl, px, fin, press_y engine
     const char* env = std::getenv("FSIBE_AUTOTUNE");
     if (env && env[0] == '0') return FSIBE_OK;
     std::lock_guard<std::mutex> lock(mu);
     const int f32 = c->fp32 ? 1 : 0;
     for (const auto& e : cache)
         if (e[0] == f32 && e[1] == c->g.nx && e[2] == c->g.ny) {
-            c->xv_nl = e[3]; c->xv_px = e[4]; c->xv_fin = e[5];
+            c->xv_nl = e[3]; c->xv_px = e[4]; c->xv_fin = e[5]; c->py_eng = e[6];
             return FSIBE_OK;
         }
     const SizeKernels<R>& K = kx_of<R>(c);
@@ -1467,10 +1490,19 @@ static int autotune_x(fsibe_ctx* c) {
         }
         choice[kind] = best;
     }
+    // k_press_y's transform engine (FP32): the paired one by default, the one-butterfly one when
+    // it is faster by 3%
+    int eng = 0;
+    const SizeKernels<R>& KY = ky_of<R>(c);
+    if (KY.press_y1) {
+        const float t0 = time_y<R>(c, KY.press_y, KY.y_smem2, KY.press_y_threads);
+        const float t1 = time_y<R>(c, KY.press_y1, KY.press_y1_smem, KY.y_threads);
+        if (t1 < 0.97f * t0) eng = 1;
+    }
     CKL(c);
     CK(c, cudaStreamSynchronize(c->stream));
-    c->xv_nl = choice[0]; c->xv_px = choice[1]; c->xv_fin = choice[2];
-    cache.push_back({f32, c->g.nx, c->g.ny, choice[0], choice[1], choice[2]});
+    c->xv_nl = choice[0]; c->xv_px = choice[1]; c->xv_fin = choice[2]; c->py_eng = eng;
+    cache.push_back({f32, c->g.nx, c->g.ny, choice[0], choice[1], choice[2], eng});
     return FSIBE_OK;
 }
 
@@ -1747,6 +1779,9 @@ int fsibe_create(const fsibe_params* p, fsibe_ctx** out) {
             if (pe[0] == '1' && c->g.ny % c->kxf.xp.rows == 0) c->xv_px = 4;
             else if (pe[0] == '0' && c->xv_px == 4) c->xv_px = 1;
         }
+        // FSIBE_PY_ENG = 0 / 1 forces k_press_y's paired / one-butterfly engine (FP32)
+        const char* ye = std::getenv("FSIBE_PY_ENG");
+        if (ye && c->fp32) c->py_eng = (ye[0] == '1') ? 1 : 0;
     }
     e = cudaDeviceSynchronize();
     if (e != cudaSuccess) { g_err = std::string("create: ") + cudaGetErrorString(e); fsibe_destroy(c); return FSIBE_ERR_CUDA; }
@@ -2372,6 +2407,12 @@ int fsibe_beam_phase_cycles(fsibe_ctx* c, long long* out32, int reset) {
     CK(c, cudaMemcpyAsync(out32, c->S->phase, 32 * sizeof(long long), cudaMemcpyDeviceToHost, c->stream));
     if (reset) CK(c, cudaMemsetAsync(c->S->phase, 0, 32 * sizeof(long long), c->stream));
     CK(c, cudaStreamSynchronize(c->stream));
+    return FSIBE_OK;
+}
+
+int fsibe_press_y_engine(fsibe_ctx* c, int32_t* eng) {
+    if (!c || !eng) return FSIBE_ERR_PARAM;
+    *eng = c->fp32 ? c->py_eng : 1;
     return FSIBE_OK;
 }
 

@@ -1208,7 +1208,8 @@ __global__ void __launch_bounds__(XRows<R, H, TRV>::THREADS, (xminb<MB, 1>())) k
 
 // Threads of k_press_y: the paired FP32 engine (two butterflies a thread) or the one-butterfly
 // engine (FP64).
-template <typename R, int NY> constexpr int press_y_threads() { return kIsF32<R> ? NY / 16 : NY / 8; }
+// ENG = 1 forces the one-butterfly engine in FP32 (the autotuner's other candidate).
+template <typename R, int NY, int ENG = 0> constexpr int press_y_threads() { return (kIsF32<R> && ENG == 0) ? NY / 16 : NY / 8; }
 
 // K5, FP32: the paired engine.  Thread u holds the row's elements 2u + h + m (NY/8) as v[2m + h];
 // the pairs are loaded from and stored to global memory as 16-byte accesses.  The arithmetic of
@@ -1254,10 +1255,10 @@ __device__ __forceinline__ void press_y_paired(const KArgs<float>& a) {
 }
 
 // K5: forward-y of the Poisson right-hand side, divergence, poisson, inverse-y -> Tq
-template <typename R, int NY>
-__global__ void __launch_bounds__(press_y_threads<R, NY>(), (kIsF32<R> && NY >= 4096) ? 2 : 1) k_press_y(KArgs<R> a) {
+template <typename R, int NY, int ENG = 0>
+__global__ void __launch_bounds__(press_y_threads<R, NY, ENG>(), (kIsF32<R> && NY >= 4096) ? 2 : 1) k_press_y(KArgs<R> a) {
     pdl_wait();     // the previous kernel of the stream has completed
-    if constexpr (kIsF32<R>) {
+    if constexpr (kIsF32<R> && ENG == 0) {
         press_y_paired<NY>(a);
         return;
     }
@@ -1379,6 +1380,8 @@ struct SizeKernels {
     void (*press_y)(KArgs<R>);
     int y_threads, y_smem1, y_smem2, y_smem_nl;
     int press_y_threads;  // the paired FP32 engine runs NY/16 threads
+    void (*press_y1)(KArgs<R>);  // FP32: k_press_y on the one-butterfly engine (NY/8 threads), or null
+    int press_y1_smem;
 };
 
 template <typename R, int H, int TR, int MB = 0, bool SPG = false>
@@ -1463,6 +1466,12 @@ inline void fill_size_kernels(SizeKernels<R>& k) {
     cudaFuncSetAttribute(k_yinv<R, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, k.y_smem1);
     cudaFuncSetAttribute(k_nl_y<R, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, k.y_smem_nl);
     cudaFuncSetAttribute(k_press_y<R, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, k.y_smem2);
+    k.press_y1 = nullptr;
+    k.press_y1_smem = 2 * k.y_smem1;
+    if constexpr (kIsF32<R>) {
+        k.press_y1 = k_press_y<R, N, 1>;
+        cudaFuncSetAttribute(k_press_y<R, N, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, k.press_y1_smem);
+    }
 }
 
 }  // namespace fsibe

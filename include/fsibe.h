@@ -281,6 +281,11 @@ int fsibe_beam_phase_cycles(fsibe_ctx* ctx, long long* out32, int reset);
  * press_x) of each: out6 = {rows, bound} for nl_x, press_x, press_fin. */
 int fsibe_tiles(fsibe_ctx* ctx, int32_t* rows3);
 int fsibe_tile_config(fsibe_ctx* ctx, int32_t* out6);
+/* The transform engine the autotuner chose for k_press_y: 0 the paired FP32 engine (two
+ * adjacent butterflies a thread), 1 the one-butterfly engine (always in the FP64 form).
+ * fsibe_create times both in the FP32 form and keeps the paired one unless the other is 3%
+ * faster; FSIBE_PY_ENG = 0 / 1 forces one. */
+int fsibe_press_y_engine(fsibe_ctx* ctx, int32_t* eng);
 
 /* CTAs of the thread-block cluster that runs the beam's Newton step (16 or 8; 0 when the
  * single-CTA kernel runs it).  Chosen at fsibe_create from what the device can place;

@@ -37,3 +37,28 @@ def test_paired_press_x_matches_the_oracle(oracle, monkeypatch, n, ns, steps):
     assert max(err.values()) < 1e-5, err
     assert rel(g.vort(), h.vort()) < 1e-5
     g.close(); h.close(); o.close()
+
+
+@pytest.mark.parametrize("n", [256, 1024])
+def test_press_y_engines_match_the_oracle(oracle, monkeypatch, n):
+    """k_press_y's two FP32 engines (FSIBE_PY_ENG=0 paired, 1 one butterfly a thread)."""
+    import fsibe_2d_gb300 as F
+    kw = dict(nx=n, ny=n, ns=n // 4, Re=500.0, dt=5e-5)
+    w = seeded_vorticity(n, seed=6)
+    o = oracle.OracleRun(make_params(**kw))
+    o.init_fields(w)
+    o.time_step(20)
+    errs = []
+    for eng in ("0", "1"):
+        monkeypatch.setenv("FSIBE_PY_ENG", eng)
+        g = F.Run(make_params(precision=FSIBE_FP32C, **kw))
+        monkeypatch.delenv("FSIBE_PY_ENG", raising=False)
+        assert g.press_y_engine() == int(eng)
+        g.init_fields(w)
+        g.time_step(20)
+        errs.append(rel(g.press(), o.press()))
+        assert rel(g.vort(), o.vort()) < 1e-5
+        g.close()
+    print(f"{n}^2 press_y engines against the oracle (pressure):", errs)
+    assert max(errs) < 1e-5
+    o.close()
