@@ -57,8 +57,26 @@ def library():
         L.fsibe_force_objective.argtypes = [C.c_void_p, C.c_int, _dp, C.c_double, C.c_int, C.c_int, _dp]
         L.fsibe_force_gradient.argtypes = [C.c_void_p, C.c_int, _dp, C.c_double, C.c_int, C.c_int, C.c_int, _dp, _dp,
                                            _dp, _dp, C.POINTER(AdjointInfo)]
+        L.fsibe_beam_phase_cycles.argtypes = [C.c_void_p, C.POINTER(C.c_longlong), C.c_int]
+        L.fsibe_running_sums.argtypes = [_dp, C.c_int32, _dp, C.POINTER(C.c_int32)]
         _lib = L
     return _lib
+
+
+def running_sums(terms):
+    """The beam kernels' running sums of integrate_position on the GPU: terms (4, n) float64;
+    returns (sums (4, n) with sums[q, k] = s_k of row q, rows that failed the step check)."""
+    t = np.ascontiguousarray(terms, dtype=np.float64)
+    if t.ndim != 2 or t.shape[0] != 4:
+        raise ValueError("terms must have shape (4, n)")
+    out = np.empty_like(t)
+    ns = C.c_int32(0)
+    L = library()
+    dp = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
+    st = L.fsibe_running_sums(dp(t), C.c_int32(t.shape[1]), dp(out), C.byref(ns))
+    if st != 0:
+        raise RuntimeError(f"fsibe_running_sums: status {st}: {L.fsibe_last_error(None).decode()}")
+    return out, ns.value
 
 
 class Run(_Run):
@@ -103,6 +121,12 @@ class Run(_Run):
         out = C.c_int32(0)
         self._call("press_y_engine", C.byref(out))
         return out.value
+
+    def beam_phase_cycles(self, reset=False):
+        """The beam kernels' 32 phase counters (fsibe_beam_phase_cycles)."""
+        out = (C.c_longlong * 32)()
+        self._call("beam_phase_cycles", out, C.c_int(1 if reset else 0))
+        return list(out)
 
     def beam_cluster(self):
         """CTAs of the cluster running the beam's Newton step (0: the single-CTA kernel)."""

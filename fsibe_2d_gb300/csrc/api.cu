@@ -45,6 +45,7 @@ void launch_init_beam(const BeamArgs& b, cudaStream_t st);
 void launch_move_beam(const BeamArgs& b, cudaStream_t st);
 int beam_smem_setup(int ns);
 int beam_cluster_setup(int ns, int want, size_t* smem_out, int* big_out);
+cudaError_t launch_running_sums(const double* src, double* dst, int n, int* nserial, cudaStream_t st);
 size_t beam_cluster_fact_floats(int ns, int R);
 void launch_beam_cluster(const BeamArgs& b, int R, size_t smem, cudaStream_t st, bool pdl);
 size_t beam_cluster_minv_floats(int ns, int R);
@@ -3141,6 +3142,28 @@ __global__ void k_static_twiddles(double2* twY, int ny, double2* twX, int hx, do
     }
 }
 }  // namespace
+
+// The beam kernels' running sums on the caller's terms (host arrays of 4 n doubles):
+// out[q n + k] = s_k of row q, and *nserial the rows the step check sent to the serial loop.
+extern "C" int fsibe_running_sums(const double* terms, int32_t n, double* out, int32_t* nserial) {
+    if (!terms || !out || !nserial) { g_err = "fsibe_running_sums: null argument"; return FSIBE_ERR_PARAM; }
+    if (n < 1 || n > (1 << 20)) { g_err = "fsibe_running_sums: n must be in [1, 2^20]"; return FSIBE_ERR_PARAM; }
+    const size_t bytes = (size_t)4 * n * sizeof(double);
+    double *d_in = nullptr, *d_out = nullptr;
+    int* d_ns = nullptr;
+    cudaError_t e = cudaMalloc(&d_in, 2 * bytes + 16);
+    if (e == cudaSuccess) {
+        d_out = d_in + 4 * (size_t)n;
+        d_ns = reinterpret_cast<int*>(d_out + 4 * (size_t)n);
+        e = cudaMemcpy(d_in, terms, bytes, cudaMemcpyHostToDevice);
+    }
+    if (e == cudaSuccess) e = launch_running_sums(d_in, d_out, n, d_ns, 0);
+    if (e == cudaSuccess) e = cudaMemcpy(out, d_out, bytes, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(nserial, d_ns, sizeof(int32_t), cudaMemcpyDeviceToHost);
+    if (d_in) cudaFree(d_in);
+    if (e != cudaSuccess) { g_err = std::string("fsibe_running_sums: ") + cudaGetErrorString(e); return FSIBE_ERR_CUDA; }
+    return FSIBE_OK;
+}
 
 extern "C" int fsibe_coftxy_static(const double* f_dev, double* fk_dev, int32_t nx, int32_t ny, void* stream) {
     if (!f_dev || !fk_dev) { g_err = "fsibe_coftxy_static: null buffer"; return FSIBE_ERR_PARAM; }

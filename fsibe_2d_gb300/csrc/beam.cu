@@ -12,6 +12,7 @@
 #include <mutex>
 
 #include "beam_impl.cuh"
+#include "running_sum.cuh"
 
 namespace fsibe {
 
@@ -369,36 +370,18 @@ __global__ void __launch_bounds__(256) k_beam(BeamArgs b) {
         sincos(th, &sn, &cn);
         w.cs[i] = cn * ds;
         w.cs[ns + 8 + i] = sn * ds;
-        w.cs[2 * (ns + 8) + i] = td * sn * ds;
+        w.cs[2 * (ns + 8) + i] = -(td * sn * ds);  // the third sum subtracts: s - a == s + (-a)
         w.cs[3 * (ns + 8) + i] = td * cn * ds;
     }
     __syncthreads();
     // the four running sums in the reference's order: the positions decide grid-aligned
-    // boxes (mask, drag window), so their roundings must be the reference's
-    if (threadIdx.x < 4) {
-        // eight terms at a time, the next eight loaded before the current ones are added (the
-        // workspace is in global memory at large ns); the order of the additions is unchanged
-        const int q = threadIdx.x;
-        const double* src = w.cs + q * (ns + 8);
-        double* dst = w.pre + q * (ns + 8);
-        double s = 0.0, v[8], nv[8];
-#pragma unroll
-        for (int u = 0; u < 8; ++u) v[u] = (u < ns) ? src[u] : 0.0;
-        for (int i = 0; i < ns; i += 8) {
-#pragma unroll
-            for (int u = 0; u < 8; ++u) nv[u] = (i + 8 + u < ns) ? src[i + 8 + u] : 0.0;
-#pragma unroll
-            for (int u = 0; u < 8; ++u) {
-                if (i + u < ns) {
-                    dst[i + u] = s;
-                    s = (q == 2) ? s - v[u] : s + v[u];
-                }
-            }
-#pragma unroll
-            for (int u = 0; u < 8; ++u) v[u] = nv[u];
-        }
+    // boxes (mask, drag window), so their roundings must be the reference's (one lane a sum in
+    // integer arithmetic, checked step by step: running_sum.cuh)
+    {
+        __shared__ int rs_flags[4];
+        const int nser = running_sums4(w.cs, ns + 8, w.pre, ns + 8, ns, rs_flags, NoIdle());
+        if (threadIdx.x == 0 && nser) S->phase[30] += nser;
     }
-    __syncthreads();
     // positions and velocities, and in the same pass each thread's terms of the emergency brake
     // (SolidSolver.f90:370-380) and of SolidEnergies (SolidSolver.f90:76-92); then block
     // reductions (per-thread partials, a shuffle tree, one warp over the warps' results), since

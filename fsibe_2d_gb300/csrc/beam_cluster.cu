@@ -31,6 +31,7 @@
 #include <mutex>
 
 #include "beam_impl.cuh"
+#include "running_sum.cuh"
 
 namespace fsibe {
 namespace {
@@ -236,7 +237,7 @@ __global__ void __launch_bounds__(256, 1) k_beam_cl(BeamArgs b) {
     w.x = x; w.tdn = tdn; w.bo5 = bo5; w.bo6 = bo6; w.oo5 = oo5; w.oo6 = oo6;
     w.old_rhs = old_rhs; w.taun_s = taun_s; w.dtab = &dtab; w.Uf = Uf; w.Lf = Lf; w.rse = rse;
 
-    long long ph_t = clock64(), ph[26] = {};
+    long long ph_t = clock64(), ph[28] = {};
     // the cluster barrier that guarantees every CTA runs before the first DSMEM access comes
     // just before that access (cl_up), so the set-up overlaps the CTAs' start
     bool cl_up = false;
@@ -658,35 +659,41 @@ __global__ void __launch_bounds__(256, 1) k_beam_cl(BeamArgs b) {
     PH(25);
     const double* thv = pcs + 8 * L;
     const double* tdv = pcs + 9 * L;
-    if (tid < 4) {
-        // the four running sums in the reference's order (the positions decide grid-aligned
-        // boxes of the mask and the drag window, so their roundings must be the reference's)
-        const double* src = pcs + tid * L;
-        double* dst = pcs + (4 + tid) * L;
-        double s = 0.0;
-        int i = 0;
-        for (; i + 8 <= ns; i += 8) {
-            double v[8];
-#pragma unroll
-            for (int u = 0; u < 8; ++u) v[u] = src[i + u];
-#pragma unroll
-            for (int u = 0; u < 8; ++u) { dst[i + u] = s; s = s + v[u]; }
-        }
-        for (; i < ns; ++i) { dst[i] = s; s = s + src[i]; }
-    } else if (released && warp > 0) {
-        for (int i = tid - 32; i < ns; i += nthr - 32) { b.th[i] = thv[i]; b.thd[i] = tdv[i]; }
-        // beam_oldold = beam_old (the state at entry)
-        for (int i = tid - 32; i < ns; i += nthr - 32) {
+    // the new angles and rates, and beam_oldold = beam_old (the state at entry); done by the
+    // threads that the running sums leave idle
+    auto copies = [&](int i0, int stride) {
+        if (!released) return;
+        for (int i = i0; i < ns; i += stride) { b.th[i] = thv[i]; b.thd[i] = tdv[i]; }
+        for (int i = i0; i < ns; i += stride) {
             b.oo[0 * ns + i] = b.x[i]; b.oo[1 * ns + i] = b.y[i]; b.oo[2 * ns + i] = bo3[i];
             b.oo[3 * ns + i] = bo4[i]; b.oo[4 * ns + i] = bo5[i]; b.oo[5 * ns + i] = bo6[i];
         }
-        if (tid == 32) {
-            S->newton_iters = iter;
-            if (S->actually_bdf2) { S->method = FSIBE_BDF2; S->actually_bdf2 = 0; }
-            S->dt_old = dt;
-        }
+    };
+    if (released && tid == 0) {
+        S->newton_iters = iter;
+        if (S->actually_bdf2) { S->method = FSIBE_BDF2; S->actually_bdf2 = 0; }
+        S->dt_old = dt;
     }
-    __syncthreads();
+    // the four running sums in the reference's order (the positions decide grid-aligned boxes
+    // of the mask and the drag window, so their roundings must be the reference's): one lane a
+    // sum in integer arithmetic, checked step by step (running_sum.cuh), while the other warps
+    // copy.  The large-beam form first stages the terms into the shared memory of the solution
+    // vectors x and xdi (32 ns + 192 bytes, at least the 32 ns needed), which the Newton loop
+    // is done with.
+    const double* src0 = pcs;
+    if (big) {
+        double* st = x;  // x, then xdi: contiguous
+        for (int i = tid; i < ns; i += nthr) {
+            st[i] = pcs[i]; st[ns + i] = pcs[L + i]; st[2 * ns + i] = pcs[2 * L + i]; st[3 * ns + i] = pcs[3 * L + i];
+        }
+        src0 = st;
+        __syncthreads();
+    }
+    {
+        __shared__ int rs_flags[4];
+        const int nser = running_sums4(src0, big ? ns : L, pcs + 4 * L, L, ns, rs_flags, copies);
+        if (tid == 0 && nser) S->phase[30] += nser;
+    }
     PH(8);
     // positions and velocities, and in the same pass each thread's terms of the emergency brake
     // (SolidSolver.f90:370-380) and of SolidEnergies (SolidSolver.f90:76-92); the block then
@@ -728,6 +735,7 @@ __global__ void __launch_bounds__(256, 1) k_beam_cl(BeamArgs b) {
         ecol[0][tid] = sk; ecol[1][tid] = sp; ecol[2][tid] = se;
         ecol[3][tid] = sax; ecol[4][tid] = say; ecol[5][tid] = mx;
         __syncthreads();
+        PH(26);
         if (warp < 6) {
             double v = 0.0;
             for (int k = lane; k < nthr; k += 32) v = (warp == 5) ? fmax(v, ecol[5][k]) : v + ecol[warp][k];
@@ -746,13 +754,14 @@ __global__ void __launch_bounds__(256, 1) k_beam_cl(BeamArgs b) {
         }
     }
     PH(9);
-    if (tid == 0)
-        for (int k = 4; k < 26; ++k) S->phase[k] += ph[k];
     if (b.fuse_adv) {
         // the end of the time step, which the host would otherwise launch next (k_advance)
         __syncthreads();
         advance_state(b.adv);
     }
+    PH(27);
+    if (tid == 0)
+        for (int k = 4; k < 28; ++k) S->phase[k] += ph[k];
 }
 
 // ---- host side ------------------------------------------------------------------------
@@ -814,6 +823,18 @@ int beam_cluster_setup(int ns, int want, size_t* smem_out, int* big_out) {
 
 // Floats of the large-beam form's global factor copies (one a CTA).
 size_t beam_cluster_fact_floats(int ns, int R) { return (size_t)R * cl_fact_floats(ns); }
+
+// The running sums on arbitrary terms (a diagnostic of their exactness): one 256-thread block,
+// the terms and sums in global memory.
+__global__ void __launch_bounds__(256, 1) k_running_sums(const double* src, double* dst, int n, int* nserial) {
+    __shared__ int flags[4];
+    const int r = running_sums4(src, n, dst, n, n, flags, NoIdle());
+    if (threadIdx.x == 0) *nserial = r;
+}
+cudaError_t launch_running_sums(const double* src, double* dst, int n, int* nserial, cudaStream_t st) {
+    k_running_sums<<<1, 256, 0, st>>>(src, dst, n, nserial);
+    return cudaGetLastError();
+}
 
 void launch_beam_cluster(const BeamArgs& b, int R, size_t smem, cudaStream_t st, bool pdl) {
     cudaLaunchConfig_t cfg = {};

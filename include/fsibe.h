@@ -267,9 +267,20 @@ int fsibe_kernel_times(fsibe_ctx* ctx, int nsteps, fsibe_kernel_time* out, int c
  * all-gather, [17] inverse products and solution updates, [21] the push and [18] the barrier
  * of the solution rows' all-gather, [6] the refinement's decisions, [23] Newton update and
  * norms, [7] saving the inverse, [24] the angles' increments to the first CTA, [25] the
- * cluster barrier after them, [8] position sums, [9] positions, brake and energies, [10]
- * the solve count.  out32 receives 32 values; reset != 0 zeroes them after reading. */
+ * cluster barrier after them, [8] position sums, [26] positions and the terms of the brake
+ * and the energies, [9] their reduction, [27] the end of the time step, [10] the solve count;
+ * [30] the running sums that failed their step check (a count, see fsibe_running_sums).
+ * out32 receives 32 values; reset != 0 zeroes them after reading. */
 int fsibe_beam_phase_cycles(fsibe_ctx* ctx, long long* out32, int reset);
+/* The beam kernels' running sums of integrate_position (integrate_position.f90:14-44) on the
+ * caller's terms, a diagnostic of their exactness: terms and out are host arrays of 4 n doubles
+ * (four rows of n); out[q n + k] = s_k with s_0 = +0 and s_(k+1) = s_k + terms[q n + k], bit
+ * for bit the serial FP64 loop.  The kernels add the terms as integers on the grid of the
+ * running value's binade, check every step with the FP64 addition and form a row that fails
+ * the check by the serial loop; *nserial receives how many rows did (the Newton kernels count
+ * them in fsibe_beam_phase_cycles' [30]).  n in [1, 2^20]; runs on the current device's
+ * legacy stream. */
+int fsibe_running_sums(const double* terms, int32_t n, double* out, int32_t* nserial);
 /* Rows per block chosen by the autotuner for the fused x-pass kernels (nl_x, press_x,
  * press_fin).  fsibe_create times four candidates per kernel on the new context's buffers --
  * half, the default and twice the default tile height, and the default tile with its

@@ -37,7 +37,7 @@ def test_oracle_exports_the_same_entry_points(oracle):
             "fsibe_ensemble_create", "fsibe_ensemble_destroy", "fsibe_ensemble_size", "fsibe_ensemble_get",
             "fsibe_ensemble_step", "fsibe_ensemble_time_steps", "fsibe_ensemble_last_error",
             "fsibe_drag_objective", "fsibe_drag_gradient", "fsibe_force_objective", "fsibe_force_gradient",
-            "fsibe_tiles", "fsibe_tile_config", "fsibe_beam_cluster", "fsibe_press_y_engine",
+            "fsibe_tiles", "fsibe_tile_config", "fsibe_beam_cluster", "fsibe_press_y_engine", "fsibe_running_sums",
             "fsibe_last_error"}
     missing = [n for n in declared_functions() if n not in skip and not hasattr(lib, "orc_" + n[len("fsibe_"):])]
     assert not missing, missing
