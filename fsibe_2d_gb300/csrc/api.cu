@@ -455,6 +455,7 @@ struct fsibe_ctx {
     double* etab = nullptr;       // integrating-factor tables (hx + ny/2 + 1)
     float2* etabf = nullptr;
     int* dcut = nullptr;          // dealiasing cut per kx
+    float* kxw = nullptr;         // (float)(kx kxs), kx in [0, hx]: the FP32 kernels' wavenumbers
     int kcut = 0;                 // first kx whose row is entirely removed by the 2/3 rule
     double* dscratch = nullptr;   // 2*nx*ny doubles (ABI transfers, packed arrays)
     double* dscratch2 = nullptr;  // nx*ny doubles
@@ -578,6 +579,7 @@ static KArgs<R> kargs(fsibe_ctx* c) {
     a.etab = c->etab;
     a.etabf = c->etabf;
     a.dcut = c->dcut;
+    a.kxw = c->kxw;
     a.kcut = c->kcut;
     a.spg = reinterpret_cast<const R*>(c->spg);
     a.s10 = reinterpret_cast<const R*>(c->s10);
@@ -889,6 +891,9 @@ static MaskArgs mask_args(fsibe_ctx* c) {
     m.x = c->beam[B_X]; m.y = c->beam[B_Y]; m.vx = c->beam[B_VX]; m.vy = c->beam[B_VY]; m.th = c->beam[B_TH];
     m.prims = c->prims; m.nprims = c->nprims; m.rect = c->rect; m.nsm = c->nsm;
     m.rdx = 1.0 / m.dx; m.rdy = 1.0 / m.dy; m.rpi = 1.0 / m.pi;
+    m.inv_delta = 1.0 / ((m.N_smooth * std::fmax(m.dx, m.dy)) * c->gerf);
+    m.inv_ds = 1.0 / m.ds;
+    m.inv_eps = 1.0 / m.eps;
     m.mo = motion_args(c);
     m.mask = c->phys[PH_MASK]; m.mvx = c->phys[PH_MVX]; m.mvy = c->phys[PH_MVY];
     m.full = c->full_mask ? 1 : 0;
@@ -1519,7 +1524,7 @@ int fsibe_destroy(fsibe_ctx* c) {
     for (void* p : c->spec) if (p) cudaFree(p);
     for (double* p : c->beam) if (p) cudaFree(p);
     void* others[] = {c->twX, c->twR, c->twY, c->S, c->red, c->oo, c->ws, c->pred, c->minv, c->minv_rse, c->d1d, c->fgeo, c->fgij, c->clws, c->prims, c->nprims,
-                      c->rect, c->counter, c->fterm, c->rows, c->dscratch, c->dscratch2, c->etab, c->etabf, c->dcut,
+                      c->rect, c->counter, c->fterm, c->rows, c->dscratch, c->dscratch2, c->etab, c->etabf, c->dcut, c->kxw,
                       c->bg, c->frame, c->spg, c->s10, c->s10_dudx, c->rect_full, c->snap};
     for (void* p : others) if (p) cudaFree(p);
     for (cudaEvent_t e : c->pool) cudaEventDestroy(e);
@@ -1601,6 +1606,7 @@ int fsibe_create(const fsibe_params* p, fsibe_ctx** out) {
     g.kx_trunc2 = kxt * kxt;
     g.ky_trunc2 = kyt * kyt;
     g.idealis = p->idealis;
+    g.inv_nxny = 1.0 / ((double)p->nx * (double)p->ny);
     c->gerf = std::fabs((std::exp(-(2.0 * 1.0) * (2.0 * 1.0)) - 1.0) / std::sqrt(g.pi));
     SizeKernels<double> dx_, dy_;
     SizeKernels<float> fx_, fy_;
@@ -1668,6 +1674,12 @@ int fsibe_create(const fsibe_params* p, fsibe_ctx** out) {
     ALLOC(c->etab, 8 * (size_t)(p->nx / 2 + p->ny / 2 + 8));
     ALLOC(c->etabf, 8 * (size_t)(p->nx / 2 + p->ny / 2 + 8));
     ALLOC(c->dcut, 4 * (size_t)(p->nx / 2 + 8));
+    ALLOC(c->kxw, 4 * (size_t)(p->nx / 2 + 8));
+    {
+        std::vector<float> kw(p->nx / 2 + 1);
+        for (int kx = 0; kx <= p->nx / 2; ++kx) kw[kx] = (float)((double)kx * g.kxs);
+        cudaMemcpy(c->kxw, kw.data(), 4 * kw.size(), cudaMemcpyHostToDevice);
+    }
     {
         // 2/3 rule (dealiase_mask.f90:9-26), evaluated with the reference's FP64 expression:
         // dcut[kx] = smallest |ky| that is removed
@@ -3218,6 +3230,7 @@ extern "C" int fsibe_coftxy_static(const double* f_dev, double* fk_dev, int32_t 
     KArgs<double> a;
     std::memset(&a, 0, sizeof(a));
     a.g.nx = nx; a.g.ny = ny; a.g.hx = hx;
+    a.g.inv_nxny = 1.0 / ((double)nx * (double)ny);
     a.phys0 = const_cast<double*>(f_dev);
     a.spec0 = T;
     a.spec1 = Sx;

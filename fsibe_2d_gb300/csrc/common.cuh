@@ -111,6 +111,7 @@ struct Geometry {
     double kxs, kys;            // 2 pi / L
     double kx_trunc2, ky_trunc2;
     int idealis;
+    double inv_nxny;            // 1 / (nx ny), the transforms' normalisation (exact: powers of two)
 };
 
 // q / b correctly rounded from rb = RN(1/b): q0 = RN(q rb), then one FMA correction

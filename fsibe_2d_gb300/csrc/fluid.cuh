@@ -40,6 +40,8 @@ struct KArgs {
     const double* etab;   // integrating factor per direction: exp(coefx kx^2) [hx], exp(coefy ky^2) [ny/2+1]
     const float2* etabf;  // the same split hi + lo (FP32-compensated form)
     const int* dcut;      // 2/3-rule: modes with |ky| >= dcut[kx] are removed (dealiase_mask.f90:9-26)
+    const float* kxw;     // FP32 form: (float)(kx kxs) for kx in [0, hx], formed on the host (the
+                          // kernels' FP64 product and conversion per element, without the FP64 pipe)
     int kcut;             // rows kx >= kcut hold no dealiased mode (dcut = 0): exact zeros after the update
     int viscous, pressure_on, penalize, op;
     int explicit_step;    // 1 on the Euler start-up step (the host's flag: nl_x runs beside k_step_begin)
@@ -55,6 +57,37 @@ struct KArgs {
 };
 
 template <typename R> constexpr bool kIsF32 = std::is_same<R, float>::value;
+
+// One warp reduces a column of n FP32 partials: their sum in float-float (Knuth's TwoSum at each
+// addition; the parts added in FP64 at the end: within a few FP64 roundings of the FP64 sum of
+// the partials, at FP32 speed -- an FP64 instruction takes its SMSP's FP64 pipe for some 64
+// cycles on this chip), or their maximum (mx).
+__device__ __forceinline__ double col_reduce_ff(const float* col, int n, bool mx) {
+    const int l = threadIdx.x & 31;
+    float s = 0.f, c = 0.f;
+    for (int i = l; i < n; i += 32) {
+        const float x = col[i];
+        if (mx) { s = fmaxf(s, x); continue; }
+        const float t = __fadd_rn(s, x), bb = __fsub_rn(t, s);
+        c = __fadd_rn(c, __fadd_rn(__fsub_rn(s, __fsub_rn(t, bb)), __fsub_rn(x, bb)));
+        s = t;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const float so = __shfl_xor_sync(0xffffffffu, s, o), co = __shfl_xor_sync(0xffffffffu, c, o);
+        if (mx) { s = fmaxf(s, so); continue; }
+        const float t = __fadd_rn(s, so), bb = __fsub_rn(t, s);
+        c = __fadd_rn(__fadd_rn(c, co), __fadd_rn(__fsub_rn(s, __fsub_rn(t, bb)), __fsub_rn(so, bb)));
+        s = t;
+    }
+    return mx ? (double)s : (double)s + (double)c;
+}
+
+// kx 2 pi / xl in the kernels' type: FP32 from the host's table, FP64 as the product
+template <typename R> __device__ __forceinline__ R kx_wave(const KArgs<R>& a, int kx) {
+    if constexpr (kIsF32<R>) return a.kxw[kx];
+    else return (double)kx * a.g.kxs;
+}
 
 // k_nl_x's parts.  The advection part needs no mask, so it can run beside the mask kernels;
 // the penalization part then adds the mask's term on the rows of the mask's box alone
@@ -282,7 +315,7 @@ __global__ void __launch_bounds__(NY / 8) k_yfwd(KArgs<R> a) {
     for (int q = 0; q < 8; ++q) buf[pad8(t + q * G)] = in[t + q * G];
     __syncthreads();
     block_fft<R, NY, false>(buf, a.twY, t);
-    const R norm = (R)(1.0 / ((double)a.g.nx * (double)a.g.ny));
+    const R norm = (R)a.g.inv_nxny;
     C2<R>* out = a.spec1 + boff + (size_t)kx * NY;
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
@@ -511,7 +544,7 @@ __device__ __forceinline__ void nl_x_tile(const KArgs<R>& a, const int iy0) {
             if (i < nout) {
                 const int rr = i % X::TR, kx = i / X::TR;
                 const size_t o = (size_t)kx * ny + iy0 + rr;
-                const R kxs = (R)((double)kx * a.g.kxs);
+                const R kxs = kx_wave<R>(a, kx);
                 a.A[o] = cadd<R>(av[u], cimul<R>(bufA[rr * X::PL + pad8(kx)], kxs));
                 a.B[o] = bufB[rr * X::PL + pad8(kx)];
             }
@@ -522,7 +555,7 @@ __device__ __forceinline__ void nl_x_tile(const KArgs<R>& a, const int iy0) {
             const size_t o = (size_t)kx * ny + iy0 + rr;
             const C2<R> xa = bufA[rr * X::PL + pad8(kx)];
             if constexpr (PART == NL_WHOLE) {
-                const R kxs = (R)((double)kx * a.g.kxs);
+                const R kxs = kx_wave<R>(a, kx);
                 a.A[o] = cadd<R>(xa, cimul<R>(bufB[rr * X::PL + pad8(kx)], kxs));
                 a.B[o] = bufC[rr * X::PL + pad8(kx)];
             } else {
@@ -637,7 +670,7 @@ __global__ void __launch_bounds__(NY / 8, (nl_y_minb<R, NY>())) k_nl_y(KArgs<R> 
     const DevScalars* S = a.S;
     const double dt1 = S->dt1, b10 = S->b10, b11 = S->b11;
     const bool expl = S->explicit_step != 0;
-    const double norm = 1.0 / ((double)g.nx * (double)g.ny);
+    const double norm = g.inv_nxny;
     const int cut = a.dcut[kx];
     C2<R> wn[8], ps[8];
 #pragma unroll
@@ -795,6 +828,9 @@ __global__ void __launch_bounds__(XRows<R, H, TRV>::THREADS,
     const double time = S->time, dt1 = S->dt1;
     const R U = (R)S->mean_u_next, V = (R)S->mean_v_next;
     const int ixmin = S->win[0], ixmax = S->win[1], iymin = S->win[2], iymax = S->win[3];
+    // FP32 form: time_avg_vort's weights time / (time + dt) and dt / (time + dt), once a block
+    __shared__ float vm_w[2];
+    if (kIsF32<R> && threadIdx.x == 0) { vm_w[0] = (float)(time / (time + dt1)); vm_w[1] = (float)(dt1 / (time + dt1)); }
 
     load_tileT<R, H, X::TR, X::PL>(bufA, a.Tu, ny, iy0, a.kcut);
     load_tileT<R, H, X::TR, X::PL>(bufB, a.Tv, ny, iy0, a.kcut);
@@ -841,7 +877,7 @@ __global__ void __launch_bounds__(XRows<R, H, TRV>::THREADS,
         for (int s = 0; s < RED_NSLOTS; ++s) f[s] = 0.f;
         float spx = 0.f, spy = 0.f;
         const float Uf = (float)Ud, Vf = (float)Vd;
-        const float ca = (float)(time / (time + dt1)), cb = (float)(dt1 / (time + dt1));
+        const float ca = vm_w[0], cb = vm_w[1];
 #pragma unroll
         for (int q = 0; q < 8; ++q) {
             const int m = t + q * X::G;
@@ -944,13 +980,15 @@ __global__ void __launch_bounds__(XRows<R, H, TRV>::THREADS,
     for (int cidx = w; cidx < NCOL; cidx += NW) {
         const bool mx = cidx == RED_UMAX2;
         double v = 0.0;
-        for (int i = l; i < X::THREADS; i += 32) {
-            double x;
-            if constexpr (kIsF32<R>) x = (double)reinterpret_cast<const float*>(bufC)[cidx * X::THREADS + i];
-            else x = reinterpret_cast<const double*>(bufC)[cidx * X::THREADS + i];
-            v = mx ? fmax(v, x) : v + x;
+        if constexpr (kIsF32<R>) {
+            v = col_reduce_ff(reinterpret_cast<const float*>(bufC) + cidx * X::THREADS, X::THREADS, mx);
+        } else {
+            for (int i = l; i < X::THREADS; i += 32) {
+                const double x = reinterpret_cast<const double*>(bufC)[cidx * X::THREADS + i];
+                v = mx ? fmax(v, x) : v + x;
+            }
+            v = mx ? warp_max(v) : warp_sum<R>(v);
         }
-        v = mx ? warp_max(v) : warp_sum<R>(v);
         if (l == 0) {
             if (cidx < RED_NSLOTS) red_s[cidx][0] = v;
             else red_s[RED_INFLOW_MEAN][1] = v;  // FP32: the sum of spy (spx is in column INFLOW_MEAN)
@@ -969,7 +1007,7 @@ __global__ void __launch_bounds__(XRows<R, H, TRV>::THREADS,
         row_r2c_reg<R, H, 2>(pxy, ra, BS, a.twR, a.twX, t);  // x and y parts together
         for (int i = threadIdx.x; i < H * X::TR; i += blockDim.x) {
             const int rr = i % X::TR, kx = i / X::TR;
-            const R kxs = (R)((double)kx * a.g.kxs);
+            const R kxs = kx_wave<R>(a, kx);
             const size_t o = (size_t)kx * ny + iy0 + rr;
             a.P1[o] = cimul<R>(bufA[rr * X::PL + pad8(kx)], kxs);
             a.P2[o] = bufB[rr * X::PL + pad8(kx)];
@@ -1044,6 +1082,9 @@ __global__ void __launch_bounds__(XPairs<H, TR>::THREADS, XPairs<H, TR>::MINB) k
     const DevScalars* S = a.S;
     const double time = S->time, dt1 = S->dt1;
     const int ixmin = S->win[0], ixmax = S->win[1], iymin = S->win[2], iymax = S->win[3];
+    // time_avg_vort's weights time / (time + dt) and dt / (time + dt), once a block
+    __shared__ float vm_w[2];
+    if (threadIdx.x == 0) { vm_w[0] = (float)(time / (time + dt1)); vm_w[1] = (float)(dt1 / (time + dt1)); }
 
     load_tileP<H, TR>(bufA, a.Tu, ny, iy0, a.kcut);
     load_tileP<H, TR>(bufB, a.Tv, ny, iy0, a.kcut);
@@ -1074,7 +1115,7 @@ __global__ void __launch_bounds__(XPairs<H, TR>::THREADS, XPairs<H, TR>::MINB) k
     for (int s = 0; s < RED_NSLOTS; ++s) f[s] = 0.f;
     float spx = 0.f, spy = 0.f;
     const float Uf = (float)Ud, Vf = (float)Vd;
-    const float ca = (float)(time / (time + dt1)), cb = (float)(dt1 / (time + dt1));
+    const float ca = vm_w[0], cb = vm_w[1];
 #pragma unroll
     for (int m = 0; m < 8; ++m) {
         const int e0 = 2 * u + m * G;  // elements e0 and e0 + 1: 16-byte accesses of the rows
@@ -1135,12 +1176,7 @@ __global__ void __launch_bounds__(XPairs<H, TR>::THREADS, XPairs<H, TR>::MINB) k
     constexpr int NW = X::THREADS / 32;
     for (int cidx = w; cidx < RED_NSLOTS + 1; cidx += NW) {
         const bool mx = cidx == RED_UMAX2;
-        double v = 0.0;
-        for (int i = l; i < X::THREADS; i += 32) {
-            const double x = (double)cols[cidx * X::THREADS + i];
-            v = mx ? fmax(v, x) : v + x;
-        }
-        v = mx ? warp_max(v) : warp_sum<float>(v);
+        const double v = col_reduce_ff(cols + cidx * X::THREADS, X::THREADS, mx);
         if (l == 0) {
             if (cidx < RED_NSLOTS) red_s[cidx][0] = v;
             else red_s[RED_INFLOW_MEAN][1] = v;  // the sum of spy (spx is in column INFLOW_MEAN)
@@ -1158,7 +1194,7 @@ __global__ void __launch_bounds__(XPairs<H, TR>::THREADS, XPairs<H, TR>::MINB) k
         row_r2c_reg2<H, 2>(pxy, ra, BS, a.twR, a.twX, u);  // x and y parts together (buffers A and B)
         for (int i = threadIdx.x; i < H * TR; i += blockDim.x) {
             const int rr = i % TR, kx = i / TR;
-            const float kxs = (float)((double)kx * a.g.kxs);
+            const float kxs = a.kxw[kx];
             const size_t o = (size_t)kx * ny + iy0 + rr;
             a.P1[o] = cimul<float>(pel(bufA + rr * X::PS, kx), kxs);
             a.P2[o] = pel(bufB + rr * X::PS, kx);
@@ -1232,7 +1268,7 @@ __device__ __forceinline__ void press_y_paired(const KArgs<float>& a) {
         fp[1][2 * m] = make_float2(y.x, y.y); fp[1][2 * m + 1] = make_float2(y.z, y.w);
     }
     block_fft2_m<NY, false, 2>(fp, buf, pair_slots(NY), a.twY, u);  // P1 and P2 together
-    const float norm = (float)(1.0 / ((double)g.nx * (double)g.ny));
+    const float norm = (float)g.inv_nxny;
     float2 qv[1][16];
 #pragma unroll
     for (int m = 0; m < 8; ++m)
@@ -1277,7 +1313,7 @@ __global__ void __launch_bounds__(press_y_threads<R, NY, ENG>(), (kIsF32<R> && N
         fp[1][q] = a.P2[row + t + q * G];
     }
     block_fft_reg_m<R, NY, false, 2>(fp, bufA, padded_len(NY), a.twY, t);  // P1 and P2 together
-    const R norm = (R)(1.0 / ((double)g.nx * (double)g.ny));
+    const R norm = (R)g.inv_nxny;
     C2<R> qv[1][8];
 #pragma unroll
     for (int q = 0; q < 8; ++q) {

@@ -429,7 +429,7 @@ __global__ void __launch_bounds__(32 * MASK_WARPS) k_mask_raster(MaskArgs a, dou
     const double dx = a.dx, dy = a.dy, mxd = fmax(dx, dy), t = a.t_beam, N = a.N_smooth;
     const double t_star = t + 2.0 * N * mxd, h = N * mxd;
     const double rcut = t + 10.0 * h * gerf;
-    const double inv_delta = 1.0 / (h * gerf), inv_ds = 1.0 / a.ds, inv_eps = 1.0 / a.eps;
+    const double inv_delta = a.inv_delta, inv_ds = a.inv_ds, inv_eps = a.inv_eps;  // FP64 quotients from the host
     const double two_mxd = 2.0 * mxd;
     const float mg = 1.0e-5f * (float)fmax((double)a.nx * dx, (double)a.ny * dy);
     const int total = *a.nprims;

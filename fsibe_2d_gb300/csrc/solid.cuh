@@ -86,6 +86,7 @@ struct MaskArgs {
                   // with the previous step's box (every cell outside [0..3] is zero), [8..11] the
                   // accumulator of the next box (empty between steps), [12] blocks done
     double rdx, rdy, rpi;  // 1/dx, 1/dy, 1/pi (correctly rounded)
+    double inv_delta, inv_ds, inv_eps;  // 1 / (N_smooth max(dx, dy) gerf), 1 / ds, 1 / eps (host quotients)
     MotionArgs mo;         // the leading edge's motion (alpha of the time)
     int nsm;      // SMs of the device (raster grid size)
     void *mask, *mvx, *mvy;  // R*[ny][nx]
