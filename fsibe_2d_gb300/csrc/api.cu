@@ -443,6 +443,7 @@ struct fsibe_ctx {
     double* oo = nullptr;
     double* ws = nullptr;
     Prim* prims = nullptr;
+    PrimG* primg = nullptr;       // the FP32 raster's per-primitive data (FP32 form)
     int *nprims = nullptr, *rect = nullptr;
     unsigned* counter = nullptr;
     double* fterm = nullptr;
@@ -889,7 +890,7 @@ static MaskArgs mask_args(fsibe_ctx* c) {
     m.t_beam = c->P.t_beam; m.N_smooth = c->P.N_smooth; m.eps = c->P.eps; m.pi = c->g.pi;
     m.angle_deg = c->P.angle_beam;
     m.x = c->beam[B_X]; m.y = c->beam[B_Y]; m.vx = c->beam[B_VX]; m.vy = c->beam[B_VY]; m.th = c->beam[B_TH];
-    m.prims = c->prims; m.nprims = c->nprims; m.rect = c->rect; m.nsm = c->nsm;
+    m.prims = c->prims; m.primg = c->fp32 ? c->primg : nullptr; m.nprims = c->nprims; m.rect = c->rect; m.nsm = c->nsm;
     m.rdx = 1.0 / m.dx; m.rdy = 1.0 / m.dy; m.rpi = 1.0 / m.pi;
     m.inv_delta = 1.0 / ((m.N_smooth * std::fmax(m.dx, m.dy)) * c->gerf);
     m.inv_ds = 1.0 / m.ds;
@@ -1523,7 +1524,7 @@ int fsibe_destroy(fsibe_ctx* c) {
     for (void* p : c->phys) if (p) cudaFree(p);
     for (void* p : c->spec) if (p) cudaFree(p);
     for (double* p : c->beam) if (p) cudaFree(p);
-    void* others[] = {c->twX, c->twR, c->twY, c->S, c->red, c->oo, c->ws, c->pred, c->minv, c->minv_rse, c->d1d, c->fgeo, c->fgij, c->clws, c->prims, c->nprims,
+    void* others[] = {c->twX, c->twR, c->twY, c->S, c->red, c->oo, c->ws, c->pred, c->minv, c->minv_rse, c->d1d, c->fgeo, c->fgij, c->clws, c->prims, c->primg, c->nprims,
                       c->rect, c->counter, c->fterm, c->rows, c->dscratch, c->dscratch2, c->etab, c->etabf, c->dcut, c->kxw,
                       c->bg, c->frame, c->spg, c->s10, c->s10_dudx, c->rect_full, c->snap};
     for (void* p : others) if (p) cudaFree(p);
@@ -1660,6 +1661,7 @@ int fsibe_create(const fsibe_params* p, fsibe_ctx** out) {
 
     }
     ALLOC(c->prims, sizeof(Prim) * (size_t)(2 * ns + 8));
+    if (c->fp32) ALLOC(c->primg, sizeof(PrimG) * (size_t)(2 * ns + 8));
     ALLOC(c->nprims, 16);
     ALLOC(c->rect, 64);
     {

@@ -47,9 +47,28 @@ __global__ void __launch_bounds__(128) k_mask_prep(MaskArgs a, double gerf) {
     const int total = nseg + nsharp + nh + ndot;
     const int i = blockIdx.x * 32 + lane;
     int bx0 = a.nx, bx1 = -1, by0 = a.ny, by1 = -1;
+    // the FP32 raster's per-primitive data (the raster's expressions for its constants)
+    const double rcut_g = t + 10.0 * (N * mx) * gerf;
+    const float mg = 1.0e-5f * (float)fmax((double)a.nx * dx, (double)a.ny * dy);
     auto emit = [&](int q, Prim& P) {
         clip_box(P.box, a.nx, a.ny);
         a.prims[q] = P;
+        if (a.primg && P.type != PRIM_SHARP) {
+            PrimG G;
+            if (P.type == PRIM_SEGMENT) {
+                G.a = make_float4((float)P.p[0], (float)P.p[1], 0.f, 0.f);
+                G.b = make_float4((float)(P.p[4] - P.p[2]), (float)((P.p[5] - P.p[3]) - t_star), 0.f, 0.f);
+                G.c = make_float4((float)P.p[6], (float)P.p[7], (float)((P.p[8] - P.p[6]) * a.inv_ds),
+                                  (float)((P.p[9] - P.p[7]) * a.inv_ds));
+            } else {
+                const float lim = (float)((P.type == PRIM_HINGE) ? t_star : rcut_g) + mg;
+                G.a = make_float4(0.f, 0.f, lim * lim, 0.f);
+                G.b = make_float4((float)P.p[2], (float)P.p[3], 0.f, 0.f);
+                G.c = (P.type == PRIM_HINGE) ? make_float4((float)P.p[4], (float)P.p[5], 0.f, 0.f)
+                                             : make_float4((float)P.p[2], (float)P.p[3], 0.f, 0.f);
+            }
+            a.primg[q] = G;
+        }
         if (P.box[0] <= P.box[1] && P.box[2] <= P.box[3]) {
             bx0 = min(bx0, P.box[0]); bx1 = max(bx1, P.box[1]);
             by0 = min(by0, P.box[2]); by1 = max(by1, P.box[3]);
@@ -258,15 +277,6 @@ __device__ __forceinline__ float smooth_step_ff(float x, float t, float inv_delt
     if (sharp) return (x <= t) ? 1.f : 0.f;
     return 0.5f * (erff((t - x) * inv_delta) + erff((x + t) * inv_delta));
 }
-
-// The FP32 form's per-primitive data, relative to the tile origin (x0, y0) so that every
-// coordinate is small and FP32 keeps it to ~1e-9:
-//   segment: a = (cos, sin, p1x - x0, p1y - y0), b = (length along the axis, lower bound of the
-//            normal offset, -, -), c = (v1x, v1y, (v2x - v1x)/ds, (v2y - v1y)/ds)
-//   hinge / dot: a = (px - x0, py - y0, R^2 limit, -), b = (beta1, beta2, -, -), c = (vx, vy, -, -)
-struct PrimG {
-    float4 a, b, c;
-};
 
 // Segment, hinge or dot q for the lane's cell at (cx, cy) from the tile origin, all in FP32:
 // the FP32 form's mask is continuous across every primitive's edge (a segment's end meets its
@@ -484,19 +494,12 @@ __global__ void __launch_bounds__(32 * MASK_WARPS) k_mask_raster(MaskArgs a, dou
                     const int e = __popc(bal & ((1u << lane) - 1u));
                     sp[warp][e] = P;
                     if constexpr (F32) {
-                        PrimG G;
-                        if (P.type == PRIM_SEGMENT) {
-                            G.a = make_float4((float)P.p[0], (float)P.p[1], (float)(P.p[10] - x0), (float)(P.p[11] - y0));
-                            G.b = make_float4((float)(P.p[4] - P.p[2]), (float)((P.p[5] - P.p[3]) - t_star), 0.f, 0.f);
-                            G.c = make_float4((float)P.p[6], (float)P.p[7], (float)((P.p[8] - P.p[6]) * inv_ds),
-                                              (float)((P.p[9] - P.p[7]) * inv_ds));
-                        } else {
-                            const float lim = (float)((P.type == PRIM_HINGE) ? t_star : rcut) + mg;
-                            G.a = make_float4((float)(P.p[0] - x0), (float)(P.p[1] - y0), lim * lim, 0.f);
-                            G.b = make_float4((float)P.p[2], (float)P.p[3], 0.f, 0.f);
-                            G.c = (P.type == PRIM_HINGE) ? make_float4((float)P.p[4], (float)P.p[5], 0.f, 0.f)
-                                                         : make_float4((float)P.p[2], (float)P.p[3], 0.f, 0.f);
-                        }
+                        // k_mask_prep's data, with this tile's offsets (two FP64 subtractions)
+                        PrimG G = a.primg[q];
+                        const bool seg = P.type == PRIM_SEGMENT;
+                        const float ox = (float)((seg ? P.p[10] : P.p[0]) - x0), oy = (float)((seg ? P.p[11] : P.p[1]) - y0);
+                        if (seg) { G.a.z = ox; G.a.w = oy; }
+                        else { G.a.x = ox; G.a.y = oy; }
                         sg[warp][e] = G;
                     } else {
                         PrimF F;

@@ -73,6 +73,16 @@ struct Prim {
     double p[12];
 };
 
+// The FP32 form's per-primitive data, relative to a raster tile's origin (x0, y0) so that every
+// coordinate is small and FP32 keeps it to ~1e-9:
+//   segment: a = (cos, sin, p1x - x0, p1y - y0), b = (length along the axis, lower bound of the
+//            normal offset, -, -), c = (v1x, v1y, (v2x - v1x)/ds, (v2y - v1y)/ds)
+//   hinge / dot: a = (px - x0, py - y0, R^2 limit, -), b = (beta1, beta2, -, -), c = (vx, vy, -, -)
+// k_mask_prep forms everything but the tile-relative offsets (zero there) once per primitive.
+struct PrimG {
+    float4 a, b, c;
+};
+
 struct MaskArgs {
     DevScalars* S;
     int until_full;  // 1: keep the previous mask once the time reaches T_fullspeed (the step's
@@ -81,6 +91,7 @@ struct MaskArgs {
     double dx, dy, ds, t_beam, N_smooth, eps, pi, angle_deg;
     const double *x, *y, *vx, *vy, *th;
     Prim* prims;
+    PrimG* primg;  // the FP32 form's data of prims (k_mask_prep), or null
     int* nprims;
     int* rect;    // [0..3] union of this step's primitive boxes (x0, x1, y0, y1), [4..7] its union
                   // with the previous step's box (every cell outside [0..3] is zero), [8..11] the
