@@ -687,9 +687,13 @@ __global__ void __launch_bounds__(128) k_forces(ForceArgs a, double dxi, double 
         const int i = ij[p][0], j = ij[p][1];
         const bool ok = !(i - 4 < 0 || j - 4 < 0 || i + 4 > a.nx - 1 || j + 4 > a.ny - 1);
         if (ok && (k < 2 || a.viscous)) {
+            // the column's nine field values loaded together, then the reference's sum in order
             const double dxv = dl[p][dxk];
-            for (int dyk = 0; dyk < 9; ++dyk)
-                R1 = R1 + dxv * dl[p][9 + dyk] * fld(f, a.fp32, (size_t)(j - 4 + dyk) * a.nx + (i - 4 + dxk));
+            double fv[9];
+#pragma unroll
+            for (int dyk = 0; dyk < 9; ++dyk) fv[dyk] = fld(f, a.fp32, (size_t)(j - 4 + dyk) * a.nx + (i - 4 + dxk));
+#pragma unroll
+            for (int dyk = 0; dyk < 9; ++dyk) R1 = R1 + dxv * dl[p][9 + dyk] * fv[dyk];
         }
         part[k][dxk] = R1;
     }
