@@ -10,10 +10,9 @@
 // the binade exactly when 2^52 < |m + RN| < 2^53 (at 2^52 the exact sum may lie below the
 // binade, where the grid is finer).  So a warp per sum takes 32 steps at a time as a prefix sum
 // of the rounded terms, up to the first step that leaves the binade, which is done by the FP64
-// addition; its result gives the next binade.  Afterwards
-// every step is checked in parallel by the FP64 addition, bits(s_k + a_k) == bits(s_(k+1)), and
-// a sum with any mismatch is formed again by the plain serial loop: the result is that loop's
-// in every case.
+// addition; its result gives the next binade.  Afterwards every step is checked in parallel by
+// the FP64 addition, bits(s_k + a_k) == bits(s_(k+1)), and a sum with any mismatch is formed
+// again by the plain serial loop: the result is that loop's in every case.
 #pragma once
 #include "common.cuh"
 

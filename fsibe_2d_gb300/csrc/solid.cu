@@ -17,6 +17,11 @@ __device__ __forceinline__ int dnint(double v) { return (int)llround(v); }  // F
 
 
 __device__ __forceinline__ double convert_angle(double a, double pi) { return (a < 0.0) ? 2.0 * pi + a : a; }
+// the same in FP32, in degrees (the FP32 form's raster: the angle of a cell about a hinge)
+__device__ __forceinline__ float deg_f(float a) {
+    if (a < 0.f) a = 6.28318530717958647692f + a;
+    return a * 57.2957795130823208768f;
+}
 
 __device__ __forceinline__ void clip_box(int* bx, int nx, int ny) {
     bx[0] = max(bx[0], 0);
@@ -98,9 +103,16 @@ __global__ void __launch_bounds__(128) k_mask_prep(MaskArgs a, double gerf) {
             emit(i, P);
         }
     } else if (warp == 1) {
-        if (hinge) a1 = atan2((a.y[i] - a.y[i - 1]), (a.x[i] - a.x[i - 1]));
+        // the hinge's two angles: FP32 in the FP32 form, whose raster tests its wedges in FP32
+        if (hinge) {
+            const double ddy = a.y[i] - a.y[i - 1], ddx = a.x[i] - a.x[i - 1];
+            a1 = a.primg ? (double)atan2f((float)ddy, (float)ddx) : atan2(ddy, ddx);
+        }
     } else if (warp == 2) {
-        if (hinge) ang2[lane] = atan2((a.y[i + 1] - a.y[i]), (a.x[i + 1] - a.x[i]));
+        if (hinge) {
+            const double ddy = a.y[i + 1] - a.y[i], ddx = a.x[i + 1] - a.x[i];
+            ang2[lane] = a.primg ? (double)atan2f((float)ddy, (float)ddx) : atan2(ddy, ddx);
+        }
     } else {
         if (hinge) {
             const double px = a.x[i], py = a.y[i];
@@ -157,8 +169,13 @@ __global__ void __launch_bounds__(128) k_mask_prep(MaskArgs a, double gerf) {
         P.type = PRIM_HINGE;
         P.box[0] = hbox[lane][0]; P.box[1] = hbox[lane][1]; P.box[2] = hbox[lane][2]; P.box[3] = hbox[lane][3];
         P.p[0] = px; P.p[1] = py;
-        P.p[2] = div_cr(convert_angle(a1, a.pi) * 180.0, a.pi, a.rpi);
-        P.p[3] = div_cr(convert_angle(a2, a.pi) * 180.0, a.pi, a.rpi);
+        if (a.primg) {  // degrees as the FP32 raster forms a cell's angle
+            P.p[2] = (double)deg_f((float)a1);
+            P.p[3] = (double)deg_f((float)a2);
+        } else {
+            P.p[2] = div_cr(convert_angle(a1, a.pi) * 180.0, a.pi, a.rpi);
+            P.p[3] = div_cr(convert_angle(a2, a.pi) * 180.0, a.pi, a.rpi);
+        }
         P.p[4] = a.vx[i]; P.p[5] = a.vy[i];
         emit(nseg + nsharp + (i - 1), P);
     }
@@ -296,9 +313,7 @@ __device__ __forceinline__ void mask_prim_f(const MaskArgs& a, const Prim& Q, co
     const float ddx = cx - G.a.x, ddy = cy - G.a.y, r2 = ddx * ddx + ddy * ddy;
     if (r2 > G.a.z) return;
     if (Q.type == PRIM_HINGE) {
-        float gf = atan2f(ddy, ddx);
-        if (gf < 0.f) gf = 6.28318530717958647692f + gf;
-        gf = gf * 57.2957795130823208768f;
+        const float gf = deg_f(atan2f(ddy, ddx));
         if (!hinge_inside<float>(gf, G.b.x, G.b.y, 0.f, nullptr)) return;
         const float Rr = sqrtf(r2);
         if (Rr <= tsf) fold_take<float>(f, smooth_step_ff(Rr, tf, idf, a.sharp), G.c.x, G.c.y, q);
