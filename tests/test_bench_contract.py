@@ -24,7 +24,7 @@ def test_reference_arm_prints_one_contract_line():
         assert k in d, k
     assert d["metric"].startswith("Mcell-steps/s at 1024^2") and d["unit"] == "Mcell-steps/s"
     assert d["higher_is_better"] is True and d["steps"] == 1 and d["value"] > 0
-    # the GPU arm's config, key for key (the driver compares the two arms' configs)
+    # the GPU arm's config, key for key: both arms report the same workload
     assert set(d["config"]) == {"workload", "nx", "ny", "ns", "parallelism", "l2"}
     assert d["config"]["nx"] == 1024 and d["config"]["ns"] == 256
     cb = d["cpu_baseline"]
